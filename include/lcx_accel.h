@@ -1,0 +1,239 @@
+/*
+ * lcx_accel.h — C ABI of the GB300 (sm_103a) acceleration-structure path.
+ *
+ * This library replaces, on one GPU, the two implementations LuisaCompute has
+ * for its Mesh/Accel path:
+ *   - the CPU backend's Embree calls
+ *     (src/rust/luisa_compute_backend_impl/src/cpu/accel.rs:205-535), and
+ *   - the CUDA backend's OptiX calls
+ *     (src/backends/cuda/cuda_mesh.cpp:31-69, cuda_accel.cpp:26-318,
+ *      cuda_builtin/cuda_device_resource.h:1742-1829).
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and
+ * returns an int status (LCX_OK == 0, negative on error).  Nothing aborts:
+ * where the reference asserts (LUISA_ASSERT / panic_abort!), this library
+ * returns LCX_ERR_INVALID_ARG and records a message readable through
+ * lcx_last_error_string().
+ *
+ * Memory contract (same as the reference, include/luisa/runtime/rtx/mesh.h:41):
+ * vertex and triangle buffers passed to lcx_mesh_build are *borrowed* device
+ * memory; they are read during the build only (the BVH keeps its own copy of
+ * the triangles in traversal order), and a mesh must be rebuilt after they
+ * change.  Ray and hit buffers are device pointers owned by the caller.
+ *
+ * Streams are `cudaStream_t` passed as `void *` (NULL = legacy default stream).
+ * All work is stream-ordered; no entry point synchronises the host except
+ * where its comment says so.
+ */
+#ifndef LCX_ACCEL_H
+#define LCX_ACCEL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define LCX_API __attribute__((visibility("default")))
+#else
+#define LCX_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+    LCX_OK = 0,
+    LCX_ERR_INVALID_ARG = -1,  /* bad handle, size, stride, alignment or index */
+    LCX_ERR_OOM = -2,          /* device allocation failed or budget exceeded */
+    LCX_ERR_NOT_BUILT = -3,    /* mesh/accel used before a successful build */
+    LCX_ERR_TIMEOUT = -4,      /* a bounded device-side wait gave up */
+    LCX_ERR_CUDA = -5,         /* a CUDA runtime call failed */
+    LCX_ERR_DEPTH = -6,        /* BVH deeper than the traversal stack */
+};
+
+/* --------------------------------------------------------- shared records */
+
+/* Ray: include/luisa/runtime/rtx/ray.h:10-16 (32 B, align 16).  Also the CPU
+ * kernel ABI `defs::Ray` (luisa_compute_cpu_kernel_defs/src/lib.rs:42-53). */
+typedef struct __attribute__((aligned(16))) LcxRay {
+    float origin[3];
+    float t_min;
+    float direction[3];
+    float t_max;
+} LcxRay;
+
+/* TriangleHit (== SurfaceHit): include/luisa/runtime/rtx/hit.h:30-46
+ * (24 B, align 8).  A miss is {~0u, ~0u, (0,0), ray.t_max}, the CPU
+ * backend's record (accel.rs:501-507); `inst == ~0u` is the miss test
+ * (include/luisa/dsl/rtx/hit.h:67).  bary = (u, v) with
+ * p = (1-u-v)*v0 + u*v1 + v*v2 (src/dsl/rtx/hit.cpp:7-20). */
+typedef struct __attribute__((aligned(8))) LcxTriangleHit {
+    uint32_t inst;
+    uint32_t prim;
+    float bary[2];
+    float committed_ray_t;
+    uint32_t _pad;
+} LcxTriangleHit;
+
+/* Triangle: include/luisa/runtime/rtx/triangle.h:7-11. */
+typedef struct LcxTriangle {
+    uint32_t i0, i1, i2;
+} LcxTriangle;
+
+/* AccelOption: include/luisa/runtime/rhi/resource.h:94-125 (motion omitted:
+ * motion blur is not on this path). */
+enum { LCX_HINT_FAST_TRACE = 0, LCX_HINT_FAST_BUILD = 1 };
+typedef struct LcxAccelOption {
+    uint32_t hint;            /* LCX_HINT_FAST_TRACE | LCX_HINT_FAST_BUILD */
+    uint8_t allow_compaction; /* accepted for ABI parity; BVHs are always exact-size */
+    uint8_t allow_update;     /* accepted; PREFER_UPDATE rebuilds (see lcx_mesh_build) */
+    uint8_t _pad[2];
+} LcxAccelOption;
+
+/* AccelBuildRequest: include/luisa/runtime/rhi/command.h:401-404. */
+enum { LCX_REQUEST_PREFER_UPDATE = 0, LCX_REQUEST_FORCE_BUILD = 1 };
+
+/* MeshBuildCommand: include/luisa/runtime/rhi/command.h:407-444.  The buffer
+ * fields are device addresses (the CUDA backend stores CUDABuffer device
+ * addresses, cuda_mesh.cpp:56-61).  Checks follow src/runtime/rtx/mesh.cpp:
+ * vertex_stride % 16 == 0, vertex offset/size multiples of the stride,
+ * triangle offset % 4 == 0, triangle size % 12 == 0. */
+typedef struct LcxMeshBuildCommand {
+    uint32_t request;
+    uint32_t _pad;
+    uint64_t vertex_buffer;
+    size_t vertex_buffer_offset;
+    size_t vertex_buffer_size;
+    size_t vertex_stride;
+    uint64_t triangle_buffer;
+    size_t triangle_buffer_offset;
+    size_t triangle_buffer_size;
+} LcxMeshBuildCommand;
+
+/* AccelBuildCommand::Modification: include/luisa/runtime/rhi/command.h:534-592
+ * (80 B, align 16, byte-identical).  affine is the row-major 3x4
+ * object-to-world matrix (command.h:557-571).  `primitive` is a mesh handle
+ * returned by lcx_mesh_create. */
+enum {
+    LCX_MOD_PRIMITIVE = 1u << 0,
+    LCX_MOD_TRANSFORM = 1u << 1,
+    LCX_MOD_OPAQUE_ON = 1u << 2,
+    LCX_MOD_OPAQUE_OFF = 1u << 3,
+    LCX_MOD_VISIBILITY = 1u << 4,
+    LCX_MOD_USER_ID = 1u << 5,
+};
+typedef struct __attribute__((aligned(16))) LcxModification {
+    uint32_t index;
+    uint32_t user_id;
+    uint32_t flags;
+    uint32_t vis_mask;
+    float affine[12];
+    uint64_t primitive;
+} LcxModification;
+
+/* Node layout used by a trace call. */
+enum {
+    LCX_NODES_FP32 = 0,  /* plain: 8-wide nodes with FP32 child boxes (208 B) */
+    LCX_NODES_QUANT8 = 1 /* 8-wide nodes, child boxes quantised to 8 bits
+                            relative to the parent, rounded outward (80 B) */
+};
+
+typedef struct LcxAccelStats {
+    uint64_t node_count;     /* wide nodes */
+    uint64_t leaf_prim_count;/* triangles (BLAS) or instances (TLAS) stored */
+    uint64_t device_bytes;   /* device memory owned by the handle */
+    uint32_t depth;          /* wide-tree depth (root = 1) */
+    uint32_t max_blas_depth; /* TLAS only: deepest referenced BLAS */
+    double sah_cost;         /* SAH cost of the binary tree (C_node=1, C_tri=1,
+                                normalised by the root surface area) */
+    double wide_sah_cost;    /* same for the 8-wide tree */
+} LcxAccelStats;
+
+/* ------------------------------------------------------------ device setup */
+
+/* Select the CUDA device used by later calls made from this thread and
+ * create the library's per-device state.  Optional: the first call of any
+ * other entry point initialises the current device. */
+LCX_API int lcx_device_init(int device);
+
+/* Message describing the last error on the calling thread ("" if none). */
+LCX_API const char *lcx_last_error_string(void);
+
+/* Library version as 0xMMmmpp. */
+LCX_API uint32_t lcx_version(void);
+
+/* ------------------------------------------------------------------- mesh */
+
+/* DeviceInterface::create_mesh / destroy_mesh:
+ * include/luisa/runtime/rhi/device_interface.h:171-172. */
+LCX_API int lcx_mesh_create(const LcxAccelOption *option, uint64_t *out_handle);
+LCX_API int lcx_mesh_destroy(uint64_t mesh);
+
+/* MeshBuildCommand visit (CPU: accel.rs:205-260; CUDA: cuda_mesh.cpp:31-69).
+ * Builds the BLAS on `stream`: Morton-code LBVH, collapsed to 8-wide nodes in
+ * both node layouts.  PREFER_UPDATE on a built mesh rebuilds as well (a
+ * refit is not offered).  Returns after enqueueing; the mesh may be used by
+ * lcx_accel_build on the same stream immediately.  Synchronises the host once
+ * to learn the tree size. */
+LCX_API int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *command, void *stream);
+
+LCX_API int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out);
+
+/* ------------------------------------------------------------------ accel */
+
+/* DeviceInterface::create_accel / destroy_accel: device_interface.h:183-184. */
+LCX_API int lcx_accel_create(const LcxAccelOption *option, uint64_t *out_handle);
+LCX_API int lcx_accel_destroy(uint64_t accel);
+
+/* AccelBuildCommand visit (CPU: accel.rs:324-447; CUDA: cuda_accel.cpp:152-318
+ * with the update_accel kernel, cuda_builtin_kernels.cu:52-111).
+ * `mods` is host memory (the command's vector).  Instance i keeps its mesh,
+ * transform, mask (default 0xff), opacity and user id until modified.
+ * instance_count == 0 is an error, as in src/runtime/rtx/accel.cpp:72-73.
+ * update_instance_buffer_only != 0 stores the modifications without
+ * rebuilding the TLAS. */
+LCX_API int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request,
+                    const LcxModification *mods, size_t mod_count,
+                    int update_instance_buffer_only, void *stream);
+
+LCX_API int lcx_accel_stats(uint64_t accel, LcxAccelStats *out);
+
+/* ----------------------------------------------------------------- queries */
+
+/* trace_closest over a batch: CPU accel.rs:449-509, CUDA
+ * cuda_device_resource.h:1784-1807.  d_rays / d_hits are device arrays of
+ * `ray_count` records.  An instance is eligible when (vis_mask & mask) != 0
+ * (accel.rs:414, cuda_device_resource.h:1776).  Back faces are not culled
+ * (cuda_mesh.cpp:15-16).  Ties in t are broken by the smaller (inst, prim),
+ * so the result does not depend on BVH topology. */
+LCX_API int lcx_trace_closest(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count,
+                      uint32_t mask, LcxTriangleHit *d_hits, void *stream);
+
+/* trace_any over a batch: CPU accel.rs:511-535 (occluded <=> any hit with
+ * t in [t_min, t_max]), CUDA cuda_device_resource.h:1809-1829.
+ * d_occluded[i] is 1 if occluded, else 0. */
+LCX_API int lcx_trace_any(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count,
+                  uint32_t mask, uint8_t *d_occluded, void *stream);
+
+/* Same queries with an explicit node layout (LCX_NODES_FP32 or
+ * LCX_NODES_QUANT8); lcx_trace_closest/any use LCX_NODES_QUANT8. */
+LCX_API int lcx_trace_closest_ex(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count,
+                         uint32_t mask, LcxTriangleHit *d_hits, uint32_t node_layout,
+                         void *stream);
+LCX_API int lcx_trace_any_ex(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count,
+                     uint32_t mask, uint8_t *d_occluded, uint32_t node_layout,
+                     void *stream);
+
+/* Counting build of the closest-hit traversal: per-ray visit counts
+ * d_counts[3*i + {0,1,2}] = {wide nodes fetched, triangles tested, instances
+ * entered}.  Used to compute algorithmic bytes per ray. */
+LCX_API int lcx_trace_closest_counts(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count,
+                             uint32_t mask, LcxTriangleHit *d_hits, uint32_t *d_counts,
+                             uint32_t node_layout, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LCX_ACCEL_H */

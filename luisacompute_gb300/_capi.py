@@ -1,0 +1,106 @@
+"""ctypes binding of the C ABI declared in include/lcx_accel.h."""
+from __future__ import annotations
+
+import ctypes
+import re
+from ctypes import POINTER, c_char_p, c_double, c_int, c_size_t, c_uint8, c_uint32, c_uint64, c_void_p
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "lcx_accel.h"
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "liblcx_accel.so"
+
+LCX_OK = 0
+LCX_ERR_INVALID_ARG = -1
+LCX_ERR_OOM = -2
+LCX_ERR_NOT_BUILT = -3
+LCX_ERR_TIMEOUT = -4
+LCX_ERR_CUDA = -5
+LCX_ERR_DEPTH = -6
+ERROR_NAMES = {0: "LCX_OK", -1: "LCX_ERR_INVALID_ARG", -2: "LCX_ERR_OOM", -3: "LCX_ERR_NOT_BUILT",
+               -4: "LCX_ERR_TIMEOUT", -5: "LCX_ERR_CUDA", -6: "LCX_ERR_DEPTH"}
+
+HINT_FAST_TRACE, HINT_FAST_BUILD = 0, 1
+REQUEST_PREFER_UPDATE, REQUEST_FORCE_BUILD = 0, 1
+NODES_FP32, NODES_QUANT8 = 0, 1
+MOD_PRIMITIVE, MOD_TRANSFORM, MOD_OPAQUE_ON, MOD_OPAQUE_OFF, MOD_VISIBILITY, MOD_USER_ID = 1, 2, 4, 8, 16, 32
+
+
+class LcxAccelOption(ctypes.Structure):
+    _fields_ = [("hint", c_uint32), ("allow_compaction", c_uint8), ("allow_update", c_uint8),
+                ("_pad", c_uint8 * 2)]
+
+
+class LcxMeshBuildCommand(ctypes.Structure):
+    _fields_ = [("request", c_uint32), ("_pad", c_uint32), ("vertex_buffer", c_uint64),
+                ("vertex_buffer_offset", c_size_t), ("vertex_buffer_size", c_size_t), ("vertex_stride", c_size_t),
+                ("triangle_buffer", c_uint64), ("triangle_buffer_offset", c_size_t),
+                ("triangle_buffer_size", c_size_t)]
+
+
+class LcxAccelStats(ctypes.Structure):
+    _fields_ = [("node_count", c_uint64), ("leaf_prim_count", c_uint64), ("device_bytes", c_uint64),
+                ("depth", c_uint32), ("max_blas_depth", c_uint32), ("sah_cost", c_double),
+                ("wide_sah_cost", c_double)]
+
+
+_SIGS = {
+    "lcx_device_init": (c_int, [c_int]),
+    "lcx_last_error_string": (c_char_p, []),
+    "lcx_version": (c_uint32, []),
+    "lcx_mesh_create": (c_int, [POINTER(LcxAccelOption), POINTER(c_uint64)]),
+    "lcx_mesh_destroy": (c_int, [c_uint64]),
+    "lcx_mesh_build": (c_int, [c_uint64, POINTER(LcxMeshBuildCommand), c_void_p]),
+    "lcx_mesh_stats": (c_int, [c_uint64, POINTER(LcxAccelStats)]),
+    "lcx_accel_create": (c_int, [POINTER(LcxAccelOption), POINTER(c_uint64)]),
+    "lcx_accel_destroy": (c_int, [c_uint64]),
+    "lcx_accel_build": (c_int, [c_uint64, c_uint32, c_uint32, c_void_p, c_size_t, c_int, c_void_p]),
+    "lcx_accel_stats": (c_int, [c_uint64, POINTER(LcxAccelStats)]),
+    "lcx_trace_closest": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p]),
+    "lcx_trace_any": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p]),
+    "lcx_trace_closest_ex": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
+    "lcx_trace_any_ex": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
+    "lcx_trace_closest_counts": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_uint32,
+                                         c_void_p]),
+}
+
+
+def declared_symbols(header: Path = HEADER) -> list:
+    """Function names declared with LCX_API in a header."""
+    text = header.read_text()
+    return sorted(set(re.findall(r"LCX_API\s+[\w\s\*]+?\b(lcx_\w+)\s*\(", text)))
+
+
+class LcxError(RuntimeError):
+    def __init__(self, code: int, where: str, message: str):
+        super().__init__(f"{where}: {ERROR_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: Path | None = None) -> ctypes.CDLL:
+    """Load liblcx_accel.so.  Raises if the library has not been built: there
+    is no fallback implementation of this path."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with luisacompute_gb300.build.build() "
+                           "(the GB300 kernels are the only implementation of this path)")
+    lib = ctypes.CDLL(str(p))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(code: int, where: str):
+    if code != LCX_OK:
+        msg = load().lcx_last_error_string()
+        raise LcxError(code, where, msg.decode() if msg else "")

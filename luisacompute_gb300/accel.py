@@ -1,0 +1,281 @@
+"""Python host mirror of LuisaCompute's Mesh / Accel API over the C ABI.
+
+Names, arguments and error behaviour follow the reference:
+  * ``Mesh(vertices, triangles)`` + ``Mesh.build(request)``   — include/luisa/runtime/rtx/mesh.h:19-141,
+    src/runtime/rtx/mesh.cpp:6-12 (borrowed vertex/triangle buffers, stride multiple of 16)
+  * ``Accel.emplace_back(mesh, transform, visibility_mask, opaque, user_id)``,
+    ``set_transform_on_update``, ``set_visibility_on_update``, ``set_opaque_on_update``,
+    ``set_user_id_on_update``, ``pop_back``, ``build(request, update_instance_buffer_only)``
+    — include/luisa/runtime/rtx/accel.h:21-134, src/runtime/rtx/accel.cpp:68-249
+  * ``Accel.trace_closest(rays, mask)`` / ``trace_any`` — batched forms of the DSL builtins
+    ``intersect`` / ``intersect_any`` (src/dsl/rtx/accel.cpp:120-150).
+Device memory is torch CUDA tensors; the work runs in liblcx_accel.so.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from ._capi import (HINT_FAST_BUILD, HINT_FAST_TRACE, MOD_OPAQUE_OFF, MOD_OPAQUE_ON, MOD_PRIMITIVE, MOD_TRANSFORM,
+                    MOD_USER_ID, MOD_VISIBILITY, NODES_FP32, NODES_QUANT8, REQUEST_FORCE_BUILD,
+                    REQUEST_PREFER_UPDATE, LcxAccelOption, LcxAccelStats, LcxMeshBuildCommand, check)
+from .scenes import MOD_DTYPE
+
+__all__ = ["AccelOption", "Mesh", "Accel", "HINT_FAST_TRACE", "HINT_FAST_BUILD", "REQUEST_FORCE_BUILD",
+           "REQUEST_PREFER_UPDATE", "NODES_FP32", "NODES_QUANT8", "stream_handle"]
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def stream_handle(stream) -> int | None:
+    """cudaStream_t of a torch stream (None = the current torch stream)."""
+    torch = _torch()
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return int(stream.cuda_stream) if hasattr(stream, "cuda_stream") else int(stream)
+
+
+class AccelOption:
+    """include/luisa/runtime/rhi/resource.h:94-125 (hint, allow_compaction, allow_update)."""
+
+    def __init__(self, hint: int = HINT_FAST_TRACE, allow_compaction: bool = True, allow_update: bool = False):
+        self.hint, self.allow_compaction, self.allow_update = hint, allow_compaction, allow_update
+
+    def c(self) -> LcxAccelOption:
+        return LcxAccelOption(self.hint, int(self.allow_compaction), int(self.allow_update))
+
+
+def _as_affine(transform) -> np.ndarray:
+    """4x4 (column vectors, as float4x4 rows here in row-major numpy) or 3x4 -> row-major 3x4
+    (the packing of Modification::set_transform, include/luisa/runtime/rhi/command.h:557-571)."""
+    m = np.asarray(transform, np.float32)
+    if m.shape == (4, 4):
+        m = m[:3, :]
+    return np.ascontiguousarray(m.reshape(12), np.float32)
+
+
+class Mesh:
+    """A BLAS over borrowed device vertex/triangle buffers."""
+
+    def __init__(self, vertices, triangles, option: AccelOption | None = None, vertex_stride: int | None = None):
+        torch = _torch()
+        self.lib = _capi.load()
+        self.vertices, self.triangles = vertices, triangles
+        if not (vertices.is_cuda and triangles.is_cuda):
+            raise ValueError("Mesh buffers must be CUDA tensors")
+        stride = vertex_stride or vertices.stride(0) * vertices.element_size()
+        self.vertex_stride = stride
+        self.vertex_size = vertices.shape[0] * stride
+        self.triangle_size = triangles.numel() * triangles.element_size()
+        if triangles.dtype not in (torch.int32, torch.uint32) or triangles.numel() % 3 != 0:
+            raise ValueError("triangles must be a (T, 3) int32/uint32 tensor")
+        h = ctypes.c_uint64(0)
+        check(self.lib.lcx_mesh_create(ctypes.byref((option or AccelOption()).c()), ctypes.byref(h)),
+              "lcx_mesh_create")
+        self.handle = h.value
+
+    def build(self, request: int = REQUEST_FORCE_BUILD, stream=None) -> "Mesh":
+        cmd = LcxMeshBuildCommand(request, 0, self.vertices.data_ptr(), 0, self.vertex_size, self.vertex_stride,
+                                  self.triangles.data_ptr(), 0, self.triangle_size)
+        check(self.lib.lcx_mesh_build(self.handle, ctypes.byref(cmd), stream_handle(stream)), "lcx_mesh_build")
+        return self
+
+    def stats(self) -> LcxAccelStats:
+        s = LcxAccelStats()
+        check(self.lib.lcx_mesh_stats(self.handle, ctypes.byref(s)), "lcx_mesh_stats")
+        return s
+
+    def destroy(self):
+        if getattr(self, "handle", 0):
+            check(self.lib.lcx_mesh_destroy(self.handle), "lcx_mesh_destroy")
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Accel:
+    """A TLAS over instanced meshes; modifications are staged and sent by build()."""
+
+    def __init__(self, option: AccelOption | None = None):
+        self.lib = _capi.load()
+        h = ctypes.c_uint64(0)
+        check(self.lib.lcx_accel_create(ctypes.byref((option or AccelOption()).c()), ctypes.byref(h)),
+              "lcx_accel_create")
+        self.handle = h.value
+        self._count = 0
+        self._mods: dict = {}
+        self._meshes: dict = {}  # keeps Python Mesh objects alive while referenced
+
+    def __len__(self):
+        return self._count
+
+    def _mod(self, index: int) -> np.ndarray:
+        if index not in self._mods:
+            m = np.zeros(1, MOD_DTYPE)[0]
+            m["index"] = index
+            self._mods[index] = m
+        return self._mods[index]
+
+    def emplace_back(self, mesh: Mesh, transform=None, visibility_mask: int = 0xFF, opaque: bool = True,
+                     user_id: int = 0) -> int:
+        index = self._count
+        m = self._mod(index)
+        m["primitive"] = mesh.handle
+        m["affine"] = _as_affine(np.eye(4) if transform is None else transform)
+        m["vis_mask"] = visibility_mask & 0xFF
+        m["user_id"] = user_id
+        m["flags"] = (MOD_PRIMITIVE | MOD_TRANSFORM | MOD_VISIBILITY | MOD_USER_ID |
+                      (MOD_OPAQUE_ON if opaque else MOD_OPAQUE_OFF))
+        self._meshes[index] = mesh
+        self._count += 1
+        return index
+
+    def emplace_back_many(self, meshes, affines: np.ndarray, masks=None):
+        """Bulk emplace_back: meshes[i] with row-major 3x4 affines[i]."""
+        n = len(meshes)
+        base = self._count
+        arr = np.zeros(n, MOD_DTYPE)
+        arr["index"] = np.arange(base, base + n)
+        arr["primitive"] = [m.handle for m in meshes]
+        arr["affine"] = np.asarray(affines, np.float32).reshape(n, 12)
+        arr["vis_mask"] = 0xFF if masks is None else np.asarray(masks) & 0xFF
+        arr["flags"] = MOD_PRIMITIVE | MOD_TRANSFORM | MOD_VISIBILITY | MOD_USER_ID | MOD_OPAQUE_ON
+        for i in range(n):
+            self._mods[base + i] = arr[i]
+            self._meshes[base + i] = meshes[i]
+        self._count += n
+
+    def pop_back(self):
+        if self._count == 0:
+            return  # the reference only warns (src/runtime/rtx/accel.cpp:108-110)
+        self._count -= 1
+        self._mods.pop(self._count, None)
+        self._meshes.pop(self._count, None)
+
+    def set_mesh_on_update(self, index: int, mesh: Mesh):
+        self._check_index(index)
+        m = self._mod(index)
+        m["primitive"] = mesh.handle
+        m["flags"] |= MOD_PRIMITIVE
+        self._meshes[index] = mesh
+
+    def set_transform_on_update(self, index: int, transform):
+        self._check_index(index)
+        m = self._mod(index)
+        m["affine"] = _as_affine(transform)
+        m["flags"] |= MOD_TRANSFORM
+
+    def set_visibility_on_update(self, index: int, visibility_mask: int):
+        self._check_index(index)
+        m = self._mod(index)
+        m["vis_mask"] = visibility_mask & 0xFF
+        m["flags"] |= MOD_VISIBILITY
+
+    def set_opaque_on_update(self, index: int, opaque: bool):
+        self._check_index(index)
+        m = self._mod(index)
+        m["flags"] = (m["flags"] & ~(MOD_OPAQUE_ON | MOD_OPAQUE_OFF)) | (MOD_OPAQUE_ON if opaque else MOD_OPAQUE_OFF)
+
+    def set_user_id_on_update(self, index: int, user_id: int):
+        self._check_index(index)
+        m = self._mod(index)
+        m["user_id"] = user_id
+        m["flags"] |= MOD_USER_ID
+
+    def _check_index(self, index: int):
+        if not 0 <= index < self._count:
+            raise IndexError(f"instance index {index} out of range [0, {self._count})")
+
+    def build(self, request: int = REQUEST_FORCE_BUILD, update_instance_buffer_only: bool = False,
+              stream=None) -> "Accel":
+        mods = np.array([self._mods[k] for k in sorted(self._mods)], MOD_DTYPE) if self._mods else \
+            np.zeros(0, MOD_DTYPE)
+        ptr = mods.ctypes.data if mods.size else None
+        check(self.lib.lcx_accel_build(self.handle, self._count, request, ptr, mods.size,
+                                       int(update_instance_buffer_only), stream_handle(stream)), "lcx_accel_build")
+        self._mods.clear()
+        return self
+
+    def stats(self) -> LcxAccelStats:
+        s = LcxAccelStats()
+        check(self.lib.lcx_accel_stats(self.handle, ctypes.byref(s)), "lcx_accel_stats")
+        return s
+
+    # ------------------------------------------------------------ queries
+    @staticmethod
+    def _rays_ptr(rays):
+        if not rays.is_cuda or not rays.is_contiguous() or rays.numel() * rays.element_size() % 32 != 0:
+            raise ValueError("rays must be a contiguous CUDA tensor of 32-byte Ray records")
+        return rays.data_ptr(), rays.numel() * rays.element_size() // 32
+
+    def trace_closest(self, rays, mask: int = 0xFF, out=None, layout: int = NODES_QUANT8, stream=None,
+                      counts=None):
+        """Closest hits as an (N, 6) int32 tensor of TriangleHit records (view floats with
+        ``hits_view``)."""
+        torch = _torch()
+        ptr, n = self._rays_ptr(rays)
+        if out is None:
+            out = torch.empty((n, 6), dtype=torch.int32, device=rays.device)
+        if counts is not None:
+            check(self.lib.lcx_trace_closest_counts(self.handle, ptr, n, mask, out.data_ptr(), counts.data_ptr(),
+                                                    layout, stream_handle(stream)), "lcx_trace_closest_counts")
+        else:
+            check(self.lib.lcx_trace_closest_ex(self.handle, ptr, n, mask, out.data_ptr(), layout,
+                                                stream_handle(stream)), "lcx_trace_closest")
+        return out
+
+    def trace_any(self, rays, mask: int = 0xFF, out=None, layout: int = NODES_QUANT8, stream=None):
+        torch = _torch()
+        ptr, n = self._rays_ptr(rays)
+        if out is None:
+            out = torch.empty(n, dtype=torch.uint8, device=rays.device)
+        check(self.lib.lcx_trace_any_ex(self.handle, ptr, n, mask, out.data_ptr(), layout, stream_handle(stream)),
+              "lcx_trace_any")
+        return out
+
+    def destroy(self):
+        if getattr(self, "handle", 0):
+            check(self.lib.lcx_accel_destroy(self.handle), "lcx_accel_destroy")
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def hits_to_numpy(hits) -> np.ndarray:
+    """(N, 6) int32 device tensor -> numpy TriangleHit records."""
+    from .scenes import HIT_DTYPE
+    return hits.cpu().numpy().view(HIT_DTYPE).reshape(-1)
+
+
+def rays_to_device(rays: np.ndarray, device="cuda"):
+    torch = _torch()
+    return torch.from_numpy(np.ascontiguousarray(rays).view(np.float32).reshape(-1, 8)).to(device)
+
+
+def mesh_from_data(md, device="cuda", option: AccelOption | None = None) -> Mesh:
+    torch = _torch()
+    v = torch.from_numpy(np.ascontiguousarray(md.vertices, np.float32)).to(device)
+    t = torch.from_numpy(np.ascontiguousarray(md.triangles).astype(np.int32)).to(device)
+    return Mesh(v, t, option)
+
+
+def accel_from_scene(scene, device="cuda", option: AccelOption | None = None, stream=None):
+    """Build every mesh and one TLAS for a scenes.Scene; returns (accel, meshes)."""
+    meshes = [mesh_from_data(m, device, option).build(stream=stream) for m in scene.meshes]
+    acc = Accel(option)
+    acc.emplace_back_many([meshes[i] for i in scene.inst_mesh], scene.inst_affine, scene.inst_mask)
+    acc.build(stream=stream)
+    return acc, meshes

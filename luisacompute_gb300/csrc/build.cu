@@ -1,0 +1,752 @@
+// build.cu — BVH construction kernels for sm_103a.
+//
+// BLAS (MeshBuildCommand, replacing Embree's rtcCommitScene in
+// src/rust/luisa_compute_backend_impl/src/cpu/accel.rs:205-260 and OptiX
+// accelBuild in src/backends/cuda/cuda_primitive.cpp:20-113) and TLAS
+// (AccelBuildCommand, replacing accel.rs:324-447 and the update_accel kernels
+// of src/backends/cuda/cuda_builtin/cuda_builtin_kernels.cu:42-111 plus the
+// IAS build of cuda_accel.cpp:26-126) share one pipeline over item boxes:
+//
+//   prep    item boxes + centroid bounds            (one thread per item)
+//   morton  63-bit Morton keys of the centroids      (one thread per item)
+//   sort    key/value radix sort                     (CUB, sort.cu)
+//   lbvh    binary radix tree + boxes, bottom-up in one pass (Apetrei 2014,
+//           "Fast and Simple Agglomerative LBVH Construction")
+//   collapse  top-down, level-synchronous inside one cooperative launch:
+//           each wide node opens its largest-area children until it has 8,
+//           subtrees of <= leaf_max items become leaf slots, children are
+//           assigned to octant slots, and internal children get contiguous
+//           node indices
+//   emit    both node layouts (FP32 and outward-rounded 8-bit) and the leaf
+//           items in traversal order
+#include <cooperative_groups.h>
+
+#include <cfloat>
+
+#include "lcx_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace lcx {
+namespace {
+
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr int kPrepBlock = 256;
+
+__device__ __forceinline__ unsigned long long spread21(uint32_t v) {
+    unsigned long long x = v & 0x1fffffu;
+    x = (x | x << 32) & 0x1f00000000ffffull;
+    x = (x | x << 16) & 0x1f0000ff0000ffull;
+    x = (x | x << 8) & 0x100f00f00f00f00full;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+    x = (x | x << 2) & 0x1249249249249249ull;
+    return x;
+}
+
+__device__ __forceinline__ bool box_empty(const float4 &lo, const float4 &hi) {
+    return !(lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z);
+}
+
+__device__ __forceinline__ float box_area(const float4 &lo, const float4 &hi) {
+    if (box_empty(lo, hi)) return 0.0f;
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+// Block-wide reduction of centroid bounds into the control block.
+__device__ __forceinline__ void reduce_centroid_bounds(float cmin[3], float cmax[3], uint32_t *ctl) {
+    __shared__ float smin[3][kPrepBlock / 32], smax[3][kPrepBlock / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float a = cmin[k], b = cmax[k];
+        for (int o = 16; o; o >>= 1) {
+            a = fminf(a, __shfl_xor_sync(~0u, a, o));
+            b = fmaxf(b, __shfl_xor_sync(~0u, b, o));
+        }
+        if (lane == 0) {
+            smin[k][warp] = a;
+            smax[k][warp] = b;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        float a = FLT_MAX, b = -FLT_MAX;
+        for (int w = 0; w < int(blockDim.x >> 5); w++) {
+            a = fminf(a, smin[k][w]);
+            b = fmaxf(b, smax[k][w]);
+        }
+        if (a <= b) {
+            atomicMin(&ctl[kCtlCenLo + k], float_to_ordered(a));
+            atomicMax(&ctl[kCtlCenHi + k], float_to_ordered(b));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kPrepBlock) k_tri_prep(TriInput in, uint32_t n, float4 *lo, float4 *hi,
+                                                         uint32_t *ctl) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    if (i < n) {
+        const uint32_t *t = reinterpret_cast<const uint32_t *>(in.tbase + 12ull * i);
+        const uint32_t i0 = t[0], i1 = t[1], i2 = t[2];
+        float4 l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f), h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
+        if (i0 >= in.vcount || i1 >= in.vcount || i2 >= in.vcount) {
+            atomicOr(&ctl[kCtlErr], kErrBadIndex);
+        } else {
+            const float4 a = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * i0));
+            const float4 b = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * i1));
+            const float4 c = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * i2));
+            l.x = fminf(fminf(l.x, a.x), fminf(b.x, c.x));
+            l.y = fminf(fminf(l.y, a.y), fminf(b.y, c.y));
+            l.z = fminf(fminf(l.z, a.z), fminf(b.z, c.z));
+            h.x = fmaxf(fmaxf(h.x, a.x), fmaxf(b.x, c.x));
+            h.y = fmaxf(fmaxf(h.y, a.y), fmaxf(b.y, c.y));
+            h.z = fmaxf(fmaxf(h.z, a.z), fmaxf(b.z, c.z));
+        }
+        if (box_empty(l, h)) {
+            l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f);
+            h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
+        } else {
+            cmin[0] = cmax[0] = 0.5f * (l.x + h.x);
+            cmin[1] = cmax[1] = 0.5f * (l.y + h.y);
+            cmin[2] = cmax[2] = 0.5f * (l.z + h.z);
+        }
+        lo[i] = l;
+        hi[i] = h;
+    }
+    reduce_centroid_bounds(cmin, cmax, ctl);
+}
+
+__global__ void __launch_bounds__(kPrepBlock) k_inst_prep(const InstState *inst, uint32_t n, float4 *lo, float4 *hi,
+                                                          float *w2o, uint32_t *ctl) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    if (i < n) {
+        const InstState &s = inst[i];
+        float m[12], w[12];
+#pragma unroll
+        for (int k = 0; k < 12; k++) m[k] = s.o2w[k];
+        affine_inverse(m, w);
+#pragma unroll
+        for (int k = 0; k < 12; k++) w2o[12ull * i + k] = w[k];
+        float4 l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f), h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
+        const BlasDesc *d = s.blas;
+        if (d != nullptr && d->valid) {
+            const float blo[3] = {d->lo[0], d->lo[1], d->lo[2]}, bhi[3] = {d->hi[0], d->hi[1], d->hi[2]};
+            float wl[3], wh[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                // interval arithmetic on the affine map, then an outward pad
+                // that covers the FP32 rounding of the sums
+                float a = m[4 * k + 3], b = m[4 * k + 3], mag = fabsf(m[4 * k + 3]);
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    const float e0 = m[4 * k + j] * blo[j], e1 = m[4 * k + j] * bhi[j];
+                    a += fminf(e0, e1);
+                    b += fmaxf(e0, e1);
+                    mag += fmaxf(fabsf(e0), fabsf(e1));
+                }
+                const float pad = mag * 0x1p-20f;
+                wl[k] = a - pad;
+                wh[k] = b + pad;
+            }
+            l = make_float4(wl[0], wl[1], wl[2], 0.0f);
+            h = make_float4(wh[0], wh[1], wh[2], 0.0f);
+            if (box_empty(l, h)) {
+                l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f);
+                h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
+            } else {
+                cmin[0] = cmax[0] = 0.5f * (l.x + h.x);
+                cmin[1] = cmax[1] = 0.5f * (l.y + h.y);
+                cmin[2] = cmax[2] = 0.5f * (l.z + h.z);
+            }
+        }
+        lo[i] = l;
+        hi[i] = h;
+    }
+    reduce_centroid_bounds(cmin, cmax, ctl);
+}
+
+__global__ void k_morton(uint32_t n, const float4 *lo, const float4 *hi, const uint32_t *ctl,
+                         unsigned long long *keys, uint32_t *vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 l = lo[i], h = hi[i];
+    unsigned long long key = 0x7fffffffffffffffull;  // empty boxes sort last
+    if (!box_empty(l, h)) {
+        const float c[3] = {0.5f * (l.x + h.x), 0.5f * (l.y + h.y), 0.5f * (l.z + h.z)};
+        uint32_t q[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float blo = ordered_to_float(ctl[kCtlCenLo + k]);
+            const float bhi = ordered_to_float(ctl[kCtlCenHi + k]);
+            const float ext = bhi - blo;
+            float f = ext > 0.0f ? (c[k] - blo) / ext : 0.0f;
+            f = fminf(fmaxf(f, 0.0f), 1.0f);
+            q[k] = min(uint32_t(f * 2097151.0f), 2097151u);
+        }
+        key = spread21(q[0]) << 2 | spread21(q[1]) << 1 | spread21(q[2]);
+    }
+    keys[i] = key;
+    vals[i] = i;
+}
+
+// delta(a) < delta(b) with delta(i) = (key_i ^ key_i+1, i ^ i+1) in lexicographic order.
+__device__ __forceinline__ bool delta_less(const unsigned long long *k, uint32_t a, uint32_t b) {
+    const unsigned long long da = k[a] ^ k[a + 1], db = k[b] ^ k[b + 1];
+    if (da != db) return da < db;
+    return (a ^ (a + 1)) < (b ^ (b + 1));
+}
+
+__global__ void k_lbvh(uint32_t n, const unsigned long long *keys, const uint32_t *vals, const float4 *lo,
+                       const float4 *hi, uint32_t *bin_child, float4 *bin_lo, float4 *bin_hi, int32_t *other,
+                       uint32_t *ctl) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (n == 1) {
+        ctl[kCtlRoot] = kLeafBit;
+        return;
+    }
+    uint32_t cur = kLeafBit | i;
+    uint32_t l = i, r = i;
+    const uint32_t item = vals[i];
+    float4 clo = lo[item], chi = hi[item];
+    for (uint32_t guard = 0; guard < n; guard++) {
+        const bool left = (l == 0) || (r != n - 1 && delta_less(keys, r, l - 1));
+        const uint32_t parent = left ? r : l - 1;
+        bin_child[2 * parent + (left ? 0 : 1)] = cur;
+        __threadfence();
+        const int32_t prev = atomicExch(&other[parent], left ? int32_t(l) : int32_t(r));
+        if (prev < 0) return;  // the sibling finishes the parent
+        __threadfence();
+        if (left)
+            r = uint32_t(prev);
+        else
+            l = uint32_t(prev);
+        const uint32_t sib = __ldcg(&bin_child[2 * parent + (left ? 1 : 0)]);
+        float4 slo, shi;
+        if (sib & kLeafBit) {
+            const uint32_t it = vals[sib & ~kLeafBit];
+            slo = lo[it];
+            shi = hi[it];
+        } else {
+            slo = __ldcg(&bin_lo[sib]);
+            shi = __ldcg(&bin_hi[sib]);
+        }
+        clo = make_float4(fminf(clo.x, slo.x), fminf(clo.y, slo.y), fminf(clo.z, slo.z), 0.0f);
+        chi = make_float4(fmaxf(chi.x, shi.x), fmaxf(chi.y, shi.y), fmaxf(chi.z, shi.z), 0.0f);
+        bin_lo[parent] = make_float4(clo.x, clo.y, clo.z, __uint_as_float(r - l + 1));
+        bin_hi[parent] = make_float4(chi.x, chi.y, chi.z, __uint_as_float(l));
+        cur = parent;
+        if (l == 0 && r == n - 1) {
+            ctl[kCtlRoot] = parent;
+            return;
+        }
+    }
+}
+
+struct TreeView {
+    const uint32_t *child;
+    const float4 *blo, *bhi;
+    const float4 *lo, *hi;  // item boxes
+    const uint32_t *vals;   // sorted item ids
+    __device__ __forceinline__ bool leaf(uint32_t id) const { return (id & kLeafBit) != 0; }
+    __device__ __forceinline__ uint32_t count(uint32_t id) const {
+        return leaf(id) ? 1u : __float_as_uint(blo[id].w);
+    }
+    __device__ __forceinline__ uint32_t first(uint32_t id) const {
+        return leaf(id) ? (id & ~kLeafBit) : __float_as_uint(bhi[id].w);
+    }
+    __device__ __forceinline__ void box(uint32_t id, float4 &l, float4 &h) const {
+        if (leaf(id)) {
+            const uint32_t it = vals[id & ~kLeafBit];
+            l = lo[it];
+            h = hi[it];
+        } else {
+            l = blo[id];
+            h = bhi[id];
+        }
+    }
+};
+
+// Open up to 8 children of binary node b, assign them to octant slots and
+// allocate their wide-node / item ranges.  desc: 12 words per wide node.
+__device__ void collapse_node(const TreeView &tv, uint32_t b, uint32_t w, int leaf_max, uint32_t *desc,
+                              uint2 *qout, uint32_t *ctl, int level) {
+    uint32_t C[8];
+    float A[8];
+    int nC;
+    if (tv.leaf(b)) {
+        C[0] = b;
+        nC = 1;
+    } else {
+        C[0] = tv.child[2 * b];
+        C[1] = tv.child[2 * b + 1];
+        nC = 2;
+    }
+    for (int k = 0; k < nC; k++) {
+        float4 l, h;
+        tv.box(C[k], l, h);
+        A[k] = box_area(l, h);
+    }
+    while (nC < 8) {
+        int best = -1;
+        float best_a = -1.0f;
+        for (int k = 0; k < nC; k++) {
+            if (!tv.leaf(C[k]) && tv.count(C[k]) > uint32_t(leaf_max) && A[k] > best_a) {
+                best_a = A[k];
+                best = k;
+            }
+        }
+        if (best < 0) break;
+        const uint32_t x = C[best];
+        C[best] = tv.child[2 * x];
+        C[nC] = tv.child[2 * x + 1];
+        float4 l, h;
+        tv.box(C[best], l, h);
+        A[best] = box_area(l, h);
+        tv.box(C[nC], l, h);
+        A[nC] = box_area(l, h);
+        nC++;
+    }
+    // octant slot assignment: greedy on dot(child centroid - node centroid, octant diagonal)
+    float4 nl, nh;
+    tv.box(b, nl, nh);
+    const float pc[3] = {0.5f * (nl.x + nh.x), 0.5f * (nl.y + nh.y), 0.5f * (nl.z + nh.z)};
+    float off[8][3];
+    for (int k = 0; k < nC; k++) {
+        float4 l, h;
+        tv.box(C[k], l, h);
+        if (box_empty(l, h)) {
+            off[k][0] = off[k][1] = off[k][2] = 0.0f;
+        } else {
+            off[k][0] = 0.5f * (l.x + h.x) - pc[0];
+            off[k][1] = 0.5f * (l.y + h.y) - pc[1];
+            off[k][2] = 0.5f * (l.z + h.z) - pc[2];
+        }
+    }
+    uint32_t slot_child[8];
+    for (int s = 0; s < 8; s++) slot_child[s] = kInvalid;
+    uint32_t used_slots = 0, used_children = 0;
+    for (int it = 0; it < nC; it++) {
+        float best = -FLT_MAX;
+        int bk = -1, bs = -1;
+        for (int k = 0; k < nC; k++) {
+            if (used_children >> k & 1u) continue;
+            for (int s = 0; s < 8; s++) {
+                if (used_slots >> s & 1u) continue;
+                const float sc = ((s & 1) ? -off[k][0] : off[k][0]) + ((s & 2) ? -off[k][1] : off[k][1]) +
+                                 ((s & 4) ? -off[k][2] : off[k][2]);
+                if (sc > best) {
+                    best = sc;
+                    bk = k;
+                    bs = s;
+                }
+            }
+        }
+        used_children |= 1u << bk;
+        used_slots |= 1u << bs;
+        slot_child[bs] = C[bk];
+    }
+    uint32_t n_int = 0, n_items = 0;
+    for (int s = 0; s < 8; s++) {
+        const uint32_t c = slot_child[s];
+        if (c == kInvalid) continue;
+        const uint32_t cnt = tv.count(c);
+        if (!tv.leaf(c) && cnt > uint32_t(leaf_max))
+            n_int++;
+        else
+            n_items += cnt;
+    }
+    const uint32_t child_base = n_int ? atomicAdd(&ctl[kCtlWideCount], n_int) : 0u;
+    const uint32_t item_base = n_items ? atomicAdd(&ctl[kCtlItemCount], n_items) : 0u;
+    const uint32_t qbase = n_int ? atomicAdd(&ctl[kCtlLevel + level + 1], n_int) : 0u;
+    uint32_t *d = desc + 12ull * w;
+    d[0] = b;
+    d[1] = child_base;
+    d[2] = item_base;
+    d[3] = 0;
+    uint32_t rank = 0;
+    for (int s = 0; s < 8; s++) {
+        const uint32_t c = slot_child[s];
+        d[4 + s] = c;
+        if (c != kInvalid && !tv.leaf(c) && tv.count(c) > uint32_t(leaf_max)) {
+            qout[qbase + rank] = make_uint2(c, child_base + rank);
+            rank++;
+        }
+    }
+}
+
+__global__ void k_collapse(TreeView tv, uint32_t n, int leaf_max, uint32_t *desc, uint2 *q0, uint2 *q1,
+                           uint32_t *ctl) {
+    cg::grid_group grid = cg::this_grid();
+    if (grid.thread_rank() == 0) {
+        q0[0] = make_uint2(ctl[kCtlRoot], 0u);
+        ctl[kCtlLevel + 0] = 1u;
+        ctl[kCtlWideCount] = 1u;
+    }
+    grid.sync();
+    int level = 0;
+    for (; level < kMaxLevels; level++) {
+        const uint32_t cnt = __ldcg(&ctl[kCtlLevel + level]);
+        if (cnt == 0) break;
+        const uint2 *qin = (level & 1) ? q1 : q0;
+        uint2 *qout = (level & 1) ? q0 : q1;
+        for (unsigned long long t = grid.thread_rank(); t < cnt; t += grid.size()) {
+            const uint2 task = qin[t];
+            collapse_node(tv, task.x, task.y, leaf_max, desc, qout, ctl, level);
+        }
+        grid.sync();
+    }
+    if (grid.thread_rank() == 0) {
+        ctl[kCtlDepth] = uint32_t(level);
+        if (level == kMaxLevels && __ldcg(&ctl[kCtlLevel + kMaxLevels]) != 0) atomicOr(&ctl[kCtlErr], kErrTooDeep);
+    }
+}
+
+// ---- emit
+__device__ __forceinline__ uint32_t quant_exp(float lo, float hi) {
+    const float x = __fdiv_ru(__fsub_ru(hi, lo), 255.0f);
+    const uint32_t bits = __float_as_uint(x);
+    uint32_t b = bits >> 23;
+    if (b == 0) return 1u;  // zero or subnormal extent: 2^-126
+    if (bits & 0x7fffffu) b += 1;
+    return min(b, 254u);
+}
+
+template <class ItemWriter>
+__device__ void emit_node(const TreeView &tv, const uint32_t *desc, uint32_t w, Node8Q *qn, Node8F *fn,
+                          int leaf_max, uint32_t *ctl, ItemWriter &&write_item, float4 &root_lo, float4 &root_hi) {
+    const uint32_t *d = desc + 12ull * w;
+    const uint32_t b = d[0], child_base = d[1], item_base = d[2];
+    float4 nl, nh;
+    tv.box(b, nl, nh);
+    root_lo = nl;
+    root_hi = nh;
+    const bool node_empty = box_empty(nl, nh);
+    const float p[3] = {node_empty ? 0.0f : nl.x, node_empty ? 0.0f : nl.y, node_empty ? 0.0f : nl.z};
+    uint32_t ex[3];
+    ex[0] = node_empty ? 127u : quant_exp(nl.x, nh.x);
+    ex[1] = node_empty ? 127u : quant_exp(nl.y, nh.y);
+    ex[2] = node_empty ? 127u : quant_exp(nl.z, nh.z);
+    Node8Q q;
+    Node8F f;
+    q.px = p[0];
+    q.py = p[1];
+    q.pz = p[2];
+    uint32_t meta_lo = 0, meta_hi = 0, imask = 0, offset = 0;
+    uint32_t qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}}, qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    for (int s = 0; s < 8; s++) {
+        const uint32_t c = d[4 + s];
+        uint32_t meta = 0;
+        float cl[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, ch[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        uint32_t ql[3] = {255u, 255u, 255u}, qh[3] = {0u, 0u, 0u};
+        if (c != kInvalid) {
+            float4 l, h;
+            tv.box(c, l, h);
+            const bool empty = box_empty(l, h);
+            const uint32_t cnt = tv.count(c);
+            if (!tv.leaf(c) && cnt > uint32_t(leaf_max)) {
+                imask |= 1u << s;
+                meta = kMetaInternal;
+            } else {
+                meta = empty ? 0u : ((cnt << 5) | offset);
+                const uint32_t first = tv.first(c);
+                for (uint32_t j = 0; j < cnt; j++) write_item(item_base + offset + j, tv.vals[first + j]);
+                offset += cnt;
+            }
+            if (!empty) {
+                cl[0] = l.x;
+                cl[1] = l.y;
+                cl[2] = l.z;
+                ch[0] = h.x;
+                ch[1] = h.y;
+                ch[2] = h.z;
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const float e = __uint_as_float(ex[k] << 23);
+                    float a = floorf(__fdiv_rd(__fsub_rd(cl[k], p[k]), e));
+                    float z = ceilf(__fdiv_ru(__fsub_ru(ch[k], p[k]), e));
+                    if (!(a >= 0.0f) || !(z <= 255.0f)) atomicOr(&ctl[kCtlErr], kErrQuant);
+                    ql[k] = uint32_t(fminf(fmaxf(a, 0.0f), 255.0f));
+                    qh[k] = uint32_t(fminf(fmaxf(z, 0.0f), 255.0f));
+                }
+            }
+        }
+        const int wsel = s >> 2, sh = (s & 3) * 8;
+        if (wsel == 0)
+            meta_lo |= meta << sh;
+        else
+            meta_hi |= meta << sh;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            qlo[k][wsel] |= ql[k] << sh;
+            qhi[k][wsel] |= qh[k] << sh;
+        }
+        f.lo_x[s] = cl[0];
+        f.lo_y[s] = cl[1];
+        f.lo_z[s] = cl[2];
+        f.hi_x[s] = ch[0];
+        f.hi_y[s] = ch[1];
+        f.hi_z[s] = ch[2];
+    }
+    q.exps = ex[0] | (ex[1] << 8) | (ex[2] << 16) | (imask << 24);
+    q.child_base = child_base;
+    q.item_base = item_base;
+    q.meta_lo = meta_lo;
+    q.meta_hi = meta_hi;
+    for (int k = 0; k < 2; k++) {
+        q.qlo_x[k] = qlo[0][k];
+        q.qlo_y[k] = qlo[1][k];
+        q.qlo_z[k] = qlo[2][k];
+        q.qhi_x[k] = qhi[0][k];
+        q.qhi_y[k] = qhi[1][k];
+        q.qhi_z[k] = qhi[2][k];
+    }
+    f.child_base = child_base;
+    f.item_base = item_base;
+    f.meta_lo = meta_lo;
+    f.meta_hi = meta_hi;
+    qn[w] = q;
+    fn[w] = f;
+}
+
+__global__ void k_emit_blas(TreeView tv, const uint32_t *desc, uint32_t wide_count, int leaf_max, TriInput in,
+                            Node8Q *qn, Node8F *fn, TriRec *tris, BlasDesc *bdesc, uint32_t *ctl, uint32_t tri_count) {
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= wide_count) return;
+    float4 rl, rh;
+    emit_node(
+        tv, desc, w, qn, fn, leaf_max, ctl,
+        [&](uint32_t pos, uint32_t prim) {
+            const uint32_t *t = reinterpret_cast<const uint32_t *>(in.tbase + 12ull * prim);
+            float4 a = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * t[0]));
+            float4 b = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * t[1]));
+            float4 c = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * t[2]));
+            a.w = __uint_as_float(prim);
+            b.w = 0.0f;
+            c.w = 0.0f;
+            tris[pos] = TriRec{a, b, c};
+        },
+        rl, rh);
+    if (w == 0) {
+        bdesc->qnodes = qn;
+        bdesc->fnodes = fn;
+        bdesc->tris = tris;
+        bdesc->node_count = wide_count;
+        bdesc->tri_count = tri_count;
+        const bool empty = box_empty(rl, rh);
+        bdesc->lo[0] = rl.x;
+        bdesc->lo[1] = rl.y;
+        bdesc->lo[2] = rl.z;
+        bdesc->hi[0] = rh.x;
+        bdesc->hi[1] = rh.y;
+        bdesc->hi[2] = rh.z;
+        bdesc->depth = ctl[kCtlDepth];
+        bdesc->valid = empty ? 0u : 1u;
+    }
+}
+
+__global__ void k_emit_tlas(TreeView tv, const uint32_t *desc, uint32_t wide_count, int leaf_max,
+                            const InstState *inst, const float *w2o, Node8Q *qn, Node8F *fn, InstRec *recs,
+                            uint32_t *ctl) {
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= wide_count) return;
+    float4 rl, rh;
+    emit_node(
+        tv, desc, w, qn, fn, leaf_max, ctl,
+        [&](uint32_t pos, uint32_t id) {
+            InstRec r;
+#pragma unroll
+            for (int k = 0; k < 12; k++) r.w2o[k] = w2o[12ull * id + k];
+            const InstState &s = inst[id];
+            const BlasDesc *d = s.blas;
+            const bool ok = d != nullptr && d->valid;
+            r.qnodes = ok ? d->qnodes : nullptr;
+            r.tris = ok ? d->tris : nullptr;
+            r.fnodes = ok ? d->fnodes : nullptr;
+            r.inst_id = id;
+            r.mask = ok ? (s.mask & 0xffu) : 0u;
+            recs[pos] = r;
+        },
+        rl, rh);
+}
+
+__global__ void k_apply_mods(const ModRec *mods, uint32_t count, InstState *inst, uint32_t instance_count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const ModRec m = mods[i];
+    if (m.index >= instance_count) return;  // validated on the host
+    InstState &s = inst[m.index];
+    // Modification flags: include/luisa/runtime/rhi/command.h:537-543
+    if (m.flags & 1u) s.blas = reinterpret_cast<const BlasDesc *>(m.primitive);
+    if (m.flags & 2u)
+        for (int k = 0; k < 12; k++) s.o2w[k] = m.affine[k];
+    if (m.flags & 4u) s.opaque = 1u;
+    else if (m.flags & 8u) s.opaque = 0u;
+    if (m.flags & 16u) s.mask = m.vis_mask & 0xffu;
+    if (m.flags & 32u) s.user_id = m.user_id;
+}
+
+__global__ void k_init_instances(InstState *inst, uint32_t begin, uint32_t end) {
+    const uint32_t i = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= end) return;
+    InstState s;
+    const float id[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    for (int k = 0; k < 12; k++) s.o2w[k] = id[k];
+    s.blas = nullptr;
+    s.mask = 0xffu;  // default visibility (accel.rs:289)
+    s.user_id = 0;
+    s.opaque = 1u;
+    s._pad[0] = s._pad[1] = s._pad[2] = 0;
+    inst[i] = s;
+}
+
+__global__ void k_wide_sah(const Node8F *fn, uint32_t wide_count, double *out) {
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0, root = 0.0;
+    auto area = [](float lx, float ly, float lz, float hx, float hy, float hz) -> double {
+        if (!(lx <= hx && ly <= hy && lz <= hz)) return 0.0;
+        const double dx = double(hx) - lx, dy = double(hy) - ly, dz = double(hz) - lz;
+        return 2.0 * (dx * dy + dy * dz + dz * dx);
+    };
+    if (w < wide_count) {
+        const Node8F &f = fn[w];
+        float lx = FLT_MAX, ly = FLT_MAX, lz = FLT_MAX, hx = -FLT_MAX, hy = -FLT_MAX, hz = -FLT_MAX;
+        for (int s = 0; s < 8; s++) {
+            const uint32_t meta = ((s < 4 ? f.meta_lo : f.meta_hi) >> ((s & 3) * 8)) & 0xffu;
+            if (meta == 0 || !(f.lo_x[s] <= f.hi_x[s])) continue;
+            lx = fminf(lx, f.lo_x[s]);
+            ly = fminf(ly, f.lo_y[s]);
+            lz = fminf(lz, f.lo_z[s]);
+            hx = fmaxf(hx, f.hi_x[s]);
+            hy = fmaxf(hy, f.hi_y[s]);
+            hz = fmaxf(hz, f.hi_z[s]);
+            if (!(meta & kMetaInternal))
+                acc += double(meta >> 5) * area(f.lo_x[s], f.lo_y[s], f.lo_z[s], f.hi_x[s], f.hi_y[s], f.hi_z[s]);
+        }
+        const double a = area(lx, ly, lz, hx, hy, hz);
+        acc += a;
+        if (w == 0) root = a;
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(~0u, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(&out[0], acc);
+    if (w == 0) out[1] = root;
+}
+
+// SAH of the binary LBVH (C_node = C_item = 1); out[0] = sum of areas,
+// out[1] = root area.
+__global__ void k_binary_sah(uint32_t n, const float4 *blo, const float4 *bhi, const float4 *lo, const float4 *hi,
+                             const uint32_t *ctl, double *out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (i < n) {
+        acc += box_area(lo[i], hi[i]);
+        if (i + 1 < n) acc += box_area(blo[i], bhi[i]);
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(~0u, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(&out[0], acc);
+    if (i == 0) {
+        const uint32_t r = ctl[kCtlRoot];
+        out[1] = (r & kLeafBit) ? box_area(lo[0], hi[0]) : box_area(blo[r], bhi[r]);
+    }
+}
+
+inline unsigned blocks_for(uint64_t n, unsigned bs) { return unsigned((n + bs - 1) / bs); }
+
+TreeView make_view(const BuildScratch &s) {
+    TreeView tv;
+    tv.child = s.bin_child;
+    tv.blo = s.bin_lo;
+    tv.bhi = s.bin_hi;
+    tv.lo = s.box_lo;
+    tv.hi = s.box_hi;
+    tv.vals = s.vals_sorted;
+    return tv;
+}
+
+cudaError_t build_common(uint32_t n, int leaf_max, BuildScratch &s, cudaStream_t st) {
+    k_morton<<<blocks_for(n, 256), 256, 0, st>>>(n, s.box_lo, s.box_hi, s.ctl, s.keys, s.vals);
+    cudaError_t e = sort_pairs(s.sort_tmp, s.sort_tmp_bytes, s.keys, s.keys_sorted, s.vals, s.vals_sorted, n, st);
+    if (e != cudaSuccess) return e;
+    if (n > 1) {
+        e = cudaMemsetAsync(s.other, 0xff, sizeof(int32_t) * (n - 1), st);
+        if (e != cudaSuccess) return e;
+    }
+    k_lbvh<<<blocks_for(n, 256), 256, 0, st>>>(n, s.keys_sorted, s.vals_sorted, s.box_lo, s.box_hi, s.bin_child,
+                                                 s.bin_lo, s.bin_hi, s.other, s.ctl);
+    // cooperative collapse: grid = co-resident blocks
+    static int grid = 0;
+    if (grid == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse, 128, 0);
+        grid = sms * (per_sm > 2 ? 2 : (per_sm > 0 ? per_sm : 1));
+    }
+    TreeView tv = make_view(s);
+    uint32_t nn = n;
+    int lm = leaf_max;
+    uint32_t *desc = s.desc;
+    uint2 *q0 = s.queue, *q1 = s.queue + (n + 1);
+    uint32_t *ctl = s.ctl;
+    void *args[] = {&tv, &nn, &lm, &desc, &q0, &q1, &ctl};
+    return cudaLaunchCooperativeKernel(reinterpret_cast<void *>(k_collapse), dim3(grid), dim3(128), args, 0, st);
+}
+
+}  // namespace
+
+cudaError_t build_tree_tris(const TriInput &in, uint32_t n, int leaf_max, BuildScratch &s, cudaStream_t st) {
+    k_tri_prep<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(in, n, s.box_lo, s.box_hi, s.ctl);
+    return build_common(n, leaf_max, s, st);
+}
+
+cudaError_t build_tree_insts(const InstState *inst, uint32_t n, int leaf_max, BuildScratch &s, cudaStream_t st) {
+    k_inst_prep<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(inst, n, s.box_lo, s.box_hi, s.w2o, s.ctl);
+    return build_common(n, leaf_max, s, st);
+}
+
+cudaError_t emit_blas(const TriInput &in, uint32_t n, int leaf_max, uint32_t wide_count, const BuildScratch &s,
+                      Node8Q *qn, Node8F *fn, TriRec *tris, BlasDesc *desc, cudaStream_t st) {
+    k_emit_blas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.desc, wide_count, leaf_max, in, qn, fn,
+                                                              tris, desc, s.ctl, n);
+    return cudaGetLastError();
+}
+
+cudaError_t emit_tlas(const InstState *inst, uint32_t n, int leaf_max, uint32_t wide_count, const BuildScratch &s,
+                      Node8Q *qn, Node8F *fn, InstRec *recs, cudaStream_t st) {
+    (void)n;
+    k_emit_tlas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.desc, wide_count, leaf_max, inst, s.w2o,
+                                                              qn, fn, recs, s.ctl);
+    return cudaGetLastError();
+}
+
+cudaError_t apply_modifications(const ModRec *mods, uint32_t count, InstState *inst, uint32_t instance_count,
+                                cudaStream_t st) {
+    if (count == 0) return cudaSuccess;
+    k_apply_mods<<<blocks_for(count, 256), 256, 0, st>>>(mods, count, inst, instance_count);
+    return cudaGetLastError();
+}
+
+cudaError_t init_instances(InstState *inst, uint32_t begin, uint32_t end, cudaStream_t st) {
+    if (end <= begin) return cudaSuccess;
+    k_init_instances<<<blocks_for(end - begin, 256), 256, 0, st>>>(inst, begin, end);
+    return cudaGetLastError();
+}
+
+cudaError_t binary_sah(const BuildScratch &s, uint32_t n, cudaStream_t st) {
+    double *out = reinterpret_cast<double *>(s.ctl + kCtlWords);
+    k_binary_sah<<<blocks_for(n, 256), 256, 0, st>>>(n, s.bin_lo, s.bin_hi, s.box_lo, s.box_hi, s.ctl, out);
+    return cudaGetLastError();
+}
+
+cudaError_t wide_sah(const Node8F *fn, uint32_t wide_count, double *d_out, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(d_out, 0, 2 * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+    k_wide_sah<<<blocks_for(wide_count, 256), 256, 0, st>>>(fn, wide_count, d_out);
+    return cudaGetLastError();
+}
+
+}  // namespace lcx

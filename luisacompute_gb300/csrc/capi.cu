@@ -1,0 +1,610 @@
+// capi.cu — the C ABI (include/lcx_accel.h): handle registry, argument
+// validation, device memory ownership and orchestration of the build and
+// trace kernels.  Mirrors the reference's DeviceInterface accel entry points
+// (include/luisa/runtime/rhi/device_interface.h:171-184) and the command
+// visits of its backends (CUDA: src/backends/cuda/cuda_command_encoder.cpp:235-243;
+// CPU: src/rust/luisa_compute_backend_impl/src/cpu/stream.rs:410-428), with
+// status codes in place of the reference's aborts.
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "lcx_internal.h"
+
+using namespace lcx;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    cudaGetLastError();  // clear sticky-free errors
+    return fail(e == cudaErrorMemoryAllocation ? LCX_ERR_OOM : LCX_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define LCX_CUDA(call, what)                               \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+constexpr uint32_t kPoolSlots = 4096;  // trace-call counters (16 B each)
+
+struct DeviceState {
+    int device = -1;
+    uint32_t *pool = nullptr;  // kPoolSlots x 4 words
+    std::atomic<uint32_t> next_slot{0};
+};
+
+std::mutex g_dev_mtx;
+DeviceState g_dev[16];
+
+int current_device_state(DeviceState **out) {
+    int dev = 0;
+    LCX_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= 16) return fail(LCX_ERR_INVALID_ARG, "device index %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_dev_mtx);
+    DeviceState &s = g_dev[dev];
+    if (s.pool == nullptr) {
+        LCX_CUDA(cudaMalloc(&s.pool, kPoolSlots * 4 * sizeof(uint32_t)), "cudaMalloc(trace pool)");
+        LCX_CUDA(cudaMemset(s.pool, 0, kPoolSlots * 4 * sizeof(uint32_t)), "cudaMemset(trace pool)");
+        s.device = dev;
+    }
+    *out = &s;
+    return LCX_OK;
+}
+
+struct MeshObj {
+    LcxAccelOption opt{};
+    int device = 0;
+    BlasDesc *d_desc = nullptr;
+    void *d_mem = nullptr;
+    size_t mem_bytes = 0;
+    uint32_t node_count = 0, tri_count = 0, depth = 0;
+    bool built = false;
+    uint64_t generation = 0;
+    double sah = 0.0;
+    Node8F *fnodes = nullptr;
+    std::mutex mtx;
+};
+
+struct AccelObj {
+    LcxAccelOption opt{};
+    int device = 0;
+    InstState *d_inst = nullptr;
+    uint32_t inst_cap = 0, inst_count = 0;
+    std::vector<uint64_t> inst_mesh;  // mesh handle per instance (0 = none)
+    void *d_mem = nullptr;
+    size_t mem_bytes = 0;
+    Node8Q *qn = nullptr;
+    Node8F *fn = nullptr;
+    InstRec *recs = nullptr;
+    uint32_t node_count = 0, depth = 0, max_blas_depth = 0, built_instances = 0;
+    bool built = false;
+    double sah = 0.0;
+    std::vector<std::pair<uint64_t, uint64_t>> mesh_gens;  // (mesh handle, generation) at TLAS build
+    std::mutex mtx;
+};
+
+std::mutex g_reg_mtx;
+std::unordered_map<uint64_t, std::shared_ptr<MeshObj>> g_meshes;
+std::unordered_map<uint64_t, std::shared_ptr<AccelObj>> g_accels;
+std::atomic<uint64_t> g_next_handle{1};
+
+std::shared_ptr<MeshObj> find_mesh(uint64_t h) {
+    std::lock_guard<std::mutex> lk(g_reg_mtx);
+    auto it = g_meshes.find(h);
+    return it == g_meshes.end() ? nullptr : it->second;
+}
+std::shared_ptr<AccelObj> find_accel(uint64_t h) {
+    std::lock_guard<std::mutex> lk(g_reg_mtx);
+    auto it = g_accels.find(h);
+    return it == g_accels.end() ? nullptr : it->second;
+}
+
+// Build scratch from the stream-ordered allocator, freed on the same stream.
+struct ScratchHolder {
+    cudaStream_t st;
+    std::vector<void *> ptrs;
+    explicit ScratchHolder(cudaStream_t s) : st(s) {}
+    cudaError_t alloc(void **p, size_t bytes) {
+        cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, st);
+        if (e == cudaSuccess) ptrs.push_back(*p);
+        return e;
+    }
+    ~ScratchHolder() {
+        for (void *p : ptrs) cudaFreeAsync(p, st);
+    }
+};
+
+int alloc_scratch(ScratchHolder &h, BuildScratch &s, uint32_t n, bool tlas) {
+    const size_t nn = std::max<uint32_t>(n, 1);
+    LCX_CUDA(h.alloc((void **)&s.box_lo, sizeof(float4) * nn), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.box_hi, sizeof(float4) * nn), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.keys, sizeof(unsigned long long) * nn), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.keys_sorted, sizeof(unsigned long long) * nn), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.vals, sizeof(uint32_t) * nn), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.vals_sorted, sizeof(uint32_t) * nn), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.bin_child, sizeof(uint32_t) * 2 * nn), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.bin_lo, sizeof(float4) * nn), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.bin_hi, sizeof(float4) * nn), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.other, sizeof(int32_t) * nn), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.desc, sizeof(uint32_t) * 12 * (nn + 1)), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.queue, sizeof(uint2) * 2 * (nn + 1)), "scratch");
+    if (tlas) LCX_CUDA(h.alloc((void **)&s.w2o, sizeof(float) * 12 * nn), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.ctl, sizeof(uint32_t) * kCtlWords + 2 * sizeof(double)), "scratch");
+    s.sort_tmp_bytes = sort_temp_bytes(uint32_t(nn));
+    LCX_CUDA(h.alloc(&s.sort_tmp, s.sort_tmp_bytes), "scratch");
+    return LCX_OK;
+}
+
+int init_ctl(const BuildScratch &s, cudaStream_t st, uint32_t *h_ctl) {
+    std::memset(h_ctl, 0, sizeof(uint32_t) * kCtlWords);
+    for (int k = 0; k < 3; k++) h_ctl[kCtlCenLo + k] = 0xffffffffu;
+    LCX_CUDA(cudaMemcpyAsync(s.ctl, h_ctl, sizeof(uint32_t) * kCtlWords, cudaMemcpyHostToDevice, st), "ctl upload");
+    LCX_CUDA(cudaMemsetAsync(reinterpret_cast<char *>(s.ctl) + sizeof(uint32_t) * kCtlWords, 0, 2 * sizeof(double), st),
+             "ctl upload");
+    return LCX_OK;
+}
+
+struct CtlReadback {
+    uint32_t words[kCtlWords];
+    double sah[2];
+};
+
+int read_ctl(const BuildScratch &s, cudaStream_t st, CtlReadback &out) {
+    LCX_CUDA(cudaMemcpyAsync(&out, s.ctl, sizeof(uint32_t) * kCtlWords + 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                             st),
+             "ctl readback");
+    LCX_CUDA(cudaStreamSynchronize(st), "build sync");
+    return LCX_OK;
+}
+
+int check_option(const LcxAccelOption *o) {
+    if (o && o->hint > LCX_HINT_FAST_BUILD) return fail(LCX_ERR_INVALID_ARG, "invalid AccelOption.hint %u", o->hint);
+    return LCX_OK;
+}
+
+int leaf_items_for(const LcxAccelOption &o) { return o.hint == LCX_HINT_FAST_BUILD ? 3 : 2; }
+
+}  // namespace
+
+extern "C" {
+
+uint32_t lcx_version(void) { return 0x000100u; }
+
+const char *lcx_last_error_string(void) { return g_last_error.c_str(); }
+
+int lcx_device_init(int device) {
+    LCX_CUDA(cudaSetDevice(device), "cudaSetDevice");
+    DeviceState *ds = nullptr;
+    return current_device_state(&ds);
+}
+
+// ------------------------------------------------------------------- mesh
+int lcx_mesh_create(const LcxAccelOption *option, uint64_t *out_handle) {
+    if (!out_handle) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_create: out_handle is null");
+    if (int r = check_option(option)) return r;
+    DeviceState *ds = nullptr;
+    if (int r = current_device_state(&ds)) return r;
+    auto m = std::make_shared<MeshObj>();
+    if (option) m->opt = *option;
+    m->device = ds->device;
+    LCX_CUDA(cudaMalloc(&m->d_desc, sizeof(BlasDesc)), "cudaMalloc(BlasDesc)");
+    LCX_CUDA(cudaMemset(m->d_desc, 0, sizeof(BlasDesc)), "cudaMemset(BlasDesc)");
+    const uint64_t h = g_next_handle.fetch_add(1);
+    {
+        std::lock_guard<std::mutex> lk(g_reg_mtx);
+        g_meshes[h] = m;
+    }
+    *out_handle = h;
+    return LCX_OK;
+}
+
+int lcx_mesh_destroy(uint64_t mesh) {
+    std::shared_ptr<MeshObj> m;
+    {
+        std::lock_guard<std::mutex> lk(g_reg_mtx);
+        auto it = g_meshes.find(mesh);
+        if (it == g_meshes.end()) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_destroy: unknown mesh handle %llu",
+                                              (unsigned long long)mesh);
+        m = it->second;
+        g_meshes.erase(it);
+    }
+    std::lock_guard<std::mutex> lk(m->mtx);
+    cudaDeviceSynchronize();  // the BVH may be in use by queued work
+    if (m->d_mem) cudaFree(m->d_mem);
+    if (m->d_desc) cudaFree(m->d_desc);
+    m->d_mem = nullptr;
+    m->d_desc = nullptr;
+    return LCX_OK;
+}
+
+int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *cmd, void *stream) {
+    auto m = find_mesh(mesh);
+    if (!m) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build: unknown mesh handle %llu", (unsigned long long)mesh);
+    if (!cmd) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build: command is null");
+    // src/runtime/rtx/mesh.cpp:41-50 and :33-39
+    if (cmd->request > LCX_REQUEST_FORCE_BUILD) return fail(LCX_ERR_INVALID_ARG, "invalid build request %u", cmd->request);
+    if (cmd->vertex_stride == 0 || cmd->vertex_stride % 16 != 0)
+        return fail(LCX_ERR_INVALID_ARG, "Vertex stride must be aligned to 16 bytes (got %zu).", cmd->vertex_stride);
+    if (cmd->vertex_buffer_offset % cmd->vertex_stride != 0 || cmd->vertex_buffer_size % cmd->vertex_stride != 0)
+        return fail(LCX_ERR_INVALID_ARG, "vertex buffer offset %zu / size %zu not aligned to vertex stride %zu",
+                    cmd->vertex_buffer_offset, cmd->vertex_buffer_size, cmd->vertex_stride);
+    if (cmd->triangle_buffer_offset % 4 != 0 || cmd->triangle_buffer_size % 12 != 0)
+        return fail(LCX_ERR_INVALID_ARG, "triangle buffer offset %zu / size %zu not aligned (4 / 12 bytes)",
+                    cmd->triangle_buffer_offset, cmd->triangle_buffer_size);
+    const uint64_t tri64 = cmd->triangle_buffer_size / 12;
+    const uint64_t vcount64 = cmd->vertex_buffer_size / cmd->vertex_stride;
+    if (tri64 >= (1ull << 31) || vcount64 >= (1ull << 32))
+        return fail(LCX_ERR_INVALID_ARG, "mesh too large (%llu triangles, %llu vertices)", (unsigned long long)tri64,
+                    (unsigned long long)vcount64);
+    if (tri64 && (cmd->vertex_buffer == 0 || cmd->triangle_buffer == 0))
+        return fail(LCX_ERR_INVALID_ARG, "null vertex or triangle buffer");
+    if ((cmd->vertex_buffer + cmd->vertex_buffer_offset) % 16 != 0 || (cmd->triangle_buffer % 4) != 0)
+        return fail(LCX_ERR_INVALID_ARG, "vertex buffer must be 16-byte aligned, triangle buffer 4-byte aligned");
+    const uint32_t n = uint32_t(tri64);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    std::lock_guard<std::mutex> lk(m->mtx);
+    if (n == 0) {
+        LCX_CUDA(cudaStreamSynchronize(st), "sync");
+        if (m->d_mem) cudaFree(m->d_mem);
+        m->d_mem = nullptr;
+        m->mem_bytes = 0;
+        m->node_count = m->tri_count = m->depth = 0;
+        m->fnodes = nullptr;
+        m->sah = 0.0;
+        LCX_CUDA(cudaMemset(m->d_desc, 0, sizeof(BlasDesc)), "cudaMemset(BlasDesc)");
+        m->built = true;
+        m->generation++;
+        return LCX_OK;
+    }
+    TriInput in;
+    in.vbase = reinterpret_cast<const unsigned char *>(cmd->vertex_buffer) + cmd->vertex_buffer_offset;
+    in.vstride = cmd->vertex_stride;
+    in.vcount = uint32_t(vcount64);
+    in.tbase = reinterpret_cast<const unsigned char *>(cmd->triangle_buffer) + cmd->triangle_buffer_offset;
+    const int leaf_max = leaf_items_for(m->opt);
+    CtlReadback rb;
+    {
+        ScratchHolder hold(st);
+        BuildScratch s;
+        if (int r = alloc_scratch(hold, s, n, false)) return r;
+        uint32_t h_ctl[kCtlWords];
+        if (int r = init_ctl(s, st, h_ctl)) return r;
+        LCX_CUDA(build_tree_tris(in, n, leaf_max, s, st), "BLAS build");
+        LCX_CUDA(binary_sah(s, n, st), "BLAS SAH");
+        if (int r = read_ctl(s, st, rb)) return r;
+        if (rb.words[kCtlErr] & kErrBadIndex)
+            return fail(LCX_ERR_INVALID_ARG, "triangle index out of range (vertex count %u)", in.vcount);
+        if (rb.words[kCtlErr] & kErrTooDeep) return fail(LCX_ERR_DEPTH, "BVH deeper than %d levels", kMaxLevels);
+        if (rb.words[kCtlItemCount] != n)
+            return fail(LCX_ERR_CUDA, "BLAS build placed %u of %u triangles", rb.words[kCtlItemCount], n);
+        const uint32_t W = rb.words[kCtlWideCount];
+        const size_t bytes = size_t(W) * (sizeof(Node8Q) + sizeof(Node8F)) + size_t(n) * sizeof(TriRec);
+        void *mem = nullptr;
+        LCX_CUDA(cudaStreamSynchronize(st), "sync");
+        if (m->d_mem) {
+            cudaFree(m->d_mem);
+            m->d_mem = nullptr;
+        }
+        LCX_CUDA(cudaMalloc(&mem, bytes), "cudaMalloc(BLAS)");
+        Node8Q *qn = static_cast<Node8Q *>(mem);
+        Node8F *fn = reinterpret_cast<Node8F *>(qn + W);
+        TriRec *tr = reinterpret_cast<TriRec *>(fn + W);
+        LCX_CUDA(emit_blas(in, n, leaf_max, W, s, qn, fn, tr, m->d_desc, st), "BLAS emit");
+        m->d_mem = mem;
+        m->mem_bytes = bytes;
+        m->node_count = W;
+        m->tri_count = n;
+        m->depth = rb.words[kCtlDepth];
+        m->fnodes = fn;
+        m->sah = rb.sah[1] > 0.0 ? rb.sah[0] / rb.sah[1] : 0.0;
+    }
+    if (rb.words[kCtlErr] & kErrQuant) return fail(LCX_ERR_INVALID_ARG, "vertex coordinates too large to quantise");
+    m->built = true;
+    m->generation++;
+    return LCX_OK;
+}
+
+int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out) {
+    auto m = find_mesh(mesh);
+    if (!m || !out) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_stats: bad arguments");
+    std::lock_guard<std::mutex> lk(m->mtx);
+    if (!m->built) return fail(LCX_ERR_NOT_BUILT, "mesh not built");
+    std::memset(out, 0, sizeof(*out));
+    out->node_count = m->node_count;
+    out->leaf_prim_count = m->tri_count;
+    out->device_bytes = m->mem_bytes + sizeof(BlasDesc);
+    out->depth = m->depth;
+    out->sah_cost = m->sah;
+    if (m->node_count) {
+        double *d = nullptr;
+        LCX_CUDA(cudaMalloc(&d, 2 * sizeof(double)), "cudaMalloc");
+        double h[2] = {0, 0};
+        cudaError_t e = wide_sah(m->fnodes, m->node_count, d, 0);
+        if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+        cudaFree(d);
+        if (e != cudaSuccess) return cuda_fail(e, "wide SAH");
+        out->wide_sah_cost = h[1] > 0.0 ? h[0] / h[1] : 0.0;
+    }
+    return LCX_OK;
+}
+
+// ------------------------------------------------------------------ accel
+int lcx_accel_create(const LcxAccelOption *option, uint64_t *out_handle) {
+    if (!out_handle) return fail(LCX_ERR_INVALID_ARG, "lcx_accel_create: out_handle is null");
+    if (int r = check_option(option)) return r;
+    DeviceState *ds = nullptr;
+    if (int r = current_device_state(&ds)) return r;
+    auto a = std::make_shared<AccelObj>();
+    if (option) a->opt = *option;
+    a->device = ds->device;
+    const uint64_t h = g_next_handle.fetch_add(1);
+    {
+        std::lock_guard<std::mutex> lk(g_reg_mtx);
+        g_accels[h] = a;
+    }
+    *out_handle = h;
+    return LCX_OK;
+}
+
+int lcx_accel_destroy(uint64_t accel) {
+    std::shared_ptr<AccelObj> a;
+    {
+        std::lock_guard<std::mutex> lk(g_reg_mtx);
+        auto it = g_accels.find(accel);
+        if (it == g_accels.end()) return fail(LCX_ERR_INVALID_ARG, "lcx_accel_destroy: unknown accel handle %llu",
+                                              (unsigned long long)accel);
+        a = it->second;
+        g_accels.erase(it);
+    }
+    std::lock_guard<std::mutex> lk(a->mtx);
+    cudaDeviceSynchronize();
+    if (a->d_mem) cudaFree(a->d_mem);
+    if (a->d_inst) cudaFree(a->d_inst);
+    a->d_mem = nullptr;
+    a->d_inst = nullptr;
+    return LCX_OK;
+}
+
+int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, const LcxModification *mods,
+                    size_t mod_count, int update_instance_buffer_only, void *stream) {
+    auto a = find_accel(accel);
+    if (!a) return fail(LCX_ERR_INVALID_ARG, "lcx_accel_build: unknown accel handle %llu", (unsigned long long)accel);
+    if (request > LCX_REQUEST_FORCE_BUILD) return fail(LCX_ERR_INVALID_ARG, "invalid build request %u", request);
+    // src/runtime/rtx/accel.cpp:72-73
+    if (instance_count == 0) return fail(LCX_ERR_INVALID_ARG, "Building acceleration structure without instances.");
+    if (mod_count && !mods) return fail(LCX_ERR_INVALID_ARG, "modifications pointer is null");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    std::lock_guard<std::mutex> lk(a->mtx);
+    // translate and validate the modifications
+    std::vector<ModRec> recs(mod_count);
+    std::vector<uint64_t> new_mesh(mod_count, 0);
+    for (size_t i = 0; i < mod_count; i++) {
+        const LcxModification &md = mods[i];
+        if (md.index >= instance_count)
+            return fail(LCX_ERR_INVALID_ARG, "modification %zu: instance index %u >= instance count %u", i, md.index,
+                        instance_count);
+        ModRec &r = recs[i];
+        r.index = md.index;
+        r.user_id = md.user_id;
+        r.flags = md.flags;
+        r.vis_mask = md.vis_mask;
+        std::memcpy(r.affine, md.affine, sizeof(r.affine));
+        r.primitive = 0;
+        r._pad = 0;
+        if (md.flags & LCX_MOD_PRIMITIVE) {
+            auto m = find_mesh(md.primitive);
+            if (!m) return fail(LCX_ERR_INVALID_ARG, "modification %zu: unknown mesh handle %llu", i,
+                                (unsigned long long)md.primitive);
+            if (!m->built) return fail(LCX_ERR_NOT_BUILT, "Mesh not built");  // accel.rs:356-358
+            r.primitive = reinterpret_cast<uint64_t>(m->d_desc);
+            new_mesh[i] = md.primitive;
+        }
+    }
+    // instance storage
+    if (instance_count > a->inst_cap) {
+        const uint32_t cap = std::max<uint32_t>(instance_count, a->inst_cap * 2);
+        InstState *p = nullptr;
+        LCX_CUDA(cudaMalloc(&p, sizeof(InstState) * cap), "cudaMalloc(instances)");
+        if (a->d_inst) {
+            LCX_CUDA(cudaMemcpyAsync(p, a->d_inst, sizeof(InstState) * a->inst_count, cudaMemcpyDeviceToDevice, st),
+                     "instance copy");
+            LCX_CUDA(cudaStreamSynchronize(st), "sync");
+            cudaFree(a->d_inst);
+        }
+        a->d_inst = p;
+        a->inst_cap = cap;
+    }
+    if (instance_count > a->inst_count) LCX_CUDA(init_instances(a->d_inst, a->inst_count, instance_count, st), "init");
+    a->inst_count = instance_count;
+    a->inst_mesh.resize(instance_count, 0);
+    for (uint32_t i = uint32_t(a->inst_mesh.size()); i < instance_count; i++) a->inst_mesh[i] = 0;
+    for (size_t i = 0; i < mod_count; i++)
+        if (new_mesh[i]) a->inst_mesh[recs[i].index] = new_mesh[i];
+    if (mod_count) {
+        ScratchHolder hold(st);
+        ModRec *d_mods = nullptr;
+        LCX_CUDA(hold.alloc((void **)&d_mods, sizeof(ModRec) * mod_count), "scratch");
+        LCX_CUDA(cudaMemcpyAsync(d_mods, recs.data(), sizeof(ModRec) * mod_count, cudaMemcpyHostToDevice, st),
+                 "modification upload");
+        LCX_CUDA(apply_modifications(d_mods, uint32_t(mod_count), a->d_inst, instance_count, st), "apply mods");
+    }
+    if (update_instance_buffer_only) return LCX_OK;
+
+    // TLAS build
+    const uint32_t n = instance_count;
+    CtlReadback rb;
+    {
+        ScratchHolder hold(st);
+        BuildScratch s;
+        if (int r = alloc_scratch(hold, s, n, true)) return r;
+        uint32_t h_ctl[kCtlWords];
+        if (int r = init_ctl(s, st, h_ctl)) return r;
+        LCX_CUDA(build_tree_insts(a->d_inst, n, 1, s, st), "TLAS build");
+        LCX_CUDA(binary_sah(s, n, st), "TLAS SAH");
+        if (int r = read_ctl(s, st, rb)) return r;
+        if (rb.words[kCtlErr] & kErrTooDeep) return fail(LCX_ERR_DEPTH, "TLAS deeper than %d levels", kMaxLevels);
+        if (rb.words[kCtlItemCount] != n)
+            return fail(LCX_ERR_CUDA, "TLAS build placed %u of %u instances", rb.words[kCtlItemCount], n);
+        const uint32_t W = rb.words[kCtlWideCount];
+        const size_t bytes = size_t(W) * (sizeof(Node8Q) + sizeof(Node8F)) + size_t(n) * sizeof(InstRec);
+        if (a->d_mem) {
+            cudaFree(a->d_mem);
+            a->d_mem = nullptr;
+        }
+        void *mem = nullptr;
+        LCX_CUDA(cudaMalloc(&mem, bytes), "cudaMalloc(TLAS)");
+        Node8Q *qn = static_cast<Node8Q *>(mem);
+        Node8F *fn = reinterpret_cast<Node8F *>(qn + W);
+        InstRec *ir = reinterpret_cast<InstRec *>(fn + W);
+        LCX_CUDA(emit_tlas(a->d_inst, n, 1, W, s, qn, fn, ir, st), "TLAS emit");
+        a->d_mem = mem;
+        a->mem_bytes = bytes;
+        a->qn = qn;
+        a->fn = fn;
+        a->recs = ir;
+        a->node_count = W;
+        a->depth = rb.words[kCtlDepth];
+        a->sah = rb.sah[1] > 0.0 ? rb.sah[0] / rb.sah[1] : 0.0;
+    }
+    // remember which mesh builds this TLAS references
+    a->mesh_gens.clear();
+    a->max_blas_depth = 0;
+    {
+        std::vector<uint64_t> uniq(a->inst_mesh.begin(), a->inst_mesh.end());
+        std::sort(uniq.begin(), uniq.end());
+        uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+        for (uint64_t h : uniq) {
+            if (!h) continue;
+            auto m = find_mesh(h);
+            if (!m) return fail(LCX_ERR_INVALID_ARG, "instance references destroyed mesh %llu", (unsigned long long)h);
+            a->mesh_gens.emplace_back(h, m->generation);
+            a->max_blas_depth = std::max(a->max_blas_depth, m->depth);
+        }
+    }
+    a->built_instances = n;
+    a->built = true;
+    return LCX_OK;
+}
+
+int lcx_accel_stats(uint64_t accel, LcxAccelStats *out) {
+    auto a = find_accel(accel);
+    if (!a || !out) return fail(LCX_ERR_INVALID_ARG, "lcx_accel_stats: bad arguments");
+    std::lock_guard<std::mutex> lk(a->mtx);
+    if (!a->built) return fail(LCX_ERR_NOT_BUILT, "accel not built");
+    std::memset(out, 0, sizeof(*out));
+    out->node_count = a->node_count;
+    out->leaf_prim_count = a->built_instances;
+    out->device_bytes = a->mem_bytes + sizeof(InstState) * a->inst_cap;
+    out->depth = a->depth;
+    out->max_blas_depth = a->max_blas_depth;
+    out->sah_cost = a->sah;
+    if (a->node_count) {
+        double *d = nullptr;
+        LCX_CUDA(cudaMalloc(&d, 2 * sizeof(double)), "cudaMalloc");
+        double h[2] = {0, 0};
+        cudaError_t e = wide_sah(a->fn, a->node_count, d, 0);
+        if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+        cudaFree(d);
+        if (e != cudaSuccess) return cuda_fail(e, "wide SAH");
+        out->wide_sah_cost = h[1] > 0.0 ? h[0] / h[1] : 0.0;
+    }
+    return LCX_OK;
+}
+
+// ---------------------------------------------------------------- queries
+static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
+                        uint8_t *d_occ, uint32_t *d_counts, uint32_t layout, void *stream) {
+    if (layout > LCX_NODES_QUANT8) return fail(LCX_ERR_INVALID_ARG, "invalid node layout %u", layout);
+    auto a = find_accel(accel);
+    if (!a) return fail(LCX_ERR_INVALID_ARG, "unknown accel handle %llu", (unsigned long long)accel);
+    if (ray_count == 0) return LCX_OK;
+    if (!d_rays || (!d_hits && !d_occ)) return fail(LCX_ERR_INVALID_ARG, "null ray or result buffer");
+    if (reinterpret_cast<uintptr_t>(d_rays) % 16 != 0) return fail(LCX_ERR_INVALID_ARG, "rays must be 16-byte aligned");
+    if (d_hits && reinterpret_cast<uintptr_t>(d_hits) % 8 != 0)
+        return fail(LCX_ERR_INVALID_ARG, "hits must be 8-byte aligned");
+    TraceParams p{};
+    {
+        std::lock_guard<std::mutex> lk(a->mtx);
+        if (!a->built) return fail(LCX_ERR_NOT_BUILT, "accel not built");
+        for (const auto &mg : a->mesh_gens) {
+            auto m = find_mesh(mg.first);
+            if (!m) return fail(LCX_ERR_NOT_BUILT, "mesh %llu was destroyed; rebuild the accel",
+                                (unsigned long long)mg.first);
+            if (m->generation != mg.second)
+                return fail(LCX_ERR_NOT_BUILT, "mesh %llu was rebuilt after the accel build; rebuild the accel",
+                            (unsigned long long)mg.first);
+        }
+        if (int(a->depth + a->max_blas_depth + 1) > kStackSize)
+            return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the traversal stack (%d)", a->depth,
+                        a->max_blas_depth, kStackSize);
+        p.tlas_q = a->qn;
+        p.tlas_f = a->fn;
+        p.insts = a->recs;
+    }
+    DeviceState *ds = nullptr;
+    if (int r = current_device_state(&ds)) return r;
+    const uint32_t slot = ds->next_slot.fetch_add(1) % kPoolSlots;
+    p.pool = ds->pool + 4 * slot;
+    p.rays = reinterpret_cast<const Ray *>(d_rays);
+    p.hits = reinterpret_cast<Hit *>(d_hits);
+    p.occluded = d_occ;
+    p.counts = d_counts;
+    p.ray_count = ray_count;
+    p.mask = mask & 0xffu;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    LCX_CUDA(cudaMemsetAsync(p.pool, 0, 4 * sizeof(uint32_t), st), "trace counter reset");
+    LCX_CUDA(launch_trace(p, int(layout), d_occ != nullptr, d_counts != nullptr, st), "trace launch");
+    return LCX_OK;
+}
+
+int lcx_trace_closest(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
+                      void *stream) {
+    if (!d_hits && ray_count) return fail(LCX_ERR_INVALID_ARG, "hits buffer is null");
+    return trace_common(accel, d_rays, ray_count, mask, d_hits, nullptr, nullptr, LCX_NODES_QUANT8, stream);
+}
+
+int lcx_trace_any(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, uint8_t *d_occluded,
+                  void *stream) {
+    if (!d_occluded && ray_count) return fail(LCX_ERR_INVALID_ARG, "occluded buffer is null");
+    return trace_common(accel, d_rays, ray_count, mask, nullptr, d_occluded, nullptr, LCX_NODES_QUANT8, stream);
+}
+
+int lcx_trace_closest_ex(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask,
+                         LcxTriangleHit *d_hits, uint32_t node_layout, void *stream) {
+    if (!d_hits && ray_count) return fail(LCX_ERR_INVALID_ARG, "hits buffer is null");
+    return trace_common(accel, d_rays, ray_count, mask, d_hits, nullptr, nullptr, node_layout, stream);
+}
+
+int lcx_trace_any_ex(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, uint8_t *d_occluded,
+                     uint32_t node_layout, void *stream) {
+    if (!d_occluded && ray_count) return fail(LCX_ERR_INVALID_ARG, "occluded buffer is null");
+    return trace_common(accel, d_rays, ray_count, mask, nullptr, d_occluded, nullptr, node_layout, stream);
+}
+
+int lcx_trace_closest_counts(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask,
+                             LcxTriangleHit *d_hits, uint32_t *d_counts, uint32_t node_layout, void *stream) {
+    if ((!d_hits || !d_counts) && ray_count) return fail(LCX_ERR_INVALID_ARG, "hits or counts buffer is null");
+    return trace_common(accel, d_rays, ray_count, mask, d_hits, nullptr, d_counts, node_layout, stream);
+}
+
+}  // extern "C"

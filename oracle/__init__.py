@@ -1,0 +1,194 @@
+"""CPU oracle for the Mesh/Accel path — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py (its cpu_baseline leg and
+the ``--impl reference`` arm) may load this module; the product never does.
+It wraps liblcx_oracle.so (lcx_oracle.cpp), a C++ restatement of the
+reference CPU backend's semantics for trace_closest / trace_any
+(src/rust/luisa_compute_backend_impl/src/cpu/accel.rs:449-535) with a
+binned-SAH BVH, the FP32 watertight triangle test and an FP64 adjudicator.
+Parity against the reference's own outputs is unpinned: the reference ships
+no golden vectors for this path and its CPU backend (Rust + Embree) cannot
+be built here.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from ctypes import POINTER, c_double, c_float, c_int, c_size_t, c_uint32, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liblcx_oracle.so"
+F64_DTYPE = np.dtype([("hit", "<i4"), ("pad", "<i4"), ("t", "<f8"), ("u", "<f8"), ("v", "<f8"),
+                      ("min_bary", "<f8")])
+
+_lib = None
+
+
+def build():
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        lib = ctypes.CDLL(str(LIB))
+        lib.lcxo_mesh_create.restype = c_void_p
+        lib.lcxo_mesh_create.argtypes = [c_void_p, c_size_t, c_size_t, c_void_p, c_size_t, c_int, c_int]
+        lib.lcxo_mesh_destroy.argtypes = [c_void_p]
+        lib.lcxo_mesh_sah.restype = c_double
+        lib.lcxo_mesh_sah.argtypes = [c_void_p]
+        lib.lcxo_mesh_depth.restype = c_uint32
+        lib.lcxo_mesh_depth.argtypes = [c_void_p]
+        lib.lcxo_accel_create.restype = c_void_p
+        lib.lcxo_accel_create.argtypes = [c_size_t, POINTER(c_void_p), c_void_p, c_void_p]
+        lib.lcxo_accel_destroy.argtypes = [c_void_p]
+        for name in ("lcxo_trace_closest", "lcxo_brute_closest"):
+            getattr(lib, name).argtypes = [c_void_p, c_void_p, c_size_t, c_uint32, c_void_p, c_int]
+        lib.lcxo_trace_any.argtypes = [c_void_p, c_void_p, c_size_t, c_uint32, c_void_p, c_int]
+        lib.lcxo_fp64_closest.argtypes = [c_void_p, c_void_p, c_size_t, c_uint32, c_void_p, c_void_p, c_int]
+        lib.lcxo_fp64_eval.argtypes = [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p]
+        lib.lcxo_affine_inverse.argtypes = [c_void_p, c_void_p]
+        lib.lcxo_intersect_triangle.restype = c_int
+        lib.lcxo_intersect_triangle.argtypes = [c_void_p, c_void_p, c_float, c_float, c_void_p, c_void_p, c_void_p,
+                                                POINTER(c_float), POINTER(c_float), POINTER(c_float)]
+        _lib = lib
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(c_void_p)
+
+
+class OracleScene:
+    """A scene (scenes.Scene) built on the CPU: one binned-SAH BVH per mesh, one over instances."""
+
+    def __init__(self, scene, leaf_size: int = 4, bins: int = 32):
+        from luisacompute_gb300.scenes import HIT_DTYPE  # noqa: F401  (layout shared with the product)
+        lib = load()
+        self.lib = lib
+        self._keep = []
+        self.meshes = []
+        for md in scene.meshes:
+            v = np.ascontiguousarray(md.vertices, np.float32)
+            t = np.ascontiguousarray(md.triangles, np.uint32)
+            self._keep += [v, t]
+            self.meshes.append(lib.lcxo_mesh_create(_ptr(v), v.shape[1], v.shape[0], _ptr(t), t.shape[0],
+                                                    leaf_size, bins))
+        n = scene.instance_count
+        arr = (c_void_p * n)(*[self.meshes[i] for i in scene.inst_mesh])
+        aff = np.ascontiguousarray(scene.inst_affine, np.float32)
+        masks = np.ascontiguousarray(scene.inst_mask, np.uint32)
+        self._keep += [aff, masks]
+        self.accel = lib.lcxo_accel_create(n, arr, _ptr(aff), _ptr(masks))
+
+    def mesh_sah(self, i: int) -> float:
+        return float(self.lib.lcxo_mesh_sah(self.meshes[i]))
+
+    def trace_closest(self, rays: np.ndarray, mask: int = 0xFF, threads: int = 0) -> np.ndarray:
+        from luisacompute_gb300.scenes import HIT_DTYPE
+        rays = np.ascontiguousarray(rays)
+        hits = np.zeros(rays.shape[0], HIT_DTYPE)
+        self.lib.lcxo_trace_closest(self.accel, _ptr(rays), rays.shape[0], mask, _ptr(hits), threads)
+        return hits
+
+    def brute_closest(self, rays: np.ndarray, mask: int = 0xFF, threads: int = 0) -> np.ndarray:
+        from luisacompute_gb300.scenes import HIT_DTYPE
+        rays = np.ascontiguousarray(rays)
+        hits = np.zeros(rays.shape[0], HIT_DTYPE)
+        self.lib.lcxo_brute_closest(self.accel, _ptr(rays), rays.shape[0], mask, _ptr(hits), threads)
+        return hits
+
+    def trace_any(self, rays: np.ndarray, mask: int = 0xFF, threads: int = 0) -> np.ndarray:
+        rays = np.ascontiguousarray(rays)
+        occ = np.zeros(rays.shape[0], np.uint8)
+        self.lib.lcxo_trace_any(self.accel, _ptr(rays), rays.shape[0], mask, _ptr(occ), threads)
+        return occ
+
+    def fp64_closest(self, rays: np.ndarray, mask: int = 0xFF, threads: int = 0):
+        from luisacompute_gb300.scenes import HIT_DTYPE
+        rays = np.ascontiguousarray(rays)
+        hits = np.zeros(rays.shape[0], HIT_DTYPE)
+        t64 = np.zeros(rays.shape[0], np.float64)
+        self.lib.lcxo_fp64_closest(self.accel, _ptr(rays), rays.shape[0], mask, _ptr(hits), _ptr(t64), threads)
+        return hits, t64
+
+    def fp64_eval(self, rays: np.ndarray, inst: np.ndarray, prim: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays)
+        inst = np.ascontiguousarray(inst, np.uint32)
+        prim = np.ascontiguousarray(prim, np.uint32)
+        out = np.zeros(rays.shape[0], F64_DTYPE)
+        self.lib.lcxo_fp64_eval(self.accel, _ptr(rays), rays.shape[0], _ptr(inst), _ptr(prim), _ptr(out))
+        return out
+
+    def close(self):
+        if self.accel:
+            self.lib.lcxo_accel_destroy(self.accel)
+            self.accel = None
+        for m in self.meshes:
+            self.lib.lcxo_mesh_destroy(m)
+        self.meshes = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def affine_inverse(o2w: np.ndarray) -> np.ndarray:
+    o2w = np.ascontiguousarray(o2w, np.float32).reshape(12)
+    out = np.zeros(12, np.float32)
+    load().lcxo_affine_inverse(_ptr(o2w), _ptr(out))
+    return out
+
+
+def intersect_triangle(o, d, tmin, tmax, v0, v1, v2):
+    """FP32 watertight test of one ray against one triangle: (hit, t, u, v)."""
+    arrs = [np.ascontiguousarray(x, np.float32) for x in (o, d, v0, v1, v2)]
+    t, u, v = c_float(0), c_float(0), c_float(0)
+    hit = load().lcxo_intersect_triangle(_ptr(arrs[0]), _ptr(arrs[1]), tmin, tmax, _ptr(arrs[2]), _ptr(arrs[3]),
+                                         _ptr(arrs[4]), ctypes.byref(t), ctypes.byref(u), ctypes.byref(v))
+    return bool(hit), t.value, u.value, v.value
+
+
+def adjudicate(scene_oracle: OracleScene, rays: np.ndarray, got: np.ndarray, want: np.ndarray,
+               rel_t: float = 1e-6, edge_eps: float = 1e-5) -> dict:
+    """Classify every ray whose (inst, prim) differs between ``got`` and ``want`` with FP64:
+    a near-tie in t (relative difference of the two FP64 hit distances <= rel_t) or an
+    edge/vertex-grazing hit (FP64 min barycentric of either triangle within edge_eps of 0).
+    Returns counts and the indices left unexplained."""
+    diff = np.nonzero((got["inst"] != want["inst"]) | (got["prim"] != want["prim"]))[0]
+    out = {"rays": int(rays.shape[0]), "disagree": int(diff.size), "near_tie": 0, "grazing": 0,
+           "unexplained": []}
+    if diff.size == 0:
+        return out
+    r = rays[diff]
+    eg = scene_oracle.fp64_eval(r, got["inst"][diff], got["prim"][diff])
+    ew = scene_oracle.fp64_eval(r, want["inst"][diff], want["prim"][diff])
+    g_miss = got["inst"][diff] == 0xFFFFFFFF
+    w_miss = want["inst"][diff] == 0xFFFFFFFF
+    for k in range(diff.size):
+        if not g_miss[k] and not w_miss[k]:
+            t0, t1 = eg["t"][k], ew["t"][k]
+            if abs(t0 - t1) <= rel_t * max(abs(t0), abs(t1), 1e-30):
+                out["near_tie"] += 1
+                continue
+        mb = []
+        if not g_miss[k]:
+            mb.append(abs(eg["min_bary"][k]))
+        if not w_miss[k]:
+            mb.append(abs(ew["min_bary"][k]))
+        if mb and min(mb) <= edge_eps:
+            out["grazing"] += 1
+            continue
+        out["unexplained"].append(int(diff[k]))
+    return out

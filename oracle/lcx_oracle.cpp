@@ -1,0 +1,736 @@
+// lcx_oracle.cpp — CPU oracle for the Mesh/Accel path.  TEST INFRASTRUCTURE:
+// the checker and the timed CPU baseline, never linked into the product.
+// Semantics follow LuisaCompute's CPU backend (citations in lcx_oracle.h);
+// the FP32 arithmetic follows Woop, Benthin & Wald, "Watertight Ray/Triangle
+// Intersection", JCGT 2(1) 2013, with the operation order fixed below.
+//
+// Compile with -ffp-contract=off: every fused multiply-add here is an
+// explicit std::fma, every other operation rounds on its own, so the results
+// are reproducible bit for bit by the CUDA kernels (which use the __f*_rn
+// intrinsics in the same order).
+#include "lcx_oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+constexpr uint32_t kInvalid = 0xffffffffu;
+
+// ------------------------------------------------------------------ FP32 math
+// (1) Affine inverse of the row-major 3x4 object-to-world matrix
+//     (include/luisa/runtime/rhi/command.h:557-571 layout).
+void affine_inverse_f32(const float *m, float *w) {
+    const float a = m[0], b = m[1], c = m[2];
+    const float d = m[4], e = m[5], f = m[6];
+    const float g = m[8], h = m[9], i = m[10];
+    const float c00 = std::fma(e, i, -(f * h));
+    const float c01 = std::fma(f, g, -(d * i));
+    const float c02 = std::fma(d, h, -(e * g));
+    const float det = std::fma(a, c00, std::fma(b, c01, c * c02));
+    const float r = 1.0f / det;
+    float R[9];
+    R[0] = c00 * r;
+    R[1] = std::fma(c, h, -(b * i)) * r;
+    R[2] = std::fma(b, f, -(c * e)) * r;
+    R[3] = c01 * r;
+    R[4] = std::fma(a, i, -(c * g)) * r;
+    R[5] = std::fma(c, d, -(a * f)) * r;
+    R[6] = c02 * r;
+    R[7] = std::fma(b, g, -(a * h)) * r;
+    R[8] = std::fma(a, e, -(b * d)) * r;
+    const float tx = m[3], ty = m[7], tz = m[11];
+    for (int k = 0; k < 3; k++) {
+        w[4 * k + 0] = R[3 * k + 0];
+        w[4 * k + 1] = R[3 * k + 1];
+        w[4 * k + 2] = R[3 * k + 2];
+        w[4 * k + 3] = -std::fma(R[3 * k + 0], tx, std::fma(R[3 * k + 1], ty, R[3 * k + 2] * tz));
+    }
+}
+
+// (2) World ray -> object ray with the world-to-object matrix.
+void transform_ray_f32(const float *w, const float *o, const float *d, float *oo, float *od) {
+    for (int k = 0; k < 3; k++) {
+        oo[k] = std::fma(w[4 * k], o[0], std::fma(w[4 * k + 1], o[1], std::fma(w[4 * k + 2], o[2], w[4 * k + 3])));
+        od[k] = std::fma(w[4 * k], d[0], std::fma(w[4 * k + 1], d[1], w[4 * k + 2] * d[2]));
+    }
+}
+
+// (3) Watertight test, per-ray part.
+struct WtRay {
+    float o[3];
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+    float tmin, tmax;
+};
+
+void wt_setup(WtRay &r, const float *o, const float *d, float tmin, float tmax) {
+    r.o[0] = o[0];
+    r.o[1] = o[1];
+    r.o[2] = o[2];
+    const float ax = std::fabs(d[0]), ay = std::fabs(d[1]), az = std::fabs(d[2]);
+    int kz = (ax >= ay) ? ((ax >= az) ? 0 : 2) : ((ay >= az) ? 1 : 2);
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    if (d[kz] < 0.0f) std::swap(kx, ky);
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.Sx = d[kx] / d[kz];
+    r.Sy = d[ky] / d[kz];
+    r.Sz = 1.0f / d[kz];
+    r.tmin = tmin;
+    r.tmax = tmax;
+}
+
+// (4) Watertight test, per-triangle part.  Returns true on a hit with
+//     t in [tmin, tmax]; (u, v) weight v1 and v2.
+bool wt_intersect(const WtRay &r, const float *v0, const float *v1, const float *v2, float &t_out,
+                  float &u_out, float &v_out) {
+    const float A[3] = {v0[0] - r.o[0], v0[1] - r.o[1], v0[2] - r.o[2]};
+    const float B[3] = {v1[0] - r.o[0], v1[1] - r.o[1], v1[2] - r.o[2]};
+    const float C[3] = {v2[0] - r.o[0], v2[1] - r.o[1], v2[2] - r.o[2]};
+    const float Ax = std::fma(-r.Sx, A[r.kz], A[r.kx]);
+    const float Ay = std::fma(-r.Sy, A[r.kz], A[r.ky]);
+    const float Bx = std::fma(-r.Sx, B[r.kz], B[r.kx]);
+    const float By = std::fma(-r.Sy, B[r.kz], B[r.ky]);
+    const float Cx = std::fma(-r.Sx, C[r.kz], C[r.kx]);
+    const float Cy = std::fma(-r.Sy, C[r.kz], C[r.ky]);
+    // edge functions with separately rounded products: swapping two vertices
+    // negates them exactly, which keeps shared edges watertight
+    const float U = Cx * By - Cy * Bx;
+    const float V = Ax * Cy - Ay * Cx;
+    const float W = Bx * Ay - By * Ax;
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = (U + V) + W;
+    if (det == 0.0f) return false;
+    const float Az = r.Sz * A[r.kz];
+    const float Bz = r.Sz * B[r.kz];
+    const float Cz = r.Sz * C[r.kz];
+    const float T = std::fma(U, Az, std::fma(V, Bz, W * Cz));
+    const float t = T / det;
+    if (!(t >= r.tmin && t <= r.tmax)) return false;
+    t_out = t;
+    u_out = V / det;
+    v_out = W / det;
+    return true;
+}
+
+// Candidate (t, inst, prim) beats the current best?  Ties in t go to the
+// smaller (inst, prim), so the answer does not depend on traversal order.
+inline bool better(float t, uint32_t inst, uint32_t prim, const LcxoHit &b) {
+    if (t < b.t) return true;
+    if (t > b.t) return false;
+    return inst < b.inst || (inst == b.inst && prim < b.prim);
+}
+
+// ----------------------------------------------------------------- FP64 math
+struct WtRay64 {
+    double o[3];
+    int kx, ky, kz;
+    double Sx, Sy, Sz;
+    double tmin, tmax;
+};
+
+void wt_setup64(WtRay64 &r, const double *o, const double *d, double tmin, double tmax) {
+    for (int k = 0; k < 3; k++) r.o[k] = o[k];
+    const double ax = std::fabs(d[0]), ay = std::fabs(d[1]), az = std::fabs(d[2]);
+    int kz = (ax >= ay) ? ((ax >= az) ? 0 : 2) : ((ay >= az) ? 1 : 2);
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    if (d[kz] < 0.0) std::swap(kx, ky);
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.Sx = d[kx] / d[kz];
+    r.Sy = d[ky] / d[kz];
+    r.Sz = 1.0 / d[kz];
+    r.tmin = tmin;
+    r.tmax = tmax;
+}
+
+// FP64 evaluation: always returns (t, u, v, min_bary) of the plane hit; `hit`
+// says whether the point is inside the triangle and t in range.
+bool wt_eval64(const WtRay64 &r, const double *v0, const double *v1, const double *v2, double &t,
+               double &u, double &v, double &min_bary) {
+    const double A[3] = {v0[0] - r.o[0], v0[1] - r.o[1], v0[2] - r.o[2]};
+    const double B[3] = {v1[0] - r.o[0], v1[1] - r.o[1], v1[2] - r.o[2]};
+    const double C[3] = {v2[0] - r.o[0], v2[1] - r.o[1], v2[2] - r.o[2]};
+    const double Ax = A[r.kx] - r.Sx * A[r.kz], Ay = A[r.ky] - r.Sy * A[r.kz];
+    const double Bx = B[r.kx] - r.Sx * B[r.kz], By = B[r.ky] - r.Sy * B[r.kz];
+    const double Cx = C[r.kx] - r.Sx * C[r.kz], Cy = C[r.ky] - r.Sy * C[r.kz];
+    const double U = Cx * By - Cy * Bx;
+    const double V = Ax * Cy - Ay * Cx;
+    const double W = Bx * Ay - By * Ax;
+    const double det = U + V + W;
+    if (det == 0.0) {
+        t = u = v = 0.0;
+        min_bary = -1.0;
+        return false;
+    }
+    const double T = U * (r.Sz * A[r.kz]) + V * (r.Sz * B[r.kz]) + W * (r.Sz * C[r.kz]);
+    t = T / det;
+    u = V / det;
+    v = W / det;
+    const double w0 = U / det;
+    min_bary = std::min(w0, std::min(u, v));
+    return min_bary >= 0.0 && t >= r.tmin && t <= r.tmax;
+}
+
+void affine_inverse_f64(const float *mf, double *w) {
+    double m[12];
+    for (int k = 0; k < 12; k++) m[k] = mf[k];
+    const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9], i = m[10];
+    const double c00 = e * i - f * h, c01 = f * g - d * i, c02 = d * h - e * g;
+    const double det = a * c00 + b * c01 + c * c02;
+    const double R[9] = {c00 / det,           (c * h - b * i) / det, (b * f - c * e) / det,
+                         c01 / det,           (a * i - c * g) / det, (c * d - a * f) / det,
+                         c02 / det,           (b * g - a * h) / det, (a * e - b * d) / det};
+    for (int k = 0; k < 3; k++) {
+        w[4 * k + 0] = R[3 * k];
+        w[4 * k + 1] = R[3 * k + 1];
+        w[4 * k + 2] = R[3 * k + 2];
+        w[4 * k + 3] = -(R[3 * k] * m[3] + R[3 * k + 1] * m[7] + R[3 * k + 2] * m[11]);
+    }
+}
+
+// --------------------------------------------------------------------- BVH
+struct Box {
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+    float hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    void grow(const float *p) {
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::min(lo[k], p[k]);
+            hi[k] = std::max(hi[k], p[k]);
+        }
+    }
+    void grow(const Box &b) {
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::min(lo[k], b.lo[k]);
+            hi[k] = std::max(hi[k], b.hi[k]);
+        }
+    }
+    bool empty() const { return !(lo[0] <= hi[0] && lo[1] <= hi[1] && lo[2] <= hi[2]); }
+    double area() const {
+        if (empty()) return 0.0;
+        const double dx = double(hi[0]) - lo[0], dy = double(hi[1]) - lo[1], dz = double(hi[2]) - lo[2];
+        return 2.0 * (dx * dy + dy * dz + dz * dx);
+    }
+};
+
+struct Node {
+    Box box;
+    uint32_t first;  // internal: left child index (right = first + 1); leaf: first item
+    uint32_t count;  // 0 = internal
+};
+
+// Top-down binned-SAH builder over item boxes (triangles or instances).
+struct Bvh {
+    std::vector<Node> nodes;
+    std::vector<uint32_t> items;  // item ids in leaf order
+    uint32_t depth = 0;
+
+    void build(const std::vector<Box> &boxes, int leaf_size, int bins) {
+        const size_t n = boxes.size();
+        items.resize(n);
+        for (size_t i = 0; i < n; i++) items[i] = uint32_t(i);
+        nodes.clear();
+        nodes.reserve(2 * n + 1);
+        std::vector<float> cen(3 * n);
+        for (size_t i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) {
+                const float c = 0.5f * (boxes[i].lo[k] + boxes[i].hi[k]);
+                cen[3 * i + k] = std::isfinite(c) ? c : 0.0f;
+            }
+        nodes.push_back(Node{});
+        if (n == 0) {
+            nodes[0].first = 0;
+            nodes[0].count = 0;
+            depth = 0;
+            return;
+        }
+        struct Task {
+            uint32_t node, begin, end, level;
+        };
+        std::vector<Task> stack{{0, 0, uint32_t(n), 1}};
+        std::vector<Box> bin_box(bins), left_acc(bins);
+        std::vector<uint32_t> bin_cnt(bins);
+        while (!stack.empty()) {
+            Task tk = stack.back();
+            stack.pop_back();
+            depth = std::max(depth, tk.level);
+            Box nb, cb;
+            for (uint32_t i = tk.begin; i < tk.end; i++) {
+                nb.grow(boxes[items[i]]);
+                cb.grow(&cen[3 * items[i]]);
+            }
+            nodes[tk.node].box = nb;
+            const uint32_t cnt = tk.end - tk.begin;
+            auto make_leaf = [&] {
+                nodes[tk.node].first = tk.begin;
+                nodes[tk.node].count = cnt;
+            };
+            if (cnt <= uint32_t(leaf_size)) {
+                make_leaf();
+                continue;
+            }
+            // binned SAH over the three axes
+            double best_cost = double(cnt) * nb.area();
+            int best_axis = -1, best_split = 0;
+            for (int ax = 0; ax < 3; ax++) {
+                const float ext = cb.hi[ax] - cb.lo[ax];
+                if (!(ext > 0.0f)) continue;
+                const float scale = float(bins) / ext;
+                std::fill(bin_box.begin(), bin_box.end(), Box{});
+                std::fill(bin_cnt.begin(), bin_cnt.end(), 0u);
+                for (uint32_t i = tk.begin; i < tk.end; i++) {
+                    int b = int((cen[3 * items[i] + ax] - cb.lo[ax]) * scale);
+                    b = std::min(std::max(b, 0), bins - 1);
+                    bin_cnt[b]++;
+                    bin_box[b].grow(boxes[items[i]]);
+                }
+                Box acc;
+                uint32_t acc_n = 0;
+                std::vector<double> left_cost(bins);
+                for (int b = 0; b < bins - 1; b++) {
+                    acc.grow(bin_box[b]);
+                    acc_n += bin_cnt[b];
+                    left_cost[b] = double(acc_n) * acc.area();
+                }
+                acc = Box{};
+                acc_n = 0;
+                for (int b = bins - 1; b > 0; b--) {
+                    acc.grow(bin_box[b]);
+                    acc_n += bin_cnt[b];
+                    const double c = left_cost[b - 1] + double(acc_n) * acc.area() + nb.area();
+                    if (c < best_cost && acc_n > 0 && acc_n < cnt) {
+                        best_cost = c;
+                        best_axis = ax;
+                        best_split = b;
+                    }
+                }
+            }
+            uint32_t mid;
+            if (best_axis < 0) {
+                if (cnt <= 16u) {
+                    make_leaf();
+                    continue;
+                }
+                // all centroids equal or SAH prefers a leaf that is too big: median split
+                mid = tk.begin + cnt / 2;
+            } else {
+                const float scale = float(bins) / (cb.hi[best_axis] - cb.lo[best_axis]);
+                auto it = std::partition(items.begin() + tk.begin, items.begin() + tk.end, [&](uint32_t id) {
+                    int b = int((cen[3 * id + best_axis] - cb.lo[best_axis]) * scale);
+                    b = std::min(std::max(b, 0), bins - 1);
+                    return b < best_split;
+                });
+                mid = uint32_t(it - items.begin());
+                if (mid == tk.begin || mid == tk.end) mid = tk.begin + cnt / 2;
+            }
+            const uint32_t l = uint32_t(nodes.size());
+            nodes.push_back(Node{});
+            nodes.push_back(Node{});
+            nodes[tk.node].first = l;
+            nodes[tk.node].count = 0;
+            stack.push_back({l + 1, mid, tk.end, tk.level + 1});
+            stack.push_back({l, tk.begin, mid, tk.level + 1});
+        }
+    }
+
+    double sah() const {
+        if (nodes.empty() || nodes[0].box.empty()) return 0.0;
+        const double ra = nodes[0].box.area();
+        double c = 0.0;
+        for (const Node &nd : nodes) c += nd.box.area() / ra * (nd.count ? double(nd.count) : 1.0);
+        return c;
+    }
+};
+
+// Robust slab test in FP32 with an outward slack on the exit distance.
+inline bool slab(const Box &b, const float *o, const float *inv, float tmin, float tmax, float &tnear) {
+    float tn = tmin, tf = tmax;
+    for (int k = 0; k < 3; k++) {
+        const float t0 = (b.lo[k] - o[k]) * inv[k];
+        const float t1 = (b.hi[k] - o[k]) * inv[k];
+        tn = std::fmax(tn, std::fmin(t0, t1));
+        tf = std::fmin(tf, std::fmax(t0, t1));
+    }
+    tnear = tn;
+    return tn <= tf + std::fabs(tf) * 0x1p-18f;
+}
+
+inline bool slab64(const Box &b, const double *o, const double *inv, double tmin, double tmax, double &tnear) {
+    double tn = tmin, tf = tmax;
+    for (int k = 0; k < 3; k++) {
+        const double t0 = (double(b.lo[k]) - o[k]) * inv[k];
+        const double t1 = (double(b.hi[k]) - o[k]) * inv[k];
+        tn = std::fmax(tn, std::fmin(t0, t1));
+        tf = std::fmin(tf, std::fmax(t0, t1));
+    }
+    tnear = tn;
+    return tn <= tf + std::fabs(tf) * 1e-9;
+}
+
+inline float safe_inv(float x) {
+    return 1.0f / (std::fabs(x) > 1e-30f ? x : std::copysign(1e-30f, x));
+}
+inline double safe_inv64(double x) { return 1.0 / (std::fabs(x) > 1e-300 ? x : std::copysign(1e-300, x)); }
+
+struct Mesh {
+    std::vector<float> v;  // 3 floats per vertex
+    std::vector<uint32_t> t;
+    Bvh bvh;
+    size_t vertex_count = 0;
+    const float *vert(uint32_t i) const { return &v[3 * size_t(i)]; }
+    bool tri_valid(uint32_t p) const {
+        return t[3 * p] < vertex_count && t[3 * p + 1] < vertex_count && t[3 * p + 2] < vertex_count;
+    }
+};
+
+struct Accel {
+    std::vector<const Mesh *> mesh;
+    std::vector<float> o2w, w2o;  // 12 floats each
+    std::vector<double> w2o64;
+    std::vector<uint32_t> mask;
+    Bvh bvh;
+};
+
+// -------------------------------------------------------- FP32 traversal
+template <bool kAny>
+bool trace_mesh(const Mesh &m, uint32_t inst, const float *o, const float *d, float tmin, LcxoHit &best) {
+    if (m.bvh.nodes.empty() || m.t.empty()) return false;
+    WtRay wr;
+    wt_setup(wr, o, d, tmin, best.t);
+    const float inv[3] = {safe_inv(d[0]), safe_inv(d[1]), safe_inv(d[2])};
+    uint32_t stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        const Node &nd = m.bvh.nodes[stack[--sp]];
+        float tn;
+        if (!slab(nd.box, o, inv, tmin, best.t, tn)) continue;
+        if (nd.count) {
+            for (uint32_t i = 0; i < nd.count; i++) {
+                const uint32_t p = m.bvh.items[nd.first + i];
+                if (!m.tri_valid(p)) continue;
+                float t, u, v;
+                wr.tmax = best.t;
+                if (wt_intersect(wr, m.vert(m.t[3 * p]), m.vert(m.t[3 * p + 1]), m.vert(m.t[3 * p + 2]), t, u, v)) {
+                    if (kAny) return true;
+                    if (better(t, inst, p, best)) best = LcxoHit{inst, p, u, v, t, 0};
+                }
+            }
+        } else {
+            const Node &l = m.bvh.nodes[nd.first], &r = m.bvh.nodes[nd.first + 1];
+            float tl, tr;
+            const bool hl = slab(l.box, o, inv, tmin, best.t, tl);
+            const bool hr = slab(r.box, o, inv, tmin, best.t, tr);
+            if (hl && hr) {
+                if (tl <= tr) {
+                    stack[sp++] = nd.first + 1;
+                    stack[sp++] = nd.first;
+                } else {
+                    stack[sp++] = nd.first;
+                    stack[sp++] = nd.first + 1;
+                }
+            } else if (hl) {
+                stack[sp++] = nd.first;
+            } else if (hr) {
+                stack[sp++] = nd.first + 1;
+            }
+        }
+    }
+    return false;
+}
+
+template <bool kAny>
+bool trace_accel(const Accel &a, const LcxoRay &ray, uint32_t mask, LcxoHit &best) {
+    best = LcxoHit{kInvalid, kInvalid, 0.0f, 0.0f, ray.tmax, 0};
+    if (a.bvh.nodes.empty()) return false;
+    const float inv[3] = {safe_inv(ray.d[0]), safe_inv(ray.d[1]), safe_inv(ray.d[2])};
+    uint32_t stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        const Node &nd = a.bvh.nodes[stack[--sp]];
+        float tn;
+        if (!slab(nd.box, ray.o, inv, ray.tmin, best.t, tn)) continue;
+        if (nd.count) {
+            for (uint32_t i = 0; i < nd.count; i++) {
+                const uint32_t id = a.bvh.items[nd.first + i];
+                if ((a.mask[id] & mask) == 0u || a.mesh[id] == nullptr) continue;
+                float oo[3], od[3];
+                transform_ray_f32(&a.w2o[12 * size_t(id)], ray.o, ray.d, oo, od);
+                if (trace_mesh<kAny>(*a.mesh[id], id, oo, od, ray.tmin, best) && kAny) return true;
+            }
+        } else {
+            stack[sp++] = nd.first + 1;
+            stack[sp++] = nd.first;
+        }
+    }
+    return false;
+}
+
+// -------------------------------------------------------- FP64 traversal
+void trace_accel64(const Accel &a, const LcxoRay &ray, uint32_t mask, LcxoHit &best, double &best_t) {
+    best = LcxoHit{kInvalid, kInvalid, 0.0f, 0.0f, ray.tmax, 0};
+    best_t = ray.tmax;
+    if (a.bvh.nodes.empty()) return;
+    const double o[3] = {ray.o[0], ray.o[1], ray.o[2]};
+    const double d[3] = {ray.d[0], ray.d[1], ray.d[2]};
+    const double inv[3] = {safe_inv64(d[0]), safe_inv64(d[1]), safe_inv64(d[2])};
+    uint32_t stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        const Node &nd = a.bvh.nodes[stack[--sp]];
+        double tn;
+        if (!slab64(nd.box, o, inv, ray.tmin, best_t, tn)) continue;
+        if (!nd.count) {
+            stack[sp++] = nd.first + 1;
+            stack[sp++] = nd.first;
+            continue;
+        }
+        for (uint32_t i = 0; i < nd.count; i++) {
+            const uint32_t id = a.bvh.items[nd.first + i];
+            if ((a.mask[id] & mask) == 0u || a.mesh[id] == nullptr) continue;
+            const Mesh &m = *a.mesh[id];
+            if (m.t.empty()) continue;
+            const double *w = &a.w2o64[12 * size_t(id)];
+            double oo[3], od[3];
+            for (int k = 0; k < 3; k++) {
+                oo[k] = w[4 * k] * o[0] + w[4 * k + 1] * o[1] + w[4 * k + 2] * o[2] + w[4 * k + 3];
+                od[k] = w[4 * k] * d[0] + w[4 * k + 1] * d[1] + w[4 * k + 2] * d[2];
+            }
+            WtRay64 wr;
+            wt_setup64(wr, oo, od, ray.tmin, ray.tmax);
+            const double binv[3] = {safe_inv64(od[0]), safe_inv64(od[1]), safe_inv64(od[2])};
+            uint32_t st2[128];
+            int sp2 = 0;
+            st2[sp2++] = 0;
+            while (sp2) {
+                const Node &bn = m.bvh.nodes[st2[--sp2]];
+                double tn2;
+                if (!slab64(bn.box, oo, binv, ray.tmin, best_t, tn2)) continue;
+                if (!bn.count) {
+                    st2[sp2++] = bn.first + 1;
+                    st2[sp2++] = bn.first;
+                    continue;
+                }
+                for (uint32_t j = 0; j < bn.count; j++) {
+                    const uint32_t p = m.bvh.items[bn.first + j];
+                    if (!m.tri_valid(p)) continue;
+                    double v0[3], v1[3], v2[3];
+                    for (int k = 0; k < 3; k++) {
+                        v0[k] = m.vert(m.t[3 * p])[k];
+                        v1[k] = m.vert(m.t[3 * p + 1])[k];
+                        v2[k] = m.vert(m.t[3 * p + 2])[k];
+                    }
+                    double t, u, v, mb;
+                    if (wt_eval64(wr, v0, v1, v2, t, u, v, mb)) {
+                        if (t < best_t || (t == best_t && (id < best.inst || (id == best.inst && p < best.prim)))) {
+                            best_t = t;
+                            best = LcxoHit{id, p, float(u), float(v), float(t), 0};
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <class F>
+void parallel_rays(size_t n, int threads, F &&f) {
+    if (threads <= 0) threads = int(std::max(1u, std::thread::hardware_concurrency()));
+    std::atomic<size_t> next{0};
+    constexpr size_t kChunk = 256;
+    auto worker = [&] {
+        for (;;) {
+            const size_t b = next.fetch_add(kChunk);
+            if (b >= n) return;
+            const size_t e = std::min(n, b + kChunk);
+            for (size_t i = b; i < e; i++) f(i);
+        }
+    };
+    if (threads == 1 || n <= kChunk) {
+        worker();
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (int i = 0; i < threads; i++) pool.emplace_back(worker);
+    for (auto &t : pool) t.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+void *lcxo_mesh_create(const float *verts, size_t stride_floats, size_t vertex_count, const uint32_t *tris,
+                       size_t tri_count, int leaf_size, int bins) {
+    auto *m = new Mesh;
+    m->vertex_count = vertex_count;
+    m->v.resize(3 * vertex_count);
+    for (size_t i = 0; i < vertex_count; i++)
+        for (int k = 0; k < 3; k++) m->v[3 * i + k] = verts[i * stride_floats + k];
+    m->t.assign(tris, tris + 3 * tri_count);
+    std::vector<Box> boxes(tri_count);
+    for (size_t p = 0; p < tri_count; p++) {
+        if (!m->tri_valid(uint32_t(p))) continue;  // empty box
+        for (int j = 0; j < 3; j++) boxes[p].grow(m->vert(m->t[3 * p + j]));
+    }
+    m->bvh.build(boxes, leaf_size > 0 ? leaf_size : 4, bins > 1 ? bins : 32);
+    return m;
+}
+
+void lcxo_mesh_destroy(void *mesh) { delete static_cast<Mesh *>(mesh); }
+double lcxo_mesh_sah(const void *mesh) { return static_cast<const Mesh *>(mesh)->bvh.sah(); }
+uint32_t lcxo_mesh_depth(const void *mesh) { return static_cast<const Mesh *>(mesh)->bvh.depth; }
+
+void *lcxo_accel_create(size_t n, void *const *meshes, const float *o2w, const uint32_t *masks) {
+    auto *a = new Accel;
+    a->mesh.resize(n);
+    a->o2w.assign(o2w, o2w + 12 * n);
+    a->w2o.resize(12 * n);
+    a->w2o64.resize(12 * n);
+    a->mask.assign(masks, masks + n);
+    std::vector<Box> boxes(n);
+    for (size_t i = 0; i < n; i++) {
+        a->mesh[i] = static_cast<const Mesh *>(meshes[i]);
+        affine_inverse_f32(&o2w[12 * i], &a->w2o[12 * i]);
+        affine_inverse_f64(&o2w[12 * i], &a->w2o64[12 * i]);
+        const Mesh *m = a->mesh[i];
+        if (!m || m->bvh.nodes.empty() || m->bvh.nodes[0].box.empty()) continue;
+        const Box &lb = m->bvh.nodes[0].box;
+        // world box of the 8 transformed corners, widened by a relative ulp so
+        // the FP32 corner arithmetic cannot shrink it
+        for (int c = 0; c < 8; c++) {
+            const double p[3] = {(c & 1) ? lb.hi[0] : lb.lo[0], (c & 2) ? lb.hi[1] : lb.lo[1],
+                                 (c & 4) ? lb.hi[2] : lb.lo[2]};
+            float q[3];
+            for (int k = 0; k < 3; k++) {
+                const float *r = &o2w[12 * i + 4 * k];
+                const double w = r[0] * p[0] + r[1] * p[1] + r[2] * p[2] + r[3];
+                q[k] = float(w);
+            }
+            boxes[i].grow(q);
+        }
+        for (int k = 0; k < 3; k++) {
+            const float pad = 1e-6f * std::max(std::fabs(boxes[i].lo[k]), std::fabs(boxes[i].hi[k])) + 1e-30f;
+            boxes[i].lo[k] -= pad;
+            boxes[i].hi[k] += pad;
+        }
+    }
+    a->bvh.build(boxes, 1, 32);
+    return a;
+}
+
+void lcxo_accel_destroy(void *accel) { delete static_cast<Accel *>(accel); }
+
+void lcxo_trace_closest(const void *accel, const LcxoRay *rays, size_t n, uint32_t mask, LcxoHit *hits,
+                        int threads) {
+    const Accel &a = *static_cast<const Accel *>(accel);
+    parallel_rays(n, threads, [&](size_t i) {
+        LcxoHit h;
+        trace_accel<false>(a, rays[i], mask, h);
+        if (h.inst == kInvalid) h = LcxoHit{kInvalid, kInvalid, 0.0f, 0.0f, rays[i].tmax, 0};
+        hits[i] = h;
+    });
+}
+
+void lcxo_trace_any(const void *accel, const LcxoRay *rays, size_t n, uint32_t mask, uint8_t *occluded,
+                    int threads) {
+    const Accel &a = *static_cast<const Accel *>(accel);
+    parallel_rays(n, threads, [&](size_t i) {
+        LcxoHit h;
+        occluded[i] = trace_accel<true>(a, rays[i], mask, h) ? 1 : 0;
+    });
+}
+
+void lcxo_brute_closest(const void *accel, const LcxoRay *rays, size_t n, uint32_t mask, LcxoHit *hits,
+                        int threads) {
+    const Accel &a = *static_cast<const Accel *>(accel);
+    parallel_rays(n, threads, [&](size_t i) {
+        const LcxoRay &ray = rays[i];
+        LcxoHit best{kInvalid, kInvalid, 0.0f, 0.0f, ray.tmax, 0};
+        for (uint32_t id = 0; id < a.mesh.size(); id++) {
+            const Mesh *m = a.mesh[id];
+            if (!m || (a.mask[id] & mask) == 0u) continue;
+            float oo[3], od[3];
+            transform_ray_f32(&a.w2o[12 * size_t(id)], ray.o, ray.d, oo, od);
+            WtRay wr;
+            wt_setup(wr, oo, od, ray.tmin, ray.tmax);
+            for (uint32_t p = 0; p < m->t.size() / 3; p++) {
+                if (!m->tri_valid(p)) continue;
+                float t, u, v;
+                if (wt_intersect(wr, m->vert(m->t[3 * p]), m->vert(m->t[3 * p + 1]), m->vert(m->t[3 * p + 2]), t, u,
+                                 v) &&
+                    better(t, id, p, best))
+                    best = LcxoHit{id, p, u, v, t, 0};
+            }
+        }
+        if (best.inst == kInvalid) best = LcxoHit{kInvalid, kInvalid, 0.0f, 0.0f, ray.tmax, 0};
+        hits[i] = best;
+    });
+}
+
+void lcxo_fp64_closest(const void *accel, const LcxoRay *rays, size_t n, uint32_t mask, LcxoHit *hits,
+                       double *t64, int threads) {
+    const Accel &a = *static_cast<const Accel *>(accel);
+    parallel_rays(n, threads, [&](size_t i) {
+        LcxoHit h;
+        double t;
+        trace_accel64(a, rays[i], mask, h, t);
+        hits[i] = h;
+        if (t64) t64[i] = t;
+    });
+}
+
+void lcxo_fp64_eval(const void *accel, const LcxoRay *rays, size_t n, const uint32_t *inst, const uint32_t *prim,
+                    LcxoF64Hit *out) {
+    const Accel &a = *static_cast<const Accel *>(accel);
+    for (size_t i = 0; i < n; i++) {
+        out[i] = LcxoF64Hit{0, 0, 0.0, 0.0, 0.0, -1.0};
+        const uint32_t id = inst[i], p = prim[i];
+        if (id >= a.mesh.size() || !a.mesh[id]) continue;
+        const Mesh &m = *a.mesh[id];
+        if (p >= m.t.size() / 3 || !m.tri_valid(p)) continue;
+        const double *w = &a.w2o64[12 * size_t(id)];
+        const LcxoRay &ray = rays[i];
+        double oo[3], od[3];
+        for (int k = 0; k < 3; k++) {
+            oo[k] = w[4 * k] * ray.o[0] + w[4 * k + 1] * ray.o[1] + w[4 * k + 2] * ray.o[2] + w[4 * k + 3];
+            od[k] = w[4 * k] * ray.d[0] + w[4 * k + 1] * ray.d[1] + w[4 * k + 2] * ray.d[2];
+        }
+        WtRay64 wr;
+        wt_setup64(wr, oo, od, ray.tmin, ray.tmax);
+        double v0[3], v1[3], v2[3];
+        for (int k = 0; k < 3; k++) {
+            v0[k] = m.vert(m.t[3 * p])[k];
+            v1[k] = m.vert(m.t[3 * p + 1])[k];
+            v2[k] = m.vert(m.t[3 * p + 2])[k];
+        }
+        double t, u, v, mb;
+        out[i].hit = wt_eval64(wr, v0, v1, v2, t, u, v, mb) ? 1 : 0;
+        out[i].t = t;
+        out[i].u = u;
+        out[i].v = v;
+        out[i].min_bary = mb;
+    }
+}
+
+void lcxo_affine_inverse(const float *o2w, float *w2o) { affine_inverse_f32(o2w, w2o); }
+
+int lcxo_intersect_triangle(const float *o, const float *d, float tmin, float tmax, const float *v0, const float *v1,
+                            const float *v2, float *t, float *u, float *v) {
+    WtRay wr;
+    wt_setup(wr, o, d, tmin, tmax);
+    return wt_intersect(wr, v0, v1, v2, *t, *u, *v) ? 1 : 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,28 @@
+"""CPU tests of the C ABI: the library builds for sm_103a, loads, and exports every declared symbol.
+No compute call is made without a GPU."""
+import ctypes
+import subprocess
+
+from luisacompute_gb300 import _capi
+
+
+def test_exports_every_declared_symbol(lcx):
+    declared = _capi.declared_symbols()
+    assert len(declared) >= 16
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_capi.LIB_PATH)], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [s for s in declared if s not in exported]
+    assert not missing, missing
+    for s in declared:
+        assert hasattr(lcx, s)
+
+
+def test_version_and_error_string(lcx):
+    assert lcx.lcx_version() == 0x000100
+    assert lcx.lcx_last_error_string() is not None
+
+
+def test_struct_sizes():
+    assert ctypes.sizeof(_capi.LcxAccelOption) == 8
+    assert ctypes.sizeof(_capi.LcxMeshBuildCommand) == 64
+    assert ctypes.sizeof(_capi.LcxAccelStats) == 48

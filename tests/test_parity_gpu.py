@@ -1,0 +1,250 @@
+"""GPU parity: the sm_103a kernels (through the C ABI) against the CPU oracle.
+
+The closest-hit rule keeps (t, inst, prim) minimal, and the GPU repeats the oracle's FP32
+operation sequence for the instance transform and the watertight test, so the expected
+result is bit-exact equality of every TriangleHit record; any disagreement is reported
+with the FP64 adjudicator's classification.
+"""
+import numpy as np
+import pytest
+
+from luisacompute_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    assert torch.cuda.is_available()
+    return torch
+
+
+def gpu_scene(scene, option=None):
+    from luisacompute_gb300.accel import accel_from_scene
+    return accel_from_scene(scene, option=option)
+
+
+def trace(acc, rays, layout, mask=0xFF):
+    from luisacompute_gb300.accel import hits_to_numpy, rays_to_device
+    import torch
+    d = rays_to_device(rays)
+    h = acc.trace_closest(d, mask=mask, layout=layout)
+    torch.cuda.synchronize()
+    return hits_to_numpy(h)
+
+
+def trace_any(acc, rays, layout, mask=0xFF):
+    from luisacompute_gb300.accel import rays_to_device
+    import torch
+    d = rays_to_device(rays)
+    o = acc.trace_any(d, mask=mask, layout=layout)
+    torch.cuda.synchronize()
+    return o.cpu().numpy()
+
+
+def assert_bit_exact(oracle_mod, osc, rays, got, want):
+    if np.array_equal(got.view(np.uint8), want.view(np.uint8)):
+        return
+    rep = oracle_mod.adjudicate(osc, rays, got, want)
+    same_id = (got["inst"] == want["inst"]) & (got["prim"] == want["prim"])
+    field_diff = int((~np.all(got.view(np.uint32).reshape(-1, 6)[:, :5] == want.view(np.uint32).reshape(-1, 6)[:, :5],
+                              axis=1) & same_id).sum())
+    raise AssertionError(f"GPU != oracle: {rep['disagree']} id mismatches (near-tie {rep['near_tie']}, grazing "
+                         f"{rep['grazing']}, unexplained {len(rep['unexplained'])}), {field_diff} field mismatches")
+
+
+@pytest.mark.parametrize("layout", [0, 1])
+def test_icosphere_primary_rays(torch_cuda, lcx, oracle_mod, layout):
+    """Icosphere subdivided 6 times (81,920 triangles), 1024x1024 jittered pinhole rays."""
+    scene = S.icosphere_scene(6)
+    rays = S.primary_rays_icosphere(1024, 1024)
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_closest(rays)
+    acc, _ = gpu_scene(scene)
+    got = trace(acc, rays, layout)
+    assert_bit_exact(oracle_mod, osc, rays, got, want)
+    assert 0.2 < (got["inst"] != S.MISS).mean() < 0.6
+
+
+def small_terrain():
+    return S.terrain_scene(n=128, sphere_count=64, sphere_subdiv=3)
+
+
+@pytest.mark.parametrize("layout", [0, 1])
+def test_terrain_incoherent(torch_cuda, lcx, oracle_mod, layout):
+    scene = small_terrain()
+    rays = S.terrain_rays(scene, 200_000, seed=4)
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_closest(rays)
+    acc, _ = gpu_scene(scene)
+    got = trace(acc, rays, layout)
+    assert_bit_exact(oracle_mod, osc, rays, got, want)
+    assert (got["inst"] > 0).sum() > 100  # some sphere instances are hit
+
+
+@pytest.mark.parametrize("layout", [0, 1])
+def test_terrain_shadow_any(torch_cuda, lcx, oracle_mod, layout):
+    scene = small_terrain()
+    rays = S.terrain_shadow_rays(scene, 200_000, seed=5)
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_any(rays)
+    acc, _ = gpu_scene(scene)
+    got = trace_any(acc, rays, layout)
+    assert np.array_equal(got, want)
+    assert 0.05 < want.mean() < 0.95
+
+
+def test_masks(torch_cuda, lcx, oracle_mod):
+    scene = small_terrain()
+    scene.inst_mask = np.array([0x01] + [0x02, 0x04] * 32, np.uint32)
+    rays = S.terrain_rays(scene, 50_000, seed=7)
+    osc = oracle_mod.OracleScene(scene)
+    acc, _ = gpu_scene(scene)
+    for mask in (0xFF, 0x01, 0x02, 0x06, 0x00):
+        got = trace(acc, rays, 1, mask)
+        want = osc.trace_closest(rays, mask)
+        assert_bit_exact(oracle_mod, osc, rays, got, want)
+        if mask == 0:
+            assert np.all(got["inst"] == S.MISS)
+        occ = trace_any(acc, rays, 1, mask)
+        assert np.array_equal(occ.astype(bool), want["inst"] != S.MISS)
+
+
+def test_layouts_identical_and_counts(torch_cuda, lcx):
+    import torch
+    scene = small_terrain()
+    rays = S.terrain_rays(scene, 100_000, seed=9)
+    from luisacompute_gb300.accel import rays_to_device, hits_to_numpy
+    acc, _ = gpu_scene(scene)
+    d = rays_to_device(rays)
+    hq = hits_to_numpy(acc.trace_closest(d, layout=1))
+    hf = hits_to_numpy(acc.trace_closest(d, layout=0))
+    assert np.array_equal(hq.view(np.uint8), hf.view(np.uint8))
+    counts = torch.zeros((rays.shape[0], 3), dtype=torch.int32, device="cuda")
+    hc = hits_to_numpy(acc.trace_closest(d, layout=1, counts=counts))
+    assert np.array_equal(hq.view(np.uint8), hc.view(np.uint8))
+    c = counts.cpu().numpy()
+    assert c[:, 0].min() >= 1 and c[:, 1].mean() > 1
+
+
+def test_miss_record_and_t_range(torch_cuda, lcx, oracle_mod):
+    scene = S.icosphere_scene(3)
+    acc, _ = gpu_scene(scene)
+    rays = np.zeros(6, S.RAY_DTYPE)
+    rays["o"] = [[0, 0, 3], [0, 0, 3], [0, 0, 3], [0, 0, 3], [5, 5, 5], [0, 0, 0]]
+    rays["d"] = [[0, 0, -1], [0, 0, -1], [0, 0, -1], [0, 0, 1], [1, 0, 0], [0, 1, 0]]
+    rays["tmin"] = [0, 0, 2.5, 0, 0, 0]
+    rays["tmax"] = [1e30, 1.5, 1e30, 1e30, 7.0, 1e30]
+    got = trace(acc, rays, 1)
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_closest(rays)
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    assert got["inst"][0] == 0 and abs(got["t"][0] - 2.0) < 2e-2       # front face
+    assert got["inst"][1] == S.MISS and got["t"][1] == np.float32(1.5)  # t_max clips
+    assert got["inst"][2] == 0 and abs(got["t"][2] - 4.0) < 2e-2       # t_min skips the front face
+    assert got["inst"][3] == S.MISS and got["inst"][4] == S.MISS
+    assert got["inst"][5] == 0 and abs(got["t"][5] - 1.0) < 2e-2       # origin inside, back face hit
+
+
+def test_edge_cases(torch_cuda, lcx, oracle_mod):
+    """Empty mesh, single triangle, degenerate triangles, scaled/rotated instances."""
+    import torch
+    from luisacompute_gb300.accel import Accel, mesh_from_data
+    empty = S.MeshData(np.zeros((3, 4), np.float32), np.zeros((0, 3), np.uint32))
+    single = S.MeshData(np.array([[0, 0, 0, 0], [1, 0, 0, 0], [0, 1, 0, 0]], np.float32),
+                        np.array([[0, 1, 2]], np.uint32))
+    degen = S.MeshData(np.array([[0, 0, 0, 0], [1, 0, 0, 0], [2, 0, 0, 0], [0, 1, 0, 0]], np.float32),
+                       np.array([[0, 1, 2], [0, 0, 0], [0, 1, 3]], np.uint32))
+    rng = np.random.default_rng(11)
+    aff = np.concatenate([S.IDENTITY[None],
+                          S.affine_rows(S.random_rotations(3, rng), np.array([0.5, 2.0, 1e-3]),
+                                        rng.uniform(-1, 1, (3, 3)))])
+    scene = S.Scene([empty, single, degen], np.array([0, 1, 2, 1]), aff, np.full(4, 0xFF, np.uint32))
+    osc = oracle_mod.OracleScene(scene)
+    meshes = [mesh_from_data(m).build() for m in scene.meshes]
+    acc = Accel()
+    for i in range(4):
+        acc.emplace_back(meshes[scene.inst_mesh[i]], scene.inst_affine[i].reshape(3, 4))
+    acc.build()
+    rays = S.sphere_rays(100_000, [-2, -2, -2], [2, 2, 2], seed=12)
+    # aim half the rays at the instances' triangles
+    tgt = rng.uniform(-1, 1, (50_000, 3)).astype(np.float32)
+    d = tgt - rays["o"][:50_000]
+    rays["d"][:50_000] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    got = trace(acc, rays, 1)
+    want = osc.trace_closest(rays)
+    assert_bit_exact(oracle_mod, osc, rays, got, want)
+    assert np.all(got["inst"] != 0)  # the empty mesh is never hit
+    torch.cuda.synchronize()
+
+
+def test_errors(torch_cuda, lcx):
+    import torch
+    from luisacompute_gb300 import LcxError
+    from luisacompute_gb300.accel import Accel, Mesh, mesh_from_data
+    from luisacompute_gb300._capi import LCX_ERR_INVALID_ARG, LCX_ERR_NOT_BUILT
+    acc = Accel()
+    with pytest.raises(LcxError) as e:
+        acc.build()  # no instances (src/runtime/rtx/accel.cpp:72-73)
+    assert e.value.code == LCX_ERR_INVALID_ARG
+    rays = torch.zeros((4, 8), dtype=torch.float32, device="cuda")
+    m = mesh_from_data(S.icosphere(1))
+    acc.emplace_back(m)
+    with pytest.raises(LcxError) as e:
+        acc.build()  # mesh not built (accel.rs:356-358)
+    assert e.value.code == LCX_ERR_NOT_BUILT
+    m.build()
+    acc.emplace_back(m)
+    acc.build()
+    acc.trace_closest(rays)
+    # rebuilt mesh invalidates the TLAS until the accel is rebuilt
+    m.build()
+    with pytest.raises(LcxError) as e:
+        acc.trace_closest(rays)
+    assert e.value.code == LCX_ERR_NOT_BUILT
+    acc.build()
+    acc.trace_closest(rays)
+    # vertex stride must be a multiple of 16 (src/runtime/rtx/mesh.cpp:44-45)
+    v = torch.zeros((12, 3), dtype=torch.float32, device="cuda")
+    t = torch.zeros((4, 3), dtype=torch.int32, device="cuda")
+    with pytest.raises(LcxError) as e:
+        Mesh(v, t).build()
+    assert e.value.code == LCX_ERR_INVALID_ARG
+    # triangle index out of range
+    v4 = torch.zeros((3, 4), dtype=torch.float32, device="cuda")
+    bad = torch.tensor([[0, 1, 7]], dtype=torch.int32, device="cuda")
+    with pytest.raises(LcxError) as e:
+        Mesh(v4, bad).build()
+    assert e.value.code == LCX_ERR_INVALID_ARG
+    torch.cuda.synchronize()
+
+
+def test_instance_updates(torch_cuda, lcx, oracle_mod):
+    """set_transform / set_visibility / update_instance_buffer_only / pop_back."""
+    from luisacompute_gb300.accel import Accel, mesh_from_data
+    sph = S.icosphere(3)
+    m = mesh_from_data(sph).build()
+    acc = Accel()
+    acc.emplace_back(m, np.eye(4))
+    acc.emplace_back(m, np.array([[1, 0, 0, 3], [0, 1, 0, 0], [0, 0, 1, 0]], np.float32))
+    acc.build()
+    rays = np.zeros(2, S.RAY_DTYPE)
+    rays["o"] = [[0, 0, 5], [3, 0, 5]]
+    rays["d"] = [[0, 0, -1], [0, 0, -1]]
+    rays["tmax"] = 1e30
+    h = trace(acc, rays, 1)
+    assert list(h["inst"]) == [0, 1]
+    acc.set_visibility_on_update(1, 0)
+    acc.build(update_instance_buffer_only=True)
+    assert list(trace(acc, rays, 1)["inst"]) == [0, 1]  # TLAS not rebuilt yet
+    acc.build()
+    assert list(trace(acc, rays, 1)["inst"]) == [0, S.MISS]
+    acc.set_visibility_on_update(1, 0xFF)
+    acc.set_transform_on_update(0, np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, -10]], np.float32))
+    acc.build()
+    h = trace(acc, rays, 1)
+    assert h["inst"][1] == 1 and h["inst"][0] == 0 and abs(h["t"][0] - 14.0) < 1e-2
+    acc.pop_back()
+    acc.build()
+    assert list(trace(acc, rays, 1)["inst"]) == [0, S.MISS]
