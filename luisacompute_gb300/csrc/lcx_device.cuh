@@ -231,10 +231,12 @@ __device__ __forceinline__ bool wt_intersect(const WtRay &r, float tmin, float t
     return true;
 }
 
-// Safe reciprocal for slab tests (a zero component becomes +-1e-30).
-__device__ __forceinline__ float safe_rcp(float x) {
-    return __fdiv_rn(1.0f, fabsf(x) > 1e-30f ? x : copysignf(1e-30f, x));
-}
+// Reciprocal for slab tests: IEEE, so a zero component gives +-inf.  A ray
+// lying in a slab plane then yields 0 * inf = NaN for that plane, which
+// fminf/fmaxf ignore: the slab does not constrain the ray, as it must not.
+// (Clamping 1/0 to a large finite value instead lets rounding decide the
+// sign of a ray that lies exactly in a box face, and culls it.)
+__device__ __forceinline__ float slab_rcp(float x) { return __fdiv_rn(1.0f, x); }
 
 // Conservative slab acceptance: exit distance widened by 2^-18 relative.
 __device__ __forceinline__ bool slab_accept(float tn, float tf) { return tn <= __fmaf_rn(fabsf(tf), 0x1p-18f, tf); }

@@ -53,9 +53,15 @@ __device__ __forceinline__ void intersect_q(const Node8Q *nodes, uint32_t idx, f
     const float sy = __uint_as_float(((n0.w >> 8) & 0xffu) << 23);
     const float sz = __uint_as_float(((n0.w >> 16) & 0xffu) << 23);
     const float adx = sx * ix, ady = sy * iy, adz = sz * iz;
+    // plane offset (p - o) / d, widened by 2^-20 of itself on each side: its two
+    // roundings can flip the sign of a face the ray lies in when d ~ 0 (1/d ~ 1e30)
     const float aox = (__uint_as_float(n0.x) - ox) * ix;
     const float aoy = (__uint_as_float(n0.y) - oy) * iy;
     const float aoz = (__uint_as_float(n0.z) - oz) * iz;
+    const float slx = fabsf(aox) * 0x1p-20f, sly = fabsf(aoy) * 0x1p-20f, slz = fabsf(aoz) * 0x1p-20f;
+    const float aoxn = aox - slx, aoxf = aox + slx;
+    const float aoyn = aoy - sly, aoyf = aoy + sly;
+    const float aozn = aoz - slz, aozf = aoz + slz;
     // near/far planes by ray direction sign (swap whole byte words)
     const bool nx = ix < 0.0f, ny = iy < 0.0f, nz = iz < 0.0f;
     const uint32_t nx0 = nx ? n3.z : n2.x, nx1 = nx ? n3.w : n2.y, fx0 = nx ? n2.x : n3.z, fx1 = nx ? n2.y : n3.w;
@@ -66,12 +72,12 @@ __device__ __forceinline__ void intersect_q(const Node8Q *nodes, uint32_t idx, f
     for (int s = 0; s < 8; s++) {
         const uint32_t k = s & 3;
         const bool hw = s >= 4;
-        const float tnx = __fmaf_rn(byte_to_float(hw ? nx1 : nx0, k), adx, aox);
-        const float tfx = __fmaf_rn(byte_to_float(hw ? fx1 : fx0, k), adx, aox);
-        const float tny = __fmaf_rn(byte_to_float(hw ? ny1 : ny0, k), ady, aoy);
-        const float tfy = __fmaf_rn(byte_to_float(hw ? fy1 : fy0, k), ady, aoy);
-        const float tnz = __fmaf_rn(byte_to_float(hw ? nz1 : nz0, k), adz, aoz);
-        const float tfz = __fmaf_rn(byte_to_float(hw ? fz1 : fz0, k), adz, aoz);
+        const float tnx = __fmaf_rn(byte_to_float(hw ? nx1 : nx0, k), adx, aoxn);
+        const float tfx = __fmaf_rn(byte_to_float(hw ? fx1 : fx0, k), adx, aoxf);
+        const float tny = __fmaf_rn(byte_to_float(hw ? ny1 : ny0, k), ady, aoyn);
+        const float tfy = __fmaf_rn(byte_to_float(hw ? fy1 : fy0, k), ady, aoyf);
+        const float tnz = __fmaf_rn(byte_to_float(hw ? nz1 : nz0, k), adz, aozn);
+        const float tfz = __fmaf_rn(byte_to_float(hw ? fz1 : fz0, k), adz, aozf);
         const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
         const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
         const uint32_t meta = ((hw ? n1.w : n1.z) >> (8 * k)) & 0xffu;
@@ -180,11 +186,12 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
                     ox = wox;
                     oy = woy;
                     oz = woz;
-                    ix = safe_rcp(wdx);
-                    iy = safe_rcp(wdy);
-                    iz = safe_rcp(wdz);
+                    ix = slab_rcp(wdx);
+                    iy = slab_rcp(wdy);
+                    iz = slab_rcp(wdz);
                     octinv = octant_inv(wdx, wdy, wdz);
-                    G = root_group(octinv);
+                    // a zero direction meets nothing; skip the walk
+                    G = (wdx == 0.0f && wdy == 0.0f && wdz == 0.0f) ? make_uint2(0, 0) : root_group(octinv);
                     sp = 0;
                     in_blas = false;
                     ray_steps = 0;
@@ -291,9 +298,9 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
                     float dx, dy, dz;
                     transform_point(w, wox, woy, woz, ox, oy, oz);
                     transform_dir(w, wdx, wdy, wdz, dx, dy, dz);
-                    ix = safe_rcp(dx);
-                    iy = safe_rcp(dy);
-                    iz = safe_rcp(dz);
+                    ix = slab_rcp(dx);
+                    iy = slab_rcp(dy);
+                    iz = slab_rcp(dz);
                     octinv = octant_inv(dx, dy, dz);
                     wt = wt_setup(ox, oy, oz, dx, dy, dz);
                     const unsigned long long qptr = (unsigned long long)pp.x | ((unsigned long long)pp.y << 32);
@@ -316,9 +323,9 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
                     ox = wox;
                     oy = woy;
                     oz = woz;
-                    ix = safe_rcp(wdx);
-                    iy = safe_rcp(wdy);
-                    iz = safe_rcp(wdz);
+                    ix = slab_rcp(wdx);
+                    iy = slab_rcp(wdy);
+                    iz = slab_rcp(wdz);
                     octinv = octant_inv(wdx, wdy, wdz);
                 }
                 if (sp == 0) {

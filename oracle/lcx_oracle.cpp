@@ -354,12 +354,15 @@ struct Bvh {
 
 // Robust slab test in FP32 with an outward slack on the exit distance.
 inline bool slab(const Box &b, const float *o, const float *inv, float tmin, float tmax, float &tnear) {
+    // near/far planes chosen by the sign of 1/d, so that a NaN (ray in the
+    // plane) reaches fmax/fmin alone and is ignored
     float tn = tmin, tf = tmax;
     for (int k = 0; k < 3; k++) {
-        const float t0 = (b.lo[k] - o[k]) * inv[k];
-        const float t1 = (b.hi[k] - o[k]) * inv[k];
-        tn = std::fmax(tn, std::fmin(t0, t1));
-        tf = std::fmin(tf, std::fmax(t0, t1));
+        const bool neg = std::signbit(inv[k]);
+        const float t0 = ((neg ? b.hi[k] : b.lo[k]) - o[k]) * inv[k];
+        const float t1 = ((neg ? b.lo[k] : b.hi[k]) - o[k]) * inv[k];
+        tn = std::fmax(tn, t0);
+        tf = std::fmin(tf, t1);
     }
     tnear = tn;
     return tn <= tf + std::fabs(tf) * 0x1p-18f;
@@ -368,19 +371,21 @@ inline bool slab(const Box &b, const float *o, const float *inv, float tmin, flo
 inline bool slab64(const Box &b, const double *o, const double *inv, double tmin, double tmax, double &tnear) {
     double tn = tmin, tf = tmax;
     for (int k = 0; k < 3; k++) {
-        const double t0 = (double(b.lo[k]) - o[k]) * inv[k];
-        const double t1 = (double(b.hi[k]) - o[k]) * inv[k];
-        tn = std::fmax(tn, std::fmin(t0, t1));
-        tf = std::fmin(tf, std::fmax(t0, t1));
+        const bool neg = std::signbit(inv[k]);
+        const double t0 = (double(neg ? b.hi[k] : b.lo[k]) - o[k]) * inv[k];
+        const double t1 = (double(neg ? b.lo[k] : b.hi[k]) - o[k]) * inv[k];
+        tn = std::fmax(tn, t0);
+        tf = std::fmin(tf, t1);
     }
     tnear = tn;
     return tn <= tf + std::fabs(tf) * 1e-9;
 }
 
-inline float safe_inv(float x) {
-    return 1.0f / (std::fabs(x) > 1e-30f ? x : std::copysign(1e-30f, x));
-}
-inline double safe_inv64(double x) { return 1.0 / (std::fabs(x) > 1e-300 ? x : std::copysign(1e-300, x)); }
+// IEEE reciprocals: a zero direction component gives +-inf, and a ray lying in
+// a slab plane gives 0 * inf = NaN there, which std::fmin/fmax ignore, so the
+// slab does not constrain that ray.
+inline float safe_inv(float x) { return 1.0f / x; }
+inline double safe_inv64(double x) { return 1.0 / x; }
 
 struct Mesh {
     std::vector<float> v;  // 3 floats per vertex

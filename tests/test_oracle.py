@@ -121,3 +121,27 @@ def test_camera_icosphere_small(oracle_mod):
     p = rays["o"][hit] + rays["d"][hit] * h["t"][hit, None]
     r = np.linalg.norm(p, axis=1)
     assert np.all((r > 0.98) & (r <= 1.0 + 1e-5))
+
+
+def test_bvh_equals_brute_axis_aligned(oracle_mod):
+    """Axis-aligned rays through icosphere vertices and along grid planes: the BVH walk must not
+    cull boxes whose faces contain the ray (zero direction components)."""
+    scene = S.icosphere_scene(3)
+    o = oracle_mod.OracleScene(scene)
+    v = scene.meshes[0].vertices[:, :3]
+    axes = np.eye(3, dtype=np.float32)
+    rays = np.zeros(6 * v.shape[0] + 6, S.RAY_DTYPE)
+    k = 0
+    for a in range(3):
+        for sgn in (1.0, -1.0):
+            d = axes[a] * sgn
+            rays["o"][k:k + v.shape[0]] = v - 3.0 * d
+            rays["d"][k:k + v.shape[0]] = d
+            k += v.shape[0]
+            rays["o"][k], rays["d"][k] = 0.0, d  # from the centre
+            k += 1
+    rays["tmax"] = 1e30
+    got = o.trace_closest(rays)
+    want = o.brute_closest(rays)
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    assert np.all(want["inst"] == 0)

@@ -248,3 +248,40 @@ def test_instance_updates(torch_cuda, lcx, oracle_mod):
     acc.pop_back()
     acc.build()
     assert list(trace(acc, rays, 1)["inst"]) == [0, S.MISS]
+
+
+@pytest.mark.parametrize("layout", [0, 1])
+def test_axis_aligned_exact_ties(torch_cuda, lcx, oracle_mod, layout):
+    """Rays along the axes through the vertices and edges of an integer grid (every hit is a
+    shared edge or vertex; the smallest (inst, prim) among equal t must win), plus rays lying
+    in the grid plane."""
+    n = 9
+    xs = np.arange(n, dtype=np.float32) - 4.0
+    X, Z = np.meshgrid(xs, xs, indexing="xy")
+    v = np.zeros((n * n, 4), np.float32)
+    v[:, 0], v[:, 2] = X.ravel(), Z.ravel()
+    idx = np.arange(n * n).reshape(n, n)
+    a, b, c, d = idx[:-1, :-1].ravel(), idx[:-1, 1:].ravel(), idx[1:, :-1].ravel(), idx[1:, 1:].ravel()
+    tris = np.concatenate([np.stack([a, c, b], 1), np.stack([b, c, d], 1)]).astype(np.uint32)
+    grid = S.MeshData(v, tris)
+    aff = np.stack([S.IDENTITY, S.IDENTITY.copy()])
+    aff[1, 7] = 2.0  # a second copy 2 units above
+    scene = S.Scene([grid], np.array([0, 0]), aff, np.full(2, 0xFF, np.uint32))
+    g = np.arange(-8, 9, dtype=np.float32) * 0.5
+    px, pz = np.meshgrid(g, g)
+    m = px.size
+    rays = np.zeros(3 * m, S.RAY_DTYPE)
+    rays["o"][:m, 0], rays["o"][:m, 1], rays["o"][:m, 2] = px.ravel(), 5.0, pz.ravel()
+    rays["d"][:m] = [0, -1, 0]
+    rays["o"][m:2 * m, 0], rays["o"][m:2 * m, 1], rays["o"][m:2 * m, 2] = px.ravel(), -5.0, pz.ravel()
+    rays["d"][m:2 * m] = [0, 1, 0]
+    rays["o"][2 * m:, 0], rays["o"][2 * m:, 2] = -6.0, pz.ravel()
+    rays["d"][2 * m:] = [1, 0, 0]
+    rays["tmax"] = 1e30
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_closest(rays)
+    assert np.array_equal(want.view(np.uint8), osc.brute_closest(rays).view(np.uint8))
+    acc, _ = gpu_scene(scene)
+    got = trace(acc, rays, layout)
+    assert_bit_exact(oracle_mod, osc, rays, got, want)
+    assert (got["inst"][:2 * m] != S.MISS).sum() >= 2 * 15 * 15
