@@ -206,7 +206,7 @@ LCX_API int lcx_accel_stats(uint64_t accel, LcxAccelStats *out);
  * `ray_count` records.  An instance is eligible when (vis_mask & mask) != 0
  * (accel.rs:414, cuda_device_resource.h:1776).  Back faces are not culled
  * (cuda_mesh.cpp:15-16).  Ties in t are broken by the smaller (inst, prim),
- * so the result does not depend on BVH topology. */
+ * so the result does not depend on BVH topology.  ray_count <= 2^31. */
 LCX_API int lcx_trace_closest(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count,
                       uint32_t mask, LcxTriangleHit *d_hits, void *stream);
 
@@ -231,6 +231,21 @@ LCX_API int lcx_trace_any_ex(uint64_t accel, const LcxRay *d_rays, uint32_t ray_
 LCX_API int lcx_trace_closest_counts(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count,
                              uint32_t mask, LcxTriangleHit *d_hits, uint32_t *d_counts,
                              uint32_t node_layout, void *stream);
+
+/* Synchronises the current device and reports whether any trace call since
+ * the last check hit a kernel-side bound: LCX_ERR_TIMEOUT when a ray exceeded
+ * the per-ray step bound (only a corrupt BVH can cause it), LCX_ERR_DEPTH when
+ * a push found the stack full.  Clears the flags.  (No counterpart in the
+ * reference, whose kernels cannot report errors.) */
+LCX_API int lcx_check_trace_errors(void);
+
+/* Traversal knobs, process-wide (no counterpart in the reference: OptiX and
+ * Embree pick theirs internally).  refill: a warp takes new rays once at
+ * least this many of its 32 lanes are idle (1..32, default 8).  postpone: a
+ * lane defers its triangle tests while fewer than this many lanes would run
+ * them (0 = never, default 8).  Results do not depend on either. */
+LCX_API int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone);
+LCX_API int lcx_get_trace_tuning(uint32_t *refill, uint32_t *postpone);
 
 #ifdef __cplusplus
 }

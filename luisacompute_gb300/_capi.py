@@ -62,6 +62,9 @@ _SIGS = {
     "lcx_trace_any_ex": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
     "lcx_trace_closest_counts": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_uint32,
                                          c_void_p]),
+    "lcx_set_trace_tuning": (c_int, [c_uint32, c_uint32]),
+    "lcx_check_trace_errors": (c_int, []),
+    "lcx_get_trace_tuning": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),
 }
 
 

@@ -46,6 +46,8 @@ int cuda_fail(cudaError_t e, const char *what) {
     } while (0)
 
 constexpr uint32_t kPoolSlots = 4096;  // trace-call counters (16 B each)
+// warps overshoot the ray counter by at most 32 each, so 2^31 keeps it from wrapping
+constexpr uint32_t kMaxTraceRays = 1u << 31;
 
 struct DeviceState {
     int device = -1;
@@ -183,6 +185,13 @@ int check_option(const LcxAccelOption *o) {
 }
 
 int leaf_items_for(const LcxAccelOption &o) { return o.hint == LCX_HINT_FAST_BUILD ? 3 : 2; }
+
+// Traversal knobs (see lcx_set_trace_tuning).
+struct TraceTuning {
+    uint32_t refill = 4;    // measured best on the terrain workload (refill sweep 1..32)
+    uint32_t postpone = 0;  // postponing did not pay on GB300 (sweep 0..12)
+};
+TraceTuning g_tune;
 
 }  // namespace
 
@@ -538,11 +547,15 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     auto a = find_accel(accel);
     if (!a) return fail(LCX_ERR_INVALID_ARG, "unknown accel handle %llu", (unsigned long long)accel);
     if (ray_count == 0) return LCX_OK;
+    if (ray_count > kMaxTraceRays)
+        return fail(LCX_ERR_INVALID_ARG, "ray_count %u exceeds %u per call (32-bit ray counter)", ray_count,
+                    kMaxTraceRays);
     if (!d_rays || (!d_hits && !d_occ)) return fail(LCX_ERR_INVALID_ARG, "null ray or result buffer");
     if (reinterpret_cast<uintptr_t>(d_rays) % 16 != 0) return fail(LCX_ERR_INVALID_ARG, "rays must be 16-byte aligned");
     if (d_hits && reinterpret_cast<uintptr_t>(d_hits) % 8 != 0)
         return fail(LCX_ERR_INVALID_ARG, "hits must be 8-byte aligned");
     TraceParams p{};
+    uint32_t depth_need = 0;
     {
         std::lock_guard<std::mutex> lk(a->mtx);
         if (!a->built) return fail(LCX_ERR_NOT_BUILT, "accel not built");
@@ -554,7 +567,8 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
                 return fail(LCX_ERR_NOT_BUILT, "mesh %llu was rebuilt after the accel build; rebuild the accel",
                             (unsigned long long)mg.first);
         }
-        if (int(a->depth + a->max_blas_depth + 1) > kStackSize)
+        depth_need = a->depth + a->max_blas_depth + 2;
+        if (int(depth_need) > kStackSize)
             return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the traversal stack (%d)", a->depth,
                         a->max_blas_depth, kStackSize);
         p.tlas_q = a->qn;
@@ -571,9 +585,46 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     p.counts = d_counts;
     p.ray_count = ray_count;
     p.mask = mask & 0xffu;
+    p.refill = g_tune.refill;
+    p.postpone = g_tune.postpone;
+    // regular pushes need at most tlas_depth + blas_depth + 2 entries; postponed
+    // triangle groups may use what is left
+    p.postpone_sp = kStackSize - int(depth_need);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     LCX_CUDA(cudaMemsetAsync(p.pool, 0, 4 * sizeof(uint32_t), st), "trace counter reset");
     LCX_CUDA(launch_trace(p, int(layout), d_occ != nullptr, d_counts != nullptr, st), "trace launch");
+    return LCX_OK;
+}
+
+int lcx_check_trace_errors(void) {
+    DeviceState *ds = nullptr;
+    if (int r = current_device_state(&ds)) return r;
+    LCX_CUDA(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    std::vector<uint32_t> h(kPoolSlots * 4);
+    LCX_CUDA(cudaMemcpy(h.data(), ds->pool, h.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost), "pool readback");
+    uint32_t flags = 0;
+    for (uint32_t i = 0; i < kPoolSlots; i++) flags |= h[4 * i + 1];
+    if (flags) {
+        for (uint32_t i = 0; i < kPoolSlots; i++) h[4 * i + 1] = 0;
+        LCX_CUDA(cudaMemcpy(ds->pool, h.data(), h.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "pool reset");
+    }
+    if (flags & 2u) return fail(LCX_ERR_TIMEOUT, "a ray exceeded the traversal step bound (corrupt BVH?)");
+    if (flags & 1u) return fail(LCX_ERR_DEPTH, "a ray overflowed the traversal stack");
+    return LCX_OK;
+}
+
+int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone) {
+    if (refill < 1 || refill > 32 || postpone > 32)
+        return fail(LCX_ERR_INVALID_ARG, "tuning out of range (refill 1..32, postpone 0..32)");
+    g_tune.refill = refill;
+    g_tune.postpone = postpone;
+    return LCX_OK;
+}
+
+int lcx_get_trace_tuning(uint32_t *refill, uint32_t *postpone) {
+    if (!refill || !postpone) return fail(LCX_ERR_INVALID_ARG, "null output");
+    *refill = g_tune.refill;
+    *postpone = g_tune.postpone;
     return LCX_OK;
 }
 

@@ -187,9 +187,9 @@ __device__ __forceinline__ WtRay wt_setup(float ox, float oy, float oz, float dx
         ky = t;
     }
     const float dkx = pick3(kx, dx, dy, dz), dky = pick3(ky, dx, dy, dz);
-    r.Sx = __fdiv_rn(dkx, dkz);
-    r.Sy = __fdiv_rn(dky, dkz);
     r.Sz = __fdiv_rn(1.0f, dkz);
+    r.Sx = __fmul_rn(dkx, r.Sz);
+    r.Sy = __fmul_rn(dky, r.Sz);
     r.perm = kx | (ky << 2) | (kz << 4);
     return r;
 }
@@ -236,7 +236,13 @@ __device__ __forceinline__ bool wt_intersect(const WtRay &r, float tmin, float t
 // fminf/fmaxf ignore: the slab does not constrain the ray, as it must not.
 // (Clamping 1/0 to a large finite value instead lets rounding decide the
 // sign of a ray that lies exactly in a box face, and culls it.)
-__device__ __forceinline__ float slab_rcp(float x) { return __fdiv_rn(1.0f, x); }
+// The approximate MUFU reciprocal (rcp.approx: 1 ulp, +-0 -> +-inf) is enough:
+// the slab acceptance carries a 2^-18 relative slack.
+__device__ __forceinline__ float slab_rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 
 // Conservative slab acceptance: exit distance widened by 2^-18 relative.
 __device__ __forceinline__ bool slab_accept(float tn, float tf) { return tn <= __fmaf_rn(fabsf(tf), 0x1p-18f, tf); }

@@ -95,6 +95,9 @@ struct TraceParams {
     uint32_t *pool;  // [0] ray counter, [1] error flags
     uint32_t ray_count;
     uint32_t mask;
+    uint32_t refill;      // refill a warp when at least this many lanes are idle (1..32)
+    uint32_t postpone;    // postpone triangle tests when fewer lanes than this would run them (0 = off)
+    int32_t postpone_sp;  // postpone only while the stack depth is below this
 };
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st);
 int trace_grid_blocks(int layout, bool any, bool counting);

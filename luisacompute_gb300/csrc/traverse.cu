@@ -5,9 +5,11 @@
 // per-ray Embree rtcIntersect1 / rtcOccluded1 calls of the CPU backend
 // (src/rust/luisa_compute_backend_impl/src/cpu/accel.rs:449-535) with one
 // batched kernel:
-//   * persistent warps: each warp takes rays from a global counter, 32 at a
-//     time, and refills its idle lanes whenever at least kRefill of them have
-//     finished (dynamic ray fetch, Aila & Laine 2009);
+//   * persistent warps: each warp takes rays from a global counter and, after
+//     every traversal step, refills its idle lanes once at least P.refill of
+//     them have finished (dynamic ray fetch, Aila & Laine 2009);
+//   * a lane whose triangles would be tested by fewer than P.postpone lanes
+//     pushes them and keeps walking nodes (postponing, Ylitie et al. 2017);
 //   * node groups: a visited node yields the hit mask of its internal
 //     children (bits ordered front to back by the ray octant) and the hit
 //     mask of its leaf items; a group with hits left is pushed on a per-thread
@@ -26,8 +28,6 @@ namespace lcx {
 namespace {
 
 constexpr int kTraceBlock = 128;
-constexpr int kRefill = 8;          // refill a warp when this many lanes are idle
-constexpr int kStepsPerFetch = 24;  // traversal steps between refill checks
 constexpr uint32_t kMaxRaySteps = 1u << 22;  // per-ray bound: a corrupt tree ends the ray, never hangs
 
 __device__ __forceinline__ uint2 root_group(uint32_t octinv) {
@@ -138,6 +138,9 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
     const uint32_t lane = threadIdx.x & 31u;
     const void *const tlas_nodes = kLayout == LCX_NODES_QUANT8 ? static_cast<const void *>(P.tlas_q)
                                                                 : static_cast<const void *>(P.tlas_f);
+    const int refill = int(P.refill);
+    const int postpone = int(P.postpone);
+    const int postpone_sp = P.postpone_sp;
 
     bool active = false, exhausted = false;
     uint32_t rid = 0;
@@ -145,23 +148,33 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
     float wox = 0, woy = 0, woz = 0, wdx = 0, wdy = 0, wdz = 1;
     float tmin = 0, best_t = 0, best_u = 0, best_v = 0;
     uint32_t best_inst = kInvalid, best_prim = kInvalid;
-    // current-space ray
+    // current-space ray (world at the TLAS level, object inside a BLAS)
     float ox = 0, oy = 0, oz = 0, ix = 1, iy = 1, iz = 1;
     uint32_t octinv = 0;
     WtRay wt{};
     uint2 G = make_uint2(0, 0);
     int sp = 0, blas_sp = 0;
-    bool in_blas = false;
+    bool in_blas = false, occluded = false;
     uint32_t cur_inst = 0;
     const void *blas_nodes = nullptr;
     const TriRec *blas_tris = nullptr;
     uint32_t c_nodes = 0, c_tris = 0, c_insts = 0;
     uint32_t ray_steps = 0;
 
+    auto push = [&](uint2 v) {
+        if (sp < kStackSize) {
+            stk[sp * kTraceBlock] = v;
+            sp++;
+        } else {
+            atomicOr(P.pool + 1, 1u);  // cannot happen within the host's depth check
+        }
+    };
+
     for (;;) {
+        // warp-synchronous refill: idle lanes take new rays as soon as enough of them are idle
         const uint32_t idle = __ballot_sync(~0u, !active);
         const int n_idle = __popc(idle);
-        if (!exhausted && n_idle >= kRefill) {
+        if (!exhausted && n_idle >= refill) {
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(P.pool, uint32_t(n_idle));
             base = __shfl_sync(~0u, base, 0);
@@ -194,6 +207,7 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
                     G = (wdx == 0.0f && wdy == 0.0f && wdz == 0.0f) ? make_uint2(0, 0) : root_group(octinv);
                     sp = 0;
                     in_blas = false;
+                    occluded = false;
                     ray_steps = 0;
                     if (kCount) c_nodes = c_tris = c_insts = 0;
                 }
@@ -205,27 +219,19 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
         }
         if (!active) continue;
 
-        bool done = false, occluded = false;
-        for (int step = 0; step < kStepsPerFetch && !done; step++) {
-            if (++ray_steps > kMaxRaySteps) {
-                atomicOr(P.pool + 1, 2u);
-                done = true;
-                break;
-            }
+        // ---- one traversal step: visit one node (or take a popped item group), then its items
+        bool done = false;
+        if (++ray_steps > kMaxRaySteps) {
+            atomicOr(P.pool + 1, 2u);
+            done = true;
+        } else {
             uint2 Gt;
             if (G.y >= 0x01000000u) {
                 const uint32_t key = __ffs(G.y >> 24) - 1u;
                 G.y &= ~(1u << (24 + key));
                 const uint32_t slot = key ^ octinv;
                 const uint32_t child = G.x + __popc(G.y & 0xffu & ((1u << slot) - 1u));
-                if (G.y >= 0x01000000u) {
-                    if (sp < kStackSize) {
-                        stk[sp * kTraceBlock] = G;
-                        sp++;
-                    } else {
-                        atomicOr(P.pool + 1, 1u);
-                    }
-                }
+                if (G.y >= 0x01000000u) push(G);
                 const void *nodes = in_blas ? blas_nodes : tlas_nodes;
                 if (kLayout == LCX_NODES_QUANT8)
                     intersect_q(static_cast<const Node8Q *>(nodes), child, ox, oy, oz, ix, iy, iz, octinv, tmin,
@@ -241,6 +247,13 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
 
             if (in_blas) {
                 while (Gt.y) {
+                    // postpone the triangles of a lane that would test them nearly alone,
+                    // while it still has nodes to walk in the meantime
+                    if (postpone > 0 && G.y >= 0x01000000u && sp < postpone_sp &&
+                        int(__popc(__activemask())) < postpone) {
+                        push(Gt);
+                        break;
+                    }
                     const uint32_t k = __ffs(Gt.y) - 1u;
                     Gt.y &= Gt.y - 1u;
                     const float4 *tp = reinterpret_cast<const float4 *>(blas_tris + Gt.x + k);
@@ -263,10 +276,7 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
                         }
                     }
                 }
-                if (kAny && occluded) {
-                    done = true;
-                    break;
-                }
+                if (kAny && occluded) done = true;
             } else {
                 while (Gt.y) {
                     const uint32_t k = __ffs(Gt.y) - 1u;
@@ -278,22 +288,8 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
                     const float4 r1 = __ldg(reinterpret_cast<const float4 *>(ip + 1));
                     const float4 r2 = __ldg(reinterpret_cast<const float4 *>(ip + 2));
                     const uint4 pp = __ldg(ip + 3);  // qnodes (x,y), tris (z,w)
-                    if (Gt.y) {
-                        if (sp < kStackSize) {
-                            stk[sp * kTraceBlock] = Gt;
-                            sp++;
-                        } else {
-                            atomicOr(P.pool + 1, 1u);
-                        }
-                    }
-                    if (G.y) {
-                        if (sp < kStackSize) {
-                            stk[sp * kTraceBlock] = G;
-                            sp++;
-                        } else {
-                            atomicOr(P.pool + 1, 1u);
-                        }
-                    }
+                    if (Gt.y) push(Gt);
+                    if (G.y) push(G);
                     const float w[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
                     float dx, dy, dz;
                     transform_point(w, wox, woy, woz, ox, oy, oz);
@@ -317,7 +313,7 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
                 }
             }
 
-            if (G.y == 0u) {
+            if (!done && G.y == 0u) {
                 if (in_blas && sp == blas_sp) {
                     in_blas = false;
                     ox = wox;

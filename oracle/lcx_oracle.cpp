@@ -81,9 +81,9 @@ void wt_setup(WtRay &r, const float *o, const float *d, float tmin, float tmax) 
     r.kx = kx;
     r.ky = ky;
     r.kz = kz;
-    r.Sx = d[kx] / d[kz];
-    r.Sy = d[ky] / d[kz];
     r.Sz = 1.0f / d[kz];
+    r.Sx = d[kx] * r.Sz;
+    r.Sy = d[ky] * r.Sz;
     r.tmin = tmin;
     r.tmax = tmax;
 }

@@ -25,12 +25,18 @@ def gpu_scene(scene, option=None):
     return accel_from_scene(scene, option=option)
 
 
+def no_kernel_errors():
+    from luisacompute_gb300 import _capi
+    _capi.check(_capi.load().lcx_check_trace_errors(), "lcx_check_trace_errors")
+
+
 def trace(acc, rays, layout, mask=0xFF):
     from luisacompute_gb300.accel import hits_to_numpy, rays_to_device
     import torch
     d = rays_to_device(rays)
     h = acc.trace_closest(d, mask=mask, layout=layout)
     torch.cuda.synchronize()
+    no_kernel_errors()
     return hits_to_numpy(h)
 
 
@@ -40,6 +46,7 @@ def trace_any(acc, rays, layout, mask=0xFF):
     d = rays_to_device(rays)
     o = acc.trace_any(d, mask=mask, layout=layout)
     torch.cuda.synchronize()
+    no_kernel_errors()
     return o.cpu().numpy()
 
 
@@ -285,3 +292,27 @@ def test_axis_aligned_exact_ties(torch_cuda, lcx, oracle_mod, layout):
     got = trace(acc, rays, layout)
     assert_bit_exact(oracle_mod, osc, rays, got, want)
     assert (got["inst"][:2 * m] != S.MISS).sum() >= 2 * 15 * 15
+
+
+@pytest.mark.parametrize("refill,postpone", [(1, 0), (8, 8), (16, 12), (32, 32), (4, 20)])
+def test_tuning_does_not_change_results(torch_cuda, lcx, oracle_mod, refill, postpone):
+    from luisacompute_gb300 import _capi
+    lib = _capi.load()
+    scene = small_terrain()
+    rays = S.terrain_rays(scene, 100_000, seed=13)
+    want = oracle_mod.OracleScene(scene).trace_closest(rays)
+    acc, _ = gpu_scene(scene)
+    old = (ctypes_u32(), ctypes_u32())
+    _capi.check(lib.lcx_get_trace_tuning(*old), "get")
+    try:
+        _capi.check(lib.lcx_set_trace_tuning(refill, postpone), "set")
+        for layout in (0, 1):
+            got = trace(acc, rays, layout)
+            assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    finally:
+        _capi.check(lib.lcx_set_trace_tuning(old[0].value, old[1].value), "set")
+
+
+def ctypes_u32():
+    import ctypes
+    return ctypes.c_uint32(0)
