@@ -1,0 +1,283 @@
+// accel_ext.hpp — C++ host side of the GB300 Mesh/Accel path, shaped like
+// LuisaCompute's own interfaces so that a backend can hand it out from
+// DeviceInterface::extension("AccelGpuExt").
+//
+//   AccelGpuExt        a DeviceExtension (include/luisa/runtime/rhi/device_interface.h:90-93)
+//                      with `static constexpr std::string_view name`, like the reference's
+//                      extensions (include/luisa/backends/ext/pinned_memory_ext.hpp:17-22);
+//                      its methods are the accel part of DeviceInterface
+//                      (device_interface.h:171-184) plus the visits of MeshBuildCommand and
+//                      AccelBuildCommand (cuda_command_encoder.cpp:235-243).
+//   MeshBuildCommand   fields of include/luisa/runtime/rhi/command.h:407-444.
+//   AccelBuildCommand  fields of command.h:594-616, Modification of command.h:534-592.
+//   Mesh / Accel       RAII host objects with the reference's staging API
+//                      (include/luisa/runtime/rtx/accel.h:21-134, src/runtime/rtx/accel.cpp:68-249).
+//
+// Header-only over the C ABI of lcx_accel.h; errors are status codes wrapped
+// in lcx::Error exceptions by the RAII layer, never aborts.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <string_view>
+#include <vector>
+
+#include "../lcx_accel.h"
+
+namespace lcx {
+
+class Error : public std::runtime_error {
+public:
+    Error(int code, const std::string &where)
+        : std::runtime_error(where + ": " + lcx_last_error_string()), code_(code) {}
+    [[nodiscard]] int code() const noexcept { return code_; }
+
+private:
+    int code_;
+};
+
+inline void check(int code, const char *where) {
+    if (code != LCX_OK) throw Error(code, where);
+}
+
+// include/luisa/runtime/rhi/resource.h:94-125
+struct AccelOption {
+    enum struct UsageHint : uint32_t { FAST_TRACE = LCX_HINT_FAST_TRACE, FAST_BUILD = LCX_HINT_FAST_BUILD };
+    UsageHint hint{UsageHint::FAST_TRACE};
+    bool allow_compaction{true};
+    bool allow_update{false};
+    [[nodiscard]] LcxAccelOption c() const noexcept {
+        LcxAccelOption o{};
+        o.hint = static_cast<uint32_t>(hint);
+        o.allow_compaction = allow_compaction;
+        o.allow_update = allow_update;
+        return o;
+    }
+};
+
+// include/luisa/runtime/rhi/command.h:401-404
+enum struct AccelBuildRequest : uint32_t {
+    PREFER_UPDATE = LCX_REQUEST_PREFER_UPDATE,
+    FORCE_BUILD = LCX_REQUEST_FORCE_BUILD,
+};
+
+// include/luisa/runtime/rhi/resource.h ResourceCreationInfo: handle + native handle
+struct ResourceCreationInfo {
+    uint64_t handle{0};
+    void *native_handle{nullptr};
+};
+
+using Ray = LcxRay;
+using TriangleHit = LcxTriangleHit;
+using Modification = LcxModification;
+
+struct MeshBuildCommand {
+    uint64_t handle;
+    AccelBuildRequest request;
+    uint64_t vertex_buffer;
+    size_t vertex_buffer_offset;
+    size_t vertex_buffer_size;
+    size_t vertex_stride;
+    uint64_t triangle_buffer;
+    size_t triangle_buffer_offset;
+    size_t triangle_buffer_size;
+};
+
+struct AccelBuildCommand {
+    uint64_t handle;
+    uint32_t instance_count;
+    AccelBuildRequest request;
+    std::vector<Modification> modifications;
+    bool update_instance_buffer_only;
+};
+
+// The device extension a backend returns from extension("AccelGpuExt").
+class AccelGpuExt {
+public:
+    static constexpr std::string_view name = "AccelGpuExt";
+
+    explicit AccelGpuExt(int device = 0) { check(lcx_device_init(device), "lcx_device_init"); }
+
+    [[nodiscard]] ResourceCreationInfo create_mesh(const AccelOption &option) const {
+        const LcxAccelOption o = option.c();
+        ResourceCreationInfo info;
+        check(lcx_mesh_create(&o, &info.handle), "create_mesh");
+        return info;
+    }
+    void destroy_mesh(uint64_t handle) const { check(lcx_mesh_destroy(handle), "destroy_mesh"); }
+
+    [[nodiscard]] ResourceCreationInfo create_accel(const AccelOption &option) const {
+        const LcxAccelOption o = option.c();
+        ResourceCreationInfo info;
+        check(lcx_accel_create(&o, &info.handle), "create_accel");
+        return info;
+    }
+    void destroy_accel(uint64_t handle) const { check(lcx_accel_destroy(handle), "destroy_accel"); }
+
+    // Command visits, stream-ordered on `stream` (a cudaStream_t).
+    void dispatch(const MeshBuildCommand &cmd, void *stream) const {
+        LcxMeshBuildCommand c{};
+        c.request = static_cast<uint32_t>(cmd.request);
+        c.vertex_buffer = cmd.vertex_buffer;
+        c.vertex_buffer_offset = cmd.vertex_buffer_offset;
+        c.vertex_buffer_size = cmd.vertex_buffer_size;
+        c.vertex_stride = cmd.vertex_stride;
+        c.triangle_buffer = cmd.triangle_buffer;
+        c.triangle_buffer_offset = cmd.triangle_buffer_offset;
+        c.triangle_buffer_size = cmd.triangle_buffer_size;
+        check(lcx_mesh_build(cmd.handle, &c, stream), "MeshBuildCommand");
+    }
+    void dispatch(const AccelBuildCommand &cmd, void *stream) const {
+        check(lcx_accel_build(cmd.handle, cmd.instance_count, static_cast<uint32_t>(cmd.request),
+                              cmd.modifications.data(), cmd.modifications.size(), cmd.update_instance_buffer_only,
+                              stream),
+              "AccelBuildCommand");
+    }
+
+    // Batched ray queries (device buffers).
+    void trace_closest(uint64_t accel, const Ray *rays, uint32_t n, uint32_t mask, TriangleHit *hits,
+                       void *stream) const {
+        check(lcx_trace_closest(accel, rays, n, mask, hits, stream), "trace_closest");
+    }
+    void trace_any(uint64_t accel, const Ray *rays, uint32_t n, uint32_t mask, uint8_t *occluded,
+                   void *stream) const {
+        check(lcx_trace_any(accel, rays, n, mask, occluded, stream), "trace_any");
+    }
+};
+
+// ---------------------------------------------------------------- RAII layer
+
+class Mesh {
+public:
+    // vertices: device float3-in-16-byte records (stride multiple of 16); triangles: device uint3
+    Mesh(const AccelGpuExt &ext, uint64_t vertex_buffer, size_t vertex_count, size_t vertex_stride,
+         uint64_t triangle_buffer, size_t triangle_count, const AccelOption &option = {})
+        : ext_(&ext), v_(vertex_buffer), v_stride_(vertex_stride), v_size_(vertex_count * vertex_stride),
+          t_(triangle_buffer), t_size_(triangle_count * sizeof(LcxTriangle)) {
+        handle_ = ext.create_mesh(option).handle;
+    }
+    Mesh(const Mesh &) = delete;
+    Mesh &operator=(const Mesh &) = delete;
+    ~Mesh() {
+        if (handle_) lcx_mesh_destroy(handle_);
+    }
+    // src/runtime/rtx/mesh.cpp:6-12
+    [[nodiscard]] MeshBuildCommand build(AccelBuildRequest request = AccelBuildRequest::FORCE_BUILD) const {
+        return MeshBuildCommand{handle_, request, v_, 0, v_size_, v_stride_, t_, 0, t_size_};
+    }
+    [[nodiscard]] uint64_t handle() const noexcept { return handle_; }
+
+private:
+    const AccelGpuExt *ext_;
+    uint64_t handle_{0};
+    uint64_t v_;
+    size_t v_stride_, v_size_;
+    uint64_t t_;
+    size_t t_size_;
+};
+
+class Accel {
+public:
+    explicit Accel(const AccelGpuExt &ext, const AccelOption &option = {}) : ext_(&ext) {
+        handle_ = ext.create_accel(option).handle;
+    }
+    Accel(const Accel &) = delete;
+    Accel &operator=(const Accel &) = delete;
+    ~Accel() {
+        if (handle_) lcx_accel_destroy(handle_);
+    }
+
+    // src/runtime/rtx/accel.cpp:88-100; transform is row-major 3x4 (command.h:557-571)
+    void emplace_back(const Mesh &mesh, const std::array<float, 12> &affine, uint8_t visibility_mask = 0xffu,
+                      bool opaque = true, uint32_t user_id = 0) {
+        const auto index = static_cast<uint32_t>(count_);
+        Modification &m = mod(index);
+        m.primitive = mesh.handle();
+        std::memcpy(m.affine, affine.data(), sizeof(m.affine));
+        m.vis_mask = visibility_mask;
+        m.user_id = user_id;
+        m.flags = LCX_MOD_PRIMITIVE | LCX_MOD_TRANSFORM | LCX_MOD_VISIBILITY | LCX_MOD_USER_ID |
+                  (opaque ? LCX_MOD_OPAQUE_ON : LCX_MOD_OPAQUE_OFF);
+        count_++;
+    }
+    void pop_back() {
+        if (count_ == 0) return;
+        count_--;
+        mods_.erase(static_cast<uint32_t>(count_));
+    }
+    void set_transform_on_update(uint32_t index, const std::array<float, 12> &affine) {
+        Modification &m = checked_mod(index);
+        std::memcpy(m.affine, affine.data(), sizeof(m.affine));
+        m.flags |= LCX_MOD_TRANSFORM;
+    }
+    void set_visibility_on_update(uint32_t index, uint8_t mask) {
+        Modification &m = checked_mod(index);
+        m.vis_mask = mask;
+        m.flags |= LCX_MOD_VISIBILITY;
+    }
+    void set_opaque_on_update(uint32_t index, bool opaque) {
+        Modification &m = checked_mod(index);
+        m.flags = (m.flags & ~uint32_t(LCX_MOD_OPAQUE_ON | LCX_MOD_OPAQUE_OFF)) |
+                  (opaque ? LCX_MOD_OPAQUE_ON : LCX_MOD_OPAQUE_OFF);
+    }
+    void set_user_id_on_update(uint32_t index, uint32_t user_id) {
+        Modification &m = checked_mod(index);
+        m.user_id = user_id;
+        m.flags |= LCX_MOD_USER_ID;
+    }
+    // src/runtime/rtx/accel.cpp:68-86 (the staged modifications are consumed)
+    [[nodiscard]] AccelBuildCommand build(AccelBuildRequest request = AccelBuildRequest::FORCE_BUILD,
+                                          bool update_instance_buffer_only = false) {
+        AccelBuildCommand cmd{handle_, static_cast<uint32_t>(count_), request, {}, update_instance_buffer_only};
+        cmd.modifications.reserve(mods_.size());
+        for (auto &kv : mods_) cmd.modifications.push_back(kv.second);
+        mods_.clear();
+        return cmd;
+    }
+    [[nodiscard]] uint64_t handle() const noexcept { return handle_; }
+    [[nodiscard]] size_t size() const noexcept { return count_; }
+
+private:
+    Modification &mod(uint32_t index) {
+        auto it = mods_.find(index);
+        if (it == mods_.end()) {
+            Modification m{};
+            m.index = index;
+            it = mods_.emplace(index, m).first;
+        }
+        return it->second;
+    }
+    Modification &checked_mod(uint32_t index) {
+        if (index >= count_) throw std::out_of_range("instance index out of range");
+        return mod(index);
+    }
+    const AccelGpuExt *ext_;
+    uint64_t handle_{0};
+    size_t count_{0};
+    std::map<uint32_t, Modification> mods_;
+};
+
+// `stream << mesh.build() << accel.build()` in the reference becomes
+// CommandStream{ext, stream} << mesh.build() << accel.build().
+class CommandStream {
+public:
+    CommandStream(const AccelGpuExt &ext, void *stream) : ext_(&ext), stream_(stream) {}
+    CommandStream &operator<<(const MeshBuildCommand &c) {
+        ext_->dispatch(c, stream_);
+        return *this;
+    }
+    CommandStream &operator<<(const AccelBuildCommand &c) {
+        ext_->dispatch(c, stream_);
+        return *this;
+    }
+
+private:
+    const AccelGpuExt *ext_;
+    void *stream_;
+};
+
+}  // namespace lcx

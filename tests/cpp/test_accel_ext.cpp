@@ -1,0 +1,97 @@
+// C++ host API test: builds a mesh + accel through lcx::AccelGpuExt with the
+// reference-shaped command flow and checks analytic hits.  Exit code 0 = pass.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "lcx/accel_ext.hpp"
+
+#define REQUIRE(c)                                                      \
+    do {                                                                \
+        if (!(c)) {                                                     \
+            std::fprintf(stderr, "FAILED %s at line %d\n", #c, __LINE__); \
+            return 1;                                                   \
+        }                                                               \
+    } while (0)
+
+int main() {
+    try {
+        lcx::AccelGpuExt ext{0};
+        REQUIRE(lcx::AccelGpuExt::name == "AccelGpuExt");
+        // unit quad in z = 0 made of two triangles
+        const float verts[4][4] = {{0, 0, 0, 0}, {1, 0, 0, 0}, {0, 1, 0, 0}, {1, 1, 0, 0}};
+        const uint32_t tris[2][3] = {{0, 1, 2}, {1, 3, 2}};
+        void *dv = nullptr, *dt = nullptr, *dr = nullptr, *dh = nullptr, *docc = nullptr;
+        REQUIRE(cudaMalloc(&dv, sizeof(verts)) == cudaSuccess);
+        REQUIRE(cudaMalloc(&dt, sizeof(tris)) == cudaSuccess);
+        cudaMemcpy(dv, verts, sizeof(verts), cudaMemcpyHostToDevice);
+        cudaMemcpy(dt, tris, sizeof(tris), cudaMemcpyHostToDevice);
+        lcx::Mesh mesh{ext, reinterpret_cast<uint64_t>(dv), 4, 16, reinterpret_cast<uint64_t>(dt), 2};
+        lcx::Accel accel{ext};
+        accel.emplace_back(mesh, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0});                 // identity
+        accel.emplace_back(mesh, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, -2}, 0x02u, true, 7);  // z = -2, mask 2
+        lcx::CommandStream stream{ext, nullptr};
+        stream << mesh.build() << accel.build();
+
+        std::vector<lcx::Ray> rays(4);
+        auto set = [&](int i, float x, float y) {
+            rays[i] = lcx::Ray{{x, y, 5.0f}, 0.0f, {0.0f, 0.0f, -1.0f}, 1e30f};
+        };
+        set(0, 0.25f, 0.25f);  // triangle 0 of instance 0
+        set(1, 0.75f, 0.75f);  // triangle 1 of instance 0
+        set(2, 2.0f, 2.0f);    // miss
+        set(3, 0.25f, 0.75f);  // triangle 0 (u = 0.25, v = 0.75 ... on edge 1-2 side)
+        REQUIRE(cudaMalloc(&dr, sizeof(lcx::Ray) * rays.size()) == cudaSuccess);
+        REQUIRE(cudaMalloc(&dh, sizeof(lcx::TriangleHit) * rays.size()) == cudaSuccess);
+        REQUIRE(cudaMalloc(&docc, rays.size()) == cudaSuccess);
+        cudaMemcpy(dr, rays.data(), sizeof(lcx::Ray) * rays.size(), cudaMemcpyHostToDevice);
+        ext.trace_closest(accel.handle(), static_cast<lcx::Ray *>(dr), 4, 0xffu, static_cast<lcx::TriangleHit *>(dh),
+                          nullptr);
+        std::vector<lcx::TriangleHit> hits(4);
+        cudaMemcpy(hits.data(), dh, sizeof(lcx::TriangleHit) * 4, cudaMemcpyDeviceToHost);
+        REQUIRE(hits[0].inst == 0 && hits[0].prim == 0 && hits[0].committed_ray_t == 5.0f);
+        REQUIRE(hits[0].bary[0] == 0.25f && hits[0].bary[1] == 0.25f);
+        REQUIRE(hits[1].inst == 0 && hits[1].prim == 1);
+        REQUIRE(hits[2].inst == 0xffffffffu && hits[2].committed_ray_t == 1e30f);
+        REQUIRE(hits[3].inst == 0);
+        // mask 2 sees only the lower instance (t = 7)
+        ext.trace_closest(accel.handle(), static_cast<lcx::Ray *>(dr), 4, 0x02u, static_cast<lcx::TriangleHit *>(dh),
+                          nullptr);
+        cudaMemcpy(hits.data(), dh, sizeof(lcx::TriangleHit) * 4, cudaMemcpyDeviceToHost);
+        REQUIRE(hits[0].inst == 1 && hits[0].committed_ray_t == 7.0f);
+        ext.trace_any(accel.handle(), static_cast<lcx::Ray *>(dr), 4, 0xffu, static_cast<uint8_t *>(docc), nullptr);
+        uint8_t occ[4];
+        cudaMemcpy(occ, docc, 4, cudaMemcpyDeviceToHost);
+        REQUIRE(occ[0] == 1 && occ[1] == 1 && occ[2] == 0 && occ[3] == 1);
+        // updates: hide instance 0, move instance 1
+        accel.set_visibility_on_update(0, 0);
+        accel.set_transform_on_update(1, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, -1});
+        stream << accel.build();
+        ext.trace_closest(accel.handle(), static_cast<lcx::Ray *>(dr), 4, 0xffu, static_cast<lcx::TriangleHit *>(dh),
+                          nullptr);
+        cudaMemcpy(hits.data(), dh, sizeof(lcx::TriangleHit) * 4, cudaMemcpyDeviceToHost);
+        REQUIRE(hits[0].inst == 1 && hits[0].committed_ray_t == 6.0f);
+        // errors surface as exceptions with the library's status code
+        bool threw = false;
+        try {
+            lcx::Accel empty{ext};
+            stream << empty.build();
+        } catch (const lcx::Error &e) {
+            threw = e.code() == LCX_ERR_INVALID_ARG;
+        }
+        REQUIRE(threw);
+        REQUIRE(lcx_check_trace_errors() == LCX_OK);
+        cudaFree(dv);
+        cudaFree(dt);
+        cudaFree(dr);
+        cudaFree(dh);
+        cudaFree(docc);
+    } catch (const std::exception &e) {
+        std::fprintf(stderr, "exception: %s\n", e.what());
+        return 1;
+    }
+    std::puts("accel_ext ok");
+    return 0;
+}
