@@ -232,6 +232,22 @@ LCX_API int lcx_trace_closest_counts(uint64_t accel, const LcxRay *d_rays, uint3
                              uint32_t mask, LcxTriangleHit *d_hits, uint32_t *d_counts,
                              uint32_t node_layout, void *stream);
 
+/* trace_closest that allocates nothing, for callers that cannot allocate
+ * device memory (an application that reserves its HBM at start-up and forbids
+ * later allocations, a plugin whose host framework owns every device
+ * allocation, a latency-bound loop that must not hit cudaMalloc's implicit
+ * device synchronisation).  No counterpart in the reference.  Same results as
+ * lcx_trace_closest (8-bit quantised nodes); the caller passes the built
+ * accel, the rays and the hit buffer.  Its scratch is a 256-byte static
+ * device array held by every GPU that loads the library until exit; the first
+ * call on a device looks up that array's device address, so make that first
+ * call before any stream capture.  All calls share the array (it is cleared at
+ * the start of each call): calls that overlap on the GPU race and must be
+ * ordered by the caller.  ray_count <= 2^31; larger counts return
+ * LCX_ERR_INVALID_ARG. */
+LCX_API int lcx_trace_closest_noalloc(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask,
+                                      LcxTriangleHit *d_hits, void *stream);
+
 /* Synchronises the current device and reports whether any trace call since
  * the last check hit a kernel-side bound: LCX_ERR_TIMEOUT when a ray exceeded
  * the per-ray step bound (only a corrupt BVH can cause it), LCX_ERR_DEPTH when

@@ -64,6 +64,7 @@ _SIGS = {
                                          c_void_p]),
     "lcx_set_trace_tuning": (c_int, [c_uint32, c_uint32]),
     "lcx_check_trace_errors": (c_int, []),
+    "lcx_trace_closest_noalloc": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p]),
     "lcx_get_trace_tuning": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),
 }
 

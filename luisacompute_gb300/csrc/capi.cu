@@ -195,6 +195,51 @@ TraceTuning g_tune;
 
 }  // namespace
 
+namespace lcx {
+
+// Validates a trace_closest call and fills everything of TraceParams except
+// `pool`, without touching device memory (no per-device state is created).
+int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
+                     uint32_t max_rays, TraceParams &p) {
+    auto a = find_accel(accel);
+    if (!a) return fail(LCX_ERR_INVALID_ARG, "unknown accel handle %llu", (unsigned long long)accel);
+    if (ray_count > max_rays)
+        return fail(LCX_ERR_INVALID_ARG, "ray_count %u exceeds the maximum of %u for this entry point", ray_count,
+                    max_rays);
+    if (ray_count && (!d_rays || !d_hits)) return fail(LCX_ERR_INVALID_ARG, "null ray or hit buffer");
+    if (reinterpret_cast<uintptr_t>(d_rays) % 16 != 0 || reinterpret_cast<uintptr_t>(d_hits) % 8 != 0)
+        return fail(LCX_ERR_INVALID_ARG, "rays must be 16-byte and hits 8-byte aligned");
+    std::lock_guard<std::mutex> lk(a->mtx);
+    if (!a->built) return fail(LCX_ERR_NOT_BUILT, "accel not built");
+    for (const auto &mg : a->mesh_gens) {
+        auto m = find_mesh(mg.first);
+        if (!m) return fail(LCX_ERR_NOT_BUILT, "mesh %llu was destroyed; rebuild the accel", (unsigned long long)mg.first);
+        if (m->generation != mg.second)
+            return fail(LCX_ERR_NOT_BUILT, "mesh %llu was rebuilt after the accel build; rebuild the accel",
+                        (unsigned long long)mg.first);
+    }
+    const uint32_t depth_need = a->depth + a->max_blas_depth + 2;
+    if (int(depth_need) > kStackSize)
+        return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the traversal stack (%d)", a->depth,
+                    a->max_blas_depth, kStackSize);
+    p = TraceParams{};
+    p.tlas_q = a->qn;
+    p.tlas_f = a->fn;
+    p.insts = a->recs;
+    p.rays = reinterpret_cast<const Ray *>(d_rays);
+    p.hits = reinterpret_cast<Hit *>(d_hits);
+    p.ray_count = ray_count;
+    p.mask = mask & 0xffu;
+    p.refill = g_tune.refill;
+    p.postpone = g_tune.postpone;
+    p.postpone_sp = kStackSize - int(depth_need);
+    return LCX_OK;
+}
+
+int record_error(int code, const char *msg) { return fail(code, "%s", msg); }
+
+}  // namespace lcx
+
 extern "C" {
 
 uint32_t lcx_version(void) { return 0x000100u; }

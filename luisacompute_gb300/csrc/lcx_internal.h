@@ -100,6 +100,12 @@ struct TraceParams {
     int32_t postpone_sp;  // postpone only while the stack depth is below this
 };
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st);
+
+// Validation + parameters of a trace_closest call with no device allocation
+// (defined in capi.cu; `pool` is left for the caller to set).
+int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
+                     uint32_t max_rays, TraceParams &p);
+int record_error(int code, const char *msg);
 int trace_grid_blocks(int layout, bool any, bool counting);
 
 }  // namespace lcx
