@@ -42,8 +42,8 @@ WORKLOAD = ("terrain 1024x1024 heightfield (2,093,058 tris) + 256 instances of a
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--rays", type=int, default=RAYS)
     ap.add_argument("--layout", type=int, default=1, help="0 = FP32 nodes, 1 = 8-bit quantised nodes")

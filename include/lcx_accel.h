@@ -257,11 +257,13 @@ LCX_API int lcx_check_trace_errors(void);
 
 /* Traversal knobs, process-wide (no counterpart in the reference: OptiX and
  * Embree pick theirs internally).  refill: a warp takes new rays once at
- * least this many of its 32 lanes are idle (1..32, default 8).  postpone: a
+ * least this many of its 32 lanes are idle (1..32, default 4).  postpone: a
  * lane defers its triangle tests while fewer than this many lanes would run
- * them (0 = never, default 8).  Results do not depend on either. */
-LCX_API int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone);
-LCX_API int lcx_get_trace_tuning(uint32_t *refill, uint32_t *postpone);
+ * them (0 = never, the default).  mode: loop structure, 0 = each step visits
+ * one node and tests its triangles (default), 1 = speculative while-while.
+ * Results do not depend on any of them. */
+LCX_API int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone, uint32_t mode);
+LCX_API int lcx_get_trace_tuning(uint32_t *refill, uint32_t *postpone, uint32_t *mode);
 
 #ifdef __cplusplus
 }

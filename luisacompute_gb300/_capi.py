@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import ctypes
+import os
 import re
 from ctypes import POINTER, c_char_p, c_double, c_int, c_size_t, c_uint8, c_uint32, c_uint64, c_void_p
 from pathlib import Path
@@ -62,10 +63,10 @@ _SIGS = {
     "lcx_trace_any_ex": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
     "lcx_trace_closest_counts": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_uint32,
                                          c_void_p]),
-    "lcx_set_trace_tuning": (c_int, [c_uint32, c_uint32]),
+    "lcx_set_trace_tuning": (c_int, [c_uint32, c_uint32, c_uint32]),
     "lcx_check_trace_errors": (c_int, []),
     "lcx_trace_closest_noalloc": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p]),
-    "lcx_get_trace_tuning": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),
+    "lcx_get_trace_tuning": (c_int, [POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
 }
 
 
@@ -90,7 +91,7 @@ def load(path: Path | None = None) -> ctypes.CDLL:
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = Path(path) if path else LIB_PATH
+    p = Path(path) if path else Path(os.environ.get("LCX_ACCEL_LIB", LIB_PATH))
     if not p.exists():
         raise RuntimeError(f"{p} is missing: build it with luisacompute_gb300.build.build() "
                            "(the GB300 kernels are the only implementation of this path)")

@@ -408,7 +408,7 @@ __global__ void k_collapse(TreeView tv, uint32_t n, int leaf_max, uint32_t *desc
 
 // ---- emit
 __device__ __forceinline__ uint32_t quant_exp(float lo, float hi) {
-    const float x = __fdiv_ru(__fsub_ru(hi, lo), 255.0f);
+    const float x = __fdiv_ru(__fsub_ru(hi, lo), kQuantRange);
     const uint32_t bits = __float_as_uint(x);
     uint32_t b = bits >> 23;
     if (b == 0) return 1u;  // zero or subnormal extent: 2^-126
@@ -426,11 +426,14 @@ __device__ void emit_node(const TreeView &tv, const uint32_t *desc, uint32_t w, 
     root_lo = nl;
     root_hi = nh;
     const bool node_empty = box_empty(nl, nh);
-    const float p[3] = {node_empty ? 0.0f : nl.x, node_empty ? 0.0f : nl.y, node_empty ? 0.0f : nl.z};
     uint32_t ex[3];
     ex[0] = node_empty ? 127u : quant_exp(nl.x, nh.x);
     ex[1] = node_empty ? 127u : quant_exp(nl.y, nh.y);
     ex[2] = node_empty ? 127u : quant_exp(nl.z, nh.z);
+    // quantisation origin one step below the node box (rounded down)
+    const float p[3] = {node_empty ? 0.0f : __fsub_rd(nl.x, __uint_as_float(ex[0] << 23)),
+                        node_empty ? 0.0f : __fsub_rd(nl.y, __uint_as_float(ex[1] << 23)),
+                        node_empty ? 0.0f : __fsub_rd(nl.z, __uint_as_float(ex[2] << 23))};
     Node8Q q;
     Node8F f;
     q.px = p[0];
@@ -450,9 +453,9 @@ __device__ void emit_node(const TreeView &tv, const uint32_t *desc, uint32_t w, 
             const uint32_t cnt = tv.count(c);
             if (!tv.leaf(c) && cnt > uint32_t(leaf_max)) {
                 imask |= 1u << s;
-                meta = kMetaInternal;
+                meta = kMetaInternalBase + uint32_t(s);
             } else {
-                meta = empty ? 0u : ((cnt << 5) | offset);
+                meta = empty ? 0u : meta_leaf(cnt, offset);
                 const uint32_t first = tv.first(c);
                 for (uint32_t j = 0; j < cnt; j++) write_item(item_base + offset + j, tv.vals[first + j]);
                 offset += cnt;
@@ -467,9 +470,10 @@ __device__ void emit_node(const TreeView &tv, const uint32_t *desc, uint32_t w, 
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
                     const float e = __uint_as_float(ex[k] << 23);
-                    float a = floorf(__fdiv_rd(__fsub_rd(cl[k], p[k]), e));
-                    float z = ceilf(__fdiv_ru(__fsub_ru(ch[k], p[k]), e));
-                    if (!(a >= 0.0f) || !(z <= 255.0f)) atomicOr(&ctl[kCtlErr], kErrQuant);
+                    // exact outward bounds, then one more step outward on each side
+                    float a = floorf(__fdiv_rd(__fsub_rd(cl[k], p[k]), e)) - 1.0f;
+                    float z = ceilf(__fdiv_ru(__fsub_ru(ch[k], p[k]), e)) + 1.0f;
+                    if (!(a >= -1.0f) || !(z <= 255.0f)) atomicOr(&ctl[kCtlErr], kErrQuant);
                     ql[k] = uint32_t(fminf(fmaxf(a, 0.0f), 255.0f));
                     qh[k] = uint32_t(fminf(fmaxf(z, 0.0f), 255.0f));
                 }
@@ -624,8 +628,8 @@ __global__ void k_wide_sah(const Node8F *fn, uint32_t wide_count, double *out) {
             hx = fmaxf(hx, f.hi_x[s]);
             hy = fmaxf(hy, f.hi_y[s]);
             hz = fmaxf(hz, f.hi_z[s]);
-            if (!(meta & kMetaInternal))
-                acc += double(meta >> 5) * area(f.lo_x[s], f.lo_y[s], f.lo_z[s], f.hi_x[s], f.hi_y[s], f.hi_z[s]);
+            if (!meta_internal(meta))
+                acc += double(meta_count(meta)) * area(f.lo_x[s], f.lo_y[s], f.lo_z[s], f.hi_x[s], f.hi_y[s], f.hi_z[s]);
         }
         const double a = area(lx, ly, lz, hx, hy, hz);
         acc += a;

@@ -190,6 +190,7 @@ int leaf_items_for(const LcxAccelOption &o) { return o.hint == LCX_HINT_FAST_BUI
 struct TraceTuning {
     uint32_t refill = 4;    // measured best on the terrain workload (refill sweep 1..32)
     uint32_t postpone = 0;  // postponing did not pay on GB300 (sweep 0..12)
+    uint32_t mode = 0;      // traversal loop structure
 };
 TraceTuning g_tune;
 
@@ -218,7 +219,7 @@ int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, u
             return fail(LCX_ERR_NOT_BUILT, "mesh %llu was rebuilt after the accel build; rebuild the accel",
                         (unsigned long long)mg.first);
     }
-    const uint32_t depth_need = a->depth + a->max_blas_depth + 2;
+    const uint32_t depth_need = a->depth + a->max_blas_depth + 3;
     if (int(depth_need) > kStackSize)
         return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the traversal stack (%d)", a->depth,
                     a->max_blas_depth, kStackSize);
@@ -232,6 +233,7 @@ int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, u
     p.mask = mask & 0xffu;
     p.refill = g_tune.refill;
     p.postpone = g_tune.postpone;
+    p.mode = g_tune.mode;
     p.postpone_sp = kStackSize - int(depth_need);
     return LCX_OK;
 }
@@ -612,7 +614,7 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
                 return fail(LCX_ERR_NOT_BUILT, "mesh %llu was rebuilt after the accel build; rebuild the accel",
                             (unsigned long long)mg.first);
         }
-        depth_need = a->depth + a->max_blas_depth + 2;
+        depth_need = a->depth + a->max_blas_depth + 3;
         if (int(depth_need) > kStackSize)
             return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the traversal stack (%d)", a->depth,
                         a->max_blas_depth, kStackSize);
@@ -632,7 +634,8 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     p.mask = mask & 0xffu;
     p.refill = g_tune.refill;
     p.postpone = g_tune.postpone;
-    // regular pushes need at most tlas_depth + blas_depth + 2 entries; postponed
+    p.mode = g_tune.mode;
+    // regular pushes need at most tlas_depth + blas_depth + 3 entries; postponed
     // triangle groups may use what is left
     p.postpone_sp = kStackSize - int(depth_need);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -658,18 +661,20 @@ int lcx_check_trace_errors(void) {
     return LCX_OK;
 }
 
-int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone) {
-    if (refill < 1 || refill > 32 || postpone > 32)
-        return fail(LCX_ERR_INVALID_ARG, "tuning out of range (refill 1..32, postpone 0..32)");
+int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone, uint32_t mode) {
+    if (refill < 1 || refill > 32 || postpone > 32 || mode > 1)
+        return fail(LCX_ERR_INVALID_ARG, "tuning out of range (refill 1..32, postpone 0..32, mode 0..1)");
     g_tune.refill = refill;
     g_tune.postpone = postpone;
+    g_tune.mode = mode;
     return LCX_OK;
 }
 
-int lcx_get_trace_tuning(uint32_t *refill, uint32_t *postpone) {
-    if (!refill || !postpone) return fail(LCX_ERR_INVALID_ARG, "null output");
+int lcx_get_trace_tuning(uint32_t *refill, uint32_t *postpone, uint32_t *mode) {
+    if (!refill || !postpone || !mode) return fail(LCX_ERR_INVALID_ARG, "null output");
     *refill = g_tune.refill;
     *postpone = g_tune.postpone;
+    *mode = g_tune.mode;
     return LCX_OK;
 }
 

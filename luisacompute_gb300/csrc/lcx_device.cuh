@@ -27,9 +27,21 @@ constexpr int kMaxLeafItems = 3;    // items per leaf slot (meta holds a 2-bit c
 constexpr int kStackSize = 32;      // traversal stack entries per thread
 constexpr int kMaxLevels = 64;      // wide-tree depth limit of the collapse
 
-// Meta byte of a child slot:  0 = empty/unreachable;  0x80 = internal node;
-// otherwise leaf with count = meta >> 5 (1..3) items at item_base + (meta & 31).
-constexpr uint8_t kMetaInternal = 0x80;
+// Meta byte of a child slot: (bits << 5) | index.  A hit child contributes
+// `bits << index` to a 32-bit hit word: internal children have bits = 1 and
+// index 24 + slot (so their hits land in bits 24..31, reordered front to back
+// by XOR with the ray's octant), leaves have bits = 2^count - 1 (count 1..3)
+// and index = offset of their items (0..23).  0 = empty or unreachable.
+constexpr uint32_t kMetaInternalBase = 0x38;  // (1 << 5) | 24
+__host__ __device__ __forceinline__ bool meta_internal(uint32_t m) { return m != 0u && (m & 0x18u) == 0x18u; }
+__host__ __device__ __forceinline__ uint32_t meta_leaf(uint32_t count, uint32_t offset) {
+    return (((1u << count) - 1u) << 5) | offset;
+}
+__device__ __forceinline__ uint32_t meta_count(uint32_t m) { return __popc(m >> 5); }
+// Quantised boxes: exponents give (hi - lo) / e <= kQuantRange and the stored
+// origin is one step below the node box, so every stored plane can be moved
+// one step outward; the traversal's folded decode is then conservative.
+constexpr float kQuantRange = 252.0f;
 
 struct __align__(16) Node8Q {
     float px, py, pz;   // quantisation origin (node box lower corner)

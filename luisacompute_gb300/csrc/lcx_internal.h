@@ -98,6 +98,7 @@ struct TraceParams {
     uint32_t refill;      // refill a warp when at least this many lanes are idle (1..32)
     uint32_t postpone;    // postpone triangle tests when fewer lanes than this would run them (0 = off)
     int32_t postpone_sp;  // postpone only while the stack depth is below this
+    uint32_t mode;        // loop structure: 0 = node + its items per step, 1 = speculative while-while
 };
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st);
 
@@ -106,6 +107,5 @@ cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counti
 int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
                      uint32_t max_rays, TraceParams &p);
 int record_error(int code, const char *msg);
-int trace_grid_blocks(int layout, bool any, bool counting);
 
 }  // namespace lcx

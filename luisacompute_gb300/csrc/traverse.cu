@@ -13,7 +13,8 @@
 //   * node groups: a visited node yields the hit mask of its internal
 //     children (bits ordered front to back by the ray octant) and the hit
 //     mask of its leaf items; a group with hits left is pushed on a per-thread
-//     stack in shared memory (kStackSize x 8 B per thread);
+//     short stack: the top kShortStack entries (8 B each) per thread in shared
+//     memory, deeper ones in local memory;
 //   * two levels: a TLAS leaf item is an instance; the ray is moved to object
 //     space with the exact FP32 sequence of lcx_device.cuh and the same loop
 //     runs over the BLAS; when the stack unwinds to the entry depth the world
@@ -28,6 +29,20 @@ namespace lcx {
 namespace {
 
 constexpr int kTraceBlock = 128;
+// Resident 128-thread blocks per SM the register budget is cut for (measured
+// on GB300, terrain workload: quantised nodes peak at 7, FP32 nodes at 6).
+#ifndef LCX_TRACE_MIN_BLOCKS_Q
+#define LCX_TRACE_MIN_BLOCKS_Q 7
+#endif
+#ifndef LCX_TRACE_MIN_BLOCKS_F
+#define LCX_TRACE_MIN_BLOCKS_F 6
+#endif
+#ifndef LCX_SHORT_STACK
+#define LCX_SHORT_STACK 16  // stack entries kept in shared memory; deeper ones go to local memory
+#endif
+constexpr int kShortStack = LCX_SHORT_STACK < kStackSize ? LCX_SHORT_STACK : kStackSize;
+constexpr int kDeep = kStackSize - kShortStack;    // entries in local memory
+constexpr int kDeepSlots = kDeep > 0 ? kDeep : 1;  // array size (1 when unused)
 constexpr uint32_t kMaxRaySteps = 1u << 22;  // per-ray bound: a corrupt tree ends the ray, never hangs
 
 __device__ __forceinline__ uint2 root_group(uint32_t octinv) {
@@ -39,57 +54,62 @@ __device__ __forceinline__ uint32_t octant_inv(float dx, float dy, float dz) {
     return ((dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u)) ^ 7u;
 }
 
-__device__ __forceinline__ float byte_to_float(uint32_t w, uint32_t k) {
-    // byte k of w as an exact float: 0x4B0000bb - 2^23
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | k)) - 8388608.0f;
+// byte k of w as the float 2^23 + byte (exact): one PRMT
+__device__ __forceinline__ float byte_magic(uint32_t w, uint32_t k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | k));
 }
 
+// Hit word contribution of a slot: (bits << index), index of internal slots
+// reordered by the ray octant.
+__device__ __forceinline__ uint32_t slot_bits(uint32_t meta, uint32_t octinv) {
+    uint32_t idx = meta & 31u;
+    idx ^= ((meta & 0x18u) == 0x18u) ? octinv : 0u;
+    return (meta >> 5) << idx;
+}
+
+// Quantised node: planes are p + e*q; with M = 2^23 + q (one PRMT) the
+// decode t = (p - o)/d + q*e/d becomes fma(M, e/d, (p - o)/d - 2^23 e/d).
+// The folded constant loses up to half a step, which the build-side one-step
+// outward dilation absorbs; the 2^-20 widening of (p - o)/d covers its own
+// rounding (and 1/d ~ 1e30 when d ~ 0).
 __device__ __forceinline__ void intersect_q(const Node8Q *nodes, uint32_t idx, float ox, float oy, float oz,
                                             float ix, float iy, float iz, uint32_t octinv, float tmin, float tmax,
                                             uint2 &G, uint2 &Gt) {
     const uint4 *p = reinterpret_cast<const uint4 *>(nodes + idx);
     const uint4 n0 = __ldg(p), n1 = __ldg(p + 1), n2 = __ldg(p + 2), n3 = __ldg(p + 3), n4 = __ldg(p + 4);
-    const float sx = __uint_as_float((n0.w & 0xffu) << 23);
-    const float sy = __uint_as_float(((n0.w >> 8) & 0xffu) << 23);
-    const float sz = __uint_as_float(((n0.w >> 16) & 0xffu) << 23);
-    const float adx = sx * ix, ady = sy * iy, adz = sz * iz;
-    // plane offset (p - o) / d, widened by 2^-20 of itself on each side: its two
-    // roundings can flip the sign of a face the ray lies in when d ~ 0 (1/d ~ 1e30)
+    const float adx = __uint_as_float((n0.w & 0xffu) << 23) * ix;
+    const float ady = __uint_as_float(((n0.w >> 8) & 0xffu) << 23) * iy;
+    const float adz = __uint_as_float(((n0.w >> 16) & 0xffu) << 23) * iz;
     const float aox = (__uint_as_float(n0.x) - ox) * ix;
     const float aoy = (__uint_as_float(n0.y) - oy) * iy;
     const float aoz = (__uint_as_float(n0.z) - oz) * iz;
+    const float fx = __fmaf_rn(-8388608.0f, adx, aox), fy = __fmaf_rn(-8388608.0f, ady, aoy),
+                fz = __fmaf_rn(-8388608.0f, adz, aoz);
     const float slx = fabsf(aox) * 0x1p-20f, sly = fabsf(aoy) * 0x1p-20f, slz = fabsf(aoz) * 0x1p-20f;
-    const float aoxn = aox - slx, aoxf = aox + slx;
-    const float aoyn = aoy - sly, aoyf = aoy + sly;
-    const float aozn = aoz - slz, aozf = aoz + slz;
+    const float cxn = fx - slx, cxf = fx + slx, cyn = fy - sly, cyf = fy + sly, czn = fz - slz, czf = fz + slz;
     // near/far planes by ray direction sign (swap whole byte words)
     const bool nx = ix < 0.0f, ny = iy < 0.0f, nz = iz < 0.0f;
     const uint32_t nx0 = nx ? n3.z : n2.x, nx1 = nx ? n3.w : n2.y, fx0 = nx ? n2.x : n3.z, fx1 = nx ? n2.y : n3.w;
     const uint32_t ny0 = ny ? n4.x : n2.z, ny1 = ny ? n4.y : n2.w, fy0 = ny ? n2.z : n4.x, fy1 = ny ? n2.w : n4.y;
     const uint32_t nz0 = nz ? n4.z : n3.x, nz1 = nz ? n4.w : n3.y, fz0 = nz ? n3.x : n4.z, fz1 = nz ? n3.y : n4.w;
-    uint32_t hits = 0, items = 0;
+    uint32_t bits = 0;
 #pragma unroll
     for (int s = 0; s < 8; s++) {
         const uint32_t k = s & 3;
         const bool hw = s >= 4;
-        const float tnx = __fmaf_rn(byte_to_float(hw ? nx1 : nx0, k), adx, aoxn);
-        const float tfx = __fmaf_rn(byte_to_float(hw ? fx1 : fx0, k), adx, aoxf);
-        const float tny = __fmaf_rn(byte_to_float(hw ? ny1 : ny0, k), ady, aoyn);
-        const float tfy = __fmaf_rn(byte_to_float(hw ? fy1 : fy0, k), ady, aoyf);
-        const float tnz = __fmaf_rn(byte_to_float(hw ? nz1 : nz0, k), adz, aozn);
-        const float tfz = __fmaf_rn(byte_to_float(hw ? fz1 : fz0, k), adz, aozf);
+        const float tnx = __fmaf_rn(byte_magic(hw ? nx1 : nx0, k), adx, cxn);
+        const float tfx = __fmaf_rn(byte_magic(hw ? fx1 : fx0, k), adx, cxf);
+        const float tny = __fmaf_rn(byte_magic(hw ? ny1 : ny0, k), ady, cyn);
+        const float tfy = __fmaf_rn(byte_magic(hw ? fy1 : fy0, k), ady, cyf);
+        const float tnz = __fmaf_rn(byte_magic(hw ? nz1 : nz0, k), adz, czn);
+        const float tfz = __fmaf_rn(byte_magic(hw ? fz1 : fz0, k), adz, czf);
         const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
         const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
         const uint32_t meta = ((hw ? n1.w : n1.z) >> (8 * k)) & 0xffu;
-        if (meta != 0u && slab_accept(tn, tf)) {
-            if (meta & kMetaInternal)
-                hits |= 1u << (s ^ octinv);
-            else
-                items |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
-        }
+        if (slab_accept(tn, tf)) bits |= slot_bits(meta, octinv);
     }
-    G = make_uint2(n1.x, hits ? ((hits << 24) | (n0.w >> 24)) : 0u);
-    Gt = make_uint2(n1.y, items);
+    G = make_uint2(n1.x, (bits >> 24) ? ((bits & 0xff000000u) | (n0.w >> 24)) : 0u);
+    Gt = make_uint2(n1.y, bits & 0x00ffffffu);
 }
 
 __device__ __forceinline__ void intersect_f(const Node8F *nodes, uint32_t idx, float ox, float oy, float oz,
@@ -99,7 +119,7 @@ __device__ __forceinline__ void intersect_f(const Node8F *nodes, uint32_t idx, f
     const uint4 hdr = __ldg(reinterpret_cast<const uint4 *>(p + 12));
     const bool nx = ix < 0.0f, ny = iy < 0.0f, nz = iz < 0.0f;
     // lo_x: p[0..1], hi_x: p[2..3], lo_y: p[4..5], hi_y: p[6..7], lo_z: p[8..9], hi_z: p[10..11]
-    uint32_t hits = 0, items = 0, imask = 0;
+    uint32_t bits = 0, imask = 0;
 #pragma unroll
     for (int half = 0; half < 2; half++) {
         const float4 lx = __ldg(p + 0 + half), hx = __ldg(p + 2 + half);
@@ -118,32 +138,20 @@ __device__ __forceinline__ void intersect_f(const Node8F *nodes, uint32_t idx, f
             const float tn = fmaxf(fmaxf(tnx * ix, tny * iy), fmaxf(tnz * iz, tmin));
             const float tf = fminf(fminf(tfx * ix, tfy * iy), fminf(tfz * iz, tmax));
             const uint32_t meta = (mw >> (8 * k)) & 0xffu;
-            if (meta & kMetaInternal) imask |= 1u << s;
-            if (meta != 0u && slab_accept(tn, tf)) {
-                if (meta & kMetaInternal)
-                    hits |= 1u << (s ^ octinv);
-                else
-                    items |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
-            }
+            if (meta_internal(meta)) imask |= 1u << s;
+            if (slab_accept(tn, tf)) bits |= slot_bits(meta, octinv);
         }
     }
-    G = make_uint2(hdr.x, hits ? ((hits << 24) | imask) : 0u);
-    Gt = make_uint2(hdr.y, items);
+    G = make_uint2(hdr.x, (bits >> 24) ? ((bits & 0xff000000u) | imask) : 0u);
+    Gt = make_uint2(hdr.y, bits & 0x00ffffffu);
 }
 
+// Per-lane traversal state and the operations both loop structures share.
 template <int kLayout, bool kAny, bool kCount>
-__global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
-    __shared__ uint2 stack_mem[kStackSize * kTraceBlock];
-    uint2 *const stk = stack_mem + threadIdx.x;
-    const uint32_t lane = threadIdx.x & 31u;
-    const void *const tlas_nodes = kLayout == LCX_NODES_QUANT8 ? static_cast<const void *>(P.tlas_q)
-                                                                : static_cast<const void *>(P.tlas_f);
-    const int refill = int(P.refill);
-    const int postpone = int(P.postpone);
-    const int postpone_sp = P.postpone_sp;
-
-    bool active = false, exhausted = false;
-    uint32_t rid = 0;
+struct Walker {
+    const TraceParams &P;
+    uint2 *stk;
+    const void *tlas_nodes;
     // world ray
     float wox = 0, woy = 0, woz = 0, wdx = 0, wdy = 0, wdz = 1;
     float tmin = 0, best_t = 0, best_u = 0, best_v = 0;
@@ -159,19 +167,197 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
     const void *blas_nodes = nullptr;
     const TriRec *blas_tris = nullptr;
     uint32_t c_nodes = 0, c_tris = 0, c_insts = 0;
-    uint32_t ray_steps = 0;
 
-    auto push = [&](uint2 v) {
-        if (sp < kStackSize) {
-            stk[sp * kTraceBlock] = v;
+    __device__ Walker(const TraceParams &p, uint2 *s, uint2 *d)
+        : P(p), stk(s), deep(d),
+          tlas_nodes(kLayout == LCX_NODES_QUANT8 ? static_cast<const void *>(p.tlas_q)
+                                                 : static_cast<const void *>(p.tlas_f)) {}
+
+    uint2 *deep;  // local-memory overflow (an array of the kernel, not of this struct,
+                  // so that the struct itself stays in registers)
+
+    // Every index below is clamped into its array as well as branched on, so a
+    // load the compiler hoists out of the untaken branch stays in bounds.
+    __device__ __forceinline__ void push(uint2 v) {
+        if (sp < kShortStack) {
+            stk[min(sp, kShortStack - 1) * kTraceBlock] = v;
+            sp++;
+        } else if (kDeep > 0 && sp < kStackSize) {
+            deep[min(max(sp - kShortStack, 0), kDeepSlots - 1)] = v;
             sp++;
         } else {
             atomicOr(P.pool + 1, 1u);  // cannot happen within the host's depth check
         }
-    };
+    }
+    __device__ __forceinline__ uint2 pop() {
+        sp--;
+        if (kDeep == 0 || sp < kShortStack) return stk[min(max(sp, 0), kShortStack - 1) * kTraceBlock];
+        return deep[min(max(sp - kShortStack, 0), kDeepSlots - 1)];
+    }
+
+    __device__ __forceinline__ void start(uint32_t rid) {
+        const float4 *rp = reinterpret_cast<const float4 *>(P.rays + rid);
+        const float4 r0 = __ldcs(rp), r1 = __ldcs(rp + 1);
+        wox = r0.x;
+        woy = r0.y;
+        woz = r0.z;
+        tmin = r0.w;
+        wdx = r1.x;
+        wdy = r1.y;
+        wdz = r1.z;
+        best_t = r1.w;
+        best_u = best_v = 0.0f;
+        best_inst = best_prim = kInvalid;
+        to_world();
+        // a zero direction meets nothing; skip the walk
+        G = (wdx == 0.0f && wdy == 0.0f && wdz == 0.0f) ? make_uint2(0, 0) : root_group(octinv);
+        sp = 0;
+        in_blas = false;
+        occluded = false;
+        if (kCount) c_nodes = c_tris = c_insts = 0;
+    }
+
+    __device__ __forceinline__ void to_world() {
+        ox = wox;
+        oy = woy;
+        oz = woz;
+        ix = slab_rcp(wdx);
+        iy = slab_rcp(wdy);
+        iz = slab_rcp(wdz);
+        octinv = octant_inv(wdx, wdy, wdz);
+    }
+
+    // Take the front child of node group G, push the rest, intersect it.
+    __device__ __forceinline__ void visit(uint2 &Gt) {
+        const uint32_t key = __ffs(G.y >> 24) - 1u;
+        G.y &= ~(1u << (24 + key));
+        const uint32_t slot = key ^ octinv;
+        const uint32_t child = G.x + __popc(G.y & 0xffu & ((1u << slot) - 1u));
+        if (G.y >= 0x01000000u) push(G);
+        const void *nodes = in_blas ? blas_nodes : tlas_nodes;
+        if (kLayout == LCX_NODES_QUANT8)
+            intersect_q(static_cast<const Node8Q *>(nodes), child, ox, oy, oz, ix, iy, iz, octinv, tmin, best_t, G,
+                        Gt);
+        else
+            intersect_f(static_cast<const Node8F *>(nodes), child, ox, oy, oz, ix, iy, iz, octinv, tmin, best_t, G,
+                        Gt);
+        if (kCount) c_nodes++;
+    }
+
+    // Test the triangles of Gt (inside a BLAS).  Returns true if trace_any is done.
+    __device__ __forceinline__ bool triangles(uint2 Gt) {
+        while (Gt.y) {
+            const uint32_t k = __ffs(Gt.y) - 1u;
+            Gt.y &= Gt.y - 1u;
+            const float4 *tp = reinterpret_cast<const float4 *>(blas_tris + Gt.x + k);
+            const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            if (kCount) c_tris++;
+            float t, u, v;
+            if (wt_intersect(wt, tmin, best_t, a, b, c, t, u, v)) {
+                if (kAny) {
+                    occluded = true;
+                    return true;
+                }
+                const uint32_t prim = __float_as_uint(a.w);
+                // t <= best_t here; equal t goes to the smaller (inst, prim)
+                if (t < best_t || cur_inst < best_inst || (cur_inst == best_inst && prim < best_prim)) {
+                    best_t = t;
+                    best_u = u;
+                    best_v = v;
+                    best_inst = cur_inst;
+                    best_prim = prim;
+                }
+            }
+        }
+        return false;
+    }
+
+    // Enter the first eligible instance of Gt (TLAS level); pushes the rest.
+    __device__ __forceinline__ void instances(uint2 Gt) {
+        while (Gt.y) {
+            const uint32_t k = __ffs(Gt.y) - 1u;
+            Gt.y &= Gt.y - 1u;
+            const uint4 *ip = reinterpret_cast<const uint4 *>(P.insts + Gt.x + k);
+            const uint4 m4 = __ldg(ip + 4);  // fnodes (x,y), inst_id (z), mask (w)
+            if ((m4.w & P.mask) == 0u) continue;
+            const float4 r0 = __ldg(reinterpret_cast<const float4 *>(ip));
+            const float4 r1 = __ldg(reinterpret_cast<const float4 *>(ip + 1));
+            const float4 r2 = __ldg(reinterpret_cast<const float4 *>(ip + 2));
+            const uint4 pp = __ldg(ip + 3);  // qnodes (x,y), tris (z,w)
+            if (Gt.y) push(Gt);
+            if (G.y) push(G);
+            const float w[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
+            float dx, dy, dz;
+            transform_point(w, wox, woy, woz, ox, oy, oz);
+            transform_dir(w, wdx, wdy, wdz, dx, dy, dz);
+            ix = slab_rcp(dx);
+            iy = slab_rcp(dy);
+            iz = slab_rcp(dz);
+            octinv = octant_inv(dx, dy, dz);
+            wt = wt_setup(ox, oy, oz, dx, dy, dz);
+            const unsigned long long qptr = (unsigned long long)pp.x | ((unsigned long long)pp.y << 32);
+            const unsigned long long fptr = (unsigned long long)m4.x | ((unsigned long long)m4.y << 32);
+            const unsigned long long tptr = (unsigned long long)pp.z | ((unsigned long long)pp.w << 32);
+            blas_nodes = reinterpret_cast<const void *>(kLayout == LCX_NODES_QUANT8 ? qptr : fptr);
+            blas_tris = reinterpret_cast<const TriRec *>(tptr);
+            cur_inst = m4.z;
+            in_blas = true;
+            blas_sp = sp;
+            G = root_group(octinv);
+            if (kCount) c_insts++;
+            return;
+        }
+    }
+
+    // With no node group left: leave a finished BLAS, pop, or report done.
+    __device__ __forceinline__ bool pop_or_done() {
+        if (in_blas && sp == blas_sp) {
+            in_blas = false;
+            to_world();
+        }
+        if (sp == 0) return true;
+        G = pop();
+        return false;
+    }
+
+    __device__ __forceinline__ void finish(uint32_t rid) {
+        if (kAny) {
+            P.occluded[rid] = occluded ? 1 : 0;
+        } else {
+            uint2 *hp = reinterpret_cast<uint2 *>(P.hits + rid);
+            __stcs(hp, make_uint2(best_inst, best_prim));
+            __stcs(hp + 1, make_uint2(__float_as_uint(best_u), __float_as_uint(best_v)));
+            __stcs(hp + 2, make_uint2(__float_as_uint(best_t), 0u));
+        }
+        if (kCount) {
+            P.counts[3ull * rid + 0] = c_nodes;
+            P.counts[3ull * rid + 1] = c_tris;
+            P.counts[3ull * rid + 2] = c_insts;
+        }
+    }
+};
+
+// kMode 0: each step visits one node and handles its items at once.
+// kMode 1: speculative while-while (Aila & Laine 2009): lanes walk nodes
+// together; a lane that finds items keeps walking (holding them in Gp) while
+// any lane of the warp is still searching, then all lanes handle items.
+template <int kLayout, bool kAny, bool kCount, int kMode>
+__global__ void __launch_bounds__(kTraceBlock,
+                                  kLayout == LCX_NODES_QUANT8 ? LCX_TRACE_MIN_BLOCKS_Q : LCX_TRACE_MIN_BLOCKS_F)
+    k_trace(TraceParams P) {
+    __shared__ uint2 stack_mem[kShortStack * kTraceBlock];
+    uint2 deep_stack[kDeepSlots];
+    const uint32_t lane = threadIdx.x & 31u;
+    Walker<kLayout, kAny, kCount> W(P, stack_mem + threadIdx.x, deep_stack);
+    const int refill = int(P.refill);
+    const int postpone = int(P.postpone);
+    const int postpone_sp = P.postpone_sp;
+
+    bool active = false, exhausted = false;
+    uint32_t rid = 0, ray_steps = 0;
 
     for (;;) {
-        // warp-synchronous refill: idle lanes take new rays as soon as enough of them are idle
+        // warp-synchronous refill: idle lanes take new rays once enough of them are idle
         const uint32_t idle = __ballot_sync(~0u, !active);
         const int n_idle = __popc(idle);
         if (!exhausted && n_idle >= refill) {
@@ -184,32 +370,8 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
                 if (my < P.ray_count) {
                     rid = my;
                     active = true;
-                    const float4 *rp = reinterpret_cast<const float4 *>(P.rays + rid);
-                    const float4 r0 = __ldcs(rp), r1 = __ldcs(rp + 1);
-                    wox = r0.x;
-                    woy = r0.y;
-                    woz = r0.z;
-                    tmin = r0.w;
-                    wdx = r1.x;
-                    wdy = r1.y;
-                    wdz = r1.z;
-                    best_t = r1.w;
-                    best_u = best_v = 0.0f;
-                    best_inst = best_prim = kInvalid;
-                    ox = wox;
-                    oy = woy;
-                    oz = woz;
-                    ix = slab_rcp(wdx);
-                    iy = slab_rcp(wdy);
-                    iz = slab_rcp(wdz);
-                    octinv = octant_inv(wdx, wdy, wdz);
-                    // a zero direction meets nothing; skip the walk
-                    G = (wdx == 0.0f && wdy == 0.0f && wdz == 0.0f) ? make_uint2(0, 0) : root_group(octinv);
-                    sp = 0;
-                    in_blas = false;
-                    occluded = false;
                     ray_steps = 0;
-                    if (kCount) c_nodes = c_tris = c_insts = 0;
+                    W.start(rid);
                 }
             }
         }
@@ -217,146 +379,84 @@ __global__ void __launch_bounds__(kTraceBlock, 4) k_trace(TraceParams P) {
             if (exhausted) break;
             continue;
         }
-        if (!active) continue;
 
-        // ---- one traversal step: visit one node (or take a popped item group), then its items
         bool done = false;
-        if (++ray_steps > kMaxRaySteps) {
-            atomicOr(P.pool + 1, 2u);
-            done = true;
-        } else {
-            uint2 Gt;
-            if (G.y >= 0x01000000u) {
-                const uint32_t key = __ffs(G.y >> 24) - 1u;
-                G.y &= ~(1u << (24 + key));
-                const uint32_t slot = key ^ octinv;
-                const uint32_t child = G.x + __popc(G.y & 0xffu & ((1u << slot) - 1u));
-                if (G.y >= 0x01000000u) push(G);
-                const void *nodes = in_blas ? blas_nodes : tlas_nodes;
-                if (kLayout == LCX_NODES_QUANT8)
-                    intersect_q(static_cast<const Node8Q *>(nodes), child, ox, oy, oz, ix, iy, iz, octinv, tmin,
-                                best_t, G, Gt);
-                else
-                    intersect_f(static_cast<const Node8F *>(nodes), child, ox, oy, oz, ix, iy, iz, octinv, tmin,
-                                best_t, G, Gt);
-                if (kCount) c_nodes++;
+        if (kMode == 0) {
+            if (!active) continue;
+            if (++ray_steps > kMaxRaySteps) {
+                atomicOr(P.pool + 1, 2u);
+                done = true;
             } else {
-                Gt = G;
-                G = make_uint2(0, 0);
-            }
-
-            if (in_blas) {
-                while (Gt.y) {
-                    // postpone the triangles of a lane that would test them nearly alone,
-                    // while it still has nodes to walk in the meantime
-                    if (postpone > 0 && G.y >= 0x01000000u && sp < postpone_sp &&
-                        int(__popc(__activemask())) < postpone) {
-                        push(Gt);
-                        break;
-                    }
-                    const uint32_t k = __ffs(Gt.y) - 1u;
-                    Gt.y &= Gt.y - 1u;
-                    const float4 *tp = reinterpret_cast<const float4 *>(blas_tris + Gt.x + k);
-                    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                    if (kCount) c_tris++;
-                    float t, u, v;
-                    if (wt_intersect(wt, tmin, best_t, a, b, c, t, u, v)) {
-                        if (kAny) {
-                            occluded = true;
-                            break;
-                        }
-                        const uint32_t prim = __float_as_uint(a.w);
-                        // t <= best_t here; equal t goes to the smaller (inst, prim)
-                        if (t < best_t || cur_inst < best_inst || (cur_inst == best_inst && prim < best_prim)) {
-                            best_t = t;
-                            best_u = u;
-                            best_v = v;
-                            best_inst = cur_inst;
-                            best_prim = prim;
-                        }
-                    }
-                }
-                if (kAny && occluded) done = true;
-            } else {
-                while (Gt.y) {
-                    const uint32_t k = __ffs(Gt.y) - 1u;
-                    Gt.y &= Gt.y - 1u;
-                    const uint4 *ip = reinterpret_cast<const uint4 *>(P.insts + Gt.x + k);
-                    const uint4 m4 = __ldg(ip + 4);  // fnodes (x,y), inst_id (z), mask (w)
-                    if ((m4.w & P.mask) == 0u) continue;
-                    const float4 r0 = __ldg(reinterpret_cast<const float4 *>(ip));
-                    const float4 r1 = __ldg(reinterpret_cast<const float4 *>(ip + 1));
-                    const float4 r2 = __ldg(reinterpret_cast<const float4 *>(ip + 2));
-                    const uint4 pp = __ldg(ip + 3);  // qnodes (x,y), tris (z,w)
-                    if (Gt.y) push(Gt);
-                    if (G.y) push(G);
-                    const float w[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
-                    float dx, dy, dz;
-                    transform_point(w, wox, woy, woz, ox, oy, oz);
-                    transform_dir(w, wdx, wdy, wdz, dx, dy, dz);
-                    ix = slab_rcp(dx);
-                    iy = slab_rcp(dy);
-                    iz = slab_rcp(dz);
-                    octinv = octant_inv(dx, dy, dz);
-                    wt = wt_setup(ox, oy, oz, dx, dy, dz);
-                    const unsigned long long qptr = (unsigned long long)pp.x | ((unsigned long long)pp.y << 32);
-                    const unsigned long long fptr = (unsigned long long)m4.x | ((unsigned long long)m4.y << 32);
-                    const unsigned long long tptr = (unsigned long long)pp.z | ((unsigned long long)pp.w << 32);
-                    blas_nodes = reinterpret_cast<const void *>(kLayout == LCX_NODES_QUANT8 ? qptr : fptr);
-                    blas_tris = reinterpret_cast<const TriRec *>(tptr);
-                    cur_inst = m4.z;
-                    in_blas = true;
-                    blas_sp = sp;
-                    G = root_group(octinv);
-                    if (kCount) c_insts++;
-                    break;
-                }
-            }
-
-            if (!done && G.y == 0u) {
-                if (in_blas && sp == blas_sp) {
-                    in_blas = false;
-                    ox = wox;
-                    oy = woy;
-                    oz = woz;
-                    ix = slab_rcp(wdx);
-                    iy = slab_rcp(wdy);
-                    iz = slab_rcp(wdz);
-                    octinv = octant_inv(wdx, wdy, wdz);
-                }
-                if (sp == 0) {
-                    done = true;
+                uint2 Gt;
+                if (W.G.y >= 0x01000000u) {
+                    W.visit(Gt);
                 } else {
-                    sp--;
-                    G = stk[sp * kTraceBlock];
+                    Gt = W.G;
+                    W.G = make_uint2(0, 0);
+                }
+                if (W.in_blas) {
+                    if (postpone > 0 && Gt.y && W.G.y >= 0x01000000u && W.sp < postpone_sp &&
+                        int(__popc(__activemask())) < postpone) {
+                        W.push(Gt);  // postpone: a lane nearly alone walks on
+                    } else if (W.triangles(Gt)) {
+                        done = true;
+                    }
+                } else {
+                    W.instances(Gt);
+                }
+                if (!done && W.G.y == 0u) done = W.pop_or_done();
+            }
+        } else {
+            // phase A: walk nodes together, postponing found item groups while others search
+            uint2 Gt = make_uint2(0, 0), Gp = make_uint2(0, 0);
+            if (active && W.G.y < 0x01000000u) {  // a popped item group
+                Gt = W.G;
+                W.G = make_uint2(0, 0);
+            }
+            for (;;) {
+                const bool has_node = active && W.G.y >= 0x01000000u;
+                const bool searching = has_node && Gt.y == 0u;
+                if (!__any_sync(~0u, searching)) break;
+                if (has_node && (Gt.y == 0u || Gp.y == 0u)) {
+                    if (++ray_steps > kMaxRaySteps) {
+                        atomicOr(P.pool + 1, 2u);
+                        W.G = make_uint2(0, 0);
+                        Gt = Gp = make_uint2(0, 0);
+                        W.sp = 0;
+                        W.blas_sp = 0;
+                        continue;
+                    }
+                    if (Gt.y) {
+                        Gp = Gt;
+                        Gt = make_uint2(0, 0);
+                    }
+                    W.visit(Gt);
                 }
             }
+            if (!active) continue;
+            // phase B: items
+            if (W.in_blas) {
+                if (W.triangles(Gt) || W.triangles(Gp)) done = true;
+            } else {
+                if (Gp.y) W.push(Gp);  // instance groups: enter one now, the rest later
+                W.instances(Gt);
+            }
+            // phase C: pop
+            if (!done && W.G.y == 0u) done = W.pop_or_done();
         }
         if (done) {
-            if (kAny) {
-                P.occluded[rid] = occluded ? 1 : 0;
-            } else {
-                uint2 *hp = reinterpret_cast<uint2 *>(P.hits + rid);
-                __stcs(hp, make_uint2(best_inst, best_prim));
-                __stcs(hp + 1, make_uint2(__float_as_uint(best_u), __float_as_uint(best_v)));
-                __stcs(hp + 2, make_uint2(__float_as_uint(best_t), 0u));
-            }
-            if (kCount) {
-                P.counts[3ull * rid + 0] = c_nodes;
-                P.counts[3ull * rid + 1] = c_tris;
-                P.counts[3ull * rid + 2] = c_insts;
-            }
+            W.finish(rid);
             active = false;
         }
     }
 }
 
-template <int L, bool A, bool C>
+template <int L, bool A, bool C, int M>
 int blocks_per_sm() {
     static int v = 0;
     if (v == 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<L, A, C>, kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<L, A, C, M>, kTraceBlock, 0);
         v = b > 0 ? b : 1;
     }
     return v;
@@ -373,39 +473,33 @@ int sm_count() {
     return v;
 }
 
-template <int L, bool A, bool C>
+template <int L, bool A, bool C, int M>
 cudaError_t launch_one(const TraceParams &p, cudaStream_t st) {
     const uint64_t warps_needed = (uint64_t(p.ray_count) + 31) / 32;
-    uint64_t grid = uint64_t(sm_count()) * blocks_per_sm<L, A, C>();
+    uint64_t grid = uint64_t(sm_count()) * blocks_per_sm<L, A, C, M>();
     const uint64_t grid_need = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
     if (grid_need < grid) grid = grid_need;
     if (grid == 0) grid = 1;
-    k_trace<L, A, C><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
+    k_trace<L, A, C, M><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
     return cudaGetLastError();
+}
+
+template <int M>
+cudaError_t launch_mode(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
+    if (layout == LCX_NODES_QUANT8) {
+        if (any) return launch_one<LCX_NODES_QUANT8, true, false, M>(p, st);
+        if (counting) return launch_one<LCX_NODES_QUANT8, false, true, M>(p, st);
+        return launch_one<LCX_NODES_QUANT8, false, false, M>(p, st);
+    }
+    if (any) return launch_one<LCX_NODES_FP32, true, false, M>(p, st);
+    if (counting) return launch_one<LCX_NODES_FP32, false, true, M>(p, st);
+    return launch_one<LCX_NODES_FP32, false, false, M>(p, st);
 }
 
 }  // namespace
 
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
-    if (layout == LCX_NODES_QUANT8) {
-        if (any) return launch_one<LCX_NODES_QUANT8, true, false>(p, st);
-        if (counting) return launch_one<LCX_NODES_QUANT8, false, true>(p, st);
-        return launch_one<LCX_NODES_QUANT8, false, false>(p, st);
-    }
-    if (any) return launch_one<LCX_NODES_FP32, true, false>(p, st);
-    if (counting) return launch_one<LCX_NODES_FP32, false, true>(p, st);
-    return launch_one<LCX_NODES_FP32, false, false>(p, st);
-}
-
-int trace_grid_blocks(int layout, bool any, bool counting) {
-    if (layout == LCX_NODES_QUANT8) {
-        if (any) return sm_count() * blocks_per_sm<LCX_NODES_QUANT8, true, false>();
-        if (counting) return sm_count() * blocks_per_sm<LCX_NODES_QUANT8, false, true>();
-        return sm_count() * blocks_per_sm<LCX_NODES_QUANT8, false, false>();
-    }
-    if (any) return sm_count() * blocks_per_sm<LCX_NODES_FP32, true, false>();
-    if (counting) return sm_count() * blocks_per_sm<LCX_NODES_FP32, false, true>();
-    return sm_count() * blocks_per_sm<LCX_NODES_FP32, false, false>();
+    return p.mode == 1 ? launch_mode<1>(p, layout, any, counting, st) : launch_mode<0>(p, layout, any, counting, st);
 }
 
 }  // namespace lcx

@@ -30,7 +30,7 @@ int main() {
         cudaMemcpy(dt, tris, sizeof(tris), cudaMemcpyHostToDevice);
         lcx::Mesh mesh{ext, reinterpret_cast<uint64_t>(dv), 4, 16, reinterpret_cast<uint64_t>(dt), 2};
         lcx::Accel accel{ext};
-        accel.emplace_back(mesh, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0});                 // identity
+        accel.emplace_back(mesh, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0}, 0x01u);          // identity, mask 1
         accel.emplace_back(mesh, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, -2}, 0x02u, true, 7);  // z = -2, mask 2
         lcx::CommandStream stream{ext, nullptr};
         stream << mesh.build() << accel.build();

@@ -294,25 +294,25 @@ def test_axis_aligned_exact_ties(torch_cuda, lcx, oracle_mod, layout):
     assert (got["inst"][:2 * m] != S.MISS).sum() >= 2 * 15 * 15
 
 
-@pytest.mark.parametrize("refill,postpone", [(1, 0), (8, 8), (16, 12), (32, 32), (4, 20)])
-def test_tuning_does_not_change_results(torch_cuda, lcx, oracle_mod, refill, postpone):
+@pytest.mark.parametrize("refill,postpone,mode", [(1, 0, 0), (8, 8, 0), (16, 12, 0), (32, 32, 0), (4, 20, 0),
+                                                  (4, 0, 1), (16, 0, 1), (1, 8, 1)])
+def test_tuning_does_not_change_results(torch_cuda, lcx, oracle_mod, refill, postpone, mode):
+    import ctypes
     from luisacompute_gb300 import _capi
     lib = _capi.load()
     scene = small_terrain()
-    rays = S.terrain_rays(scene, 100_000, seed=13)
-    want = oracle_mod.OracleScene(scene).trace_closest(rays)
+    rays = np.concatenate([S.terrain_rays(scene, 100_000, seed=13), S.terrain_shadow_rays(scene, 50_000, seed=14)])
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_closest(rays)
+    want_any = osc.trace_any(rays)
     acc, _ = gpu_scene(scene)
-    old = (ctypes_u32(), ctypes_u32())
+    old = [ctypes.c_uint32(0) for _ in range(3)]
     _capi.check(lib.lcx_get_trace_tuning(*old), "get")
     try:
-        _capi.check(lib.lcx_set_trace_tuning(refill, postpone), "set")
+        _capi.check(lib.lcx_set_trace_tuning(refill, postpone, mode), "set")
         for layout in (0, 1):
             got = trace(acc, rays, layout)
             assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+            assert np.array_equal(trace_any(acc, rays, layout), want_any)
     finally:
-        _capi.check(lib.lcx_set_trace_tuning(old[0].value, old[1].value), "set")
-
-
-def ctypes_u32():
-    import ctypes
-    return ctypes.c_uint32(0)
+        _capi.check(lib.lcx_set_trace_tuning(old[0].value, old[1].value, old[2].value), "set")
