@@ -178,6 +178,16 @@ LCX_API int lcx_mesh_destroy(uint64_t mesh);
  * to learn the tree size. */
 LCX_API int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *command, void *stream);
 
+/* Many MeshBuildCommands at once (no single counterpart in the reference,
+ * whose backends build one Mesh per command: CPU accel.rs:205-260, CUDA
+ * cuda_mesh.cpp:31-69 with one host sync each at cuda_primitive.cpp:74).
+ * All meshes' triangles go through one sort, one LBVH pass, one cooperative
+ * collapse and one emit into one shared device block; the host synchronises
+ * once.  Results equal `count` separate lcx_mesh_build calls on the same
+ * commands.  A mesh may appear once; all or none are rebuilt. */
+LCX_API int lcx_mesh_build_batch(const uint64_t *meshes, const LcxMeshBuildCommand *commands, uint32_t count,
+                                 void *stream);
+
 LCX_API int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out);
 
 /* ------------------------------------------------------------------ accel */
@@ -254,6 +264,13 @@ LCX_API int lcx_trace_closest_noalloc(uint64_t accel, const LcxRay *d_rays, uint
  * a push found the stack full.  Clears the flags.  (No counterpart in the
  * reference, whose kernels cannot report errors.) */
 LCX_API int lcx_check_trace_errors(void);
+
+/* Build knobs, process-wide, for builds that start after the call (no
+ * counterpart in the reference).  leaf_max: triangles per leaf slot, 1..3, or
+ * 0 to follow AccelOption.hint (FAST_TRACE 2, FAST_BUILD 3); width: children
+ * per wide node, 2..8 (default 8).  Results of queries do not depend on them. */
+LCX_API int lcx_set_build_tuning(uint32_t leaf_max, uint32_t width);
+LCX_API int lcx_get_build_tuning(uint32_t *leaf_max, uint32_t *width);
 
 /* Traversal knobs, process-wide (no counterpart in the reference: OptiX and
  * Embree pick theirs internally).  refill: a warp takes new rays once at

@@ -254,6 +254,20 @@ class Accel:
             pass
 
 
+def build_meshes(meshes, request: int = REQUEST_FORCE_BUILD, stream=None):
+    """Build many meshes with one lcx_mesh_build_batch call (one sort, one LBVH pass,
+    one collapse and one emit for all of them)."""
+    lib = _capi.load()
+    n = len(meshes)
+    handles = (ctypes.c_uint64 * n)(*[m.handle for m in meshes])
+    cmds = (LcxMeshBuildCommand * n)()
+    for i, m in enumerate(meshes):
+        cmds[i] = LcxMeshBuildCommand(request, 0, m.vertices.data_ptr(), 0, m.vertex_size, m.vertex_stride,
+                                      m.triangles.data_ptr(), 0, m.triangle_size)
+    check(lib.lcx_mesh_build_batch(handles, cmds, n, stream_handle(stream)), "lcx_mesh_build_batch")
+    return meshes
+
+
 def hits_to_numpy(hits) -> np.ndarray:
     """(N, 6) int32 device tensor -> numpy TriangleHit records."""
     from .scenes import HIT_DTYPE
@@ -272,9 +286,13 @@ def mesh_from_data(md, device="cuda", option: AccelOption | None = None) -> Mesh
     return Mesh(v, t, option)
 
 
-def accel_from_scene(scene, device="cuda", option: AccelOption | None = None, stream=None):
-    """Build every mesh and one TLAS for a scenes.Scene; returns (accel, meshes)."""
-    meshes = [mesh_from_data(m, device, option).build(stream=stream) for m in scene.meshes]
+def accel_from_scene(scene, device="cuda", option: AccelOption | None = None, stream=None, batch: bool = False):
+    """Build every mesh and one TLAS for a scenes.Scene; returns (accel, meshes).
+    batch=True builds all meshes with one lcx_mesh_build_batch call."""
+    if batch:
+        meshes = build_meshes([mesh_from_data(m, device, option) for m in scene.meshes], stream=stream)
+    else:
+        meshes = [mesh_from_data(m, device, option).build(stream=stream) for m in scene.meshes]
     acc = Accel(option)
     acc.emplace_back_many([meshes[i] for i in scene.inst_mesh], scene.inst_affine, scene.inst_mask)
     acc.build(stream=stream)

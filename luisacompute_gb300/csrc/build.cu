@@ -5,20 +5,25 @@
 // accelBuild in src/backends/cuda/cuda_primitive.cpp:20-113) and TLAS
 // (AccelBuildCommand, replacing accel.rs:324-447 and the update_accel kernels
 // of src/backends/cuda/cuda_builtin/cuda_builtin_kernels.cu:42-111 plus the
-// IAS build of cuda_accel.cpp:26-126) share one pipeline over item boxes:
+// IAS build of cuda_accel.cpp:26-126) share one pipeline over *segments*: a
+// segment is one BVH's items (one mesh's triangles, or a TLAS's instances),
+// and a batch of thousands of uneven meshes is built in the same launches as
+// a single one:
 //
-//   prep    item boxes + centroid bounds            (one thread per item)
-//   morton  63-bit Morton keys of the centroids      (one thread per item)
-//   sort    key/value radix sort                     (CUB, sort.cu)
-//   lbvh    binary radix tree + boxes, bottom-up in one pass (Apetrei 2014,
-//           "Fast and Simple Agglomerative LBVH Construction")
-//   collapse  top-down, level-synchronous inside one cooperative launch:
-//           each wide node opens its largest-area children until it has 8,
-//           subtrees of <= leaf_max items become leaf slots, children are
-//           assigned to octant slots, and internal children get contiguous
-//           node indices
-//   emit    both node layouts (FP32 and outward-rounded 8-bit) and the leaf
-//           items in traversal order
+//   prep      item boxes + per-segment centroid bounds   (one thread per item)
+//   morton    key = segment id above a Morton code of the centroid
+//   sort      key/value radix sort of all items of all segments (CUB, sort.cu)
+//   lbvh      one bottom-up pass builds every segment's binary radix tree
+//             (Apetrei 2014, "Fast and Simple Agglomerative LBVH
+//             Construction"); a thread stops at its segment's root, so trees
+//             of different segments never merge
+//   collapse  one cooperative launch, level-synchronous over all segments:
+//             each wide node opens its largest-area children up to the node
+//             width, subtrees of <= leaf_max items become leaf slots, children
+//             go to octant slots and internal children get contiguous indices
+//   emit      both node layouts and the leaf items of every segment into
+//             shared pools; a segment's root is wide node s, its indices are
+//             stored relative to it, its items relative to its item offset
 #include <cooperative_groups.h>
 
 #include <cfloat>
@@ -53,76 +58,100 @@ __device__ __forceinline__ float box_area(const float4 &lo, const float4 &hi) {
     return 2.0f * (dx * dy + dy * dz + dz * dx);
 }
 
-// Block-wide reduction of centroid bounds into the control block.
-__device__ __forceinline__ void reduce_centroid_bounds(float cmin[3], float cmax[3], uint32_t *ctl) {
-    __shared__ float smin[3][kPrepBlock / 32], smax[3][kPrepBlock / 32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        float a = cmin[k], b = cmax[k];
-        for (int o = 16; o; o >>= 1) {
-            a = fminf(a, __shfl_xor_sync(~0u, a, o));
-            b = fmaxf(b, __shfl_xor_sync(~0u, b, o));
-        }
-        if (lane == 0) {
-            smin[k][warp] = a;
-            smax[k][warp] = b;
-        }
+__device__ __forceinline__ double box_area_d(float lx, float ly, float lz, float hx, float hy, float hz) {
+    if (!(lx <= hx && ly <= hy && lz <= hz)) return 0.0;
+    const double dx = double(hx) - lx, dy = double(hy) - ly, dz = double(hz) - lz;
+    return 2.0 * (dx * dy + dy * dz + dz * dx);
+}
+
+// Segment of global item i: binary search over the segment table.
+__device__ __forceinline__ uint32_t segment_of(const SegInput *segs, uint32_t nseg, uint32_t i) {
+    uint32_t lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (segs[mid].item_offset <= i)
+            lo = mid;
+        else
+            hi = mid - 1;
     }
-    __syncthreads();
-    if (threadIdx.x < 3) {
-        const int k = threadIdx.x;
-        float a = FLT_MAX, b = -FLT_MAX;
-        for (int w = 0; w < int(blockDim.x >> 5); w++) {
-            a = fminf(a, smin[k][w]);
-            b = fmaxf(b, smax[k][w]);
+    return lo;
+}
+
+// Centroid bounds into the per-segment control words; warps whose lanes share
+// a segment reduce first (most warps, as segments are contiguous).
+__device__ __forceinline__ void add_centroid(uint32_t seg, bool valid, const float c[3], uint32_t *segctl) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t seg0 = __shfl_sync(~0u, seg, 0);
+    const bool uniform = __all_sync(~0u, seg == seg0);
+    if (uniform) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            float a = valid ? c[k] : FLT_MAX, b = valid ? c[k] : -FLT_MAX;
+            for (int o = 16; o; o >>= 1) {
+                a = fminf(a, __shfl_xor_sync(~0u, a, o));
+                b = fmaxf(b, __shfl_xor_sync(~0u, b, o));
+            }
+            if (lane == 0 && a <= b) {
+                atomicMin(&segctl[kSegWords * seg0 + kSegCenLo + k], float_to_ordered(a));
+                atomicMax(&segctl[kSegWords * seg0 + kSegCenHi + k], float_to_ordered(b));
+            }
         }
-        if (a <= b) {
-            atomicMin(&ctl[kCtlCenLo + k], float_to_ordered(a));
-            atomicMax(&ctl[kCtlCenHi + k], float_to_ordered(b));
+    } else if (valid) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            atomicMin(&segctl[kSegWords * seg + kSegCenLo + k], float_to_ordered(c[k]));
+            atomicMax(&segctl[kSegWords * seg + kSegCenHi + k], float_to_ordered(c[k]));
         }
     }
 }
 
-__global__ void __launch_bounds__(kPrepBlock) k_tri_prep(TriInput in, uint32_t n, float4 *lo, float4 *hi,
-                                                         uint32_t *ctl) {
+__global__ void __launch_bounds__(kPrepBlock) k_tri_prep(const SegInput *segs, uint32_t nseg, uint32_t n, float4 *lo,
+                                                         float4 *hi, uint32_t *segctl, uint32_t *ctl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    if (i < n) {
-        const uint32_t *t = reinterpret_cast<const uint32_t *>(in.tbase + 12ull * i);
+    const bool in = i < n;
+    const uint32_t s = in ? segment_of(segs, nseg, i) : 0u;
+    float c[3] = {0, 0, 0};
+    bool valid = false;
+    if (in) {
+        const SegInput g = segs[s];
+        const uint32_t local = i - g.item_offset;
+        const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * local);
         const uint32_t i0 = t[0], i1 = t[1], i2 = t[2];
         float4 l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f), h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
-        if (i0 >= in.vcount || i1 >= in.vcount || i2 >= in.vcount) {
+        if (i0 >= g.vcount || i1 >= g.vcount || i2 >= g.vcount) {
+            atomicOr(&segctl[kSegWords * s + kSegErr], kErrBadIndex);
             atomicOr(&ctl[kCtlErr], kErrBadIndex);
         } else {
-            const float4 a = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * i0));
-            const float4 b = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * i1));
-            const float4 c = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * i2));
-            l.x = fminf(fminf(l.x, a.x), fminf(b.x, c.x));
-            l.y = fminf(fminf(l.y, a.y), fminf(b.y, c.y));
-            l.z = fminf(fminf(l.z, a.z), fminf(b.z, c.z));
-            h.x = fmaxf(fmaxf(h.x, a.x), fmaxf(b.x, c.x));
-            h.y = fmaxf(fmaxf(h.y, a.y), fmaxf(b.y, c.y));
-            h.z = fmaxf(fmaxf(h.z, a.z), fmaxf(b.z, c.z));
+            const float4 a = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i0));
+            const float4 b = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i1));
+            const float4 cc = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i2));
+            l.x = fminf(fminf(l.x, a.x), fminf(b.x, cc.x));
+            l.y = fminf(fminf(l.y, a.y), fminf(b.y, cc.y));
+            l.z = fminf(fminf(l.z, a.z), fminf(b.z, cc.z));
+            h.x = fmaxf(fmaxf(h.x, a.x), fmaxf(b.x, cc.x));
+            h.y = fmaxf(fmaxf(h.y, a.y), fmaxf(b.y, cc.y));
+            h.z = fmaxf(fmaxf(h.z, a.z), fmaxf(b.z, cc.z));
         }
         if (box_empty(l, h)) {
             l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f);
             h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
         } else {
-            cmin[0] = cmax[0] = 0.5f * (l.x + h.x);
-            cmin[1] = cmax[1] = 0.5f * (l.y + h.y);
-            cmin[2] = cmax[2] = 0.5f * (l.z + h.z);
+            valid = true;
+            c[0] = 0.5f * (l.x + h.x);
+            c[1] = 0.5f * (l.y + h.y);
+            c[2] = 0.5f * (l.z + h.z);
         }
         lo[i] = l;
         hi[i] = h;
     }
-    reduce_centroid_bounds(cmin, cmax, ctl);
+    add_centroid(s, valid, c, segctl);
 }
 
 __global__ void __launch_bounds__(kPrepBlock) k_inst_prep(const InstState *inst, uint32_t n, float4 *lo, float4 *hi,
-                                                          float *w2o, uint32_t *ctl) {
+                                                          float *w2o, uint32_t *segctl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float c[3] = {0, 0, 0};
+    bool valid = false;
     if (i < n) {
         const InstState &s = inst[i];
         float m[12], w[12];
@@ -158,38 +187,41 @@ __global__ void __launch_bounds__(kPrepBlock) k_inst_prep(const InstState *inst,
                 l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f);
                 h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
             } else {
-                cmin[0] = cmax[0] = 0.5f * (l.x + h.x);
-                cmin[1] = cmax[1] = 0.5f * (l.y + h.y);
-                cmin[2] = cmax[2] = 0.5f * (l.z + h.z);
+                valid = true;
+                c[0] = 0.5f * (l.x + h.x);
+                c[1] = 0.5f * (l.y + h.y);
+                c[2] = 0.5f * (l.z + h.z);
             }
         }
         lo[i] = l;
         hi[i] = h;
     }
-    reduce_centroid_bounds(cmin, cmax, ctl);
+    add_centroid(0, valid, c, segctl);
 }
 
-__global__ void k_morton(uint32_t n, const float4 *lo, const float4 *hi, const uint32_t *ctl,
-                         unsigned long long *keys, uint32_t *vals) {
+__global__ void k_morton(const SegInput *segs, uint32_t nseg, uint32_t n, uint32_t axis_bits, const float4 *lo,
+                         const float4 *hi, const uint32_t *segctl, unsigned long long *keys, uint32_t *vals) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const uint32_t s = nseg > 1 ? segment_of(segs, nseg, i) : 0u;
     const float4 l = lo[i], h = hi[i];
-    unsigned long long key = 0x7fffffffffffffffull;  // empty boxes sort last
+    const uint32_t qmax = (1u << axis_bits) - 1u;
+    unsigned long long code = (1ull << (3 * axis_bits)) - 1ull;  // empty boxes sort last in their segment
     if (!box_empty(l, h)) {
         const float c[3] = {0.5f * (l.x + h.x), 0.5f * (l.y + h.y), 0.5f * (l.z + h.z)};
         uint32_t q[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            const float blo = ordered_to_float(ctl[kCtlCenLo + k]);
-            const float bhi = ordered_to_float(ctl[kCtlCenHi + k]);
+            const float blo = ordered_to_float(segctl[kSegWords * s + kSegCenLo + k]);
+            const float bhi = ordered_to_float(segctl[kSegWords * s + kSegCenHi + k]);
             const float ext = bhi - blo;
             float f = ext > 0.0f ? (c[k] - blo) / ext : 0.0f;
             f = fminf(fmaxf(f, 0.0f), 1.0f);
-            q[k] = min(uint32_t(f * 2097151.0f), 2097151u);
+            q[k] = min(uint32_t(f * float(qmax)), qmax);
         }
-        key = spread21(q[0]) << 2 | spread21(q[1]) << 1 | spread21(q[2]);
+        code = spread21(q[0]) << 2 | spread21(q[1]) << 1 | spread21(q[2]);
     }
-    keys[i] = key;
+    keys[i] = (static_cast<unsigned long long>(s) << (3 * axis_bits)) | code;
     vals[i] = i;
 }
 
@@ -200,17 +232,25 @@ __device__ __forceinline__ bool delta_less(const unsigned long long *k, uint32_t
     return (a ^ (a + 1)) < (b ^ (b + 1));
 }
 
-__global__ void k_lbvh(uint32_t n, const unsigned long long *keys, const uint32_t *vals, const float4 *lo,
-                       const float4 *hi, uint32_t *bin_child, float4 *bin_lo, float4 *bin_hi, int32_t *other,
-                       uint32_t *ctl) {
+// Binary node j (0 <= j < n-1) covers sorted items [first, first + count);
+// bin_lo.w / bin_hi.w hold count / first as bits.  A segment's keys differ
+// from its neighbours' in the segment bits, so its boundary deltas are larger
+// than every inner one and the merges stay inside it; the thread that
+// completes the node spanning the whole segment records it as the root.
+__global__ void k_lbvh(const SegInput *segs, uint32_t n, uint32_t seg_shift, const unsigned long long *keys,
+                       const uint32_t *vals, const float4 *lo, const float4 *hi, uint32_t *bin_child, float4 *bin_lo,
+                       float4 *bin_hi, int32_t *other, uint32_t *segctl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (n == 1) {
-        ctl[kCtlRoot] = kLeafBit;
-        return;
-    }
+    const uint32_t s = seg_shift < 64 ? uint32_t(keys[i] >> seg_shift) : 0u;
+    const uint32_t seg_first = segs[s].item_offset;
+    const uint32_t seg_last = seg_first + segs[s].item_count - 1;
     uint32_t cur = kLeafBit | i;
     uint32_t l = i, r = i;
+    if (l == seg_first && r == seg_last) {
+        segctl[kSegWords * s + kSegRoot] = cur;
+        return;
+    }
     const uint32_t item = vals[i];
     float4 clo = lo[item], chi = hi[item];
     for (uint32_t guard = 0; guard < n; guard++) {
@@ -240,8 +280,8 @@ __global__ void k_lbvh(uint32_t n, const unsigned long long *keys, const uint32_
         bin_lo[parent] = make_float4(clo.x, clo.y, clo.z, __uint_as_float(r - l + 1));
         bin_hi[parent] = make_float4(chi.x, chi.y, chi.z, __uint_as_float(l));
         cur = parent;
-        if (l == 0 && r == n - 1) {
-            ctl[kCtlRoot] = parent;
+        if (l == seg_first && r == seg_last) {
+            segctl[kSegWords * s + kSegRoot] = parent;
             return;
         }
     }
@@ -252,12 +292,17 @@ struct TreeView {
     const float4 *blo, *bhi;
     const float4 *lo, *hi;  // item boxes
     const uint32_t *vals;   // sorted item ids
+    const unsigned long long *keys;
+    uint32_t seg_shift;     // segment = key >> seg_shift (64: a single segment)
     __device__ __forceinline__ bool leaf(uint32_t id) const { return (id & kLeafBit) != 0; }
     __device__ __forceinline__ uint32_t count(uint32_t id) const {
         return leaf(id) ? 1u : __float_as_uint(blo[id].w);
     }
     __device__ __forceinline__ uint32_t first(uint32_t id) const {
         return leaf(id) ? (id & ~kLeafBit) : __float_as_uint(bhi[id].w);
+    }
+    __device__ __forceinline__ uint32_t segment(uint32_t id) const {
+        return seg_shift < 64 ? uint32_t(keys[first(id)] >> seg_shift) : 0u;
     }
     __device__ __forceinline__ void box(uint32_t id, float4 &l, float4 &h) const {
         if (leaf(id)) {
@@ -271,10 +316,12 @@ struct TreeView {
     }
 };
 
-// Open up to 8 children of binary node b, assign them to octant slots and
-// allocate their wide-node / item ranges.  desc: 12 words per wide node.
-__device__ void collapse_node(const TreeView &tv, uint32_t b, uint32_t w, int leaf_max, uint32_t *desc,
-                              uint2 *qout, uint32_t *ctl, int level) {
+// Open up to `width` children of binary node b, assign them to octant slots
+// and allocate their wide-node / item ranges.  desc: 12 words per wide node
+// (binary node, child base, item base, segment, 8 slot children).
+__device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t b, uint32_t w, uint32_t seg,
+                              int leaf_max, int width, uint32_t *desc, uint2 *qout, uint32_t *ctl, uint32_t *segctl,
+                              int level) {
     uint32_t C[8];
     float A[8];
     int nC;
@@ -291,7 +338,7 @@ __device__ void collapse_node(const TreeView &tv, uint32_t b, uint32_t w, int le
         tv.box(C[k], l, h);
         A[k] = box_area(l, h);
     }
-    while (nC < 8) {
+    while (nC < width) {
         int best = -1;
         float best_a = -1.0f;
         for (int k = 0; k < nC; k++) {
@@ -319,7 +366,7 @@ __device__ void collapse_node(const TreeView &tv, uint32_t b, uint32_t w, int le
     for (int k = 0; k < nC; k++) {
         float4 l, h;
         tv.box(C[k], l, h);
-        if (box_empty(l, h)) {
+        if (box_empty(l, h) || box_empty(nl, nh)) {
             off[k][0] = off[k][1] = off[k][2] = 0.0f;
         } else {
             off[k][0] = 0.5f * (l.x + h.x) - pc[0];
@@ -331,15 +378,16 @@ __device__ void collapse_node(const TreeView &tv, uint32_t b, uint32_t w, int le
     for (int s = 0; s < 8; s++) slot_child[s] = kInvalid;
     uint32_t used_slots = 0, used_children = 0;
     for (int it = 0; it < nC; it++) {
-        float best = -FLT_MAX;
+        float best = -INFINITY;
         int bk = -1, bs = -1;
         for (int k = 0; k < nC; k++) {
             if (used_children >> k & 1u) continue;
             for (int s = 0; s < 8; s++) {
                 if (used_slots >> s & 1u) continue;
-                const float sc = ((s & 1) ? -off[k][0] : off[k][0]) + ((s & 2) ? -off[k][1] : off[k][1]) +
-                                 ((s & 4) ? -off[k][2] : off[k][2]);
-                if (sc > best) {
+                float sc = ((s & 1) ? -off[k][0] : off[k][0]) + ((s & 2) ? -off[k][1] : off[k][1]) +
+                           ((s & 4) ? -off[k][2] : off[k][2]);
+                if (!(sc == sc)) sc = -FLT_MAX;  // NaN never blocks an assignment
+                if (bk < 0 || sc > best) {
                     best = sc;
                     bk = k;
                     bs = s;
@@ -360,14 +408,17 @@ __device__ void collapse_node(const TreeView &tv, uint32_t b, uint32_t w, int le
         else
             n_items += cnt;
     }
+    uint32_t *sc = segctl + kSegWords * seg;
     const uint32_t child_base = n_int ? atomicAdd(&ctl[kCtlWideCount], n_int) : 0u;
-    const uint32_t item_base = n_items ? atomicAdd(&ctl[kCtlItemCount], n_items) : 0u;
+    const uint32_t item_base = n_items ? segs[seg].item_offset + atomicAdd(&sc[kSegItems], n_items) : 0u;
     const uint32_t qbase = n_int ? atomicAdd(&ctl[kCtlLevel + level + 1], n_int) : 0u;
+    if (n_int) atomicAdd(&sc[kSegNodes], n_int);
+    atomicMax(&sc[kSegDepth], uint32_t(level + 1));
     uint32_t *d = desc + 12ull * w;
     d[0] = b;
     d[1] = child_base;
     d[2] = item_base;
-    d[3] = 0;
+    d[3] = seg;
     uint32_t rank = 0;
     for (int s = 0; s < 8; s++) {
         const uint32_t c = slot_child[s];
@@ -379,15 +430,22 @@ __device__ void collapse_node(const TreeView &tv, uint32_t b, uint32_t w, int le
     }
 }
 
-__global__ void k_collapse(TreeView tv, uint32_t n, int leaf_max, uint32_t *desc, uint2 *q0, uint2 *q1,
-                           uint32_t *ctl) {
+// Level 0 tasks: the root of every non-empty segment s becomes wide node s.
+__global__ void k_collapse_init(const SegInput *segs, uint32_t nseg, uint32_t *segctl, uint2 *q0, uint32_t *desc,
+                                uint32_t *ctl) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) ctl[kCtlWideCount] = nseg;
+    if (s >= nseg) return;
+    desc[12ull * s + 3] = s;  // keeps the root slot of an empty segment identifiable
+    if (segs[s].item_count == 0) return;
+    const uint32_t pos = atomicAdd(&ctl[kCtlLevel + 0], 1u);
+    q0[pos] = make_uint2(segctl[kSegWords * s + kSegRoot], s);
+    segctl[kSegWords * s + kSegNodes] = 1u;
+}
+
+__global__ void k_collapse(TreeView tv, const SegInput *segs, int leaf_max, int width, uint32_t *desc, uint2 *q0,
+                           uint2 *q1, uint32_t *ctl, uint32_t *segctl) {
     cg::grid_group grid = cg::this_grid();
-    if (grid.thread_rank() == 0) {
-        q0[0] = make_uint2(ctl[kCtlRoot], 0u);
-        ctl[kCtlLevel + 0] = 1u;
-        ctl[kCtlWideCount] = 1u;
-    }
-    grid.sync();
     int level = 0;
     for (; level < kMaxLevels; level++) {
         const uint32_t cnt = __ldcg(&ctl[kCtlLevel + level]);
@@ -396,7 +454,8 @@ __global__ void k_collapse(TreeView tv, uint32_t n, int leaf_max, uint32_t *desc
         uint2 *qout = (level & 1) ? q0 : q1;
         for (unsigned long long t = grid.thread_rank(); t < cnt; t += grid.size()) {
             const uint2 task = qin[t];
-            collapse_node(tv, task.x, task.y, leaf_max, desc, qout, ctl, level);
+            const uint32_t seg = tv.segment(task.x);
+            collapse_node(tv, segs, task.x, task.y, seg, leaf_max, width, desc, qout, ctl, segctl, level);
         }
         grid.sync();
     }
@@ -416,15 +475,21 @@ __device__ __forceinline__ uint32_t quant_exp(float lo, float hi) {
     return min(b, 254u);
 }
 
+// Writes wide node w (both layouts, indices relative to its segment) and its
+// leaf items; accumulates the segment's wide SAH (sum of node areas + leaf
+// areas x counts) into sah[2 seg], its root area into sah[2 seg + 1].
 template <class ItemWriter>
-__device__ void emit_node(const TreeView &tv, const uint32_t *desc, uint32_t w, Node8Q *qn, Node8F *fn,
-                          int leaf_max, uint32_t *ctl, ItemWriter &&write_item, float4 &root_lo, float4 &root_hi) {
+__device__ void emit_node(const TreeView &tv, const SegInput *segs, const uint32_t *desc, uint32_t w, Node8Q *qn,
+                          Node8F *fn, int leaf_max, uint32_t *ctl, double *sah, ItemWriter &&write_item,
+                          float4 &node_lo, float4 &node_hi) {
     const uint32_t *d = desc + 12ull * w;
-    const uint32_t b = d[0], child_base = d[1], item_base = d[2];
+    const uint32_t b = d[0], child_base = d[1], item_base = d[2], seg = d[3];
+    const uint32_t root = seg;  // wide index of the segment's root
+    const uint32_t item_offset = segs[seg].item_offset;
     float4 nl, nh;
     tv.box(b, nl, nh);
-    root_lo = nl;
-    root_hi = nh;
+    node_lo = nl;
+    node_hi = nh;
     const bool node_empty = box_empty(nl, nh);
     uint32_t ex[3];
     ex[0] = node_empty ? 127u : quant_exp(nl.x, nh.x);
@@ -441,6 +506,7 @@ __device__ void emit_node(const TreeView &tv, const uint32_t *desc, uint32_t w, 
     q.pz = p[2];
     uint32_t meta_lo = 0, meta_hi = 0, imask = 0, offset = 0;
     uint32_t qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}}, qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    double area_acc = box_area_d(nl.x, nl.y, nl.z, nh.x, nh.y, nh.z);
     for (int s = 0; s < 8; s++) {
         const uint32_t c = d[4 + s];
         uint32_t meta = 0;
@@ -457,8 +523,10 @@ __device__ void emit_node(const TreeView &tv, const uint32_t *desc, uint32_t w, 
             } else {
                 meta = empty ? 0u : meta_leaf(cnt, offset);
                 const uint32_t first = tv.first(c);
-                for (uint32_t j = 0; j < cnt; j++) write_item(item_base + offset + j, tv.vals[first + j]);
+                for (uint32_t j = 0; j < cnt; j++)
+                    write_item(item_base + offset + j, tv.vals[first + j] - item_offset, seg);
                 offset += cnt;
+                area_acc += double(cnt) * box_area_d(l.x, l.y, l.z, h.x, h.y, h.z);
             }
             if (!empty) {
                 cl[0] = l.x;
@@ -496,9 +564,11 @@ __device__ void emit_node(const TreeView &tv, const uint32_t *desc, uint32_t w, 
         f.hi_y[s] = ch[1];
         f.hi_z[s] = ch[2];
     }
+    const uint32_t cb = imask ? child_base - root : 0u;
+    const uint32_t ib = offset ? item_base - item_offset : 0u;
     q.exps = ex[0] | (ex[1] << 8) | (ex[2] << 16) | (imask << 24);
-    q.child_base = child_base;
-    q.item_base = item_base;
+    q.child_base = cb;
+    q.item_base = ib;
     q.meta_lo = meta_lo;
     q.meta_hi = meta_hi;
     for (int k = 0; k < 2; k++) {
@@ -509,59 +579,82 @@ __device__ void emit_node(const TreeView &tv, const uint32_t *desc, uint32_t w, 
         q.qhi_y[k] = qhi[1][k];
         q.qhi_z[k] = qhi[2][k];
     }
-    f.child_base = child_base;
-    f.item_base = item_base;
+    f.child_base = cb;
+    f.item_base = ib;
     f.meta_lo = meta_lo;
     f.meta_hi = meta_hi;
     qn[w] = q;
     fn[w] = f;
+    if (sah != nullptr) {
+        atomicAdd(&sah[2 * seg], area_acc);
+        if (w == root) sah[2 * seg + 1] = box_area_d(nl.x, nl.y, nl.z, nh.x, nh.y, nh.z);
+    }
 }
 
-__global__ void k_emit_blas(TreeView tv, const uint32_t *desc, uint32_t wide_count, int leaf_max, TriInput in,
-                            Node8Q *qn, Node8F *fn, TriRec *tris, BlasDesc *bdesc, uint32_t *ctl, uint32_t tri_count) {
+__global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *desc, uint32_t wide_count,
+                            int leaf_max, Node8Q *qn, Node8F *fn, TriRec *tris, const uint32_t *segctl,
+                            uint32_t *ctl, double *sah) {
     const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= wide_count) return;
+    const uint32_t seg = desc[12ull * w + 3];
+    if (segs[seg].item_count == 0) {  // root slot of an empty segment
+        if (w == seg) {
+            BlasDesc *bd = segs[seg].desc;
+            bd->qnodes = nullptr;
+            bd->fnodes = nullptr;
+            bd->tris = nullptr;
+            bd->node_count = 0;
+            bd->tri_count = 0;
+            bd->depth = 0;
+            bd->valid = 0;
+        }
+        return;
+    }
     float4 rl, rh;
     emit_node(
-        tv, desc, w, qn, fn, leaf_max, ctl,
-        [&](uint32_t pos, uint32_t prim) {
-            const uint32_t *t = reinterpret_cast<const uint32_t *>(in.tbase + 12ull * prim);
-            float4 a = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * t[0]));
-            float4 b = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * t[1]));
-            float4 c = __ldg(reinterpret_cast<const float4 *>(in.vbase + in.vstride * t[2]));
+        tv, segs, desc, w, qn, fn, leaf_max, ctl, sah,
+        [&](uint32_t pos, uint32_t prim, uint32_t s) {
+            const SegInput &g = segs[s];
+            const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * prim);
+            float4 a = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * t[0]));
+            float4 b = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * t[1]));
+            float4 c = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * t[2]));
             a.w = __uint_as_float(prim);
             b.w = 0.0f;
             c.w = 0.0f;
             tris[pos] = TriRec{a, b, c};
         },
         rl, rh);
-    if (w == 0) {
-        bdesc->qnodes = qn;
-        bdesc->fnodes = fn;
-        bdesc->tris = tris;
-        bdesc->node_count = wide_count;
-        bdesc->tri_count = tri_count;
+    if (w == seg) {  // the segment's root writes the BLAS descriptor
+        const SegInput &g = segs[seg];
+        BlasDesc *bd = g.desc;
+        const uint32_t *sc = segctl + kSegWords * seg;
+        bd->qnodes = qn + seg;
+        bd->fnodes = fn + seg;
+        bd->tris = tris + g.item_offset;
+        bd->node_count = sc[kSegNodes];
+        bd->tri_count = g.item_count;
         const bool empty = box_empty(rl, rh);
-        bdesc->lo[0] = rl.x;
-        bdesc->lo[1] = rl.y;
-        bdesc->lo[2] = rl.z;
-        bdesc->hi[0] = rh.x;
-        bdesc->hi[1] = rh.y;
-        bdesc->hi[2] = rh.z;
-        bdesc->depth = ctl[kCtlDepth];
-        bdesc->valid = empty ? 0u : 1u;
+        bd->lo[0] = rl.x;
+        bd->lo[1] = rl.y;
+        bd->lo[2] = rl.z;
+        bd->hi[0] = rh.x;
+        bd->hi[1] = rh.y;
+        bd->hi[2] = rh.z;
+        bd->depth = sc[kSegDepth];
+        bd->valid = empty ? 0u : 1u;
     }
 }
 
-__global__ void k_emit_tlas(TreeView tv, const uint32_t *desc, uint32_t wide_count, int leaf_max,
-                            const InstState *inst, const float *w2o, Node8Q *qn, Node8F *fn, InstRec *recs,
-                            uint32_t *ctl) {
+__global__ void k_emit_tlas(TreeView tv, const SegInput *segs, const uint32_t *desc, uint32_t wide_count,
+                            int leaf_max, const InstState *inst, const float *w2o, Node8Q *qn, Node8F *fn,
+                            InstRec *recs, uint32_t *ctl, double *sah) {
     const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= wide_count) return;
     float4 rl, rh;
     emit_node(
-        tv, desc, w, qn, fn, leaf_max, ctl,
-        [&](uint32_t pos, uint32_t id) {
+        tv, segs, desc, w, qn, fn, leaf_max, ctl, sah,
+        [&](uint32_t pos, uint32_t id, uint32_t) {
             InstRec r;
 #pragma unroll
             for (int k = 0; k < 12; k++) r.w2o[k] = w2o[12ull * id + k];
@@ -608,53 +701,23 @@ __global__ void k_init_instances(InstState *inst, uint32_t begin, uint32_t end) 
     inst[i] = s;
 }
 
-__global__ void k_wide_sah(const Node8F *fn, uint32_t wide_count, double *out) {
-    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-    double acc = 0.0, root = 0.0;
-    auto area = [](float lx, float ly, float lz, float hx, float hy, float hz) -> double {
-        if (!(lx <= hx && ly <= hy && lz <= hz)) return 0.0;
-        const double dx = double(hx) - lx, dy = double(hy) - ly, dz = double(hz) - lz;
-        return 2.0 * (dx * dy + dy * dz + dz * dx);
-    };
-    if (w < wide_count) {
-        const Node8F &f = fn[w];
-        float lx = FLT_MAX, ly = FLT_MAX, lz = FLT_MAX, hx = -FLT_MAX, hy = -FLT_MAX, hz = -FLT_MAX;
-        for (int s = 0; s < 8; s++) {
-            const uint32_t meta = ((s < 4 ? f.meta_lo : f.meta_hi) >> ((s & 3) * 8)) & 0xffu;
-            if (meta == 0 || !(f.lo_x[s] <= f.hi_x[s])) continue;
-            lx = fminf(lx, f.lo_x[s]);
-            ly = fminf(ly, f.lo_y[s]);
-            lz = fminf(lz, f.lo_z[s]);
-            hx = fmaxf(hx, f.hi_x[s]);
-            hy = fmaxf(hy, f.hi_y[s]);
-            hz = fmaxf(hz, f.hi_z[s]);
-            if (!meta_internal(meta))
-                acc += double(meta_count(meta)) * area(f.lo_x[s], f.lo_y[s], f.lo_z[s], f.hi_x[s], f.hi_y[s], f.hi_z[s]);
-        }
-        const double a = area(lx, ly, lz, hx, hy, hz);
-        acc += a;
-        if (w == 0) root = a;
-    }
-    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(~0u, acc, o);
-    if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(&out[0], acc);
-    if (w == 0) out[1] = root;
-}
-
-// SAH of the binary LBVH (C_node = C_item = 1); out[0] = sum of areas,
-// out[1] = root area.
-__global__ void k_binary_sah(uint32_t n, const float4 *blo, const float4 *bhi, const float4 *lo, const float4 *hi,
-                             const uint32_t *ctl, double *out) {
+// SAH of every segment's binary LBVH (C_node = C_item = 1): out[2 s] = sum of
+// areas, out[2 s + 1] = root area.
+__global__ void k_binary_sah(uint32_t n, uint32_t seg_shift, const unsigned long long *keys, const uint32_t *vals,
+                             const float4 *blo, const float4 *bhi, const float4 *lo, const float4 *hi,
+                             const SegInput *segs, const uint32_t *segctl, double *out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    double acc = 0.0;
-    if (i < n) {
-        acc += box_area(lo[i], hi[i]);
-        if (i + 1 < n) acc += box_area(blo[i], bhi[i]);
-    }
-    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(~0u, acc, o);
-    if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(&out[0], acc);
-    if (i == 0) {
-        const uint32_t r = ctl[kCtlRoot];
-        out[1] = (r & kLeafBit) ? box_area(lo[0], hi[0]) : box_area(blo[r], bhi[r]);
+    if (i >= n) return;
+    const uint32_t s = seg_shift < 64 ? uint32_t(keys[i] >> seg_shift) : 0u;
+    const uint32_t it = vals[i];
+    double acc = box_area(lo[it], hi[it]);
+    // internal node i splits items i | i+1: it belongs to the segment iff both do
+    const uint32_t last = segs[s].item_offset + segs[s].item_count - 1;
+    if (i < last) acc += box_area(blo[i], bhi[i]);
+    atomicAdd(&out[2 * s], acc);
+    if (i == segs[s].item_offset) {
+        const uint32_t r = segctl[kSegWords * s + kSegRoot];
+        out[2 * s + 1] = (r & kLeafBit) ? box_area(lo[it], hi[it]) : box_area(blo[r], bhi[r]);
     }
 }
 
@@ -668,20 +731,12 @@ TreeView make_view(const BuildScratch &s) {
     tv.lo = s.box_lo;
     tv.hi = s.box_hi;
     tv.vals = s.vals_sorted;
+    tv.keys = s.keys_sorted;
+    tv.seg_shift = s.nseg > 1 ? 3 * s.axis_bits : 64;
     return tv;
 }
 
-cudaError_t build_common(uint32_t n, int leaf_max, BuildScratch &s, cudaStream_t st) {
-    k_morton<<<blocks_for(n, 256), 256, 0, st>>>(n, s.box_lo, s.box_hi, s.ctl, s.keys, s.vals);
-    cudaError_t e = sort_pairs(s.sort_tmp, s.sort_tmp_bytes, s.keys, s.keys_sorted, s.vals, s.vals_sorted, n, st);
-    if (e != cudaSuccess) return e;
-    if (n > 1) {
-        e = cudaMemsetAsync(s.other, 0xff, sizeof(int32_t) * (n - 1), st);
-        if (e != cudaSuccess) return e;
-    }
-    k_lbvh<<<blocks_for(n, 256), 256, 0, st>>>(n, s.keys_sorted, s.vals_sorted, s.box_lo, s.box_hi, s.bin_child,
-                                                 s.bin_lo, s.bin_hi, s.other, s.ctl);
-    // cooperative collapse: grid = co-resident blocks
+int collapse_grid() {
     static int grid = 0;
     if (grid == 0) {
         int dev = 0, sms = 0, per_sm = 0;
@@ -690,40 +745,69 @@ cudaError_t build_common(uint32_t n, int leaf_max, BuildScratch &s, cudaStream_t
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse, 128, 0);
         grid = sms * (per_sm > 2 ? 2 : (per_sm > 0 ? per_sm : 1));
     }
+    return grid;
+}
+
+cudaError_t build_common(BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
+    const uint32_t n = s.n;
+    k_morton<<<blocks_for(n, 256), 256, 0, st>>>(s.segs, s.nseg, n, s.axis_bits, s.box_lo, s.box_hi, s.segctl,
+                                                  s.keys, s.vals);
+    cudaError_t e = sort_pairs(s.sort_tmp, s.sort_tmp_bytes, s.keys, s.keys_sorted, s.vals, s.vals_sorted, n,
+                               3 * s.axis_bits + s.seg_bits, st);
+    if (e != cudaSuccess) return e;
+    if (n > 1) {
+        e = cudaMemsetAsync(s.other, 0xff, sizeof(int32_t) * (n - 1), st);
+        if (e != cudaSuccess) return e;
+    }
+    const uint32_t shift = s.nseg > 1 ? 3 * s.axis_bits : 64;
+    k_lbvh<<<blocks_for(n, 256), 256, 0, st>>>(s.segs, n, shift, s.keys_sorted, s.vals_sorted, s.box_lo, s.box_hi,
+                                                 s.bin_child, s.bin_lo, s.bin_hi, s.other, s.segctl);
+    k_binary_sah<<<blocks_for(n, 256), 256, 0, st>>>(n, shift, s.keys_sorted, s.vals_sorted, s.bin_lo, s.bin_hi,
+                                                       s.box_lo, s.box_hi, s.segs, s.segctl, s.bin_sah);
+    k_collapse_init<<<blocks_for(s.nseg, 256), 256, 0, st>>>(s.segs, s.nseg, s.segctl, s.queue, s.desc, s.ctl);
     TreeView tv = make_view(s);
-    uint32_t nn = n;
-    int lm = leaf_max;
+    const SegInput *segs = s.segs;
+    int lm = bp.leaf_max, width = bp.width;
     uint32_t *desc = s.desc;
-    uint2 *q0 = s.queue, *q1 = s.queue + (n + 1);
-    uint32_t *ctl = s.ctl;
-    void *args[] = {&tv, &nn, &lm, &desc, &q0, &q1, &ctl};
-    return cudaLaunchCooperativeKernel(reinterpret_cast<void *>(k_collapse), dim3(grid), dim3(128), args, 0, st);
+    uint2 *q0 = s.queue, *q1 = s.queue + s.queue_len;
+    uint32_t *ctl = s.ctl, *segctl = s.segctl;
+    void *args[] = {&tv, &segs, &lm, &width, &desc, &q0, &q1, &ctl, &segctl};
+    return cudaLaunchCooperativeKernel(reinterpret_cast<void *>(k_collapse), dim3(collapse_grid()), dim3(128), args, 0,
+                                       st);
 }
 
 }  // namespace
 
-cudaError_t build_tree_tris(const TriInput &in, uint32_t n, int leaf_max, BuildScratch &s, cudaStream_t st) {
-    k_tri_prep<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(in, n, s.box_lo, s.box_hi, s.ctl);
-    return build_common(n, leaf_max, s, st);
+uint32_t morton_axis_bits(uint32_t nseg, uint32_t *seg_bits) {
+    uint32_t sb = 0;
+    while (nseg > 1 && (1u << sb) < nseg) sb++;
+    *seg_bits = sb;
+    const uint32_t ab = (63 - sb) / 3;
+    return ab > 21 ? 21 : ab;
 }
 
-cudaError_t build_tree_insts(const InstState *inst, uint32_t n, int leaf_max, BuildScratch &s, cudaStream_t st) {
-    k_inst_prep<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(inst, n, s.box_lo, s.box_hi, s.w2o, s.ctl);
-    return build_common(n, leaf_max, s, st);
+cudaError_t build_tree_tris(BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
+    k_tri_prep<<<blocks_for(s.n, kPrepBlock), kPrepBlock, 0, st>>>(s.segs, s.nseg, s.n, s.box_lo, s.box_hi, s.segctl,
+                                                                   s.ctl);
+    return build_common(s, bp, st);
 }
 
-cudaError_t emit_blas(const TriInput &in, uint32_t n, int leaf_max, uint32_t wide_count, const BuildScratch &s,
-                      Node8Q *qn, Node8F *fn, TriRec *tris, BlasDesc *desc, cudaStream_t st) {
-    k_emit_blas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.desc, wide_count, leaf_max, in, qn, fn,
-                                                              tris, desc, s.ctl, n);
+cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
+    k_inst_prep<<<blocks_for(s.n, kPrepBlock), kPrepBlock, 0, st>>>(inst, s.n, s.box_lo, s.box_hi, s.w2o, s.segctl);
+    return build_common(s, bp, st);
+}
+
+cudaError_t emit_blas(const BuildScratch &s, const BuildParams &bp, uint32_t wide_count, Node8Q *qn, Node8F *fn,
+                      TriRec *tris, double *wide_sah, cudaStream_t st) {
+    k_emit_blas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.segs, s.desc, wide_count, bp.leaf_max,
+                                                              qn, fn, tris, s.segctl, s.ctl, wide_sah);
     return cudaGetLastError();
 }
 
-cudaError_t emit_tlas(const InstState *inst, uint32_t n, int leaf_max, uint32_t wide_count, const BuildScratch &s,
-                      Node8Q *qn, Node8F *fn, InstRec *recs, cudaStream_t st) {
-    (void)n;
-    k_emit_tlas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.desc, wide_count, leaf_max, inst, s.w2o,
-                                                              qn, fn, recs, s.ctl);
+cudaError_t emit_tlas(const InstState *inst, const BuildScratch &s, const BuildParams &bp, uint32_t wide_count,
+                      Node8Q *qn, Node8F *fn, InstRec *recs, double *wide_sah, cudaStream_t st) {
+    k_emit_tlas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.segs, s.desc, wide_count, bp.leaf_max,
+                                                              inst, s.w2o, qn, fn, recs, s.ctl, wide_sah);
     return cudaGetLastError();
 }
 
@@ -737,19 +821,6 @@ cudaError_t apply_modifications(const ModRec *mods, uint32_t count, InstState *i
 cudaError_t init_instances(InstState *inst, uint32_t begin, uint32_t end, cudaStream_t st) {
     if (end <= begin) return cudaSuccess;
     k_init_instances<<<blocks_for(end - begin, 256), 256, 0, st>>>(inst, begin, end);
-    return cudaGetLastError();
-}
-
-cudaError_t binary_sah(const BuildScratch &s, uint32_t n, cudaStream_t st) {
-    double *out = reinterpret_cast<double *>(s.ctl + kCtlWords);
-    k_binary_sah<<<blocks_for(n, 256), 256, 0, st>>>(n, s.bin_lo, s.bin_hi, s.box_lo, s.box_hi, s.ctl, out);
-    return cudaGetLastError();
-}
-
-cudaError_t wide_sah(const Node8F *fn, uint32_t wide_count, double *d_out, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(d_out, 0, 2 * sizeof(double), st);
-    if (e != cudaSuccess) return e;
-    k_wide_sah<<<blocks_for(wide_count, 256), 256, 0, st>>>(fn, wide_count, d_out);
     return cudaGetLastError();
 }
 

@@ -73,17 +73,27 @@ int current_device_state(DeviceState **out) {
     return LCX_OK;
 }
 
+// Device memory that holds built BVHs; a batch build shares one block
+// between its meshes, which keep it alive by reference.
+struct DevBlock {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    ~DevBlock() {
+        if (ptr) cudaFree(ptr);  // cudaFree waits for work still using it
+    }
+};
+
 struct MeshObj {
     LcxAccelOption opt{};
     int device = 0;
     BlasDesc *d_desc = nullptr;
-    void *d_mem = nullptr;
-    size_t mem_bytes = 0;
+    std::shared_ptr<DevBlock> block;  // nodes + triangles (possibly shared by a batch)
+    double *wide_sah = nullptr;       // in `block`: 2 doubles of this mesh's segment
+    size_t mem_bytes = 0;             // this mesh's share of the block
     uint32_t node_count = 0, tri_count = 0, depth = 0;
     bool built = false;
     uint64_t generation = 0;
     double sah = 0.0;
-    Node8F *fnodes = nullptr;
     std::mutex mtx;
 };
 
@@ -93,8 +103,8 @@ struct AccelObj {
     InstState *d_inst = nullptr;
     uint32_t inst_cap = 0, inst_count = 0;
     std::vector<uint64_t> inst_mesh;  // mesh handle per instance (0 = none)
-    void *d_mem = nullptr;
-    size_t mem_bytes = 0;
+    std::shared_ptr<DevBlock> block;
+    double *wide_sah = nullptr;
     Node8Q *qn = nullptr;
     Node8F *fn = nullptr;
     InstRec *recs = nullptr;
@@ -136,8 +146,19 @@ struct ScratchHolder {
     }
 };
 
-int alloc_scratch(ScratchHolder &h, BuildScratch &s, uint32_t n, bool tlas) {
+// Allocates the scratch of a build over n items in the given segments and
+// uploads the segment table and initial control words.
+int alloc_scratch(ScratchHolder &h, BuildScratch &s, const std::vector<SegInput> &segs, uint32_t n, bool tlas) {
     const size_t nn = std::max<uint32_t>(n, 1);
+    s.n = n;
+    s.nseg = uint32_t(segs.size());
+    s.axis_bits = morton_axis_bits(s.nseg, &s.seg_bits);
+    s.queue_len = n + s.nseg + 1;
+    SegInput *d_segs = nullptr;
+    LCX_CUDA(h.alloc((void **)&d_segs, sizeof(SegInput) * s.nseg), "scratch");
+    s.segs = d_segs;
+    LCX_CUDA(h.alloc((void **)&s.segctl, sizeof(uint32_t) * kSegWords * s.nseg), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.bin_sah, sizeof(double) * 2 * s.nseg), "scratch");
     LCX_CUDA(h.alloc((void **)&s.box_lo, sizeof(float4) * nn), "scratch");
     LCX_CUDA(h.alloc((void **)&s.box_hi, sizeof(float4) * nn), "scratch");
     LCX_CUDA(h.alloc((void **)&s.keys, sizeof(unsigned long long) * nn), "scratch");
@@ -148,33 +169,43 @@ int alloc_scratch(ScratchHolder &h, BuildScratch &s, uint32_t n, bool tlas) {
     LCX_CUDA(h.alloc((void **)&s.bin_lo, sizeof(float4) * nn), "scratch");
     LCX_CUDA(h.alloc((void **)&s.bin_hi, sizeof(float4) * nn), "scratch");
     LCX_CUDA(h.alloc((void **)&s.other, sizeof(int32_t) * nn), "scratch");
-    LCX_CUDA(h.alloc((void **)&s.desc, sizeof(uint32_t) * 12 * (nn + 1)), "scratch");
-    LCX_CUDA(h.alloc((void **)&s.queue, sizeof(uint2) * 2 * (nn + 1)), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.desc, sizeof(uint32_t) * 12 * s.queue_len), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.queue, sizeof(uint2) * 2 * s.queue_len), "scratch");
     if (tlas) LCX_CUDA(h.alloc((void **)&s.w2o, sizeof(float) * 12 * nn), "scratch");
-    LCX_CUDA(h.alloc((void **)&s.ctl, sizeof(uint32_t) * kCtlWords + 2 * sizeof(double)), "scratch");
+    LCX_CUDA(h.alloc((void **)&s.ctl, sizeof(uint32_t) * kCtlWords), "scratch");
     s.sort_tmp_bytes = sort_temp_bytes(uint32_t(nn));
     LCX_CUDA(h.alloc(&s.sort_tmp, s.sort_tmp_bytes), "scratch");
+    // uploads: segment table, control words (centroid minima start at the largest ordered value)
+    std::vector<uint32_t> segctl(size_t(kSegWords) * s.nseg, 0u);
+    for (uint32_t i = 0; i < s.nseg; i++)
+        for (int k = 0; k < 3; k++) segctl[size_t(kSegWords) * i + kSegCenLo + k] = 0xffffffffu;
+    LCX_CUDA(cudaMemcpyAsync(d_segs, segs.data(), sizeof(SegInput) * s.nseg, cudaMemcpyHostToDevice, h.st),
+             "segment upload");
+    LCX_CUDA(cudaMemcpyAsync(s.segctl, segctl.data(), sizeof(uint32_t) * segctl.size(), cudaMemcpyHostToDevice, h.st),
+             "segment upload");
+    LCX_CUDA(cudaMemsetAsync(s.bin_sah, 0, sizeof(double) * 2 * s.nseg, h.st), "scratch init");
+    LCX_CUDA(cudaMemsetAsync(s.ctl, 0, sizeof(uint32_t) * kCtlWords, h.st), "scratch init");
+    // (copies from pageable memory return once the source has been staged)
     return LCX_OK;
 }
 
-int init_ctl(const BuildScratch &s, cudaStream_t st, uint32_t *h_ctl) {
-    std::memset(h_ctl, 0, sizeof(uint32_t) * kCtlWords);
-    for (int k = 0; k < 3; k++) h_ctl[kCtlCenLo + k] = 0xffffffffu;
-    LCX_CUDA(cudaMemcpyAsync(s.ctl, h_ctl, sizeof(uint32_t) * kCtlWords, cudaMemcpyHostToDevice, st), "ctl upload");
-    LCX_CUDA(cudaMemsetAsync(reinterpret_cast<char *>(s.ctl) + sizeof(uint32_t) * kCtlWords, 0, 2 * sizeof(double), st),
-             "ctl upload");
-    return LCX_OK;
-}
-
-struct CtlReadback {
-    uint32_t words[kCtlWords];
-    double sah[2];
+struct BuildReadback {
+    std::vector<uint32_t> ctl, segctl;
+    std::vector<double> bin_sah;
 };
 
-int read_ctl(const BuildScratch &s, cudaStream_t st, CtlReadback &out) {
-    LCX_CUDA(cudaMemcpyAsync(&out, s.ctl, sizeof(uint32_t) * kCtlWords + 2 * sizeof(double), cudaMemcpyDeviceToHost,
+int read_back(const BuildScratch &s, cudaStream_t st, BuildReadback &out) {
+    out.ctl.resize(kCtlWords);
+    out.segctl.resize(size_t(kSegWords) * s.nseg);
+    out.bin_sah.resize(2 * size_t(s.nseg));
+    LCX_CUDA(cudaMemcpyAsync(out.ctl.data(), s.ctl, sizeof(uint32_t) * kCtlWords, cudaMemcpyDeviceToHost, st),
+             "readback");
+    LCX_CUDA(cudaMemcpyAsync(out.segctl.data(), s.segctl, sizeof(uint32_t) * out.segctl.size(), cudaMemcpyDeviceToHost,
                              st),
-             "ctl readback");
+             "readback");
+    LCX_CUDA(cudaMemcpyAsync(out.bin_sah.data(), s.bin_sah, sizeof(double) * out.bin_sah.size(),
+                             cudaMemcpyDeviceToHost, st),
+             "readback");
     LCX_CUDA(cudaStreamSynchronize(st), "build sync");
     return LCX_OK;
 }
@@ -185,6 +216,139 @@ int check_option(const LcxAccelOption *o) {
 }
 
 int leaf_items_for(const LcxAccelOption &o) { return o.hint == LCX_HINT_FAST_BUILD ? 3 : 2; }
+
+// Build knobs (see lcx_set_build_tuning); 0 = derive from the AccelOption hint.
+struct BuildTuning {
+    int leaf_max = 0;
+    int width = 8;
+};
+BuildTuning g_build_tune;
+
+BuildParams build_params_for(const LcxAccelOption &o) {
+    BuildParams bp;
+    bp.leaf_max = g_build_tune.leaf_max > 0 ? g_build_tune.leaf_max : leaf_items_for(o);
+    bp.width = g_build_tune.width;
+    return bp;
+}
+
+int validate_mesh_command(const LcxMeshBuildCommand *cmd, uint64_t &tri64, uint64_t &vcount64) {
+    if (!cmd) return fail(LCX_ERR_INVALID_ARG, "mesh build command is null");
+    // src/runtime/rtx/mesh.cpp:41-50 and :33-39
+    if (cmd->request > LCX_REQUEST_FORCE_BUILD) return fail(LCX_ERR_INVALID_ARG, "invalid build request %u", cmd->request);
+    if (cmd->vertex_stride == 0 || cmd->vertex_stride % 16 != 0)
+        return fail(LCX_ERR_INVALID_ARG, "Vertex stride must be aligned to 16 bytes (got %zu).", cmd->vertex_stride);
+    if (cmd->vertex_buffer_offset % cmd->vertex_stride != 0 || cmd->vertex_buffer_size % cmd->vertex_stride != 0)
+        return fail(LCX_ERR_INVALID_ARG, "vertex buffer offset %zu / size %zu not aligned to vertex stride %zu",
+                    cmd->vertex_buffer_offset, cmd->vertex_buffer_size, cmd->vertex_stride);
+    if (cmd->triangle_buffer_offset % 4 != 0 || cmd->triangle_buffer_size % 12 != 0)
+        return fail(LCX_ERR_INVALID_ARG, "triangle buffer offset %zu / size %zu not aligned (4 / 12 bytes)",
+                    cmd->triangle_buffer_offset, cmd->triangle_buffer_size);
+    tri64 = cmd->triangle_buffer_size / 12;
+    vcount64 = cmd->vertex_buffer_size / cmd->vertex_stride;
+    if (tri64 >= (1ull << 31) || vcount64 >= (1ull << 32))
+        return fail(LCX_ERR_INVALID_ARG, "mesh too large (%llu triangles, %llu vertices)", (unsigned long long)tri64,
+                    (unsigned long long)vcount64);
+    if (tri64 && (cmd->vertex_buffer == 0 || cmd->triangle_buffer == 0))
+        return fail(LCX_ERR_INVALID_ARG, "null vertex or triangle buffer");
+    if ((cmd->vertex_buffer + cmd->vertex_buffer_offset) % 16 != 0 || (cmd->triangle_buffer % 4) != 0)
+        return fail(LCX_ERR_INVALID_ARG, "vertex buffer must be 16-byte aligned, triangle buffer 4-byte aligned");
+    return LCX_OK;
+}
+
+// Builds the BLASes of `meshes` (locked by the caller) from `cmds` in one
+// segmented pipeline: one sort, one LBVH pass, one cooperative collapse and
+// one emit for all of them, into one shared device block.  Synchronises the
+// host once to size the block.
+int build_meshes(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand *cmds, cudaStream_t st) {
+    const size_t count = meshes.size();
+    std::vector<SegInput> segs(count);
+    uint64_t total = 0;
+    for (size_t i = 0; i < count; i++) {
+        uint64_t tri64 = 0, v64 = 0;
+        if (int r = validate_mesh_command(&cmds[i], tri64, v64)) return r;
+        SegInput &g = segs[i];
+        g.vbase = reinterpret_cast<const unsigned char *>(cmds[i].vertex_buffer) + cmds[i].vertex_buffer_offset;
+        g.vstride = cmds[i].vertex_stride;
+        g.tbase = reinterpret_cast<const unsigned char *>(cmds[i].triangle_buffer) + cmds[i].triangle_buffer_offset;
+        g.vcount = uint32_t(v64);
+        g.item_offset = uint32_t(total);
+        g.item_count = uint32_t(tri64);
+        g._pad = 0;
+        g.desc = meshes[i]->d_desc;
+        total += tri64;
+        if (total >= (1ull << 31)) return fail(LCX_ERR_INVALID_ARG, "batch too large (%llu triangles)",
+                                               (unsigned long long)total);
+    }
+    const BuildParams bp = build_params_for(meshes[0]->opt);
+    if (total == 0) {
+        LCX_CUDA(cudaStreamSynchronize(st), "sync");
+        for (MeshObj *m : meshes) {
+            LCX_CUDA(cudaMemset(m->d_desc, 0, sizeof(BlasDesc)), "cudaMemset(BlasDesc)");
+            m->block.reset();
+            m->wide_sah = nullptr;
+            m->mem_bytes = 0;
+            m->node_count = m->tri_count = m->depth = 0;
+            m->sah = 0.0;
+            m->built = true;
+            m->generation++;
+        }
+        return LCX_OK;
+    }
+    const uint32_t n = uint32_t(total);
+    BuildReadback rb;
+    std::shared_ptr<DevBlock> block;
+    {
+        ScratchHolder hold(st);
+        BuildScratch s;
+        if (int r = alloc_scratch(hold, s, segs, n, false)) return r;
+        LCX_CUDA(build_tree_tris(s, bp, st), "BLAS build");
+        if (int r = read_back(s, st, rb)) return r;
+        if (rb.ctl[kCtlErr] & kErrBadIndex) {
+            for (size_t i = 0; i < count; i++)
+                if (rb.segctl[kSegWords * i + kSegErr] & kErrBadIndex)
+                    return fail(LCX_ERR_INVALID_ARG, "mesh %zu of the build: triangle index out of range (vertex count %u)",
+                                i, segs[i].vcount);
+            return fail(LCX_ERR_INVALID_ARG, "triangle index out of range");
+        }
+        if (rb.ctl[kCtlErr] & kErrTooDeep) return fail(LCX_ERR_DEPTH, "BVH deeper than %d levels", kMaxLevels);
+        for (size_t i = 0; i < count; i++)
+            if (rb.segctl[kSegWords * i + kSegItems] != segs[i].item_count)
+                return fail(LCX_ERR_CUDA, "BLAS build placed %u of %u triangles of mesh %zu",
+                            rb.segctl[kSegWords * i + kSegItems], segs[i].item_count, i);
+        const uint32_t W = rb.ctl[kCtlWideCount];
+        const size_t q_bytes = size_t(W) * sizeof(Node8Q), f_bytes = size_t(W) * sizeof(Node8F);
+        const size_t t_bytes = size_t(n) * sizeof(TriRec), sah_bytes = 2 * sizeof(double) * count;
+        block = std::make_shared<DevBlock>();
+        block->bytes = q_bytes + f_bytes + t_bytes + sah_bytes;
+        LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(BLAS)");
+        Node8Q *qn = static_cast<Node8Q *>(block->ptr);
+        Node8F *fn = reinterpret_cast<Node8F *>(reinterpret_cast<char *>(block->ptr) + q_bytes);
+        TriRec *tr = reinterpret_cast<TriRec *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes);
+        double *wsah = reinterpret_cast<double *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes + t_bytes);
+        LCX_CUDA(cudaMemsetAsync(wsah, 0, sah_bytes, st), "cudaMemset");
+        LCX_CUDA(emit_blas(s, bp, W, qn, fn, tr, wsah, st), "BLAS emit");
+        for (size_t i = 0; i < count; i++) {
+            MeshObj *m = meshes[i];
+            const uint32_t *sc = &rb.segctl[kSegWords * i];
+            m->wide_sah = wsah + 2 * i;
+            m->node_count = segs[i].item_count ? sc[kSegNodes] : 0u;
+            m->tri_count = segs[i].item_count;
+            m->depth = segs[i].item_count ? sc[kSegDepth] : 0u;
+            m->mem_bytes = size_t(m->node_count) * (sizeof(Node8Q) + sizeof(Node8F)) + size_t(m->tri_count) * sizeof(TriRec);
+            const double ra = rb.bin_sah[2 * i + 1];
+            m->sah = ra > 0.0 ? rb.bin_sah[2 * i] / ra : 0.0;
+        }
+    }
+    // the old blocks are released only after the new BLASes are enqueued; a
+    // block shared with other meshes lives on until they are rebuilt too
+    for (MeshObj *m : meshes) {
+        m->block = block;
+        m->built = true;
+        m->generation++;
+    }
+    if (rb.ctl[kCtlErr] & kErrQuant) return fail(LCX_ERR_INVALID_ARG, "vertex coordinates too large to quantise");
+    return LCX_OK;
+}
 
 // Traversal knobs (see lcx_set_trace_tuning).
 struct TraceTuning {
@@ -286,9 +450,8 @@ int lcx_mesh_destroy(uint64_t mesh) {
     }
     std::lock_guard<std::mutex> lk(m->mtx);
     cudaDeviceSynchronize();  // the BVH may be in use by queued work
-    if (m->d_mem) cudaFree(m->d_mem);
+    m->block.reset();
     if (m->d_desc) cudaFree(m->d_desc);
-    m->d_mem = nullptr;
     m->d_desc = nullptr;
     return LCX_OK;
 }
@@ -297,87 +460,30 @@ int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *cmd, void *stream) 
     auto m = find_mesh(mesh);
     if (!m) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build: unknown mesh handle %llu", (unsigned long long)mesh);
     if (!cmd) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build: command is null");
-    // src/runtime/rtx/mesh.cpp:41-50 and :33-39
-    if (cmd->request > LCX_REQUEST_FORCE_BUILD) return fail(LCX_ERR_INVALID_ARG, "invalid build request %u", cmd->request);
-    if (cmd->vertex_stride == 0 || cmd->vertex_stride % 16 != 0)
-        return fail(LCX_ERR_INVALID_ARG, "Vertex stride must be aligned to 16 bytes (got %zu).", cmd->vertex_stride);
-    if (cmd->vertex_buffer_offset % cmd->vertex_stride != 0 || cmd->vertex_buffer_size % cmd->vertex_stride != 0)
-        return fail(LCX_ERR_INVALID_ARG, "vertex buffer offset %zu / size %zu not aligned to vertex stride %zu",
-                    cmd->vertex_buffer_offset, cmd->vertex_buffer_size, cmd->vertex_stride);
-    if (cmd->triangle_buffer_offset % 4 != 0 || cmd->triangle_buffer_size % 12 != 0)
-        return fail(LCX_ERR_INVALID_ARG, "triangle buffer offset %zu / size %zu not aligned (4 / 12 bytes)",
-                    cmd->triangle_buffer_offset, cmd->triangle_buffer_size);
-    const uint64_t tri64 = cmd->triangle_buffer_size / 12;
-    const uint64_t vcount64 = cmd->vertex_buffer_size / cmd->vertex_stride;
-    if (tri64 >= (1ull << 31) || vcount64 >= (1ull << 32))
-        return fail(LCX_ERR_INVALID_ARG, "mesh too large (%llu triangles, %llu vertices)", (unsigned long long)tri64,
-                    (unsigned long long)vcount64);
-    if (tri64 && (cmd->vertex_buffer == 0 || cmd->triangle_buffer == 0))
-        return fail(LCX_ERR_INVALID_ARG, "null vertex or triangle buffer");
-    if ((cmd->vertex_buffer + cmd->vertex_buffer_offset) % 16 != 0 || (cmd->triangle_buffer % 4) != 0)
-        return fail(LCX_ERR_INVALID_ARG, "vertex buffer must be 16-byte aligned, triangle buffer 4-byte aligned");
-    const uint32_t n = uint32_t(tri64);
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     std::lock_guard<std::mutex> lk(m->mtx);
-    if (n == 0) {
-        LCX_CUDA(cudaStreamSynchronize(st), "sync");
-        if (m->d_mem) cudaFree(m->d_mem);
-        m->d_mem = nullptr;
-        m->mem_bytes = 0;
-        m->node_count = m->tri_count = m->depth = 0;
-        m->fnodes = nullptr;
-        m->sah = 0.0;
-        LCX_CUDA(cudaMemset(m->d_desc, 0, sizeof(BlasDesc)), "cudaMemset(BlasDesc)");
-        m->built = true;
-        m->generation++;
-        return LCX_OK;
+    return build_meshes({m.get()}, cmd, static_cast<cudaStream_t>(stream));
+}
+
+int lcx_mesh_build_batch(const uint64_t *meshes, const LcxMeshBuildCommand *cmds, uint32_t count, void *stream) {
+    if (count == 0) return LCX_OK;
+    if (!meshes || !cmds) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build_batch: null arguments");
+    std::vector<std::shared_ptr<MeshObj>> objs(count);
+    for (uint32_t i = 0; i < count; i++) {
+        objs[i] = find_mesh(meshes[i]);
+        if (!objs[i]) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build_batch: unknown mesh handle %llu (entry %u)",
+                                  (unsigned long long)meshes[i], i);
     }
-    TriInput in;
-    in.vbase = reinterpret_cast<const unsigned char *>(cmd->vertex_buffer) + cmd->vertex_buffer_offset;
-    in.vstride = cmd->vertex_stride;
-    in.vcount = uint32_t(vcount64);
-    in.tbase = reinterpret_cast<const unsigned char *>(cmd->triangle_buffer) + cmd->triangle_buffer_offset;
-    const int leaf_max = leaf_items_for(m->opt);
-    CtlReadback rb;
-    {
-        ScratchHolder hold(st);
-        BuildScratch s;
-        if (int r = alloc_scratch(hold, s, n, false)) return r;
-        uint32_t h_ctl[kCtlWords];
-        if (int r = init_ctl(s, st, h_ctl)) return r;
-        LCX_CUDA(build_tree_tris(in, n, leaf_max, s, st), "BLAS build");
-        LCX_CUDA(binary_sah(s, n, st), "BLAS SAH");
-        if (int r = read_ctl(s, st, rb)) return r;
-        if (rb.words[kCtlErr] & kErrBadIndex)
-            return fail(LCX_ERR_INVALID_ARG, "triangle index out of range (vertex count %u)", in.vcount);
-        if (rb.words[kCtlErr] & kErrTooDeep) return fail(LCX_ERR_DEPTH, "BVH deeper than %d levels", kMaxLevels);
-        if (rb.words[kCtlItemCount] != n)
-            return fail(LCX_ERR_CUDA, "BLAS build placed %u of %u triangles", rb.words[kCtlItemCount], n);
-        const uint32_t W = rb.words[kCtlWideCount];
-        const size_t bytes = size_t(W) * (sizeof(Node8Q) + sizeof(Node8F)) + size_t(n) * sizeof(TriRec);
-        void *mem = nullptr;
-        LCX_CUDA(cudaStreamSynchronize(st), "sync");
-        if (m->d_mem) {
-            cudaFree(m->d_mem);
-            m->d_mem = nullptr;
-        }
-        LCX_CUDA(cudaMalloc(&mem, bytes), "cudaMalloc(BLAS)");
-        Node8Q *qn = static_cast<Node8Q *>(mem);
-        Node8F *fn = reinterpret_cast<Node8F *>(qn + W);
-        TriRec *tr = reinterpret_cast<TriRec *>(fn + W);
-        LCX_CUDA(emit_blas(in, n, leaf_max, W, s, qn, fn, tr, m->d_desc, st), "BLAS emit");
-        m->d_mem = mem;
-        m->mem_bytes = bytes;
-        m->node_count = W;
-        m->tri_count = n;
-        m->depth = rb.words[kCtlDepth];
-        m->fnodes = fn;
-        m->sah = rb.sah[1] > 0.0 ? rb.sah[0] / rb.sah[1] : 0.0;
-    }
-    if (rb.words[kCtlErr] & kErrQuant) return fail(LCX_ERR_INVALID_ARG, "vertex coordinates too large to quantise");
-    m->built = true;
-    m->generation++;
-    return LCX_OK;
+    // lock in address order (no deadlock with concurrent batches); duplicates are an error
+    std::vector<MeshObj *> order(count);
+    for (uint32_t i = 0; i < count; i++) order[i] = objs[i].get();
+    std::vector<MeshObj *> sorted = order;
+    std::sort(sorted.begin(), sorted.end());
+    for (uint32_t i = 1; i < count; i++)
+        if (sorted[i] == sorted[i - 1]) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build_batch: a mesh appears twice");
+    std::vector<std::unique_lock<std::mutex>> locks;
+    locks.reserve(count);
+    for (MeshObj *m : sorted) locks.emplace_back(m->mtx);
+    return build_meshes(order, cmds, static_cast<cudaStream_t>(stream));
 }
 
 int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out) {
@@ -391,14 +497,9 @@ int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out) {
     out->device_bytes = m->mem_bytes + sizeof(BlasDesc);
     out->depth = m->depth;
     out->sah_cost = m->sah;
-    if (m->node_count) {
-        double *d = nullptr;
-        LCX_CUDA(cudaMalloc(&d, 2 * sizeof(double)), "cudaMalloc");
+    if (m->wide_sah) {
         double h[2] = {0, 0};
-        cudaError_t e = wide_sah(m->fnodes, m->node_count, d, 0);
-        if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
-        cudaFree(d);
-        if (e != cudaSuccess) return cuda_fail(e, "wide SAH");
+        LCX_CUDA(cudaMemcpy(h, m->wide_sah, sizeof(h), cudaMemcpyDeviceToHost), "wide SAH readback");
         out->wide_sah_cost = h[1] > 0.0 ? h[0] / h[1] : 0.0;
     }
     return LCX_OK;
@@ -434,9 +535,8 @@ int lcx_accel_destroy(uint64_t accel) {
     }
     std::lock_guard<std::mutex> lk(a->mtx);
     cudaDeviceSynchronize();
-    if (a->d_mem) cudaFree(a->d_mem);
+    a->block.reset();
     if (a->d_inst) cudaFree(a->d_inst);
-    a->d_mem = nullptr;
     a->d_inst = nullptr;
     return LCX_OK;
 }
@@ -491,9 +591,9 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
         a->inst_cap = cap;
     }
     if (instance_count > a->inst_count) LCX_CUDA(init_instances(a->d_inst, a->inst_count, instance_count, st), "init");
-    a->inst_count = instance_count;
     a->inst_mesh.resize(instance_count, 0);
-    for (uint32_t i = uint32_t(a->inst_mesh.size()); i < instance_count; i++) a->inst_mesh[i] = 0;
+    for (uint32_t i = a->inst_count; i < instance_count; i++) a->inst_mesh[i] = 0;
+    a->inst_count = instance_count;
     for (size_t i = 0; i < mod_count; i++)
         if (new_mesh[i]) a->inst_mesh[recs[i].index] = new_mesh[i];
     if (mod_count) {
@@ -506,42 +606,44 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     }
     if (update_instance_buffer_only) return LCX_OK;
 
-    // TLAS build
+    // TLAS build: one segment of instances, one instance per leaf slot
     const uint32_t n = instance_count;
-    CtlReadback rb;
+    BuildParams bp = build_params_for(a->opt);
+    bp.leaf_max = 1;
+    BuildReadback rb;
+    std::shared_ptr<DevBlock> block;
     {
         ScratchHolder hold(st);
         BuildScratch s;
-        if (int r = alloc_scratch(hold, s, n, true)) return r;
-        uint32_t h_ctl[kCtlWords];
-        if (int r = init_ctl(s, st, h_ctl)) return r;
-        LCX_CUDA(build_tree_insts(a->d_inst, n, 1, s, st), "TLAS build");
-        LCX_CUDA(binary_sah(s, n, st), "TLAS SAH");
-        if (int r = read_ctl(s, st, rb)) return r;
-        if (rb.words[kCtlErr] & kErrTooDeep) return fail(LCX_ERR_DEPTH, "TLAS deeper than %d levels", kMaxLevels);
-        if (rb.words[kCtlItemCount] != n)
-            return fail(LCX_ERR_CUDA, "TLAS build placed %u of %u instances", rb.words[kCtlItemCount], n);
-        const uint32_t W = rb.words[kCtlWideCount];
-        const size_t bytes = size_t(W) * (sizeof(Node8Q) + sizeof(Node8F)) + size_t(n) * sizeof(InstRec);
-        if (a->d_mem) {
-            cudaFree(a->d_mem);
-            a->d_mem = nullptr;
-        }
-        void *mem = nullptr;
-        LCX_CUDA(cudaMalloc(&mem, bytes), "cudaMalloc(TLAS)");
-        Node8Q *qn = static_cast<Node8Q *>(mem);
-        Node8F *fn = reinterpret_cast<Node8F *>(qn + W);
-        InstRec *ir = reinterpret_cast<InstRec *>(fn + W);
-        LCX_CUDA(emit_tlas(a->d_inst, n, 1, W, s, qn, fn, ir, st), "TLAS emit");
-        a->d_mem = mem;
-        a->mem_bytes = bytes;
+        std::vector<SegInput> segs(1);
+        segs[0] = SegInput{nullptr, 0, nullptr, 0, 0, n, 0, nullptr};
+        if (int r = alloc_scratch(hold, s, segs, n, true)) return r;
+        LCX_CUDA(build_tree_insts(a->d_inst, s, bp, st), "TLAS build");
+        if (int r = read_back(s, st, rb)) return r;
+        if (rb.ctl[kCtlErr] & kErrTooDeep) return fail(LCX_ERR_DEPTH, "TLAS deeper than %d levels", kMaxLevels);
+        if (rb.segctl[kSegItems] != n)
+            return fail(LCX_ERR_CUDA, "TLAS build placed %u of %u instances", rb.segctl[kSegItems], n);
+        const uint32_t W = rb.ctl[kCtlWideCount];
+        const size_t q_bytes = size_t(W) * sizeof(Node8Q), f_bytes = size_t(W) * sizeof(Node8F);
+        const size_t r_bytes = size_t(n) * sizeof(InstRec);
+        block = std::make_shared<DevBlock>();
+        block->bytes = q_bytes + f_bytes + r_bytes + 2 * sizeof(double);
+        LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(TLAS)");
+        Node8Q *qn = static_cast<Node8Q *>(block->ptr);
+        Node8F *fn = reinterpret_cast<Node8F *>(reinterpret_cast<char *>(block->ptr) + q_bytes);
+        InstRec *ir = reinterpret_cast<InstRec *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes);
+        double *wsah = reinterpret_cast<double *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes + r_bytes);
+        LCX_CUDA(cudaMemsetAsync(wsah, 0, 2 * sizeof(double), st), "cudaMemset");
+        LCX_CUDA(emit_tlas(a->d_inst, s, bp, W, qn, fn, ir, wsah, st), "TLAS emit");
         a->qn = qn;
         a->fn = fn;
         a->recs = ir;
+        a->wide_sah = wsah;
         a->node_count = W;
-        a->depth = rb.words[kCtlDepth];
-        a->sah = rb.sah[1] > 0.0 ? rb.sah[0] / rb.sah[1] : 0.0;
+        a->depth = rb.segctl[kSegDepth];
+        a->sah = rb.bin_sah[1] > 0.0 ? rb.bin_sah[0] / rb.bin_sah[1] : 0.0;
     }
+    a->block = block;
     // remember which mesh builds this TLAS references
     a->mesh_gens.clear();
     a->max_blas_depth = 0;
@@ -570,20 +672,30 @@ int lcx_accel_stats(uint64_t accel, LcxAccelStats *out) {
     std::memset(out, 0, sizeof(*out));
     out->node_count = a->node_count;
     out->leaf_prim_count = a->built_instances;
-    out->device_bytes = a->mem_bytes + sizeof(InstState) * a->inst_cap;
+    out->device_bytes = (a->block ? a->block->bytes : 0) + sizeof(InstState) * a->inst_cap;
     out->depth = a->depth;
     out->max_blas_depth = a->max_blas_depth;
     out->sah_cost = a->sah;
-    if (a->node_count) {
-        double *d = nullptr;
-        LCX_CUDA(cudaMalloc(&d, 2 * sizeof(double)), "cudaMalloc");
+    if (a->wide_sah) {
         double h[2] = {0, 0};
-        cudaError_t e = wide_sah(a->fn, a->node_count, d, 0);
-        if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
-        cudaFree(d);
-        if (e != cudaSuccess) return cuda_fail(e, "wide SAH");
+        LCX_CUDA(cudaMemcpy(h, a->wide_sah, sizeof(h), cudaMemcpyDeviceToHost), "wide SAH readback");
         out->wide_sah_cost = h[1] > 0.0 ? h[0] / h[1] : 0.0;
     }
+    return LCX_OK;
+}
+
+int lcx_set_build_tuning(uint32_t leaf_max, uint32_t width) {
+    if (leaf_max > 3 || width < 2 || width > 8)
+        return fail(LCX_ERR_INVALID_ARG, "build tuning out of range (leaf_max 0..3, width 2..8)");
+    g_build_tune.leaf_max = int(leaf_max);
+    g_build_tune.width = int(width);
+    return LCX_OK;
+}
+
+int lcx_get_build_tuning(uint32_t *leaf_max, uint32_t *width) {
+    if (!leaf_max || !width) return fail(LCX_ERR_INVALID_ARG, "null output");
+    *leaf_max = uint32_t(g_build_tune.leaf_max);
+    *width = uint32_t(g_build_tune.width);
     return LCX_OK;
 }
 

@@ -11,37 +11,38 @@
 
 namespace lcx {
 
-// Per-build device scratch, sized for `n` items.
-struct BuildScratch {
-    float4 *box_lo = nullptr;        // n   item boxes
-    float4 *box_hi = nullptr;        // n
-    unsigned long long *keys = nullptr;  // n   Morton keys
-    unsigned long long *keys_sorted = nullptr;
-    uint32_t *vals = nullptr;        // n   item ids
-    uint32_t *vals_sorted = nullptr;
-    uint32_t *bin_child = nullptr;   // 2(n-1)
-    float4 *bin_lo = nullptr;        // n-1 (w = count bits)
-    float4 *bin_hi = nullptr;        // n-1 (w = first bits)
-    int32_t *other = nullptr;        // n-1
-    uint32_t *desc = nullptr;        // (n+1) * 12 words
-    uint2 *queue = nullptr;          // 2 (n+1)
-    float *w2o = nullptr;            // TLAS: 12 n
-    uint32_t *ctl = nullptr;         // control words (see build.cu)
-    void *sort_tmp = nullptr;
-    size_t sort_tmp_bytes = 0;
+// One BVH of a build: a mesh's triangles (BLAS) or a TLAS's instances.
+struct SegInput {
+    const unsigned char *vbase;  // vertex buffer + offset (BLAS)
+    uint64_t vstride;
+    const unsigned char *tbase;  // triangle buffer + offset (BLAS)
+    uint32_t vcount;
+    uint32_t item_offset;        // first item of this segment among all items of the build
+    uint32_t item_count;
+    uint32_t _pad;
+    BlasDesc *desc;              // BLAS descriptor the emit fills in (null for a TLAS)
+};
+static_assert(sizeof(SegInput) == 48, "SegInput is 48 B");
+
+// Per-segment control words.
+enum : int {
+    kSegCenLo = 0,  // 3 ordered-uint words
+    kSegCenHi = 3,  // 3 ordered-uint words
+    kSegRoot = 6,
+    kSegItems = 7,
+    kSegNodes = 8,
+    kSegDepth = 9,
+    kSegErr = 10,
+    kSegWords = 12,
 };
 
-// Control block layout (uint32 words).
+// Global control words.
 enum : int {
     kCtlWideCount = 0,
-    kCtlItemCount = 1,
-    kCtlDepth = 2,
-    kCtlErr = 3,
-    kCtlRoot = 4,
-    kCtlCenLo = 8,    // 3 ordered-uint words
-    kCtlCenHi = 12,   // 3 ordered-uint words
-    kCtlLevel = 16,   // kMaxLevels + 1 words
-    kCtlWords = 16 + kMaxLevels + 2,
+    kCtlDepth = 1,
+    kCtlErr = 2,
+    kCtlLevel = 4,  // kMaxLevels + 1 words
+    kCtlWords = 4 + kMaxLevels + 4,
 };
 
 enum : uint32_t {
@@ -50,38 +51,59 @@ enum : uint32_t {
     kErrQuant = 4u,
 };
 
-size_t sort_temp_bytes(uint32_t n);
-cudaError_t sort_pairs(void *tmp, size_t tmp_bytes, const unsigned long long *kin, unsigned long long *kout,
-                       const uint32_t *vin, uint32_t *vout, uint32_t n, cudaStream_t s);
-
-struct TriInput {
-    const unsigned char *vbase;  // vertex buffer + offset
-    size_t vstride;
-    uint32_t vcount;
-    const unsigned char *tbase;  // triangle buffer + offset
+struct BuildParams {
+    int leaf_max = 2;  // items per leaf slot, 1..3
+    int width = 8;     // children per wide node, 2..8
 };
 
-// Phase 1: item boxes + Morton keys + sort + LBVH + collapse.  Leaves
-// ctl words on the device; the caller reads wide/item counts back.
-cudaError_t build_tree_tris(const TriInput &in, uint32_t n, int leaf_max, BuildScratch &s, cudaStream_t st);
-cudaError_t build_tree_insts(const InstState *inst, uint32_t n, int leaf_max, BuildScratch &s, cudaStream_t st);
+// Per-build device scratch, sized for n items in nseg segments.
+struct BuildScratch {
+    uint32_t n = 0, nseg = 0;
+    uint32_t axis_bits = 21, seg_bits = 0;  // Morton bits per axis, segment-id bits above them
+    uint32_t queue_len = 0;
+    const SegInput *segs = nullptr;  // nseg
+    uint32_t *segctl = nullptr;      // nseg * kSegWords
+    double *bin_sah = nullptr;       // 2 nseg: binary-tree SAH sums and root areas
+    float4 *box_lo = nullptr;        // n item boxes
+    float4 *box_hi = nullptr;
+    unsigned long long *keys = nullptr;  // n keys
+    unsigned long long *keys_sorted = nullptr;
+    uint32_t *vals = nullptr;  // n item ids
+    uint32_t *vals_sorted = nullptr;
+    uint32_t *bin_child = nullptr;  // 2 n
+    float4 *bin_lo = nullptr;       // n (w = count bits)
+    float4 *bin_hi = nullptr;       // n (w = first bits)
+    int32_t *other = nullptr;       // n
+    uint32_t *desc = nullptr;       // queue_len * 12 words
+    uint2 *queue = nullptr;         // 2 queue_len
+    float *w2o = nullptr;           // TLAS: 12 n
+    uint32_t *ctl = nullptr;        // kCtlWords
+    void *sort_tmp = nullptr;
+    size_t sort_tmp_bytes = 0;
+};
 
-// Phase 2: write both node layouts and the leaf items.
-cudaError_t emit_blas(const TriInput &in, uint32_t n, int leaf_max, uint32_t wide_count, const BuildScratch &s,
-                      Node8Q *qn, Node8F *fn, TriRec *tris, BlasDesc *desc, cudaStream_t st);
-cudaError_t emit_tlas(const InstState *inst, uint32_t n, int leaf_max, uint32_t wide_count, const BuildScratch &s,
-                      Node8Q *qn, Node8F *fn, InstRec *recs, cudaStream_t st);
+size_t sort_temp_bytes(uint32_t n);
+cudaError_t sort_pairs(void *tmp, size_t tmp_bytes, const unsigned long long *kin, unsigned long long *kout,
+                       const uint32_t *vin, uint32_t *vout, uint32_t n, uint32_t end_bit, cudaStream_t s);
+
+// Morton bits per axis for nseg segments; *seg_bits receives the bits of the segment id.
+uint32_t morton_axis_bits(uint32_t nseg, uint32_t *seg_bits);
+
+// Phase 1: item boxes + keys + sort + LBVH + collapse of every segment.  The
+// caller reads ctl (wide node count, errors) and segctl back.
+cudaError_t build_tree_tris(BuildScratch &s, const BuildParams &bp, cudaStream_t st);
+cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const BuildParams &bp, cudaStream_t st);
+
+// Phase 2: write both node layouts and the leaf items; wide_sah (2 nseg
+// doubles, zeroed by the caller, may be null) receives the per-segment wide SAH.
+cudaError_t emit_blas(const BuildScratch &s, const BuildParams &bp, uint32_t wide_count, Node8Q *qn, Node8F *fn,
+                      TriRec *tris, double *wide_sah, cudaStream_t st);
+cudaError_t emit_tlas(const InstState *inst, const BuildScratch &s, const BuildParams &bp, uint32_t wide_count,
+                      Node8Q *qn, Node8F *fn, InstRec *recs, double *wide_sah, cudaStream_t st);
 
 cudaError_t apply_modifications(const ModRec *mods, uint32_t count, InstState *inst, uint32_t instance_count,
                                 cudaStream_t st);
 cudaError_t init_instances(InstState *inst, uint32_t begin, uint32_t end, cudaStream_t st);
-
-// SAH of the binary tree of the last build_tree_* call (written after the
-// control words; read back with them).
-cudaError_t binary_sah(const BuildScratch &s, uint32_t n, cudaStream_t st);
-
-// Wide-tree SAH (C_node = 1, C_item = 1, normalised by the root area).
-cudaError_t wide_sah(const Node8F *fn, uint32_t wide_count, double *d_out, cudaStream_t st);
 
 // Traversal.
 struct TraceParams {

@@ -16,9 +16,9 @@ size_t sort_temp_bytes(uint32_t n) {
 }
 
 cudaError_t sort_pairs(void *tmp, size_t tmp_bytes, const unsigned long long *kin, unsigned long long *kout,
-                       const uint32_t *vin, uint32_t *vout, uint32_t n, cudaStream_t s) {
+                       const uint32_t *vin, uint32_t *vout, uint32_t n, uint32_t end_bit, cudaStream_t s) {
     size_t bytes = tmp_bytes;
-    return cub::DeviceRadixSort::SortPairs(tmp, bytes, kin, kout, vin, vout, int(n), 0, 63, s);
+    return cub::DeviceRadixSort::SortPairs(tmp, bytes, kin, kout, vin, vout, int(n), 0, int(end_bit), s);
 }
 
 }  // namespace lcx
