@@ -73,8 +73,21 @@ def _pad_vertices(v3: np.ndarray) -> np.ndarray:
     return v
 
 
+_ICO_CACHE: dict = {}
+
+
 def icosphere(subdiv: int, radius: float = 1.0) -> MeshData:
     """Icosahedron subdivided ``subdiv`` times: 20*4^s triangles, 10*4^s+2 vertices."""
+    if radius == 1.0 and subdiv in _ICO_CACHE:
+        v, f = _ICO_CACHE[subdiv]
+        return MeshData(v.copy(), f.copy())
+    m = _icosphere(subdiv, radius)
+    if radius == 1.0:
+        _ICO_CACHE[subdiv] = (m.vertices.copy(), m.triangles.copy())
+    return m
+
+
+def _icosphere(subdiv: int, radius: float) -> MeshData:
     t = (1.0 + 5.0 ** 0.5) / 2.0
     v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
                   [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
@@ -281,8 +294,8 @@ def displaced_mesh(tri_target: int, rng: np.random.Generator) -> MeshData:
         ny = max(2, int(round(cells / (nx - 1))) + 1)
         m = grid_mesh(nx, ny)
         extent = 2.0
-    v = m.vertices.copy()
-    v[:, :3] += rng.normal(0.0, 0.01 * extent, (v.shape[0], 3)).astype(np.float32)
+    v = m.vertices
+    v[:, :3] += (rng.standard_normal((v.shape[0], 3), dtype=np.float32) * np.float32(0.01 * extent))
     return MeshData(v, m.triangles)
 
 
