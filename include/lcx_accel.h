@@ -226,6 +226,26 @@ LCX_API int lcx_trace_closest(uint64_t accel, const LcxRay *d_rays, uint32_t ray
 LCX_API int lcx_trace_any(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count,
                   uint32_t mask, uint8_t *d_occluded, void *stream);
 
+/* One ray batch of a multi-job launch: `ray_count` rays against `accel`,
+ * written to `out` (LcxTriangleHit[] when any == 0, uint8_t[] when any != 0). */
+typedef struct LcxTraceJob {
+    uint64_t accel;
+    const LcxRay *rays;
+    void *out;
+    uint32_t ray_count;
+    uint32_t mask;
+    uint32_t any;
+    uint32_t _pad;
+} LcxTraceJob;
+
+/* Many ray batches against many accels in one launch per query kind
+ * (continuous batching; no counterpart in the reference, whose queries run
+ * inside one user kernel per dispatch).  Persistent warps take global ray
+ * indices and each lane serves its ray's job, so jobs of any size and scene
+ * share the GPU.  Results equal one lcx_trace_closest / lcx_trace_any call
+ * per job.  At most 2^31 rays per kind. */
+LCX_API int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout, void *stream);
+
 /* Same queries with an explicit node layout (LCX_NODES_FP32 or
  * LCX_NODES_QUANT8); lcx_trace_closest/any use LCX_NODES_QUANT8. */
 LCX_API int lcx_trace_closest_ex(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count,

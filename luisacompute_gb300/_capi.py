@@ -39,6 +39,11 @@ class LcxMeshBuildCommand(ctypes.Structure):
                 ("triangle_buffer_size", c_size_t)]
 
 
+class LcxTraceJob(ctypes.Structure):
+    _fields_ = [("accel", c_uint64), ("rays", c_void_p), ("out", c_void_p), ("ray_count", c_uint32),
+                ("mask", c_uint32), ("any", c_uint32), ("_pad", c_uint32)]
+
+
 class LcxAccelStats(ctypes.Structure):
     _fields_ = [("node_count", c_uint64), ("leaf_prim_count", c_uint64), ("device_bytes", c_uint64),
                 ("depth", c_uint32), ("max_blas_depth", c_uint32), ("sah_cost", c_double),
@@ -68,6 +73,7 @@ _SIGS = {
                                          c_void_p]),
     "lcx_set_trace_tuning": (c_int, [c_uint32, c_uint32, c_uint32]),
     "lcx_check_trace_errors": (c_int, []),
+    "lcx_trace_jobs": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p]),
     "lcx_trace_closest_noalloc": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p]),
     "lcx_get_trace_tuning": (c_int, [POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
 }

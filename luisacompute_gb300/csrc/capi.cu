@@ -756,6 +756,73 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     return LCX_OK;
 }
 
+int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout, void *stream) {
+    if (count == 0) return LCX_OK;
+    if (!jobs) return fail(LCX_ERR_INVALID_ARG, "lcx_trace_jobs: jobs is null");
+    if (node_layout > LCX_NODES_QUANT8) return fail(LCX_ERR_INVALID_ARG, "invalid node layout %u", node_layout);
+    std::vector<DevJob> groups[2];  // [0] closest, [1] any
+    uint64_t totals[2] = {0, 0};
+    uint32_t depth_need = 0;
+    for (uint32_t i = 0; i < count; i++) {
+        const LcxTraceJob &j = jobs[i];
+        if (j.ray_count == 0) continue;
+        if (!j.rays || !j.out) return fail(LCX_ERR_INVALID_ARG, "job %u: null ray or result buffer", i);
+        if (reinterpret_cast<uintptr_t>(j.rays) % 16 != 0 || (!j.any && reinterpret_cast<uintptr_t>(j.out) % 8 != 0))
+            return fail(LCX_ERR_INVALID_ARG, "job %u: rays must be 16-byte and hits 8-byte aligned", i);
+        auto a = find_accel(j.accel);
+        if (!a) return fail(LCX_ERR_INVALID_ARG, "job %u: unknown accel handle %llu", i, (unsigned long long)j.accel);
+        std::lock_guard<std::mutex> lk(a->mtx);
+        if (!a->built) return fail(LCX_ERR_NOT_BUILT, "job %u: accel not built", i);
+        for (const auto &mg : a->mesh_gens) {
+            auto m = find_mesh(mg.first);
+            if (!m || m->generation != mg.second)
+                return fail(LCX_ERR_NOT_BUILT, "job %u: a mesh of the accel was destroyed or rebuilt; rebuild the accel",
+                            i);
+        }
+        const uint32_t need = a->depth + a->max_blas_depth + 3;
+        if (int(need) > kStackSize) return fail(LCX_ERR_DEPTH, "job %u: BVH too deep for the traversal stack", i);
+        depth_need = std::max(depth_need, need);
+        const int g = j.any ? 1 : 0;
+        DevJob d{};
+        d.tlas_q = a->qn;
+        d.tlas_f = a->fn;
+        d.insts = a->recs;
+        d.rays = reinterpret_cast<const Ray *>(j.rays);
+        d.out = j.out;
+        d.first = uint32_t(totals[g]);
+        d.count = j.ray_count;
+        d.mask = j.mask & 0xffu;
+        totals[g] += j.ray_count;
+        if (totals[g] > kMaxTraceRays) return fail(LCX_ERR_INVALID_ARG, "lcx_trace_jobs: more than 2^31 rays");
+        groups[g].push_back(d);
+    }
+    DeviceState *ds = nullptr;
+    if (int r = current_device_state(&ds)) return r;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    for (int g = 0; g < 2; g++) {
+        if (groups[g].empty()) continue;
+        ScratchHolder hold(st);
+        DevJob *d_jobs = nullptr;
+        LCX_CUDA(hold.alloc((void **)&d_jobs, sizeof(DevJob) * groups[g].size()), "job table");
+        LCX_CUDA(cudaMemcpyAsync(d_jobs, groups[g].data(), sizeof(DevJob) * groups[g].size(), cudaMemcpyHostToDevice,
+                                 st),
+                 "job table upload");
+        TraceParams p{};
+        const uint32_t slot = ds->next_slot.fetch_add(1) % kPoolSlots;
+        p.pool = ds->pool + 4 * slot;
+        p.ray_count = uint32_t(totals[g]);
+        p.refill = g_tune.refill;
+        p.postpone = 0;
+        p.postpone_sp = kStackSize - int(depth_need);
+        p.mode = 0;
+        p.jobs = d_jobs;
+        p.job_count = uint32_t(groups[g].size());
+        LCX_CUDA(cudaMemsetAsync(p.pool, 0, 4 * sizeof(uint32_t), st), "trace counter reset");
+        LCX_CUDA(launch_trace(p, int(node_layout), g == 1, false, st), "multi-job trace launch");
+    }
+    return LCX_OK;
+}
+
 int lcx_check_trace_errors(void) {
     DeviceState *ds = nullptr;
     if (int r = current_device_state(&ds)) return r;

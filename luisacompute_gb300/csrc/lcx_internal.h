@@ -106,6 +106,20 @@ cudaError_t apply_modifications(const ModRec *mods, uint32_t count, InstState *i
 cudaError_t init_instances(InstState *inst, uint32_t begin, uint32_t end, cudaStream_t st);
 
 // Traversal.
+// One job of a multi-job trace launch: a ray batch against one TLAS.
+struct __align__(16) DevJob {
+    const Node8Q *tlas_q;
+    const Node8F *tlas_f;
+    const InstRec *insts;
+    const Ray *rays;
+    void *out;       // Hit[] (closest) or uint8_t[] (any)
+    uint32_t first;  // global index of the job's first ray in the launch
+    uint32_t count;
+    uint32_t mask;
+    uint32_t _pad;
+};
+static_assert(sizeof(DevJob) == 56 || sizeof(DevJob) == 64, "DevJob size");
+
 struct TraceParams {
     const Node8Q *tlas_q;
     const Node8F *tlas_f;
@@ -121,6 +135,8 @@ struct TraceParams {
     uint32_t postpone;    // postpone triangle tests when fewer lanes than this would run them (0 = off)
     int32_t postpone_sp;  // postpone only while the stack depth is below this
     uint32_t mode;        // loop structure: 0 = node + its items per step, 1 = speculative while-while
+    const DevJob *jobs;   // non-null: a multi-job launch over job_count jobs (ray_count = their sum)
+    uint32_t job_count;
 };
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st);
 

@@ -147,11 +147,18 @@ __device__ __forceinline__ void intersect_f(const Node8F *nodes, uint32_t idx, f
 }
 
 // Per-lane traversal state and the operations both loop structures share.
-template <int kLayout, bool kAny, bool kCount>
+// kMulti: the launch serves several jobs (scenes); each lane takes its job's
+// TLAS, instance table, mask and buffers when it takes a ray.
+template <int kLayout, bool kAny, bool kCount, bool kMulti = false>
 struct Walker {
     const TraceParams &P;
     uint2 *stk;
     const void *tlas_nodes;
+    const InstRec *insts;
+    const Ray *rays;
+    void *out;
+    uint32_t mask;
+    uint32_t slot = 0;  // ray index within its job
     // world ray
     float wox = 0, woy = 0, woz = 0, wdx = 0, wdy = 0, wdz = 1;
     float tmin = 0, best_t = 0, best_u = 0, best_v = 0;
@@ -171,7 +178,9 @@ struct Walker {
     __device__ Walker(const TraceParams &p, uint2 *s, uint2 *d)
         : P(p), stk(s), deep(d),
           tlas_nodes(kLayout == LCX_NODES_QUANT8 ? static_cast<const void *>(p.tlas_q)
-                                                 : static_cast<const void *>(p.tlas_f)) {}
+                                                 : static_cast<const void *>(p.tlas_f)),
+          insts(p.insts), rays(p.rays),
+          out(kAny ? static_cast<void *>(p.occluded) : static_cast<void *>(p.hits)), mask(p.mask) {}
 
     uint2 *deep;  // local-memory overflow (an array of the kernel, not of this struct,
                   // so that the struct itself stays in registers)
@@ -196,7 +205,26 @@ struct Walker {
     }
 
     __device__ __forceinline__ void start(uint32_t rid) {
-        const float4 *rp = reinterpret_cast<const float4 *>(P.rays + rid);
+        slot = rid;
+        if (kMulti) {  // job of global ray rid: last job whose first ray is <= rid
+            uint32_t lo = 0, hi = P.job_count - 1;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (__ldg(&P.jobs[mid].first) <= rid)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const DevJob &j = P.jobs[lo];
+            tlas_nodes = kLayout == LCX_NODES_QUANT8 ? static_cast<const void *>(j.tlas_q)
+                                                     : static_cast<const void *>(j.tlas_f);
+            insts = j.insts;
+            rays = j.rays;
+            out = j.out;
+            mask = j.mask;
+            slot = rid - j.first;
+        }
+        const float4 *rp = reinterpret_cast<const float4 *>((kMulti ? rays : P.rays) + slot);
         const float4 r0 = __ldcs(rp), r1 = __ldcs(rp + 1);
         wox = r0.x;
         woy = r0.y;
@@ -277,9 +305,9 @@ struct Walker {
         while (Gt.y) {
             const uint32_t k = __ffs(Gt.y) - 1u;
             Gt.y &= Gt.y - 1u;
-            const uint4 *ip = reinterpret_cast<const uint4 *>(P.insts + Gt.x + k);
+            const uint4 *ip = reinterpret_cast<const uint4 *>((kMulti ? insts : P.insts) + Gt.x + k);
             const uint4 m4 = __ldg(ip + 4);  // fnodes (x,y), inst_id (z), mask (w)
-            if ((m4.w & P.mask) == 0u) continue;
+            if ((m4.w & (kMulti ? mask : P.mask)) == 0u) continue;
             const float4 r0 = __ldg(reinterpret_cast<const float4 *>(ip));
             const float4 r1 = __ldg(reinterpret_cast<const float4 *>(ip + 1));
             const float4 r2 = __ldg(reinterpret_cast<const float4 *>(ip + 2));
@@ -321,10 +349,11 @@ struct Walker {
     }
 
     __device__ __forceinline__ void finish(uint32_t rid) {
+        if (kMulti) rid = slot;
         if (kAny) {
-            P.occluded[rid] = occluded ? 1 : 0;
+            (kMulti ? static_cast<uint8_t *>(out) : P.occluded)[rid] = occluded ? 1 : 0;
         } else {
-            uint2 *hp = reinterpret_cast<uint2 *>(P.hits + rid);
+            uint2 *hp = reinterpret_cast<uint2 *>((kMulti ? static_cast<Hit *>(out) : P.hits) + rid);
             __stcs(hp, make_uint2(best_inst, best_prim));
             __stcs(hp + 1, make_uint2(__float_as_uint(best_u), __float_as_uint(best_v)));
             __stcs(hp + 2, make_uint2(__float_as_uint(best_t), 0u));
@@ -341,14 +370,14 @@ struct Walker {
 // kMode 1: speculative while-while (Aila & Laine 2009): lanes walk nodes
 // together; a lane that finds items keeps walking (holding them in Gp) while
 // any lane of the warp is still searching, then all lanes handle items.
-template <int kLayout, bool kAny, bool kCount, int kMode>
+template <int kLayout, bool kAny, bool kCount, int kMode, bool kMulti>
 __global__ void __launch_bounds__(kTraceBlock,
                                   kLayout == LCX_NODES_QUANT8 ? LCX_TRACE_MIN_BLOCKS_Q : LCX_TRACE_MIN_BLOCKS_F)
     k_trace(TraceParams P) {
     __shared__ uint2 stack_mem[kShortStack * kTraceBlock];
     uint2 deep_stack[kDeepSlots];
     const uint32_t lane = threadIdx.x & 31u;
-    Walker<kLayout, kAny, kCount> W(P, stack_mem + threadIdx.x, deep_stack);
+    Walker<kLayout, kAny, kCount, kMulti> W(P, stack_mem + threadIdx.x, deep_stack);
     const int refill = int(P.refill);
     const int postpone = int(P.postpone);
     const int postpone_sp = P.postpone_sp;
@@ -451,12 +480,12 @@ __global__ void __launch_bounds__(kTraceBlock,
     }
 }
 
-template <int L, bool A, bool C, int M>
+template <int L, bool A, bool C, int M, bool X>
 int blocks_per_sm() {
     static int v = 0;
     if (v == 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<L, A, C, M>, kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<L, A, C, M, X>, kTraceBlock, 0);
         v = b > 0 ? b : 1;
     }
     return v;
@@ -473,14 +502,14 @@ int sm_count() {
     return v;
 }
 
-template <int L, bool A, bool C, int M>
+template <int L, bool A, bool C, int M, bool X = false>
 cudaError_t launch_one(const TraceParams &p, cudaStream_t st) {
     const uint64_t warps_needed = (uint64_t(p.ray_count) + 31) / 32;
-    uint64_t grid = uint64_t(sm_count()) * blocks_per_sm<L, A, C, M>();
+    uint64_t grid = uint64_t(sm_count()) * blocks_per_sm<L, A, C, M, X>();
     const uint64_t grid_need = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
     if (grid_need < grid) grid = grid_need;
     if (grid == 0) grid = 1;
-    k_trace<L, A, C, M><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
+    k_trace<L, A, C, M, X><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -499,6 +528,13 @@ cudaError_t launch_mode(const TraceParams &p, int layout, bool any, bool countin
 }  // namespace
 
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
+    if (p.jobs != nullptr) {  // multi-job launches: loop mode 0, no counting
+        if (layout == LCX_NODES_QUANT8)
+            return any ? launch_one<LCX_NODES_QUANT8, true, false, 0, true>(p, st)
+                       : launch_one<LCX_NODES_QUANT8, false, false, 0, true>(p, st);
+        return any ? launch_one<LCX_NODES_FP32, true, false, 0, true>(p, st)
+                   : launch_one<LCX_NODES_FP32, false, false, 0, true>(p, st);
+    }
     return p.mode == 1 ? launch_mode<1>(p, layout, any, counting, st) : launch_mode<0>(p, layout, any, counting, st);
 }
 

@@ -1,0 +1,397 @@
+"""Continuous-batching ray-query serving over HBM-resident scenes.
+
+A request is a batch of rays (closest or any hit) against one scene; some requests bring a new
+scene that must be built before their rays run.  Two servers process the same arrival trace:
+
+* ``ContinuousServer`` — requests that have arrived wait in a queue; whenever one of ``slots``
+  CUDA streams is free, the ready requests (scene resident, FIFO order, up to ``max_batch_rays``)
+  form one batch: their rays are copied in, traced with one ``lcx_trace_jobs`` launch per query
+  kind (each lane of the persistent kernel serves its ray's job), and copied back.  Batches on
+  different streams overlap on the device.  Scene builds run on their own thread and stream, so
+  an upload never blocks admission.  Scenes live in an HBM budget with LRU eviction of scenes
+  no queued or in-flight request needs; an evicted scene is rebuilt on demand.
+* ``PlainServer`` — one request at a time: build if needed, copy in, one trace call, copy out,
+  wait, next.
+
+Latency is arrival -> results in host memory.  No counterpart in the reference (its queries run
+inside one user kernel per dispatch); the scenes, builds and queries are the Mesh/Accel path.
+"""
+from __future__ import annotations
+
+import ctypes
+import queue
+import threading
+import time
+from collections import OrderedDict, deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi
+from . import scenes as S
+from .accel import Accel, mesh_from_data, stream_handle
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float            # seconds after the start of the run
+    scene: int                # scene id
+    rays: np.ndarray          # RAY_DTYPE
+    any_hit: bool
+    new_scene: S.MeshData | None = None  # uploaded (and built) before the rays run
+    # filled in by the server
+    done: float = -1.0
+    result: np.ndarray | None = None
+
+
+@dataclass
+class _Resident:
+    mesh: object
+    accel: Accel
+    nbytes: int
+    pins: int = 0
+
+
+class SceneStore:
+    """Scenes by id: host data always, device BVHs within `budget_bytes` (LRU eviction)."""
+
+    def __init__(self, scenes: dict, budget_bytes: int):
+        self.host = dict(scenes)         # id -> MeshData
+        self.budget = budget_bytes
+        self.res: OrderedDict = OrderedDict()  # id -> _Resident, most recent last
+        self.used = 0
+        self.lock = threading.Lock()
+        self.builds = 0
+        self.evictions = 0
+
+    def warm(self, ids, stream=None) -> None:
+        """Build scenes `ids` (as many as the budget holds) before serving starts."""
+        import torch
+        stream = stream or torch.cuda.current_stream()
+        for sid in ids:
+            self.build(sid, None, stream)
+        torch.cuda.synchronize()
+
+    def resident(self, sid: int) -> bool:
+        with self.lock:
+            return sid in self.res
+
+    def pin(self, sid: int) -> _Resident:
+        """Keep scene `sid` resident until unpin; returns its resident record."""
+        with self.lock:
+            r = self.res[sid]
+            r.pins += 1
+            self.res.move_to_end(sid)
+            return r
+
+    def unpin(self, r: _Resident):
+        with self.lock:
+            r.pins -= 1
+
+    def _evict_for(self, need: int):
+        for sid in list(self.res.keys()):
+            if self.used + need <= self.budget:
+                break
+            r = self.res[sid]
+            if r.pins == 0:
+                del self.res[sid]
+                self.used -= r.nbytes
+                self.evictions += 1
+                r.accel.destroy()
+                r.mesh.destroy()
+
+    def build(self, sid: int, data: S.MeshData | None, stream) -> None:
+        """Upload and build scene `sid` on `stream`; `data` registers a new scene under a new id
+        (scene ids are never reused, so no request races a replacement)."""
+        import torch
+        if data is not None:
+            with self.lock:
+                if sid in self.host:
+                    raise ValueError(f"scene id {sid} already exists")
+                self.host[sid] = data
+        md = self.host[sid]
+        est = md.vertices.nbytes + md.triangles.nbytes + md.tri_count * 110 + (1 << 16)
+        with self.lock:
+            self._evict_for(est)
+        with torch.cuda.stream(stream):
+            mesh = mesh_from_data(md)
+        mesh.build(stream=stream)
+        acc = Accel()
+        acc.emplace_back(mesh)
+        acc.build(stream=stream)
+        nbytes = est  # BVH ~ 2 x 288 B / 11 tris + 48 B per triangle, plus the uploaded buffers
+        with self.lock:
+            self.res[sid] = _Resident(mesh, acc, nbytes)
+            self.used += nbytes
+            self.builds += 1
+
+
+class _Slot:
+    def __init__(self, max_rays: int):
+        import torch
+        self.stream = torch.cuda.Stream()
+        self.rays = torch.empty(max_rays * 8, dtype=torch.float32, device="cuda")
+        self.hits = torch.empty(max_rays * 6, dtype=torch.int32, device="cuda")
+        self.occ = torch.empty(max_rays, dtype=torch.uint8, device="cuda")
+        self.event = None
+        self.batch = []
+
+
+_PIN_CACHE: dict = {}
+
+
+def _pinned(a: np.ndarray):
+    """Pinned host copy of a ray array (shared by the requests that reuse it)."""
+    import torch
+    key = id(a)
+    hit = _PIN_CACHE.get(key)
+    if hit is not None and hit[0] is a:
+        return hit[1]
+    t = torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).pin_memory()
+    _PIN_CACHE[key] = (a, t)
+    return t
+
+
+class ContinuousServer:
+    def __init__(self, store: SceneStore, slots: int = 4, max_batch_rays: int = 1 << 23, layout: int = 1):
+        self.store = store
+        self.lib = _capi.load()
+        self.layout = layout
+        self.max_batch_rays = max_batch_rays
+        self.slots = [_Slot(max_batch_rays) for _ in range(slots)]
+        self.build_q: queue.Queue = queue.Queue()
+        self.built: queue.Queue = queue.Queue()
+        self.batches = 0
+
+    def _builder(self):
+        import torch
+        stream = torch.cuda.Stream()
+        while True:
+            item = self.build_q.get()
+            if item is None:
+                return
+            sid, data = item
+            try:
+                self.store.build(sid, data, stream)
+                torch.cuda.current_stream().wait_stream(stream)
+                stream.synchronize()
+                self.built.put((sid, None))
+            except Exception as e:  # reported to the loop
+                self.built.put((sid, e))
+
+    def run(self, requests: list) -> list:
+        import torch
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        for r in reqs:
+            r._h_rays = _pinned(r.rays)
+            r._h_out = torch.empty(r.rays.shape[0] * (1 if r.any_hit else 24), dtype=torch.uint8).pin_memory()
+        builder = threading.Thread(target=self._builder, daemon=True)
+        builder.start()
+        pending = deque()       # arrived, scene may not be resident yet
+        building = set()        # scene ids being built
+        waiting_new = {}        # scene id -> requests whose new scene is being uploaded
+        nxt = 0
+        done = 0
+        t0 = time.perf_counter()
+        try:
+            while done < len(reqs):
+                progressed = False
+                now = time.perf_counter() - t0
+                # arrivals
+                while nxt < len(reqs) and reqs[nxt].arrival <= now:
+                    r = reqs[nxt]
+                    nxt += 1
+                    if r.new_scene is not None:
+                        waiting_new.setdefault(r.scene, []).append(r)
+                        if r.scene not in building:
+                            building.add(r.scene)
+                            self.build_q.put((r.scene, r.new_scene))
+                    else:
+                        pending.append(r)
+                # finished builds
+                while True:
+                    try:
+                        sid, err = self.built.get_nowait()
+                    except queue.Empty:
+                        break
+                    if err is not None:
+                        raise err
+                    progressed = True
+                    building.discard(sid)
+                    for r in waiting_new.pop(sid, []):
+                        pending.appendleft(r)
+                # completed batches
+                for sl in self.slots:
+                    if sl.event is not None and sl.event.query():
+                        t = time.perf_counter() - t0
+                        for r in sl.batch:
+                            r.done = t
+                            self.store.unpin(r._pin)
+                            done += 1
+                        progressed = True
+                        sl.event = None
+                        sl.batch = []
+                # scenes evicted while queued: rebuild on demand
+                for r in pending:
+                    if not self.store.resident(r.scene) and r.scene not in building:
+                        building.add(r.scene)
+                        self.build_q.put((r.scene, None))
+                # dispatch: one batch per free slot
+                for sl in self.slots:
+                    if sl.event is not None or not pending:
+                        continue
+                    batch, total, keep = [], 0, deque()
+                    while pending:
+                        r = pending.popleft()
+                        n = r.rays.shape[0]
+                        if not self.store.resident(r.scene) or (batch and total + n > self.max_batch_rays):
+                            keep.append(r)
+                            continue
+                        batch.append(r)
+                        total += n
+                    pending = keep
+                    if not batch:
+                        break
+                    self._launch(sl, batch)
+                    self.batches += 1
+                    progressed = True
+                if not progressed:
+                    time.sleep(20e-6)  # let the builder thread run (GIL) while waiting
+        finally:
+            self.build_q.put(None)
+            builder.join(timeout=30)
+        return reqs
+
+    def _launch(self, sl: _Slot, batch: list):
+        import torch
+        jobs = (_capi.LcxTraceJob * len(batch))()
+        with torch.cuda.stream(sl.stream):
+            off_r = 0
+            for i, r in enumerate(batch):
+                n = r.rays.shape[0]
+                r._pin = self.store.pin(r.scene)
+                acc = r._pin.accel
+                seg = sl.rays[off_r * 8:(off_r + n) * 8]
+                seg.view(torch.uint8).copy_(r._h_rays, non_blocking=True)
+                out = sl.occ[off_r:off_r + n] if r.any_hit else sl.hits[off_r * 6:(off_r + n) * 6]
+                jobs[i] = _capi.LcxTraceJob(acc.handle, seg.data_ptr(), out.data_ptr(), n, 0xFF,
+                                            1 if r.any_hit else 0, 0)
+                r._d_out = out
+                off_r += n
+            _capi.check(self.lib.lcx_trace_jobs(jobs, len(batch), self.layout, stream_handle(sl.stream)),
+                        "lcx_trace_jobs")
+            for r in batch:
+                r._h_out.copy_(r._d_out.view(torch.uint8), non_blocking=True)
+            sl.event = torch.cuda.Event()
+            sl.event.record(sl.stream)
+        sl.batch = batch
+
+
+class PlainServer:
+    """One request at a time on one stream (the baseline)."""
+
+    def __init__(self, store: SceneStore, layout: int = 1):
+        self.store = store
+        self.layout = layout
+
+    def run(self, requests: list) -> list:
+        import torch
+        from .accel import rays_to_device
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        stream = torch.cuda.Stream()
+        for r in reqs:
+            r._h_rays = _pinned(r.rays)
+            r._h_out = torch.empty(r.rays.shape[0] * (1 if r.any_hit else 24), dtype=torch.uint8).pin_memory()
+        t0 = time.perf_counter()
+        for r in reqs:
+            while time.perf_counter() - t0 < r.arrival:
+                pass
+            if r.new_scene is not None or not self.store.resident(r.scene):
+                self.store.build(r.scene, r.new_scene, stream)
+            pin = self.store.pin(r.scene)
+            acc = pin.accel
+            with torch.cuda.stream(stream):
+                d = torch.empty(r.rays.shape[0] * 8, dtype=torch.float32, device="cuda")
+                d.view(torch.uint8).copy_(r._h_rays, non_blocking=True)
+                d = d.view(-1, 8)
+                if r.any_hit:
+                    out = acc.trace_any(d, layout=self.layout, stream=stream)
+                else:
+                    out = acc.trace_closest(d, layout=self.layout, stream=stream)
+                r._h_out.copy_(out.view(torch.uint8).reshape(-1), non_blocking=True)
+            stream.synchronize()
+            self.store.unpin(pin)
+            r.done = time.perf_counter() - t0
+        return reqs
+
+
+def results(reqs: list) -> list:
+    """Per-request results as numpy (TriangleHit records or occlusion bytes)."""
+    out = []
+    for r in reqs:
+        a = r._h_out.numpy()
+        out.append(a.copy() if r.any_hit else a.view(S.HIT_DTYPE).copy())
+    return out
+
+
+def latency_stats(reqs: list) -> dict:
+    """p50/p99 latency (ms) overall, for queries on resident scenes, for requests that upload a
+    scene, and for 0.5M..2M-ray queries; aggregate Grays/s over the run."""
+    lat = np.array([r.done - r.arrival for r in reqs]) * 1e3
+    rays = np.array([r.rays.shape[0] for r in reqs])
+    up = np.array([r.new_scene is not None for r in reqs])
+    mid = (rays >= 500_000) & (rays <= 2_000_000) & ~up
+    span = max(r.done for r in reqs) - min(r.arrival for r in reqs)
+
+    def pct(mask, q):
+        return float(np.percentile(lat[mask], q)) if mask.any() else None
+
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "max_ms": float(lat.max()),
+            "queries": {"p50_ms": pct(~up, 50), "p99_ms": pct(~up, 99), "count": int((~up).sum())},
+            "uploads": {"p50_ms": pct(up, 50), "p99_ms": pct(up, 99), "count": int(up.sum())},
+            "queries_0.5M_to_2M_rays": {"p50_ms": pct(mid, 50), "p99_ms": pct(mid, 99), "count": int(mid.sum())},
+            "requests": len(reqs), "rays": int(rays.sum()), "span_s": span,
+            "grays_per_s": float(rays.sum() / span / 1e9)}
+
+
+def make_workload(n_scenes=64, n_requests=2000, rate_hz=1000.0, tri_lo=10_000, tri_hi=4_000_000,
+                  ray_lo=1_000, ray_hi=4_000_000, new_scene_frac=0.08, seed=11, ray_pool=0):
+    """Scenes log-uniform in [tri_lo, tri_hi] triangles (generated like the batched-build meshes);
+    Poisson arrivals at rate_hz; ray counts log-uniform in [ray_lo, ray_hi], half camera rays and
+    half sphere-uniform rays, half closest and half any; new_scene_frac of requests upload a new
+    scene (under a fresh id).  ray_pool > 0 draws each request's rays from that many pre-generated
+    sets per kind (bounded host memory for long runs)."""
+    rng = np.random.default_rng(seed)
+    tri = np.exp(rng.uniform(np.log(tri_lo), np.log(tri_hi), n_scenes)).astype(np.int64)
+    scenes = {i: S.displaced_mesh(int(t), rng) for i, t in enumerate(tri)}
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_hz, n_requests))
+    counts = np.exp(rng.uniform(np.log(ray_lo), np.log(ray_hi), n_requests)).astype(np.int64)
+
+    def make_rays(n, coherent, seed_):
+        if coherent:
+            w = max(1, int(np.sqrt(n)))
+            return S.camera_rays(w, (n + w - 1) // w, eye=(0.0, 0.0, 3.5), seed=seed_)[:n]
+        return S.sphere_rays(n, [-1.3, -1.3, -1.3], [1.3, 1.3, 1.3], seed=seed_)
+
+    pool = None
+    if ray_pool > 0:
+        sizes = np.exp(np.linspace(np.log(ray_lo), np.log(ray_hi), ray_pool)).astype(np.int64)
+        pool = {c: [make_rays(int(n), c, 1000 + 2 * i + int(c)) for i, n in enumerate(sizes)] for c in (0, 1)}
+    reqs = []
+    for k in range(n_requests):
+        sid = int(rng.integers(0, n_scenes))
+        n = int(counts[k])
+        coherent = rng.random() < 0.5
+        if pool is None:
+            rays = make_rays(n, coherent, int(rng.integers(1 << 30)))
+        else:
+            sets = pool[int(coherent)]
+            rays = sets[int(np.argmin([abs(np.log(s.shape[0] / n)) for s in sets]))]
+        new = None
+        if rng.random() < new_scene_frac:  # a new scene under a fresh id, built before the rays run
+            new = S.displaced_mesh(int(tri[sid]), rng)
+            sid = n_scenes + k
+        reqs.append(Request(k, float(arrivals[k]), sid, rays, bool(rng.random() < 0.5), new))
+    return scenes, reqs
