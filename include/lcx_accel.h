@@ -278,6 +278,45 @@ LCX_API int lcx_trace_closest_counts(uint64_t accel, const LcxRay *d_rays, uint3
 LCX_API int lcx_trace_closest_noalloc(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask,
                                       LcxTriangleHit *d_hits, void *stream);
 
+/* ------------------------------------------------------ wavefront path tracer */
+
+/* Geometry and material of one mesh for shading (device pointers): float3-in-16-B
+ * vertices, uint3 triangles, one grey Lambert albedo per triangle. */
+typedef struct LcxPtMesh {
+    const void *vertices;
+    uint64_t vertex_stride;
+    const uint32_t *triangles;
+    const float *albedo;
+} LcxPtMesh;
+
+typedef struct LcxPtParams {
+    uint32_t width, height, spp, max_bounces;
+    uint32_t rr_start;   /* Russian roulette from this bounce on */
+    uint32_t seed;
+    float eye[3], target[3], up[3];
+    float tan_half_fov;  /* tan(vertical field of view / 2) */
+    float light_pos[3], light_intensity[3];
+    float env[3];        /* constant environment radiance */
+} LcxPtParams;
+
+typedef struct LcxPtStats {
+    uint64_t closest_rays, any_rays;
+    uint32_t bounces;
+    float ms;            /* device time of the frame */
+} LcxPtStats;
+
+/* Renders one frame of diffuse path tracing over `accel` (the shape of the
+ * reference's src/tests/test_path_tracing.cpp, as a wavefront): per bounce one
+ * lcx_trace_closest over the live paths, shading, one lcx_trace_any over the
+ * shadow rays; the surviving paths are compacted between bounces.
+ * inst_mesh / inst_o2w (host arrays) give each TLAS instance's mesh and
+ * object-to-world transform.  d_image: width*height*3 floats (linear RGB,
+ * the mean over spp).  d_first_hits (optional): the first bounce's hit of every
+ * path, path = pixel * spp + sample.  Synchronises the host once per bounce. */
+LCX_API int lcx_pt_render(uint64_t accel, const LcxPtMesh *meshes, uint32_t mesh_count, const uint32_t *inst_mesh,
+                          const float *inst_o2w, uint32_t instance_count, const LcxPtParams *params, float *d_image,
+                          LcxTriangleHit *d_first_hits, LcxPtStats *stats, void *stream);
+
 /* Synchronises the current device and reports whether any trace call since
  * the last check hit a kernel-side bound: LCX_ERR_TIMEOUT when a ray exceeded
  * the per-ray step bound (only a corrupt BVH can cause it), LCX_ERR_DEPTH when

@@ -44,6 +44,22 @@ class LcxTraceJob(ctypes.Structure):
                 ("mask", c_uint32), ("any", c_uint32), ("_pad", c_uint32)]
 
 
+class LcxPtMesh(ctypes.Structure):
+    _fields_ = [("vertices", c_void_p), ("vertex_stride", c_uint64), ("triangles", c_void_p), ("albedo", c_void_p)]
+
+
+class LcxPtParams(ctypes.Structure):
+    _fields_ = [("width", c_uint32), ("height", c_uint32), ("spp", c_uint32), ("max_bounces", c_uint32),
+                ("rr_start", c_uint32), ("seed", c_uint32), ("eye", ctypes.c_float * 3),
+                ("target", ctypes.c_float * 3), ("up", ctypes.c_float * 3), ("tan_half_fov", ctypes.c_float),
+                ("light_pos", ctypes.c_float * 3), ("light_intensity", ctypes.c_float * 3),
+                ("env", ctypes.c_float * 3)]
+
+
+class LcxPtStats(ctypes.Structure):
+    _fields_ = [("closest_rays", c_uint64), ("any_rays", c_uint64), ("bounces", c_uint32), ("ms", ctypes.c_float)]
+
+
 class LcxAccelStats(ctypes.Structure):
     _fields_ = [("node_count", c_uint64), ("leaf_prim_count", c_uint64), ("device_bytes", c_uint64),
                 ("depth", c_uint32), ("max_blas_depth", c_uint32), ("sah_cost", c_double),
@@ -74,6 +90,8 @@ _SIGS = {
     "lcx_set_trace_tuning": (c_int, [c_uint32, c_uint32, c_uint32]),
     "lcx_check_trace_errors": (c_int, []),
     "lcx_trace_jobs": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p]),
+    "lcx_pt_render": (c_int, [c_uint64, c_void_p, c_uint32, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p,
+                              c_void_p, c_void_p, c_void_p]),
     "lcx_trace_closest_noalloc": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p]),
     "lcx_get_trace_tuning": (c_int, [POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
 }

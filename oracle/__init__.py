@@ -57,6 +57,7 @@ def load():
         lib.lcxo_fp64_closest.argtypes = [c_void_p, c_void_p, c_size_t, c_uint32, c_void_p, c_void_p, c_int]
         lib.lcxo_fp64_eval.argtypes = [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p]
         lib.lcxo_affine_inverse.argtypes = [c_void_p, c_void_p]
+        lib.lcxo_pathtrace.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]
         lib.lcxo_intersect_triangle.restype = c_int
         lib.lcxo_intersect_triangle.argtypes = [c_void_p, c_void_p, c_float, c_float, c_void_p, c_void_p, c_void_p,
                                                 POINTER(c_float), POINTER(c_float), POINTER(c_float)]
@@ -128,6 +129,17 @@ class OracleScene:
         out = np.zeros(rays.shape[0], F64_DTYPE)
         self.lib.lcxo_fp64_eval(self.accel, _ptr(rays), rays.shape[0], _ptr(inst), _ptr(prim), _ptr(out))
         return out
+
+    def pathtrace(self, scene, albedo, prm, threads: int = 0):
+        """CPU restatement of lcx_pt_render: (image HxWx3, first-bounce hits)."""
+        from luisacompute_gb300.scenes import HIT_DTYPE
+        arrs = [np.ascontiguousarray(albedo[m], np.float32) for m in scene.inst_mesh]
+        self._keep += arrs
+        ptrs = (c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        img = np.zeros(prm.height * prm.width * 3, np.float32)
+        hits = np.zeros(prm.width * prm.height * prm.spp, HIT_DTYPE)
+        self.lib.lcxo_pathtrace(self.accel, ptrs, ctypes.byref(prm), _ptr(img), _ptr(hits), threads)
+        return img.reshape(prm.height, prm.width, 3), hits
 
     def close(self):
         if self.accel:

@@ -10,6 +10,10 @@
 // intrinsics in the same order).
 #include "lcx_oracle.h"
 
+// the path tracer's sampling arithmetic is shared with the GPU kernels (it is
+// this project's, not the reference's); the geometry and traversal are not
+#include "../luisacompute_gb300/csrc/pt_math.cuh"
+
 #include <algorithm>
 #include <atomic>
 #include <cfloat>
@@ -727,6 +731,94 @@ void lcxo_fp64_eval(const void *accel, const LcxoRay *rays, size_t n, const uint
         out[i].v = v;
         out[i].min_bary = mb;
     }
+}
+
+void lcxo_pathtrace(const void *accel, const float *const *albedo, const LcxoPtParams *params, float *image,
+                    LcxoHit *first_hits, int threads) {
+    const Accel &a = *static_cast<const Accel *>(accel);
+    const LcxoPtParams P = *params;
+    const size_t n = size_t(P.width) * P.height * P.spp;
+    std::vector<float> rad(3 * n, 0.0f);
+    parallel_rays(n, threads, [&](size_t idx) {
+        using namespace lcx::pt;
+        const uint32_t i = uint32_t(idx);
+        const uint32_t pixel = i / P.spp;
+        const uint32_t px = pixel % P.width, py = pixel / P.width;
+        float fwd[3] = {P.target[0] - P.eye[0], P.target[1] - P.eye[1], P.target[2] - P.eye[2]};
+        normalize3(fwd);
+        float right[3] = {fwd[1] * P.up[2] - fwd[2] * P.up[1], fwd[2] * P.up[0] - fwd[0] * P.up[2],
+                          fwd[0] * P.up[1] - fwd[1] * P.up[0]};
+        normalize3(right);
+        const float up[3] = {right[1] * fwd[2] - right[2] * fwd[1], right[2] * fwd[0] - right[0] * fwd[2],
+                             right[0] * fwd[1] - right[1] * fwd[0]};
+        const float jx = uniform(P.seed, i, 0, 0), jy = uniform(P.seed, i, 0, 1);
+        const float sx = ((((float(px) + jx) / float(P.width)) * 2.0f - 1.0f) * P.tan_half_fov) *
+                         (float(P.width) / float(P.height));
+        const float sy = (1.0f - ((float(py) + jy) / float(P.height)) * 2.0f) * P.tan_half_fov;
+        float d[3];
+        for (int k = 0; k < 3; k++) d[k] = std::fma(sx, right[k], std::fma(sy, up[k], fwd[k]));
+        normalize3(d);
+        LcxoRay ray{{P.eye[0], P.eye[1], P.eye[2]}, 0.0f, {d[0], d[1], d[2]}, 1e30f};
+        float T[3] = {1.0f, 1.0f, 1.0f}, R[3] = {0.0f, 0.0f, 0.0f};
+        for (uint32_t b = 0; b < P.max_bounces; b++) {
+            LcxoHit h;
+            trace_accel<false>(a, ray, 0xffu, h);
+            if (h.inst == kInvalid) h = LcxoHit{kInvalid, kInvalid, 0.0f, 0.0f, ray.tmax, 0};
+            if (b == 0 && first_hits) first_hits[i] = h;
+            if (h.inst == kInvalid) {
+                for (int k = 0; k < 3; k++) R[k] = std::fma(T[k], P.env[k], R[k]);
+                break;
+            }
+            const Mesh &m = *a.mesh[h.inst];
+            const float *v0 = m.vert(m.t[3 * h.prim]), *v1 = m.vert(m.t[3 * h.prim + 1]),
+                        *v2 = m.vert(m.t[3 * h.prim + 2]);
+            const float e1[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+            const float e2[3] = {v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2]};
+            const float no[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                                 e1[0] * e2[1] - e1[1] * e2[0]};
+            const float *w = &a.w2o[12 * size_t(h.inst)];
+            float N[3];
+            for (int k = 0; k < 3; k++) N[k] = std::fma(w[k], no[0], std::fma(w[4 + k], no[1], w[8 + k] * no[2]));
+            normalize3(N);
+            if (std::fma(N[0], ray.d[0], std::fma(N[1], ray.d[1], N[2] * ray.d[2])) > 0.0f)
+                for (int k = 0; k < 3; k++) N[k] = -N[k];
+            const float p[3] = {std::fma(h.t, ray.d[0], ray.o[0]), std::fma(h.t, ray.d[1], ray.o[1]),
+                                std::fma(h.t, ray.d[2], ray.o[2])};
+            const float po[3] = {offset_coord(p[0], N[0]), offset_coord(p[1], N[1]), offset_coord(p[2], N[2])};
+            const float alb = albedo[h.inst][h.prim];
+            float wl[3] = {P.light_pos[0] - po[0], P.light_pos[1] - po[1], P.light_pos[2] - po[2]};
+            const float dist2 = std::fma(wl[0], wl[0], std::fma(wl[1], wl[1], wl[2] * wl[2]));
+            const float dist = std::sqrt(dist2);
+            for (int k = 0; k < 3; k++) wl[k] = wl[k] / dist;
+            const float cosl = std::fma(N[0], wl[0], std::fma(N[1], wl[1], N[2] * wl[2]));
+            if (cosl > 0.0f) {
+                LcxoRay sr{{po[0], po[1], po[2]}, 0.0f, {wl[0], wl[1], wl[2]}, dist};
+                LcxoHit sh;
+                if (!trace_accel<true>(a, sr, 0xffu, sh)) {
+                    const float f = ((alb * 0.318309886f) * cosl) / dist2;
+                    for (int k = 0; k < 3; k++) R[k] = R[k] + (T[k] * f) * P.light_intensity[k];
+                }
+            }
+            if (b + 1 >= P.max_bounces) break;
+            for (int k = 0; k < 3; k++) T[k] = T[k] * alb;
+            if (b + 1 >= P.rr_start) {
+                const float q = std::fmin(0.95f, std::fmax(T[0], std::fmax(T[1], T[2])));
+                if (uniform(P.seed, i, b + 1, 2) >= q) break;
+                for (int k = 0; k < 3; k++) T[k] = T[k] / q;
+            }
+            float nd[3];
+            cosine_dir(N, uniform(P.seed, i, b + 1, 0), uniform(P.seed, i, b + 1, 1), nd);
+            ray = LcxoRay{{po[0], po[1], po[2]}, 0.0f, {nd[0], nd[1], nd[2]}, 1e30f};
+        }
+        for (int k = 0; k < 3; k++) rad[3 * size_t(i) + k] = R[k];
+    });
+    const float inv = 1.0f / float(P.spp);
+    for (size_t pix = 0; pix < size_t(P.width) * P.height; pix++)
+        for (int k = 0; k < 3; k++) {
+            float acc = 0.0f;
+            for (uint32_t s = 0; s < P.spp; s++) acc = acc + rad[3 * (pix * P.spp + s) + k];
+            image[3 * pix + k] = acc * inv;
+        }
 }
 
 void lcxo_affine_inverse(const float *o2w, float *w2o) { affine_inverse_f32(o2w, w2o); }

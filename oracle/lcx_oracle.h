@@ -85,6 +85,21 @@ void lcxo_fp64_closest(const void *accel, const LcxoRay *rays, size_t n, uint32_
 void lcxo_fp64_eval(const void *accel, const LcxoRay *rays, size_t n, const uint32_t *inst,
                     const uint32_t *prim, LcxoF64Hit *out);
 
+/* Path tracer parameters: byte-identical to LcxPtParams of include/lcx_accel.h. */
+typedef struct LcxoPtParams {
+    uint32_t width, height, spp, max_bounces, rr_start, seed;
+    float eye[3], target[3], up[3];
+    float tan_half_fov;
+    float light_pos[3], light_intensity[3];
+    float env[3];
+} LcxoPtParams;
+
+/* The wavefront tracer's algorithm, one path at a time on the CPU: albedo[i]
+ * points at the per-triangle albedo of instance i's mesh.  image: width *
+ * height * 3 floats; first_hits (optional): the first bounce of every path. */
+void lcxo_pathtrace(const void *accel, const float *const *albedo, const LcxoPtParams *params, float *image,
+                    LcxoHit *first_hits, int threads);
+
 /* The FP32 operation sequences the GPU kernels must reproduce bit for bit. */
 void lcxo_affine_inverse(const float *o2w, float *w2o);
 int lcxo_intersect_triangle(const float *o, const float *d, float tmin, float tmax,
