@@ -330,6 +330,11 @@ LCX_API int lcx_check_trace_errors(void);
  * per wide node, 2..8 (default 8).  Results of queries do not depend on them. */
 LCX_API int lcx_set_build_tuning(uint32_t leaf_max, uint32_t width);
 LCX_API int lcx_get_build_tuning(uint32_t *leaf_max, uint32_t *width);
+/* Morton-code options for later builds: blas_cube / tlas_cube = 1 normalise
+ * centroids by the largest extent on all axes (0: each axis by its own);
+ * tlas_size_bits = size-class bits above the TLAS Morton code (extended Morton
+ * codes; 0 = off).  Defaults 1, 0, 0. */
+LCX_API int lcx_set_build_morton(uint32_t blas_cube, uint32_t tlas_cube, uint32_t tlas_size_bits);
 
 /* Traversal knobs, process-wide (no counterpart in the reference: OptiX and
  * Embree pick theirs internally).  refill: a warp takes new rays once at

@@ -199,29 +199,51 @@ __global__ void __launch_bounds__(kPrepBlock) k_inst_prep(const InstState *inst,
     add_centroid(0, valid, c, segctl);
 }
 
-__global__ void k_morton(const SegInput *segs, uint32_t nseg, uint32_t n, uint32_t axis_bits, const float4 *lo,
-                         const float4 *hi, const uint32_t *segctl, unsigned long long *keys, uint32_t *vals) {
+// Morton key of an item.  With cube = 1 the centroid is normalised by the
+// segment's largest centroid extent on every axis (so a flat segment does not
+// get as many splits across its thin axis as along its wide ones); with
+// cube = 0 each axis by its own extent.  With size_bits > 0 (extended Morton
+// codes, Vinkler, Bittner & Havran 2017) the top bits below the segment id
+// hold a size class, log2(segment extent / item diagonal), so large items meet
+// near the root instead of deep among small neighbours.
+__global__ void k_morton(const SegInput *segs, uint32_t nseg, uint32_t n, uint32_t axis_bits, uint32_t size_bits,
+                         uint32_t cube, const float4 *lo, const float4 *hi, const uint32_t *segctl,
+                         unsigned long long *keys, uint32_t *vals) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t s = nseg > 1 ? segment_of(segs, nseg, i) : 0u;
     const float4 l = lo[i], h = hi[i];
     const uint32_t qmax = (1u << axis_bits) - 1u;
-    unsigned long long code = (1ull << (3 * axis_bits)) - 1ull;  // empty boxes sort last in their segment
+    const uint32_t code_bits = 3 * axis_bits;
+    unsigned long long code = (1ull << code_bits) - 1ull;  // empty boxes sort last in their segment
     if (!box_empty(l, h)) {
         const float c[3] = {0.5f * (l.x + h.x), 0.5f * (l.y + h.y), 0.5f * (l.z + h.z)};
+        float blo[3], ax[3], ext = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            blo[k] = ordered_to_float(segctl[kSegWords * s + kSegCenLo + k]);
+            ax[k] = ordered_to_float(segctl[kSegWords * s + kSegCenHi + k]) - blo[k];
+            ext = fmaxf(ext, ax[k]);
+        }
         uint32_t q[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            const float blo = ordered_to_float(segctl[kSegWords * s + kSegCenLo + k]);
-            const float bhi = ordered_to_float(segctl[kSegWords * s + kSegCenHi + k]);
-            const float ext = bhi - blo;
-            float f = ext > 0.0f ? (c[k] - blo) / ext : 0.0f;
+            const float e = cube ? ext : ax[k];
+            float f = e > 0.0f ? (c[k] - blo[k]) / e : 0.0f;
             f = fminf(fmaxf(f, 0.0f), 1.0f);
             q[k] = min(uint32_t(f * float(qmax)), qmax);
         }
         code = spread21(q[0]) << 2 | spread21(q[1]) << 1 | spread21(q[2]);
+        if (size_bits) {
+            const float dx = h.x - l.x, dy = h.y - l.y, dz = h.z - l.z;
+            const float diag = sqrtf(dx * dx + dy * dy + dz * dz);
+            const uint32_t cmax = (1u << size_bits) - 1u;
+            float cls = ext > 0.0f && diag > 0.0f ? floorf(log2f(ext / diag)) + 1.0f : float(cmax);
+            cls = fminf(fmaxf(cls, 0.0f), float(cmax));
+            code = (static_cast<unsigned long long>(cls) << (code_bits - size_bits)) | (code >> size_bits);
+        }
     }
-    keys[i] = (static_cast<unsigned long long>(s) << (3 * axis_bits)) | code;
+    keys[i] = (static_cast<unsigned long long>(s) << code_bits) | code;
     vals[i] = i;
 }
 
@@ -750,8 +772,8 @@ int collapse_grid() {
 
 cudaError_t build_common(BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
     const uint32_t n = s.n;
-    k_morton<<<blocks_for(n, 256), 256, 0, st>>>(s.segs, s.nseg, n, s.axis_bits, s.box_lo, s.box_hi, s.segctl,
-                                                  s.keys, s.vals);
+    k_morton<<<blocks_for(n, 256), 256, 0, st>>>(s.segs, s.nseg, n, s.axis_bits, bp.size_bits, bp.cube, s.box_lo,
+                                                  s.box_hi, s.segctl, s.keys, s.vals);
     cudaError_t e = sort_pairs(s.sort_tmp, s.sort_tmp_bytes, s.keys, s.keys_sorted, s.vals, s.vals_sorted, n,
                                3 * s.axis_bits + s.seg_bits, st);
     if (e != cudaSuccess) return e;

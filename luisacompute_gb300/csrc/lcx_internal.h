@@ -52,8 +52,10 @@ enum : uint32_t {
 };
 
 struct BuildParams {
-    int leaf_max = 2;  // items per leaf slot, 1..3
-    int width = 8;     // children per wide node, 2..8
+    int leaf_max = 2;        // items per leaf slot, 1..3
+    int width = 8;           // children per wide node, 2..8
+    uint32_t size_bits = 0;  // extended-Morton size-class bits (TLAS builds)
+    uint32_t cube = 1;       // normalise centroids by the largest extent on every axis (else per axis)
 };
 
 // Per-build device scratch, sized for n items in nseg segments.
