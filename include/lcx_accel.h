@@ -345,6 +345,14 @@ LCX_API int lcx_set_build_morton(uint32_t blas_cube, uint32_t tlas_cube, uint32_
  * Results do not depend on any of them. */
 LCX_API int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone, uint32_t mode);
 LCX_API int lcx_get_trace_tuning(uint32_t *refill, uint32_t *postpone, uint32_t *mode);
+/* Ray reordering for later lcx_trace_closest / lcx_trace_any calls (and their
+ * _ex / _counts forms): the rays of a call are sorted by direction octant and
+ * the Morton code of the origin's cell in the scene box (`bits` per axis,
+ * 1..9; 0 = off) and traversed in that order; calls with fewer than min_rays
+ * rays are not reordered.  The results are the same bit for bit.  A tuning
+ * knob with no reference counterpart. */
+LCX_API int lcx_set_trace_reorder(uint32_t bits, uint32_t min_rays);
+LCX_API int lcx_get_trace_reorder(uint32_t *bits, uint32_t *min_rays);
 
 #ifdef __cplusplus
 }

@@ -363,6 +363,13 @@ struct TraceTuning {
 };
 TraceTuning g_tune;
 
+// Ray reordering (see lcx_set_trace_reorder): origin Morton bits per axis, 0 = off.
+struct ReorderTuning {
+    uint32_t bits = 0;
+    uint32_t min_rays = 1u << 16;
+};
+ReorderTuning g_reorder;
+
 }  // namespace
 
 namespace lcx {
@@ -767,9 +774,17 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     // triangle groups may use what is left
     p.postpone_sp = kStackSize - int(depth_need);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    LCX_CUDA(cudaMemsetAsync(p.pool, 0, 4 * sizeof(uint32_t), st), "trace counter reset");
-    LCX_CUDA(launch_trace(p, int(layout), d_occ != nullptr, d_counts != nullptr, st), "trace launch");
-    return LCX_OK;
+    ReorderScratch rs;
+    const uint32_t rbits = g_reorder.bits;
+    if (rbits != 0 && ray_count >= g_reorder.min_rays) {
+        if (int r = reorder_begin(p.rays, ray_count, p.tlas_f, rbits, st, &rs)) return r;
+        p.order = rs.order;
+    }
+    cudaError_t e = cudaMemsetAsync(p.pool, 0, 4 * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = launch_trace(p, int(layout), d_occ != nullptr, d_counts != nullptr, st);
+    const int released = reorder_end(&rs, st);
+    if (e != cudaSuccess) return cuda_fail(e, "trace launch");
+    return released;
 }
 
 int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout, void *stream) {
@@ -862,6 +877,20 @@ int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone, uint32_t mode) {
     g_tune.refill = refill;
     g_tune.postpone = postpone;
     g_tune.mode = mode;
+    return LCX_OK;
+}
+
+int lcx_set_trace_reorder(uint32_t bits, uint32_t min_rays) {
+    if (bits > 9) return fail(LCX_ERR_INVALID_ARG, "reorder bits out of range (0 = off, 1..9)");
+    g_reorder.bits = bits;
+    g_reorder.min_rays = min_rays;
+    return LCX_OK;
+}
+
+int lcx_get_trace_reorder(uint32_t *bits, uint32_t *min_rays) {
+    if (!bits || !min_rays) return fail(LCX_ERR_INVALID_ARG, "null output");
+    *bits = g_reorder.bits;
+    *min_rays = g_reorder.min_rays;
     return LCX_OK;
 }
 

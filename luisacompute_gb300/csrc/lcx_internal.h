@@ -139,8 +139,20 @@ struct TraceParams {
     uint32_t mode;        // loop structure: 0 = node + its items per step, 1 = speculative while-while
     const DevJob *jobs;   // non-null: a multi-job launch over job_count jobs (ray_count = their sum)
     uint32_t job_count;
+    const uint32_t *order;  // non-null: the k-th ray taken is rays[order[k]] (single-job launches)
 };
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st);
+
+// Ray reordering (reorder.cu): sorts the rays of a call by (direction octant,
+// origin Morton cell of the TLAS root box, `bits` per axis) into a
+// permutation held in stream-ordered scratch until reorder_end.
+struct ReorderScratch {
+    void *mem = nullptr;
+    const uint32_t *order = nullptr;
+};
+int reorder_begin(const Ray *rays, uint32_t n, const Node8F *tlas_root, uint32_t bits, cudaStream_t st,
+                  ReorderScratch *rs);
+int reorder_end(ReorderScratch *rs, cudaStream_t st);
 
 // Validation + parameters of a trace_closest call with no device allocation
 // (defined in capi.cu; `pool` is left for the caller to set).

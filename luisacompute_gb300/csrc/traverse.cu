@@ -224,6 +224,9 @@ struct Walker {
             mask = j.mask;
             slot = rid - j.first;
         }
+        else if (P.order != nullptr) {
+            slot = __ldg(P.order + rid);
+        }
         const float4 *rp = reinterpret_cast<const float4 *>((kMulti ? rays : P.rays) + slot);
         const float4 r0 = __ldcs(rp), r1 = __ldcs(rp + 1);
         wox = r0.x;
@@ -348,8 +351,8 @@ struct Walker {
         return false;
     }
 
-    __device__ __forceinline__ void finish(uint32_t rid) {
-        if (kMulti) rid = slot;
+    __device__ __forceinline__ void finish() {
+        const uint32_t rid = slot;
         if (kAny) {
             (kMulti ? static_cast<uint8_t *>(out) : P.occluded)[rid] = occluded ? 1 : 0;
         } else {
@@ -474,7 +477,7 @@ __global__ void __launch_bounds__(kTraceBlock,
             if (!done && W.G.y == 0u) done = W.pop_or_done();
         }
         if (done) {
-            W.finish(rid);
+            W.finish();
             active = false;
         }
     }

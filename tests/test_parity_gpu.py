@@ -316,3 +316,38 @@ def test_tuning_does_not_change_results(torch_cuda, lcx, oracle_mod, refill, pos
             assert np.array_equal(trace_any(acc, rays, layout), want_any)
     finally:
         _capi.check(lib.lcx_set_trace_tuning(old[0].value, old[1].value, old[2].value), "set")
+
+
+@pytest.mark.parametrize("bits", [1, 6, 9])
+def test_ray_reorder_does_not_change_results(torch_cuda, lcx, oracle_mod, bits):
+    """Reordered calls (sorted by octant and origin cell) give the oracle's records bit for bit,
+    for closest, any, both layouts, the counting kernel and a call below min_rays."""
+    import ctypes
+    from luisacompute_gb300 import _capi
+    from luisacompute_gb300.accel import rays_to_device
+    lib = _capi.load()
+    scene = small_terrain()
+    rays = np.concatenate([S.terrain_rays(scene, 100_000, seed=15), S.terrain_shadow_rays(scene, 50_000, seed=16)])
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_closest(rays)
+    want_any = osc.trace_any(rays)
+    acc, _ = gpu_scene(scene)
+    plain_counts = torch_cuda.zeros((rays.shape[0], 3), dtype=torch_cuda.int32, device="cuda")
+    acc.trace_closest(rays_to_device(rays), layout=1, counts=plain_counts)
+    old = [ctypes.c_uint32(0) for _ in range(2)]
+    _capi.check(lib.lcx_get_trace_reorder(*old), "get")
+    try:
+        _capi.check(lib.lcx_set_trace_reorder(bits, 0), "set")
+        for layout in (0, 1):
+            got = trace(acc, rays, layout)
+            assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+            assert np.array_equal(trace_any(acc, rays, layout), want_any)
+        counts = torch_cuda.zeros_like(plain_counts)
+        acc.trace_closest(rays_to_device(rays), layout=1, counts=counts)
+        assert torch_cuda.equal(counts, plain_counts)  # a ray's walk does not depend on its neighbours
+        _capi.check(lib.lcx_set_trace_reorder(bits, rays.shape[0] + 1), "set")  # below min_rays: not reordered
+        assert np.array_equal(trace(acc, rays, 1).view(np.uint8), want.view(np.uint8))
+        assert lib.lcx_set_trace_reorder(10, 0) == _capi.LCX_ERR_INVALID_ARG
+    finally:
+        _capi.check(lib.lcx_set_trace_reorder(old[0].value, old[1].value), "set")
+    no_kernel_errors()
