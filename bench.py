@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--layout", type=int, default=1, help="0 = FP32 nodes, 1 = 8-bit quantised nodes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the autotuner (build and traversal knobs stay at their defaults)")
     ap.add_argument("--workload", default="terrain", choices=["terrain", "batch_build", "serving", "pathtrace"],
                     help="terrain: the headline trace_closest benchmark; batch_build: 4096 BLAS builds; "
                          "serving: continuous batching vs one request at a time; "
@@ -411,6 +413,13 @@ def main():
     scene, rays = make_workload(args.rays)
     n = rays.shape[0]
     stream = torch.cuda.current_stream()
+    tuned = None
+    if not args.no_autotune:
+        # knobs picked on a separate sample of the same distribution (1M rays, other seed)
+        from luisacompute_gb300 import autotune
+        sample = rays_to_device(S.terrain_rays(scene, min(n, 1 << 20), seed=40))
+        tuned = autotune.tune(scene, sample, layout=args.layout).to_json()
+        del sample
     t0 = time.perf_counter()
     acc, meshes = accel_from_scene(scene)
     torch.cuda.synchronize()
@@ -502,6 +511,8 @@ def main():
                          "kernel": "k_trace<quant8, closest>" if args.layout == 1 else "k_trace<fp32, closest>"},
             "clocks": clocks.summary(),
             "gpu_launches": args.steps}
+    if tuned is not None:
+        line["config"]["autotune"] = tuned
 
     if rank == 0 and not args.no_extra:
         extra = {"build_wall_s_all_meshes_and_tlas": build_wall_s}

@@ -326,7 +326,7 @@ LCX_API int lcx_check_trace_errors(void);
 
 /* Build knobs, process-wide, for builds that start after the call (no
  * counterpart in the reference).  leaf_max: triangles per leaf slot, 1..3, or
- * 0 to follow AccelOption.hint (FAST_TRACE 2, FAST_BUILD 3); width: children
+ * 0 to follow AccelOption.hint (FAST_TRACE 1, FAST_BUILD 3); width: children
  * per wide node, 2..8 (default 8).  Results of queries do not depend on them. */
 LCX_API int lcx_set_build_tuning(uint32_t leaf_max, uint32_t width);
 LCX_API int lcx_get_build_tuning(uint32_t *leaf_max, uint32_t *width);
@@ -335,6 +335,7 @@ LCX_API int lcx_get_build_tuning(uint32_t *leaf_max, uint32_t *width);
  * tlas_size_bits = size-class bits above the TLAS Morton code (extended Morton
  * codes; 0 = off).  Defaults 1, 0, 0. */
 LCX_API int lcx_set_build_morton(uint32_t blas_cube, uint32_t tlas_cube, uint32_t tlas_size_bits);
+LCX_API int lcx_get_build_morton(uint32_t *blas_cube, uint32_t *tlas_cube, uint32_t *tlas_size_bits);
 
 /* Traversal knobs, process-wide (no counterpart in the reference: OptiX and
  * Embree pick theirs internally).  refill: a warp takes new rays once at
@@ -352,6 +353,12 @@ LCX_API int lcx_get_trace_tuning(uint32_t *refill, uint32_t *postpone, uint32_t 
  * rays are not reordered.  The results are the same bit for bit.  A tuning
  * knob with no reference counterpart. */
 LCX_API int lcx_set_trace_reorder(uint32_t bits, uint32_t min_rays);
+/* Traversal stack entries per thread kept in shared memory (8, 16 or 24; the
+ * rest of the 32-entry stack lives in local memory) for later single-job
+ * closest / any calls in loop mode 0.  Default 16.  Results do not depend on
+ * it.  A tuning knob with no reference counterpart. */
+LCX_API int lcx_set_trace_stack(uint32_t short_entries);
+LCX_API int lcx_get_trace_stack(uint32_t *short_entries);
 LCX_API int lcx_get_trace_reorder(uint32_t *bits, uint32_t *min_rays);
 
 #ifdef __cplusplus

@@ -140,6 +140,7 @@ struct TraceParams {
     const DevJob *jobs;   // non-null: a multi-job launch over job_count jobs (ray_count = their sum)
     uint32_t job_count;
     const uint32_t *order;  // non-null: the k-th ray taken is rays[order[k]] (single-job launches)
+    uint32_t short_stack;   // shared-memory stack entries per thread: 8, 16 or 24 (single-job, mode 0)
 };
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st);
 

@@ -37,12 +37,10 @@ constexpr int kTraceBlock = 128;
 #ifndef LCX_TRACE_MIN_BLOCKS_F
 #define LCX_TRACE_MIN_BLOCKS_F 6
 #endif
-#ifndef LCX_SHORT_STACK
-#define LCX_SHORT_STACK 16  // stack entries kept in shared memory; deeper ones go to local memory
-#endif
-constexpr int kShortStack = LCX_SHORT_STACK < kStackSize ? LCX_SHORT_STACK : kStackSize;
-constexpr int kDeep = kStackSize - kShortStack;    // entries in local memory
-constexpr int kDeepSlots = kDeep > 0 ? kDeep : 1;  // array size (1 when unused)
+// Stack entries kept in shared memory per thread (the rest of the kStackSize
+// entries go to local memory): a launch-time choice among 8, 16 (default) and
+// 24 for the single-job closest / any kernels; 16 for the others.
+constexpr int kDefaultShortStack = 16;
 constexpr uint32_t kMaxRaySteps = 1u << 22;  // per-ray bound: a corrupt tree ends the ray, never hangs
 
 __device__ __forceinline__ uint2 root_group(uint32_t octinv) {
@@ -149,8 +147,12 @@ __device__ __forceinline__ void intersect_f(const Node8F *nodes, uint32_t idx, f
 // Per-lane traversal state and the operations both loop structures share.
 // kMulti: the launch serves several jobs (scenes); each lane takes its job's
 // TLAS, instance table, mask and buffers when it takes a ray.
-template <int kLayout, bool kAny, bool kCount, bool kMulti = false>
+template <int kLayout, bool kAny, bool kCount, bool kMulti, int kShort>
 struct Walker {
+    static constexpr int kShortStack = kShort < kStackSize ? kShort : kStackSize;
+    static constexpr int kDeep = kStackSize - kShortStack;    // entries in local memory
+    static constexpr int kDeepSlots = kDeep > 0 ? kDeep : 1;  // array size (1 when unused)
+
     const TraceParams &P;
     uint2 *stk;
     const void *tlas_nodes;
@@ -373,14 +375,15 @@ struct Walker {
 // kMode 1: speculative while-while (Aila & Laine 2009): lanes walk nodes
 // together; a lane that finds items keeps walking (holding them in Gp) while
 // any lane of the warp is still searching, then all lanes handle items.
-template <int kLayout, bool kAny, bool kCount, int kMode, bool kMulti>
+template <int kLayout, bool kAny, bool kCount, int kMode, bool kMulti, int kShort>
 __global__ void __launch_bounds__(kTraceBlock,
                                   kLayout == LCX_NODES_QUANT8 ? LCX_TRACE_MIN_BLOCKS_Q : LCX_TRACE_MIN_BLOCKS_F)
     k_trace(TraceParams P) {
-    __shared__ uint2 stack_mem[kShortStack * kTraceBlock];
-    uint2 deep_stack[kDeepSlots];
+    using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort>;
+    __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
+    uint2 deep_stack[W_t::kDeepSlots];
     const uint32_t lane = threadIdx.x & 31u;
-    Walker<kLayout, kAny, kCount, kMulti> W(P, stack_mem + threadIdx.x, deep_stack);
+    W_t W(P, stack_mem + threadIdx.x, deep_stack);
     const int refill = int(P.refill);
     const int postpone = int(P.postpone);
     const int postpone_sp = P.postpone_sp;
@@ -483,12 +486,12 @@ __global__ void __launch_bounds__(kTraceBlock,
     }
 }
 
-template <int L, bool A, bool C, int M, bool X>
+template <int L, bool A, bool C, int M, bool X, int S>
 int blocks_per_sm() {
     static int v = 0;
     if (v == 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<L, A, C, M, X>, kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<L, A, C, M, X, S>, kTraceBlock, 0);
         v = b > 0 ? b : 1;
     }
     return v;
@@ -505,26 +508,36 @@ int sm_count() {
     return v;
 }
 
-template <int L, bool A, bool C, int M, bool X = false>
+template <int L, bool A, bool C, int M, bool X = false, int S = kDefaultShortStack>
 cudaError_t launch_one(const TraceParams &p, cudaStream_t st) {
     const uint64_t warps_needed = (uint64_t(p.ray_count) + 31) / 32;
-    uint64_t grid = uint64_t(sm_count()) * blocks_per_sm<L, A, C, M, X>();
+    uint64_t grid = uint64_t(sm_count()) * blocks_per_sm<L, A, C, M, X, S>();
     const uint64_t grid_need = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
     if (grid_need < grid) grid = grid_need;
     if (grid == 0) grid = 1;
-    k_trace<L, A, C, M, X><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
+    k_trace<L, A, C, M, X, S><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
     return cudaGetLastError();
+}
+
+// Single-job, loop mode 0 closest / any kernels: short stack of 8, 16 or 24 entries.
+template <int L, bool A>
+cudaError_t launch_stack(const TraceParams &p, cudaStream_t st) {
+    if (p.short_stack == 8) return launch_one<L, A, false, 0, false, 8>(p, st);
+    if (p.short_stack == 24) return launch_one<L, A, false, 0, false, 24>(p, st);
+    return launch_one<L, A, false, 0, false, kDefaultShortStack>(p, st);
 }
 
 template <int M>
 cudaError_t launch_mode(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
     if (layout == LCX_NODES_QUANT8) {
-        if (any) return launch_one<LCX_NODES_QUANT8, true, false, M>(p, st);
         if (counting) return launch_one<LCX_NODES_QUANT8, false, true, M>(p, st);
+        if (M == 0) return any ? launch_stack<LCX_NODES_QUANT8, true>(p, st) : launch_stack<LCX_NODES_QUANT8, false>(p, st);
+        if (any) return launch_one<LCX_NODES_QUANT8, true, false, M>(p, st);
         return launch_one<LCX_NODES_QUANT8, false, false, M>(p, st);
     }
-    if (any) return launch_one<LCX_NODES_FP32, true, false, M>(p, st);
     if (counting) return launch_one<LCX_NODES_FP32, false, true, M>(p, st);
+    if (M == 0) return any ? launch_stack<LCX_NODES_FP32, true>(p, st) : launch_stack<LCX_NODES_FP32, false>(p, st);
+    if (any) return launch_one<LCX_NODES_FP32, true, false, M>(p, st);
     return launch_one<LCX_NODES_FP32, false, false, M>(p, st);
 }
 

@@ -26,3 +26,24 @@ def test_struct_sizes():
     assert ctypes.sizeof(_capi.LcxAccelOption) == 8
     assert ctypes.sizeof(_capi.LcxMeshBuildCommand) == 64
     assert ctypes.sizeof(_capi.LcxAccelStats) == 48
+
+
+def test_tuning_knobs_round_trip_and_range_checks(lcx):
+    """Every knob the autotuner sets is host state: settable, readable and range-checked
+    without a GPU."""
+    from luisacompute_gb300 import autotune as A
+    old = A.current()
+    try:
+        cfg = A.Config(leaf_max=3, width=4, blas_cube=0, refill=16, short_stack=24, mode=1, reorder_bits=7)
+        A.apply(cfg)
+        assert A.current() == cfg
+        assert lcx.lcx_set_trace_stack(12) == _capi.LCX_ERR_INVALID_ARG
+        assert lcx.lcx_set_trace_reorder(10, 0) == _capi.LCX_ERR_INVALID_ARG
+        assert lcx.lcx_set_build_tuning(4, 8) == _capi.LCX_ERR_INVALID_ARG
+        assert lcx.lcx_set_build_tuning(2, 9) == _capi.LCX_ERR_INVALID_ARG
+        assert lcx.lcx_set_build_morton(2, 0, 0) == _capi.LCX_ERR_INVALID_ARG
+        assert lcx.lcx_set_trace_tuning(0, 0, 0) == _capi.LCX_ERR_INVALID_ARG
+        assert A.current() == cfg  # rejected calls change nothing
+    finally:
+        A.apply(old)
+    assert A.current() == old
