@@ -170,7 +170,8 @@ def cpu_baseline(scene, rays, budget_s=12.0, threads=0):
 def run_batch_build(args):
     """4096 meshes, triangle counts log-uniform in [64, 262144] (icospheres or grids with 1 % Gaussian
     vertex displacement), built with one lcx_mesh_build_batch call per step; then a TLAS over
-    100,000 random affine instances.  Metric: Mtris/s of the batched BLAS build."""
+    100,000 random affine instances.  Metric: Mtris/s of the batched BLAS build.  The build knobs
+    (leaf size, node width, Morton normalisation) are autotuned on the first 512 meshes first."""
     import torch
     from luisacompute_gb300 import build as B
     B.build()
@@ -179,18 +180,27 @@ def run_batch_build(args):
     datas = S.batch_meshes(args.meshes, seed=6)
     gen_s = time.perf_counter() - t0
     total = sum(m.tri_count for m in datas)
+    tuned = None
+    if not args.no_autotune:
+        from luisacompute_gb300 import autotune
+        tuned = autotune.tune_batch_build(datas, sample=512).to_json()
     meshes = [mesh_from_data(m) for m in datas]
     torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
 
     def timed(fn, reps):
+        """Mean seconds per call: CUDA events on the current stream (each batched build also
+        synchronises once on the host for its node count, inside the timed span)."""
         torch.cuda.synchronize()
-        t = time.perf_counter()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
         for _ in range(reps):
             fn()
+        e1.record(stream)
         torch.cuda.synchronize()
-        return (time.perf_counter() - t) / reps
+        return e0.elapsed_time(e1) / 1e3 / reps
 
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(3, args.warmup)):
         build_meshes(meshes)
     with ClockSampler(0) as clocks:
         batch_s = timed(lambda: build_meshes(meshes), args.steps)
@@ -207,45 +217,59 @@ def run_batch_build(args):
                         rng.uniform(-50, 50, (args.instances, 3)))
     acc = Accel()
     acc.emplace_back_many([meshes[i] for i in pick], aff)
-    t = time.perf_counter()
-    acc.build()
-    torch.cuda.synchronize()
-    tlas_first_s = time.perf_counter() - t
+    tlas_first_s = timed(lambda: acc.build(), 1)
     tlas_s = timed(lambda: acc.build(), 3)
     st = acc.stats()
-    # SAH against the oracle's binned-SAH build on a sample of meshes
+    wide = [m.stats().wide_sah_cost for m in meshes]
+    # kernels of ours per batched build: tri_prep, morton, lbvh, binary_sah, collapse_init, collapse, emit
+    line = {"metric": "Mtris/s batched BLAS build (4096 meshes)", "value": total / batch_s / 1e6, "unit": "Mtris/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": batch_s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"{len(meshes)} meshes, {total} triangles, counts log-uniform [64, 262144], "
+                                   "icosphere or grid with 1% Gaussian displacement; one lcx_mesh_build_batch per step",
+                       "generation_s": gen_s,
+                       "l2": "inputs (vertices + indices, ~2.6 GB) and outputs exceed the 129 MB L2"},
+            "clocks": clocks.summary(), "gpu_launches": 7 * args.steps,
+            "extra": {"one_by_one_mtris_s_first_256": sub_tris / single_s / 1e6,
+                      "batched_mtris_s_first_256": sub_tris / batch_sub_s / 1e6,
+                      "mean_wide_sah": float(np.mean(wide)),
+                      "tlas_instances": args.instances, "tlas_build_ms": tlas_s * 1e3,
+                      "tlas_first_build_ms": tlas_first_s * 1e3,
+                      "tlas": {"nodes": int(st.node_count), "depth": int(st.depth), "sah": st.sah_cost,
+                               "wide_sah": st.wide_sah_cost}}}
+    if tuned is not None:
+        line["config"]["autotune"] = tuned
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_build(datas, meshes, rng)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def cpu_baseline_build(datas, meshes, rng, count=16):
+    """The oracle's binned-SAH build (32 bins, leaf size 4, one thread) timed on a sample of the
+    batch, with its SAH beside the SAH of our build of the same meshes."""
     import oracle
     oracle.build()
     lib = oracle.load()
-    sample = rng.choice(len(meshes), 16, replace=False)
-    sah = []
+    sample = rng.choice(len(meshes), count, replace=False)
+    sah, tris, secs = [], 0, 0.0
     for i in sample:
         md = datas[i]
         v = np.ascontiguousarray(md.vertices)
         tt = np.ascontiguousarray(md.triangles)
+        t = time.perf_counter()
         om = lib.lcxo_mesh_create(v.ctypes.data, 4, v.shape[0], tt.ctypes.data, tt.shape[0], 4, 32)
+        secs += time.perf_counter() - t
+        tris += md.tri_count
         ms = meshes[i].stats()
         sah.append({"tris": int(md.tri_count), "oracle_binned_sah": float(lib.lcxo_mesh_sah(om)),
                     "ours_binary_lbvh": ms.sah_cost, "ours_wide": ms.wide_sah_cost, "ours_depth": int(ms.depth)})
         lib.lcxo_mesh_destroy(om)
     ratio = float(np.median([x["ours_binary_lbvh"] / x["oracle_binned_sah"] for x in sah]))
-    line = {"metric": "Mtris/s batched BLAS build (4096 meshes)", "value": total / batch_s / 1e6, "unit": "Mtris/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": batch_s * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded)",
-            "config": {"workload": f"{len(meshes)} meshes, {total} triangles, counts log-uniform [64, 262144], "
-                                   "icosphere or grid with 1% Gaussian displacement; one lcx_mesh_build_batch per step",
-                       "generation_s": gen_s},
-            "clocks": clocks.summary(), "gpu_launches": None,
-            "extra": {"one_by_one_mtris_s_first_256": sub_tris / single_s / 1e6,
-                      "batched_mtris_s_first_256": sub_tris / batch_sub_s / 1e6,
-                      "tlas_instances": args.instances, "tlas_build_ms": tlas_s * 1e3,
-                      "tlas_first_build_ms": tlas_first_s * 1e3,
-                      "tlas": {"nodes": int(st.node_count), "depth": int(st.depth), "sah": st.sah_cost,
-                               "wide_sah": st.wide_sah_cost},
-                      "sah_sample": sah, "median_sah_ratio_ours_lbvh_to_oracle_binned": ratio}}
-    print(json.dumps(line), flush=True)
-    return 0
+    return {"value": tris / secs / 1e6, "unit": "Mtris/s", "cores": 1, "kind": "port",
+            "sample": f"{count} meshes of the batch ({tris} triangles), oracle binned-SAH build",
+            "sah_sample": sah, "median_sah_ratio_ours_lbvh_to_oracle_binned": ratio}
 
 
 def run_serving(args):
@@ -303,54 +327,75 @@ def run_serving(args):
 def run_pathtrace(args):
     """Wavefront diffuse path tracing, 1920x1080, 4 spp, up to 8 bounces, Russian roulette from bounce
     3, point light + constant environment, grey albedo U[0.2, 0.8] per triangle (seed 7), on the
-    terrain scene (heightfield + 256 instanced spheres) and on the icosphere scene.  Checked against
-    the CPU restatement: first-bounce hits per path and the image (RMSE)."""
+    terrain scene (heightfield + 256 instanced spheres) and on the icosphere scene.  A frame is timed
+    with CUDA events around lcx_pt_render (its per-bounce host synchronisations included).  The
+    cpu_baseline leg renders the same frame with the CPU restatement and compares first-bounce hits
+    per path and the image (RMSE)."""
     import torch
     from luisacompute_gb300 import build as B
     B.build()
     from luisacompute_gb300 import pathtrace as PT
     from luisacompute_gb300.accel import accel_from_scene
-    import oracle
-    oracle.build()
-    out = []
+    stream = torch.cuda.current_stream()
+    out, launches = [], 0
+    steps = max(1, args.steps)
     for name, scene, eye in (("terrain + 256 instanced spheres", S.terrain_scene(), (0.0, 0.8, 2.4)),
                              ("icosphere subdiv 6", S.icosphere_scene(6), (0.0, 0.0, 3.0))):
         acc, meshes = accel_from_scene(scene)
         alb = PT.albedos(scene)
+        d_alb = PT.albedos_to_device(alb)
         prm = PT.params(width=1920, height=1080, spp=4, max_bounces=8, rr_start=3, eye=eye)
-        for _ in range(max(1, args.warmup)):
-            PT.render(scene, acc, meshes, alb, prm)
+        for _ in range(max(3, args.warmup)):
+            PT.render(scene, acc, meshes, d_alb, prm)
         times, stats = [], None
         with ClockSampler(0) as clocks:
-            for _ in range(max(1, args.steps)):
-                t0 = time.perf_counter()
-                img, _, stats = PT.render(scene, acc, meshes, alb, prm)
-                times.append(time.perf_counter() - t0)
-        img, hits, st = PT.render(scene, acc, meshes, alb, prm, first_hits=True)
-        t0 = time.perf_counter()
-        osc = oracle.OracleScene(scene)
-        cimg, chits = osc.pathtrace(scene, alb, prm)
-        cpu_s = time.perf_counter() - t0
-        agree = float((hits.view(np.uint32).reshape(-1, 6)[:, :2] == chits.view(np.uint32).reshape(-1, 6)[:, :2]).all(1).mean())
-        rmse = float(np.sqrt(np.mean((img - cimg) ** 2)))
-        wall = float(np.median(times))
-        out.append({"scene": name, "s_per_frame_wall": wall, "ms_per_frame_device": stats.ms,
-                    "rays_closest": int(stats.closest_rays), "rays_any": int(stats.any_rays),
-                    "bounces": int(stats.bounces),
-                    "grays_per_s": (stats.closest_rays + stats.any_rays) / (stats.ms / 1e3) / 1e9,
-                    "first_hit_agreement": agree, "image_rmse_vs_cpu": rmse,
-                    "image_mean": float(img.mean()),
-                    "cpu_restatement_s_per_frame": cpu_s, "cpu_cores": os.cpu_count(), "clocks": clocks.summary()})
+            for _ in range(steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                img, _, stats = PT.render(scene, acc, meshes, d_alb, prm, stream=stream)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1) / 1e3)
+                launches += int(stats.launches) if not out else 0
+        frame = float(np.median(times))
+        row = {"scene": name, "s_per_frame": frame, "ms_per_frame_render_kernels": stats.ms,
+               "rays_closest": int(stats.closest_rays), "rays_any": int(stats.any_rays),
+               "bounces": int(stats.bounces), "launches_per_frame": int(stats.launches),
+               "grays_per_s": (stats.closest_rays + stats.any_rays) / frame / 1e9,
+               "image_mean": float(img.mean()), "clocks": clocks.summary()}
+        if not args.no_cpu_baseline:
+            row["cpu_baseline"] = cpu_baseline_pathtrace(scene, acc, meshes, alb, prm)
+        out.append(row)
     line = {"metric": "s/frame wavefront path tracing 1920x1080x4spp (terrain scene)",
-            "value": out[0]["s_per_frame_wall"], "unit": "s", "n_gpus": 1, "steps": max(1, args.steps),
-            "warmup": max(1, args.warmup), "ms_per_step": out[0]["s_per_frame_wall"] * 1e3,
+            "value": out[0]["s_per_frame"], "unit": "s", "n_gpus": 1, "steps": steps,
+            "warmup": max(3, args.warmup), "ms_per_step": out[0]["s_per_frame"] * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)",
             "config": {"workload": "wavefront diffuse path tracing, 1920x1080, 4 spp, <= 8 bounces, RR from 3, "
-                                   "shadow rays via trace_any, compaction between bounces"},
-            "scenes": out}
+                                   "shadow rays via trace_any, compaction between bounces",
+                       "l2": "8.3M paths: rays (265 MB), hits and path state exceed the 129 MB L2"},
+            "gpu_launches": launches, "scenes": out}
+    if "cpu_baseline" in out[0]:
+        line["cpu_baseline"] = out[0]["cpu_baseline"]
     print(json.dumps(line), flush=True)
     return 0
+
+
+def cpu_baseline_pathtrace(scene, acc, meshes, alb, prm):
+    """The CPU restatement of the wavefront tracer on all host cores, one frame, with the GPU
+    frame's first-bounce hits and image compared against it."""
+    from luisacompute_gb300 import pathtrace as PT
+    import oracle
+    oracle.build()
+    img, hits, _ = PT.render(scene, acc, meshes, alb, prm, first_hits=True)
+    t0 = time.perf_counter()
+    osc = oracle.OracleScene(scene)
+    cimg, chits = osc.pathtrace(scene, alb, prm)
+    cpu_s = time.perf_counter() - t0
+    agree = float((hits.view(np.uint32).reshape(-1, 6)[:, :2] == chits.view(np.uint32).reshape(-1, 6)[:, :2]).all(1).mean())
+    return {"value": cpu_s, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "one full frame (BVH build included)", "first_hit_agreement": agree,
+            "image_rmse_vs_gpu": float(np.sqrt(np.mean((img - cimg) ** 2)))}
 
 
 def run_reference(args):

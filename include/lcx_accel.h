@@ -303,6 +303,8 @@ typedef struct LcxPtStats {
     uint64_t closest_rays, any_rays;
     uint32_t bounces;
     float ms;            /* device time of the frame */
+    uint32_t launches;   /* kernels of this library launched for the frame */
+    uint32_t _pad;
 } LcxPtStats;
 
 /* Renders one frame of diffuse path tracing over `accel` (the shape of the

@@ -57,7 +57,8 @@ class LcxPtParams(ctypes.Structure):
 
 
 class LcxPtStats(ctypes.Structure):
-    _fields_ = [("closest_rays", c_uint64), ("any_rays", c_uint64), ("bounces", c_uint32), ("ms", ctypes.c_float)]
+    _fields_ = [("closest_rays", c_uint64), ("any_rays", c_uint64), ("bounces", c_uint32), ("ms", ctypes.c_float),
+                ("launches", c_uint32), ("_pad", c_uint32)]
 
 
 class LcxAccelStats(ctypes.Structure):

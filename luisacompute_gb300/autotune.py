@@ -240,3 +240,53 @@ def load(path, scene) -> Config | None:
     c = Config(**cfg)
     apply(c)
     return c
+
+
+def tune_batch_build(datas, *, sample: int = 512, reps: int = 3, sah_slack: float = 0.10,
+                     space: dict | None = None, log=None) -> TuneResult:
+    """Tunes the build knobs for batched BLAS builds (``lcx_mesh_build_batch``) on the first
+    ``sample`` meshes of ``datas`` (scenes.MeshData): among every point of the grid ``space``
+    (leaf size x node width x Morton normalisation) whose mean wide-BVH SAH is within
+    ``sah_slack`` of the best one, the fastest build wins.  Build time is the median of
+    ``reps`` CUDA-event timings.  Leaves the winner applied; ``default_ms`` / ``tuned_ms`` are
+    the build times of the starting and the chosen configuration."""
+    import itertools
+
+    import torch
+    t_start = time.perf_counter()
+    space = BUILD_SPACE if space is None else space
+    meshes = [mesh_from_data(m) for m in datas[:sample]]
+    start = current()
+    trials = []
+    try:
+        keys = list(space)
+        grid = [dict(zip(keys, vals)) for vals in itertools.product(*(space[k] for k in keys))]
+        for point in grid:
+            cfg = replace(start, **point)
+            apply(cfg)
+            build_meshes(meshes)  # warm-up
+            times = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                build_meshes(meshes)
+                e1.record()
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1))
+            times.sort()
+            sah = [m.stats().wide_sah_cost for m in meshes]
+            trials.append({**asdict(cfg), "build_ms": times[len(times) // 2], "mean_wide_sah": float(sum(sah) / len(sah))})
+            if log:
+                log(f"autotune build {point}: {trials[-1]['build_ms']:.2f} ms, SAH {trials[-1]['mean_wide_sah']:.3f}")
+        best_sah = min(t["mean_wide_sah"] for t in trials)
+        ok = [t for t in trials if t["mean_wide_sah"] <= best_sah * (1.0 + sah_slack)]
+        win = min(ok, key=lambda t: t["build_ms"])
+        best = Config(**{k: win[k] for k in asdict(start)})
+        apply(best)
+        ref = replace(start, leaf_max=start.leaf_max or 1)
+        default = [t for t in trials if all(t[k] == v for k, v in asdict(ref).items())]
+        default_ms = default[0]["build_ms"] if default else float("nan")
+    finally:
+        for m in meshes:
+            m.destroy()
+    return TuneResult(best, default_ms, win["build_ms"], trials, time.perf_counter() - t_start)

@@ -64,6 +64,20 @@ __device__ __forceinline__ double box_area_d(float lx, float ly, float lz, float
     return 2.0 * (dx * dy + dy * dz + dz * dx);
 }
 
+// out[2 seg] += v from every calling lane: one atomic per warp when the whole
+// warp is present and in one segment (a segment's items and nodes are
+// contiguous, so that is the common case), else one per lane.
+__device__ __forceinline__ void seg_sum(double *out, uint32_t seg, double v) {
+    const uint32_t mask = __activemask();
+    if (mask == 0xffffffffu && __match_any_sync(mask, seg) == mask) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+        if ((threadIdx.x & 31u) == 0u) atomicAdd(&out[2 * seg], v);
+    } else {
+        atomicAdd(&out[2 * seg], v);
+    }
+}
+
 // Segment of global item i: binary search over the segment table.
 __device__ __forceinline__ uint32_t segment_of(const SegInput *segs, uint32_t nseg, uint32_t i) {
     uint32_t lo = 0, hi = nseg - 1;
@@ -608,7 +622,7 @@ __device__ void emit_node(const TreeView &tv, const SegInput *segs, const uint32
     qn[w] = q;
     fn[w] = f;
     if (sah != nullptr) {
-        atomicAdd(&sah[2 * seg], area_acc);
+        seg_sum(sah, seg, area_acc);
         if (w == root) sah[2 * seg + 1] = box_area_d(nl.x, nl.y, nl.z, nh.x, nh.y, nh.z);
     }
 }
@@ -736,7 +750,7 @@ __global__ void k_binary_sah(uint32_t n, uint32_t seg_shift, const unsigned long
     // internal node i splits items i | i+1: it belongs to the segment iff both do
     const uint32_t last = segs[s].item_offset + segs[s].item_count - 1;
     if (i < last) acc += box_area(blo[i], bhi[i]);
-    atomicAdd(&out[2 * s], acc);
+    seg_sum(out, s, acc);
     if (i == segs[s].item_offset) {
         const uint32_t r = segctl[kSegWords * s + kSegRoot];
         out[2 * s + 1] = (r & kLeafBit) ? box_area(lo[it], hi[it]) : box_area(blo[r], bhi[r]);

@@ -155,6 +155,11 @@ int reorder_begin(const Ray *rays, uint32_t n, const Node8F *tlas_root, uint32_t
                   ReorderScratch *rs);
 int reorder_end(ReorderScratch *rs, cudaStream_t st);
 
+// The current device's stream-ordered memory pool for per-call scratch
+// (reorder.cu): freed blocks stay in the pool for the next call instead of
+// being returned to the driver at every synchronisation.
+int scratch_pool(cudaMemPool_t *out);
+
 // Validation + parameters of a trace_closest call with no device allocation
 // (defined in capi.cu; `pool` is left for the caller to set).
 int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,

@@ -204,14 +204,17 @@ __global__ void k_pt_resolve(LcxPtParams P, const float *rad, float *image) {
 
 inline unsigned blocks(uint64_t n, unsigned b) { return unsigned((n + b - 1) / b); }
 
-// Frees on scope exit, stream-ordered.
+// Per-frame buffers from the device's scratch pool (kept between frames);
+// freed on scope exit, stream-ordered.
 struct PtScratch {
     cudaStream_t st;
+    cudaMemPool_t pool = nullptr;
     std::vector<void *> ptrs;
     explicit PtScratch(cudaStream_t s) : st(s) {}
     template <class T>
     cudaError_t alloc(T **p, size_t count) {
-        cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(p), sizeof(T) * (count ? count : 1), st);
+        if (!pool && scratch_pool(&pool) != LCX_OK) return cudaErrorMemoryAllocation;
+        cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void **>(p), sizeof(T) * (count ? count : 1), pool, st);
         if (e == cudaSuccess) ptrs.push_back(*p);
         return e;
     }
@@ -285,7 +288,7 @@ extern "C" int lcx_pt_render(uint64_t accel, const LcxPtMesh *meshes, uint32_t m
     k_pt_generate<<<blocks(n, 256), 256, 0, st>>>(P, B.rays[0], B.path[0], B.thr, B.rad);
     uint32_t live = n;
     uint64_t closest_rays = 0, any_rays = 0;
-    uint32_t bounces = 0;
+    uint32_t bounces = 0, launches = 2;  // k_pt_prep_insts, k_pt_generate
     int cur = 0;
     for (uint32_t b = 0; b < P.max_bounces && live > 0; b++) {
         PT_TRY(cudaMemsetAsync(B.counts, 0, 4 * sizeof(uint32_t), st));
@@ -295,6 +298,7 @@ extern "C" int lcx_pt_render(uint64_t accel, const LcxPtMesh *meshes, uint32_t m
         if (b == 0 && d_first_hits)
             PT_TRY(cudaMemcpyAsync(d_first_hits, B.hits, sizeof(Hit) * n, cudaMemcpyDeviceToDevice, st));
         closest_rays += live;
+        launches += 2;  // k_trace, k_pt_shade
         k_pt_shade<<<blocks(live, 128), 128, 0, st>>>(P, b, live, B.rays[cur], B.hits, B.path[cur], d_meshes, d_insts,
                                                        B.thr, B.rad, B.rays[cur ^ 1], B.path[cur ^ 1], B.srays,
                                                        B.spath, B.pending, B.counts);
@@ -306,6 +310,7 @@ extern "C" int lcx_pt_render(uint64_t accel, const LcxPtMesh *meshes, uint32_t m
             r = lcx_trace_any(accel, reinterpret_cast<const LcxRay *>(B.srays), h_counts[1], 0xffu, B.occ, stream);
             if (r != LCX_OK) return r;
             any_rays += h_counts[1];
+            launches += 2;  // k_trace, k_pt_shadow
             k_pt_shadow<<<blocks(h_counts[1], 256), 256, 0, st>>>(h_counts[1], B.occ, B.spath, B.pending, B.rad);
         }
         live = h_counts[0];
@@ -325,6 +330,7 @@ extern "C" int lcx_pt_render(uint64_t accel, const LcxPtMesh *meshes, uint32_t m
         stats->any_rays = any_rays;
         stats->bounces = bounces;
         stats->ms = ms;
+        stats->launches = launches + 1;  // + k_pt_resolve
     }
     return LCX_OK;
 #undef PT_TRY

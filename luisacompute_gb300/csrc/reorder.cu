@@ -10,8 +10,9 @@
 // same bit for bit with or without reordering.
 //
 // Scratch (keys, permutation, CUB temporary storage) comes from a per-device
-// stream-ordered memory pool and is released on the call's stream after the
-// traversal, so concurrent calls on different streams never share it.
+// stream-ordered memory pool (scratch_pool, also used by the path tracer) and
+// is released on the call's stream after the traversal, so concurrent calls on
+// different streams never share it.
 #include <cub/device/device_radix_sort.cuh>
 
 #include <cstdio>
@@ -89,6 +90,8 @@ struct PoolEntry {
 std::mutex g_pool_mtx;
 PoolEntry g_pools[64];
 
+}  // namespace
+
 // A memory pool of our own per device that keeps freed blocks for reuse.
 int scratch_pool(cudaMemPool_t *out) {
     int dev = 0;
@@ -109,8 +112,6 @@ int scratch_pool(cudaMemPool_t *out) {
     *out = e.pool;
     return LCX_OK;
 }
-
-}  // namespace
 
 int reorder_begin(const Ray *rays, uint32_t n, const Node8F *tlas_root, uint32_t bits, cudaStream_t st,
                   ReorderScratch *rs) {

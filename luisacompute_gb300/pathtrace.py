@@ -32,12 +32,20 @@ def params(width=1920, height=1080, spp=4, max_bounces=8, rr_start=3, seed=7, ey
     return p
 
 
+def albedos_to_device(albedo_host):
+    """The per-mesh albedo arrays as CUDA tensors, for repeated `render` calls."""
+    import torch
+    return [torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda() for a in albedo_host]
+
+
 def render(scene: S.Scene, acc, meshes, albedo_host, prm, first_hits: bool = False, stream=None):
     """Renders `scene` (already built as `acc` over `meshes`); returns (image HxWx3 float32,
-    first-bounce hits or None, LcxPtStats)."""
+    first-bounce hits or None, LcxPtStats).  `albedo_host` holds one float32 array per mesh:
+    numpy arrays are uploaded for this call, CUDA tensors (see `albedos_to_device`) are used
+    in place."""
     import torch
     lib = _capi.load()
-    dev_alb = [torch.from_numpy(a).cuda() for a in albedo_host]
+    dev_alb = [a if isinstance(a, torch.Tensor) else torch.from_numpy(a).cuda() for a in albedo_host]
     mt = (_capi.LcxPtMesh * len(meshes))()
     for i, m in enumerate(meshes):
         mt[i] = _capi.LcxPtMesh(m.vertices.data_ptr(), m.vertex_stride, m.triangles.data_ptr(), dev_alb[i].data_ptr())

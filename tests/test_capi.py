@@ -26,6 +26,7 @@ def test_struct_sizes():
     assert ctypes.sizeof(_capi.LcxAccelOption) == 8
     assert ctypes.sizeof(_capi.LcxMeshBuildCommand) == 64
     assert ctypes.sizeof(_capi.LcxAccelStats) == 48
+    assert ctypes.sizeof(_capi.LcxPtStats) == 32
 
 
 def test_tuning_knobs_round_trip_and_range_checks(lcx):
