@@ -55,7 +55,7 @@ def parse():
                     help="terrain: the headline trace_closest benchmark; batch_build: 4096 BLAS builds; "
                          "serving: continuous batching vs one request at a time; "
                          "pathtrace: wavefront path tracing 1920x1080x4spp")
-    ap.add_argument("--requests", type=int, default=500)
+    ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--rate", type=float, default=800.0, help="serving: Poisson arrival rate (requests/s)")
     ap.add_argument("--budget-gb", type=float, default=8.0, help="serving: HBM budget for scenes")
     ap.add_argument("--meshes", type=int, default=4096)
@@ -305,8 +305,9 @@ def run_serving(args):
         store_p.warm(sorted(scenes))
         rp = V.PlainServer(store_p).run(clone())
         runs[rate] = {"rate_hz": rate, "generation_s": gen_s,
-                      "continuous": {**V.latency_stats(rc), "batches": cont.batches, "builds": store_c.builds,
-                                     "evictions": store_c.evictions},
+                      "continuous": {**V.latency_stats(rc), "batches": cont.batches, "chunks": cont.chunks,
+                                     "trace_launches": cont.trace_launches,
+                                     "builds": store_c.builds, "evictions": store_c.evictions},
                       "plain_one_at_a_time": {**V.latency_stats(rp), "builds": store_p.builds,
                                               "evictions": store_p.evictions},
                       "clocks": clocks.summary()}
@@ -318,8 +319,10 @@ def run_serving(args):
             "data": "synthetic (seeded)",
             "config": {"workload": f"64 resident scenes log-uniform 10k..4M tris, {args.requests} Poisson requests, "
                                    "1k..4M rays (half camera, half incoherent; half closest, half any), "
-                                   f"8% upload a new scene, HBM budget {args.budget_gb:g} GiB, 4 stream slots"},
-            "runs": list(runs.values()), "clocks": base["clocks"]}
+                                   f"8% upload a new scene, HBM budget {args.budget_gb:g} GiB, 4 stream slots, "
+                                   "<= 1M rays per launch, <= 2M rays in flight, fewest-remaining-rays first"},
+            "runs": list(runs.values()), "clocks": base["clocks"],
+            "gpu_launches": base["continuous"]["trace_launches"]}
     print(json.dumps(line), flush=True)
     return 0
 

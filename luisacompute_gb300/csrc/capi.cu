@@ -12,6 +12,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <shared_mutex>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -80,6 +81,25 @@ struct DevBlock {
     size_t bytes = 0;
     ~DevBlock() {
         if (ptr) cudaFree(ptr);  // cudaFree waits for work still using it
+    }
+};
+
+// BVH lifetime.  Trace calls hold g_life_mtx shared from the accel lookup
+// until their kernel is enqueued; releasing BVH memory (destroy, rebuild) holds
+// it exclusively, so the implicit device synchronisation of cudaFree covers
+// every kernel that read the old pointers, whichever thread launched it.  The
+// exclusive lock is never requested while a mesh or accel mutex is held (a
+// build hands its replaced blocks to a Retired declared before its mutex
+// guard), so a trace holding the shared lock and waiting for such a mutex
+// cannot deadlock with it.  Order: g_life_mtx, registry, object mutexes.
+std::shared_mutex g_life_mtx;
+
+struct Retired {
+    std::vector<std::shared_ptr<DevBlock>> blocks;
+    ~Retired() {
+        if (blocks.empty()) return;
+        std::unique_lock<std::shared_mutex> lk(g_life_mtx);
+        blocks.clear();
     }
 };
 
@@ -267,7 +287,8 @@ int validate_mesh_command(const LcxMeshBuildCommand *cmd, uint64_t &tri64, uint6
 // segmented pipeline: one sort, one LBVH pass, one cooperative collapse and
 // one emit for all of them, into one shared device block.  Synchronises the
 // host once to size the block.
-int build_meshes(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand *cmds, cudaStream_t st) {
+int build_meshes(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand *cmds, cudaStream_t st,
+                 Retired &retired) {
     const size_t count = meshes.size();
     std::vector<SegInput> segs(count);
     uint64_t total = 0;
@@ -292,6 +313,7 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand
         LCX_CUDA(cudaStreamSynchronize(st), "sync");
         for (MeshObj *m : meshes) {
             LCX_CUDA(cudaMemset(m->d_desc, 0, sizeof(BlasDesc)), "cudaMemset(BlasDesc)");
+            if (m->block) retired.blocks.push_back(std::move(m->block));
             m->block.reset();
             m->wide_sah = nullptr;
             m->mem_bytes = 0;
@@ -350,6 +372,7 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand
     // the old blocks are released only after the new BLASes are enqueued; a
     // block shared with other meshes lives on until they are rebuilt too
     for (MeshObj *m : meshes) {
+        if (m->block) retired.blocks.push_back(std::move(m->block));
         m->block = block;
         m->built = true;
         m->generation++;
@@ -420,6 +443,8 @@ int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, u
 
 int record_error(int code, const char *msg) { return fail(code, "%s", msg); }
 
+std::shared_mutex &lifetime_mutex() { return g_life_mtx; }
+
 }  // namespace lcx
 
 extern "C" {
@@ -455,6 +480,7 @@ int lcx_mesh_create(const LcxAccelOption *option, uint64_t *out_handle) {
 }
 
 int lcx_mesh_destroy(uint64_t mesh) {
+    std::unique_lock<std::shared_mutex> life(g_life_mtx);
     std::shared_ptr<MeshObj> m;
     {
         std::lock_guard<std::mutex> lk(g_reg_mtx);
@@ -476,8 +502,9 @@ int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *cmd, void *stream) 
     auto m = find_mesh(mesh);
     if (!m) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build: unknown mesh handle %llu", (unsigned long long)mesh);
     if (!cmd) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build: command is null");
+    Retired retired;  // released after the mutex below
     std::lock_guard<std::mutex> lk(m->mtx);
-    return build_meshes({m.get()}, cmd, static_cast<cudaStream_t>(stream));
+    return build_meshes({m.get()}, cmd, static_cast<cudaStream_t>(stream), retired);
 }
 
 int lcx_mesh_build_batch(const uint64_t *meshes, const LcxMeshBuildCommand *cmds, uint32_t count, void *stream) {
@@ -496,10 +523,11 @@ int lcx_mesh_build_batch(const uint64_t *meshes, const LcxMeshBuildCommand *cmds
     std::sort(sorted.begin(), sorted.end());
     for (uint32_t i = 1; i < count; i++)
         if (sorted[i] == sorted[i - 1]) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build_batch: a mesh appears twice");
+    Retired retired;  // released after the mutexes below
     std::vector<std::unique_lock<std::mutex>> locks;
     locks.reserve(count);
     for (MeshObj *m : sorted) locks.emplace_back(m->mtx);
-    return build_meshes(order, cmds, static_cast<cudaStream_t>(stream));
+    return build_meshes(order, cmds, static_cast<cudaStream_t>(stream), retired);
 }
 
 int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out) {
@@ -540,6 +568,7 @@ int lcx_accel_create(const LcxAccelOption *option, uint64_t *out_handle) {
 }
 
 int lcx_accel_destroy(uint64_t accel) {
+    std::unique_lock<std::shared_mutex> life(g_life_mtx);
     std::shared_ptr<AccelObj> a;
     {
         std::lock_guard<std::mutex> lk(g_reg_mtx);
@@ -566,6 +595,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     if (instance_count == 0) return fail(LCX_ERR_INVALID_ARG, "Building acceleration structure without instances.");
     if (mod_count && !mods) return fail(LCX_ERR_INVALID_ARG, "modifications pointer is null");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Retired retired;  // the replaced TLAS block, released after the mutex below
     std::lock_guard<std::mutex> lk(a->mtx);
     // translate and validate the modifications
     std::vector<ModRec> recs(mod_count);
@@ -661,6 +691,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
         a->depth = rb.segctl[kSegDepth];
         a->sah = rb.bin_sah[1] > 0.0 ? rb.bin_sah[0] / rb.bin_sah[1] : 0.0;
     }
+    if (a->block) retired.blocks.push_back(std::move(a->block));
     a->block = block;
     // remember which mesh builds this TLAS references
     a->mesh_gens.clear();
@@ -738,6 +769,7 @@ int lcx_get_build_tuning(uint32_t *leaf_max, uint32_t *width) {
 static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
                         uint8_t *d_occ, uint32_t *d_counts, uint32_t layout, void *stream) {
     if (layout > LCX_NODES_QUANT8) return fail(LCX_ERR_INVALID_ARG, "invalid node layout %u", layout);
+    std::shared_lock<std::shared_mutex> life(g_life_mtx);  // until the kernel is enqueued
     auto a = find_accel(accel);
     if (!a) return fail(LCX_ERR_INVALID_ARG, "unknown accel handle %llu", (unsigned long long)accel);
     if (ray_count == 0) return LCX_OK;
@@ -804,6 +836,7 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
     if (count == 0) return LCX_OK;
     if (!jobs) return fail(LCX_ERR_INVALID_ARG, "lcx_trace_jobs: jobs is null");
     if (node_layout > LCX_NODES_QUANT8) return fail(LCX_ERR_INVALID_ARG, "invalid node layout %u", node_layout);
+    std::shared_lock<std::shared_mutex> life(g_life_mtx);  // until the kernels are enqueued
     std::vector<DevJob> groups[2];  // [0] closest, [1] any
     uint64_t totals[2] = {0, 0};
     uint32_t depth_need = 0;

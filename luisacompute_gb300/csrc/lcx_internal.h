@@ -2,6 +2,7 @@
 // the kernel translation units (build.cu, traverse.cu, sort.cu).
 #pragma once
 
+#include <shared_mutex>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -165,5 +166,9 @@ int scratch_pool(cudaMemPool_t *out);
 int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
                      uint32_t max_rays, TraceParams &p);
 int record_error(int code, const char *msg);
+
+// BVH lifetime lock (capi.cu): a trace holds it shared from validating its
+// accel until its kernel is enqueued; freeing BVH memory holds it exclusively.
+std::shared_mutex &lifetime_mutex();
 
 }  // namespace lcx

@@ -57,6 +57,7 @@ int scratch_address(uint32_t **out) {
 extern "C" int lcx_trace_closest_noalloc(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask,
                                          LcxTriangleHit *d_hits, void *stream) {
     lcx::TraceParams p;
+    std::shared_lock<std::shared_mutex> life(lcx::lifetime_mutex());  // until the kernel is enqueued
     if (int r = lcx::trace_params_for(accel, d_rays, ray_count, mask, d_hits, kNoAllocMaxRays, p)) return r;
     if (ray_count == 0) return LCX_OK;
     uint32_t *scratch = nullptr;

@@ -4,12 +4,17 @@ A request is a batch of rays (closest or any hit) against one scene; some reques
 scene that must be built before their rays run.  Two servers process the same arrival trace:
 
 * ``ContinuousServer`` — requests that have arrived wait in a queue; whenever one of ``slots``
-  CUDA streams is free, the ready requests (scene resident, FIFO order, up to ``max_batch_rays``)
-  form one batch: their rays are copied in, traced with one ``lcx_trace_jobs`` launch per query
-  kind (each lane of the persistent kernel serves its ray's job), and copied back.  Batches on
-  different streams overlap on the device.  Scene builds run on their own thread and stream, so
-  an upload never blocks admission.  Scenes live in an HBM budget with LRU eviction of scenes
-  no queued or in-flight request needs; an evicted scene is rebuilt on demand.
+  CUDA streams is free, ready work (scene resident) forms one batch of at most ``max_batch_rays``
+  rays: requests with the fewest rays left go first (shortest remaining work; a request that has
+  waited ``max_wait_s`` goes first regardless), and a request larger than what is left of the
+  batch contributes a chunk of its rays and keeps the rest queued, so no launch holds the GPU
+  for long and a small request never waits behind a whole large one.  The batch's rays are
+  copied in, traced with one ``lcx_trace_jobs`` launch per query kind (each lane of the
+  persistent kernel serves its ray's job), and copied back; a request completes with its last
+  chunk.  Batches on different streams overlap on the device; the query streams have a higher
+  priority than the build stream.  Scene builds run on their own thread and stream, so an
+  upload never blocks admission.  Scenes live in an HBM budget with LRU eviction of scenes no
+  queued or in-flight request needs; an evicted scene is rebuilt on demand.
 * ``PlainServer`` — one request at a time: build if needed, copy in, one trace call, copy out,
   wait, next.
 
@@ -29,7 +34,7 @@ import numpy as np
 
 from . import _capi
 from . import scenes as S
-from .accel import Accel, mesh_from_data, stream_handle
+from .accel import Accel, Mesh, stream_handle
 
 
 @dataclass
@@ -41,6 +46,7 @@ class Request:
     any_hit: bool
     new_scene: S.MeshData | None = None  # uploaded (and built) before the rays run
     # filled in by the server
+    dispatched: float = -1.0  # first launch of any of its rays (seconds after the start)
     done: float = -1.0
     result: np.ndarray | None = None
 
@@ -85,11 +91,25 @@ class SceneStore:
             self.res.move_to_end(sid)
             return r
 
+    def try_pin(self, sid: int):
+        """pin(sid) if the scene is resident, else None, in one step (no eviction in between)."""
+        with self.lock:
+            r = self.res.get(sid)
+            if r is None:
+                return None
+            r.pins += 1
+            self.res.move_to_end(sid)
+            return r
+
     def unpin(self, r: _Resident):
         with self.lock:
             r.pins -= 1
 
-    def _evict_for(self, need: int):
+    def _evict_for(self, need: int) -> list:
+        """Under the lock: unregisters least recently used unpinned scenes until `need` bytes fit
+        and returns them; the caller destroys them after releasing the lock (a destroy waits for
+        the device, which must not hold up pin/try_pin)."""
+        victims = []
         for sid in list(self.res.keys()):
             if self.used + need <= self.budget:
                 break
@@ -98,8 +118,14 @@ class SceneStore:
                 del self.res[sid]
                 self.used -= r.nbytes
                 self.evictions += 1
-                r.accel.destroy()
-                r.mesh.destroy()
+                victims.append(r)
+        return victims
+
+    @staticmethod
+    def _destroy(victims: list):
+        for r in victims:
+            r.accel.destroy()
+            r.mesh.destroy()
 
     def build(self, sid: int, data: S.MeshData | None, stream) -> None:
         """Upload and build scene `sid` on `stream`; `data` registers a new scene under a new id
@@ -111,16 +137,23 @@ class SceneStore:
                     raise ValueError(f"scene id {sid} already exists")
                 self.host[sid] = data
         md = self.host[sid]
-        est = md.vertices.nbytes + md.triangles.nbytes + md.tri_count * 110 + (1 << 16)
+        # uploaded buffers + BVH (~0.36 wide nodes x 288 B + 48 B per triangle at leaf size 1)
+        est = md.vertices.nbytes + md.triangles.nbytes + md.tri_count * 160 + (1 << 16)
         with self.lock:
-            self._evict_for(est)
-        with torch.cuda.stream(stream):
-            mesh = mesh_from_data(md)
+            victims = self._evict_for(est)
+        self._destroy(victims)
+        hv, ht = _pinned_mesh(md)
+        with torch.cuda.stream(stream):  # asynchronous copies from pinned staging
+            v = torch.empty(hv.shape, dtype=torch.float32, device="cuda")
+            v.copy_(hv, non_blocking=True)
+            t = torch.empty(ht.shape, dtype=torch.int32, device="cuda")
+            t.copy_(ht, non_blocking=True)
+        mesh = Mesh(v, t)
         mesh.build(stream=stream)
         acc = Accel()
         acc.emplace_back(mesh)
         acc.build(stream=stream)
-        nbytes = est  # BVH ~ 2 x 288 B / 11 tris + 48 B per triangle, plus the uploaded buffers
+        nbytes = est
         with self.lock:
             self.res[sid] = _Resident(mesh, acc, nbytes)
             self.used += nbytes
@@ -130,7 +163,7 @@ class SceneStore:
 class _Slot:
     def __init__(self, max_rays: int):
         import torch
-        self.stream = torch.cuda.Stream()
+        self.stream = torch.cuda.Stream(priority=-1)  # queries ahead of the build stream
         self.rays = torch.empty(max_rays * 8, dtype=torch.float32, device="cuda")
         self.hits = torch.empty(max_rays * 6, dtype=torch.int32, device="cuda")
         self.occ = torch.empty(max_rays, dtype=torch.uint8, device="cuda")
@@ -153,20 +186,56 @@ def _pinned(a: np.ndarray):
     return t
 
 
+_PIN_MESH: dict = {}
+
+
+def _pinned_mesh(md: S.MeshData):
+    """Pinned host copies of a scene's vertices (float32) and indices (as int32, same bits):
+    where a server receives uploads, so the device copies are asynchronous."""
+    import torch
+    hit = _PIN_MESH.get(id(md))
+    if hit is not None and hit[0] is md:
+        return hit[1], hit[2]
+    v = torch.from_numpy(np.ascontiguousarray(md.vertices, np.float32)).pin_memory()
+    t = torch.from_numpy(np.ascontiguousarray(md.triangles).view(np.int32)).pin_memory()
+    _PIN_MESH[id(md)] = (md, v, t)
+    return v, t
+
+
 class ContinuousServer:
-    def __init__(self, store: SceneStore, slots: int = 4, max_batch_rays: int = 1 << 23, layout: int = 1):
+    # Defaults measured on GB300 (64 displaced-mesh scenes, 800 requests/s): 1M-ray launches with
+    # at most 2M rays in flight gave the lowest p99 for 0.5M-2M-ray queries (11-13 ms, against
+    # 22 ms for 2M-ray launches without an in-flight bound); serialising the kernels was worse.
+    def __init__(self, store: SceneStore, slots: int = 4, max_batch_rays: int = 1 << 20, layout: int = 1,
+                 max_wait_s: float = 0.05, min_chunk: int = 1 << 16, max_inflight_rays: int | None = 2 << 20,
+                 build_priority: int = 0, max_concurrent_kernels: int | None = None):
         self.store = store
         self.lib = _capi.load()
         self.layout = layout
         self.max_batch_rays = max_batch_rays
+        # rays launched and not yet complete, over all slots: bounds how much work a new
+        # request can find ahead of it on the device
+        self.max_inflight_rays = max_inflight_rays or slots * max_batch_rays
+        self.build_priority = build_priority
+        # trace kernels allowed to run at once: a batch's kernel waits for the kernel launched
+        # this many batches before it (copies of every slot still overlap); None = no limit
+        self.max_concurrent_kernels = max_concurrent_kernels
+        self._kernel_events = deque()
+        self.inflight = 0
+        self.max_wait_s = max_wait_s
+        self.min_chunk = min_chunk
         self.slots = [_Slot(max_batch_rays) for _ in range(slots)]
         self.build_q: queue.Queue = queue.Queue()
         self.built: queue.Queue = queue.Queue()
         self.batches = 0
+        self.chunks = 0
+        self.trace_launches = 0  # lcx_trace_jobs launches one kernel per query kind in a batch
+        # per batch: (launch time, completion time seen by the loop, [(request id, first ray, rays)])
+        self.timeline = []
 
     def _builder(self):
         import torch
-        stream = torch.cuda.Stream()
+        stream = torch.cuda.Stream(priority=self.build_priority)  # 0: below the query streams (-1)
         while True:
             item = self.build_q.get()
             if item is None:
@@ -180,15 +249,46 @@ class ContinuousServer:
             except Exception as e:  # reported to the loop
                 self.built.put((sid, e))
 
+    def _take(self, pending: list, now: float):
+        """The next batch: (request, first ray, ray count) pieces, fewest remaining rays first
+        (requests waiting longer than max_wait_s before all others), at most max_batch_rays and
+        at most what max_inflight_rays leaves."""
+        cap = min(self.max_batch_rays, self.max_inflight_rays - self.inflight)
+        if cap < min(self.min_chunk, self.max_batch_rays):
+            return []
+        ready = sorted(pending, key=lambda r: (now - r.arrival < self.max_wait_s, r.rays.shape[0] - r._next,
+                                               r.arrival))
+        batch, total = [], 0
+        for r in ready:
+            room = cap - total
+            left = r.rays.shape[0] - r._next
+            if room <= 0:
+                break
+            if left > room and room < self.min_chunk and batch:
+                continue
+            pin = self.store.try_pin(r.scene)  # pinned with the selection: cannot be evicted in between
+            if pin is None:
+                continue
+            r._pins.append(pin)
+            n = min(left, room)
+            batch.append((r, r._next, n))
+            r._next += n
+            r._out += 1
+            total += n
+        return batch
+
     def run(self, requests: list) -> list:
         import torch
         reqs = sorted(requests, key=lambda r: r.arrival)
         for r in reqs:
             r._h_rays = _pinned(r.rays)
             r._h_out = torch.empty(r.rays.shape[0] * (1 if r.any_hit else 24), dtype=torch.uint8).pin_memory()
+            r._next, r._out, r._pins = 0, 0, []
+            if r.new_scene is not None:
+                _pinned_mesh(r.new_scene)
         builder = threading.Thread(target=self._builder, daemon=True)
         builder.start()
-        pending = deque()       # arrived, scene may not be resident yet
+        pending = []            # arrived, with rays not yet dispatched
         building = set()        # scene ids being built
         waiting_new = {}        # scene id -> requests whose new scene is being uploaded
         nxt = 0
@@ -219,16 +319,19 @@ class ContinuousServer:
                         raise err
                     progressed = True
                     building.discard(sid)
-                    for r in waiting_new.pop(sid, []):
-                        pending.appendleft(r)
+                    pending.extend(waiting_new.pop(sid, []))
                 # completed batches
                 for sl in self.slots:
                     if sl.event is not None and sl.event.query():
                         t = time.perf_counter() - t0
-                        for r in sl.batch:
-                            r.done = t
-                            self.store.unpin(r._pin)
-                            done += 1
+                        for r, _, n in sl.batch:
+                            self.store.unpin(r._pins.pop())
+                            self.inflight -= n
+                            r._out -= 1
+                            if r._out == 0 and r._next == r.rays.shape[0]:
+                                r.done = t
+                                done += 1
+                        self.timeline.append((sl.t_launch, t, [(r.rid, f, n) for r, f, n in sl.batch]))
                         progressed = True
                         sl.event = None
                         sl.batch = []
@@ -241,20 +344,13 @@ class ContinuousServer:
                 for sl in self.slots:
                     if sl.event is not None or not pending:
                         continue
-                    batch, total, keep = [], 0, deque()
-                    while pending:
-                        r = pending.popleft()
-                        n = r.rays.shape[0]
-                        if not self.store.resident(r.scene) or (batch and total + n > self.max_batch_rays):
-                            keep.append(r)
-                            continue
-                        batch.append(r)
-                        total += n
-                    pending = keep
+                    batch = self._take(pending, time.perf_counter() - t0)
                     if not batch:
                         break
-                    self._launch(sl, batch)
+                    pending = [r for r in pending if r._next < r.rays.shape[0]]
+                    self._launch(sl, batch, time.perf_counter() - t0)
                     self.batches += 1
+                    self.chunks += len(batch)
                     progressed = True
                 if not progressed:
                     time.sleep(20e-6)  # let the builder thread run (GIL) while waiting
@@ -263,29 +359,44 @@ class ContinuousServer:
             builder.join(timeout=30)
         return reqs
 
-    def _launch(self, sl: _Slot, batch: list):
+    def _launch(self, sl: _Slot, batch: list, now: float = -1.0):
         import torch
         jobs = (_capi.LcxTraceJob * len(batch))()
+        for r, _, n in batch:
+            self.inflight += n
+            if r.dispatched < 0:
+                r.dispatched = now
         with torch.cuda.stream(sl.stream):
-            off_r = 0
-            for i, r in enumerate(batch):
-                n = r.rays.shape[0]
-                r._pin = self.store.pin(r.scene)
-                acc = r._pin.accel
-                seg = sl.rays[off_r * 8:(off_r + n) * 8]
-                seg.view(torch.uint8).copy_(r._h_rays, non_blocking=True)
-                out = sl.occ[off_r:off_r + n] if r.any_hit else sl.hits[off_r * 6:(off_r + n) * 6]
-                jobs[i] = _capi.LcxTraceJob(acc.handle, seg.data_ptr(), out.data_ptr(), n, 0xFF,
+            off = 0
+            outs = []
+            for i, (r, first, n) in enumerate(batch):
+                pin = r._pins[-1]
+                seg = sl.rays[off * 8:(off + n) * 8]
+                seg.view(torch.uint8).copy_(r._h_rays[first * 32:(first + n) * 32], non_blocking=True)
+                out = sl.occ[off:off + n] if r.any_hit else sl.hits[off * 6:(off + n) * 6]
+                jobs[i] = _capi.LcxTraceJob(pin.accel.handle, seg.data_ptr(), out.data_ptr(), n, 0xFF,
                                             1 if r.any_hit else 0, 0)
-                r._d_out = out
-                off_r += n
+                k = 1 if r.any_hit else 24
+                outs.append((r._h_out[first * k:(first + n) * k], out))
+                off += n
+            k = self.max_concurrent_kernels
+            if k is not None and len(self._kernel_events) >= k:
+                sl.stream.wait_event(self._kernel_events[-k])
             _capi.check(self.lib.lcx_trace_jobs(jobs, len(batch), self.layout, stream_handle(sl.stream)),
                         "lcx_trace_jobs")
-            for r in batch:
-                r._h_out.copy_(r._d_out.view(torch.uint8), non_blocking=True)
+            if k is not None:
+                ev = torch.cuda.Event()
+                ev.record(sl.stream)
+                self._kernel_events.append(ev)
+                while len(self._kernel_events) > k:
+                    self._kernel_events.popleft()
+            self.trace_launches += len({r.any_hit for r, _, _ in batch})
+            for host, dev in outs:
+                host.copy_(dev.view(torch.uint8), non_blocking=True)
             sl.event = torch.cuda.Event()
             sl.event.record(sl.stream)
         sl.batch = batch
+        sl.t_launch = now
 
 
 class PlainServer:
@@ -303,6 +414,8 @@ class PlainServer:
         for r in reqs:
             r._h_rays = _pinned(r.rays)
             r._h_out = torch.empty(r.rays.shape[0] * (1 if r.any_hit else 24), dtype=torch.uint8).pin_memory()
+            if r.new_scene is not None:
+                _pinned_mesh(r.new_scene)
         t0 = time.perf_counter()
         for r in reqs:
             while time.perf_counter() - t0 < r.arrival:
