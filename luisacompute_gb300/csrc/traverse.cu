@@ -30,12 +30,13 @@ namespace {
 
 constexpr int kTraceBlock = 128;
 // Resident 128-thread blocks per SM the register budget is cut for (measured
-// on GB300, terrain workload: quantised nodes peak at 7, FP32 nodes at 6).
+// on GB300, terrain workload: quantised nodes peak at 7 -- 8 spills and drops
+// 1.77 -> 1.65 Grays/s -- and FP32 nodes at 7, 1.61 -> 1.62 over 6).
 #ifndef LCX_TRACE_MIN_BLOCKS_Q
 #define LCX_TRACE_MIN_BLOCKS_Q 7
 #endif
 #ifndef LCX_TRACE_MIN_BLOCKS_F
-#define LCX_TRACE_MIN_BLOCKS_F 6
+#define LCX_TRACE_MIN_BLOCKS_F 7
 #endif
 // Stack entries kept in shared memory per thread (the rest of the kStackSize
 // entries go to local memory): a launch-time choice among 8, 16 (default) and
@@ -73,6 +74,9 @@ __device__ __forceinline__ uint32_t slot_bits(uint32_t meta, uint32_t octinv) {
 #endif
 #ifndef LCX_MINMAX3
 #define LCX_MINMAX3 0  // three-input float min/max for the slab distances
+#endif
+#ifndef LCX_PREFETCH
+#define LCX_PREFETCH 0  // 1: prefetch the next node into L1 (measured: 1.77 -> 1.66 Grays/s, so off)
 #endif
 
 // The meta bytes of four slots at once (the compressed-wide-BVH decode of
@@ -343,6 +347,18 @@ struct Walker {
             intersect_f(static_cast<const Node8F *>(nodes), child, ox, oy, oz, ix, iy, iz, octinv, tmin, best_t, G,
                         Gt);
         if (kCount) c_nodes++;
+#if LCX_PREFETCH
+        if (G.y >= 0x01000000u) {  // the node the next step visits: the front child of G
+            const uint32_t nkey = __ffs(G.y >> 24) - 1u;
+            const uint32_t nslot = nkey ^ octinv;
+            const uint32_t next = G.x + __popc(G.y & 0xffu & ((1u << nslot) - 1u));
+            const char *np = kLayout == LCX_NODES_QUANT8
+                                 ? reinterpret_cast<const char *>(static_cast<const Node8Q *>(nodes) + next)
+                                 : reinterpret_cast<const char *>(static_cast<const Node8F *>(nodes) + next);
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(np));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(np + (kLayout == LCX_NODES_QUANT8 ? 79 : 207)));
+        }
+#endif
     }
 
     // Test the triangles of Gt (inside a BLAS).  Returns true if trace_any is done.
