@@ -75,6 +75,14 @@ __device__ __forceinline__ uint32_t slot_bits(uint32_t meta, uint32_t octinv) {
 #ifndef LCX_MINMAX3
 #define LCX_MINMAX3 0  // three-input float min/max for the slab distances
 #endif
+// Loop mode 0 with the triangle tests spread over the warp (coop_triangles):
+// results identical, but measured slower on GB300 (terrain workload, closest
+// hit 1.78 -> 1.56 Grays/s): with ~4 pending triangles per warp-step, the
+// prefix scan, owner search and shuffles cost what the one or two divergent
+// iterations they replace cost.  Off.
+#ifndef LCX_COOP_TRIS
+#define LCX_COOP_TRIS 0
+#endif
 #ifndef LCX_PREFETCH
 #define LCX_PREFETCH 0  // 1: prefetch the next node into L1 (measured: 1.77 -> 1.66 Grays/s, so off)
 #endif
@@ -389,6 +397,96 @@ struct Walker {
         return false;
     }
 
+    // Triangle tests spread over the whole warp.  Every lane of the warp calls
+    // this together; a lane with `has` owns the triangles of its group Gt.
+    // Task j (in lane order of the owners) goes to lane j mod 32, which takes
+    // the owner's ray, interval and triangle pointer by shuffles.  Each owner's
+    // hits are reduced in shared memory by one 64-bit atomicMin over
+    // (ordered t, prim): all of an owner's triangles belong to its current
+    // instance, so this minimum followed by the usual update rule gives the
+    // same record as testing them one by one.  Returns true for an owner whose
+    // any-hit query found a hit.
+    __device__ __forceinline__ bool coop_triangles(uint2 Gt, bool has, uint32_t lane, unsigned long long *keys,
+                                                   float2 *uvs) {
+        const uint32_t cnt = has ? __popc(Gt.y) : 0u;
+        const uint32_t owners = __ballot_sync(~0u, cnt != 0u);
+        if (owners == 0u) return false;
+        if (kCount) c_tris += cnt;
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(~0u, incl, o);
+            if (lane >= uint32_t(o)) incl += v;
+        }
+        const uint32_t total = __shfl_sync(~0u, incl, 31);
+        const uint32_t excl = incl - cnt;
+        const uint32_t wbase = threadIdx.x & ~31u;
+        if (cnt) keys[threadIdx.x] = ~0ull;
+        __syncwarp();
+        for (uint32_t r0 = 0; r0 < total; r0 += 32) {
+            const uint32_t j = r0 + lane;
+            uint32_t own = 0, k = 0;
+            bool work = false;
+            for (uint32_t rem = owners; rem; rem &= rem - 1u) {
+                const uint32_t o = __ffs(rem) - 1u;
+                const uint32_t oe = __shfl_sync(~0u, excl, o), oc = __shfl_sync(~0u, cnt, o);
+                if (j >= oe && j < oe + oc) {
+                    own = o;
+                    k = j - oe;
+                    work = true;
+                }
+            }
+            WtRay r;
+            r.ox = __shfl_sync(~0u, wt.ox, own);
+            r.oy = __shfl_sync(~0u, wt.oy, own);
+            r.oz = __shfl_sync(~0u, wt.oz, own);
+            r.Sx = __shfl_sync(~0u, wt.Sx, own);
+            r.Sy = __shfl_sync(~0u, wt.Sy, own);
+            r.Sz = __shfl_sync(~0u, wt.Sz, own);
+            r.perm = __shfl_sync(~0u, wt.perm, own);
+            const float lo = __shfl_sync(~0u, tmin, own), hi = __shfl_sync(~0u, best_t, own);
+            const uint32_t gx = __shfl_sync(~0u, Gt.x, own), gy = __shfl_sync(~0u, Gt.y, own);
+            const unsigned long long tp =
+                __shfl_sync(~0u, static_cast<unsigned long long>(reinterpret_cast<uintptr_t>(blas_tris)), own);
+            unsigned long long key = ~0ull;
+            float t = 0.0f, u = 0.0f, v = 0.0f;
+            if (work) {
+                const uint32_t bit = __fns(gy, 0u, int(k) + 1);  // k-th set bit of the owner's group
+                const float4 *q = reinterpret_cast<const float4 *>(reinterpret_cast<const TriRec *>(tp) + gx + bit);
+                const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+                if (wt_intersect(r, lo, hi, a, b, c, t, u, v)) {
+                    key = kAny ? 0ull
+                               : (static_cast<unsigned long long>(float_to_ordered(t)) << 32) | __float_as_uint(a.w);
+                    atomicMin(&keys[wbase + own], key);
+                }
+            }
+            if (!kAny) {
+                __syncwarp();
+                if (key != ~0ull && key == keys[wbase + own]) uvs[wbase + own] = make_float2(u, v);
+                __syncwarp();
+            }
+        }
+        __syncwarp();
+        if (!cnt) return false;
+        const unsigned long long best = keys[threadIdx.x];
+        if (best == ~0ull) return false;
+        if (kAny) {
+            occluded = true;
+            return true;
+        }
+        const float bt = ordered_to_float(uint32_t(best >> 32));
+        const uint32_t prim = uint32_t(best);
+        if (bt < best_t || cur_inst < best_inst || (cur_inst == best_inst && prim < best_prim)) {
+            const float2 uv = uvs[threadIdx.x];
+            best_t = bt;
+            best_u = uv.x;
+            best_v = uv.y;
+            best_inst = cur_inst;
+            best_prim = prim;
+        }
+        return false;
+    }
+
     // Enter the first eligible instance of Gt (TLAS level); pushes the rest.
     __device__ __forceinline__ void instances(uint2 Gt) {
         while (Gt.y) {
@@ -465,6 +563,8 @@ __global__ void __launch_bounds__(kTraceBlock,
     k_trace(TraceParams P) {
     using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
+    __shared__ unsigned long long coop_keys[kTraceBlock];  // per owner lane: min (ordered t, prim)
+    __shared__ float2 coop_uv[kTraceBlock];                 // per owner lane: barycentrics of that minimum
     uint2 deep_stack[W_t::kDeepSlots];
     const uint32_t lane = threadIdx.x & 31u;
     W_t W(P, stack_mem + threadIdx.x, deep_stack);
@@ -501,6 +601,30 @@ __global__ void __launch_bounds__(kTraceBlock,
 
         bool done = false;
         if (kMode == 0) {
+#if LCX_COOP_TRIS
+            // every lane stays in the step: the triangle phase is warp-wide
+            uint2 Gt = make_uint2(0, 0);
+            bool tri = false;
+            if (active) {
+                if (++ray_steps > kMaxRaySteps) {
+                    atomicOr(P.pool + 1, 2u);
+                    done = true;
+                } else {
+                    if (W.G.y >= 0x01000000u) {
+                        W.visit(Gt);
+                    } else {
+                        Gt = W.G;
+                        W.G = make_uint2(0, 0);
+                    }
+                    if (W.in_blas)
+                        tri = Gt.y != 0u;
+                    else
+                        W.instances(Gt);
+                }
+            }
+            if (W.coop_triangles(Gt, tri, lane, coop_keys, coop_uv)) done = true;
+            if (active && !done && W.G.y == 0u) done = W.pop_or_done();
+#else
             if (!active) continue;
             if (++ray_steps > kMaxRaySteps) {
                 atomicOr(P.pool + 1, 2u);
@@ -525,6 +649,7 @@ __global__ void __launch_bounds__(kTraceBlock,
                 }
                 if (!done && W.G.y == 0u) done = W.pop_or_done();
             }
+#endif
         } else {
             // phase A: walk nodes together, postponing found item groups while others search
             uint2 Gt = make_uint2(0, 0), Gp = make_uint2(0, 0);
@@ -563,7 +688,7 @@ __global__ void __launch_bounds__(kTraceBlock,
             // phase C: pop
             if (!done && W.G.y == 0u) done = W.pop_or_done();
         }
-        if (done) {
+        if (active && done) {
             W.finish();
             active = false;
         }
