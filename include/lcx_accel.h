@@ -87,7 +87,7 @@ enum { LCX_HINT_FAST_TRACE = 0, LCX_HINT_FAST_BUILD = 1 };
 typedef struct LcxAccelOption {
     uint32_t hint;            /* LCX_HINT_FAST_TRACE | LCX_HINT_FAST_BUILD */
     uint8_t allow_compaction; /* accepted for ABI parity; BVHs are always exact-size */
-    uint8_t allow_update;     /* accepted; PREFER_UPDATE rebuilds (see lcx_mesh_build) */
+    uint8_t allow_update;     /* meshes: keep what a refit needs (see lcx_mesh_build) */
     uint8_t _pad[2];
 } LcxAccelOption;
 
@@ -147,7 +147,8 @@ typedef struct LcxAccelStats {
     uint32_t max_blas_depth; /* TLAS only: deepest referenced BLAS */
     double sah_cost;         /* SAH cost of the binary tree (C_node=1, C_tri=1,
                                 normalised by the root surface area) */
-    double wide_sah_cost;    /* same for the 8-wide tree */
+    double wide_sah_cost;    /* same for the 8-wide tree (as built; a refit keeps it) */
+    uint64_t refits;         /* BLAS: refits since the last full build */
 } LcxAccelStats;
 
 /* ------------------------------------------------------------ device setup */
@@ -172,10 +173,17 @@ LCX_API int lcx_mesh_destroy(uint64_t mesh);
 
 /* MeshBuildCommand visit (CPU: accel.rs:205-260; CUDA: cuda_mesh.cpp:31-69).
  * Builds the BLAS on `stream`: Morton-code LBVH, collapsed to 8-wide nodes in
- * both node layouts.  PREFER_UPDATE on a built mesh rebuilds as well (a
- * refit is not offered).  Returns after enqueueing; the mesh may be used by
+ * both node layouts.  Returns after enqueueing; the mesh may be used by
  * lcx_accel_build on the same stream immediately.  Synchronises the host once
- * to learn the tree size. */
+ * to learn the tree size.
+ * PREFER_UPDATE (the OptiX update of cuda_mesh.cpp:42-67): a mesh created with
+ * allow_update and already built is refit in place -- same topology, triangle
+ * records and boxes recomputed from the buffers of the command -- when its
+ * triangle count is unchanged and the call covers every mesh built together
+ * with it (for lcx_mesh_build_batch: the same set of meshes); otherwise it is
+ * rebuilt.  Either way the accels over it must be built again.  A refit
+ * synchronises the host once, to report bad indices.  Hit records are the same
+ * as after a full build of the new geometry (they do not depend on topology). */
 LCX_API int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *command, void *stream);
 
 /* Many MeshBuildCommands at once (no single counterpart in the reference,

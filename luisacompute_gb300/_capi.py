@@ -64,7 +64,7 @@ class LcxPtStats(ctypes.Structure):
 class LcxAccelStats(ctypes.Structure):
     _fields_ = [("node_count", c_uint64), ("leaf_prim_count", c_uint64), ("device_bytes", c_uint64),
                 ("depth", c_uint32), ("max_blas_depth", c_uint32), ("sah_cost", c_double),
-                ("wide_sah_cost", c_double)]
+                ("wide_sah_cost", c_double), ("refits", c_uint64)]
 
 
 _SIGS = {

@@ -511,13 +511,44 @@ __device__ __forceinline__ uint32_t quant_exp(float lo, float hi) {
     return min(b, 254u);
 }
 
+// Quantisation frame of a node box: per-axis exponents and the origin one
+// step below the box (rounded down).  Shared by the emit and the refit.
+__device__ __forceinline__ void quant_frame(const float4 &nl, const float4 &nh, uint32_t ex[3], float p[3]) {
+    const bool node_empty = box_empty(nl, nh);
+    ex[0] = node_empty ? 127u : quant_exp(nl.x, nh.x);
+    ex[1] = node_empty ? 127u : quant_exp(nl.y, nh.y);
+    ex[2] = node_empty ? 127u : quant_exp(nl.z, nh.z);
+    p[0] = node_empty ? 0.0f : __fsub_rd(nl.x, __uint_as_float(ex[0] << 23));
+    p[1] = node_empty ? 0.0f : __fsub_rd(nl.y, __uint_as_float(ex[1] << 23));
+    p[2] = node_empty ? 0.0f : __fsub_rd(nl.z, __uint_as_float(ex[2] << 23));
+}
+
+// Outward 8-bit bounds of a non-empty child box in the frame (ex, p): exact
+// outward bounds, then one more step outward on each side.
+__device__ __forceinline__ void quant_child(const float cl[3], const float ch[3], const uint32_t ex[3], const float p[3],
+                                            uint32_t ql[3], uint32_t qh[3], uint32_t *ctl) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float e = __uint_as_float(ex[k] << 23);
+        float a = floorf(__fdiv_rd(__fsub_rd(cl[k], p[k]), e)) - 1.0f;
+        float z = ceilf(__fdiv_ru(__fsub_ru(ch[k], p[k]), e)) + 1.0f;
+        if (!(a >= -1.0f) || !(z <= 255.0f)) atomicOr(&ctl[kCtlErr], kErrQuant);
+        ql[k] = uint32_t(fminf(fmaxf(a, 0.0f), 255.0f));
+        qh[k] = uint32_t(fminf(fmaxf(z, 0.0f), 255.0f));
+    }
+}
+
 // Writes wide node w (both layouts, indices relative to its segment) and its
 // leaf items; accumulates the segment's wide SAH (sum of node areas + leaf
 // areas x counts) into sah[2 seg], its root area into sah[2 seg + 1].
+// rtab (optional, meshes built for refit): entry c = parent of wide node c plus
+// one in the low word (0 for a root), (segment << 3 | slot in the parent) in
+// the high word; written by the parent for each internal child, by the root
+// for itself.
 template <class ItemWriter>
 __device__ void emit_node(const TreeView &tv, const SegInput *segs, const uint32_t *desc, uint32_t w, Node8Q *qn,
-                          Node8F *fn, int leaf_max, uint32_t *ctl, double *sah, ItemWriter &&write_item,
-                          float4 &node_lo, float4 &node_hi) {
+                          Node8F *fn, int leaf_max, uint32_t *ctl, double *sah, unsigned long long *rtab,
+                          ItemWriter &&write_item, float4 &node_lo, float4 &node_hi) {
     const uint32_t *d = desc + 12ull * w;
     const uint32_t b = d[0], child_base = d[1], item_base = d[2], seg = d[3];
     const uint32_t root = seg;  // wide index of the segment's root
@@ -526,15 +557,9 @@ __device__ void emit_node(const TreeView &tv, const SegInput *segs, const uint32
     tv.box(b, nl, nh);
     node_lo = nl;
     node_hi = nh;
-    const bool node_empty = box_empty(nl, nh);
     uint32_t ex[3];
-    ex[0] = node_empty ? 127u : quant_exp(nl.x, nh.x);
-    ex[1] = node_empty ? 127u : quant_exp(nl.y, nh.y);
-    ex[2] = node_empty ? 127u : quant_exp(nl.z, nh.z);
-    // quantisation origin one step below the node box (rounded down)
-    const float p[3] = {node_empty ? 0.0f : __fsub_rd(nl.x, __uint_as_float(ex[0] << 23)),
-                        node_empty ? 0.0f : __fsub_rd(nl.y, __uint_as_float(ex[1] << 23)),
-                        node_empty ? 0.0f : __fsub_rd(nl.z, __uint_as_float(ex[2] << 23))};
+    float p[3];
+    quant_frame(nl, nh, ex, p);
     Node8Q q;
     Node8F f;
     q.px = p[0];
@@ -554,6 +579,9 @@ __device__ void emit_node(const TreeView &tv, const SegInput *segs, const uint32
             const bool empty = box_empty(l, h);
             const uint32_t cnt = tv.count(c);
             if (!tv.leaf(c) && cnt > uint32_t(leaf_max)) {
+                if (rtab != nullptr)
+                    rtab[child_base + __popc(imask)] =
+                        (static_cast<unsigned long long>((seg << 3) | uint32_t(s)) << 32) | (w + 1u);
                 imask |= 1u << s;
                 meta = kMetaInternalBase + uint32_t(s);
             } else {
@@ -571,16 +599,7 @@ __device__ void emit_node(const TreeView &tv, const SegInput *segs, const uint32
                 ch[0] = h.x;
                 ch[1] = h.y;
                 ch[2] = h.z;
-#pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    const float e = __uint_as_float(ex[k] << 23);
-                    // exact outward bounds, then one more step outward on each side
-                    float a = floorf(__fdiv_rd(__fsub_rd(cl[k], p[k]), e)) - 1.0f;
-                    float z = ceilf(__fdiv_ru(__fsub_ru(ch[k], p[k]), e)) + 1.0f;
-                    if (!(a >= -1.0f) || !(z <= 255.0f)) atomicOr(&ctl[kCtlErr], kErrQuant);
-                    ql[k] = uint32_t(fminf(fmaxf(a, 0.0f), 255.0f));
-                    qh[k] = uint32_t(fminf(fmaxf(z, 0.0f), 255.0f));
-                }
+                quant_child(cl, ch, ex, p, ql, qh, ctl);
             }
         }
         const int wsel = s >> 2, sh = (s & 3) * 8;
@@ -621,6 +640,7 @@ __device__ void emit_node(const TreeView &tv, const SegInput *segs, const uint32
     f.meta_hi = meta_hi;
     qn[w] = q;
     fn[w] = f;
+    if (rtab != nullptr && w == root) rtab[w] = static_cast<unsigned long long>(seg << 3) << 32;
     if (sah != nullptr) {
         seg_sum(sah, seg, area_acc);
         if (w == root) sah[2 * seg + 1] = box_area_d(nl.x, nl.y, nl.z, nh.x, nh.y, nh.z);
@@ -629,7 +649,7 @@ __device__ void emit_node(const TreeView &tv, const SegInput *segs, const uint32
 
 __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *desc, uint32_t wide_count,
                             int leaf_max, Node8Q *qn, Node8F *fn, TriRec *tris, const uint32_t *segctl,
-                            uint32_t *ctl, double *sah) {
+                            uint32_t *ctl, double *sah, unsigned long long *rtab) {
     const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= wide_count) return;
     const uint32_t seg = desc[12ull * w + 3];
@@ -648,7 +668,7 @@ __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *d
     }
     float4 rl, rh;
     emit_node(
-        tv, segs, desc, w, qn, fn, leaf_max, ctl, sah,
+        tv, segs, desc, w, qn, fn, leaf_max, ctl, sah, rtab,
         [&](uint32_t pos, uint32_t prim, uint32_t s) {
             const SegInput &g = segs[s];
             const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * prim);
@@ -689,7 +709,7 @@ __global__ void k_emit_tlas(TreeView tv, const SegInput *segs, const uint32_t *d
     if (w >= wide_count) return;
     float4 rl, rh;
     emit_node(
-        tv, segs, desc, w, qn, fn, leaf_max, ctl, sah,
+        tv, segs, desc, w, qn, fn, leaf_max, ctl, sah, nullptr,
         [&](uint32_t pos, uint32_t id, uint32_t) {
             InstRec r;
 #pragma unroll
@@ -834,9 +854,9 @@ cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const Build
 }
 
 cudaError_t emit_blas(const BuildScratch &s, const BuildParams &bp, uint32_t wide_count, Node8Q *qn, Node8F *fn,
-                      TriRec *tris, double *wide_sah, cudaStream_t st) {
+                      TriRec *tris, double *wide_sah, unsigned long long *rtab, cudaStream_t st) {
     k_emit_blas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.segs, s.desc, wide_count, bp.leaf_max,
-                                                              qn, fn, tris, s.segctl, s.ctl, wide_sah);
+                                                              qn, fn, tris, s.segctl, s.ctl, wide_sah, rtab);
     return cudaGetLastError();
 }
 
@@ -857,6 +877,199 @@ cudaError_t apply_modifications(const ModRec *mods, uint32_t count, InstState *i
 cudaError_t init_instances(InstState *inst, uint32_t begin, uint32_t end, cudaStream_t st) {
     if (end <= begin) return cudaSuccess;
     k_init_instances<<<blocks_for(end - begin, 256), 256, 0, st>>>(inst, begin, end);
+    return cudaGetLastError();
+}
+
+// ---- refit: same topology, new vertices
+namespace {
+
+// Box of one item from its vertices, as k_tri_prep computes it.
+__device__ __forceinline__ void item_box(const float4 &a, const float4 &b, const float4 &c, float l[3], float h[3]) {
+    l[0] = fminf(fminf(FLT_MAX, a.x), fminf(b.x, c.x));
+    l[1] = fminf(fminf(FLT_MAX, a.y), fminf(b.y, c.y));
+    l[2] = fminf(fminf(FLT_MAX, a.z), fminf(b.z, c.z));
+    h[0] = fmaxf(fmaxf(-FLT_MAX, a.x), fmaxf(b.x, c.x));
+    h[1] = fmaxf(fmaxf(-FLT_MAX, a.y), fmaxf(b.y, c.y));
+    h[2] = fmaxf(fmaxf(-FLT_MAX, a.z), fmaxf(b.z, c.z));
+}
+
+__device__ __forceinline__ bool box3_empty(const float l[3], const float h[3]) {
+    return !(l[0] <= h[0] && l[1] <= h[1] && l[2] <= h[2]);
+}
+
+// Bottom-up refit over the wide nodes of one BLAS block: a thread starts at a
+// node without internal children, rewrites the triangle records of its leaf
+// slots from the current buffers (by the prim id each record keeps) and their
+// boxes, takes its node box as the union of its slots, writes it into the
+// parent's slot and goes on with the parent if it is the last of the parent's
+// internal children to arrive (the parent's counter).  Boxes written by other
+// threads are read with ld.cg after the counter says they are complete.
+__global__ void k_refit(const SegInput *segs, uint32_t nseg, uint32_t W, const unsigned long long *rtab,
+                        const Node8Q *qn, Node8F *fn, TriRec *tris, uint32_t *counters, uint32_t *ctl) {
+    uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    if ((__ldg(&qn[w].exps) >> 24) != 0u) return;
+    for (int level = 0; level <= kMaxLevels; level++) {
+        const unsigned long long te = __ldg(&rtab[w]);
+        const uint32_t hiw = uint32_t(te >> 32), parent1 = uint32_t(te);
+        const uint32_t seg = hiw >> 3, pslot = hiw & 7u;
+        if (seg >= nseg) {  // cannot happen for a table the build wrote
+            atomicOr(&ctl[kCtlErr], kErrBadIndex);
+            return;
+        }
+        const SegInput g = segs[seg];
+        Node8F &f = fn[w];
+        const uint32_t meta_lo = __ldcg(&f.meta_lo), meta_hi = __ldcg(&f.meta_hi), ib = __ldcg(&f.item_base);
+        float nl[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, nh[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (int s = 0; s < 8; s++) {
+            const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xffu;
+            if (meta == 0u) continue;
+            float cl[3], ch[3];
+            if (meta_internal(meta)) {
+                cl[0] = __ldcg(&f.lo_x[s]);
+                cl[1] = __ldcg(&f.lo_y[s]);
+                cl[2] = __ldcg(&f.lo_z[s]);
+                ch[0] = __ldcg(&f.hi_x[s]);
+                ch[1] = __ldcg(&f.hi_y[s]);
+                ch[2] = __ldcg(&f.hi_z[s]);
+            } else {
+                cl[0] = cl[1] = cl[2] = FLT_MAX;
+                ch[0] = ch[1] = ch[2] = -FLT_MAX;
+                const uint32_t cnt = meta_count(meta), off = meta & 31u;
+                for (uint32_t j = 0; j < cnt; j++) {
+                    if (ib + off + j >= g.item_count) {  // cannot happen for a node the build wrote
+                        atomicOr(&ctl[kCtlErr], kErrBadIndex);
+                        continue;
+                    }
+                    TriRec *r = tris + (size_t(g.item_offset) + ib + off + j);
+                    const uint32_t prim = __float_as_uint(r->v0.w);
+                    if (prim >= g.item_count) {  // cannot happen for a record the build wrote
+                        atomicOr(&ctl[kCtlErr], kErrBadIndex);
+                        continue;
+                    }
+                    const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * prim);
+                    const uint32_t i0 = t[0], i1 = t[1], i2 = t[2];
+                    if (i0 >= g.vcount || i1 >= g.vcount || i2 >= g.vcount) {
+                        atomicOr(&ctl[kCtlErr], kErrBadIndex);
+                        continue;
+                    }
+                    float4 a = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i0));
+                    float4 b = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i1));
+                    float4 c = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i2));
+                    float il[3], ih[3];
+                    item_box(a, b, c, il, ih);
+                    if (!box3_empty(il, ih)) {
+#pragma unroll
+                        for (int k = 0; k < 3; k++) {
+                            cl[k] = fminf(cl[k], il[k]);
+                            ch[k] = fmaxf(ch[k], ih[k]);
+                        }
+                    }
+                    a.w = __uint_as_float(prim);
+                    b.w = 0.0f;
+                    c.w = 0.0f;
+                    *r = TriRec{a, b, c};
+                }
+                f.lo_x[s] = cl[0];
+                f.lo_y[s] = cl[1];
+                f.lo_z[s] = cl[2];
+                f.hi_x[s] = ch[0];
+                f.hi_y[s] = ch[1];
+                f.hi_z[s] = ch[2];
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                nl[k] = fminf(nl[k], cl[k]);
+                nh[k] = fmaxf(nh[k], ch[k]);
+            }
+        }
+        if (parent1 == 0u) {  // a segment root: its box for the TLAS builds
+            BlasDesc *bd = g.desc;
+            if (bd != nullptr) {
+                const bool empty = box3_empty(nl, nh);
+                for (int k = 0; k < 3; k++) {
+                    bd->lo[k] = empty ? FLT_MAX : nl[k];
+                    bd->hi[k] = empty ? -FLT_MAX : nh[k];
+                }
+                bd->valid = empty ? 0u : 1u;
+            }
+            return;
+        }
+        const uint32_t parent = parent1 - 1u;
+        if (parent >= W || pslot > 7u) {  // cannot happen for a table the build wrote
+            atomicOr(&ctl[kCtlErr], kErrBadIndex);
+            return;
+        }
+        Node8F &pf = fn[parent];
+        pf.lo_x[pslot] = nl[0];
+        pf.lo_y[pslot] = nl[1];
+        pf.lo_z[pslot] = nl[2];
+        pf.hi_x[pslot] = nh[0];
+        pf.hi_y[pslot] = nh[1];
+        pf.hi_z[pslot] = nh[2];
+        __threadfence();
+        const uint32_t need = __popc(__ldg(&qn[parent].exps) >> 24);
+        if (atomicAdd(&counters[parent], 1u) + 1u != need) return;
+        __threadfence();
+        w = parent;
+    }
+    atomicOr(&ctl[kCtlErr], kErrTooDeep);
+}
+
+// Re-encodes the quantised node from the refit FP32 node: node box = union of
+// the slot boxes, then the emit's frame and outward child bounds.
+__global__ void k_requantize(uint32_t W, Node8Q *qn, const Node8F *fn, uint32_t *ctl) {
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    const Node8F &f = fn[w];
+    float4 nl = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f), nh = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
+    for (int s = 0; s < 8; s++) {
+        nl.x = fminf(nl.x, f.lo_x[s]);
+        nl.y = fminf(nl.y, f.lo_y[s]);
+        nl.z = fminf(nl.z, f.lo_z[s]);
+        nh.x = fmaxf(nh.x, f.hi_x[s]);
+        nh.y = fmaxf(nh.y, f.hi_y[s]);
+        nh.z = fmaxf(nh.z, f.hi_z[s]);
+    }
+    uint32_t ex[3];
+    float p[3];
+    quant_frame(nl, nh, ex, p);
+    Node8Q q = qn[w];
+    q.px = p[0];
+    q.py = p[1];
+    q.pz = p[2];
+    q.exps = ex[0] | (ex[1] << 8) | (ex[2] << 16) | (q.exps & 0xff000000u);
+    uint32_t qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}}, qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    for (int s = 0; s < 8; s++) {
+        const float cl[3] = {f.lo_x[s], f.lo_y[s], f.lo_z[s]}, ch[3] = {f.hi_x[s], f.hi_y[s], f.hi_z[s]};
+        uint32_t ql[3] = {255u, 255u, 255u}, qh[3] = {0u, 0u, 0u};
+        if (!box3_empty(cl, ch)) quant_child(cl, ch, ex, p, ql, qh, ctl);
+        const int wsel = s >> 2, sh = (s & 3) * 8;
+        for (int k = 0; k < 3; k++) {
+            qlo[k][wsel] |= ql[k] << sh;
+            qhi[k][wsel] |= qh[k] << sh;
+        }
+    }
+    for (int k = 0; k < 2; k++) {
+        q.qlo_x[k] = qlo[0][k];
+        q.qlo_y[k] = qlo[1][k];
+        q.qlo_z[k] = qlo[2][k];
+        q.qhi_x[k] = qhi[0][k];
+        q.qhi_y[k] = qhi[1][k];
+        q.qhi_z[k] = qhi[2][k];
+    }
+    qn[w] = q;
+}
+
+}  // namespace
+
+cudaError_t refit_blas(const SegInput *segs, uint32_t nseg, uint32_t W, const unsigned long long *rtab, Node8Q *qn,
+                       Node8F *fn, TriRec *tris, uint32_t *counters, uint32_t *ctl, cudaStream_t st) {
+    if (W == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(uint32_t) * W, st);
+    if (e != cudaSuccess) return e;
+    k_refit<<<blocks_for(W, 128), 128, 0, st>>>(segs, nseg, W, rtab, qn, fn, tris, counters, ctl);
+    k_requantize<<<blocks_for(W, 128), 128, 0, st>>>(W, qn, fn, ctl);
     return cudaGetLastError();
 }
 

@@ -79,6 +79,12 @@ int current_device_state(DeviceState **out) {
 struct DevBlock {
     void *ptr = nullptr;
     size_t bytes = 0;
+    // BLAS blocks built with allow_update: the layout and the parent table a refit needs
+    unsigned long long *rtab = nullptr;
+    uint32_t wide = 0, nseg = 0;
+    Node8Q *qn = nullptr;
+    Node8F *fn = nullptr;
+    TriRec *tris = nullptr;
     ~DevBlock() {
         if (ptr) cudaFree(ptr);  // cudaFree waits for work still using it
     }
@@ -111,6 +117,8 @@ struct MeshObj {
     double *wide_sah = nullptr;       // in `block`: 2 doubles of this mesh's segment
     size_t mem_bytes = 0;             // this mesh's share of the block
     uint32_t node_count = 0, tri_count = 0, depth = 0;
+    uint32_t seg = 0;  // segment (position in its build) within `block`
+    uint64_t refits = 0;  // refits since the last full build
     bool built = false;
     uint64_t generation = 0;
     double sah = 0.0;
@@ -287,6 +295,58 @@ int validate_mesh_command(const LcxMeshBuildCommand *cmd, uint64_t &tri64, uint6
 // segmented pipeline: one sort, one LBVH pass, one cooperative collapse and
 // one emit for all of them, into one shared device block.  Synchronises the
 // host once to size the block.
+constexpr int kNoRefit = 1;  // try_refit: the call is not a refit; build instead
+
+// PREFER_UPDATE on meshes created with allow_update: when the call covers every
+// mesh of one BVH block (as built together) and no triangle count changed,
+// the block is refit in place (same topology, new triangle records and boxes)
+// instead of rebuilt.  One host synchronisation, to report bad indices.
+// `segs`: the call's validated segments in call order.  Otherwise kNoRefit.
+int try_refit(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand *cmds, const std::vector<SegInput> &segs,
+              cudaStream_t st) {
+    const size_t count = meshes.size();
+    DevBlock *blk = meshes[0]->block.get();
+    if (!blk || !blk->rtab || blk->nseg != count) return kNoRefit;
+    std::vector<SegInput> ordered(count);
+    std::vector<bool> seen(count, false);
+    for (size_t i = 0; i < count; i++) {
+        const MeshObj *m = meshes[i];
+        if (cmds[i].request != LCX_REQUEST_PREFER_UPDATE || !m->opt.allow_update || !m->built ||
+            m->block.get() != blk || m->seg >= count || seen[m->seg] || segs[i].item_count != m->tri_count ||
+            segs[i].item_count == 0)
+            return kNoRefit;
+        seen[m->seg] = true;
+        ordered[m->seg] = segs[i];
+    }
+    uint32_t off = 0;
+    for (size_t k = 0; k < count; k++) {  // the build's item offsets: prefix sums in segment order
+        ordered[k].item_offset = off;
+        off += ordered[k].item_count;
+    }
+    ScratchHolder hold(st);
+    SegInput *d_segs = nullptr;
+    uint32_t *counters = nullptr, *ctl = nullptr;
+    LCX_CUDA(hold.alloc((void **)&d_segs, sizeof(SegInput) * count), "refit scratch");
+    LCX_CUDA(hold.alloc((void **)&counters, sizeof(uint32_t) * std::max<uint32_t>(blk->wide, 1)), "refit scratch");
+    LCX_CUDA(hold.alloc((void **)&ctl, sizeof(uint32_t) * kCtlWords), "refit scratch");
+    LCX_CUDA(cudaMemcpyAsync(d_segs, ordered.data(), sizeof(SegInput) * count, cudaMemcpyHostToDevice, st),
+             "refit segment upload");
+    LCX_CUDA(cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * kCtlWords, st), "refit scratch init");
+    LCX_CUDA(refit_blas(d_segs, uint32_t(count), blk->wide, blk->rtab, blk->qn, blk->fn, blk->tris, counters, ctl, st),
+             "BLAS refit");
+    uint32_t err = 0;
+    LCX_CUDA(cudaMemcpyAsync(&err, ctl + kCtlErr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "refit readback");
+    LCX_CUDA(cudaStreamSynchronize(st), "refit sync");
+    if (err & kErrBadIndex) return fail(LCX_ERR_INVALID_ARG, "refit: triangle index out of range");
+    if (err & kErrTooDeep) return fail(LCX_ERR_DEPTH, "refit: BVH deeper than %d levels", kMaxLevels);
+    if (err & kErrQuant) return fail(LCX_ERR_INVALID_ARG, "refit: vertex coordinates too large to quantise");
+    for (MeshObj *m : meshes) {
+        m->generation++;  // accels over these meshes must be built again
+        m->refits++;
+    }
+    return LCX_OK;
+}
+
 int build_meshes(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand *cmds, cudaStream_t st,
                  Retired &retired) {
     const size_t count = meshes.size();
@@ -307,6 +367,10 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand
         total += tri64;
         if (total >= (1ull << 31)) return fail(LCX_ERR_INVALID_ARG, "batch too large (%llu triangles)",
                                                (unsigned long long)total);
+    }
+    {
+        const int r = try_refit(meshes, cmds, segs, st);
+        if (r != kNoRefit) return r;
     }
     const BuildParams bp = build_params_for(meshes[0]->opt);
     if (total == 0) {
@@ -348,23 +412,37 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand
         const uint32_t W = rb.ctl[kCtlWideCount];
         const size_t q_bytes = size_t(W) * sizeof(Node8Q), f_bytes = size_t(W) * sizeof(Node8F);
         const size_t t_bytes = size_t(n) * sizeof(TriRec), sah_bytes = 2 * sizeof(double) * count;
+        bool want_rtab = false;
+        for (MeshObj *m : meshes) want_rtab = want_rtab || m->opt.allow_update;
+        const size_t r_bytes = want_rtab ? size_t(W) * sizeof(unsigned long long) : 0;
         block = std::make_shared<DevBlock>();
-        block->bytes = q_bytes + f_bytes + t_bytes + sah_bytes;
+        block->bytes = q_bytes + f_bytes + t_bytes + sah_bytes + r_bytes;
         LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(BLAS)");
         Node8Q *qn = static_cast<Node8Q *>(block->ptr);
         Node8F *fn = reinterpret_cast<Node8F *>(reinterpret_cast<char *>(block->ptr) + q_bytes);
         TriRec *tr = reinterpret_cast<TriRec *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes);
         double *wsah = reinterpret_cast<double *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes + t_bytes);
+        unsigned long long *rtab =
+            want_rtab ? reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(wsah) + sah_bytes) : nullptr;
+        block->rtab = rtab;
+        block->wide = W;
+        block->nseg = uint32_t(count);
+        block->qn = qn;
+        block->fn = fn;
+        block->tris = tr;
         LCX_CUDA(cudaMemsetAsync(wsah, 0, sah_bytes, st), "cudaMemset");
-        LCX_CUDA(emit_blas(s, bp, W, qn, fn, tr, wsah, st), "BLAS emit");
+        LCX_CUDA(emit_blas(s, bp, W, qn, fn, tr, wsah, rtab, st), "BLAS emit");
         for (size_t i = 0; i < count; i++) {
             MeshObj *m = meshes[i];
             const uint32_t *sc = &rb.segctl[kSegWords * i];
             m->wide_sah = wsah + 2 * i;
+            m->seg = uint32_t(i);
+            m->refits = 0;
             m->node_count = segs[i].item_count ? sc[kSegNodes] : 0u;
             m->tri_count = segs[i].item_count;
             m->depth = segs[i].item_count ? sc[kSegDepth] : 0u;
-            m->mem_bytes = size_t(m->node_count) * (sizeof(Node8Q) + sizeof(Node8F)) + size_t(m->tri_count) * sizeof(TriRec);
+            m->mem_bytes = size_t(m->node_count) * (sizeof(Node8Q) + sizeof(Node8F) + (rtab ? 8 : 0)) +
+                           size_t(m->tri_count) * sizeof(TriRec);
             const double ra = rb.bin_sah[2 * i + 1];
             m->sah = ra > 0.0 ? rb.bin_sah[2 * i] / ra : 0.0;
         }
@@ -541,6 +619,7 @@ int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out) {
     out->device_bytes = m->mem_bytes + sizeof(BlasDesc);
     out->depth = m->depth;
     out->sah_cost = m->sah;
+    out->refits = m->refits;
     if (m->wide_sah) {
         double h[2] = {0, 0};
         LCX_CUDA(cudaMemcpy(h, m->wide_sah, sizeof(h), cudaMemcpyDeviceToHost), "wide SAH readback");

@@ -100,7 +100,14 @@ cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const Build
 // Phase 2: write both node layouts and the leaf items; wide_sah (2 nseg
 // doubles, zeroed by the caller, may be null) receives the per-segment wide SAH.
 cudaError_t emit_blas(const BuildScratch &s, const BuildParams &bp, uint32_t wide_count, Node8Q *qn, Node8F *fn,
-                      TriRec *tris, double *wide_sah, cudaStream_t st);
+                      TriRec *tris, double *wide_sah, unsigned long long *rtab, cudaStream_t st);
+// Refit (build.cu): new triangle records and boxes for a BLAS block whose
+// topology is kept (rtab written by its build), from the segments' current
+// buffers; bottom-up over the W wide nodes, then both node layouts re-encoded.
+// Every segment must hold triangles (an empty segment's root is not written).
+// counters: W words of scratch; ctl: kCtlWords zeroed words (errors).
+cudaError_t refit_blas(const SegInput *segs, uint32_t nseg, uint32_t W, const unsigned long long *rtab, Node8Q *qn,
+                       Node8F *fn, TriRec *tris, uint32_t *counters, uint32_t *ctl, cudaStream_t st);
 cudaError_t emit_tlas(const InstState *inst, const BuildScratch &s, const BuildParams &bp, uint32_t wide_count,
                       Node8Q *qn, Node8F *fn, InstRec *recs, double *wide_sah, cudaStream_t st);
 

@@ -25,7 +25,7 @@ def test_version_and_error_string(lcx):
 def test_struct_sizes():
     assert ctypes.sizeof(_capi.LcxAccelOption) == 8
     assert ctypes.sizeof(_capi.LcxMeshBuildCommand) == 64
-    assert ctypes.sizeof(_capi.LcxAccelStats) == 48
+    assert ctypes.sizeof(_capi.LcxAccelStats) == 56
     assert ctypes.sizeof(_capi.LcxPtStats) == 32
 
 
