@@ -219,6 +219,21 @@ LCX_API int lcx_accel_stats(uint64_t accel, LcxAccelStats *out);
 
 /* ----------------------------------------------------------------- queries */
 
+/* Device view of a built accel, for lcx::ray_query in user CUDA kernels
+ * (include/lcx/ray_query.cuh: RayQuery with per-candidate callbacks,
+ * include/luisa/dsl/rtx/ray_query.h:17-240).  The reference hands the accel
+ * to kernels through its DSL binding; this is that handle as plain pointers.
+ * Valid until the accel is built again or destroyed, or a mesh it instances
+ * is rebuilt or refit.  Fails like a trace call on an accel that is not
+ * ready (LCX_ERR_NOT_BUILT, LCX_ERR_DEPTH). */
+typedef struct LcxAccelView {
+    const void *tlas_nodes;  /* the TLAS's 8-bit quantised nodes (device) */
+    const void *instances;   /* its leaf instance records (device) */
+    uint32_t stack_need;     /* stack entries a query needs (<= 32) */
+    uint32_t _pad;
+} LcxAccelView;
+LCX_API int lcx_accel_device_view(uint64_t accel, LcxAccelView *out);
+
 /* trace_closest over a batch: CPU accel.rs:449-509, CUDA
  * cuda_device_resource.h:1784-1807.  d_rays / d_hits are device arrays of
  * `ray_count` records.  An instance is eligible when (vis_mask & mask) != 0

@@ -56,6 +56,10 @@ class LcxPtParams(ctypes.Structure):
                 ("env", ctypes.c_float * 3)]
 
 
+class LcxAccelView(ctypes.Structure):
+    _fields_ = [("tlas_nodes", c_void_p), ("instances", c_void_p), ("stack_need", c_uint32), ("_pad", c_uint32)]
+
+
 class LcxPtStats(ctypes.Structure):
     _fields_ = [("closest_rays", c_uint64), ("any_rays", c_uint64), ("bounces", c_uint32), ("ms", ctypes.c_float),
                 ("launches", c_uint32), ("_pad", c_uint32)]
@@ -79,6 +83,7 @@ _SIGS = {
     "lcx_set_build_tuning": (c_int, [c_uint32, c_uint32]),
     "lcx_get_build_tuning": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),
     "lcx_set_build_morton": (c_int, [c_uint32, c_uint32, c_uint32]),
+    "lcx_accel_device_view": (c_int, [c_uint64, POINTER(LcxAccelView)]),
     "lcx_get_build_morton": (c_int, [POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
     "lcx_set_trace_reorder": (c_int, [c_uint32, c_uint32]),
     "lcx_set_trace_stack": (c_int, [c_uint32]),

@@ -32,11 +32,15 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblcx_accel.so")
 
 
+PUBLIC_HEADERS = ["lcx_accel.h", "lcx/bvh_device.cuh", "lcx/node_test.cuh"]
+
+
 def _stamp() -> str:
     h = hashlib.sha256()
     for f in SOURCES + HEADERS:
         h.update((CSRC / f).read_bytes())
-    h.update((ROOT / "include" / "lcx_accel.h").read_bytes())
+    for f in PUBLIC_HEADERS:
+        h.update((ROOT / "include" / f).read_bytes())
     h.update(" ".join(NVCC_FLAGS).encode())
     h.update(os.uname().machine.encode())
     return h.hexdigest()

@@ -911,6 +911,28 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     return released;
 }
 
+int lcx_accel_device_view(uint64_t accel, LcxAccelView *out) {
+    if (!out) return fail(LCX_ERR_INVALID_ARG, "lcx_accel_device_view: out is null");
+    auto a = find_accel(accel);
+    if (!a) return fail(LCX_ERR_INVALID_ARG, "unknown accel handle %llu", (unsigned long long)accel);
+    std::lock_guard<std::mutex> lk(a->mtx);
+    if (!a->built) return fail(LCX_ERR_NOT_BUILT, "accel not built");
+    for (const auto &mg : a->mesh_gens) {
+        auto m = find_mesh(mg.first);
+        if (!m || m->generation != mg.second)
+            return fail(LCX_ERR_NOT_BUILT, "a mesh of the accel was destroyed, rebuilt or refit; rebuild the accel");
+    }
+    const uint32_t need = a->depth + a->max_blas_depth + 3;
+    if (int(need) > kStackSize)
+        return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the query stack (%d)", a->depth,
+                    a->max_blas_depth, kStackSize);
+    out->tlas_nodes = a->qn;
+    out->instances = a->recs;
+    out->stack_need = need;
+    out->_pad = 0;
+    return LCX_OK;
+}
+
 int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout, void *stream) {
     if (count == 0) return LCX_OK;
     if (!jobs) return fail(LCX_ERR_INVALID_ARG, "lcx_trace_jobs: jobs is null");

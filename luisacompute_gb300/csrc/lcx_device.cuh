@@ -1,280 +1,4 @@
-// lcx_device.cuh — device-side layouts and arithmetic of the sm_103a
-// acceleration-structure path.
-//
-// HBM layout of one BVH (BLAS over triangles, TLAS over instances):
-//   * wide nodes, 8 children each, stored twice:
-//       Node8Q  80 B  child boxes quantised to 8 bits relative to the node box,
-//                     rounded outward (5 x 16 B vector loads);
-//       Node8F 208 B  child boxes in FP32 (13 x 16 B vector loads);
-//     internal children of a node are contiguous from `child_base`, leaf
-//     items of a node are contiguous from `item_base`, so a node names its
-//     whole subtree frontier with two integers and eight meta bytes.
-//   * leaf items in traversal order: TriRec (48 B, the three vertices as
-//     float4, prim id in v0.w) for a BLAS, InstRec (80 B) for a TLAS.
-// Child slots are assigned by octant (the child whose centroid lies toward
-// octant s goes to slot s), so a ray visits slots in order s ^ (octant ^ 7),
-// an approximately front-to-back order without sorting.
+// The device-side layouts and arithmetic live in the public header, which
+// user kernels that call lcx::ray_query (include/lcx/ray_query.cuh) share.
 #pragma once
-
-#include <cstdint>
-#include <cuda_runtime.h>
-
-namespace lcx {
-
-constexpr uint32_t kInvalid = 0xffffffffu;
-constexpr int kWide = 8;
-constexpr int kMaxLeafItems = 3;    // items per leaf slot (meta holds a 2-bit count)
-constexpr int kStackSize = 32;      // traversal stack entries per thread
-constexpr int kMaxLevels = 64;      // wide-tree depth limit of the collapse
-
-// Meta byte of a child slot: (bits << 5) | index.  A hit child contributes
-// `bits << index` to a 32-bit hit word: internal children have bits = 1 and
-// index 24 + slot (so their hits land in bits 24..31, reordered front to back
-// by XOR with the ray's octant), leaves have bits = 2^count - 1 (count 1..3)
-// and index = offset of their items (0..23).  0 = empty or unreachable.
-constexpr uint32_t kMetaInternalBase = 0x38;  // (1 << 5) | 24
-__host__ __device__ __forceinline__ bool meta_internal(uint32_t m) { return m != 0u && (m & 0x18u) == 0x18u; }
-__host__ __device__ __forceinline__ uint32_t meta_leaf(uint32_t count, uint32_t offset) {
-    return (((1u << count) - 1u) << 5) | offset;
-}
-__device__ __forceinline__ uint32_t meta_count(uint32_t m) { return __popc(m >> 5); }
-// Quantised boxes: exponents give (hi - lo) / e <= kQuantRange and the stored
-// origin is one step below the node box, so every stored plane can be moved
-// one step outward; the traversal's folded decode is then conservative.
-constexpr float kQuantRange = 252.0f;
-
-struct __align__(16) Node8Q {
-    float px, py, pz;   // quantisation origin (node box lower corner)
-    uint32_t exps;      // ex | ey << 8 | ez << 16 | imask << 24
-    uint32_t child_base;
-    uint32_t item_base;
-    uint32_t meta_lo, meta_hi;
-    uint32_t qlo_x[2], qlo_y[2], qlo_z[2], qhi_x[2], qhi_y[2], qhi_z[2];
-};
-static_assert(sizeof(Node8Q) == 80, "Node8Q is 80 B");
-
-struct __align__(16) Node8F {
-    float lo_x[8], hi_x[8], lo_y[8], hi_y[8], lo_z[8], hi_z[8];
-    uint32_t child_base;
-    uint32_t item_base;
-    uint32_t meta_lo, meta_hi;
-};
-static_assert(sizeof(Node8F) == 208, "Node8F is 208 B");
-
-struct __align__(16) TriRec {
-    float4 v0;  // xyz, w = prim id bits
-    float4 v1;
-    float4 v2;
-};
-static_assert(sizeof(TriRec) == 48, "TriRec is 48 B");
-
-// Device descriptor of a built BLAS (one per mesh handle, fixed address).
-struct __align__(16) BlasDesc {
-    const Node8Q *qnodes;
-    const Node8F *fnodes;
-    const TriRec *tris;
-    uint32_t node_count;
-    uint32_t tri_count;
-    float lo[3];
-    uint32_t depth;
-    float hi[3];
-    uint32_t valid;  // 1 when built with at least one triangle
-};
-
-// Instance as stored in TLAS leaf order.
-struct __align__(16) InstRec {
-    float w2o[12];            // world-to-object, row-major 3x4
-    const Node8Q *qnodes;
-    const TriRec *tris;
-    const Node8F *fnodes;
-    uint32_t inst_id;
-    uint32_t mask;
-};
-static_assert(sizeof(InstRec) == 80, "InstRec is 80 B");
-
-// Instance state by instance index (what Modifications edit).
-struct __align__(16) InstState {
-    float o2w[12];
-    const BlasDesc *blas;     // null = no mesh
-    uint32_t mask;
-    uint32_t user_id;
-    uint32_t opaque;
-    uint32_t _pad[3];
-};
-static_assert(sizeof(InstState) == 80, "InstState is 80 B");
-
-struct __align__(16) ModRec {  // == LcxModification with primitive translated
-    uint32_t index, user_id, flags, vis_mask;
-    float affine[12];
-    uint64_t primitive;  // BlasDesc device address (0 = none)
-    uint64_t _pad;
-};
-static_assert(sizeof(ModRec) == 80, "ModRec is 80 B");
-
-struct __align__(16) Ray {
-    float ox, oy, oz, tmin;
-    float dx, dy, dz, tmax;
-};
-
-struct __align__(8) Hit {
-    uint32_t inst, prim;
-    float u, v;
-    float t;
-    uint32_t pad;
-};
-
-// ------------------------------------------------------------------------
-// The FP32 operation sequences below are reproduced bit for bit by the
-// oracle (explicit fma, every other operation separately rounded).
-
-// Affine inverse of a row-major 3x4 object-to-world matrix
-// (include/luisa/runtime/rhi/command.h:557-571 layout).
-__device__ __forceinline__ void affine_inverse(const float *m, float *w) {
-    const float a = m[0], b = m[1], c = m[2];
-    const float d = m[4], e = m[5], f = m[6];
-    const float g = m[8], h = m[9], i = m[10];
-    const float c00 = __fmaf_rn(e, i, -__fmul_rn(f, h));
-    const float c01 = __fmaf_rn(f, g, -__fmul_rn(d, i));
-    const float c02 = __fmaf_rn(d, h, -__fmul_rn(e, g));
-    const float det = __fmaf_rn(a, c00, __fmaf_rn(b, c01, __fmul_rn(c, c02)));
-    const float r = __fdiv_rn(1.0f, det);
-    float R[9];
-    R[0] = __fmul_rn(c00, r);
-    R[1] = __fmul_rn(__fmaf_rn(c, h, -__fmul_rn(b, i)), r);
-    R[2] = __fmul_rn(__fmaf_rn(b, f, -__fmul_rn(c, e)), r);
-    R[3] = __fmul_rn(c01, r);
-    R[4] = __fmul_rn(__fmaf_rn(a, i, -__fmul_rn(c, g)), r);
-    R[5] = __fmul_rn(__fmaf_rn(c, d, -__fmul_rn(a, f)), r);
-    R[6] = __fmul_rn(c02, r);
-    R[7] = __fmul_rn(__fmaf_rn(b, g, -__fmul_rn(a, h)), r);
-    R[8] = __fmul_rn(__fmaf_rn(a, e, -__fmul_rn(b, d)), r);
-    const float tx = m[3], ty = m[7], tz = m[11];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        w[4 * k + 0] = R[3 * k + 0];
-        w[4 * k + 1] = R[3 * k + 1];
-        w[4 * k + 2] = R[3 * k + 2];
-        w[4 * k + 3] = -__fmaf_rn(R[3 * k + 0], tx, __fmaf_rn(R[3 * k + 1], ty, __fmul_rn(R[3 * k + 2], tz)));
-    }
-}
-
-// World ray -> object ray.
-__device__ __forceinline__ void transform_point(const float *w, float x, float y, float z, float &ox, float &oy,
-                                                float &oz) {
-    ox = __fmaf_rn(w[0], x, __fmaf_rn(w[1], y, __fmaf_rn(w[2], z, w[3])));
-    oy = __fmaf_rn(w[4], x, __fmaf_rn(w[5], y, __fmaf_rn(w[6], z, w[7])));
-    oz = __fmaf_rn(w[8], x, __fmaf_rn(w[9], y, __fmaf_rn(w[10], z, w[11])));
-}
-__device__ __forceinline__ void transform_dir(const float *w, float x, float y, float z, float &ox, float &oy,
-                                              float &oz) {
-    ox = __fmaf_rn(w[0], x, __fmaf_rn(w[1], y, __fmul_rn(w[2], z)));
-    oy = __fmaf_rn(w[4], x, __fmaf_rn(w[5], y, __fmul_rn(w[6], z)));
-    oz = __fmaf_rn(w[8], x, __fmaf_rn(w[9], y, __fmul_rn(w[10], z)));
-}
-
-// Watertight ray/triangle test (Woop, Benthin, Wald, JCGT 2013), per-ray part.
-struct WtRay {
-    float ox, oy, oz;
-    float Sx, Sy, Sz;
-    uint32_t perm;  // kx | ky << 2 | kz << 4
-};
-
-__device__ __forceinline__ float pick3(uint32_t k, float a, float b, float c) {
-    return k == 0 ? a : (k == 1 ? b : c);
-}
-
-__device__ __forceinline__ WtRay wt_setup(float ox, float oy, float oz, float dx, float dy, float dz) {
-    WtRay r;
-    r.ox = ox;
-    r.oy = oy;
-    r.oz = oz;
-    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
-    const uint32_t kz = (ax >= ay) ? ((ax >= az) ? 0u : 2u) : ((ay >= az) ? 1u : 2u);
-    uint32_t kx = kz + 1 == 3 ? 0 : kz + 1;
-    uint32_t ky = kx + 1 == 3 ? 0 : kx + 1;
-    const float dkz = pick3(kz, dx, dy, dz);
-    if (dkz < 0.0f) {
-        const uint32_t t = kx;
-        kx = ky;
-        ky = t;
-    }
-    const float dkx = pick3(kx, dx, dy, dz), dky = pick3(ky, dx, dy, dz);
-    r.Sz = __fdiv_rn(1.0f, dkz);
-    r.Sx = __fmul_rn(dkx, r.Sz);
-    r.Sy = __fmul_rn(dky, r.Sz);
-    r.perm = kx | (ky << 2) | (kz << 4);
-    return r;
-}
-
-// Per-triangle part: returns true for a hit with t in [tmin, tmax].
-__device__ __forceinline__ bool wt_intersect(const WtRay &r, float tmin, float tmax, const float4 &v0,
-                                             const float4 &v1, const float4 &v2, float &t_out, float &u_out,
-                                             float &v_out) {
-    const uint32_t kx = r.perm & 3u, ky = (r.perm >> 2) & 3u, kz = (r.perm >> 4) & 3u;
-    const float a0 = __fsub_rn(v0.x, r.ox), a1 = __fsub_rn(v0.y, r.oy), a2 = __fsub_rn(v0.z, r.oz);
-    const float b0 = __fsub_rn(v1.x, r.ox), b1 = __fsub_rn(v1.y, r.oy), b2 = __fsub_rn(v1.z, r.oz);
-    const float c0 = __fsub_rn(v2.x, r.ox), c1 = __fsub_rn(v2.y, r.oy), c2 = __fsub_rn(v2.z, r.oz);
-    const float Akx = pick3(kx, a0, a1, a2), Aky = pick3(ky, a0, a1, a2), Akz = pick3(kz, a0, a1, a2);
-    const float Bkx = pick3(kx, b0, b1, b2), Bky = pick3(ky, b0, b1, b2), Bkz = pick3(kz, b0, b1, b2);
-    const float Ckx = pick3(kx, c0, c1, c2), Cky = pick3(ky, c0, c1, c2), Ckz = pick3(kz, c0, c1, c2);
-    const float Ax = __fmaf_rn(-r.Sx, Akz, Akx);
-    const float Ay = __fmaf_rn(-r.Sy, Akz, Aky);
-    const float Bx = __fmaf_rn(-r.Sx, Bkz, Bkx);
-    const float By = __fmaf_rn(-r.Sy, Bkz, Bky);
-    const float Cx = __fmaf_rn(-r.Sx, Ckz, Ckx);
-    const float Cy = __fmaf_rn(-r.Sy, Ckz, Cky);
-    // edge functions with separately rounded products: swapping two vertices
-    // negates them exactly, which keeps shared edges watertight
-    const float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
-    const float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
-    const float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
-    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
-    const float det = __fadd_rn(__fadd_rn(U, V), W);
-    if (det == 0.0f) return false;
-    const float Az = __fmul_rn(r.Sz, Akz);
-    const float Bz = __fmul_rn(r.Sz, Bkz);
-    const float Cz = __fmul_rn(r.Sz, Ckz);
-    const float T = __fmaf_rn(U, Az, __fmaf_rn(V, Bz, __fmul_rn(W, Cz)));
-    const float t = __fdiv_rn(T, det);
-    if (!(t >= tmin && t <= tmax)) return false;
-    t_out = t;
-    u_out = __fdiv_rn(V, det);
-    v_out = __fdiv_rn(W, det);
-    return true;
-}
-
-// Reciprocal for slab tests: IEEE, so a zero component gives +-inf.  A ray
-// lying in a slab plane then yields 0 * inf = NaN for that plane, which
-// fminf/fmaxf ignore: the slab does not constrain the ray, as it must not.
-// (Clamping 1/0 to a large finite value instead lets rounding decide the
-// sign of a ray that lies exactly in a box face, and culls it.)
-// The approximate MUFU reciprocal (rcp.approx: 1 ulp, +-0 -> +-inf) is enough:
-// the slab acceptance carries a 2^-18 relative slack.
-__device__ __forceinline__ float slab_rcp(float x) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
-// Conservative slab acceptance: exit distance widened by 2^-18 relative.
-__device__ __forceinline__ bool slab_accept(float tn, float tf) { return tn <= __fmaf_rn(fabsf(tf), 0x1p-18f, tf); }
-
-// Ordered-int encoding of floats for atomicMin/atomicMax.
-__device__ __forceinline__ uint32_t float_to_ordered(float f) {
-    const uint32_t u = __float_as_uint(f);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__host__ __device__ __forceinline__ float ordered_to_float(uint32_t u) {
-#ifdef __CUDA_ARCH__
-    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
-#else
-    union {
-        uint32_t u;
-        float f;
-    } x;
-    x.u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
-    return x.f;
-#endif
-}
-
-}  // namespace lcx
+#include "lcx/bvh_device.cuh"
