@@ -62,7 +62,7 @@ struct __align__(16) Node8F {
 static_assert(sizeof(Node8F) == 208, "Node8F is 208 B");
 
 struct __align__(16) TriRec {
-    float4 v0;  // xyz, w = prim id bits
+    float4 v0;  // xyz, w = prim id bits (procedural BLAS: v0 = AABB min + prim id, v1 = AABB max)
     float4 v1;
     float4 v2;
 };
@@ -78,8 +78,12 @@ struct __align__(16) BlasDesc {
     float lo[3];
     uint32_t depth;
     float hi[3];
-    uint32_t valid;  // 1 when built with at least one triangle
+    uint32_t valid;  // bit 0: built with at least one item; bit 1: procedural (AABB items)
 };
+// InstRec.mask of a procedural instance: its visibility mask in bits 8..15 and
+// bit 31 set, so the trace kernels' test (ray mask & mask), ray masks being
+// 8 bits, never enters it; lcx::ray_query decodes it.
+constexpr uint32_t kInstProcedural = 0x80000000u;
 
 // Instance as stored in TLAS leaf order.
 struct __align__(16) InstRec {

@@ -46,19 +46,45 @@ enum CandidateAction : int {
     kTerminate = 3            // end the query without committing it
 };
 
-// One ray against `view`.  `mask`: instances with (mask & instance mask) == 0
-// are skipped.  Returns the closest committed hit, or the miss record
-// {~0u, ~0u, (0,0), t_max}.
-template <class OnCandidate>
-__device__ LcxTriangleHit ray_query(const LcxAccelView &view, const LcxRay &ray, uint32_t mask,
-                                    OnCandidate &&on_candidate) {
+// An AABB of a procedural primitive the ray passes through (the reference's
+// ProceduralCandidate, ray_query.h:43-66): the callback intersects its own
+// primitive and commits a distance.
+struct ProceduralCandidate {
+    uint32_t inst, prim;
+    float aabb_min[3], aabb_max[3];  // object space, as built
+    float obj_origin[3], obj_dir[3]; // the ray in the instance's object space (same t as in world space)
+    LcxRay ray;                      // the world ray; t_max = the closest committed distance so far
+};
+struct ProceduralDecision {
+    int action;  // CandidateAction
+    float t;     // distance committed with kCommit / kCommitAndTerminate; kept iff t_min <= t < ray.t_max
+};
+
+// Committed hit of a query with procedural primitives (the reference's
+// CommittedHit, cpu_kernel_defs/src/lib.rs:70-76).
+enum HitType : uint32_t { kHitMiss = 0, kHitTriangle = 1, kHitProcedural = 2 };
+struct CommittedHit {
+    uint32_t inst, prim;
+    float bary_u, bary_v;  // triangles only
+    uint32_t type;         // HitType
+    float t;               // t_max of the ray for a miss
+};
+
+// One ray against `view`, triangles and procedural primitives.  `mask`:
+// instances with (mask & instance mask) == 0 are skipped.  Returns the closest
+// committed hit; a miss is {~0u, ~0u, (0,0), kHitMiss, t_max}.
+template <class OnCandidate, class OnProcedural>
+__device__ CommittedHit ray_query(const LcxAccelView &view, const LcxRay &ray, uint32_t mask,
+                                  OnCandidate &&on_candidate, OnProcedural &&on_procedural) {
     const Node8Q *tlas = static_cast<const Node8Q *>(view.tlas_nodes);
     const InstRec *insts = static_cast<const InstRec *>(view.instances);
     const float wox = ray.origin[0], woy = ray.origin[1], woz = ray.origin[2];
     const float wdx = ray.direction[0], wdy = ray.direction[1], wdz = ray.direction[2];
     const float tmin = ray.t_min;
     float best_t = ray.t_max, best_u = 0.0f, best_v = 0.0f;
-    uint32_t best_inst = kInvalid, best_prim = kInvalid;
+    uint32_t best_inst = kInvalid, best_prim = kInvalid, best_type = kHitMiss;
+    bool cur_proc = false;
+    float odx = 0.0f, ody = 0.0f, odz = 0.0f;  // object-space direction of the current instance
     mask &= 0xffu;
 
     float ox = wox, oy = woy, oz = woz;
@@ -87,7 +113,46 @@ __device__ LcxTriangleHit ray_query(const LcxAccelView &view, const LcxRay &ray,
             Gt = G;
             G = make_uint2(0, 0);
         }
-        if (in_blas) {
+        if (in_blas && cur_proc) {
+            while (Gt.y && !stop) {  // procedural candidates: AABBs the ray passes through
+                const uint32_t k = __ffs(Gt.y) - 1u;
+                Gt.y &= Gt.y - 1u;
+                const float4 *tp = reinterpret_cast<const float4 *>(tris + Gt.x + k);
+                const float4 lo = __ldg(tp), hi = __ldg(tp + 1);
+                const float tnx = ((ix < 0.0f ? hi.x : lo.x) - ox) * ix, tfx = ((ix < 0.0f ? lo.x : hi.x) - ox) * ix;
+                const float tny = ((iy < 0.0f ? hi.y : lo.y) - oy) * iy, tfy = ((iy < 0.0f ? lo.y : hi.y) - oy) * iy;
+                const float tnz = ((iz < 0.0f ? hi.z : lo.z) - oz) * iz, tfz = ((iz < 0.0f ? lo.z : hi.z) - oz) * iz;
+                const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+                const float tf = fminf(fminf(tfx, tfy), fminf(tfz, best_t));
+                if (!slab_accept(tn, tf)) continue;
+                ProceduralCandidate pc;
+                pc.inst = cur_inst;
+                pc.prim = __float_as_uint(lo.w);
+                pc.aabb_min[0] = lo.x;
+                pc.aabb_min[1] = lo.y;
+                pc.aabb_min[2] = lo.z;
+                pc.aabb_max[0] = hi.x;
+                pc.aabb_max[1] = hi.y;
+                pc.aabb_max[2] = hi.z;
+                pc.obj_origin[0] = ox;
+                pc.obj_origin[1] = oy;
+                pc.obj_origin[2] = oz;
+                pc.obj_dir[0] = odx;
+                pc.obj_dir[1] = ody;
+                pc.obj_dir[2] = odz;
+                pc.ray = ray;
+                pc.ray.t_max = best_t;
+                const ProceduralDecision dec = on_procedural(pc);
+                if ((dec.action == kCommit || dec.action == kCommitAndTerminate) && dec.t >= tmin && dec.t < best_t) {
+                    best_t = dec.t;
+                    best_u = best_v = 0.0f;
+                    best_inst = cur_inst;
+                    best_prim = pc.prim;
+                    best_type = kHitProcedural;
+                }
+                if (dec.action == kCommitAndTerminate || dec.action == kTerminate) stop = true;
+            }
+        } else if (in_blas) {
             while (Gt.y && !stop) {  // candidate triangles
                 const uint32_t k = __ffs(Gt.y) - 1u;
                 Gt.y &= Gt.y - 1u;
@@ -104,6 +169,7 @@ __device__ LcxTriangleHit ray_query(const LcxAccelView &view, const LcxRay &ray,
                         best_v = v;
                         best_inst = cur_inst;
                         best_prim = prim;
+                        best_type = kHitTriangle;
                     }
                 }
                 if (act == kCommitAndTerminate || act == kTerminate) stop = true;
@@ -114,7 +180,8 @@ __device__ LcxTriangleHit ray_query(const LcxAccelView &view, const LcxRay &ray,
                 Gt.y &= Gt.y - 1u;
                 const uint4 *ip = reinterpret_cast<const uint4 *>(insts + Gt.x + k);
                 const uint4 m4 = __ldg(ip + 4);  // fnodes (x,y), inst id (z), mask (w)
-                if ((m4.w & mask) == 0u) continue;
+                const bool proc = (m4.w & kInstProcedural) != 0u;
+                if ((((proc ? m4.w >> 8 : m4.w) & 0xffu) & mask) == 0u) continue;
                 const float4 r0 = __ldg(reinterpret_cast<const float4 *>(ip));
                 const float4 r1 = __ldg(reinterpret_cast<const float4 *>(ip + 1));
                 const float4 r2 = __ldg(reinterpret_cast<const float4 *>(ip + 2));
@@ -130,6 +197,10 @@ __device__ LcxTriangleHit ray_query(const LcxAccelView &view, const LcxRay &ray,
                 iz = slab_rcp(dz);
                 octinv = octant_inv(dx, dy, dz);
                 wt = wt_setup(ox, oy, oz, dx, dy, dz);
+                odx = dx;
+                ody = dy;
+                odz = dz;
+                cur_proc = proc;
                 blas = reinterpret_cast<const Node8Q *>((unsigned long long)pp.x | ((unsigned long long)pp.y << 32));
                 tris = reinterpret_cast<const TriRec *>((unsigned long long)pp.z | ((unsigned long long)pp.w << 32));
                 cur_inst = m4.z;
@@ -154,12 +225,30 @@ __device__ LcxTriangleHit ray_query(const LcxAccelView &view, const LcxRay &ray,
             G = stk[--sp];
         }
     }
-    LcxTriangleHit h;
+    CommittedHit h;
     h.inst = best_inst;
     h.prim = best_prim;
-    h.bary[0] = best_u;
-    h.bary[1] = best_v;
-    h.committed_ray_t = best_t;
+    h.bary_u = best_u;
+    h.bary_v = best_v;
+    h.type = best_type;
+    h.t = best_t;
+    return h;
+}
+
+// Triangles only (procedural instances are passed over): the TriangleHit
+// record of the closest committed triangle.
+template <class OnCandidate>
+__device__ LcxTriangleHit ray_query(const LcxAccelView &view, const LcxRay &ray, uint32_t mask,
+                                    OnCandidate &&on_candidate) {
+    const CommittedHit c = ray_query(view, ray, mask, on_candidate, [](const ProceduralCandidate &) {
+        return ProceduralDecision{kSkip, 0.0f};
+    });
+    LcxTriangleHit h;
+    h.inst = c.inst;
+    h.prim = c.prim;
+    h.bary[0] = c.bary_u;
+    h.bary[1] = c.bary_v;
+    h.committed_ray_t = c.t;
     h._pad = 0u;
     return h;
 }

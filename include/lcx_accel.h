@@ -198,6 +198,33 @@ LCX_API int lcx_mesh_build_batch(const uint64_t *meshes, const LcxMeshBuildComma
 
 LCX_API int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out);
 
+/* ------------------------------------------------------ procedural primitive */
+
+/* ProceduralPrimitiveBuildCommand: include/luisa/runtime/rhi/command.h:488-512
+ * (CPU backend: accel.rs:84-141, Embree user geometry).  aabb_buffer: device
+ * address of `Aabb` records {float min[3]; float max[3];} (24 B,
+ * src/rust/luisa_compute_cpu_kernel_defs/src/lib.rs:56-59); size in bytes. */
+typedef struct LcxProceduralBuildCommand {
+    uint32_t request;          /* LCX_REQUEST_* */
+    uint32_t _pad;
+    uint64_t aabb_buffer;
+    size_t aabb_buffer_offset;
+    size_t aabb_buffer_size;
+} LcxProceduralBuildCommand;
+
+/* DeviceInterface::create_procedural_primitive / destroy_procedural_primitive:
+ * device_interface.h:174-175.  A procedural primitive is a BLAS over AABBs; an
+ * accel instances it like a mesh (Modification.primitive = its handle).  The
+ * trace calls (lcx_trace_*) do not see procedural instances, as the
+ * reference's trace_closest / trace_any do not; lcx::ray_query
+ * (include/lcx/ray_query.cuh) offers their AABB candidates to a callback that
+ * commits its own distance. */
+LCX_API int lcx_procedural_create(const LcxAccelOption *option, uint64_t *out_handle);
+LCX_API int lcx_procedural_destroy(uint64_t handle);
+/* Builds (PREFER_UPDATE with allow_update: refits) on `stream`, like
+ * lcx_mesh_build.  Empty boxes (min > max on an axis) are never reported. */
+LCX_API int lcx_procedural_build(uint64_t handle, const LcxProceduralBuildCommand *command, void *stream);
+
 /* ------------------------------------------------------------------ accel */
 
 /* DeviceInterface::create_accel / destroy_accel: device_interface.h:183-184. */

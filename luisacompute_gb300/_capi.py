@@ -56,6 +56,11 @@ class LcxPtParams(ctypes.Structure):
                 ("env", ctypes.c_float * 3)]
 
 
+class LcxProceduralBuildCommand(ctypes.Structure):
+    _fields_ = [("request", c_uint32), ("_pad", c_uint32), ("aabb_buffer", c_uint64),
+                ("aabb_buffer_offset", c_size_t), ("aabb_buffer_size", c_size_t)]
+
+
 class LcxAccelView(ctypes.Structure):
     _fields_ = [("tlas_nodes", c_void_p), ("instances", c_void_p), ("stack_need", c_uint32), ("_pad", c_uint32)]
 
@@ -84,6 +89,9 @@ _SIGS = {
     "lcx_get_build_tuning": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),
     "lcx_set_build_morton": (c_int, [c_uint32, c_uint32, c_uint32]),
     "lcx_accel_device_view": (c_int, [c_uint64, POINTER(LcxAccelView)]),
+    "lcx_procedural_create": (c_int, [POINTER(LcxAccelOption), POINTER(c_uint64)]),
+    "lcx_procedural_destroy": (c_int, [c_uint64]),
+    "lcx_procedural_build": (c_int, [c_uint64, POINTER(LcxProceduralBuildCommand), c_void_p]),
     "lcx_get_build_morton": (c_int, [POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
     "lcx_set_trace_reorder": (c_int, [c_uint32, c_uint32]),
     "lcx_set_trace_stack": (c_int, [c_uint32]),

@@ -23,7 +23,7 @@ from ._capi import (HINT_FAST_BUILD, HINT_FAST_TRACE, MOD_OPAQUE_OFF, MOD_OPAQUE
                     REQUEST_PREFER_UPDATE, LcxAccelOption, LcxAccelStats, LcxMeshBuildCommand, check)
 from .scenes import MOD_DTYPE
 
-__all__ = ["AccelOption", "Mesh", "Accel", "HINT_FAST_TRACE", "HINT_FAST_BUILD", "REQUEST_FORCE_BUILD",
+__all__ = ["AccelOption", "Mesh", "ProceduralPrimitive", "Accel", "HINT_FAST_TRACE", "HINT_FAST_BUILD", "REQUEST_FORCE_BUILD",
            "REQUEST_PREFER_UPDATE", "NODES_FP32", "NODES_QUANT8", "stream_handle"]
 
 
@@ -93,6 +93,46 @@ class Mesh:
     def destroy(self):
         if getattr(self, "handle", 0):
             check(self.lib.lcx_mesh_destroy(self.handle), "lcx_mesh_destroy")
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class ProceduralPrimitive:
+    """A BLAS over AABBs (include/luisa/runtime/rtx/procedural_primitive.h): ``aabbs`` is an (N, 6)
+    float32 CUDA tensor of (min xyz, max xyz) records, borrowed like a mesh's buffers.  Instanced by
+    an Accel like a Mesh; only lcx::ray_query (user kernels) reports its candidates."""
+
+    def __init__(self, aabbs, option: AccelOption | None = None):
+        torch = _torch()
+        self.lib = _capi.load()
+        if not aabbs.is_cuda or aabbs.dtype != torch.float32 or aabbs.dim() != 2 or aabbs.shape[1] != 6 \
+                or not aabbs.is_contiguous():
+            raise ValueError("aabbs must be a contiguous (N, 6) float32 CUDA tensor")
+        self.aabbs = aabbs
+        h = ctypes.c_uint64(0)
+        check(self.lib.lcx_procedural_create(ctypes.byref((option or AccelOption()).c()), ctypes.byref(h)),
+              "lcx_procedural_create")
+        self.handle = h.value
+
+    def build(self, request: int = REQUEST_FORCE_BUILD, stream=None) -> "ProceduralPrimitive":
+        cmd = _capi.LcxProceduralBuildCommand(request, 0, self.aabbs.data_ptr(), 0, self.aabbs.numel() * 4)
+        check(self.lib.lcx_procedural_build(self.handle, ctypes.byref(cmd), stream_handle(stream)),
+              "lcx_procedural_build")
+        return self
+
+    def stats(self) -> LcxAccelStats:
+        s = LcxAccelStats()
+        check(self.lib.lcx_mesh_stats(self.handle, ctypes.byref(s)), "lcx_mesh_stats")
+        return s
+
+    def destroy(self):
+        if getattr(self, "handle", 0):
+            check(self.lib.lcx_procedural_destroy(self.handle), "lcx_procedural_destroy")
             self.handle = 0
 
     def __del__(self):

@@ -129,13 +129,28 @@ __global__ void __launch_bounds__(kPrepBlock) k_tri_prep(const SegInput *segs, u
     if (in) {
         const SegInput g = segs[s];
         const uint32_t local = i - g.item_offset;
-        const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * local);
-        const uint32_t i0 = t[0], i1 = t[1], i2 = t[2];
         float4 l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f), h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
-        if (i0 >= g.vcount || i1 >= g.vcount || i2 >= g.vcount) {
+        uint32_t i0 = 0, i1 = 0, i2 = 0;
+        bool bad = false;
+        if (g.kind == kSegAabbs) {  // the item box is the AABB record (min xyz, max xyz)
+            const float *bx = reinterpret_cast<const float *>(g.vbase + 24ull * local);
+            l.x = bx[0];
+            l.y = bx[1];
+            l.z = bx[2];
+            h.x = bx[3];
+            h.y = bx[4];
+            h.z = bx[5];
+        } else {
+            const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * local);
+            i0 = t[0];
+            i1 = t[1];
+            i2 = t[2];
+            bad = i0 >= g.vcount || i1 >= g.vcount || i2 >= g.vcount;
+        }
+        if (bad) {
             atomicOr(&segctl[kSegWords * s + kSegErr], kErrBadIndex);
             atomicOr(&ctl[kCtlErr], kErrBadIndex);
-        } else {
+        } else if (g.kind != kSegAabbs) {
             const float4 a = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i0));
             const float4 b = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i1));
             const float4 cc = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i2));
@@ -176,7 +191,7 @@ __global__ void __launch_bounds__(kPrepBlock) k_inst_prep(const InstState *inst,
         for (int k = 0; k < 12; k++) w2o[12ull * i + k] = w[k];
         float4 l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f), h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
         const BlasDesc *d = s.blas;
-        if (d != nullptr && d->valid) {
+        if (d != nullptr && (d->valid & 1u)) {
             const float blo[3] = {d->lo[0], d->lo[1], d->lo[2]}, bhi[3] = {d->hi[0], d->hi[1], d->hi[2]};
             float wl[3], wh[3];
 #pragma unroll
@@ -671,6 +686,12 @@ __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *d
         tv, segs, desc, w, qn, fn, leaf_max, ctl, sah, rtab,
         [&](uint32_t pos, uint32_t prim, uint32_t s) {
             const SegInput &g = segs[s];
+            if (g.kind == kSegAabbs) {
+                const float *bx = reinterpret_cast<const float *>(g.vbase + 24ull * prim);
+                tris[pos] = TriRec{make_float4(bx[0], bx[1], bx[2], __uint_as_float(prim)),
+                                   make_float4(bx[3], bx[4], bx[5], 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
+                return;
+            }
             const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * prim);
             float4 a = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * t[0]));
             float4 b = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * t[1]));
@@ -698,7 +719,7 @@ __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *d
         bd->hi[1] = rh.y;
         bd->hi[2] = rh.z;
         bd->depth = sc[kSegDepth];
-        bd->valid = empty ? 0u : 1u;
+        bd->valid = (empty ? 0u : 1u) | (g.kind == kSegAabbs ? 2u : 0u);
     }
 }
 
@@ -716,12 +737,12 @@ __global__ void k_emit_tlas(TreeView tv, const SegInput *segs, const uint32_t *d
             for (int k = 0; k < 12; k++) r.w2o[k] = w2o[12ull * id + k];
             const InstState &s = inst[id];
             const BlasDesc *d = s.blas;
-            const bool ok = d != nullptr && d->valid;
+            const bool ok = d != nullptr && (d->valid & 1u);
             r.qnodes = ok ? d->qnodes : nullptr;
             r.tris = ok ? d->tris : nullptr;
             r.fnodes = ok ? d->fnodes : nullptr;
             r.inst_id = id;
-            r.mask = ok ? (s.mask & 0xffu) : 0u;
+            r.mask = !ok ? 0u : (d->valid & 2u) ? (((s.mask & 0xffu) << 8) | kInstProcedural) : (s.mask & 0xffu);
             recs[pos] = r;
         },
         rl, rh);
@@ -947,6 +968,20 @@ __global__ void k_refit(const SegInput *segs, uint32_t nseg, uint32_t W, const u
                         atomicOr(&ctl[kCtlErr], kErrBadIndex);
                         continue;
                     }
+                    if (g.kind == kSegAabbs) {
+                        const float *bx = reinterpret_cast<const float *>(g.vbase + 24ull * prim);
+                        const float il[3] = {bx[0], bx[1], bx[2]}, ih[3] = {bx[3], bx[4], bx[5]};
+                        if (!box3_empty(il, ih)) {
+#pragma unroll
+                            for (int k = 0; k < 3; k++) {
+                                cl[k] = fminf(cl[k], il[k]);
+                                ch[k] = fmaxf(ch[k], ih[k]);
+                            }
+                        }
+                        *r = TriRec{make_float4(il[0], il[1], il[2], __uint_as_float(prim)),
+                                    make_float4(ih[0], ih[1], ih[2], 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
+                        continue;
+                    }
                     const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * prim);
                     const uint32_t i0 = t[0], i1 = t[1], i2 = t[2];
                     if (i0 >= g.vcount || i1 >= g.vcount || i2 >= g.vcount) {
@@ -991,7 +1026,7 @@ __global__ void k_refit(const SegInput *segs, uint32_t nseg, uint32_t W, const u
                     bd->lo[k] = empty ? FLT_MAX : nl[k];
                     bd->hi[k] = empty ? -FLT_MAX : nh[k];
                 }
-                bd->valid = empty ? 0u : 1u;
+                bd->valid = (empty ? 0u : 1u) | (g.kind == kSegAabbs ? 2u : 0u);
             }
             return;
         }

@@ -117,6 +117,7 @@ struct MeshObj {
     double *wide_sah = nullptr;       // in `block`: 2 doubles of this mesh's segment
     size_t mem_bytes = 0;             // this mesh's share of the block
     uint32_t node_count = 0, tri_count = 0, depth = 0;
+    uint32_t kind = kSegTriangles;  // or kSegAabbs: a procedural primitive (lcx_procedural_*)
     uint32_t seg = 0;  // segment (position in its build) within `block`
     uint64_t refits = 0;  // refits since the last full build
     bool built = false;
@@ -302,8 +303,8 @@ constexpr int kNoRefit = 1;  // try_refit: the call is not a refit; build instea
 // the block is refit in place (same topology, new triangle records and boxes)
 // instead of rebuilt.  One host synchronisation, to report bad indices.
 // `segs`: the call's validated segments in call order.  Otherwise kNoRefit.
-int try_refit(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand *cmds, const std::vector<SegInput> &segs,
-              cudaStream_t st) {
+int try_refit(const std::vector<MeshObj *> &meshes, const std::vector<uint32_t> &requests,
+              const std::vector<SegInput> &segs, cudaStream_t st) {
     const size_t count = meshes.size();
     DevBlock *blk = meshes[0]->block.get();
     if (!blk || !blk->rtab || blk->nseg != count) return kNoRefit;
@@ -311,7 +312,7 @@ int try_refit(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand *c
     std::vector<bool> seen(count, false);
     for (size_t i = 0; i < count; i++) {
         const MeshObj *m = meshes[i];
-        if (cmds[i].request != LCX_REQUEST_PREFER_UPDATE || !m->opt.allow_update || !m->built ||
+        if (requests[i] != LCX_REQUEST_PREFER_UPDATE || !m->opt.allow_update || !m->built ||
             m->block.get() != blk || m->seg >= count || seen[m->seg] || segs[i].item_count != m->tri_count ||
             segs[i].item_count == 0)
             return kNoRefit;
@@ -347,12 +348,16 @@ int try_refit(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand *c
     return LCX_OK;
 }
 
-int build_meshes(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand *cmds, cudaStream_t st,
-                 Retired &retired) {
+// Segments of mesh build commands (validated), item offsets in call order.
+int mesh_segments(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand *cmds, std::vector<SegInput> &segs,
+                  std::vector<uint32_t> &requests) {
     const size_t count = meshes.size();
-    std::vector<SegInput> segs(count);
+    segs.assign(count, SegInput{});
+    requests.assign(count, 0u);
     uint64_t total = 0;
     for (size_t i = 0; i < count; i++) {
+        if (meshes[i]->kind != kSegTriangles)
+            return fail(LCX_ERR_INVALID_ARG, "entry %zu: a procedural primitive takes lcx_procedural_build", i);
         uint64_t tri64 = 0, v64 = 0;
         if (int r = validate_mesh_command(&cmds[i], tri64, v64)) return r;
         SegInput &g = segs[i];
@@ -362,14 +367,24 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const LcxMeshBuildCommand
         g.vcount = uint32_t(v64);
         g.item_offset = uint32_t(total);
         g.item_count = uint32_t(tri64);
-        g._pad = 0;
+        g.kind = kSegTriangles;
         g.desc = meshes[i]->d_desc;
+        requests[i] = cmds[i].request;
         total += tri64;
         if (total >= (1ull << 31)) return fail(LCX_ERR_INVALID_ARG, "batch too large (%llu triangles)",
                                                (unsigned long long)total);
     }
+    return LCX_OK;
+}
+
+// Builds (or refits) the BVHs of `meshes` from their segments in one pass.
+int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInput> &segs,
+                 const std::vector<uint32_t> &requests, cudaStream_t st, Retired &retired) {
+    const size_t count = meshes.size();
+    uint64_t total = 0;
+    for (const SegInput &g : segs) total += g.item_count;
     {
-        const int r = try_refit(meshes, cmds, segs, st);
+        const int r = try_refit(meshes, requests, segs, st);
         if (r != kNoRefit) return r;
     }
     const BuildParams bp = build_params_for(meshes[0]->opt);
@@ -576,13 +591,61 @@ int lcx_mesh_destroy(uint64_t mesh) {
     return LCX_OK;
 }
 
+int lcx_procedural_create(const LcxAccelOption *option, uint64_t *out_handle) {
+    if (int r = lcx_mesh_create(option, out_handle)) return r;
+    auto m = find_mesh(*out_handle);
+    m->kind = kSegAabbs;
+    return LCX_OK;
+}
+
+int lcx_procedural_destroy(uint64_t handle) {
+    auto m = find_mesh(handle);
+    if (m && m->kind != kSegAabbs) return fail(LCX_ERR_INVALID_ARG, "lcx_procedural_destroy: handle is a mesh");
+    return lcx_mesh_destroy(handle);
+}
+
+int lcx_procedural_build(uint64_t handle, const LcxProceduralBuildCommand *cmd, void *stream) {
+    auto m = find_mesh(handle);
+    if (!m || m->kind != kSegAabbs)
+        return fail(LCX_ERR_INVALID_ARG, "lcx_procedural_build: unknown procedural primitive handle %llu",
+                    (unsigned long long)handle);
+    if (!cmd) return fail(LCX_ERR_INVALID_ARG, "lcx_procedural_build: command is null");
+    if (cmd->request > LCX_REQUEST_FORCE_BUILD) return fail(LCX_ERR_INVALID_ARG, "invalid build request %u", cmd->request);
+    if (cmd->aabb_buffer_size % 24 != 0)
+        return fail(LCX_ERR_INVALID_ARG, "AABB buffer size %zu is not a multiple of 24 bytes", cmd->aabb_buffer_size);
+    const uint64_t count = cmd->aabb_buffer_size / 24;
+    if (count >= (1ull << 31)) return fail(LCX_ERR_INVALID_ARG, "too many AABBs (%llu)", (unsigned long long)count);
+    if (count && !cmd->aabb_buffer) return fail(LCX_ERR_INVALID_ARG, "AABB buffer is null");
+    if ((cmd->aabb_buffer + cmd->aabb_buffer_offset) % 4 != 0)
+        return fail(LCX_ERR_INVALID_ARG, "AABB buffer address must be 4-byte aligned");
+    Retired retired;  // released after the mutex below
+    std::lock_guard<std::mutex> lk(m->mtx);
+    std::vector<MeshObj *> ms{m.get()};
+    SegInput g{};
+    g.vbase = reinterpret_cast<const unsigned char *>(cmd->aabb_buffer) + cmd->aabb_buffer_offset;
+    g.vstride = 24;
+    g.tbase = nullptr;
+    g.vcount = uint32_t(count);
+    g.item_offset = 0;
+    g.item_count = uint32_t(count);
+    g.kind = kSegAabbs;
+    g.desc = m->d_desc;
+    std::vector<SegInput> segs{g};
+    std::vector<uint32_t> req{cmd->request};
+    return build_meshes(ms, segs, req, static_cast<cudaStream_t>(stream), retired);
+}
+
 int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *cmd, void *stream) {
     auto m = find_mesh(mesh);
     if (!m) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build: unknown mesh handle %llu", (unsigned long long)mesh);
     if (!cmd) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build: command is null");
     Retired retired;  // released after the mutex below
     std::lock_guard<std::mutex> lk(m->mtx);
-    return build_meshes({m.get()}, cmd, static_cast<cudaStream_t>(stream), retired);
+    std::vector<MeshObj *> ms{m.get()};
+    std::vector<SegInput> segs;
+    std::vector<uint32_t> req;
+    if (int r = mesh_segments(ms, cmd, segs, req)) return r;
+    return build_meshes(ms, segs, req, static_cast<cudaStream_t>(stream), retired);
 }
 
 int lcx_mesh_build_batch(const uint64_t *meshes, const LcxMeshBuildCommand *cmds, uint32_t count, void *stream) {
@@ -605,7 +668,10 @@ int lcx_mesh_build_batch(const uint64_t *meshes, const LcxMeshBuildCommand *cmds
     std::vector<std::unique_lock<std::mutex>> locks;
     locks.reserve(count);
     for (MeshObj *m : sorted) locks.emplace_back(m->mtx);
-    return build_meshes(order, cmds, static_cast<cudaStream_t>(stream), retired);
+    std::vector<SegInput> segs;
+    std::vector<uint32_t> req;
+    if (int r = mesh_segments(order, cmds, segs, req)) return r;
+    return build_meshes(order, segs, req, static_cast<cudaStream_t>(stream), retired);
 }
 
 int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out) {

@@ -20,9 +20,10 @@ struct SegInput {
     uint32_t vcount;
     uint32_t item_offset;        // first item of this segment among all items of the build
     uint32_t item_count;
-    uint32_t _pad;
+    uint32_t kind;               // kSegTriangles (vbase, tbase) or kSegAabbs (vbase: 24-byte AABBs)
     BlasDesc *desc;              // BLAS descriptor the emit fills in (null for a TLAS)
 };
+enum : uint32_t { kSegTriangles = 0, kSegAabbs = 1 };
 static_assert(sizeof(SegInput) == 48, "SegInput is 48 B");
 
 // Per-segment control words.

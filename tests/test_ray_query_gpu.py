@@ -97,3 +97,95 @@ def test_device_view_follows_accel_state(lcx):
     acc.build()
     assert _view(acc).tlas_nodes
     torch.cuda.synchronize()
+
+
+def _sphere_aabbs(n, rng):
+    c = rng.uniform(-1.0, 1.0, (n, 3))
+    r = rng.uniform(0.03, 0.15, n)
+    return np.concatenate([c - r[:, None], c + r[:, None]], 1).astype(np.float32)
+
+
+def _spheres_fp64(rays, aabbs, affines):
+    """Closest sphere hit per ray in FP64: (t, inst, prim), inf / ~0 for a miss."""
+    lo, hi = aabbs[:, :3].astype(np.float64), aabbs[:, 3:].astype(np.float64)
+    cen, rad = 0.5 * (lo + hi), 0.5 * (hi[:, 0] - lo[:, 0])
+    best_t = np.full(rays.shape[0], np.inf)
+    best_i = np.full(rays.shape[0], S.MISS, np.uint32)
+    best_p = np.full(rays.shape[0], S.MISS, np.uint32)
+    o, d = rays["o"].astype(np.float64), rays["d"].astype(np.float64)
+    tmin, tmax = rays["tmin"].astype(np.float64), rays["tmax"].astype(np.float64)
+    for inst, aff in enumerate(affines):
+        a = aff.astype(np.float64).reshape(3, 4)
+        inv = np.linalg.inv(a[:, :3])
+        oo = (o - a[:, 3]) @ inv.T
+        dd = d @ inv.T
+        for s0 in range(0, rays.shape[0], 4096):
+            sl = slice(s0, s0 + 4096)
+            oc = oo[sl, None, :] - cen[None]
+            A = (dd[sl] ** 2).sum(1)[:, None]
+            B = (oc * dd[sl, None, :]).sum(2)
+            C = (oc ** 2).sum(2) - rad[None] ** 2
+            disc = B * B - A * C
+            sq = np.sqrt(np.maximum(disc, 0.0))
+            t0, t1 = (-B - sq) / A, (-B + sq) / A
+            t = np.where(t0 >= tmin[sl, None], t0, t1)
+            ok = (disc >= 0) & (t >= tmin[sl, None]) & (t < tmax[sl, None])
+            t = np.where(ok, t, np.inf)
+            j = t.argmin(1)
+            tj = t[np.arange(t.shape[0]), j]
+            better = tj < best_t[sl]
+            best_t[sl] = np.where(better, tj, best_t[sl])
+            best_i[sl] = np.where(better, inst, best_i[sl])
+            best_p[sl] = np.where(better, j, best_p[sl])
+    return best_t, best_i, best_p
+
+
+def test_procedural_primitives(lcx, oracle_mod, rq):
+    import torch
+    from luisacompute_gb300.accel import Accel, ProceduralPrimitive, hits_to_numpy, mesh_from_data, rays_to_device
+    rng = np.random.default_rng(51)
+    aabbs = _sphere_aabbs(300, rng)
+    prim = ProceduralPrimitive(torch.from_numpy(aabbs).cuda()).build()
+    tri = S.icosphere(3, radius=0.4)
+    mesh = mesh_from_data(tri).build()
+    affines = [S.affine_rows(S.random_rotations(1, rng), np.array([1.5]), np.array([[0.2, -0.1, 0.3]]))[0],
+               np.array([1, 0, 0, 0.5, 0, 1, 0, -0.4, 0, 0, 1, 0.1], np.float32)]
+    acc = Accel()
+    acc.emplace_back(prim, affines[0])
+    acc.emplace_back(prim, affines[1])
+    acc.emplace_back(mesh, S.IDENTITY)
+    acc.build()
+    rays = S.sphere_rays(20_000, [-2.0] * 3, [2.0] * 3, seed=52)
+    d = rays_to_device(rays)
+    n = rays.shape[0]
+    # plain traces do not see procedural instances: the oracle with those slots invisible
+    oscene = S.Scene([tri, S.icosphere(1)], np.array([1, 1, 0]), np.stack(affines + [S.IDENTITY]).astype(np.float32),
+                     np.array([0, 0, 0xFF], np.uint32))
+    osc = oracle_mod.OracleScene(oscene)
+    tri_hits = hits_to_numpy(acc.trace_closest(d))
+    assert np.array_equal(tri_hits.view(np.uint8), osc.trace_closest(rays).view(np.uint8))
+    assert np.array_equal(acc.trace_any(d).cpu().numpy(), osc.trace_any(rays))
+    # ray_query with triangles and spheres: the closer of the two, spheres checked against FP64
+    hits = torch.empty((n, 6), dtype=torch.int32, device="cuda")
+    assert rq.rq_run(ctypes.byref(_view(acc)), d.data_ptr(), n, 3, 1, hits.data_ptr(), None) == 0
+    got = hits_to_numpy(hits)
+    st, si, sp = _spheres_fp64(rays, aabbs, affines)
+    tt = np.where(tri_hits["inst"] != S.MISS, tri_hits["t"].astype(np.float64), np.inf)
+    sphere_first = st < tt
+    with np.errstate(invalid="ignore"):  # inf - inf where both miss
+        clear = ~(np.abs(st - tt) <= 1e-4 * np.minimum(st, tt))  # not a near-tie between the two kinds
+    kind = got["pad"]
+    # FP32 and FP64 may disagree on a grazing ray's discriminant: allow a handful of those
+    assert (kind[clear & sphere_first & np.isfinite(st)] != 2).sum() <= 5
+    assert (kind[clear & ~sphere_first & np.isfinite(tt)] != 1).sum() <= 5
+    assert (kind[~np.isfinite(st) & ~np.isfinite(tt)] != 0).sum() <= 5
+    sel = clear & sphere_first & np.isfinite(st) & (kind == 2)
+    assert sel.sum() > 1000
+    same = (got["inst"][sel] == si[sel]) & (got["prim"][sel] == sp[sel])
+    assert same.mean() > 0.999  # the rest: two spheres at nearly equal distance
+    # the callback's FP32 quadratic loses digits for near-tangent rays (catastrophic cancellation)
+    rel = np.abs(got["t"][sel][same] - st[sel][same]) / np.maximum(st[sel][same], 1e-3)
+    assert np.median(rel) < 1e-6 and rel.max() < 2e-3
+    tri_sel = clear & ~sphere_first & np.isfinite(tt) & (kind == 1)
+    for f in ("inst", "prim", "t"):
+        assert np.array_equal(got[f][tri_sel], tri_hits[f][tri_sel])
