@@ -87,6 +87,16 @@ struct MeshBuildCommand {
     size_t triangle_buffer_size;
 };
 
+// include/luisa/runtime/rhi/command.h:488-512; aabb_buffer: device address of
+// 24-byte {float min[3], max[3]} records.
+struct ProceduralPrimitiveBuildCommand {
+    uint64_t handle;
+    AccelBuildRequest request;
+    uint64_t aabb_buffer;
+    size_t aabb_buffer_offset;
+    size_t aabb_buffer_size;
+};
+
 struct AccelBuildCommand {
     uint64_t handle;
     uint32_t instance_count;
@@ -110,6 +120,17 @@ public:
     }
     void destroy_mesh(uint64_t handle) const { check(lcx_mesh_destroy(handle), "destroy_mesh"); }
 
+    // device_interface.h:174-175: a BLAS over AABBs, instanced like a mesh
+    [[nodiscard]] ResourceCreationInfo create_procedural_primitive(const AccelOption &option) const {
+        const LcxAccelOption o = option.c();
+        ResourceCreationInfo info;
+        check(lcx_procedural_create(&o, &info.handle), "create_procedural_primitive");
+        return info;
+    }
+    void destroy_procedural_primitive(uint64_t handle) const {
+        check(lcx_procedural_destroy(handle), "destroy_procedural_primitive");
+    }
+
     [[nodiscard]] ResourceCreationInfo create_accel(const AccelOption &option) const {
         const LcxAccelOption o = option.c();
         ResourceCreationInfo info;
@@ -131,6 +152,25 @@ public:
         c.triangle_buffer_size = cmd.triangle_buffer_size;
         check(lcx_mesh_build(cmd.handle, &c, stream), "MeshBuildCommand");
     }
+    // A command list's MeshBuildCommands at once: one segmented build, one host sync
+    // (PREFER_UPDATE of meshes built together with allow_update: one refit).
+    void dispatch(const std::vector<MeshBuildCommand> &cmds, void *stream) const {
+        std::vector<uint64_t> handles(cmds.size());
+        std::vector<LcxMeshBuildCommand> cs(cmds.size());
+        for (size_t i = 0; i < cmds.size(); i++) {
+            handles[i] = cmds[i].handle;
+            cs[i] = LcxMeshBuildCommand{static_cast<uint32_t>(cmds[i].request), 0u, cmds[i].vertex_buffer,
+                                        cmds[i].vertex_buffer_offset, cmds[i].vertex_buffer_size,
+                                        cmds[i].vertex_stride, cmds[i].triangle_buffer,
+                                        cmds[i].triangle_buffer_offset, cmds[i].triangle_buffer_size};
+        }
+        check(lcx_mesh_build_batch(handles.data(), cs.data(), uint32_t(cmds.size()), stream), "MeshBuildCommand batch");
+    }
+    void dispatch(const ProceduralPrimitiveBuildCommand &cmd, void *stream) const {
+        const LcxProceduralBuildCommand c{static_cast<uint32_t>(cmd.request), 0u, cmd.aabb_buffer,
+                                          cmd.aabb_buffer_offset, cmd.aabb_buffer_size};
+        check(lcx_procedural_build(cmd.handle, &c, stream), "ProceduralPrimitiveBuildCommand");
+    }
     void dispatch(const AccelBuildCommand &cmd, void *stream) const {
         check(lcx_accel_build(cmd.handle, cmd.instance_count, static_cast<uint32_t>(cmd.request),
                               cmd.modifications.data(), cmd.modifications.size(), cmd.update_instance_buffer_only,
@@ -146,6 +186,21 @@ public:
     void trace_any(uint64_t accel, const Ray *rays, uint32_t n, uint32_t mask, uint8_t *occluded,
                    void *stream) const {
         check(lcx_trace_any(accel, rays, n, mask, occluded, stream), "trace_any");
+    }
+    // Ray batches of many jobs (accels, closest or any) in one launch per kind.
+    void trace_jobs(const std::vector<LcxTraceJob> &jobs, void *stream, uint32_t layout = LCX_NODES_QUANT8) const {
+        check(lcx_trace_jobs(jobs.data(), uint32_t(jobs.size()), layout, stream), "trace_jobs");
+    }
+    // The accel for lcx::ray_query in the backend's own kernels (include/lcx/ray_query.cuh).
+    [[nodiscard]] LcxAccelView device_view(uint64_t accel) const {
+        LcxAccelView v{};
+        check(lcx_accel_device_view(accel, &v), "device_view");
+        return v;
+    }
+    [[nodiscard]] LcxAccelStats mesh_stats(uint64_t mesh) const {
+        LcxAccelStats s{};
+        check(lcx_mesh_stats(mesh, &s), "mesh_stats");
+        return s;
     }
 };
 
@@ -180,6 +235,31 @@ private:
     size_t t_size_;
 };
 
+class ProceduralPrimitive {
+public:
+    // aabbs: device array of `count` 24-byte {float min[3], max[3]} records
+    ProceduralPrimitive(const AccelGpuExt &ext, uint64_t aabbs, size_t count, const AccelOption &option = {})
+        : ext_(&ext), aabbs_(aabbs), size_(count * 24) {
+        handle_ = ext.create_procedural_primitive(option).handle;
+    }
+    ProceduralPrimitive(const ProceduralPrimitive &) = delete;
+    ProceduralPrimitive &operator=(const ProceduralPrimitive &) = delete;
+    ~ProceduralPrimitive() {
+        if (handle_) lcx_procedural_destroy(handle_);
+    }
+    [[nodiscard]] ProceduralPrimitiveBuildCommand build(
+        AccelBuildRequest request = AccelBuildRequest::FORCE_BUILD) const {
+        return ProceduralPrimitiveBuildCommand{handle_, request, aabbs_, 0, size_};
+    }
+    [[nodiscard]] uint64_t handle() const noexcept { return handle_; }
+
+private:
+    const AccelGpuExt *ext_;
+    uint64_t handle_{0};
+    uint64_t aabbs_;
+    size_t size_;
+};
+
 class Accel {
 public:
     explicit Accel(const AccelGpuExt &ext, const AccelOption &option = {}) : ext_(&ext) {
@@ -194,9 +274,17 @@ public:
     // src/runtime/rtx/accel.cpp:88-100; transform is row-major 3x4 (command.h:557-571)
     void emplace_back(const Mesh &mesh, const std::array<float, 12> &affine, uint8_t visibility_mask = 0xffu,
                       bool opaque = true, uint32_t user_id = 0) {
+        emplace_handle(mesh.handle(), affine, visibility_mask, opaque, user_id);
+    }
+    void emplace_back(const ProceduralPrimitive &prim, const std::array<float, 12> &affine,
+                      uint8_t visibility_mask = 0xffu, bool opaque = true, uint32_t user_id = 0) {
+        emplace_handle(prim.handle(), affine, visibility_mask, opaque, user_id);
+    }
+    void emplace_handle(uint64_t primitive, const std::array<float, 12> &affine, uint8_t visibility_mask,
+                        bool opaque, uint32_t user_id) {
         const auto index = static_cast<uint32_t>(count_);
         Modification &m = mod(index);
-        m.primitive = mesh.handle();
+        m.primitive = primitive;
         std::memcpy(m.affine, affine.data(), sizeof(m.affine));
         m.vis_mask = visibility_mask;
         m.user_id = user_id;
@@ -271,6 +359,14 @@ public:
         return *this;
     }
     CommandStream &operator<<(const AccelBuildCommand &c) {
+        ext_->dispatch(c, stream_);
+        return *this;
+    }
+    CommandStream &operator<<(const std::vector<MeshBuildCommand> &c) {
+        ext_->dispatch(c, stream_);
+        return *this;
+    }
+    CommandStream &operator<<(const ProceduralPrimitiveBuildCommand &c) {
         ext_->dispatch(c, stream_);
         return *this;
     }

@@ -4,6 +4,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "lcx/accel_ext.hpp"
@@ -73,6 +74,40 @@ int main() {
                           nullptr);
         cudaMemcpy(hits.data(), dh, sizeof(lcx::TriangleHit) * 4, cudaMemcpyDeviceToHost);
         REQUIRE(hits[0].inst == 1 && hits[0].committed_ray_t == 6.0f);
+        // batched builds and refit: two meshes built together with allow_update, refit together
+        lcx::AccelOption upd;
+        upd.allow_update = true;
+        lcx::Mesh ma{ext, reinterpret_cast<uint64_t>(dv), 4, 16, reinterpret_cast<uint64_t>(dt), 2, upd};
+        lcx::Mesh mb{ext, reinterpret_cast<uint64_t>(dv), 4, 16, reinterpret_cast<uint64_t>(dt), 2, upd};
+        stream << std::vector<lcx::MeshBuildCommand>{ma.build(), mb.build()};
+        REQUIRE(ext.mesh_stats(ma.handle()).refits == 0);
+        stream << std::vector<lcx::MeshBuildCommand>{ma.build(lcx::AccelBuildRequest::PREFER_UPDATE),
+                                                     mb.build(lcx::AccelBuildRequest::PREFER_UPDATE)};
+        REQUIRE(ext.mesh_stats(ma.handle()).refits == 1 && ext.mesh_stats(mb.handle()).refits == 1);
+        // a procedural primitive (one AABB above the quad): instanced, invisible to trace calls
+        const float box[6] = {0.0f, 0.0f, 1.0f, 1.0f, 1.0f, 2.0f};
+        void *dbox = nullptr;
+        REQUIRE(cudaMalloc(&dbox, sizeof(box)) == cudaSuccess);
+        cudaMemcpy(dbox, box, sizeof(box), cudaMemcpyHostToDevice);
+        lcx::ProceduralPrimitive prim{ext, reinterpret_cast<uint64_t>(dbox), 1};
+        lcx::Accel mixed{ext};
+        mixed.emplace_back(ma, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0});
+        mixed.emplace_back(prim, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0});
+        stream << prim.build() << mixed.build();
+        ext.trace_closest(mixed.handle(), static_cast<lcx::Ray *>(dr), 4, 0xffu, static_cast<lcx::TriangleHit *>(dh),
+                          nullptr);
+        cudaMemcpy(hits.data(), dh, sizeof(lcx::TriangleHit) * 4, cudaMemcpyDeviceToHost);
+        REQUIRE(hits[0].inst == 0 && hits[0].committed_ray_t == 5.0f);  // the box at z in [1, 2] is not hit
+        const LcxAccelView view = ext.device_view(mixed.handle());
+        REQUIRE(view.tlas_nodes != nullptr && view.instances != nullptr && view.stack_need <= 32);
+        // the same rays as one job of a multi-job launch
+        std::vector<LcxTraceJob> jobs{
+            LcxTraceJob{mixed.handle(), static_cast<const LcxRay *>(dr), dh, 4u, 0xffu, 0u, 0u}};
+        ext.trace_jobs(jobs, nullptr);
+        std::vector<lcx::TriangleHit> hits2(4);
+        cudaMemcpy(hits2.data(), dh, sizeof(lcx::TriangleHit) * 4, cudaMemcpyDeviceToHost);
+        REQUIRE(std::memcmp(hits2.data(), hits.data(), sizeof(lcx::TriangleHit) * 4) == 0);
+        cudaFree(dbox);
         // errors surface as exceptions with the library's status code
         bool threw = false;
         try {
