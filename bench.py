@@ -229,7 +229,31 @@ def run_batch_build(args):
     build_meshes(upd, request=REQUEST_PREFER_UPDATE)
     refit_s = timed(lambda: build_meshes(upd, request=REQUEST_PREFER_UPDATE), 5)
     refits = int(upd[0].stats().refits)
-    del upd
+    # the same refit without host synchronisation, a TLAS refit over the 100,000 instances, and
+    # both captured once as a CUDA graph and replayed (a rigid or skinned animation frame)
+    from luisacompute_gb300.accel import set_refit_sync
+    set_refit_sync(False)
+    try:
+        refit_async_s = timed(lambda: build_meshes(upd, request=REQUEST_PREFER_UPDATE), 5)
+        uacc = Accel(AccelOption(allow_update=True))
+        uacc.emplace_back_many([upd[i] for i in pick], aff)
+        uacc.build()
+        tlas_rebuild_s = timed(lambda: uacc.build(), 3)
+        uacc.build(request=REQUEST_PREFER_UPDATE)
+        tlas_refit_s = timed(lambda: uacc.build(request=REQUEST_PREFER_UPDATE), 5)
+        tlas_refits = int(uacc.stats().refits)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            build_meshes(upd, request=REQUEST_PREFER_UPDATE)
+            uacc.build(request=REQUEST_PREFER_UPDATE)
+        graph.replay()
+        graph_s = timed(graph.replay, 5)
+        from luisacompute_gb300 import _capi
+        _capi.check(_capi.load().lcx_check_trace_errors(), "refit errors")
+    finally:
+        set_refit_sync(True)
+    del graph, uacc, upd
     # kernels of ours per batched build: tri_prep, morton, lbvh, binary_sah, collapse_init, collapse, emit
     # (the timed loop; the refit figures in "extra" come after it)
     line = {"metric": "Mtris/s batched BLAS build (4096 meshes)", "value": total / batch_s / 1e6, "unit": "Mtris/s",
@@ -246,8 +270,15 @@ def run_batch_build(args):
                       "mean_wide_sah": float(np.mean(wide)),
                       "refit": {"build_ms": upd_build_s * 1e3, "refit_ms": refit_s * 1e3,
                                 "refit_mtris_s": total / refit_s / 1e6, "refits_counted": refits,
+                                "refit_async_ms": refit_async_s * 1e3,
+                                "tlas_rebuild_ms": tlas_rebuild_s * 1e3, "tlas_refit_ms": tlas_refit_s * 1e3,
+                                "tlas_refits_counted": tlas_refits,
+                                "graph_frame_ms": graph_s * 1e3,
                                 "what": "the same 4096 meshes created with allow_update: one batched build vs "
-                                        "one batched PREFER_UPDATE (refit in place, topology kept)"},
+                                        "one batched PREFER_UPDATE (refit in place, topology kept; refit_ms "
+                                        "synchronises once for errors, refit_async_ms does not); a TLAS over "
+                                        "the 100,000 instances rebuilt vs refit; graph_frame_ms = BLAS refit of "
+                                        "all 4096 meshes + TLAS refit captured as one CUDA graph, per replay"},
                       "tlas_instances": args.instances, "tlas_build_ms": tlas_s * 1e3,
                       "tlas_first_build_ms": tlas_first_s * 1e3,
                       "tlas": {"nodes": int(st.node_count), "depth": int(st.depth), "sah": st.sah_cost,

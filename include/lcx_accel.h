@@ -87,7 +87,7 @@ enum { LCX_HINT_FAST_TRACE = 0, LCX_HINT_FAST_BUILD = 1 };
 typedef struct LcxAccelOption {
     uint32_t hint;            /* LCX_HINT_FAST_TRACE | LCX_HINT_FAST_BUILD */
     uint8_t allow_compaction; /* accepted for ABI parity; BVHs are always exact-size */
-    uint8_t allow_update;     /* meshes: keep what a refit needs (see lcx_mesh_build) */
+    uint8_t allow_update;     /* keep what a refit needs (see lcx_mesh_build, lcx_accel_build) */
     uint8_t _pad[2];
 } LcxAccelOption;
 
@@ -148,7 +148,7 @@ typedef struct LcxAccelStats {
     double sah_cost;         /* SAH cost of the binary tree (C_node=1, C_tri=1,
                                 normalised by the root surface area) */
     double wide_sah_cost;    /* same for the 8-wide tree (as built; a refit keeps it) */
-    uint64_t refits;         /* BLAS: refits since the last full build */
+    uint64_t refits;         /* refits since the last full build (SAH figures: that build's) */
 } LcxAccelStats;
 
 /* ------------------------------------------------------------ device setup */
@@ -237,7 +237,12 @@ LCX_API int lcx_accel_destroy(uint64_t accel);
  * transform, mask (default 0xff), opacity and user id until modified.
  * instance_count == 0 is an error, as in src/runtime/rtx/accel.cpp:72-73.
  * update_instance_buffer_only != 0 stores the modifications without
- * rebuilding the TLAS. */
+ * rebuilding the TLAS.  PREFER_UPDATE on an accel created with allow_update,
+ * built before with the same instance_count: the TLAS is refit in place (same
+ * topology; new instance boxes, transforms, masks and BLAS references from
+ * the current meshes, rebuilt or refit) with kernels only -- no host
+ * synchronisation, no allocation, so it can be captured in a CUDA graph.
+ * Otherwise the TLAS is rebuilt (the OptiX update of cuda_accel.cpp). */
 LCX_API int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request,
                     const LcxModification *mods, size_t mod_count,
                     int update_instance_buffer_only, void *stream);
@@ -250,8 +255,8 @@ LCX_API int lcx_accel_stats(uint64_t accel, LcxAccelStats *out);
  * (include/lcx/ray_query.cuh: RayQuery with per-candidate callbacks,
  * include/luisa/dsl/rtx/ray_query.h:17-240).  The reference hands the accel
  * to kernels through its DSL binding; this is that handle as plain pointers.
- * Valid until the accel is built again or destroyed, or a mesh it instances
- * is rebuilt or refit.  Fails like a trace call on an accel that is not
+ * Valid until the accel is rebuilt (a refit keeps it valid) or destroyed, or
+ * a mesh it instances is rebuilt or refit without the accel being built again.  Fails like a trace call on an accel that is not
  * ready (LCX_ERR_NOT_BUILT, LCX_ERR_DEPTH). */
 typedef struct LcxAccelView {
     const void *tlas_nodes;  /* the TLAS's 8-bit quantised nodes (device) */
@@ -372,9 +377,21 @@ LCX_API int lcx_pt_render(uint64_t accel, const LcxPtMesh *meshes, uint32_t mesh
 /* Synchronises the current device and reports whether any trace call since
  * the last check hit a kernel-side bound: LCX_ERR_TIMEOUT when a ray exceeded
  * the per-ray step bound (only a corrupt BVH can cause it), LCX_ERR_DEPTH when
- * a push found the stack full.  Clears the flags.  (No counterpart in the
- * reference, whose kernels cannot report errors.) */
+ * a push found the stack full.  Also reports refits run without host
+ * synchronisation (lcx_set_refit_sync(0)) that met a triangle index out of
+ * range or unquantisable coordinates (LCX_ERR_INVALID_ARG).  Clears the flags.
+ * (No counterpart in the reference, whose kernels cannot report errors.) */
 LCX_API int lcx_check_trace_errors(void);
+
+/* Refit mode for later PREFER_UPDATE mesh builds (lcx_mesh_build and
+ * lcx_mesh_build_batch on meshes created with allow_update): 1 (default)
+ * synchronises the host once to report bad indices from the call itself; 0
+ * only enqueues kernels (no host synchronisation, no allocation, so a refit
+ * can be captured in a CUDA graph) and leaves errors for
+ * lcx_check_trace_errors.  TLAS refits (lcx_accel_build with PREFER_UPDATE on
+ * an accel created with allow_update, same instance count, meshes built)
+ * never synchronise.  No counterpart in the reference. */
+LCX_API int lcx_set_refit_sync(uint32_t sync);
 
 /* Build knobs, process-wide, for builds that start after the call (no
  * counterpart in the reference).  leaf_max: triangles per leaf slot, 1..3, or

@@ -95,6 +95,7 @@ _SIGS = {
     "lcx_get_build_morton": (c_int, [POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
     "lcx_set_trace_reorder": (c_int, [c_uint32, c_uint32]),
     "lcx_set_trace_stack": (c_int, [c_uint32]),
+    "lcx_set_refit_sync": (c_int, [c_uint32]),
     "lcx_get_trace_stack": (c_int, [POINTER(c_uint32)]),
     "lcx_get_trace_reorder": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),
     "lcx_accel_create": (c_int, [POINTER(LcxAccelOption), POINTER(c_uint64)]),

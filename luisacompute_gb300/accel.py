@@ -308,6 +308,13 @@ def build_meshes(meshes, request: int = REQUEST_FORCE_BUILD, stream=None):
     return meshes
 
 
+def set_refit_sync(sync: bool):
+    """Refit mode of later PREFER_UPDATE mesh builds: True synchronises once to report bad
+    indices from the call; False only enqueues kernels (capturable in a CUDA graph) and leaves
+    errors for ``lcx_check_trace_errors``."""
+    check(_capi.load().lcx_set_refit_sync(1 if sync else 0), "lcx_set_refit_sync")
+
+
 def hits_to_numpy(hits) -> np.ndarray:
     """(N, 6) int32 device tensor -> numpy TriangleHit records."""
     from .scenes import HIT_DTYPE

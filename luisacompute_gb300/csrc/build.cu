@@ -723,28 +723,31 @@ __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *d
     }
 }
 
+// TLAS leaf record of instance `id` (its inverse transform from k_inst_prep).
+__device__ __forceinline__ InstRec make_inst_rec(uint32_t id, const InstState *inst, const float *w2o) {
+    InstRec r;
+#pragma unroll
+    for (int k = 0; k < 12; k++) r.w2o[k] = w2o[12ull * id + k];
+    const InstState &s = inst[id];
+    const BlasDesc *d = s.blas;
+    const bool ok = d != nullptr && (d->valid & 1u);
+    r.qnodes = ok ? d->qnodes : nullptr;
+    r.tris = ok ? d->tris : nullptr;
+    r.fnodes = ok ? d->fnodes : nullptr;
+    r.inst_id = id;
+    r.mask = !ok ? 0u : (d->valid & 2u) ? (((s.mask & 0xffu) << 8) | kInstProcedural) : (s.mask & 0xffu);
+    return r;
+}
+
 __global__ void k_emit_tlas(TreeView tv, const SegInput *segs, const uint32_t *desc, uint32_t wide_count,
                             int leaf_max, const InstState *inst, const float *w2o, Node8Q *qn, Node8F *fn,
-                            InstRec *recs, uint32_t *ctl, double *sah) {
+                            InstRec *recs, uint32_t *ctl, double *sah, unsigned long long *rtab) {
     const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= wide_count) return;
     float4 rl, rh;
     emit_node(
-        tv, segs, desc, w, qn, fn, leaf_max, ctl, sah, nullptr,
-        [&](uint32_t pos, uint32_t id, uint32_t) {
-            InstRec r;
-#pragma unroll
-            for (int k = 0; k < 12; k++) r.w2o[k] = w2o[12ull * id + k];
-            const InstState &s = inst[id];
-            const BlasDesc *d = s.blas;
-            const bool ok = d != nullptr && (d->valid & 1u);
-            r.qnodes = ok ? d->qnodes : nullptr;
-            r.tris = ok ? d->tris : nullptr;
-            r.fnodes = ok ? d->fnodes : nullptr;
-            r.inst_id = id;
-            r.mask = !ok ? 0u : (d->valid & 2u) ? (((s.mask & 0xffu) << 8) | kInstProcedural) : (s.mask & 0xffu);
-            recs[pos] = r;
-        },
+        tv, segs, desc, w, qn, fn, leaf_max, ctl, sah, rtab,
+        [&](uint32_t pos, uint32_t id, uint32_t) { recs[pos] = make_inst_rec(id, inst, w2o); },
         rl, rh);
 }
 
@@ -882,9 +885,10 @@ cudaError_t emit_blas(const BuildScratch &s, const BuildParams &bp, uint32_t wid
 }
 
 cudaError_t emit_tlas(const InstState *inst, const BuildScratch &s, const BuildParams &bp, uint32_t wide_count,
-                      Node8Q *qn, Node8F *fn, InstRec *recs, double *wide_sah, cudaStream_t st) {
+                      Node8Q *qn, Node8F *fn, InstRec *recs, double *wide_sah, unsigned long long *rtab,
+                      cudaStream_t st) {
     k_emit_tlas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.segs, s.desc, wide_count, bp.leaf_max,
-                                                              inst, s.w2o, qn, fn, recs, s.ctl, wide_sah);
+                                                              inst, s.w2o, qn, fn, recs, s.ctl, wide_sah, rtab);
     return cudaGetLastError();
 }
 
@@ -918,28 +922,49 @@ __device__ __forceinline__ bool box3_empty(const float l[3], const float h[3]) {
     return !(l[0] <= h[0] && l[1] <= h[1] && l[2] <= h[2]);
 }
 
-// Bottom-up refit over the wide nodes of one BLAS block: a thread starts at a
-// node without internal children, rewrites the triangle records of its leaf
-// slots from the current buffers (by the prim id each record keeps) and their
-// boxes, takes its node box as the union of its slots, writes it into the
-// parent's slot and goes on with the parent if it is the last of the parent's
-// internal children to arrive (the parent's counter).  Boxes written by other
-// threads are read with ld.cg after the counter says they are complete.
-__global__ void k_refit(const SegInput *segs, uint32_t nseg, uint32_t W, const unsigned long long *rtab,
-                        const Node8Q *qn, Node8F *fn, TriRec *tris, uint32_t *counters, uint32_t *ctl) {
+// Bottom-up refit over the wide nodes of one BVH block (a BLAS block or a
+// TLAS): a thread starts at a node without internal children, rewrites the
+// leaf records of its leaf slots (triangles or AABBs from the segment's
+// current buffers, by the prim id each record keeps; TLAS: the instance
+// records, from the instance states) and their boxes, takes its node box as
+// the union of its slots, writes it into the parent's slot and goes on with
+// the parent if it is the last of the parent's internal children to arrive
+// (the parent's counter).  Boxes written by other threads are read with ld.cg
+// after the counter says they are complete.
+struct RefitArgs {
+    uint32_t W;
+    const unsigned long long *rtab;
+    const Node8Q *qn;
+    Node8F *fn;
+    uint32_t *counters, *ctl;
+    // BLAS blocks
+    const SegInput *segs;
+    uint32_t nseg;
+    TriRec *tris;
+    // TLAS
+    const InstState *inst;
+    const float4 *ilo, *ihi;  // instance world boxes (k_inst_prep)
+    const float *w2o;
+    InstRec *recs;
+    uint32_t ninst;
+};
+
+template <bool kTlas>
+__global__ void k_refit(RefitArgs A) {
     uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= W) return;
-    if ((__ldg(&qn[w].exps) >> 24) != 0u) return;
+    if (w >= A.W) return;
+    if ((__ldg(&A.qn[w].exps) >> 24) != 0u) return;
     for (int level = 0; level <= kMaxLevels; level++) {
-        const unsigned long long te = __ldg(&rtab[w]);
+        const unsigned long long te = __ldg(&A.rtab[w]);
         const uint32_t hiw = uint32_t(te >> 32), parent1 = uint32_t(te);
         const uint32_t seg = hiw >> 3, pslot = hiw & 7u;
-        if (seg >= nseg) {  // cannot happen for a table the build wrote
-            atomicOr(&ctl[kCtlErr], kErrBadIndex);
+        if (seg >= (kTlas ? 1u : A.nseg)) {  // cannot happen for a table the build wrote
+            atomicOr(&A.ctl[kCtlErr], kErrBadIndex);
             return;
         }
-        const SegInput g = segs[seg];
-        Node8F &f = fn[w];
+        SegInput g{};
+        if (!kTlas) g = A.segs[seg];
+        Node8F &f = A.fn[w];
         const uint32_t meta_lo = __ldcg(&f.meta_lo), meta_hi = __ldcg(&f.meta_hi), ib = __ldcg(&f.item_base);
         float nl[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, nh[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
         for (int s = 0; s < 8; s++) {
@@ -958,41 +983,62 @@ __global__ void k_refit(const SegInput *segs, uint32_t nseg, uint32_t W, const u
                 ch[0] = ch[1] = ch[2] = -FLT_MAX;
                 const uint32_t cnt = meta_count(meta), off = meta & 31u;
                 for (uint32_t j = 0; j < cnt; j++) {
-                    if (ib + off + j >= g.item_count) {  // cannot happen for a node the build wrote
-                        atomicOr(&ctl[kCtlErr], kErrBadIndex);
-                        continue;
-                    }
-                    TriRec *r = tris + (size_t(g.item_offset) + ib + off + j);
-                    const uint32_t prim = __float_as_uint(r->v0.w);
-                    if (prim >= g.item_count) {  // cannot happen for a record the build wrote
-                        atomicOr(&ctl[kCtlErr], kErrBadIndex);
-                        continue;
-                    }
-                    if (g.kind == kSegAabbs) {
-                        const float *bx = reinterpret_cast<const float *>(g.vbase + 24ull * prim);
-                        const float il[3] = {bx[0], bx[1], bx[2]}, ih[3] = {bx[3], bx[4], bx[5]};
-                        if (!box3_empty(il, ih)) {
-#pragma unroll
-                            for (int k = 0; k < 3; k++) {
-                                cl[k] = fminf(cl[k], il[k]);
-                                ch[k] = fmaxf(ch[k], ih[k]);
-                            }
-                        }
-                        *r = TriRec{make_float4(il[0], il[1], il[2], __uint_as_float(prim)),
-                                    make_float4(ih[0], ih[1], ih[2], 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
-                        continue;
-                    }
-                    const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * prim);
-                    const uint32_t i0 = t[0], i1 = t[1], i2 = t[2];
-                    if (i0 >= g.vcount || i1 >= g.vcount || i2 >= g.vcount) {
-                        atomicOr(&ctl[kCtlErr], kErrBadIndex);
-                        continue;
-                    }
-                    float4 a = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i0));
-                    float4 b = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i1));
-                    float4 c = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i2));
                     float il[3], ih[3];
-                    item_box(a, b, c, il, ih);
+                    if (kTlas) {
+                        const uint32_t pos = ib + off + j;
+                        if (pos >= A.ninst) {  // cannot happen for a node the build wrote
+                            atomicOr(&A.ctl[kCtlErr], kErrBadIndex);
+                            continue;
+                        }
+                        const uint32_t id = A.recs[pos].inst_id;
+                        if (id >= A.ninst) {
+                            atomicOr(&A.ctl[kCtlErr], kErrBadIndex);
+                            continue;
+                        }
+                        const float4 l = A.ilo[id], h = A.ihi[id];
+                        il[0] = l.x;
+                        il[1] = l.y;
+                        il[2] = l.z;
+                        ih[0] = h.x;
+                        ih[1] = h.y;
+                        ih[2] = h.z;
+                        A.recs[pos] = make_inst_rec(id, A.inst, A.w2o);
+                    } else {
+                        if (ib + off + j >= g.item_count) {  // cannot happen for a node the build wrote
+                            atomicOr(&A.ctl[kCtlErr], kErrBadIndex);
+                            continue;
+                        }
+                        TriRec *r = A.tris + (size_t(g.item_offset) + ib + off + j);
+                        const uint32_t prim = __float_as_uint(r->v0.w);
+                        if (prim >= g.item_count) {  // cannot happen for a record the build wrote
+                            atomicOr(&A.ctl[kCtlErr], kErrBadIndex);
+                            continue;
+                        }
+                        if (g.kind == kSegAabbs) {
+                            const float *bx = reinterpret_cast<const float *>(g.vbase + 24ull * prim);
+                            for (int k = 0; k < 3; k++) {
+                                il[k] = bx[k];
+                                ih[k] = bx[3 + k];
+                            }
+                            *r = TriRec{make_float4(il[0], il[1], il[2], __uint_as_float(prim)),
+                                        make_float4(ih[0], ih[1], ih[2], 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
+                        } else {
+                            const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * prim);
+                            const uint32_t i0 = t[0], i1 = t[1], i2 = t[2];
+                            if (i0 >= g.vcount || i1 >= g.vcount || i2 >= g.vcount) {
+                                atomicOr(&A.ctl[kCtlErr], kErrBadIndex);
+                                continue;
+                            }
+                            float4 a = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i0));
+                            float4 b = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i1));
+                            float4 c = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i2));
+                            item_box(a, b, c, il, ih);
+                            a.w = __uint_as_float(prim);
+                            b.w = 0.0f;
+                            c.w = 0.0f;
+                            *r = TriRec{a, b, c};
+                        }
+                    }
                     if (!box3_empty(il, ih)) {
 #pragma unroll
                         for (int k = 0; k < 3; k++) {
@@ -1000,10 +1046,6 @@ __global__ void k_refit(const SegInput *segs, uint32_t nseg, uint32_t W, const u
                             ch[k] = fmaxf(ch[k], ih[k]);
                         }
                     }
-                    a.w = __uint_as_float(prim);
-                    b.w = 0.0f;
-                    c.w = 0.0f;
-                    *r = TriRec{a, b, c};
                 }
                 f.lo_x[s] = cl[0];
                 f.lo_y[s] = cl[1];
@@ -1018,8 +1060,8 @@ __global__ void k_refit(const SegInput *segs, uint32_t nseg, uint32_t W, const u
                 nh[k] = fmaxf(nh[k], ch[k]);
             }
         }
-        if (parent1 == 0u) {  // a segment root: its box for the TLAS builds
-            BlasDesc *bd = g.desc;
+        if (parent1 == 0u) {  // a root: a BLAS root's box for the TLAS builds
+            BlasDesc *bd = kTlas ? nullptr : g.desc;
             if (bd != nullptr) {
                 const bool empty = box3_empty(nl, nh);
                 for (int k = 0; k < 3; k++) {
@@ -1031,11 +1073,11 @@ __global__ void k_refit(const SegInput *segs, uint32_t nseg, uint32_t W, const u
             return;
         }
         const uint32_t parent = parent1 - 1u;
-        if (parent >= W || pslot > 7u) {  // cannot happen for a table the build wrote
-            atomicOr(&ctl[kCtlErr], kErrBadIndex);
+        if (parent >= A.W || pslot > 7u) {  // cannot happen for a table the build wrote
+            atomicOr(&A.ctl[kCtlErr], kErrBadIndex);
             return;
         }
-        Node8F &pf = fn[parent];
+        Node8F &pf = A.fn[parent];
         pf.lo_x[pslot] = nl[0];
         pf.lo_y[pslot] = nl[1];
         pf.lo_z[pslot] = nl[2];
@@ -1043,12 +1085,12 @@ __global__ void k_refit(const SegInput *segs, uint32_t nseg, uint32_t W, const u
         pf.hi_y[pslot] = nh[1];
         pf.hi_z[pslot] = nh[2];
         __threadfence();
-        const uint32_t need = __popc(__ldg(&qn[parent].exps) >> 24);
-        if (atomicAdd(&counters[parent], 1u) + 1u != need) return;
+        const uint32_t need = __popc(__ldg(&A.qn[parent].exps) >> 24);
+        if (atomicAdd(&A.counters[parent], 1u) + 1u != need) return;
         __threadfence();
         w = parent;
     }
-    atomicOr(&ctl[kCtlErr], kErrTooDeep);
+    atomicOr(&A.ctl[kCtlErr], kErrTooDeep);
 }
 
 // Re-encodes the quantised node from the refit FP32 node: node box = union of
@@ -1103,7 +1145,43 @@ cudaError_t refit_blas(const SegInput *segs, uint32_t nseg, uint32_t W, const un
     if (W == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(uint32_t) * W, st);
     if (e != cudaSuccess) return e;
-    k_refit<<<blocks_for(W, 128), 128, 0, st>>>(segs, nseg, W, rtab, qn, fn, tris, counters, ctl);
+    RefitArgs A{};
+    A.W = W;
+    A.rtab = rtab;
+    A.qn = qn;
+    A.fn = fn;
+    A.counters = counters;
+    A.ctl = ctl;
+    A.segs = segs;
+    A.nseg = nseg;
+    A.tris = tris;
+    k_refit<false><<<blocks_for(W, 128), 128, 0, st>>>(A);
+    k_requantize<<<blocks_for(W, 128), 128, 0, st>>>(W, qn, fn, ctl);
+    return cudaGetLastError();
+}
+
+cudaError_t refit_tlas(const InstState *inst, uint32_t n, float4 *ilo, float4 *ihi, float *w2o, uint32_t *segctl,
+                       uint32_t W, const unsigned long long *rtab, Node8Q *qn, Node8F *fn, InstRec *recs,
+                       uint32_t *counters, uint32_t *ctl, cudaStream_t st) {
+    if (W == 0 || n == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(uint32_t) * W, st);
+    if (e != cudaSuccess) return e;
+    // instance world boxes and inverses, as a build computes them (segctl: scratch)
+    k_inst_prep<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(inst, n, ilo, ihi, w2o, segctl);
+    RefitArgs A{};
+    A.W = W;
+    A.rtab = rtab;
+    A.qn = qn;
+    A.fn = fn;
+    A.counters = counters;
+    A.ctl = ctl;
+    A.inst = inst;
+    A.ilo = ilo;
+    A.ihi = ihi;
+    A.w2o = w2o;
+    A.recs = recs;
+    A.ninst = n;
+    k_refit<true><<<blocks_for(W, 128), 128, 0, st>>>(A);
     k_requantize<<<blocks_for(W, 128), 128, 0, st>>>(W, qn, fn, ctl);
     return cudaGetLastError();
 }

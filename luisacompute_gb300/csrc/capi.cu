@@ -47,13 +47,18 @@ int cuda_fail(cudaError_t e, const char *what) {
     } while (0)
 
 constexpr uint32_t kPoolSlots = 4096;  // trace-call counters (16 B each)
+// the last kGraphSlots slots go to calls captured into CUDA graphs, whose slot is
+// fixed at capture, so a replay never shares a counter with a live call
+constexpr uint32_t kGraphSlots = 512;
 // warps overshoot the ray counter by at most 32 each, so 2^31 keeps it from wrapping
 constexpr uint32_t kMaxTraceRays = 1u << 31;
 
 struct DeviceState {
     int device = -1;
     uint32_t *pool = nullptr;  // kPoolSlots x 4 words
+    uint32_t *refit_ctl = nullptr;  // kCtlWords words: errors of refits that do not synchronise
     std::atomic<uint32_t> next_slot{0};
+    std::atomic<uint32_t> next_graph_slot{0};
 };
 
 std::mutex g_dev_mtx;
@@ -68,6 +73,8 @@ int current_device_state(DeviceState **out) {
     if (s.pool == nullptr) {
         LCX_CUDA(cudaMalloc(&s.pool, kPoolSlots * 4 * sizeof(uint32_t)), "cudaMalloc(trace pool)");
         LCX_CUDA(cudaMemset(s.pool, 0, kPoolSlots * 4 * sizeof(uint32_t)), "cudaMemset(trace pool)");
+        LCX_CUDA(cudaMalloc(&s.refit_ctl, kCtlWords * sizeof(uint32_t)), "cudaMalloc(refit errors)");
+        LCX_CUDA(cudaMemset(s.refit_ctl, 0, kCtlWords * sizeof(uint32_t)), "cudaMemset(refit errors)");
         s.device = dev;
     }
     *out = &s;
@@ -79,12 +86,19 @@ int current_device_state(DeviceState **out) {
 struct DevBlock {
     void *ptr = nullptr;
     size_t bytes = 0;
-    // BLAS blocks built with allow_update: the layout and the parent table a refit needs
+    // blocks built with allow_update: the layout, the parent table and the
+    // scratch a refit needs (all in this allocation, so a refit allocates nothing)
     unsigned long long *rtab = nullptr;
     uint32_t wide = 0, nseg = 0;
     Node8Q *qn = nullptr;
     Node8F *fn = nullptr;
-    TriRec *tris = nullptr;
+    TriRec *tris = nullptr;           // BLAS
+    uint32_t *counters = nullptr;     // wide words
+    SegInput *d_segs = nullptr;       // BLAS: the segment table of the last build or refit
+    std::vector<SegInput> h_segs;     // its host copy
+    float4 *ilo = nullptr, *ihi = nullptr;  // TLAS: instance boxes
+    float *w2o = nullptr;             // TLAS: instance inverses
+    uint32_t *segctl = nullptr;       // TLAS: kSegWords words
     ~DevBlock() {
         if (ptr) cudaFree(ptr);  // cudaFree waits for work still using it
     }
@@ -132,6 +146,8 @@ struct AccelObj {
     InstState *d_inst = nullptr;
     uint32_t inst_cap = 0, inst_count = 0;
     std::vector<uint64_t> inst_mesh;  // mesh handle per instance (0 = none)
+    std::vector<uint64_t> uniq_mesh;  // the distinct nonzero handles of inst_mesh
+    bool uniq_dirty = true;           // inst_mesh changed since uniq_mesh was made
     std::shared_ptr<DevBlock> block;
     double *wide_sah = nullptr;
     Node8Q *qn = nullptr;
@@ -139,8 +155,11 @@ struct AccelObj {
     InstRec *recs = nullptr;
     uint32_t node_count = 0, depth = 0, max_blas_depth = 0, built_instances = 0;
     bool built = false;
+    bool pending_rebuild = false;  // an instance's primitive changed since the last full build
+    uint64_t refits = 0;           // TLAS refits since the last full build
     double sah = 0.0;
     std::vector<std::pair<uint64_t, uint64_t>> mesh_gens;  // (mesh handle, generation) at TLAS build
+    uint64_t checked_epoch = 0;  // g_mesh_epoch when mesh_gens was last found current
     std::mutex mtx;
 };
 
@@ -158,6 +177,29 @@ std::shared_ptr<AccelObj> find_accel(uint64_t h) {
     std::lock_guard<std::mutex> lk(g_reg_mtx);
     auto it = g_accels.find(h);
     return it == g_accels.end() ? nullptr : it->second;
+}
+
+// Bumped (after the change) by every mesh build, refit and destroy, so a trace
+// over an accel whose meshes did not change skips the per-mesh lookups.
+std::atomic<uint64_t> g_mesh_epoch{1};
+void bump_mesh_epoch() { g_mesh_epoch.fetch_add(1, std::memory_order_acq_rel); }
+
+// Whether every mesh the accel's TLAS references still exists with the
+// generation it was built against; else the first stale handle and whether it
+// was destroyed.  The caller holds a->mtx.
+bool meshes_current(AccelObj *a, uint64_t *stale = nullptr, bool *destroyed = nullptr) {
+    const uint64_t epoch = g_mesh_epoch.load(std::memory_order_acquire);
+    if (a->checked_epoch == epoch) return true;
+    for (const auto &mg : a->mesh_gens) {
+        auto m = find_mesh(mg.first);
+        if (!m || m->generation != mg.second) {
+            if (stale) *stale = mg.first;
+            if (destroyed) *destroyed = !m;
+            return false;
+        }
+    }
+    a->checked_epoch = epoch;
+    return true;
 }
 
 // Build scratch from the stream-ordered allocator, freed on the same stream.
@@ -296,7 +338,19 @@ int validate_mesh_command(const LcxMeshBuildCommand *cmd, uint64_t &tri64, uint6
 // segmented pipeline: one sort, one LBVH pass, one cooperative collapse and
 // one emit for all of them, into one shared device block.  Synchronises the
 // host once to size the block.
+// Whether `st` is being captured into a CUDA graph: host-to-device copies from
+// pageable memory cannot be captured, so the calls that would make one fail.
+bool capturing(cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return cs == cudaStreamCaptureStatusActive;
+}
+
 constexpr int kNoRefit = 1;  // try_refit: the call is not a refit; build instead
+bool g_refit_sync = true;    // lcx_set_refit_sync
 
 // PREFER_UPDATE on meshes created with allow_update: when the call covers every
 // mesh of one BVH block (as built together) and no triangle count changed,
@@ -324,27 +378,45 @@ int try_refit(const std::vector<MeshObj *> &meshes, const std::vector<uint32_t> 
         ordered[k].item_offset = off;
         off += ordered[k].item_count;
     }
-    ScratchHolder hold(st);
-    SegInput *d_segs = nullptr;
-    uint32_t *counters = nullptr, *ctl = nullptr;
-    LCX_CUDA(hold.alloc((void **)&d_segs, sizeof(SegInput) * count), "refit scratch");
-    LCX_CUDA(hold.alloc((void **)&counters, sizeof(uint32_t) * std::max<uint32_t>(blk->wide, 1)), "refit scratch");
-    LCX_CUDA(hold.alloc((void **)&ctl, sizeof(uint32_t) * kCtlWords), "refit scratch");
-    LCX_CUDA(cudaMemcpyAsync(d_segs, ordered.data(), sizeof(SegInput) * count, cudaMemcpyHostToDevice, st),
-             "refit segment upload");
-    LCX_CUDA(cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * kCtlWords, st), "refit scratch init");
-    LCX_CUDA(refit_blas(d_segs, uint32_t(count), blk->wide, blk->rtab, blk->qn, blk->fn, blk->tris, counters, ctl, st),
-             "BLAS refit");
-    uint32_t err = 0;
-    LCX_CUDA(cudaMemcpyAsync(&err, ctl + kCtlErr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "refit readback");
-    LCX_CUDA(cudaStreamSynchronize(st), "refit sync");
-    if (err & kErrBadIndex) return fail(LCX_ERR_INVALID_ARG, "refit: triangle index out of range");
-    if (err & kErrTooDeep) return fail(LCX_ERR_DEPTH, "refit: BVH deeper than %d levels", kMaxLevels);
-    if (err & kErrQuant) return fail(LCX_ERR_INVALID_ARG, "refit: vertex coordinates too large to quantise");
+    // the segment table stays on the device: buffers that did not move need no upload,
+    // so such a refit only enqueues a memset and three kernels (capturable in a CUDA graph)
+    if (blk->h_segs.size() != count || std::memcmp(blk->h_segs.data(), ordered.data(), sizeof(SegInput) * count)) {
+        if (capturing(st))
+            return fail(LCX_ERR_INVALID_ARG,
+                        "refit in a CUDA graph capture: the mesh buffers moved since the last refit; refit once "
+                        "outside the capture first");
+        LCX_CUDA(cudaMemcpyAsync(blk->d_segs, ordered.data(), sizeof(SegInput) * count, cudaMemcpyHostToDevice, st),
+                 "refit segment upload");
+        blk->h_segs = ordered;
+    }
+    DeviceState *ds = nullptr;
+    if (int r = current_device_state(&ds)) return r;
+    if (!g_refit_sync) {  // errors go to the device's refit error word (lcx_check_trace_errors)
+        LCX_CUDA(refit_blas(blk->d_segs, uint32_t(count), blk->wide, blk->rtab, blk->qn, blk->fn, blk->tris,
+                            blk->counters, ds->refit_ctl, st),
+                 "BLAS refit");
+    } else {
+        if (capturing(st))
+            return fail(LCX_ERR_INVALID_ARG, "refit in a CUDA graph capture needs lcx_set_refit_sync(0)");
+        ScratchHolder hold(st);
+        uint32_t *ctl = nullptr;
+        LCX_CUDA(hold.alloc((void **)&ctl, sizeof(uint32_t) * kCtlWords), "refit scratch");
+        LCX_CUDA(cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * kCtlWords, st), "refit scratch init");
+        LCX_CUDA(refit_blas(blk->d_segs, uint32_t(count), blk->wide, blk->rtab, blk->qn, blk->fn, blk->tris,
+                            blk->counters, ctl, st),
+                 "BLAS refit");
+        uint32_t err = 0;
+        LCX_CUDA(cudaMemcpyAsync(&err, ctl + kCtlErr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "refit readback");
+        LCX_CUDA(cudaStreamSynchronize(st), "refit sync");
+        if (err & kErrBadIndex) return fail(LCX_ERR_INVALID_ARG, "refit: triangle index out of range");
+        if (err & kErrTooDeep) return fail(LCX_ERR_DEPTH, "refit: BVH deeper than %d levels", kMaxLevels);
+        if (err & kErrQuant) return fail(LCX_ERR_INVALID_ARG, "refit: vertex coordinates too large to quantise");
+    }
     for (MeshObj *m : meshes) {
         m->generation++;  // accels over these meshes must be built again
         m->refits++;
     }
+    bump_mesh_epoch();
     return LCX_OK;
 }
 
@@ -387,6 +459,10 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
         const int r = try_refit(meshes, requests, segs, st);
         if (r != kNoRefit) return r;
     }
+    if (capturing(st))  // a build sizes its block on the host
+        return fail(LCX_ERR_INVALID_ARG,
+                    "mesh build in a CUDA graph capture: only refits (PREFER_UPDATE, allow_update, every mesh of the "
+                    "block, same triangle counts, asynchronous refit mode) can be captured");
     const BuildParams bp = build_params_for(meshes[0]->opt);
     if (total == 0) {
         LCX_CUDA(cudaStreamSynchronize(st), "sync");
@@ -401,6 +477,7 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
             m->built = true;
             m->generation++;
         }
+        bump_mesh_epoch();
         return LCX_OK;
     }
     const uint32_t n = uint32_t(total);
@@ -429,7 +506,11 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
         const size_t t_bytes = size_t(n) * sizeof(TriRec), sah_bytes = 2 * sizeof(double) * count;
         bool want_rtab = false;
         for (MeshObj *m : meshes) want_rtab = want_rtab || m->opt.allow_update;
-        const size_t r_bytes = want_rtab ? size_t(W) * sizeof(unsigned long long) : 0;
+        // refit data: parent table, counters, segment table (16-byte aligned)
+        const size_t r_bytes =
+            want_rtab ? ((size_t(W) * (sizeof(unsigned long long) + sizeof(uint32_t)) + 15) & ~size_t(15)) +
+                            sizeof(SegInput) * count
+                      : 0;
         block = std::make_shared<DevBlock>();
         block->bytes = q_bytes + f_bytes + t_bytes + sah_bytes + r_bytes;
         LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(BLAS)");
@@ -445,6 +526,15 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
         block->qn = qn;
         block->fn = fn;
         block->tris = tr;
+        if (rtab) {
+            block->counters = reinterpret_cast<uint32_t *>(rtab + W);
+            block->d_segs = reinterpret_cast<SegInput *>(
+                reinterpret_cast<char *>(rtab) + ((size_t(W) * (sizeof(unsigned long long) + sizeof(uint32_t)) + 15) &
+                                                  ~size_t(15)));
+            LCX_CUDA(cudaMemcpyAsync(block->d_segs, segs.data(), sizeof(SegInput) * count, cudaMemcpyHostToDevice, st),
+                     "refit segment table");
+            block->h_segs = segs;
+        }
         LCX_CUDA(cudaMemsetAsync(wsah, 0, sah_bytes, st), "cudaMemset");
         LCX_CUDA(emit_blas(s, bp, W, qn, fn, tr, wsah, rtab, st), "BLAS emit");
         for (size_t i = 0; i < count; i++) {
@@ -470,6 +560,7 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
         m->built = true;
         m->generation++;
     }
+    bump_mesh_epoch();
     if (rb.ctl[kCtlErr] & kErrQuant) return fail(LCX_ERR_INVALID_ARG, "vertex coordinates too large to quantise");
     return LCX_OK;
 }
@@ -508,12 +599,13 @@ int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, u
         return fail(LCX_ERR_INVALID_ARG, "rays must be 16-byte and hits 8-byte aligned");
     std::lock_guard<std::mutex> lk(a->mtx);
     if (!a->built) return fail(LCX_ERR_NOT_BUILT, "accel not built");
-    for (const auto &mg : a->mesh_gens) {
-        auto m = find_mesh(mg.first);
-        if (!m) return fail(LCX_ERR_NOT_BUILT, "mesh %llu was destroyed; rebuild the accel", (unsigned long long)mg.first);
-        if (m->generation != mg.second)
-            return fail(LCX_ERR_NOT_BUILT, "mesh %llu was rebuilt after the accel build; rebuild the accel",
-                        (unsigned long long)mg.first);
+    {
+        uint64_t h = 0;
+        bool gone = false;
+        if (!meshes_current(a.get(), &h, &gone))
+            return fail(LCX_ERR_NOT_BUILT, gone ? "mesh %llu was destroyed; rebuild the accel"
+                                                : "mesh %llu was rebuilt after the accel build; rebuild the accel",
+                        (unsigned long long)h);
     }
     const uint32_t depth_need = a->depth + a->max_blas_depth + 3;
     if (int(depth_need) > kStackSize)
@@ -583,6 +675,7 @@ int lcx_mesh_destroy(uint64_t mesh) {
         m = it->second;
         g_meshes.erase(it);
     }
+    bump_mesh_epoch();
     std::lock_guard<std::mutex> lk(m->mtx);
     cudaDeviceSynchronize();  // the BVH may be in use by queued work
     m->block.reset();
@@ -740,8 +833,19 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     if (instance_count == 0) return fail(LCX_ERR_INVALID_ARG, "Building acceleration structure without instances.");
     if (mod_count && !mods) return fail(LCX_ERR_INVALID_ARG, "modifications pointer is null");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    Retired retired;  // the replaced TLAS block, released after the mutex below
+    Retired retired;  // the replaced TLAS block, released after the locks below
+    // no mesh referenced below can be destroyed (its BLAS descriptor freed) before
+    // the build's kernels are enqueued
+    std::shared_lock<std::shared_mutex> life(g_life_mtx);
     std::lock_guard<std::mutex> lk(a->mtx);
+    // in a CUDA graph capture only a TLAS refit without modifications can run
+    // (modifications are host data; a build sizes its block on the host)
+    if (capturing(st) &&
+        (mod_count || update_instance_buffer_only || request != LCX_REQUEST_PREFER_UPDATE || !a->opt.allow_update ||
+         !a->built || a->pending_rebuild || instance_count != a->built_instances || !a->block || !a->block->rtab))
+        return fail(LCX_ERR_INVALID_ARG,
+                    "lcx_accel_build in a CUDA graph capture: only a TLAS refit without modifications can be captured "
+                    "(apply modifications with update_instance_buffer_only outside the capture)");
     // translate and validate the modifications
     std::vector<ModRec> recs(mod_count);
     std::vector<uint64_t> new_mesh(mod_count, 0);
@@ -782,11 +886,16 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
         a->inst_cap = cap;
     }
     if (instance_count > a->inst_count) LCX_CUDA(init_instances(a->d_inst, a->inst_count, instance_count, st), "init");
+    if (instance_count != a->inst_count) a->uniq_dirty = true;
     a->inst_mesh.resize(instance_count, 0);
     for (uint32_t i = a->inst_count; i < instance_count; i++) a->inst_mesh[i] = 0;
     a->inst_count = instance_count;
     for (size_t i = 0; i < mod_count; i++)
-        if (new_mesh[i]) a->inst_mesh[recs[i].index] = new_mesh[i];
+        if (new_mesh[i]) {
+            a->inst_mesh[recs[i].index] = new_mesh[i];
+            a->uniq_dirty = true;
+            a->pending_rebuild = true;  // as cuda_accel.cpp:184-185: a primitive change forces a rebuild
+        }
     if (mod_count) {
         ScratchHolder hold(st);
         ModRec *d_mods = nullptr;
@@ -797,8 +906,48 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     }
     if (update_instance_buffer_only) return LCX_OK;
 
-    // TLAS build: one segment of instances, one instance per leaf slot
+    // every referenced mesh must exist and be built before a kernel reads its descriptor
+    std::vector<std::pair<uint64_t, uint64_t>> gens;
+    uint32_t max_blas_depth = 0;
+    {
+        if (a->uniq_dirty) {
+            std::vector<uint64_t> &uniq = a->uniq_mesh;
+            uniq.assign(a->inst_mesh.begin(), a->inst_mesh.end());
+            std::sort(uniq.begin(), uniq.end());
+            uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+            if (!uniq.empty() && uniq[0] == 0) uniq.erase(uniq.begin());
+            a->uniq_dirty = false;
+        }
+        for (uint64_t h : a->uniq_mesh) {
+            auto m = find_mesh(h);
+            if (!m) return fail(LCX_ERR_INVALID_ARG, "instance references destroyed mesh %llu", (unsigned long long)h);
+            if (!m->built) return fail(LCX_ERR_NOT_BUILT, "Mesh not built");
+            gens.emplace_back(h, m->generation);
+            max_blas_depth = std::max(max_blas_depth, m->depth);
+        }
+    }
     const uint32_t n = instance_count;
+
+    // PREFER_UPDATE of an accel created with allow_update, built with the same
+    // instance count and no instance primitive changed since (the rebuild rules
+    // of cuda_accel.cpp:261-267): refit the TLAS (same topology, new instance
+    // boxes and records); kernels only, no host synchronisation
+    DevBlock *tb = a->block.get();
+    if (request == LCX_REQUEST_PREFER_UPDATE && a->opt.allow_update && a->built && !a->pending_rebuild && tb &&
+        tb->rtab && n == a->built_instances) {
+        DeviceState *ds = nullptr;
+        if (int r = current_device_state(&ds)) return r;
+        LCX_CUDA(refit_tlas(a->d_inst, n, tb->ilo, tb->ihi, tb->w2o, tb->segctl, tb->wide, tb->rtab, a->qn, a->fn,
+                            a->recs, tb->counters, ds->refit_ctl, st),
+                 "TLAS refit");
+        a->mesh_gens = gens;
+        a->checked_epoch = 0;
+        a->max_blas_depth = max_blas_depth;
+        a->refits++;
+        return LCX_OK;
+    }
+
+    // TLAS build: one segment of instances, one instance per leaf slot
     BuildParams bp = build_params_for(a->opt);
     bp.leaf_max = 1;
     bp.size_bits = g_build_tune.tlas_size_bits;
@@ -819,15 +968,36 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
         const uint32_t W = rb.ctl[kCtlWideCount];
         const size_t q_bytes = size_t(W) * sizeof(Node8Q), f_bytes = size_t(W) * sizeof(Node8F);
         const size_t r_bytes = size_t(n) * sizeof(InstRec);
+        // refit data (allow_update): parent table + counters, instance boxes and inverses, segment words
+        const size_t tab_bytes = (size_t(W) * (sizeof(unsigned long long) + sizeof(uint32_t)) + 15) & ~size_t(15);
+        const size_t u_bytes =
+            a->opt.allow_update ? tab_bytes + size_t(n) * (2 * sizeof(float4) + 12 * sizeof(float)) +
+                                      sizeof(uint32_t) * kSegWords
+                                : 0;
         block = std::make_shared<DevBlock>();
-        block->bytes = q_bytes + f_bytes + r_bytes + 2 * sizeof(double);
+        block->bytes = q_bytes + f_bytes + r_bytes + 2 * sizeof(double) + u_bytes;
         LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(TLAS)");
         Node8Q *qn = static_cast<Node8Q *>(block->ptr);
         Node8F *fn = reinterpret_cast<Node8F *>(reinterpret_cast<char *>(block->ptr) + q_bytes);
         InstRec *ir = reinterpret_cast<InstRec *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes);
         double *wsah = reinterpret_cast<double *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes + r_bytes);
+        unsigned long long *rtab = nullptr;
+        if (a->opt.allow_update) {
+            char *u = reinterpret_cast<char *>(wsah) + 2 * sizeof(double);
+            rtab = reinterpret_cast<unsigned long long *>(u);
+            block->rtab = rtab;
+            block->counters = reinterpret_cast<uint32_t *>(rtab + W);
+            block->ilo = reinterpret_cast<float4 *>(u + tab_bytes);
+            block->ihi = block->ilo + n;
+            block->w2o = reinterpret_cast<float *>(block->ihi + n);
+            block->segctl = reinterpret_cast<uint32_t *>(block->w2o + 12ull * n);
+            block->wide = W;
+            block->nseg = 1;
+            block->qn = qn;
+            block->fn = fn;
+        }
         LCX_CUDA(cudaMemsetAsync(wsah, 0, 2 * sizeof(double), st), "cudaMemset");
-        LCX_CUDA(emit_tlas(a->d_inst, s, bp, W, qn, fn, ir, wsah, st), "TLAS emit");
+        LCX_CUDA(emit_tlas(a->d_inst, s, bp, W, qn, fn, ir, wsah, rtab, st), "TLAS emit");
         a->qn = qn;
         a->fn = fn;
         a->recs = ir;
@@ -839,22 +1009,13 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     if (a->block) retired.blocks.push_back(std::move(a->block));
     a->block = block;
     // remember which mesh builds this TLAS references
-    a->mesh_gens.clear();
-    a->max_blas_depth = 0;
-    {
-        std::vector<uint64_t> uniq(a->inst_mesh.begin(), a->inst_mesh.end());
-        std::sort(uniq.begin(), uniq.end());
-        uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
-        for (uint64_t h : uniq) {
-            if (!h) continue;
-            auto m = find_mesh(h);
-            if (!m) return fail(LCX_ERR_INVALID_ARG, "instance references destroyed mesh %llu", (unsigned long long)h);
-            a->mesh_gens.emplace_back(h, m->generation);
-            a->max_blas_depth = std::max(a->max_blas_depth, m->depth);
-        }
-    }
+    a->mesh_gens = gens;
+    a->checked_epoch = 0;
+    a->max_blas_depth = max_blas_depth;
     a->built_instances = n;
     a->built = true;
+    a->pending_rebuild = false;
+    a->refits = 0;
     return LCX_OK;
 }
 
@@ -869,6 +1030,7 @@ int lcx_accel_stats(uint64_t accel, LcxAccelStats *out) {
     out->device_bytes = (a->block ? a->block->bytes : 0) + sizeof(InstState) * a->inst_cap;
     out->depth = a->depth;
     out->max_blas_depth = a->max_blas_depth;
+    out->refits = a->refits;
     out->sah_cost = a->sah;
     if (a->wide_sah) {
         double h[2] = {0, 0};
@@ -911,6 +1073,19 @@ int lcx_get_build_tuning(uint32_t *leaf_max, uint32_t *width) {
 }
 
 // ---------------------------------------------------------------- queries
+// Counter slot of a trace call on `st`: round robin over the live slots, or
+// over the graph slots while `st` is being captured.
+static uint32_t trace_slot(DeviceState *ds, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+        (void)cudaGetLastError();  // the legacy stream during another stream's capture: the launch reports it
+        cs = cudaStreamCaptureStatusNone;
+    }
+    if (cs == cudaStreamCaptureStatusActive)
+        return kPoolSlots - kGraphSlots + ds->next_graph_slot.fetch_add(1) % kGraphSlots;
+    return ds->next_slot.fetch_add(1) % (kPoolSlots - kGraphSlots);
+}
+
 static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
                         uint8_t *d_occ, uint32_t *d_counts, uint32_t layout, void *stream) {
     if (layout > LCX_NODES_QUANT8) return fail(LCX_ERR_INVALID_ARG, "invalid node layout %u", layout);
@@ -930,14 +1105,12 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     {
         std::lock_guard<std::mutex> lk(a->mtx);
         if (!a->built) return fail(LCX_ERR_NOT_BUILT, "accel not built");
-        for (const auto &mg : a->mesh_gens) {
-            auto m = find_mesh(mg.first);
-            if (!m) return fail(LCX_ERR_NOT_BUILT, "mesh %llu was destroyed; rebuild the accel",
-                                (unsigned long long)mg.first);
-            if (m->generation != mg.second)
-                return fail(LCX_ERR_NOT_BUILT, "mesh %llu was rebuilt after the accel build; rebuild the accel",
-                            (unsigned long long)mg.first);
-        }
+        uint64_t h = 0;
+        bool gone = false;
+        if (!meshes_current(a.get(), &h, &gone))
+            return fail(LCX_ERR_NOT_BUILT, gone ? "mesh %llu was destroyed; rebuild the accel"
+                                                : "mesh %llu was rebuilt after the accel build; rebuild the accel",
+                        (unsigned long long)h);
         depth_need = a->depth + a->max_blas_depth + 3;
         if (int(depth_need) > kStackSize)
             return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the traversal stack (%d)", a->depth,
@@ -948,8 +1121,8 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     }
     DeviceState *ds = nullptr;
     if (int r = current_device_state(&ds)) return r;
-    const uint32_t slot = ds->next_slot.fetch_add(1) % kPoolSlots;
-    p.pool = ds->pool + 4 * slot;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    p.pool = ds->pool + 4 * trace_slot(ds, st);
     p.rays = reinterpret_cast<const Ray *>(d_rays);
     p.hits = reinterpret_cast<Hit *>(d_hits);
     p.occluded = d_occ;
@@ -963,7 +1136,6 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     // regular pushes need at most tlas_depth + blas_depth + 3 entries; postponed
     // triangle groups may use what is left
     p.postpone_sp = kStackSize - int(depth_need);
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     ReorderScratch rs;
     const uint32_t rbits = g_reorder.bits;
     if (rbits != 0 && ray_count >= g_reorder.min_rays) {
@@ -983,11 +1155,8 @@ int lcx_accel_device_view(uint64_t accel, LcxAccelView *out) {
     if (!a) return fail(LCX_ERR_INVALID_ARG, "unknown accel handle %llu", (unsigned long long)accel);
     std::lock_guard<std::mutex> lk(a->mtx);
     if (!a->built) return fail(LCX_ERR_NOT_BUILT, "accel not built");
-    for (const auto &mg : a->mesh_gens) {
-        auto m = find_mesh(mg.first);
-        if (!m || m->generation != mg.second)
-            return fail(LCX_ERR_NOT_BUILT, "a mesh of the accel was destroyed, rebuilt or refit; rebuild the accel");
-    }
+    if (!meshes_current(a.get()))
+        return fail(LCX_ERR_NOT_BUILT, "a mesh of the accel was destroyed, rebuilt or refit; rebuild the accel");
     const uint32_t need = a->depth + a->max_blas_depth + 3;
     if (int(need) > kStackSize)
         return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the query stack (%d)", a->depth,
@@ -1017,12 +1186,9 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
         if (!a) return fail(LCX_ERR_INVALID_ARG, "job %u: unknown accel handle %llu", i, (unsigned long long)j.accel);
         std::lock_guard<std::mutex> lk(a->mtx);
         if (!a->built) return fail(LCX_ERR_NOT_BUILT, "job %u: accel not built", i);
-        for (const auto &mg : a->mesh_gens) {
-            auto m = find_mesh(mg.first);
-            if (!m || m->generation != mg.second)
-                return fail(LCX_ERR_NOT_BUILT, "job %u: a mesh of the accel was destroyed or rebuilt; rebuild the accel",
-                            i);
-        }
+        if (!meshes_current(a.get()))
+            return fail(LCX_ERR_NOT_BUILT, "job %u: a mesh of the accel was destroyed or rebuilt; rebuild the accel",
+                        i);
         const uint32_t need = a->depth + a->max_blas_depth + 3;
         if (int(need) > kStackSize) return fail(LCX_ERR_DEPTH, "job %u: BVH too deep for the traversal stack", i);
         depth_need = std::max(depth_need, need);
@@ -1052,8 +1218,7 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
                                  st),
                  "job table upload");
         TraceParams p{};
-        const uint32_t slot = ds->next_slot.fetch_add(1) % kPoolSlots;
-        p.pool = ds->pool + 4 * slot;
+        p.pool = ds->pool + 4 * trace_slot(ds, st);
         p.ray_count = uint32_t(totals[g]);
         p.refill = g_tune.refill;
         p.postpone = 0;
@@ -1079,6 +1244,13 @@ int lcx_check_trace_errors(void) {
         for (uint32_t i = 0; i < kPoolSlots; i++) h[4 * i + 1] = 0;
         LCX_CUDA(cudaMemcpy(ds->pool, h.data(), h.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "pool reset");
     }
+    uint32_t rerr = 0;  // errors of refits that did not synchronise
+    LCX_CUDA(cudaMemcpy(&rerr, ds->refit_ctl + kCtlErr, sizeof(uint32_t), cudaMemcpyDeviceToHost), "refit readback");
+    if (rerr) {
+        LCX_CUDA(cudaMemset(ds->refit_ctl, 0, kCtlWords * sizeof(uint32_t)), "refit error reset");
+        if (rerr & kErrTooDeep) return fail(LCX_ERR_DEPTH, "an asynchronous refit met a BVH deeper than expected");
+        return fail(LCX_ERR_INVALID_ARG, "an asynchronous refit failed (bad index or unquantisable coordinates)");
+    }
     if (flags & 2u) return fail(LCX_ERR_TIMEOUT, "a ray exceeded the traversal step bound (corrupt BVH?)");
     if (flags & 1u) return fail(LCX_ERR_DEPTH, "a ray overflowed the traversal stack");
     return LCX_OK;
@@ -1090,6 +1262,12 @@ int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone, uint32_t mode) {
     g_tune.refill = refill;
     g_tune.postpone = postpone;
     g_tune.mode = mode;
+    return LCX_OK;
+}
+
+int lcx_set_refit_sync(uint32_t sync) {
+    if (sync > 1) return fail(LCX_ERR_INVALID_ARG, "lcx_set_refit_sync: 0 or 1");
+    g_refit_sync = sync != 0;
     return LCX_OK;
 }
 

@@ -109,8 +109,15 @@ cudaError_t emit_blas(const BuildScratch &s, const BuildParams &bp, uint32_t wid
 // counters: W words of scratch; ctl: kCtlWords zeroed words (errors).
 cudaError_t refit_blas(const SegInput *segs, uint32_t nseg, uint32_t W, const unsigned long long *rtab, Node8Q *qn,
                        Node8F *fn, TriRec *tris, uint32_t *counters, uint32_t *ctl, cudaStream_t st);
+// TLAS refit (same topology): instance boxes and inverses from the current
+// instance states, then the bottom-up refit rewriting the instance records.
+// ilo/ihi/w2o: n-sized scratch; segctl: kSegWords words of scratch.
+cudaError_t refit_tlas(const InstState *inst, uint32_t n, float4 *ilo, float4 *ihi, float *w2o, uint32_t *segctl,
+                       uint32_t W, const unsigned long long *rtab, Node8Q *qn, Node8F *fn, InstRec *recs,
+                       uint32_t *counters, uint32_t *ctl, cudaStream_t st);
 cudaError_t emit_tlas(const InstState *inst, const BuildScratch &s, const BuildParams &bp, uint32_t wide_count,
-                      Node8Q *qn, Node8F *fn, InstRec *recs, double *wide_sah, cudaStream_t st);
+                      Node8Q *qn, Node8F *fn, InstRec *recs, double *wide_sah, unsigned long long *rtab,
+                      cudaStream_t st);
 
 cudaError_t apply_modifications(const ModRec *mods, uint32_t count, InstState *inst, uint32_t instance_count,
                                 cudaStream_t st);

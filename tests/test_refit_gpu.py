@@ -131,3 +131,199 @@ def test_refit_batch_and_fallbacks(lcx, oracle_mod):
     plain.build(request=REQUEST_PREFER_UPDATE)
     assert plain.stats().refits == 0
     _check(oracle_mod, _accel([plain]), [datas[2]], rays)
+
+
+# ------------------------------------------------------------------ TLAS refit
+# PREFER_UPDATE on an accel created with allow_update (src/backends/cuda/cuda_accel.cpp:261-320:
+# update unless the instance count or an instance's primitive changed). The refit recomputes the
+# instance boxes and records from the current transforms, masks and meshes; hit records must equal
+# the oracle's on the new scene bit for bit.
+
+def _check_scene(oracle_mod, acc, scene, rays, layouts=(0, 1)):
+    import torch
+    from luisacompute_gb300 import _capi
+    from luisacompute_gb300.accel import hits_to_numpy, rays_to_device
+    want = oracle_mod.OracleScene(scene).trace_closest(rays)
+    for layout in layouts:
+        got = hits_to_numpy(acc.trace_closest(rays_to_device(rays), layout=layout))
+        torch.cuda.synchronize()
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), f"layout {layout}"
+    _capi.check(_capi.load().lcx_check_trace_errors(), "trace errors")
+    return want
+
+
+def _placements(rng, n, spread=1.5):
+    return S.affine_rows(S.random_rotations(n, rng), rng.uniform(0.15, 0.4, n), rng.uniform(-spread, spread, (n, 3)))
+
+
+def test_tlas_refit_moving_instances(lcx, oracle_mod):
+    import torch
+    from luisacompute_gb300.accel import REQUEST_PREFER_UPDATE, Accel, AccelOption, build_meshes
+    rng = np.random.default_rng(11)
+    datas = [S.displaced_mesh(int(n), rng) for n in (1_500, 6_000, 400)]
+    meshes = build_meshes(_device(datas))
+    n = 300
+    inst_mesh = np.arange(n) % 3
+    aff = _placements(rng, n)
+    masks = np.full(n, 0xFF, np.uint32)
+    acc = Accel(AccelOption(allow_update=True))
+    acc.emplace_back_many([meshes[i] for i in inst_mesh], aff)
+    acc.build()
+    nodes = acc.stats().node_count
+    rays = S.sphere_rays(80_000, [-2.0] * 3, [2.0] * 3, seed=41)
+    _check_scene(oracle_mod, acc, S.Scene(datas, inst_mesh, aff, masks), rays)
+    # move every instance a little, hide a few: refit twice
+    for step in (1, 2):
+        aff = aff.copy()
+        aff[:, [3, 7, 11]] += rng.normal(0.0, 0.1, (n, 3)).astype(np.float32)
+        for i in range(n):
+            acc.set_transform_on_update(i, aff[i].reshape(3, 4))
+        hidden = rng.choice(n, 20, replace=False)
+        masks[:] = 0xFF
+        masks[hidden] = 0
+        for i in range(n):
+            acc.set_visibility_on_update(i, int(masks[i]))
+        acc.build(request=REQUEST_PREFER_UPDATE)
+        st = acc.stats()
+        assert st.refits == step and st.node_count == nodes
+        _check_scene(oracle_mod, acc, S.Scene(datas, inst_mesh, aff, masks), rays)
+    # the instances' meshes are refit: the TLAS refit takes their new boxes
+    datas = [_deform(md, rng, 0.02, 1.3) for md in datas]
+    for m, md in zip(meshes, datas):
+        m.vertices.copy_(torch.from_numpy(md.vertices).cuda())
+    build_meshes(meshes, request=REQUEST_PREFER_UPDATE)
+    assert all(m.stats().refits == 1 for m in meshes)
+    acc.build(request=REQUEST_PREFER_UPDATE)
+    assert acc.stats().refits == 3
+    _check_scene(oracle_mod, acc, S.Scene(datas, inst_mesh, aff, masks), rays)
+    # an instance's primitive changed: rebuilt, as cuda_accel.cpp:184-185
+    inst_mesh = inst_mesh.copy()
+    inst_mesh[0] = 1
+    acc.set_mesh_on_update(0, meshes[1])
+    acc.build(request=REQUEST_PREFER_UPDATE)
+    assert acc.stats().refits == 0
+    _check_scene(oracle_mod, acc, S.Scene(datas, inst_mesh, aff, masks), rays)
+    # a later PREFER_UPDATE refits again
+    acc.build(request=REQUEST_PREFER_UPDATE)
+    assert acc.stats().refits == 1
+    # FORCE_BUILD and an accel without allow_update rebuild
+    acc.build()
+    assert acc.stats().refits == 0
+    plain = Accel(AccelOption(allow_update=False))
+    plain.emplace_back_many([meshes[i] for i in inst_mesh], aff, masks)
+    plain.build()
+    plain.build(request=REQUEST_PREFER_UPDATE)
+    assert plain.stats().refits == 0
+    _check_scene(oracle_mod, plain, S.Scene(datas, inst_mesh, aff, masks), rays, layouts=(0,))
+
+
+def test_async_refit_reports_errors(lcx, oracle_mod):
+    """With lcx_set_refit_sync(0) a refit only enqueues kernels; a bad index is reported by the
+    next lcx_check_trace_errors, and the flag is cleared after the report."""
+    import torch
+    from luisacompute_gb300 import _capi
+    from luisacompute_gb300.accel import REQUEST_PREFER_UPDATE, set_refit_sync
+    rng = np.random.default_rng(12)
+    md = S.displaced_mesh(3_000, rng)
+    (mesh,) = _device([md])
+    mesh.build()
+    set_refit_sync(False)
+    try:
+        md = _deform(md, rng, 0.01)
+        mesh.vertices.copy_(torch.from_numpy(md.vertices).cuda())
+        mesh.build(request=REQUEST_PREFER_UPDATE)
+        assert mesh.stats().refits == 1
+        assert lcx.lcx_check_trace_errors() == 0
+        _check(oracle_mod, _accel([mesh]), [md], S.sphere_rays(30_000, [-1.3] * 3, [1.3] * 3, seed=42))
+        # one index past the vertex count: the refit kernel flags it (and skips the read)
+        bad = md.triangles.astype(np.int32).copy()
+        bad[7, 1] = md.vertices.shape[0]
+        mesh.triangles.copy_(torch.from_numpy(bad).cuda())
+        mesh.build(request=REQUEST_PREFER_UPDATE)  # returns at once
+        assert lcx.lcx_check_trace_errors() == _capi.LCX_ERR_INVALID_ARG
+        assert lcx.lcx_check_trace_errors() == 0
+    finally:
+        set_refit_sync(True)
+
+
+@pytest.mark.filterwarnings("ignore:The CUDA Graph is empty")  # the refused captures end empty
+def test_refit_frame_in_cuda_graph(lcx, oracle_mod):
+    """An animation frame captured once in a CUDA graph and replayed: a torch kernel writes each
+    mesh's new vertices, the BLASes and the TLAS are refit and rays are traced. Between replays
+    the host moves instances with update_instance_buffer_only; every replay must match the oracle
+    on the frame's vertices (read back) and transforms. Calls that cannot be captured (a build,
+    synchronous refit) fail with an error instead of breaking the capture silently."""
+    import torch
+    from luisacompute_gb300 import _capi
+    from luisacompute_gb300.accel import (REQUEST_PREFER_UPDATE, Accel, AccelOption, build_meshes, hits_to_numpy,
+                                          rays_to_device, set_refit_sync)
+    rng = np.random.default_rng(13)
+    datas = [S.displaced_mesh(int(n), rng) for n in (2_000, 7_000, 600)]
+    meshes = build_meshes(_device(datas))
+    n = 120
+    inst_mesh = np.arange(n) % 3
+    aff = _placements(rng, n)
+    acc = Accel(AccelOption(allow_update=True))
+    acc.emplace_back_many([meshes[i] for i in inst_mesh], aff)
+    acc.build()
+    rays = S.sphere_rays(50_000, [-2.0] * 3, [2.0] * 3, seed=43)
+    d_rays = rays_to_device(rays)
+    out = torch.empty((rays.shape[0], 6), dtype=torch.int32, device="cuda")
+    base = [m.vertices.clone() for m in meshes]
+    disp = []
+    for md in datas:
+        d = np.zeros_like(md.vertices)
+        d[:, :3] = rng.normal(0.0, 0.02, (md.vertices.shape[0], 3))
+        disp.append(torch.from_numpy(d).cuda())
+    phase = torch.zeros(1, device="cuda")
+    old_bits, old_min = ctypes_pair(lcx.lcx_get_trace_reorder)
+    _capi.check(lcx.lcx_set_trace_reorder(0, old_min), "reorder off")
+    set_refit_sync(False)
+    try:
+        # a first refit outside the capture puts the segment table on the device
+        build_meshes(meshes, request=REQUEST_PREFER_UPDATE)
+        acc.build(request=REQUEST_PREFER_UPDATE)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            for m, b, d in zip(meshes, base, disp):
+                m.vertices.copy_(b + d * phase)
+            build_meshes(meshes, request=REQUEST_PREFER_UPDATE)
+            acc.build(request=REQUEST_PREFER_UPDATE)
+            acc.trace_closest(d_rays, out=out)
+        for frame, p in enumerate((0.0, 1.0, -2.5, 4.0)):
+            if frame >= 2:  # move a third of the instances between replays
+                aff = aff.copy()
+                moved = rng.choice(n, n // 3, replace=False)
+                aff[moved, 3] += rng.normal(0.0, 0.2, moved.size).astype(np.float32)
+                for i in moved:
+                    acc.set_transform_on_update(int(i), aff[i].reshape(3, 4))
+                acc.build(update_instance_buffer_only=True)
+            phase.fill_(p)
+            g.replay()
+            torch.cuda.synchronize()
+            frame_datas = [S.MeshData(m.vertices.cpu().numpy(), md.triangles) for m, md in zip(meshes, datas)]
+            want = oracle_mod.OracleScene(S.Scene(frame_datas, inst_mesh, aff, np.full(n, 0xFF, np.uint32))) \
+                .trace_closest(rays)
+            got = hits_to_numpy(out)
+            assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), f"frame {frame}"
+            assert (got["inst"] != 0xFFFFFFFF).mean() > 0.05
+            _capi.check(lcx.lcx_check_trace_errors(), "trace / refit errors")
+        # what cannot be captured is refused before any work is enqueued
+        for call in (lambda: acc.build(), lambda: (set_refit_sync(True), build_meshes(
+                meshes, request=REQUEST_PREFER_UPDATE))):
+            g2 = torch.cuda.CUDAGraph()
+            with pytest.raises(_capi.LcxError):
+                with torch.cuda.graph(g2):
+                    call()
+            set_refit_sync(False)
+    finally:
+        set_refit_sync(True)
+        _capi.check(lcx.lcx_set_trace_reorder(old_bits, old_min), "reorder restore")
+
+
+def ctypes_pair(fn):
+    import ctypes
+    a, b = ctypes.c_uint32(), ctypes.c_uint32()
+    _ = fn(ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
