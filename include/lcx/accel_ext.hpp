@@ -187,6 +187,15 @@ public:
                    void *stream) const {
         check(lcx_trace_any(accel, rays, n, mask, occluded, stream), "trace_any");
     }
+    // The same queries over host buffers (the CPU backend's form), copies overlapped with the traversal.
+    void trace_closest_host(uint64_t accel, const Ray *rays, uint32_t n, uint32_t mask, TriangleHit *hits,
+                            void *stream, uint32_t layout = LCX_NODES_QUANT8) const {
+        check(lcx_trace_closest_host(accel, rays, n, mask, hits, layout, stream), "trace_closest_host");
+    }
+    void trace_any_host(uint64_t accel, const Ray *rays, uint32_t n, uint32_t mask, uint8_t *occluded, void *stream,
+                        uint32_t layout = LCX_NODES_QUANT8) const {
+        check(lcx_trace_any_host(accel, rays, n, mask, occluded, layout, stream), "trace_any_host");
+    }
     // Ray batches of many jobs (accels, closest or any) in one launch per kind.
     void trace_jobs(const std::vector<LcxTraceJob> &jobs, void *stream, uint32_t layout = LCX_NODES_QUANT8) const {
         check(lcx_trace_jobs(jobs.data(), uint32_t(jobs.size()), layout, stream), "trace_jobs");

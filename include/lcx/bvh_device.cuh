@@ -27,6 +27,33 @@ constexpr int kMaxLeafItems = 3;    // items per leaf slot (meta holds a 2-bit c
 constexpr int kStackSize = 32;      // traversal stack entries per thread
 constexpr int kMaxLevels = 64;      // wide-tree depth limit of the collapse
 
+#ifndef LCX_L2_KEEP
+#define LCX_L2_KEEP 0
+#endif
+
+// Loads of BVH data (nodes, leaf items, instance records) by the traversal:
+// the read-only path.  LCX_L2_KEEP=1 adds an L2 evict-last policy, so that the
+// rays and hits streaming through L2 (loaded and stored evict-first, .cs)
+// would be evicted first; measured 2 % slower on the incoherent terrain
+// workload (1.730 vs 1.770 Grays/s), so it is off.
+__device__ __forceinline__ uint4 bvh_ld(const uint4 *p) {
+#if LCX_L2_KEEP
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    uint4 v;
+    asm("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(p), "l"(pol));
+    return v;
+#else
+    return __ldg(p);
+#endif
+}
+__device__ __forceinline__ float4 bvh_ld(const float4 *p) {
+    const uint4 v = bvh_ld(reinterpret_cast<const uint4 *>(p));
+    return make_float4(__uint_as_float(v.x), __uint_as_float(v.y), __uint_as_float(v.z), __uint_as_float(v.w));
+}
+
 // Meta byte of a child slot: (bits << 5) | index.  A hit child contributes
 // `bits << index` to a 32-bit hit word: internal children have bits = 1 and
 // index 24 + slot (so their hits land in bits 24..31, reordered front to back

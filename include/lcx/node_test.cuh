@@ -91,7 +91,7 @@ __device__ __forceinline__ void intersect_q(const Node8Q *nodes, uint32_t idx, f
                                             float ix, float iy, float iz, uint32_t octinv, float tmin, float tmax,
                                             uint2 &G, uint2 &Gt) {
     const uint4 *p = reinterpret_cast<const uint4 *>(nodes + idx);
-    const uint4 n0 = __ldg(p), n1 = __ldg(p + 1), n2 = __ldg(p + 2), n3 = __ldg(p + 3), n4 = __ldg(p + 4);
+    const uint4 n0 = bvh_ld(p), n1 = bvh_ld(p + 1), n2 = bvh_ld(p + 2), n3 = bvh_ld(p + 3), n4 = bvh_ld(p + 4);
     const float adx = __uint_as_float((n0.w & 0xffu) << 23) * ix;
     const float ady = __uint_as_float(((n0.w >> 8) & 0xffu) << 23) * iy;
     const float adz = __uint_as_float(((n0.w >> 16) & 0xffu) << 23) * iz;
@@ -142,7 +142,7 @@ __device__ __forceinline__ void intersect_f(const Node8F *nodes, uint32_t idx, f
                                             float ix, float iy, float iz, uint32_t octinv, float tmin, float tmax,
                                             uint2 &G, uint2 &Gt) {
     const float4 *p = reinterpret_cast<const float4 *>(nodes + idx);
-    const uint4 hdr = __ldg(reinterpret_cast<const uint4 *>(p + 12));
+    const uint4 hdr = bvh_ld(reinterpret_cast<const uint4 *>(p + 12));
     const bool nx = ix < 0.0f, ny = iy < 0.0f, nz = iz < 0.0f;
     // lo_x: p[0..1], hi_x: p[2..3], lo_y: p[4..5], hi_y: p[6..7], lo_z: p[8..9], hi_z: p[10..11]
     uint32_t bits = 0, imask = 0;
@@ -153,9 +153,9 @@ __device__ __forceinline__ void intersect_f(const Node8F *nodes, uint32_t idx, f
 #endif
 #pragma unroll
     for (int half = 0; half < 2; half++) {
-        const float4 lx = __ldg(p + 0 + half), hx = __ldg(p + 2 + half);
-        const float4 ly = __ldg(p + 4 + half), hy = __ldg(p + 6 + half);
-        const float4 lz = __ldg(p + 8 + half), hz = __ldg(p + 10 + half);
+        const float4 lx = bvh_ld(p + 0 + half), hx = bvh_ld(p + 2 + half);
+        const float4 ly = bvh_ld(p + 4 + half), hy = bvh_ld(p + 6 + half);
+        const float4 lz = bvh_ld(p + 8 + half), hz = bvh_ld(p + 10 + half);
         const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
         const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
         const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};

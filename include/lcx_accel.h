@@ -310,6 +310,29 @@ LCX_API int lcx_trace_any_ex(uint64_t accel, const LcxRay *d_rays, uint32_t ray_
                      uint32_t mask, uint8_t *d_occluded, uint32_t node_layout,
                      void *stream);
 
+/* The same queries over HOST buffers, for callers whose rays and results live
+ * in host memory -- the form of the reference's CPU backend, whose
+ * trace_closest / trace_any read and write host arrays
+ * (src/rust/luisa_compute_backend_impl/src/cpu/accel.rs:449-535).  The rays
+ * stream through device staging in chunks (lcx_set_host_chunk, default 2^21
+ * rays; a ring of 4 chunks of staging, 56 B per ray, kept in a memory pool): the copy in of one chunk, the traversal of the previous one and the
+ * copy out of the one before run at once.  Stream-ordered like the device
+ * forms: the work starts after `stream`'s earlier work and `stream` waits for
+ * the last result copy, so h_hits / h_occluded are complete once `stream` is
+ * synchronised.  Results equal the device forms'.  Pinned host memory
+ * (cudaHostAlloc / cudaHostRegister) overlaps the copies with the traversal;
+ * pageable memory works but serialises them.  Cannot be captured in a CUDA
+ * graph. */
+LCX_API int lcx_trace_closest_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count,
+                                   uint32_t mask, LcxTriangleHit *h_hits, uint32_t node_layout,
+                                   void *stream);
+LCX_API int lcx_trace_any_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count,
+                               uint32_t mask, uint8_t *h_occluded, uint32_t node_layout,
+                               void *stream);
+/* Rays per chunk of the host-buffer traces (2^14..2^26).  A tuning knob with
+ * no reference counterpart. */
+LCX_API int lcx_set_host_chunk(uint32_t rays);
+
 /* Counting build of the closest-hit traversal: per-ray visit counts
  * d_counts[3*i + {0,1,2}] = {wide nodes fetched, triangles tested, instances
  * entered}.  Used to compute algorithmic bytes per ray. */

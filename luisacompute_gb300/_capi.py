@@ -95,6 +95,9 @@ _SIGS = {
     "lcx_get_build_morton": (c_int, [POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
     "lcx_set_trace_reorder": (c_int, [c_uint32, c_uint32]),
     "lcx_set_trace_stack": (c_int, [c_uint32]),
+    "lcx_trace_closest_host": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
+    "lcx_trace_any_host": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
+    "lcx_set_host_chunk": (c_int, [c_uint32]),
     "lcx_set_refit_sync": (c_int, [c_uint32]),
     "lcx_get_trace_stack": (c_int, [POINTER(c_uint32)]),
     "lcx_get_trace_reorder": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),

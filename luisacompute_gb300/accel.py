@@ -282,6 +282,39 @@ class Accel:
               "lcx_trace_any")
         return out
 
+    # ------------------------------------------------- host-buffer queries
+    @staticmethod
+    def _host_ptr(buf, rec: int, what: str):
+        """(address, records) of a contiguous host buffer: a CPU torch tensor (pinned for
+        overlapped copies) or a numpy array."""
+        if isinstance(buf, np.ndarray):
+            if not buf.flags.c_contiguous or buf.nbytes % rec:
+                raise ValueError(f"{what}: contiguous array of {rec}-byte records expected")
+            return buf.ctypes.data, buf.nbytes // rec
+        if buf.is_cuda or not buf.is_contiguous() or buf.numel() * buf.element_size() % rec:
+            raise ValueError(f"{what}: contiguous CPU tensor of {rec}-byte records expected")
+        return buf.data_ptr(), buf.numel() * buf.element_size() // rec
+
+    def trace_closest_host(self, rays, out, mask: int = 0xFF, layout: int = NODES_QUANT8, stream=None):
+        """lcx_trace_closest_host: rays and hits in host memory; `out` is complete once `stream`
+        (default: the current torch stream) is synchronised."""
+        rp, n = self._host_ptr(rays, 32, "rays")
+        hp, m = self._host_ptr(out, 24, "hits")
+        if m < n:
+            raise ValueError("hit buffer smaller than the ray count")
+        check(self.lib.lcx_trace_closest_host(self.handle, rp, n, mask, hp, layout, stream_handle(stream)),
+              "lcx_trace_closest_host")
+        return out
+
+    def trace_any_host(self, rays, out, mask: int = 0xFF, layout: int = NODES_QUANT8, stream=None):
+        rp, n = self._host_ptr(rays, 32, "rays")
+        op, m = self._host_ptr(out, 1, "occluded")
+        if m < n:
+            raise ValueError("occluded buffer smaller than the ray count")
+        check(self.lib.lcx_trace_any_host(self.handle, rp, n, mask, op, layout, stream_handle(stream)),
+              "lcx_trace_any_host")
+        return out
+
     def destroy(self):
         if getattr(self, "handle", 0):
             check(self.lib.lcx_accel_destroy(self.handle), "lcx_accel_destroy")

@@ -208,7 +208,7 @@ struct Walker {
             const uint32_t k = __ffs(Gt.y) - 1u;
             Gt.y &= Gt.y - 1u;
             const float4 *tp = reinterpret_cast<const float4 *>(blas_tris + Gt.x + k);
-            const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            const float4 a = bvh_ld(tp), b = bvh_ld(tp + 1), c = bvh_ld(tp + 2);
             if (kCount) c_tris++;
             float t, u, v;
             if (wt_intersect(wt, tmin, best_t, a, b, c, t, u, v)) {
@@ -286,7 +286,7 @@ struct Walker {
             if (work) {
                 const uint32_t bit = __fns(gy, 0u, int(k) + 1);  // k-th set bit of the owner's group
                 const float4 *q = reinterpret_cast<const float4 *>(reinterpret_cast<const TriRec *>(tp) + gx + bit);
-                const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+                const float4 a = bvh_ld(q), b = bvh_ld(q + 1), c = bvh_ld(q + 2);
                 if (wt_intersect(r, lo, hi, a, b, c, t, u, v)) {
                     key = kAny ? 0ull
                                : (static_cast<unsigned long long>(float_to_ordered(t)) << 32) | __float_as_uint(a.w);
@@ -326,12 +326,12 @@ struct Walker {
             const uint32_t k = __ffs(Gt.y) - 1u;
             Gt.y &= Gt.y - 1u;
             const uint4 *ip = reinterpret_cast<const uint4 *>((kMulti ? insts : P.insts) + Gt.x + k);
-            const uint4 m4 = __ldg(ip + 4);  // fnodes (x,y), inst_id (z), mask (w)
+            const uint4 m4 = bvh_ld(ip + 4);  // fnodes (x,y), inst_id (z), mask (w)
             if ((m4.w & (kMulti ? mask : P.mask)) == 0u) continue;
-            const float4 r0 = __ldg(reinterpret_cast<const float4 *>(ip));
-            const float4 r1 = __ldg(reinterpret_cast<const float4 *>(ip + 1));
-            const float4 r2 = __ldg(reinterpret_cast<const float4 *>(ip + 2));
-            const uint4 pp = __ldg(ip + 3);  // qnodes (x,y), tris (z,w)
+            const float4 r0 = bvh_ld(reinterpret_cast<const float4 *>(ip));
+            const float4 r1 = bvh_ld(reinterpret_cast<const float4 *>(ip + 1));
+            const float4 r2 = bvh_ld(reinterpret_cast<const float4 *>(ip + 2));
+            const uint4 pp = bvh_ld(ip + 3);  // qnodes (x,y), tris (z,w)
             if (Gt.y) push(Gt);
             if (G.y) push(G);
             const float w[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};

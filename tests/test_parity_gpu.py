@@ -351,3 +351,51 @@ def test_ray_reorder_does_not_change_results(torch_cuda, lcx, oracle_mod, bits):
     finally:
         _capi.check(lib.lcx_set_trace_reorder(old[0].value, old[1].value), "set")
     no_kernel_errors()
+
+
+@pytest.mark.parametrize("chunk", [1 << 14, 1 << 20])
+def test_host_buffer_traces(torch_cuda, lcx, oracle_mod, chunk):
+    """lcx_trace_closest_host / lcx_trace_any_host (rays and results in host memory, chunked
+    through device staging with copies overlapped): the oracle's records bit for bit, for pinned
+    and pageable buffers, a ray count that is not a multiple of the chunk (with 2^14: 13 chunks
+    through the 4-slot staging ring), both layouts, on a side stream; the empty call is a no-op."""
+    from luisacompute_gb300 import _capi
+    lib = _capi.load()
+    scene = small_terrain()
+    rays = np.concatenate([S.terrain_rays(scene, 150_000, seed=17), S.terrain_shadow_rays(scene, 50_003, seed=18)])
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_closest(rays)
+    want_any = osc.trace_any(rays)
+    acc, _ = gpu_scene(scene)
+    _capi.check(lib.lcx_set_host_chunk(chunk), "chunk")
+    try:
+        side = torch_cuda.cuda.Stream()
+        for layout in (0, 1):
+            # pinned torch tensors
+            h_rays = torch_cuda.from_numpy(rays.view(np.float32).reshape(-1, 8)).pin_memory()
+            h_hits = torch_cuda.full((rays.shape[0], 6), -7, dtype=torch_cuda.int32).pin_memory()
+            h_occ = torch_cuda.full((rays.shape[0],), 9, dtype=torch_cuda.uint8).pin_memory()
+            acc.trace_closest_host(h_rays, h_hits, layout=layout, stream=side)
+            acc.trace_any_host(h_rays, h_occ, layout=layout, stream=side)
+            side.synchronize()
+            got = h_hits.numpy().view(want.dtype).reshape(-1)
+            assert_bit_exact(oracle_mod, osc, rays, got, want)
+            assert np.array_equal(h_occ.numpy(), want_any)
+            # pageable numpy arrays on the current stream
+            got2 = np.zeros_like(want)
+            occ2 = np.zeros(rays.shape[0], np.uint8)
+            acc.trace_closest_host(np.ascontiguousarray(rays), got2, layout=layout)
+            acc.trace_any_host(np.ascontiguousarray(rays), occ2, layout=layout)
+            torch_cuda.cuda.synchronize()
+            assert np.array_equal(got2.view(np.uint8), want.view(np.uint8))
+            assert np.array_equal(occ2, want_any)
+        empty = np.zeros(0, rays.dtype)
+        acc.trace_closest_host(empty, np.zeros(0, want.dtype))
+        with pytest.raises(ValueError):
+            acc.trace_closest_host(rays, np.zeros(10, want.dtype))
+        assert lib.lcx_trace_closest_host(acc.handle, rays.ctypes.data, 16, 0xFF, None, 1, None) \
+            == _capi.LCX_ERR_INVALID_ARG
+        assert lib.lcx_set_host_chunk(100) == _capi.LCX_ERR_INVALID_ARG
+    finally:
+        _capi.check(lib.lcx_set_host_chunk(1 << 21), "chunk")
+    no_kernel_errors()
