@@ -206,6 +206,12 @@ public:
         check(lcx_accel_device_view(accel, &v), "device_view");
         return v;
     }
+    // The accel's instances for device-side edits (include/lcx/accel_instances.cuh).
+    [[nodiscard]] LcxInstanceBuffer instance_buffer(uint64_t accel) const {
+        LcxInstanceBuffer b{};
+        check(lcx_accel_instance_buffer(accel, &b), "instance_buffer");
+        return b;
+    }
     [[nodiscard]] LcxAccelStats mesh_stats(uint64_t mesh) const {
         LcxAccelStats s{};
         check(lcx_mesh_stats(mesh, &s), "mesh_stats");

@@ -266,6 +266,21 @@ typedef struct LcxAccelView {
 } LcxAccelView;
 LCX_API int lcx_accel_device_view(uint64_t accel, LcxAccelView *out);
 
+/* The accel's instance records in device memory, for kernels that read or
+ * edit instances in place (include/lcx/accel_instances.cuh: the reference's
+ * device-side Accel::set_instance_transform / visibility / opacity / user_id
+ * and getters, src/backends/cuda/cuda_builtin/cuda_device_resource.h:1450-1512).
+ * Edits take effect at the next lcx_accel_build (PREFER_UPDATE refits an
+ * accel created with allow_update).  Valid until an lcx_accel_build grows the
+ * instance count past its capacity, or the accel is destroyed.  Fails with
+ * LCX_ERR_NOT_BUILT while the accel has no instances. */
+typedef struct LcxInstanceBuffer {
+    void *states;    /* `count` 80-byte InstState records (include/lcx/bvh_device.cuh) */
+    uint32_t count;  /* instance count of the last lcx_accel_build */
+    uint32_t _pad;
+} LcxInstanceBuffer;
+LCX_API int lcx_accel_instance_buffer(uint64_t accel, LcxInstanceBuffer *out);
+
 /* trace_closest over a batch: CPU accel.rs:449-509, CUDA
  * cuda_device_resource.h:1784-1807.  d_rays / d_hits are device arrays of
  * `ray_count` records.  An instance is eligible when (vis_mask & mask) != 0

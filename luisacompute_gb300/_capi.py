@@ -61,6 +61,10 @@ class LcxProceduralBuildCommand(ctypes.Structure):
                 ("aabb_buffer_offset", c_size_t), ("aabb_buffer_size", c_size_t)]
 
 
+class LcxInstanceBuffer(ctypes.Structure):
+    _fields_ = [("states", c_void_p), ("count", c_uint32), ("_pad", c_uint32)]
+
+
 class LcxAccelView(ctypes.Structure):
     _fields_ = [("tlas_nodes", c_void_p), ("instances", c_void_p), ("stack_need", c_uint32), ("_pad", c_uint32)]
 
@@ -98,6 +102,7 @@ _SIGS = {
     "lcx_trace_closest_host": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
     "lcx_trace_any_host": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
     "lcx_set_host_chunk": (c_int, [c_uint32]),
+    "lcx_accel_instance_buffer": (c_int, [c_uint64, POINTER(LcxInstanceBuffer)]),
     "lcx_set_refit_sync": (c_int, [c_uint32]),
     "lcx_get_trace_stack": (c_int, [POINTER(c_uint32)]),
     "lcx_get_trace_reorder": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),

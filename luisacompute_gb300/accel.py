@@ -282,6 +282,13 @@ class Accel:
               "lcx_trace_any")
         return out
 
+    def instance_buffer(self):
+        """lcx_accel_instance_buffer: the instance records for device-side edits
+        (include/lcx/accel_instances.cuh)."""
+        b = _capi.LcxInstanceBuffer()
+        check(self.lib.lcx_accel_instance_buffer(self.handle, ctypes.byref(b)), "lcx_accel_instance_buffer")
+        return b
+
     # ------------------------------------------------- host-buffer queries
     @staticmethod
     def _host_ptr(buf, rec: int, what: str):

@@ -32,7 +32,7 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblcx_accel.so")
 
 
-PUBLIC_HEADERS = ["lcx_accel.h", "lcx/bvh_device.cuh", "lcx/node_test.cuh"]
+PUBLIC_HEADERS = ["lcx_accel.h", "lcx/bvh_device.cuh", "lcx/node_test.cuh", "lcx/accel_instances.cuh"]
 
 
 def _stamp() -> str:

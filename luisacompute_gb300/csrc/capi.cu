@@ -1154,6 +1154,18 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     return released;
 }
 
+int lcx_accel_instance_buffer(uint64_t accel, LcxInstanceBuffer *out) {
+    if (!out) return fail(LCX_ERR_INVALID_ARG, "lcx_accel_instance_buffer: out is null");
+    auto a = find_accel(accel);
+    if (!a) return fail(LCX_ERR_INVALID_ARG, "unknown accel handle %llu", (unsigned long long)accel);
+    std::lock_guard<std::mutex> lk(a->mtx);
+    if (!a->d_inst || a->inst_count == 0) return fail(LCX_ERR_NOT_BUILT, "accel has no instances");
+    out->states = a->d_inst;
+    out->count = a->inst_count;
+    out->_pad = 0;
+    return LCX_OK;
+}
+
 int lcx_accel_device_view(uint64_t accel, LcxAccelView *out) {
     if (!out) return fail(LCX_ERR_INVALID_ARG, "lcx_accel_device_view: out is null");
     auto a = find_accel(accel);
