@@ -446,11 +446,15 @@ LCX_API int lcx_get_build_morton(uint32_t *blas_cube, uint32_t *tlas_cube, uint3
 
 /* Traversal knobs, process-wide (no counterpart in the reference: OptiX and
  * Embree pick theirs internally).  refill: a warp takes new rays once at
- * least this many of its 32 lanes are idle (1..32, default 4).  postpone: a
- * lane defers its triangle tests while fewer than this many lanes would run
- * them (0 = never, the default).  mode: loop structure, 0 = each step visits
- * one node and tests its triangles (default), 1 = speculative while-while.
- * Results do not depend on any of them. */
+ * least this many of its 32 lanes are idle (1..32, default 4).  mode: loop
+ * structure -- 2 (default) = deferred triangle batches: each warp queues the
+ * triangles its lanes find and tests them 32 at a time (quantised-node,
+ * single-job, non-counting calls; the others run mode 0); 0 = each step
+ * visits one node and tests its triangles; 1 = speculative while-while.
+ * postpone: in mode 2, the queue size that starts a batch (1..32; 0 = 24 for
+ * closest, 16 for any hit); in modes 0 and 1, a lane defers its triangle tests
+ * while fewer than this many lanes would run them (0 = never).  Results do
+ * not depend on any of them. */
 LCX_API int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone, uint32_t mode);
 LCX_API int lcx_get_trace_tuning(uint32_t *refill, uint32_t *postpone, uint32_t *mode);
 /* Ray reordering for later lcx_trace_closest / lcx_trace_any calls (and their

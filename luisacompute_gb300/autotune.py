@@ -10,7 +10,9 @@ It measures, on the caller's own scene and rays, and picks:
 * traversal knobs (``lcx_set_trace_tuning`` / ``lcx_set_trace_stack`` / ``lcx_set_trace_reorder``):
   - ray-pool refill threshold: the number of idle lanes at which a warp takes new rays, 1..32;
   - shared-memory stack depth: 8, 16 or 24 entries per thread;
-  - loop structure: 0 (node + its items per step) or 1 (speculative while-while);
+  - loop structure: 2 (deferred triangle batches, the default), 0 (node + its items per step) or
+    1 (speculative while-while);
+  - mode 2's flush size (``postpone``): 0 (24 closest / 16 any), 12 or 32 queued tests;
   - ray reordering: off, or sorted by octant and 7-bit origin Morton cell.
 
 Search: coordinate descent, build knobs first (each trial builds every mesh with one batched
@@ -38,7 +40,8 @@ from . import _capi
 from .accel import NODES_QUANT8, Accel, build_meshes, mesh_from_data
 
 BUILD_SPACE = {"leaf_max": [1, 2, 3], "width": [8, 6, 4], "blas_cube": [1, 0]}
-TRACE_SPACE = {"refill": [1, 2, 4, 8, 16, 32], "short_stack": [8, 16, 24], "mode": [0, 1], "reorder_bits": [0, 7]}
+TRACE_SPACE = {"refill": [1, 2, 4, 8, 16, 32], "short_stack": [8, 16, 24], "mode": [2, 0, 1], "postpone": [0, 12, 32],
+               "reorder_bits": [0, 7]}
 
 
 @dataclass
@@ -48,8 +51,9 @@ class Config:
     blas_cube: int = 1
     refill: int = 4
     short_stack: int = 16
-    mode: int = 0
+    mode: int = 2
     reorder_bits: int = 0
+    postpone: int = 0
 
 
 @dataclass
@@ -83,7 +87,7 @@ def current() -> Config:
     _capi.check(lib.lcx_get_trace_stack(ss), "lcx_get_trace_stack")
     rb, rm = _u32(2)
     _capi.check(lib.lcx_get_trace_reorder(rb, rm), "lcx_get_trace_reorder")
-    return Config(lm.value, w.value, bc.value, rf.value, ss.value, md.value, rb.value)
+    return Config(lm.value, w.value, bc.value, rf.value, ss.value, md.value, rb.value, pp.value)
 
 
 def apply(cfg: Config):
@@ -91,13 +95,11 @@ def apply(cfg: Config):
     lib = _capi.load()
     bc, tc, sb = _u32(3)
     _capi.check(lib.lcx_get_build_morton(bc, tc, sb), "lcx_get_build_morton")
-    rf, pp, md = _u32(3)
-    _capi.check(lib.lcx_get_trace_tuning(rf, pp, md), "lcx_get_trace_tuning")
     rb, rm = _u32(2)
     _capi.check(lib.lcx_get_trace_reorder(rb, rm), "lcx_get_trace_reorder")
     _capi.check(lib.lcx_set_build_tuning(cfg.leaf_max, cfg.width), "lcx_set_build_tuning")
     _capi.check(lib.lcx_set_build_morton(cfg.blas_cube, tc.value, sb.value), "lcx_set_build_morton")
-    _capi.check(lib.lcx_set_trace_tuning(cfg.refill, pp.value, cfg.mode), "lcx_set_trace_tuning")
+    _capi.check(lib.lcx_set_trace_tuning(cfg.refill, cfg.postpone, cfg.mode), "lcx_set_trace_tuning")
     _capi.check(lib.lcx_set_trace_stack(cfg.short_stack), "lcx_set_trace_stack")
     _capi.check(lib.lcx_set_trace_reorder(cfg.reorder_bits, rm.value), "lcx_set_trace_reorder")
 

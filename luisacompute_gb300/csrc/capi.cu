@@ -573,8 +573,8 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
 // Traversal knobs (see lcx_set_trace_tuning).
 struct TraceTuning {
     uint32_t refill = 4;    // measured best on the terrain workload (refill sweep 1..32)
-    uint32_t postpone = 0;  // postponing did not pay on GB300 (sweep 0..12)
-    uint32_t mode = 0;      // traversal loop structure
+    uint32_t postpone = 0;  // modes 0 / 1: postponing did not pay (sweep 0..24); mode 2: 0 = per-kind flush size
+    uint32_t mode = 2;      // traversal loop structure: deferred triangle batches (quantised nodes; FP32 runs mode 0)
     uint32_t short_stack = 16;  // shared-memory stack entries per thread (8, 16, 24)
 };
 TraceTuning g_tune;
@@ -1274,8 +1274,8 @@ int lcx_check_trace_errors(void) {
 }
 
 int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone, uint32_t mode) {
-    if (refill < 1 || refill > 32 || postpone > 32 || mode > 1)
-        return fail(LCX_ERR_INVALID_ARG, "tuning out of range (refill 1..32, postpone 0..32, mode 0..1)");
+    if (refill < 1 || refill > 32 || postpone > 32 || mode > 2)
+        return fail(LCX_ERR_INVALID_ARG, "tuning out of range (refill 1..32, postpone 0..32, mode 0..2)");
     g_tune.refill = refill;
     g_tune.postpone = postpone;
     g_tune.mode = mode;

@@ -528,6 +528,320 @@ __global__ void __launch_bounds__(kTraceBlock,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Loop mode 2: deferred triangle batches.
+//
+// In modes 0 and 1 a lane tests the triangles of a visited node at once.  A
+// ray meets about 2 triangles in about 19 steps, so those tests run with a
+// couple of the warp's lanes active, and on the incoherent terrain workload
+// they take about half of the kernel's time (measured by running every
+// triangle test twice: 4.73 -> 6.98 ms; every node test twice: 4.73 -> 4.76).
+// Here a lane only queues its triangles: each warp keeps a shared-memory queue
+// of (triangle record, ray record) entries and tests them one per lane, 32 at
+// a time, once P.postpone of them have gathered (default 32), when the queue
+// is full, when a finished ray has no place to wait for its entries, or when
+// the warp runs out of rays.
+//
+// Ray records: each lane has two in shared memory -- its ray in the object
+// space of an instance (the watertight-test setup), tmin and the instance id
+// -- written when the lane enters an instance, alternating, so that entries of
+// the previous instance stay valid.  Entering an instance whose record still
+// has queued entries flushes the queue first.
+// A ray whose walk ends with entries queued retires into the lane's retire
+// slot (its best hit so far) and the lane takes a new ray; the retired ray's
+// record is written after the next flush.  A lane whose retire slot is taken
+// waits for that flush.
+// Results: per ray record, the minimum (ordered t, prim) by a 64-bit
+// atomicMin and the barycentrics of that minimum.  The owner merges each
+// record's minimum into its ray's best with the closest-hit rule, so the
+// result does not depend on the order of the tests.  Entries are tested
+// against the ray's best t at the flush, never below the best t an immediate
+// test would have used, so every triangle that can hold or tie the closest
+// hit is still tested: the records equal modes 0 and 1 bit for bit (any hit:
+// the same flags).  Single-job closest / any launches with quantised nodes and
+// without counting; 1.77 -> 1.90 Grays/s on the terrain workload (visits per
+// ray 16.95 -> 17.76 nodes, 2.17 -> 2.42 triangle tests: the lagging best t
+// culls less; 31.7 tests per flush on average).
+#ifndef LCX_DEFER_CAP
+#define LCX_DEFER_CAP 64
+#endif
+#ifndef LCX_DEFER_MIN_BLOCKS
+#define LCX_DEFER_MIN_BLOCKS 7
+#endif
+#ifndef LCX_DEFER_STACK
+#define LCX_DEFER_STACK 8
+#endif
+constexpr int kDeferCap = LCX_DEFER_CAP;  // queued triangle tests per warp
+
+struct DeferQueue {
+    const TriRec *tri[kDeferCap];
+    uint32_t rec[kDeferCap];       // ray record: lane | slot << 5
+    float rr[9][64];               // per record: ox oy oz Sx Sy Sz perm tmin inst (perm, inst as bits)
+    unsigned long long key[64];    // per record: min (ordered t << 32 | prim)
+    float2 uv[64];                 // per record: barycentrics of that minimum
+    float tmax[64];                // per record: the owner's best t at the flush
+    float ret_t[32], ret_u[32], ret_v[32];
+    uint32_t ret_inst[32], ret_prim[32], ret_rid[32];
+};
+
+template <int kLayout, bool kAny, int kShort>
+__global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_deferred(TraceParams P) {
+    using W_t = Walker<kLayout, kAny, false, false, kShort>;
+    __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
+    __shared__ DeferQueue queues[kTraceBlock / 32];
+    uint2 deep_stack[W_t::kDeepSlots];
+    const uint32_t lane = threadIdx.x & 31u;
+    DeferQueue &Q = queues[threadIdx.x >> 5];
+    W_t W(P, stack_mem + threadIdx.x, deep_stack);
+    const int refill = int(P.refill);
+    // queue size that starts a flush: P.postpone, or 24 for closest / 16 for any hit (measured on the
+    // terrain workload: closest 1.860 / 1.896 / 1.886 / 1.869 Grays/s at 32 / 24 / 16 / 12; any hit
+    // 3.10 / 3.20 / 3.25 / 3.26)
+    const uint32_t flush_at = P.postpone >= 1 && P.postpone <= uint32_t(kDeferCap) ? P.postpone : (kAny ? 16u : 24u);
+
+    bool active = false, exhausted = false;
+    uint32_t rid = 0, ray_steps = 0;
+    uint32_t qn = 0;        // queued entries (warp-uniform)
+    uint32_t pend = 0;      // bit s: a queued entry uses this lane's record s
+    uint32_t mine = 0;      // bit s: record s belongs to the lane's current ray (else to the retired one)
+    uint32_t cur = 1;       // record of the current instance
+    bool retired = false;   // the retire slot holds a ray waiting for queued results
+    bool ret_occ = false;
+
+    // Test every queued entry (all lanes call it together), merge the results
+    // into their rays and write out the retired rays.
+    auto flush = [&]() {
+#pragma unroll
+        for (uint32_t s = 0; s < 2; s++) {
+            if ((pend >> s) & 1u) {
+                const uint32_t r = lane + 32u * s;
+                Q.tmax[r] = ((mine >> s) & 1u) ? W.best_t : Q.ret_t[lane];
+                Q.key[r] = ~0ull;
+            }
+        }
+        __syncwarp();
+        for (uint32_t base = 0; base < qn; base += 32u) {
+            const uint32_t j = base + lane;
+            bool hit = false;
+            unsigned long long key = ~0ull;
+            uint32_t r = 0;
+            float t = 0.0f, u = 0.0f, v = 0.0f;
+            if (j < qn) {
+                r = Q.rec[j];
+                WtRay ray;
+                ray.ox = Q.rr[0][r];
+                ray.oy = Q.rr[1][r];
+                ray.oz = Q.rr[2][r];
+                ray.Sx = Q.rr[3][r];
+                ray.Sy = Q.rr[4][r];
+                ray.Sz = Q.rr[5][r];
+                ray.perm = __float_as_uint(Q.rr[6][r]);
+                const float lo = Q.rr[7][r], hi = Q.tmax[r];
+                const float4 *tp = reinterpret_cast<const float4 *>(Q.tri[j]);
+                const float4 a = bvh_ld(tp), b = bvh_ld(tp + 1), c = bvh_ld(tp + 2);
+                if (wt_intersect(ray, lo, hi, a, b, c, t, u, v)) {
+                    hit = true;
+                    key = kAny ? 0ull
+                               : (static_cast<unsigned long long>(float_to_ordered(t)) << 32) | __float_as_uint(a.w);
+                    atomicMin(&Q.key[r], key);
+                }
+            }
+            if (!kAny) {
+                __syncwarp();
+                if (hit && key == Q.key[r]) Q.uv[r] = make_float2(u, v);
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (uint32_t s = 0; s < 2; s++) {
+            if (!((pend >> s) & 1u)) continue;
+            const uint32_t r = lane + 32u * s;
+            const unsigned long long k = Q.key[r];
+            if (k == ~0ull) continue;
+            const bool cur_ray = (mine >> s) & 1u;
+            if (kAny) {
+                if (cur_ray)
+                    W.occluded = true;
+                else
+                    ret_occ = true;
+                continue;
+            }
+            const float t = ordered_to_float(uint32_t(k >> 32));
+            const uint32_t prim = uint32_t(k);
+            const uint32_t inst = __float_as_uint(Q.rr[8][r]);
+            const float2 uv = Q.uv[r];
+            // lexicographic (t, inst, prim): the other record's minimum may already
+            // have lowered the best t of this flush
+            if (cur_ray) {
+                if (t < W.best_t || (t == W.best_t && (inst < W.best_inst || (inst == W.best_inst && prim < W.best_prim)))) {
+                    W.best_t = t;
+                    W.best_u = uv.x;
+                    W.best_v = uv.y;
+                    W.best_inst = inst;
+                    W.best_prim = prim;
+                }
+            } else {
+                const float bt = Q.ret_t[lane];
+                const uint32_t bi = Q.ret_inst[lane], bp = Q.ret_prim[lane];
+                if (t < bt || (t == bt && (inst < bi || (inst == bi && prim < bp)))) {
+                    Q.ret_t[lane] = t;
+                    Q.ret_u[lane] = uv.x;
+                    Q.ret_v[lane] = uv.y;
+                    Q.ret_inst[lane] = inst;
+                    Q.ret_prim[lane] = prim;
+                }
+            }
+        }
+        if (retired) {  // its last queued tests are done
+            const uint32_t ro = Q.ret_rid[lane];
+            if (kAny) {
+                P.occluded[ro] = ret_occ ? 1 : 0;
+            } else {
+                uint2 *hp = reinterpret_cast<uint2 *>(P.hits + ro);
+                __stcs(hp, make_uint2(Q.ret_inst[lane], Q.ret_prim[lane]));
+                __stcs(hp + 1, make_uint2(__float_as_uint(Q.ret_u[lane]), __float_as_uint(Q.ret_v[lane])));
+                __stcs(hp + 2, make_uint2(__float_as_uint(Q.ret_t[lane]), 0u));
+            }
+            retired = false;
+        }
+        pend = 0;
+        qn = 0;
+        __syncwarp();
+    };
+
+    for (;;) {
+        // refill: idle lanes take new rays once enough of them are idle
+        const uint32_t idle = __ballot_sync(~0u, !active);
+        const int n_idle = __popc(idle);
+        if (!exhausted && n_idle >= refill) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(P.pool, uint32_t(n_idle));
+            base = __shfl_sync(~0u, base, 0);
+            if (uint64_t(base) + uint64_t(n_idle) >= P.ray_count) exhausted = true;
+            if (!active) {
+                const uint32_t my = base + __popc(idle & ((1u << lane) - 1u));
+                if (my < P.ray_count) {
+                    rid = my;
+                    active = true;
+                    ray_steps = 0;
+                    mine = 0;
+                    W.start(rid);
+                }
+            }
+        }
+        if (__ballot_sync(~0u, active) == 0u) {
+            if (qn != 0u || __any_sync(~0u, retired)) flush();
+            if (exhausted) break;
+            continue;
+        }
+
+        // 1. visit a node (or take a popped item group)
+        uint2 Gt = make_uint2(0, 0);
+        if (active) {
+            if (kAny && W.occluded) {  // a flush found a hit: end the walk
+                W.G = make_uint2(0, 0);
+                W.sp = 0;
+                W.blas_sp = 0;
+            } else if (++ray_steps > kMaxRaySteps) {
+                atomicOr(P.pool + 1, 2u);
+                W.G = make_uint2(0, 0);
+                W.sp = 0;
+                W.blas_sp = 0;
+            } else if (W.G.y >= 0x01000000u) {
+                W.visit(Gt);
+            } else {
+                Gt = W.G;
+                W.G = make_uint2(0, 0);
+            }
+        }
+
+        // 2. queue the triangles found inside a BLAS (warp-wide prefix over the lanes' counts)
+        const bool has_tris = active && W.in_blas && Gt.y != 0u;
+        if (__any_sync(~0u, has_tris)) {
+            uint32_t bits = has_tris ? Gt.y : 0u;
+            const TriRec *tbase = has_tris ? W.blas_tris + Gt.x : nullptr;
+            for (;;) {
+                const uint32_t cnt = __popc(bits);
+                uint32_t incl = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t x = __shfl_up_sync(~0u, incl, o);
+                    if (lane >= uint32_t(o)) incl += x;
+                }
+                const uint32_t total = __shfl_sync(~0u, incl, 31);
+                if (total == 0u) break;
+                const uint32_t space = uint32_t(kDeferCap) - qn;
+                uint32_t pos = qn + incl - cnt;
+                while (bits != 0u && pos < uint32_t(kDeferCap)) {
+                    const uint32_t k = __ffs(bits) - 1u;
+                    bits &= bits - 1u;
+                    Q.tri[pos] = tbase + k;
+                    Q.rec[pos] = lane | (cur << 5);
+                    pend |= 1u << cur;
+                    pos++;
+                }
+                if (total <= space) {
+                    qn += total;
+                    break;
+                }
+                qn = uint32_t(kDeferCap);
+                flush();
+            }
+        }
+
+        // 3. enter instances (TLAS items); the record to be written must be free
+        const bool enter = active && !W.in_blas && Gt.y != 0u;
+        if (__any_sync(~0u, enter && ((pend >> (cur ^ 1u)) & 1u))) flush();
+        if (enter) {
+            W.instances(Gt);
+            if (W.in_blas) {
+                cur ^= 1u;
+                const uint32_t r = lane + 32u * cur;
+                Q.rr[0][r] = W.wt.ox;
+                Q.rr[1][r] = W.wt.oy;
+                Q.rr[2][r] = W.wt.oz;
+                Q.rr[3][r] = W.wt.Sx;
+                Q.rr[4][r] = W.wt.Sy;
+                Q.rr[5][r] = W.wt.Sz;
+                Q.rr[6][r] = __uint_as_float(W.wt.perm);
+                Q.rr[7][r] = W.tmin;
+                Q.rr[8][r] = __uint_as_float(W.cur_inst);
+                mine |= 1u << cur;
+            }
+        }
+
+        // 4. pop; a finished ray with queued tests retires (or waits while the retire slot is taken)
+        bool blocked = false;
+        if (active && W.G.y == 0u) {
+            if (W.pop_or_done()) {
+                if (pend & mine) {
+                    if (retired) {
+                        blocked = true;
+                    } else {
+                        Q.ret_t[lane] = W.best_t;
+                        Q.ret_u[lane] = W.best_u;
+                        Q.ret_v[lane] = W.best_v;
+                        Q.ret_inst[lane] = W.best_inst;
+                        Q.ret_prim[lane] = W.best_prim;
+                        Q.ret_rid[lane] = W.slot;
+                        ret_occ = W.occluded;
+                        retired = true;
+                        mine = 0;
+                        active = false;
+                    }
+                } else {
+                    W.finish();
+                    mine = 0;
+                    active = false;
+                }
+            }
+        }
+
+        // 5. test the queue once it is full enough, or a finished ray is waiting on it
+        if (qn >= flush_at || __any_sync(~0u, blocked)) flush();
+    }
+}
+
 template <int L, bool A, bool C, int M, bool X, int S>
 int blocks_per_sm() {
     static int v = 0;
@@ -569,6 +883,23 @@ cudaError_t launch_stack(const TraceParams &p, cudaStream_t st) {
     return launch_one<L, A, false, 0, false, kDefaultShortStack>(p, st);
 }
 
+template <int L, bool A, int S>
+cudaError_t launch_deferred(const TraceParams &p, cudaStream_t st) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_deferred<L, A, S>, kTraceBlock, 0);
+        per_sm = b > 0 ? b : 1;
+    }
+    const uint64_t warps_needed = (uint64_t(p.ray_count) + 31) / 32;
+    uint64_t grid = uint64_t(sm_count()) * uint64_t(per_sm);
+    const uint64_t grid_need = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
+    if (grid_need < grid) grid = grid_need;
+    if (grid == 0) grid = 1;
+    k_trace_deferred<L, A, S><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
 template <int M>
 cudaError_t launch_mode(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
     if (layout == LCX_NODES_QUANT8) {
@@ -593,6 +924,12 @@ cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counti
         return any ? launch_one<LCX_NODES_FP32, true, false, 0, true>(p, st)
                    : launch_one<LCX_NODES_FP32, false, false, 0, true>(p, st);
     }
+    // deferred triangle batches: single-job quantised-node launches without counting (with FP32
+    // nodes mode 2 measured slower than mode 0, 1.06-1.10 vs 1.62 Grays/s, so those run mode 0)
+    if (p.mode == 2 && !counting && layout == LCX_NODES_QUANT8)
+        return any ? launch_deferred<LCX_NODES_QUANT8, true, LCX_DEFER_STACK>(p, st)
+                   : launch_deferred<LCX_NODES_QUANT8, false, LCX_DEFER_STACK>(p, st);
+    if (p.mode == 2) return launch_mode<0>(p, layout, any, counting, st);
     return p.mode == 1 ? launch_mode<1>(p, layout, any, counting, st) : launch_mode<0>(p, layout, any, counting, st);
 }
 

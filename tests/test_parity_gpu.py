@@ -295,7 +295,8 @@ def test_axis_aligned_exact_ties(torch_cuda, lcx, oracle_mod, layout):
 
 
 @pytest.mark.parametrize("refill,postpone,mode", [(1, 0, 0), (8, 8, 0), (16, 12, 0), (32, 32, 0), (4, 20, 0),
-                                                  (4, 0, 1), (16, 0, 1), (1, 8, 1)])
+                                                  (4, 0, 1), (16, 0, 1), (1, 8, 1),
+                                                  (4, 0, 2), (1, 1, 2), (8, 16, 2), (32, 32, 2), (2, 5, 2)])
 def test_tuning_does_not_change_results(torch_cuda, lcx, oracle_mod, refill, postpone, mode):
     import ctypes
     from luisacompute_gb300 import _capi
