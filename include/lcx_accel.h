@@ -433,7 +433,7 @@ LCX_API int lcx_set_refit_sync(uint32_t sync);
 
 /* Build knobs, process-wide, for builds that start after the call (no
  * counterpart in the reference).  leaf_max: triangles per leaf slot, 1..3, or
- * 0 to follow AccelOption.hint (FAST_TRACE 1, FAST_BUILD 3); width: children
+ * 0 to follow AccelOption.hint (FAST_TRACE 2, FAST_BUILD 3); width: children
  * per wide node, 2..8 (default 8).  Results of queries do not depend on them. */
 LCX_API int lcx_set_build_tuning(uint32_t leaf_max, uint32_t width);
 LCX_API int lcx_get_build_tuning(uint32_t *leaf_max, uint32_t *width);

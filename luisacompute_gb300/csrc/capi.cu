@@ -294,7 +294,10 @@ int check_option(const LcxAccelOption *o) {
 // Triangles per leaf slot by hint.  Measured on GB300 (terrain workload, 8.4M
 // incoherent rays, quantised nodes): 1 -> 1.66, 2 -> 1.58, 3 -> 1.49 Grays/s,
 // with 741k / 343k / 306k wide nodes; FAST_BUILD takes the smallest tree.
-int leaf_items_for(const LcxAccelOption &o) { return o.hint == LCX_HINT_FAST_BUILD ? 3 : 1; }
+// Items per leaf slot by hint.  FAST_TRACE 2: with the deferred triangle batches
+// (traversal mode 2) two per leaf traced fastest on the terrain workload
+// (closest 1.895 / 1.955 / 1.933 Grays/s at 1 / 2 / 3; any hit 3.26 / 3.37 / 3.36).
+int leaf_items_for(const LcxAccelOption &o) { return o.hint == LCX_HINT_FAST_BUILD ? 3 : 2; }
 
 // Build knobs (see lcx_set_build_tuning); 0 = derive from the AccelOption hint.
 struct BuildTuning {
