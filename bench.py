@@ -533,6 +533,13 @@ def main():
     del counts
     node_bytes = 80 if args.layout == 1 else 208
     bytes_per_ray = 32 + 24 + c[0] * node_bytes + c[1] * 48 + c[2] * 80
+    import ctypes
+    from luisacompute_gb300 import _capi
+    knobs = [ctypes.c_uint32(0) for _ in range(3)]
+    _capi.check(_capi.load().lcx_get_trace_tuning(*knobs), "lcx_get_trace_tuning")
+    deferred = knobs[2].value == 2 and args.layout == 1  # loop mode 2 runs quantised-node calls
+    kernel_name = ("k_trace_deferred<quant8, closest> (loop mode 2)" if deferred else
+                   f"k_trace<{'quant8' if args.layout == 1 else 'fp32'}, closest> (loop mode {knobs[2].value})")
 
     for _ in range(max(3, args.warmup)):
         acc.trace_closest(d_rays, out=d_hits, layout=args.layout)
@@ -612,7 +619,8 @@ def main():
                          "traffic": None if traffic_pr is None else traffic_pr * n,
                          "algorithmic_bytes_per_ray": bytes_per_ray,
                          "visits_per_ray": {"nodes": c[0], "triangles": c[1], "instances": c[2]},
-                         "kernel": "k_trace<quant8, closest>" if args.layout == 1 else "k_trace<fp32, closest>"},
+                         "kernel": kernel_name,
+                         "visits_from": "the counting pass (loop mode 0); mode 2 visits ~5 % more nodes"},
             "clocks": clocks.summary(),
             "gpu_launches": args.steps}
     if tuned is not None:

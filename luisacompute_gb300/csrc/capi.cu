@@ -110,9 +110,14 @@ struct DevBlock {
 };
 
 // BVH lifetime.  Trace calls hold g_life_mtx shared from the accel lookup
-// until their kernel is enqueued; releasing BVH memory (destroy, rebuild) holds
-// it exclusively, so the implicit device synchronisation of cudaFree covers
-// every kernel that read the old pointers, whichever thread launched it.  The
+// until their kernel is enqueued.  Releasing BVH memory (destroy, rebuild)
+// takes it exclusively once, as a barrier: a destroy unregisters the object
+// under it (no later trace can find it), a rebuild's replaced blocks are
+// already unreachable; once the lock has been held, every trace that read the
+// old pointers has enqueued its kernel, whichever thread launched it.  The
+// device synchronisation that waits for those kernels and the frees then run
+// outside the lock, so traces on other objects are not held up while the
+// device drains (a serving loop evicting scenes keeps dispatching).  The
 // exclusive lock is never requested while a mesh or accel mutex is held (a
 // build hands its replaced blocks to a Retired declared before its mutex
 // guard), so a trace holding the shared lock and waiting for such a mutex
@@ -123,7 +128,11 @@ struct Retired {
     std::vector<std::shared_ptr<DevBlock>> blocks;
     ~Retired() {
         if (blocks.empty()) return;
-        std::unique_lock<std::shared_mutex> lk(g_life_mtx);
+        // a barrier, not a critical section: once the exclusive lock has been held, every
+        // trace that looked up these blocks has enqueued its kernel; the wait for those
+        // kernels and the frees happen outside it, so traces on other objects go on
+        { std::unique_lock<std::shared_mutex> lk(g_life_mtx); }
+        cudaDeviceSynchronize();
         blocks.clear();
     }
 };
@@ -673,19 +682,22 @@ int lcx_mesh_create(const LcxAccelOption *option, uint64_t *out_handle) {
 }
 
 int lcx_mesh_destroy(uint64_t mesh) {
-    std::unique_lock<std::shared_mutex> life(g_life_mtx);
     std::shared_ptr<MeshObj> m;
     {
+        // under the exclusive lifetime lock: every trace that found this mesh has enqueued
+        // its kernel, and no later one can find it (or an accel still referencing it)
+        std::unique_lock<std::shared_mutex> life(g_life_mtx);
         std::lock_guard<std::mutex> lk(g_reg_mtx);
         auto it = g_meshes.find(mesh);
         if (it == g_meshes.end()) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_destroy: unknown mesh handle %llu",
                                               (unsigned long long)mesh);
         m = it->second;
         g_meshes.erase(it);
+        bump_mesh_epoch();
     }
-    bump_mesh_epoch();
+    // outside it: traces on other objects go on while queued work that may read this BVH drains
     std::lock_guard<std::mutex> lk(m->mtx);
-    cudaDeviceSynchronize();  // the BVH may be in use by queued work
+    cudaDeviceSynchronize();
     m->block.reset();
     if (m->d_desc) cudaFree(m->d_desc);
     m->d_desc = nullptr;
@@ -814,9 +826,10 @@ int lcx_accel_create(const LcxAccelOption *option, uint64_t *out_handle) {
 }
 
 int lcx_accel_destroy(uint64_t accel) {
-    std::unique_lock<std::shared_mutex> life(g_life_mtx);
     std::shared_ptr<AccelObj> a;
     {
+        // as lcx_mesh_destroy: the exclusive lock only orders this after traces that found the accel
+        std::unique_lock<std::shared_mutex> life(g_life_mtx);
         std::lock_guard<std::mutex> lk(g_reg_mtx);
         auto it = g_accels.find(accel);
         if (it == g_accels.end()) return fail(LCX_ERR_INVALID_ARG, "lcx_accel_destroy: unknown accel handle %llu",
@@ -1241,9 +1254,9 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
         p.pool = ds->pool + 4 * trace_slot(ds, st);
         p.ray_count = uint32_t(totals[g]);
         p.refill = g_tune.refill;
-        p.postpone = 0;
+        p.mode = g_tune.mode == 2 ? 2u : 0u;  // multi-job kernels: mode 2 (quantised nodes) or 0
+        p.postpone = p.mode == 2 ? g_tune.postpone : 0u;
         p.postpone_sp = kStackSize - int(depth_need);
-        p.mode = 0;
         p.jobs = d_jobs;
         p.job_count = uint32_t(groups[g].size());
         LCX_CUDA(cudaMemsetAsync(p.pool, 0, 4 * sizeof(uint32_t), st), "trace counter reset");

@@ -558,8 +558,8 @@ __global__ void __launch_bounds__(kTraceBlock,
 // against the ray's best t at the flush, never below the best t an immediate
 // test would have used, so every triangle that can hold or tie the closest
 // hit is still tested: the records equal modes 0 and 1 bit for bit (any hit:
-// the same flags).  Single-job closest / any launches with quantised nodes and
-// without counting; 1.77 -> 1.90 Grays/s on the terrain workload (visits per
+// the same flags).  Closest / any launches (single or multi-job) with quantised
+// nodes and without counting; 1.77 -> 1.90 Grays/s on the terrain workload (visits per
 // ray 16.95 -> 17.76 nodes, 2.17 -> 2.42 triangle tests: the lagging best t
 // culls less; 31.7 tests per flush on average).
 #ifndef LCX_DEFER_CAP
@@ -582,11 +582,12 @@ struct DeferQueue {
     float tmax[64];                // per record: the owner's best t at the flush
     float ret_t[32], ret_u[32], ret_v[32];
     uint32_t ret_inst[32], ret_prim[32], ret_rid[32];
+    void *ret_out[32];             // multi-job launches: the retired ray's output buffer
 };
 
-template <int kLayout, bool kAny, int kShort>
+template <int kLayout, bool kAny, int kShort, bool kMulti>
 __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_deferred(TraceParams P) {
-    using W_t = Walker<kLayout, kAny, false, false, kShort>;
+    using W_t = Walker<kLayout, kAny, false, kMulti, kShort>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
     __shared__ DeferQueue queues[kTraceBlock / 32];
     uint2 deep_stack[W_t::kDeepSlots];
@@ -695,9 +696,9 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
         if (retired) {  // its last queued tests are done
             const uint32_t ro = Q.ret_rid[lane];
             if (kAny) {
-                P.occluded[ro] = ret_occ ? 1 : 0;
+                (kMulti ? static_cast<uint8_t *>(Q.ret_out[lane]) : P.occluded)[ro] = ret_occ ? 1 : 0;
             } else {
-                uint2 *hp = reinterpret_cast<uint2 *>(P.hits + ro);
+                uint2 *hp = reinterpret_cast<uint2 *>((kMulti ? static_cast<Hit *>(Q.ret_out[lane]) : P.hits) + ro);
                 __stcs(hp, make_uint2(Q.ret_inst[lane], Q.ret_prim[lane]));
                 __stcs(hp + 1, make_uint2(__float_as_uint(Q.ret_u[lane]), __float_as_uint(Q.ret_v[lane])));
                 __stcs(hp + 2, make_uint2(__float_as_uint(Q.ret_t[lane]), 0u));
@@ -824,6 +825,7 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
                         Q.ret_inst[lane] = W.best_inst;
                         Q.ret_prim[lane] = W.best_prim;
                         Q.ret_rid[lane] = W.slot;
+                        if (kMulti) Q.ret_out[lane] = W.out;
                         ret_occ = W.occluded;
                         retired = true;
                         mine = 0;
@@ -883,12 +885,12 @@ cudaError_t launch_stack(const TraceParams &p, cudaStream_t st) {
     return launch_one<L, A, false, 0, false, kDefaultShortStack>(p, st);
 }
 
-template <int L, bool A, int S>
+template <int L, bool A, int S, bool X = false>
 cudaError_t launch_deferred(const TraceParams &p, cudaStream_t st) {
     static int per_sm = 0;
     if (per_sm == 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_deferred<L, A, S>, kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_deferred<L, A, S, X>, kTraceBlock, 0);
         per_sm = b > 0 ? b : 1;
     }
     const uint64_t warps_needed = (uint64_t(p.ray_count) + 31) / 32;
@@ -896,7 +898,7 @@ cudaError_t launch_deferred(const TraceParams &p, cudaStream_t st) {
     const uint64_t grid_need = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
     if (grid_need < grid) grid = grid_need;
     if (grid == 0) grid = 1;
-    k_trace_deferred<L, A, S><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
+    k_trace_deferred<L, A, S, X><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -917,7 +919,10 @@ cudaError_t launch_mode(const TraceParams &p, int layout, bool any, bool countin
 }  // namespace
 
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
-    if (p.jobs != nullptr) {  // multi-job launches: loop mode 0, no counting
+    if (p.jobs != nullptr) {  // multi-job launches: no counting; mode 2 with quantised nodes, else mode 0
+        if (p.mode == 2 && layout == LCX_NODES_QUANT8)
+            return any ? launch_deferred<LCX_NODES_QUANT8, true, LCX_DEFER_STACK, true>(p, st)
+                       : launch_deferred<LCX_NODES_QUANT8, false, LCX_DEFER_STACK, true>(p, st);
         if (layout == LCX_NODES_QUANT8)
             return any ? launch_one<LCX_NODES_QUANT8, true, false, 0, true>(p, st)
                        : launch_one<LCX_NODES_QUANT8, false, false, 0, true>(p, st);

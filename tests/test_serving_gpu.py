@@ -62,14 +62,32 @@ def test_trace_jobs_equals_single_calls(lcx):
         outs.append(o)
         jobs[i] = _capi.LcxTraceJob(accs[i % 3][0].handle, d.data_ptr(), o.data_ptr(), d.shape[0], 0xFF,
                                     1 if anyhit else 0, 0)
-    for layout in (0, 1):
-        _capi.check(lib.lcx_trace_jobs(jobs, len(ray_sets), layout, None), "lcx_trace_jobs")
-        torch.cuda.synchronize()
-        for i, d in enumerate(d_rays):
-            acc = accs[i % 3][0]
-            if i % 2 == 1:
-                assert torch.equal(outs[i], acc.trace_any(d, layout=layout))
-            else:
-                assert np.array_equal(hits_to_numpy(outs[i].view(-1, 6)).view(np.uint8),
-                                      hits_to_numpy(acc.trace_closest(d, layout=layout)).view(np.uint8))
+    import ctypes
+    old = [ctypes.c_uint32(0) for _ in range(3)]
+    _capi.check(lib.lcx_get_trace_tuning(*old), "get")
+    try:
+        # single calls in loop mode 0 are the reference; the multi-job launch runs in mode 2
+        # (deferred triangle batches, the default for quantised nodes) and in mode 0
+        _capi.check(lib.lcx_set_trace_tuning(old[0].value, 0, 0), "mode 0")
+        want = {}
+        for layout in (0, 1):
+            for i, d in enumerate(d_rays):
+                acc = accs[i % 3][0]
+                want[layout, i] = (acc.trace_any(d, layout=layout).cpu() if i % 2 == 1 else
+                                   hits_to_numpy(acc.trace_closest(d, layout=layout)).view(np.uint8))
+        for mode, post in ((2, 0), (2, 3), (0, 0)):
+            _capi.check(lib.lcx_set_trace_tuning(old[0].value, post, mode), "mode")
+            for layout in (0, 1):
+                for o in outs:
+                    o.zero_()
+                _capi.check(lib.lcx_trace_jobs(jobs, len(ray_sets), layout, None), "lcx_trace_jobs")
+                torch.cuda.synchronize()
+                for i, d in enumerate(d_rays):
+                    if i % 2 == 1:
+                        assert torch.equal(outs[i].cpu(), want[layout, i]), (mode, layout, i)
+                    else:
+                        assert np.array_equal(hits_to_numpy(outs[i].view(-1, 6)).view(np.uint8), want[layout, i]), \
+                            (mode, layout, i)
+    finally:
+        _capi.check(lib.lcx_set_trace_tuning(old[0].value, old[1].value, old[2].value), "restore")
     _capi.check(lib.lcx_check_trace_errors(), "errors")
