@@ -443,6 +443,16 @@ LCX_API int lcx_get_build_tuning(uint32_t *leaf_max, uint32_t *width);
  * codes; 0 = off).  Defaults 1, 0, 0. */
 LCX_API int lcx_set_build_morton(uint32_t blas_cube, uint32_t tlas_cube, uint32_t tlas_size_bits);
 LCX_API int lcx_get_build_morton(uint32_t *blas_cube, uint32_t *tlas_cube, uint32_t *tlas_size_bits);
+/* Triangle splitting for later builds of FAST_TRACE meshes created without
+ * allow_update (the spatial splits of the high-quality builder the reference
+ * asks Embree for, cpu/accel.rs:58-61): triangles whose box is much larger
+ * than the triangle get extra references with tighter boxes, at most
+ * fraction x (triangles of the mesh) of them (0 = off; 0..4, default 0).
+ * Every reference stores the whole triangle, so hit records do not change; a
+ * RayQuery triangle callback may see a triangle more than once (as with the
+ * reference's OptiX and Embree builders). */
+LCX_API int lcx_set_build_split(float fraction);
+LCX_API int lcx_get_build_split(float *fraction);
 
 /* Traversal knobs, process-wide (no counterpart in the reference: OptiX and
  * Embree pick theirs internally).  refill: a warp takes new rays once at

@@ -103,6 +103,8 @@ _SIGS = {
     "lcx_trace_any_host": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
     "lcx_set_host_chunk": (c_int, [c_uint32]),
     "lcx_accel_instance_buffer": (c_int, [c_uint64, POINTER(LcxInstanceBuffer)]),
+    "lcx_set_build_split": (c_int, [ctypes.c_float]),
+    "lcx_get_build_split": (c_int, [POINTER(ctypes.c_float)]),
     "lcx_set_refit_sync": (c_int, [c_uint32]),
     "lcx_get_trace_stack": (c_int, [POINTER(c_uint32)]),
     "lcx_get_trace_reorder": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),

@@ -6,7 +6,8 @@ It measures, on the caller's own scene and rays, and picks:
   - node width: children per wide node, 2..8;
   - leaf size: items per leaf slot, 1..3 (the collapse schedule: subtrees of at most this many
     triangles become leaf slots, everything larger is opened);
-  - Morton normalisation of BLAS centroids: by the largest extent ("cube") or per axis.
+  - Morton normalisation of BLAS centroids: by the largest extent ("cube") or per axis;
+  - triangle splitting of FAST_TRACE meshes: extra references as a fraction of the triangles.
 * traversal knobs (``lcx_set_trace_tuning`` / ``lcx_set_trace_stack`` / ``lcx_set_trace_reorder``):
   - ray-pool refill threshold: the number of idle lanes at which a warp takes new rays, 1..32;
   - shared-memory stack depth: 8, 16 or 24 entries per thread;
@@ -39,7 +40,7 @@ from pathlib import Path
 from . import _capi
 from .accel import NODES_QUANT8, Accel, build_meshes, mesh_from_data
 
-BUILD_SPACE = {"leaf_max": [1, 2, 3], "width": [8, 6, 4], "blas_cube": [1, 0]}
+BUILD_SPACE = {"leaf_max": [1, 2, 3], "width": [8, 6, 4], "blas_cube": [1, 0], "split": [0.0, 1.0, 3.0]}
 TRACE_SPACE = {"refill": [1, 2, 4, 8, 16, 32], "short_stack": [8, 16, 24], "mode": [2, 0, 1], "postpone": [0, 12, 32],
                "reorder_bits": [0, 7]}
 
@@ -54,6 +55,7 @@ class Config:
     mode: int = 2
     reorder_bits: int = 0
     postpone: int = 0
+    split: float = 0.0
 
 
 @dataclass
@@ -87,7 +89,10 @@ def current() -> Config:
     _capi.check(lib.lcx_get_trace_stack(ss), "lcx_get_trace_stack")
     rb, rm = _u32(2)
     _capi.check(lib.lcx_get_trace_reorder(rb, rm), "lcx_get_trace_reorder")
-    return Config(lm.value, w.value, bc.value, rf.value, ss.value, md.value, rb.value, pp.value)
+    sp = ctypes.c_float(0.0)
+    _capi.check(lib.lcx_get_build_split(ctypes.byref(sp)), "lcx_get_build_split")
+    return Config(lm.value, w.value, bc.value, rf.value, ss.value, md.value, rb.value, pp.value,
+                  round(sp.value, 6))
 
 
 def apply(cfg: Config):
@@ -99,6 +104,7 @@ def apply(cfg: Config):
     _capi.check(lib.lcx_get_trace_reorder(rb, rm), "lcx_get_trace_reorder")
     _capi.check(lib.lcx_set_build_tuning(cfg.leaf_max, cfg.width), "lcx_set_build_tuning")
     _capi.check(lib.lcx_set_build_morton(cfg.blas_cube, tc.value, sb.value), "lcx_set_build_morton")
+    _capi.check(lib.lcx_set_build_split(ctypes.c_float(cfg.split)), "lcx_set_build_split")
     _capi.check(lib.lcx_set_trace_tuning(cfg.refill, cfg.postpone, cfg.mode), "lcx_set_trace_tuning")
     _capi.check(lib.lcx_set_trace_stack(cfg.short_stack), "lcx_set_trace_stack")
     _capi.check(lib.lcx_set_trace_reorder(cfg.reorder_bits, rm.value), "lcx_set_trace_reorder")

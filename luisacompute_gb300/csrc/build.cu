@@ -28,6 +28,8 @@
 
 #include <cfloat>
 
+#include <cub/device/device_scan.cuh>
+
 #include "lcx_internal.h"
 
 namespace cg = cooperative_groups;
@@ -174,6 +176,332 @@ __global__ void __launch_bounds__(kPrepBlock) k_tri_prep(const SegInput *segs, u
         hi[i] = h;
     }
     add_centroid(s, valid, c, segctl);
+}
+
+// ---------------------------------------------------------------------------
+// Triangle splitting (FAST_TRACE builds; the counterpart of the spatial splits
+// of Embree's RTC_BUILD_QUALITY_HIGH that the reference's CPU backend asks for,
+// cpu/accel.rs:58-61).  A triangle whose box is much larger than the triangle
+// (a long diagonal sliver) overlaps many others and is tested by many rays
+// that do not hit it.  Before the Morton sort such triangles get several
+// references, each with a box around one piece of the triangle, so the tree
+// is built over tighter boxes (Karras & Aila, "Fast Parallel Construction of
+// High-Quality Bounding Volume Hierarchies", 2013, triangle splitting).
+// Every reference of a triangle stores the whole triangle, so a ray tests the
+// same triangle with the same arithmetic through any of them: hit records do
+// not change, a triangle is only found in more leaves.
+//
+// Budget: the extra references of a mesh (segment) are at most
+// floor(fraction * its triangles), shared out within the mesh in proportion
+// to each triangle's weight max(0, A_box - 2 A_tri), quantised to 20 bits of
+// the mesh's largest weight so that the counts are deterministic
+// (A_box = dx dy + dy dz + dz dx of its box: an axis-aligned right triangle
+// scores 0), at most kMaxRefs per triangle.
+// Pieces: the triangle's box is split recursively at the midpoint of its
+// longest axis; each half is tightened to the box of the triangle clipped to
+// it (Sutherland-Hodgman against the half's six planes), padded outward by
+// 2^-19 of the coordinate magnitude and cut back to the half.  The halves
+// share the split plane exactly and each padded box contains its part of the
+// triangle, so the references' boxes cover the whole triangle.
+constexpr uint32_t kMaxRefs = 16;
+
+__device__ __forceinline__ float tri_area2(const float4 &a, const float4 &b, const float4 &c) {
+    const float ux = b.x - a.x, uy = b.y - a.y, uz = b.z - a.z;
+    const float vx = c.x - a.x, vy = c.y - a.y, vz = c.z - a.z;
+    const float cx = uy * vz - uz * vy, cy = uz * vx - ux * vz, cz = ux * vy - uy * vx;
+    return sqrtf(cx * cx + cy * cy + cz * cz);  // twice the area
+}
+
+// Per-segment atomics of the split kernels, one per warp when the warp's items
+// share a segment (a single-mesh build would otherwise send every thread's
+// atomic to the same word).
+__device__ __forceinline__ void seg_add_u64(unsigned long long *a, uint32_t seg, bool in, unsigned long long v) {
+    const uint32_t seg0 = __shfl_sync(~0u, seg, 0);
+    if (__all_sync(~0u, !in || seg == seg0)) {
+        unsigned long long t = in ? v : 0ull;
+        for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(~0u, t, o);
+        if ((threadIdx.x & 31u) == 0u && t) atomicAdd(&a[seg0], t);
+    } else if (in && v) {
+        atomicAdd(&a[seg], v);
+    }
+}
+__device__ __forceinline__ void seg_add_u32(uint32_t *a, uint32_t seg, bool in, uint32_t v) {
+    const uint32_t seg0 = __shfl_sync(~0u, seg, 0);
+    if (__all_sync(~0u, !in || seg == seg0)) {
+        uint32_t t = in ? v : 0u;
+        for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(~0u, t, o);
+        if ((threadIdx.x & 31u) == 0u && t) atomicAdd(&a[seg0], t);
+    } else if (in && v) {
+        atomicAdd(&a[seg], v);
+    }
+}
+__device__ __forceinline__ void seg_max_u32(uint32_t *a, uint32_t seg, bool in, uint32_t v) {
+    const uint32_t seg0 = __shfl_sync(~0u, seg, 0);
+    if (__all_sync(~0u, !in || seg == seg0)) {
+        uint32_t t = in ? v : 0u;
+        for (int o = 16; o; o >>= 1) t = max(t, __shfl_xor_sync(~0u, t, o));
+        if ((threadIdx.x & 31u) == 0u && t) atomicMax(&a[seg0], t);
+    } else if (in && v) {
+        atomicMax(&a[seg], v);
+    }
+}
+
+__global__ void __launch_bounds__(kPrepBlock) k_split_weight(const SegInput *segs, uint32_t nseg, uint32_t n,
+                                                             float *wts, uint32_t *wmax, uint32_t *segctl,
+                                                             uint32_t *ctl) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = i < n;
+    const uint32_t s = in ? segment_of(segs, nseg, i) : 0u;
+    float w = 0.0f;
+    if (in) {
+    const SegInput g = segs[s];
+    const uint32_t local = i - g.item_offset;
+    const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * local);
+    const uint32_t i0 = t[0], i1 = t[1], i2 = t[2];
+    if (i0 >= g.vcount || i1 >= g.vcount || i2 >= g.vcount) {
+        atomicOr(&segctl[kSegWords * s + kSegErr], kErrBadIndex);
+        atomicOr(&ctl[kCtlErr], kErrBadIndex);
+    } else {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i0));
+        const float4 b = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i1));
+        const float4 c = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i2));
+        const float dx = fmaxf(fmaxf(a.x, b.x), c.x) - fminf(fminf(a.x, b.x), c.x);
+        const float dy = fmaxf(fmaxf(a.y, b.y), c.y) - fminf(fminf(a.y, b.y), c.y);
+        const float dz = fmaxf(fmaxf(a.z, b.z), c.z) - fminf(fminf(a.z, b.z), c.z);
+        const float abox = dx * dy + dy * dz + dz * dx;
+        const float v = abox - tri_area2(a, b, c);  // A_box - 2 A_tri
+        w = v > 0.0f && isfinite(v) ? v : 0.0f;
+    }
+    wts[i] = w;
+    }
+    seg_max_u32(wmax, s, in, __float_as_uint(w));  // non-negative floats order as their bits
+}
+
+// Weights as integers relative to the segment's largest (so the sums, and the
+// reference counts, do not depend on the order of the atomics): q in [0, 2^20].
+__global__ void __launch_bounds__(kPrepBlock) k_split_quant(const SegInput *segs, uint32_t nseg, uint32_t n,
+                                                            float *wts, const uint32_t *wmax,
+                                                            unsigned long long *qsum) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = i < n;
+    const uint32_t s = in ? segment_of(segs, nseg, i) : 0u;
+    uint32_t q = 0;
+    if (in) {
+        const float m = __uint_as_float(wmax[s]);
+        const float w = wts[i];
+        q = m > 0.0f ? uint32_t(fminf(w / m, 1.0f) * 1048576.0f) : 0u;
+        reinterpret_cast<uint32_t *>(wts)[i] = q;
+    }
+    seg_add_u64(qsum, s, in, q);
+}
+
+// refs[i] = 1 + this triangle's extra references; seg_refs[s] += refs of segment s.
+__global__ void __launch_bounds__(kPrepBlock) k_split_assign(const SegInput *segs, uint32_t nseg, uint32_t n,
+                                                             const uint32_t *q, const unsigned long long *qsum,
+                                                             float fraction, uint32_t *refs, uint32_t *seg_refs) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = i < n;
+    const uint32_t s = in ? segment_of(segs, nseg, i) : 0u;
+    uint32_t extra = 0;
+    if (in) {
+        const unsigned long long total = qsum[s];
+        const unsigned long long budget =
+            static_cast<unsigned long long>(floorf(fraction * float(segs[s].item_count)));
+        if (total > 0ull) {
+            const unsigned long long e = budget * q[i] / total;  // < 2^33 * 2^21
+            extra = e >= kMaxRefs - 1 ? kMaxRefs - 1 : uint32_t(e);
+        }
+        refs[i] = 1u + extra;
+    }
+    seg_add_u32(seg_refs, s, in, in ? 1u + extra : 0u);
+}
+
+// Clip the convex polygon P (n vertices) to the half-space x[axis] >= v (keep_ge) or <= v.
+__device__ __forceinline__ int clip_plane(float (*P)[3], int n, float (*Q)[3], int axis, float v, bool keep_ge) {
+    int m = 0;
+    for (int k = 0; k < n; k++) {
+        const float *A = P[k], *B = P[(k + 1) % n];
+        const float da = keep_ge ? A[axis] - v : v - A[axis];
+        const float db = keep_ge ? B[axis] - v : v - B[axis];
+        if (da >= 0.0f) {
+            Q[m][0] = A[0];
+            Q[m][1] = A[1];
+            Q[m][2] = A[2];
+            m++;
+        }
+        if ((da >= 0.0f) != (db >= 0.0f)) {
+            const float t = da / (da - db);
+            for (int j = 0; j < 3; j++) Q[m][j] = A[j] + t * (B[j] - A[j]);
+            Q[m][axis] = v;
+            m++;
+        }
+    }
+    return m;
+}
+
+// The box of (triangle within [lo, hi]), padded outward and cut back to [lo, hi].
+// Returns false if the clipped triangle is empty.
+__device__ bool tight_box(const float4 &a, const float4 &b, const float4 &c, const float lo[3], const float hi[3],
+                          float tl[3], float th[3]) {
+    float P[10][3], Q[10][3];
+    P[0][0] = a.x;
+    P[0][1] = a.y;
+    P[0][2] = a.z;
+    P[1][0] = b.x;
+    P[1][1] = b.y;
+    P[1][2] = b.z;
+    P[2][0] = c.x;
+    P[2][1] = c.y;
+    P[2][2] = c.z;
+    int n = 3;
+    for (int axis = 0; axis < 3 && n > 0; axis++) {
+        n = clip_plane(P, n, Q, axis, lo[axis], true);
+        if (n == 0) break;
+        n = clip_plane(Q, n, P, axis, hi[axis], false);
+    }
+    if (n == 0) return false;
+    float mag = 0.0f;
+    for (int j = 0; j < 3; j++) {
+        tl[j] = FLT_MAX;
+        th[j] = -FLT_MAX;
+        mag = fmaxf(mag, fmaxf(fabsf(lo[j]), fabsf(hi[j])));
+    }
+    for (int k = 0; k < n; k++)
+        for (int j = 0; j < 3; j++) {
+            tl[j] = fminf(tl[j], P[k][j]);
+            th[j] = fmaxf(th[j], P[k][j]);
+        }
+    const float pad = mag * 0x1p-19f + 1e-30f;
+    for (int j = 0; j < 3; j++) {
+        tl[j] = fmaxf(tl[j] - pad, lo[j]);
+        th[j] = fminf(th[j] + pad, hi[j]);
+    }
+    return tl[0] <= th[0] && tl[1] <= th[1] && tl[2] <= th[2];
+}
+
+__device__ __forceinline__ void add_centroid_range(uint32_t seg, bool valid, const float cl[3], const float ch[3],
+                                                   uint32_t *segctl) {
+    if (!valid) return;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        atomicMin(&segctl[kSegWords * seg + kSegCenLo + k], float_to_ordered(cl[k]));
+        atomicMax(&segctl[kSegWords * seg + kSegCenHi + k], float_to_ordered(ch[k]));
+    }
+}
+
+// Writes the references of triangle i: boxes at ref_off[i] .. + refs[i] - 1 (in the
+// reference-space item arrays) and their triangle's local index; centroid bounds of
+// the reference segments.  tsegs: the triangle-space segment table.
+__global__ void __launch_bounds__(kPrepBlock) k_split_emit(const SegInput *tsegs, uint32_t nseg, uint32_t n,
+                                                           const uint32_t *refs, const uint32_t *ref_off, float4 *lo,
+                                                           float4 *hi, uint32_t *ref_prim, uint32_t *segctl) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t s = segment_of(tsegs, nseg, i);
+    const SegInput g = tsegs[s];
+    const uint32_t local = i - g.item_offset;
+    const uint32_t r = refs[i], base = ref_off[i];
+    for (uint32_t k = 0; k < r; k++) ref_prim[base + k] = local;
+    const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * local);
+    const uint32_t i0 = t[0], i1 = t[1], i2 = t[2];
+    const float4 E0 = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f), E1 = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
+    if (i0 >= g.vcount || i1 >= g.vcount || i2 >= g.vcount) {  // reported by k_split_weight
+        for (uint32_t k = 0; k < r; k++) {
+            lo[base + k] = E0;
+            hi[base + k] = E1;
+        }
+        return;
+    }
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i0));
+    const float4 b = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i1));
+    const float4 c = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i2));
+    float cl[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, ch[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    bool any = false;
+    // pieces as (box, references) on a small stack; a piece with one reference is written
+    float sl[6][3], sh[6][3];
+    uint32_t sc[6];
+    int sp = 0;
+    sl[0][0] = fminf(fminf(a.x, b.x), c.x);
+    sl[0][1] = fminf(fminf(a.y, b.y), c.y);
+    sl[0][2] = fminf(fminf(a.z, b.z), c.z);
+    sh[0][0] = fmaxf(fmaxf(a.x, b.x), c.x);
+    sh[0][1] = fmaxf(fmaxf(a.y, b.y), c.y);
+    sh[0][2] = fmaxf(fmaxf(a.z, b.z), c.z);
+    sc[0] = r;
+    sp = 1;
+    uint32_t out = 0;
+    while (sp > 0) {
+        sp--;
+        float bl[3] = {sl[sp][0], sl[sp][1], sl[sp][2]}, bh[3] = {sh[sp][0], sh[sp][1], sh[sp][2]};
+        const uint32_t cnt = sc[sp];
+        const bool valid = bl[0] <= bh[0] && bl[1] <= bh[1] && bl[2] <= bh[2] && isfinite(bl[0] + bl[1] + bl[2]) &&
+                           isfinite(bh[0] + bh[1] + bh[2]);
+        int axis = 0;
+        float ext = bh[0] - bl[0];
+        for (int j = 1; j < 3; j++)
+            if (bh[j] - bl[j] > ext) {
+                ext = bh[j] - bl[j];
+                axis = j;
+            }
+        const float mid = 0.5f * (bl[axis] + bh[axis]);
+        if (cnt == 1u || !valid || !(mid > bl[axis] && mid < bh[axis]) || sp + 2 > 6) {
+            // one reference gets the box; any others of this piece stay empty
+            for (uint32_t k = 0; k < cnt; k++) {
+                const bool first = k == 0 && valid;
+                lo[base + out] = first ? make_float4(bl[0], bl[1], bl[2], 0.0f) : E0;
+                hi[base + out] = first ? make_float4(bh[0], bh[1], bh[2], 0.0f) : E1;
+                if (first) {
+                    any = true;
+                    for (int j = 0; j < 3; j++) {
+                        const float cj = 0.5f * (bl[j] + bh[j]);
+                        cl[j] = fminf(cl[j], cj);
+                        ch[j] = fmaxf(ch[j], cj);
+                    }
+                }
+                out++;
+            }
+            continue;
+        }
+        float ll[3] = {bl[0], bl[1], bl[2]}, lh[3] = {bh[0], bh[1], bh[2]};
+        float rl[3] = {bl[0], bl[1], bl[2]}, rh[3] = {bh[0], bh[1], bh[2]};
+        lh[axis] = mid;
+        rl[axis] = mid;
+        float tl1[3], th1[3], tl2[3], th2[3];
+        const bool okl = tight_box(a, b, c, ll, lh, tl1, th1);
+        const bool okr = tight_box(a, b, c, rl, rh, tl2, th2);
+        if (!okl || !okr) {  // all of the piece on one side: keep splitting that side
+            const float *nl = okl ? tl1 : tl2, *nh = okl ? th1 : th2;
+            if (!okl && !okr) {
+                nl = bl;
+                nh = bh;
+            }
+            for (int j = 0; j < 3; j++) {
+                sl[sp][j] = nl[j];
+                sh[sp][j] = nh[j];
+            }
+            sc[sp] = (okl || okr) ? cnt : 1u;
+            sp++;
+            if (!okl && !okr)  // cannot happen for a finite triangle; write the rest empty
+                for (uint32_t k = 1; k < cnt; k++) {
+                    lo[base + out] = E0;
+                    hi[base + out] = E1;
+                    out++;
+                }
+            continue;
+        }
+        const uint32_t cl_n = cnt / 2u, cr_n = cnt - cl_n;
+        for (int j = 0; j < 3; j++) {
+            sl[sp][j] = tl1[j];
+            sh[sp][j] = th1[j];
+        }
+        sc[sp++] = cl_n;
+        for (int j = 0; j < 3; j++) {
+            sl[sp][j] = tl2[j];
+            sh[sp][j] = th2[j];
+        }
+        sc[sp++] = cr_n;
+    }
+    add_centroid_range(s, any, cl, ch, segctl);
 }
 
 __global__ void __launch_bounds__(kPrepBlock) k_inst_prep(const InstState *inst, uint32_t n, float4 *lo, float4 *hi,
@@ -664,7 +992,7 @@ __device__ void emit_node(const TreeView &tv, const SegInput *segs, const uint32
 
 __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *desc, uint32_t wide_count,
                             int leaf_max, Node8Q *qn, Node8F *fn, TriRec *tris, const uint32_t *segctl,
-                            uint32_t *ctl, double *sah, unsigned long long *rtab) {
+                            uint32_t *ctl, double *sah, unsigned long long *rtab, const uint32_t *ref_prim) {
     const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= wide_count) return;
     const uint32_t seg = desc[12ull * w + 3];
@@ -684,8 +1012,10 @@ __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *d
     float4 rl, rh;
     emit_node(
         tv, segs, desc, w, qn, fn, leaf_max, ctl, sah, rtab,
-        [&](uint32_t pos, uint32_t prim, uint32_t s) {
+        [&](uint32_t pos, uint32_t item, uint32_t s) {
             const SegInput &g = segs[s];
+            // a reference of a split build names its triangle (local index of the mesh)
+            const uint32_t prim = ref_prim != nullptr ? ref_prim[g.item_offset + item] : item;
             if (g.kind == kSegAabbs) {
                 const float *bx = reinterpret_cast<const float *>(g.vbase + 24ull * prim);
                 tris[pos] = TriRec{make_float4(bx[0], bx[1], bx[2], __uint_as_float(prim)),
@@ -867,9 +1197,37 @@ uint32_t morton_axis_bits(uint32_t nseg, uint32_t *seg_bits) {
 }
 
 cudaError_t build_tree_tris(BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
-    k_tri_prep<<<blocks_for(s.n, kPrepBlock), kPrepBlock, 0, st>>>(s.segs, s.nseg, s.n, s.box_lo, s.box_hi, s.segctl,
-                                                                   s.ctl);
+    if (s.ref_prim == nullptr)  // with triangle splitting split_emit has written the item boxes
+        k_tri_prep<<<blocks_for(s.n, kPrepBlock), kPrepBlock, 0, st>>>(s.segs, s.nseg, s.n, s.box_lo, s.box_hi,
+                                                                       s.segctl, s.ctl);
     return build_common(s, bp, st);
+}
+
+cudaError_t split_count(const SegInput *tsegs, uint32_t nseg, uint32_t n, float fraction, float *wts,
+                        unsigned long long *sums, uint32_t *refs, uint32_t *seg_refs, uint32_t *segctl, uint32_t *ctl,
+                        cudaStream_t st) {
+    uint32_t *wmax = reinterpret_cast<uint32_t *>(sums + nseg);
+    cudaError_t e = cudaMemsetAsync(sums, 0, sizeof(unsigned long long) * nseg + sizeof(uint32_t) * nseg, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(seg_refs, 0, sizeof(uint32_t) * nseg, st);
+    if (e != cudaSuccess) return e;
+    k_split_weight<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(tsegs, nseg, n, wts, wmax, segctl, ctl);
+    k_split_quant<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(tsegs, nseg, n, wts, wmax, sums);
+    k_split_assign<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(
+        tsegs, nseg, n, reinterpret_cast<const uint32_t *>(wts), sums, fraction, refs, seg_refs);
+    return cudaGetLastError();
+}
+
+cudaError_t exclusive_sum(void *tmp, size_t *tmp_bytes, const uint32_t *in, uint32_t *out, uint32_t n,
+                          cudaStream_t st) {
+    return cub::DeviceScan::ExclusiveSum(tmp, *tmp_bytes, in, out, int(n), st);
+}
+
+cudaError_t split_emit(const SegInput *tsegs, uint32_t nseg, uint32_t n, const uint32_t *refs, const uint32_t *ref_off,
+                       BuildScratch &s, uint32_t *ref_prim, cudaStream_t st) {
+    k_split_emit<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(tsegs, nseg, n, refs, ref_off, s.box_lo, s.box_hi,
+                                                                   ref_prim, s.segctl);
+    s.ref_prim = ref_prim;
+    return cudaGetLastError();
 }
 
 cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
@@ -880,7 +1238,8 @@ cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const Build
 cudaError_t emit_blas(const BuildScratch &s, const BuildParams &bp, uint32_t wide_count, Node8Q *qn, Node8F *fn,
                       TriRec *tris, double *wide_sah, unsigned long long *rtab, cudaStream_t st) {
     k_emit_blas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.segs, s.desc, wide_count, bp.leaf_max,
-                                                              qn, fn, tris, s.segctl, s.ctl, wide_sah, rtab);
+                                                              qn, fn, tris, s.segctl, s.ctl, wide_sah, rtab,
+                                                              s.ref_prim);
     return cudaGetLastError();
 }
 

@@ -145,6 +145,7 @@ struct MeshObj {
     double *wide_sah = nullptr;       // in `block`: 2 doubles of this mesh's segment
     size_t mem_bytes = 0;             // this mesh's share of the block
     uint32_t node_count = 0, tri_count = 0, depth = 0;
+    uint32_t ref_count = 0;  // leaf items: tri_count, or more with triangle splitting
     uint32_t kind = kSegTriangles;  // or kSegAabbs: a procedural primitive (lcx_procedural_*)
     uint32_t seg = 0;  // segment (position in its build) within `block`
     uint64_t refits = 0;  // refits since the last full build
@@ -316,6 +317,13 @@ struct BuildTuning {
     // cut node visits per ray 17.7 -> 16.5; cube or size-class TLAS codes raised
     // the TLAS SAH 22.9 -> 30.7+ and slowed traversal, so both stay off.
     uint32_t blas_cube = 1, tlas_cube = 0, tlas_size_bits = 0;
+    // triangle splitting of FAST_TRACE meshes without allow_update (lcx_set_build_split):
+    // extra references as a fraction of the triangles.  Off by default: on the terrain
+    // workload it makes no splits at 0.3 (axis-aligned right triangles weigh 0) and costs
+    // traversal at 1 and 3 (1.525 -> 1.467 / 1.364 Grays/s); on a displaced 1M-triangle mesh
+    // it takes 0.61 -> 0.68 / 1.00 Grays/s (nodes per ray 27.7 -> 13.0 at 3).  The
+    // autotuner and callers with such meshes turn it on.
+    float split = 0.0f;
 };
 BuildTuning g_build_tune;
 
@@ -324,6 +332,7 @@ BuildParams build_params_for(const LcxAccelOption &o) {
     bp.leaf_max = g_build_tune.leaf_max > 0 ? g_build_tune.leaf_max : leaf_items_for(o);
     bp.width = g_build_tune.width;
     bp.cube = g_build_tune.blas_cube;
+    bp.split = (o.hint == LCX_HINT_FAST_TRACE && !o.allow_update) ? g_build_tune.split : 0.0f;
     return bp;
 }
 
@@ -489,7 +498,7 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
             m->block.reset();
             m->wide_sah = nullptr;
             m->mem_bytes = 0;
-            m->node_count = m->tri_count = m->depth = 0;
+            m->node_count = m->tri_count = m->ref_count = m->depth = 0;
             m->sah = 0.0;
             m->built = true;
             m->generation++;
@@ -500,10 +509,77 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
     const uint32_t n = uint32_t(total);
     BuildReadback rb;
     std::shared_ptr<DevBlock> block;
+    bool want_rtab = false;
+    for (MeshObj *m : meshes) want_rtab = want_rtab || m->opt.allow_update;
     {
         ScratchHolder hold(st);
         BuildScratch s;
-        if (int r = alloc_scratch(hold, s, segs, n, false)) return r;
+        // triangle splitting: FAST_TRACE triangle meshes, none of them kept for refits
+        bool split = bp.split > 0.0f && !want_rtab;
+        for (const SegInput &g : segs) split = split && g.kind == kSegTriangles;
+        std::vector<SegInput> rsegs;  // the segments in reference space
+        uint32_t n_items = n;
+        SegInput *d_tsegs = nullptr;
+        uint32_t *d_refs = nullptr, *d_ref_off = nullptr;
+        if (split) {
+            const uint32_t nseg = uint32_t(count);
+            float *wts = nullptr;
+            unsigned long long *wsum = nullptr;  // per segment: weight sums, then the largest weights
+            uint32_t *seg_refs = nullptr, *ctl1 = nullptr, *segctl1 = nullptr;
+            LCX_CUDA(hold.alloc((void **)&d_tsegs, sizeof(SegInput) * nseg), "split scratch");
+            LCX_CUDA(hold.alloc((void **)&wts, sizeof(float) * n), "split scratch");
+            LCX_CUDA(hold.alloc((void **)&wsum, (sizeof(unsigned long long) + sizeof(uint32_t)) * nseg),
+                     "split scratch");
+            LCX_CUDA(hold.alloc((void **)&d_refs, sizeof(uint32_t) * n), "split scratch");
+            LCX_CUDA(hold.alloc((void **)&d_ref_off, sizeof(uint32_t) * n), "split scratch");
+            LCX_CUDA(hold.alloc((void **)&seg_refs, sizeof(uint32_t) * nseg), "split scratch");
+            LCX_CUDA(hold.alloc((void **)&segctl1, sizeof(uint32_t) * kSegWords * nseg), "split scratch");
+            LCX_CUDA(hold.alloc((void **)&ctl1, sizeof(uint32_t) * kCtlWords), "split scratch");
+            LCX_CUDA(cudaMemcpyAsync(d_tsegs, segs.data(), sizeof(SegInput) * nseg, cudaMemcpyHostToDevice, st),
+                     "segment upload");
+            LCX_CUDA(cudaMemsetAsync(segctl1, 0, sizeof(uint32_t) * kSegWords * nseg, st), "split scratch init");
+            LCX_CUDA(cudaMemsetAsync(ctl1, 0, sizeof(uint32_t) * kCtlWords, st), "split scratch init");
+            LCX_CUDA(split_count(d_tsegs, nseg, n, bp.split, wts, wsum, d_refs, seg_refs, segctl1, ctl1, st),
+                     "split counts");
+            size_t scan_bytes = 0;
+            LCX_CUDA(exclusive_sum(nullptr, &scan_bytes, d_refs, d_ref_off, n, st), "scan size");
+            void *scan_tmp = nullptr;
+            LCX_CUDA(hold.alloc(&scan_tmp, scan_bytes), "split scratch");
+            LCX_CUDA(exclusive_sum(scan_tmp, &scan_bytes, d_refs, d_ref_off, n, st), "reference offsets");
+            std::vector<uint32_t> h_refs(nseg), h_err(nseg * size_t(kSegWords)), h_ctl(kCtlWords);
+            LCX_CUDA(cudaMemcpyAsync(h_refs.data(), seg_refs, sizeof(uint32_t) * nseg, cudaMemcpyDeviceToHost, st),
+                     "split readback");
+            LCX_CUDA(cudaMemcpyAsync(h_err.data(), segctl1, sizeof(uint32_t) * h_err.size(), cudaMemcpyDeviceToHost, st),
+                     "split readback");
+            LCX_CUDA(cudaMemcpyAsync(h_ctl.data(), ctl1, sizeof(uint32_t) * kCtlWords, cudaMemcpyDeviceToHost, st),
+                     "split readback");
+            LCX_CUDA(cudaStreamSynchronize(st), "split sync");
+            if (h_ctl[kCtlErr] & kErrBadIndex) {
+                for (size_t i = 0; i < count; i++)
+                    if (h_err[kSegWords * i + kSegErr] & kErrBadIndex)
+                        return fail(LCX_ERR_INVALID_ARG,
+                                    "mesh %zu of the build: triangle index out of range (vertex count %u)", i,
+                                    segs[i].vcount);
+                return fail(LCX_ERR_INVALID_ARG, "triangle index out of range");
+            }
+            rsegs = segs;
+            uint64_t off = 0;
+            for (size_t i = 0; i < count; i++) {
+                rsegs[i].item_offset = uint32_t(off);
+                rsegs[i].item_count = h_refs[i];
+                off += h_refs[i];
+            }
+            if (off >= (1ull << 31)) return fail(LCX_ERR_INVALID_ARG, "too many triangle references (%llu)",
+                                                 (unsigned long long)off);
+            n_items = uint32_t(off);
+        }
+        const std::vector<SegInput> &isegs = split ? rsegs : segs;  // the build's items
+        if (int r = alloc_scratch(hold, s, isegs, n_items, false)) return r;
+        if (split) {
+            uint32_t *ref_prim = nullptr;
+            LCX_CUDA(hold.alloc((void **)&ref_prim, sizeof(uint32_t) * n_items), "split scratch");
+            LCX_CUDA(split_emit(d_tsegs, uint32_t(count), n, d_refs, d_ref_off, s, ref_prim, st), "triangle split");
+        }
         LCX_CUDA(build_tree_tris(s, bp, st), "BLAS build");
         if (int r = read_back(s, st, rb)) return r;
         if (rb.ctl[kCtlErr] & kErrBadIndex) {
@@ -515,14 +591,12 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
         }
         if (rb.ctl[kCtlErr] & kErrTooDeep) return fail(LCX_ERR_DEPTH, "BVH deeper than %d levels", kMaxLevels);
         for (size_t i = 0; i < count; i++)
-            if (rb.segctl[kSegWords * i + kSegItems] != segs[i].item_count)
-                return fail(LCX_ERR_CUDA, "BLAS build placed %u of %u triangles of mesh %zu",
-                            rb.segctl[kSegWords * i + kSegItems], segs[i].item_count, i);
+            if (rb.segctl[kSegWords * i + kSegItems] != isegs[i].item_count)
+                return fail(LCX_ERR_CUDA, "BLAS build placed %u of %u items of mesh %zu",
+                            rb.segctl[kSegWords * i + kSegItems], isegs[i].item_count, i);
         const uint32_t W = rb.ctl[kCtlWideCount];
         const size_t q_bytes = size_t(W) * sizeof(Node8Q), f_bytes = size_t(W) * sizeof(Node8F);
-        const size_t t_bytes = size_t(n) * sizeof(TriRec), sah_bytes = 2 * sizeof(double) * count;
-        bool want_rtab = false;
-        for (MeshObj *m : meshes) want_rtab = want_rtab || m->opt.allow_update;
+        const size_t t_bytes = size_t(n_items) * sizeof(TriRec), sah_bytes = 2 * sizeof(double) * count;
         // refit data: parent table, counters, segment table (16-byte aligned)
         const size_t r_bytes =
             want_rtab ? ((size_t(W) * (sizeof(unsigned long long) + sizeof(uint32_t)) + 15) & ~size_t(15)) +
@@ -562,9 +636,10 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
             m->refits = 0;
             m->node_count = segs[i].item_count ? sc[kSegNodes] : 0u;
             m->tri_count = segs[i].item_count;
+            m->ref_count = isegs[i].item_count;
             m->depth = segs[i].item_count ? sc[kSegDepth] : 0u;
             m->mem_bytes = size_t(m->node_count) * (sizeof(Node8Q) + sizeof(Node8F) + (rtab ? 8 : 0)) +
-                           size_t(m->tri_count) * sizeof(TriRec);
+                           size_t(m->ref_count) * sizeof(TriRec);
             const double ra = rb.bin_sah[2 * i + 1];
             m->sah = ra > 0.0 ? rb.bin_sah[2 * i] / ra : 0.0;
         }
@@ -794,7 +869,7 @@ int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out) {
     if (!m->built) return fail(LCX_ERR_NOT_BUILT, "mesh not built");
     std::memset(out, 0, sizeof(*out));
     out->node_count = m->node_count;
-    out->leaf_prim_count = m->tri_count;
+    out->leaf_prim_count = m->ref_count;
     out->device_bytes = m->mem_bytes + sizeof(BlasDesc);
     out->depth = m->depth;
     out->sah_cost = m->sah;
@@ -1058,6 +1133,19 @@ int lcx_accel_stats(uint64_t accel, LcxAccelStats *out) {
         LCX_CUDA(cudaMemcpy(h, a->wide_sah, sizeof(h), cudaMemcpyDeviceToHost), "wide SAH readback");
         out->wide_sah_cost = h[1] > 0.0 ? h[0] / h[1] : 0.0;
     }
+    return LCX_OK;
+}
+
+int lcx_set_build_split(float fraction) {
+    if (!(fraction >= 0.0f && fraction <= 4.0f))
+        return fail(LCX_ERR_INVALID_ARG, "split fraction must be in [0, 4]");
+    g_build_tune.split = fraction;
+    return LCX_OK;
+}
+
+int lcx_get_build_split(float *fraction) {
+    if (!fraction) return fail(LCX_ERR_INVALID_ARG, "null output");
+    *fraction = g_build_tune.split;
     return LCX_OK;
 }
 

@@ -58,6 +58,7 @@ struct BuildParams {
     int width = 8;           // children per wide node, 2..8
     uint32_t size_bits = 0;  // extended-Morton size-class bits (TLAS builds)
     uint32_t cube = 1;       // normalise centroids by the largest extent on every axis (else per axis)
+    float split = 0.0f;      // triangle splitting: extra references, as a fraction of the triangles (0 = off)
 };
 
 // Per-build device scratch, sized for n items in nseg segments.
@@ -84,6 +85,7 @@ struct BuildScratch {
     uint32_t *ctl = nullptr;        // kCtlWords
     void *sort_tmp = nullptr;
     size_t sort_tmp_bytes = 0;
+    const uint32_t *ref_prim = nullptr;  // split builds: triangle (local index) of each item (reference)
 };
 
 size_t sort_temp_bytes(uint32_t n);
@@ -97,6 +99,22 @@ uint32_t morton_axis_bits(uint32_t nseg, uint32_t *seg_bits);
 // caller reads ctl (wide node count, errors) and segctl back.
 cudaError_t build_tree_tris(BuildScratch &s, const BuildParams &bp, cudaStream_t st);
 cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const BuildParams &bp, cudaStream_t st);
+
+// Triangle splitting (split builds).  split_count: per triangle 1 + its extra
+// references (refs; at most fraction x the segment's triangles extra per
+// segment) and per segment their sum (seg_refs; wts: n words, sums: 12 nseg
+// bytes of scratch), from the
+// triangle-space segments tsegs; bad indices are flagged in segctl / ctl as by
+// a build.  exclusive_sum: CUB exclusive scan (tmp null: size query).
+// split_emit: the reference boxes into s (reference-space scratch) at ref_off,
+// the triangle of each reference into ref_prim, and the centroid bounds.
+cudaError_t split_count(const SegInput *tsegs, uint32_t nseg, uint32_t n, float fraction, float *wts,
+                        unsigned long long *sums, uint32_t *refs, uint32_t *seg_refs, uint32_t *segctl, uint32_t *ctl,
+                        cudaStream_t st);
+cudaError_t exclusive_sum(void *tmp, size_t *tmp_bytes, const uint32_t *in, uint32_t *out, uint32_t n,
+                          cudaStream_t st);
+cudaError_t split_emit(const SegInput *tsegs, uint32_t nseg, uint32_t n, const uint32_t *refs, const uint32_t *ref_off,
+                       BuildScratch &s, uint32_t *ref_prim, cudaStream_t st);
 
 // Phase 2: write both node layouts and the leaf items; wide_sah (2 nseg
 // doubles, zeroed by the caller, may be null) receives the per-segment wide SAH.
