@@ -123,6 +123,20 @@ struct __align__(16) InstRec {
 };
 static_assert(sizeof(InstRec) == 80, "InstRec is 80 B");
 
+// Motion of a motion instance (matrix keyframes; AccelOption::Motion,
+// include/luisa/runtime/rhi/resource.h:105-117): `count` row-major 3x4
+// object-to-world matrices spaced evenly over [t0, t1], interpolated linearly
+// per element.  flags bit 0: the instance vanishes before t0 (else the time is
+// clamped), bit 1: after t1.
+struct __align__(16) MotionDesc {
+    const float *keys;
+    uint32_t count;
+    float t0, t1;
+    uint32_t flags;
+    uint32_t _pad[2];
+};
+static_assert(sizeof(MotionDesc) == 32, "MotionDesc is 32 B");
+
 // Instance state by instance index (what Modifications edit).
 struct __align__(16) InstState {
     float o2w[12];
@@ -130,15 +144,21 @@ struct __align__(16) InstState {
     uint32_t mask;
     uint32_t user_id;
     uint32_t opaque;
-    uint32_t _pad[3];
+    uint32_t _pad0;
+    const MotionDesc *motion;  // null = a static instance (o2w)
 };
 static_assert(sizeof(InstState) == 80, "InstState is 80 B");
+
+// TLAS leaf records of motion instances carry this bit with the visibility mask
+// shifted up by 8 (like procedural ones), so the kernels without motion support
+// never enter them; the MotionDesc address sits in the first 8 bytes of w2o.
+constexpr uint32_t kInstMotion = 0x40000000u;
 
 struct __align__(16) ModRec {  // == LcxModification with primitive translated
     uint32_t index, user_id, flags, vis_mask;
     float affine[12];
     uint64_t primitive;  // BlasDesc device address (0 = none)
-    uint64_t _pad;
+    uint64_t motion;     // with a primitive: MotionDesc device address of a motion instance (0 = static)
 };
 static_assert(sizeof(ModRec) == 80, "ModRec is 80 B");
 
@@ -187,6 +207,24 @@ __device__ __forceinline__ void affine_inverse(const float *m, float *w) {
         w[4 * k + 2] = R[3 * k + 2];
         w[4 * k + 3] = -__fmaf_rn(R[3 * k + 0], tx, __fmaf_rn(R[3 * k + 1], ty, __fmul_rn(R[3 * k + 2], tz)));
     }
+}
+
+// Object-to-world matrix of a motion instance at `time`; false when the
+// instance has vanished at that time.  Segment and fraction:
+// u = (time - t0) / (t1 - t0) clamped to [0, 1] (NaN -> 0), x = u (count - 1),
+// i = min(floor(x), count - 2), f = x - i; element k = fma(f, K1[k] - K0[k], K0[k]).
+__device__ __forceinline__ bool motion_matrix(const MotionDesc &md, float time, float m[12]) {
+    if ((md.flags & 1u) && time < md.t0) return false;
+    if ((md.flags & 2u) && time > md.t1) return false;
+    float u = __fdiv_rn(__fsub_rn(time, md.t0), __fsub_rn(md.t1, md.t0));
+    u = u >= 0.0f ? (u <= 1.0f ? u : 1.0f) : 0.0f;
+    const float x = __fmul_rn(u, float(md.count - 1u));
+    const uint32_t i = min(uint32_t(floorf(x)), md.count - 2u);
+    const float f = __fsub_rn(x, float(i));
+    const float *k0 = md.keys + 12ull * i, *k1 = k0 + 12;
+#pragma unroll
+    for (int k = 0; k < 12; k++) m[k] = __fmaf_rn(f, __fsub_rn(k1[k], k0[k]), k0[k]);
+    return true;
 }
 
 // World ray -> object ray.

@@ -249,6 +249,43 @@ LCX_API int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t re
 
 LCX_API int lcx_accel_stats(uint64_t accel, LcxAccelStats *out);
 
+/* ------------------------------------------------------ motion instances */
+
+/* AccelOption::Motion (include/luisa/runtime/rhi/resource.h:101-118) for a
+ * motion instance (MotionInstance, include/luisa/runtime/rtx/motion_instance.h):
+ * keyframe_count >= 2 keyframes spaced evenly over [time_start, time_end]
+ * (time_end > time_start); a ray time before time_start (after time_end)
+ * makes the instance vanish if vanish_start (vanish_end) is set, else it is
+ * clamped.  Only LCX_MOTION_MATRIX keyframes are supported (the reference's
+ * SRT mode is not: interpolated rotations need swept bounds). */
+enum { LCX_MOTION_MATRIX = 0, LCX_MOTION_SRT = 1 };
+typedef struct LcxMotionOption {
+    uint32_t keyframe_count;
+    float time_start;
+    float time_end;
+    uint8_t vanish_start;
+    uint8_t vanish_end;
+    uint8_t mode;        /* LCX_MOTION_MATRIX */
+    uint8_t _pad;
+} LcxMotionOption;
+
+/* A motion instance of a built triangle mesh (Device::create_motion_instance).
+ * Its keyframes start as identities.  An accel instances it by passing its
+ * handle as a Modification's primitive; the TLAS then bounds the mesh over
+ * all keyframes, and traces move it by the keyframe matrices interpolated
+ * linearly per element at each ray's time (OptiX's matrix motion transform,
+ * the CUDA backend's path).  Accels that instance it keep its memory alive;
+ * destroying it, or building it again with new keyframes, makes their traces
+ * fail until they are built again.  No CPU-backend counterpart. */
+LCX_API int lcx_motion_instance_create(uint64_t mesh, const LcxMotionOption *option, uint64_t *out_handle);
+LCX_API int lcx_motion_instance_destroy(uint64_t motion_instance);
+/* `count` (== keyframe_count) row-major 3x4 object-to-world matrices, host
+ * memory (MotionInstance::set_keyframes with the reference's float4x4
+ * matrices, packed as Modification::set_transform packs them). */
+LCX_API int lcx_motion_instance_set_keyframes(uint64_t motion_instance, const float *matrices, uint32_t count);
+/* Uploads the keyframes on `stream` (MotionInstance::build). */
+LCX_API int lcx_motion_instance_build(uint64_t motion_instance, void *stream);
+
 /* ----------------------------------------------------------------- queries */
 
 /* Device view of a built accel, for lcx::ray_query in user CUDA kernels
@@ -324,6 +361,19 @@ LCX_API int lcx_trace_closest_ex(uint64_t accel, const LcxRay *d_rays, uint32_t 
 LCX_API int lcx_trace_any_ex(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count,
                      uint32_t mask, uint8_t *d_occluded, uint32_t node_layout,
                      void *stream);
+
+/* Queries with a time per ray (DSL Accel::intersect_motion /
+ * intersect_any_motion, include/luisa/dsl/rtx/accel.h:47-48): d_times holds
+ * ray_count floats (null: time 0).  Static instances ignore the time.  Any
+ * trace of an accel that instances a motion instance runs the motion kernels
+ * (time 0 for the calls without times); lcx_trace_jobs and
+ * lcx_accel_device_view reject such accels. */
+LCX_API int lcx_trace_closest_motion(uint64_t accel, const LcxRay *d_rays, const float *d_times,
+                                     uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
+                                     uint32_t node_layout, void *stream);
+LCX_API int lcx_trace_any_motion(uint64_t accel, const LcxRay *d_rays, const float *d_times,
+                                 uint32_t ray_count, uint32_t mask, uint8_t *d_occluded,
+                                 uint32_t node_layout, void *stream);
 
 /* The same queries over HOST buffers, for callers whose rays and results live
  * in host memory -- the form of the reference's CPU backend, whose

@@ -13,6 +13,8 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "liblcx_accel.so"
 
 LCX_OK = 0
 LCX_ERR_INVALID_ARG = -1
+LCX_MOTION_MATRIX = 0
+LCX_MOTION_SRT = 1
 LCX_ERR_OOM = -2
 LCX_ERR_NOT_BUILT = -3
 LCX_ERR_TIMEOUT = -4
@@ -65,6 +67,11 @@ class LcxInstanceBuffer(ctypes.Structure):
     _fields_ = [("states", c_void_p), ("count", c_uint32), ("_pad", c_uint32)]
 
 
+class LcxMotionOption(ctypes.Structure):
+    _fields_ = [("keyframe_count", c_uint32), ("time_start", ctypes.c_float), ("time_end", ctypes.c_float),
+                ("vanish_start", c_uint8), ("vanish_end", c_uint8), ("mode", c_uint8), ("_pad", c_uint8)]
+
+
 class LcxAccelView(ctypes.Structure):
     _fields_ = [("tlas_nodes", c_void_p), ("instances", c_void_p), ("stack_need", c_uint32), ("_pad", c_uint32)]
 
@@ -105,6 +112,13 @@ _SIGS = {
     "lcx_accel_instance_buffer": (c_int, [c_uint64, POINTER(LcxInstanceBuffer)]),
     "lcx_set_build_split": (c_int, [ctypes.c_float]),
     "lcx_get_build_split": (c_int, [POINTER(ctypes.c_float)]),
+    "lcx_motion_instance_create": (c_int, [c_uint64, c_void_p, POINTER(c_uint64)]),
+    "lcx_motion_instance_destroy": (c_int, [c_uint64]),
+    "lcx_motion_instance_set_keyframes": (c_int, [c_uint64, c_void_p, c_uint32]),
+    "lcx_motion_instance_build": (c_int, [c_uint64, c_void_p]),
+    "lcx_trace_closest_motion": (c_int, [c_uint64, c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32,
+                                         c_void_p]),
+    "lcx_trace_any_motion": (c_int, [c_uint64, c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
     "lcx_set_refit_sync": (c_int, [c_uint32]),
     "lcx_get_trace_stack": (c_int, [POINTER(c_uint32)]),
     "lcx_get_trace_reorder": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),

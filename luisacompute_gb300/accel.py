@@ -273,6 +273,29 @@ class Accel:
                                                 stream_handle(stream)), "lcx_trace_closest")
         return out
 
+    def trace_closest_motion(self, rays, times=None, mask: int = 0xFF, out=None, layout: int = NODES_QUANT8,
+                             stream=None):
+        """lcx_trace_closest_motion: rays with a time each (a float32 CUDA tensor, None = 0)."""
+        torch = _torch()
+        ptr, n = self._rays_ptr(rays)
+        if out is None:
+            out = torch.empty((n, 6), dtype=torch.int32, device=rays.device)
+        tp = 0 if times is None else times.data_ptr()
+        check(self.lib.lcx_trace_closest_motion(self.handle, ptr, tp or None, n, mask, out.data_ptr(), layout,
+                                                stream_handle(stream)), "lcx_trace_closest_motion")
+        return out
+
+    def trace_any_motion(self, rays, times=None, mask: int = 0xFF, out=None, layout: int = NODES_QUANT8,
+                         stream=None):
+        torch = _torch()
+        ptr, n = self._rays_ptr(rays)
+        if out is None:
+            out = torch.empty(n, dtype=torch.uint8, device=rays.device)
+        tp = 0 if times is None else times.data_ptr()
+        check(self.lib.lcx_trace_any_motion(self.handle, ptr, tp or None, n, mask, out.data_ptr(), layout,
+                                            stream_handle(stream)), "lcx_trace_any_motion")
+        return out
+
     def trace_any(self, rays, mask: int = 0xFF, out=None, layout: int = NODES_QUANT8, stream=None):
         torch = _torch()
         ptr, n = self._rays_ptr(rays)
@@ -325,6 +348,48 @@ class Accel:
     def destroy(self):
         if getattr(self, "handle", 0):
             check(self.lib.lcx_accel_destroy(self.handle), "lcx_accel_destroy")
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class MotionInstance:
+    """A motion instance (include/luisa/runtime/rtx/motion_instance.h) of a built mesh: matrix
+    keyframes (row-major 3x4 or 4x4 each) spaced evenly over [time_start, time_end].  An Accel
+    instances it like a mesh (``emplace_back``); traces move it at each ray's time
+    (``trace_closest_motion``)."""
+
+    def __init__(self, mesh: Mesh, keyframes, time_start: float = 0.0, time_end: float = 1.0,
+                 vanish_start: bool = False, vanish_end: bool = False, stream=None):
+        self.lib = _capi.load()
+        self.mesh = mesh
+        keys = np.stack([_as_affine(k) for k in keyframes])
+        opt = _capi.LcxMotionOption(keys.shape[0], time_start, time_end, int(vanish_start), int(vanish_end),
+                                    _capi.LCX_MOTION_MATRIX, 0)
+        h = ctypes.c_uint64(0)
+        check(self.lib.lcx_motion_instance_create(mesh.handle, ctypes.byref(opt), ctypes.byref(h)),
+              "lcx_motion_instance_create")
+        self.handle = h.value
+        self.set_keyframes(keys)
+        self.build(stream)
+
+    def set_keyframes(self, keyframes):
+        keys = np.ascontiguousarray(np.stack([_as_affine(k) for k in keyframes]), np.float32)
+        check(self.lib.lcx_motion_instance_set_keyframes(self.handle, keys.ctypes.data, keys.shape[0]),
+              "lcx_motion_instance_set_keyframes")
+        self.keys = keys
+
+    def build(self, stream=None) -> "MotionInstance":
+        check(self.lib.lcx_motion_instance_build(self.handle, stream_handle(stream)), "lcx_motion_instance_build")
+        return self
+
+    def destroy(self):
+        if getattr(self, "handle", 0):
+            check(self.lib.lcx_motion_instance_destroy(self.handle), "lcx_motion_instance_destroy")
             self.handle = 0
 
     def __del__(self):

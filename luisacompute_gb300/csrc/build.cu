@@ -512,8 +512,13 @@ __global__ void __launch_bounds__(kPrepBlock) k_inst_prep(const InstState *inst,
     if (i < n) {
         const InstState &s = inst[i];
         float m[12], w[12];
+        const MotionDesc *md = s.motion;
+        if (md != nullptr) {  // a motion instance: keyframe 0 stands in (its w2o is not used)
+            for (int k = 0; k < 12; k++) m[k] = md->keys[k];
+        } else {
 #pragma unroll
-        for (int k = 0; k < 12; k++) m[k] = s.o2w[k];
+            for (int k = 0; k < 12; k++) m[k] = s.o2w[k];
+        }
         affine_inverse(m, w);
 #pragma unroll
         for (int k = 0; k < 12; k++) w2o[12ull * i + k] = w[k];
@@ -521,22 +526,31 @@ __global__ void __launch_bounds__(kPrepBlock) k_inst_prep(const InstState *inst,
         const BlasDesc *d = s.blas;
         if (d != nullptr && (d->valid & 1u)) {
             const float blo[3] = {d->lo[0], d->lo[1], d->lo[2]}, bhi[3] = {d->hi[0], d->hi[1], d->hi[2]};
-            float wl[3], wh[3];
+            float wl[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, wh[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            // a static instance: its matrix; a motion instance: the union over its keyframes,
+            // which bounds the linear interpolation of the matrices (a point moves along the
+            // segment between its keyframe positions), padded for the FP32 interpolation
+            const uint32_t nkey = md != nullptr ? md->count : 1u;
+            const float rel = md != nullptr ? 0x1p-17f : 0x1p-20f;
+            for (uint32_t key = 0; key < nkey; key++) {
+                if (md != nullptr)
+                    for (int k = 0; k < 12; k++) m[k] = md->keys[12ull * key + k];
 #pragma unroll
-            for (int k = 0; k < 3; k++) {
-                // interval arithmetic on the affine map, then an outward pad
-                // that covers the FP32 rounding of the sums
-                float a = m[4 * k + 3], b = m[4 * k + 3], mag = fabsf(m[4 * k + 3]);
+                for (int k = 0; k < 3; k++) {
+                    // interval arithmetic on the affine map, then an outward pad
+                    // that covers the FP32 rounding of the sums
+                    float a = m[4 * k + 3], b = m[4 * k + 3], mag = fabsf(m[4 * k + 3]);
 #pragma unroll
-                for (int j = 0; j < 3; j++) {
-                    const float e0 = m[4 * k + j] * blo[j], e1 = m[4 * k + j] * bhi[j];
-                    a += fminf(e0, e1);
-                    b += fmaxf(e0, e1);
-                    mag += fmaxf(fabsf(e0), fabsf(e1));
+                    for (int j = 0; j < 3; j++) {
+                        const float e0 = m[4 * k + j] * blo[j], e1 = m[4 * k + j] * bhi[j];
+                        a += fminf(e0, e1);
+                        b += fmaxf(e0, e1);
+                        mag += fmaxf(fabsf(e0), fabsf(e1));
+                    }
+                    const float pad = mag * rel;
+                    wl[k] = fminf(wl[k], a - pad);
+                    wh[k] = fmaxf(wh[k], b + pad);
                 }
-                const float pad = mag * 0x1p-20f;
-                wl[k] = a - pad;
-                wh[k] = b + pad;
             }
             l = make_float4(wl[0], wl[1], wl[2], 0.0f);
             h = make_float4(wh[0], wh[1], wh[2], 0.0f);
@@ -1065,7 +1079,15 @@ __device__ __forceinline__ InstRec make_inst_rec(uint32_t id, const InstState *i
     r.tris = ok ? d->tris : nullptr;
     r.fnodes = ok ? d->fnodes : nullptr;
     r.inst_id = id;
-    r.mask = !ok ? 0u : (d->valid & 2u) ? (((s.mask & 0xffu) << 8) | kInstProcedural) : (s.mask & 0xffu);
+    r.mask = !ok                ? 0u
+             : (d->valid & 2u)  ? (((s.mask & 0xffu) << 8) | kInstProcedural)
+             : s.motion != nullptr ? (((s.mask & 0xffu) << 8) | kInstMotion)
+                                   : (s.mask & 0xffu);
+    if (ok && s.motion != nullptr) {  // the MotionDesc address instead of an inverse
+        const unsigned long long a = reinterpret_cast<unsigned long long>(s.motion);
+        r.w2o[0] = __uint_as_float(uint32_t(a));
+        r.w2o[1] = __uint_as_float(uint32_t(a >> 32));
+    }
     return r;
 }
 
@@ -1088,7 +1110,10 @@ __global__ void k_apply_mods(const ModRec *mods, uint32_t count, InstState *inst
     if (m.index >= instance_count) return;  // validated on the host
     InstState &s = inst[m.index];
     // Modification flags: include/luisa/runtime/rhi/command.h:537-543
-    if (m.flags & 1u) s.blas = reinterpret_cast<const BlasDesc *>(m.primitive);
+    if (m.flags & 1u) {
+        s.blas = reinterpret_cast<const BlasDesc *>(m.primitive);
+        s.motion = reinterpret_cast<const MotionDesc *>(m.motion);
+    }
     if (m.flags & 2u)
         for (int k = 0; k < 12; k++) s.o2w[k] = m.affine[k];
     if (m.flags & 4u) s.opaque = 1u;
@@ -1107,7 +1132,8 @@ __global__ void k_init_instances(InstState *inst, uint32_t begin, uint32_t end) 
     s.mask = 0xffu;  // default visibility (accel.rs:289)
     s.user_id = 0;
     s.opaque = 1u;
-    s._pad[0] = s._pad[1] = s._pad[2] = 0;
+    s._pad0 = 0;
+    s.motion = nullptr;
     inst[i] = s;
 }
 

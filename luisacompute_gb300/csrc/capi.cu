@@ -6,6 +6,8 @@
 // CPU: src/rust/luisa_compute_backend_impl/src/cpu/stream.rs:410-428), with
 // status codes in place of the reference's aborts.
 #include <algorithm>
+#include <cmath>
+#include <unordered_set>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -126,14 +128,16 @@ std::shared_mutex g_life_mtx;
 
 struct Retired {
     std::vector<std::shared_ptr<DevBlock>> blocks;
+    std::vector<std::shared_ptr<void>> others;  // motion instances an accel let go of
     ~Retired() {
-        if (blocks.empty()) return;
+        if (blocks.empty() && others.empty()) return;
         // a barrier, not a critical section: once the exclusive lock has been held, every
         // trace that looked up these blocks has enqueued its kernel; the wait for those
         // kernels and the frees happen outside it, so traces on other objects go on
         { std::unique_lock<std::shared_mutex> lk(g_life_mtx); }
         cudaDeviceSynchronize();
         blocks.clear();
+        others.clear();
     }
 };
 
@@ -155,12 +159,35 @@ struct MeshObj {
     std::mutex mtx;
 };
 
+// A motion instance (MotionInstance, include/luisa/runtime/rtx/motion_instance.h):
+// a child mesh moved by matrix keyframes; device memory holds the keyframes
+// and the MotionDesc that TLAS records point to.  Accels that instance it hold
+// a reference, so the memory outlives them; `alive` and `generation` make
+// their traces fail once it is destroyed or its keyframes are rebuilt.
+struct MotionObj {
+    uint64_t child = 0;  // mesh handle
+    LcxMotionOption opt{};
+    std::vector<float> keys;  // keyframe_count x 12 (row-major 3x4 object-to-world)
+    void *mem = nullptr;      // MotionDesc (32 B) + keys
+    MotionDesc *d_md = nullptr;
+    bool built = false;
+    std::atomic<bool> alive{true};
+    uint64_t generation = 0;
+    std::mutex mtx;
+    ~MotionObj() {
+        if (mem) cudaFree(mem);
+    }
+};
+
 struct AccelObj {
     LcxAccelOption opt{};
     int device = 0;
     InstState *d_inst = nullptr;
     uint32_t inst_cap = 0, inst_count = 0;
     std::vector<uint64_t> inst_mesh;  // mesh handle per instance (0 = none)
+    std::vector<std::shared_ptr<MotionObj>> inst_motion;  // motion instance per instance (null = static)
+    std::vector<std::pair<std::shared_ptr<MotionObj>, uint64_t>> motion_gens;  // at the TLAS build
+    bool has_motion = false;
     std::vector<uint64_t> uniq_mesh;  // the distinct nonzero handles of inst_mesh
     bool uniq_dirty = true;           // inst_mesh changed since uniq_mesh was made
     std::shared_ptr<DevBlock> block;
@@ -193,6 +220,12 @@ std::shared_ptr<AccelObj> find_accel(uint64_t h) {
     auto it = g_accels.find(h);
     return it == g_accels.end() ? nullptr : it->second;
 }
+std::unordered_map<uint64_t, std::shared_ptr<MotionObj>> g_motions;
+std::shared_ptr<MotionObj> find_motion(uint64_t h) {
+    std::lock_guard<std::mutex> lk(g_reg_mtx);
+    auto it = g_motions.find(h);
+    return it == g_motions.end() ? nullptr : it->second;
+}
 
 // Bumped (after the change) by every mesh build, refit and destroy, so a trace
 // over an accel whose meshes did not change skips the per-mesh lookups.
@@ -213,6 +246,12 @@ bool meshes_current(AccelObj *a, uint64_t *stale = nullptr, bool *destroyed = nu
             return false;
         }
     }
+    for (const auto &mg : a->motion_gens)
+        if (!mg.first->alive.load() || mg.first->generation != mg.second) {
+            if (stale) *stale = 0;
+            if (destroyed) *destroyed = !mg.first->alive.load();
+            return false;
+        }
     a->checked_epoch = epoch;
     return true;
 }
@@ -707,6 +746,7 @@ int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, u
     p.tlas_q = a->qn;
     p.tlas_f = a->fn;
     p.insts = a->recs;
+    p.motion = a->has_motion;
     p.rays = reinterpret_cast<const Ray *>(d_rays);
     p.hits = reinterpret_cast<Hit *>(d_hits);
     p.ray_count = ray_count;
@@ -945,6 +985,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     // translate and validate the modifications
     std::vector<ModRec> recs(mod_count);
     std::vector<uint64_t> new_mesh(mod_count, 0);
+    std::vector<std::shared_ptr<MotionObj>> new_motion(mod_count);
     for (size_t i = 0; i < mod_count; i++) {
         const LcxModification &md = mods[i];
         if (md.index >= instance_count)
@@ -957,14 +998,25 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
         r.vis_mask = md.vis_mask;
         std::memcpy(r.affine, md.affine, sizeof(r.affine));
         r.primitive = 0;
-        r._pad = 0;
+        r.motion = 0;
         if (md.flags & LCX_MOD_PRIMITIVE) {
-            auto m = find_mesh(md.primitive);
-            if (!m) return fail(LCX_ERR_INVALID_ARG, "modification %zu: unknown mesh handle %llu", i,
-                                (unsigned long long)md.primitive);
+            uint64_t mesh = md.primitive;
+            auto m = find_mesh(mesh);
+            if (!m) {  // a motion instance: its mesh, moved by its keyframes
+                auto mo = find_motion(md.primitive);
+                if (!mo) return fail(LCX_ERR_INVALID_ARG, "modification %zu: unknown mesh handle %llu", i,
+                                     (unsigned long long)md.primitive);
+                if (!mo->built) return fail(LCX_ERR_NOT_BUILT, "motion instance not built");
+                mesh = mo->child;
+                m = find_mesh(mesh);
+                if (!m) return fail(LCX_ERR_INVALID_ARG, "modification %zu: the motion instance's mesh was destroyed",
+                                    i);
+                r.motion = reinterpret_cast<uint64_t>(mo->d_md);
+                new_motion[i] = std::move(mo);
+            }
             if (!m->built) return fail(LCX_ERR_NOT_BUILT, "Mesh not built");  // accel.rs:356-358
             r.primitive = reinterpret_cast<uint64_t>(m->d_desc);
-            new_mesh[i] = md.primitive;
+            new_mesh[i] = mesh;
         }
     }
     // instance storage
@@ -985,13 +1037,25 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     if (instance_count != a->inst_count) a->uniq_dirty = true;
     a->inst_mesh.resize(instance_count, 0);
     for (uint32_t i = a->inst_count; i < instance_count; i++) a->inst_mesh[i] = 0;
+    for (size_t i = instance_count; i < a->inst_motion.size(); i++)  // queued traces may still read it
+        if (a->inst_motion[i]) retired.others.push_back(std::move(a->inst_motion[i]));
+    a->inst_motion.resize(instance_count);
     a->inst_count = instance_count;
+    bool motion_changed = false;
     for (size_t i = 0; i < mod_count; i++)
         if (new_mesh[i]) {
             a->inst_mesh[recs[i].index] = new_mesh[i];
+            auto &slot = a->inst_motion[recs[i].index];
+            if (slot || new_motion[i]) motion_changed = true;
+            if (slot) retired.others.push_back(std::move(slot));
+            slot = std::move(new_motion[i]);
             a->uniq_dirty = true;
             a->pending_rebuild = true;  // as cuda_accel.cpp:184-185: a primitive change forces a rebuild
         }
+    if (motion_changed) {
+        a->has_motion = false;
+        for (const auto &mo : a->inst_motion) a->has_motion = a->has_motion || mo != nullptr;
+    }
     if (mod_count) {
         ScratchHolder hold(st);
         ModRec *d_mods = nullptr;
@@ -1023,6 +1087,15 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
         }
     }
     const uint32_t n = instance_count;
+    std::vector<std::pair<std::shared_ptr<MotionObj>, uint64_t>> mgens;
+    if (a->has_motion) {
+        std::unordered_set<MotionObj *> seen;
+        for (const auto &mo : a->inst_motion) {
+            if (!mo || !seen.insert(mo.get()).second) continue;
+            if (!mo->alive.load()) return fail(LCX_ERR_INVALID_ARG, "an instance references a destroyed motion instance");
+            mgens.emplace_back(mo, mo->generation);
+        }
+    }
 
     // PREFER_UPDATE of an accel created with allow_update, built with the same
     // instance count and no instance primitive changed since (the rebuild rules
@@ -1037,6 +1110,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
                             a->recs, tb->counters, ds->refit_ctl, st),
                  "TLAS refit");
         a->mesh_gens = gens;
+        a->motion_gens = mgens;
         a->checked_epoch = 0;
         a->max_blas_depth = max_blas_depth;
         a->refits++;
@@ -1106,6 +1180,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     a->block = block;
     // remember which mesh builds this TLAS references
     a->mesh_gens = gens;
+    a->motion_gens = mgens;
     a->checked_epoch = 0;
     a->max_blas_depth = max_blas_depth;
     a->built_instances = n;
@@ -1196,7 +1271,8 @@ static uint32_t trace_slot(DeviceState *ds, cudaStream_t st) {
 }
 
 static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
-                        uint8_t *d_occ, uint32_t *d_counts, uint32_t layout, void *stream) {
+                        uint8_t *d_occ, uint32_t *d_counts, uint32_t layout, void *stream,
+                        const float *d_times = nullptr) {
     if (layout > LCX_NODES_QUANT8) return fail(LCX_ERR_INVALID_ARG, "invalid node layout %u", layout);
     std::shared_lock<std::shared_mutex> life(g_life_mtx);  // until the kernel is enqueued
     auto a = find_accel(accel);
@@ -1227,7 +1303,11 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
         p.tlas_q = a->qn;
         p.tlas_f = a->fn;
         p.insts = a->recs;
+        p.motion = a->has_motion;
     }
+    p.times = d_times;
+    if (d_times && reinterpret_cast<uintptr_t>(d_times) % 4 != 0)
+        return fail(LCX_ERR_INVALID_ARG, "times must be 4-byte aligned");
     DeviceState *ds = nullptr;
     if (int r = current_device_state(&ds)) return r;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -1278,6 +1358,8 @@ int lcx_accel_device_view(uint64_t accel, LcxAccelView *out) {
     if (!a->built) return fail(LCX_ERR_NOT_BUILT, "accel not built");
     if (!meshes_current(a.get()))
         return fail(LCX_ERR_NOT_BUILT, "a mesh of the accel was destroyed, rebuilt or refit; rebuild the accel");
+    if (a->has_motion)
+        return fail(LCX_ERR_INVALID_ARG, "lcx::ray_query does not trace motion instances");
     const uint32_t need = a->depth + a->max_blas_depth + 3;
     if (int(need) > kStackSize)
         return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the query stack (%d)", a->depth,
@@ -1310,6 +1392,9 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
         if (!meshes_current(a.get()))
             return fail(LCX_ERR_NOT_BUILT, "job %u: a mesh of the accel was destroyed or rebuilt; rebuild the accel",
                         i);
+        if (a->has_motion)
+            return fail(LCX_ERR_INVALID_ARG, "job %u: accels with motion instances are traced with "
+                                             "lcx_trace_closest_motion / lcx_trace_any_motion", i);
         const uint32_t need = a->depth + a->max_blas_depth + 3;
         if (int(need) > kStackSize) return fail(LCX_ERR_DEPTH, "job %u: BVH too deep for the traversal stack", i);
         depth_need = std::max(depth_need, need);
@@ -1544,6 +1629,103 @@ static int trace_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count, 
         if (x) cudaEventDestroy(x);  // released once completed
     if (status != LCX_OK) return status;
     if (first != cudaSuccess) return cuda_fail(first, "host-buffer trace");
+    return LCX_OK;
+}
+
+int lcx_trace_closest_motion(uint64_t accel, const LcxRay *d_rays, const float *d_times, uint32_t ray_count,
+                             uint32_t mask, LcxTriangleHit *d_hits, uint32_t node_layout, void *stream) {
+    if (!d_hits && ray_count) return fail(LCX_ERR_INVALID_ARG, "hits buffer is null");
+    return trace_common(accel, d_rays, ray_count, mask, d_hits, nullptr, nullptr, node_layout, stream, d_times);
+}
+
+int lcx_trace_any_motion(uint64_t accel, const LcxRay *d_rays, const float *d_times, uint32_t ray_count, uint32_t mask,
+                         uint8_t *d_occluded, uint32_t node_layout, void *stream) {
+    if (!d_occluded && ray_count) return fail(LCX_ERR_INVALID_ARG, "occluded buffer is null");
+    return trace_common(accel, d_rays, ray_count, mask, nullptr, d_occluded, nullptr, node_layout, stream, d_times);
+}
+
+int lcx_motion_instance_create(uint64_t mesh, const LcxMotionOption *option, uint64_t *out_handle) {
+    if (!option || !out_handle) return fail(LCX_ERR_INVALID_ARG, "lcx_motion_instance_create: null argument");
+    const LcxMotionOption &o = *option;
+    if (o.keyframe_count < 2) return fail(LCX_ERR_INVALID_ARG, "a motion instance needs at least 2 keyframes");
+    if (o.keyframe_count > (1u << 16)) return fail(LCX_ERR_INVALID_ARG, "too many keyframes (%u)", o.keyframe_count);
+    if (!(o.time_end > o.time_start) || !std::isfinite(o.time_start) || !std::isfinite(o.time_end))
+        return fail(LCX_ERR_INVALID_ARG, "motion time range must be finite with time_end > time_start");
+    if (o.mode != LCX_MOTION_MATRIX)
+        return fail(LCX_ERR_INVALID_ARG, "only matrix keyframes are supported (SRT keyframes are not)");
+    auto m = find_mesh(mesh);
+    if (!m) return fail(LCX_ERR_INVALID_ARG, "lcx_motion_instance_create: unknown mesh handle %llu",
+                        (unsigned long long)mesh);
+    if (m->kind != kSegTriangles) return fail(LCX_ERR_INVALID_ARG, "motion instances of procedural primitives are not supported");
+    auto mo = std::make_shared<MotionObj>();
+    mo->child = mesh;
+    mo->opt = o;
+    mo->keys.assign(size_t(o.keyframe_count) * 12, 0.0f);
+    for (uint32_t k = 0; k < o.keyframe_count; k++) {  // identity keyframes
+        mo->keys[12 * k + 0] = 1.0f;
+        mo->keys[12 * k + 5] = 1.0f;
+        mo->keys[12 * k + 10] = 1.0f;
+    }
+    LCX_CUDA(cudaMalloc(&mo->mem, sizeof(MotionDesc) + sizeof(float) * mo->keys.size()), "cudaMalloc(motion)");
+    mo->d_md = static_cast<MotionDesc *>(mo->mem);
+    const uint64_t h = g_next_handle.fetch_add(1);
+    {
+        std::lock_guard<std::mutex> lk(g_reg_mtx);
+        g_motions.emplace(h, std::move(mo));
+    }
+    *out_handle = h;
+    return LCX_OK;
+}
+
+int lcx_motion_instance_destroy(uint64_t handle) {
+    std::shared_ptr<MotionObj> mo;
+    {
+        std::unique_lock<std::shared_mutex> life(g_life_mtx);  // traces that found it have enqueued
+        std::lock_guard<std::mutex> lk(g_reg_mtx);
+        auto it = g_motions.find(handle);
+        if (it == g_motions.end()) return fail(LCX_ERR_INVALID_ARG, "lcx_motion_instance_destroy: unknown handle %llu",
+                                               (unsigned long long)handle);
+        mo = it->second;
+        g_motions.erase(it);
+        mo->alive.store(false);
+        bump_mesh_epoch();
+    }
+    // accels that instance it keep its memory until they let go of it
+    cudaDeviceSynchronize();
+    mo.reset();
+    return LCX_OK;
+}
+
+int lcx_motion_instance_set_keyframes(uint64_t handle, const float *matrices, uint32_t count) {
+    auto mo = find_motion(handle);
+    if (!mo) return fail(LCX_ERR_INVALID_ARG, "unknown motion instance handle %llu", (unsigned long long)handle);
+    if (!matrices || count != mo->opt.keyframe_count)
+        return fail(LCX_ERR_INVALID_ARG, "expected %u keyframes", mo->opt.keyframe_count);
+    std::lock_guard<std::mutex> lk(mo->mtx);
+    mo->keys.assign(matrices, matrices + size_t(count) * 12);
+    return LCX_OK;
+}
+
+int lcx_motion_instance_build(uint64_t handle, void *stream) {
+    auto mo = find_motion(handle);
+    if (!mo) return fail(LCX_ERR_INVALID_ARG, "unknown motion instance handle %llu", (unsigned long long)handle);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (capturing(st)) return fail(LCX_ERR_INVALID_ARG, "a motion instance build cannot be captured (host keyframes)");
+    std::lock_guard<std::mutex> lk(mo->mtx);
+    MotionDesc md{};
+    md.keys = reinterpret_cast<const float *>(reinterpret_cast<char *>(mo->mem) + sizeof(MotionDesc));
+    md.count = mo->opt.keyframe_count;
+    md.t0 = mo->opt.time_start;
+    md.t1 = mo->opt.time_end;
+    md.flags = (mo->opt.vanish_start ? 1u : 0u) | (mo->opt.vanish_end ? 2u : 0u);
+    // pageable sources: the calls return once the data has been staged
+    LCX_CUDA(cudaMemcpyAsync(mo->mem, &md, sizeof(md), cudaMemcpyHostToDevice, st), "motion upload");
+    LCX_CUDA(cudaMemcpyAsync(const_cast<float *>(md.keys), mo->keys.data(), sizeof(float) * mo->keys.size(),
+                             cudaMemcpyHostToDevice, st),
+             "motion upload");
+    mo->built = true;
+    mo->generation++;  // accels over it must be built again (their boxes bound the keyframes)
+    bump_mesh_epoch();
     return LCX_OK;
 }
 

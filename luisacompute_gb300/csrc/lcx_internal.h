@@ -175,6 +175,8 @@ struct TraceParams {
     uint32_t job_count;
     const uint32_t *order;  // non-null: the k-th ray taken is rays[order[k]] (single-job launches)
     uint32_t short_stack;   // shared-memory stack entries per thread: 8, 16 or 24 (single-job, mode 0)
+    bool motion;            // the accel has motion instances: the motion kernels (mode 0) run the call
+    const float *times;     // motion launches: per-ray times (null: time 0)
 };
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st);
 

@@ -60,7 +60,7 @@ constexpr uint32_t kMaxRaySteps = 1u << 22;  // per-ray bound: a corrupt tree en
 // Per-lane traversal state and the operations both loop structures share.
 // kMulti: the launch serves several jobs (scenes); each lane takes its job's
 // TLAS, instance table, mask and buffers when it takes a ray.
-template <int kLayout, bool kAny, bool kCount, bool kMulti, int kShort>
+template <int kLayout, bool kAny, bool kCount, bool kMulti, int kShort, bool kMotion = false>
 struct Walker {
     static constexpr int kShortStack = kShort < kStackSize ? kShort : kStackSize;
     static constexpr int kDeep = kStackSize - kShortStack;    // entries in local memory
@@ -77,6 +77,7 @@ struct Walker {
     // world ray
     float wox = 0, woy = 0, woz = 0, wdx = 0, wdy = 0, wdz = 1;
     float tmin = 0, best_t = 0, best_u = 0, best_v = 0;
+    float time = 0;  // motion launches: the ray's time
     uint32_t best_inst = kInvalid, best_prim = kInvalid;
     // current-space ray (world at the TLAS level, object inside a BLAS)
     float ox = 0, oy = 0, oz = 0, ix = 1, iy = 1, iz = 1;
@@ -152,6 +153,7 @@ struct Walker {
         wdy = r1.y;
         wdz = r1.z;
         best_t = r1.w;
+        if (kMotion) time = P.times != nullptr ? __ldg(P.times + slot) : 0.0f;
         best_u = best_v = 0.0f;
         best_inst = best_prim = kInvalid;
         to_world();
@@ -327,14 +329,38 @@ struct Walker {
             Gt.y &= Gt.y - 1u;
             const uint4 *ip = reinterpret_cast<const uint4 *>((kMulti ? insts : P.insts) + Gt.x + k);
             const uint4 m4 = bvh_ld(ip + 4);  // fnodes (x,y), inst_id (z), mask (w)
-            if ((m4.w & (kMulti ? mask : P.mask)) == 0u) continue;
-            const float4 r0 = bvh_ld(reinterpret_cast<const float4 *>(ip));
-            const float4 r1 = bvh_ld(reinterpret_cast<const float4 *>(ip + 1));
-            const float4 r2 = bvh_ld(reinterpret_cast<const float4 *>(ip + 2));
+            float w[12];
+            if constexpr (!kMotion) {
+                if ((m4.w & (kMulti ? mask : P.mask)) == 0u) continue;
+                const float4 r0 = bvh_ld(reinterpret_cast<const float4 *>(ip));
+                const float4 r1 = bvh_ld(reinterpret_cast<const float4 *>(ip + 1));
+                const float4 r2 = bvh_ld(reinterpret_cast<const float4 *>(ip + 2));
+                w[0] = r0.x, w[1] = r0.y, w[2] = r0.z, w[3] = r0.w;
+                w[4] = r1.x, w[5] = r1.y, w[6] = r1.z, w[7] = r1.w;
+                w[8] = r2.x, w[9] = r2.y, w[10] = r2.z, w[11] = r2.w;
+            } else {  // a motion instance: the matrix at the ray's time, inverted as a static one is
+                uint32_t vis = m4.w;
+                const bool moving = (vis & (kInstMotion | kInstProcedural)) == kInstMotion;
+                if (moving) vis = (vis >> 8) & 0xffu;
+                if ((vis & (kMulti ? mask : P.mask)) == 0u) continue;
+                const float4 r0 = bvh_ld(reinterpret_cast<const float4 *>(ip));
+                const float4 r1 = bvh_ld(reinterpret_cast<const float4 *>(ip + 1));
+                const float4 r2 = bvh_ld(reinterpret_cast<const float4 *>(ip + 2));
+                w[0] = r0.x, w[1] = r0.y, w[2] = r0.z, w[3] = r0.w;
+                w[4] = r1.x, w[5] = r1.y, w[6] = r1.z, w[7] = r1.w;
+                w[8] = r2.x, w[9] = r2.y, w[10] = r2.z, w[11] = r2.w;
+                if (moving) {
+                    const MotionDesc *md = reinterpret_cast<const MotionDesc *>(
+                        (unsigned long long)__float_as_uint(r0.x) |
+                        ((unsigned long long)__float_as_uint(r0.y) << 32));
+                    float m[12];
+                    if (!motion_matrix(*md, time, m)) continue;  // vanished at this time
+                    affine_inverse(m, w);
+                }
+            }
             const uint4 pp = bvh_ld(ip + 3);  // qnodes (x,y), tris (z,w)
             if (Gt.y) push(Gt);
             if (G.y) push(G);
-            const float w[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
             float dx, dy, dz;
             transform_point(w, wox, woy, woz, ox, oy, oz);
             transform_dir(w, wdx, wdy, wdz, dx, dy, dz);
@@ -390,11 +416,11 @@ struct Walker {
 // kMode 1: speculative while-while (Aila & Laine 2009): lanes walk nodes
 // together; a lane that finds items keeps walking (holding them in Gp) while
 // any lane of the warp is still searching, then all lanes handle items.
-template <int kLayout, bool kAny, bool kCount, int kMode, bool kMulti, int kShort>
+template <int kLayout, bool kAny, bool kCount, int kMode, bool kMulti, int kShort, bool kMotion = false>
 __global__ void __launch_bounds__(kTraceBlock,
                                   kLayout == LCX_NODES_QUANT8 ? LCX_TRACE_MIN_BLOCKS_Q : LCX_TRACE_MIN_BLOCKS_F)
     k_trace(TraceParams P) {
-    using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort>;
+    using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort, kMotion>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
     __shared__ unsigned long long coop_keys[kTraceBlock];  // per owner lane: min (ordered t, prim)
     __shared__ float2 coop_uv[kTraceBlock];                 // per owner lane: barycentrics of that minimum
@@ -844,12 +870,12 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
     }
 }
 
-template <int L, bool A, bool C, int M, bool X, int S>
+template <int L, bool A, bool C, int M, bool X, int S, bool Mo = false>
 int blocks_per_sm() {
     static int v = 0;
     if (v == 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<L, A, C, M, X, S>, kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<L, A, C, M, X, S, Mo>, kTraceBlock, 0);
         v = b > 0 ? b : 1;
     }
     return v;
@@ -866,14 +892,14 @@ int sm_count() {
     return v;
 }
 
-template <int L, bool A, bool C, int M, bool X = false, int S = kDefaultShortStack>
+template <int L, bool A, bool C, int M, bool X = false, int S = kDefaultShortStack, bool Mo = false>
 cudaError_t launch_one(const TraceParams &p, cudaStream_t st) {
     const uint64_t warps_needed = (uint64_t(p.ray_count) + 31) / 32;
-    uint64_t grid = uint64_t(sm_count()) * blocks_per_sm<L, A, C, M, X, S>();
+    uint64_t grid = uint64_t(sm_count()) * blocks_per_sm<L, A, C, M, X, S, Mo>();
     const uint64_t grid_need = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
     if (grid_need < grid) grid = grid_need;
     if (grid == 0) grid = 1;
-    k_trace<L, A, C, M, X, S><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
+    k_trace<L, A, C, M, X, S, Mo><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -919,6 +945,16 @@ cudaError_t launch_mode(const TraceParams &p, int layout, bool any, bool countin
 }  // namespace
 
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
+    if (p.motion) {  // accels with motion instances: loop mode 0 with per-ray times
+        if (layout == LCX_NODES_QUANT8) {
+            if (counting) return launch_one<LCX_NODES_QUANT8, false, true, 0, false, kDefaultShortStack, true>(p, st);
+            return any ? launch_one<LCX_NODES_QUANT8, true, false, 0, false, kDefaultShortStack, true>(p, st)
+                       : launch_one<LCX_NODES_QUANT8, false, false, 0, false, kDefaultShortStack, true>(p, st);
+        }
+        if (counting) return launch_one<LCX_NODES_FP32, false, true, 0, false, kDefaultShortStack, true>(p, st);
+        return any ? launch_one<LCX_NODES_FP32, true, false, 0, false, kDefaultShortStack, true>(p, st)
+                   : launch_one<LCX_NODES_FP32, false, false, 0, false, kDefaultShortStack, true>(p, st);
+    }
     if (p.jobs != nullptr) {  // multi-job launches: no counting; mode 2 with quantised nodes, else mode 0
         if (p.mode == 2 && layout == LCX_NODES_QUANT8)
             return any ? launch_deferred<LCX_NODES_QUANT8, true, LCX_DEFER_STACK, true>(p, st)

@@ -57,6 +57,8 @@ def load():
         lib.lcxo_fp64_closest.argtypes = [c_void_p, c_void_p, c_size_t, c_uint32, c_void_p, c_void_p, c_int]
         lib.lcxo_fp64_eval.argtypes = [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p]
         lib.lcxo_affine_inverse.argtypes = [c_void_p, c_void_p]
+        lib.lcxo_trace_motion.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_uint32, c_int,
+                                          c_void_p, c_void_p, c_int]
         lib.lcxo_pathtrace.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]
         lib.lcxo_intersect_triangle.restype = c_int
         lib.lcxo_intersect_triangle.argtypes = [c_void_p, c_void_p, c_float, c_float, c_void_p, c_void_p, c_void_p,
@@ -67,6 +69,11 @@ def load():
 
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(c_void_p)
+
+
+class LcxoMotion(ctypes.Structure):
+    _fields_ = [("keys", ctypes.POINTER(ctypes.c_float)), ("count", ctypes.c_uint32), ("t0", ctypes.c_float),
+                ("t1", ctypes.c_float), ("flags", ctypes.c_uint32)]
 
 
 class OracleScene:
@@ -107,6 +114,28 @@ class OracleScene:
         hits = np.zeros(rays.shape[0], HIT_DTYPE)
         self.lib.lcxo_brute_closest(self.accel, _ptr(rays), rays.shape[0], mask, _ptr(hits), threads)
         return hits
+
+    def trace_motion(self, rays: np.ndarray, times: np.ndarray, motion: list, mask: int = 0xFF, any_hit: bool = False,
+                     threads: int = 0):
+        """Rays with per-ray times over the scene whose instance i moves by motion[i] = (keys (k, 12)
+        float32, t0, t1, flags) or stays static (None); lcxo_trace_motion."""
+        from luisacompute_gb300.scenes import HIT_DTYPE
+        import ctypes
+        rays = np.ascontiguousarray(rays)
+        times = np.ascontiguousarray(times, np.float32)
+        arr = (LcxoMotion * len(motion))()
+        keep = []
+        for i, mo in enumerate(motion):
+            if mo is None:
+                continue
+            keys = np.ascontiguousarray(mo[0], np.float32).reshape(-1, 12)
+            keep.append(keys)
+            arr[i] = LcxoMotion(keys.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), keys.shape[0], mo[1], mo[2], mo[3])
+        hits = np.zeros(rays.shape[0], HIT_DTYPE)
+        occ = np.zeros(rays.shape[0], np.uint8)
+        self.lib.lcxo_trace_motion(self.accel, arr, _ptr(rays), _ptr(times), rays.shape[0], mask, int(any_hit),
+                                   _ptr(hits), _ptr(occ), threads)
+        return occ if any_hit else hits
 
     def trace_any(self, rays: np.ndarray, mask: int = 0xFF, threads: int = 0) -> np.ndarray:
         rays = np.ascontiguousarray(rays)

@@ -823,6 +823,56 @@ void lcxo_pathtrace(const void *accel, const float *const *albedo, const LcxoPtP
 
 void lcxo_affine_inverse(const float *o2w, float *w2o) { affine_inverse_f32(o2w, w2o); }
 
+// include/lcx/bvh_device.cuh motion_matrix, operation for operation
+static bool motion_matrix_f32(const LcxoMotion &md, float time, float m[12]) {
+    if ((md.flags & 1u) && time < md.t0) return false;
+    if ((md.flags & 2u) && time > md.t1) return false;
+    float u = (time - md.t0) / (md.t1 - md.t0);
+    u = u >= 0.0f ? (u <= 1.0f ? u : 1.0f) : 0.0f;
+    const float x = u * float(md.count - 1u);
+    uint32_t i = uint32_t(std::floor(x));
+    if (i > md.count - 2u) i = md.count - 2u;
+    const float f = x - float(i);
+    const float *k0 = md.keys + 12 * size_t(i), *k1 = k0 + 12;
+    for (int k = 0; k < 12; k++) m[k] = std::fma(f, k1[k] - k0[k], k0[k]);
+    return true;
+}
+
+void lcxo_trace_motion(const void *accel, const LcxoMotion *motion, const LcxoRay *rays, const float *times,
+                       size_t n, uint32_t mask, int any, LcxoHit *hits, uint8_t *occluded, int threads) {
+    const Accel &a = *static_cast<const Accel *>(accel);
+    parallel_rays(n, threads, [&](size_t r) {
+        const LcxoRay &ray = rays[r];
+        LcxoHit best{kInvalid, kInvalid, 0.0f, 0.0f, ray.tmax, 0};
+        bool occ = false;
+        for (uint32_t id = 0; id < a.mesh.size() && !occ; id++) {
+            const Mesh *m = a.mesh[id];
+            if (!m || (a.mask[id] & mask) == 0u) continue;
+            float w[12];
+            const float *wp = &a.w2o[12 * size_t(id)];
+            if (motion[id].keys != nullptr) {
+                float mm[12];
+                if (!motion_matrix_f32(motion[id], times[r], mm)) continue;
+                affine_inverse_f32(mm, w);
+                wp = w;
+            }
+            float oo[3], od[3];
+            transform_ray_f32(wp, ray.o, ray.d, oo, od);
+            if (any) {
+                if (trace_mesh<true>(*m, id, oo, od, ray.tmin, best)) occ = true;
+            } else {
+                trace_mesh<false>(*m, id, oo, od, ray.tmin, best);
+            }
+        }
+        if (any) {
+            occluded[r] = occ ? 1 : 0;
+        } else {
+            if (best.inst == kInvalid) best = LcxoHit{kInvalid, kInvalid, 0.0f, 0.0f, ray.tmax, 0};
+            hits[r] = best;
+        }
+    });
+}
+
 int lcxo_intersect_triangle(const float *o, const float *d, float tmin, float tmax, const float *v0, const float *v1,
                             const float *v2, float *t, float *u, float *v) {
     WtRay wr;

@@ -102,6 +102,21 @@ void lcxo_pathtrace(const void *accel, const float *const *albedo, const LcxoPtP
 
 /* The FP32 operation sequences the GPU kernels must reproduce bit for bit. */
 void lcxo_affine_inverse(const float *o2w, float *w2o);
+
+/* Motion instances (the product's matrix keyframes): instance i moves when
+ * motion[i].keys is non-null -- `count` row-major 3x4 object-to-world
+ * matrices over [t0, t1]; flags bit 0 / 1: vanish before t0 / after t1.  The
+ * interpolation restates motion_matrix of include/lcx/bvh_device.cuh with the
+ * same FP32 sequence; the inverse is affine_inverse_f32.  Every instance is
+ * tested (no TLAS), each through its mesh BVH.  times: one per ray. */
+typedef struct LcxoMotion {
+    const float *keys;
+    uint32_t count;
+    float t0, t1;
+    uint32_t flags;
+} LcxoMotion;
+void lcxo_trace_motion(const void *accel, const LcxoMotion *motion, const LcxoRay *rays, const float *times,
+                       size_t n, uint32_t mask, int any, LcxoHit *hits, uint8_t *occluded, int threads);
 int lcxo_intersect_triangle(const float *o, const float *d, float tmin, float tmax,
                             const float *v0, const float *v1, const float *v2, float *t,
                             float *u, float *v);

@@ -1,0 +1,123 @@
+"""Motion instances (MotionInstance, include/luisa/runtime/rtx/motion_instance.h; the DSL's
+intersect_motion / intersect_any_motion with a time per ray, include/luisa/dsl/rtx/accel.h:47-48).
+
+Matrix keyframes are interpolated per element at each ray's time and inverted with the static
+instances' FP32 sequence; the oracle restates both (lcxo_trace_motion), so the records must be the
+same bit for bit, for times inside, before and after the motion range (clamped, or vanished when
+the motion asks for it) and NaN times."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from luisacompute_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _keyframes(rng, k, spread=1.0):
+    return S.affine_rows(S.random_rotations(k, rng), rng.uniform(0.2, 0.5, k), rng.uniform(-spread, spread, (k, 3)))
+
+
+def _setup(rng, allow_update=False):
+    import torch
+    from luisacompute_gb300.accel import Accel, AccelOption, MotionInstance, mesh_from_data
+    datas = [S.icosphere(3), S.displaced_mesh(3_000, rng), S.grid_mesh(20, 20)]
+    meshes = [mesh_from_data(d).build() for d in datas]
+    n_static, n_motion = 5, 7
+    inst_mesh = np.array([i % 3 for i in range(n_static + n_motion)])
+    aff = _keyframes(rng, n_static + n_motion)
+    motion_specs = [None] * n_static
+    motions = []
+    for j in range(n_motion):
+        k = 2 + j % 3
+        keys = _keyframes(rng, k)
+        t0, t1 = (0.0, 1.0) if j % 2 == 0 else (0.25, 0.75)
+        flags = j % 4  # bit 0: vanish before, bit 1: vanish after
+        mo = MotionInstance(meshes[inst_mesh[n_static + j]], keys.reshape(-1, 3, 4), t0, t1,
+                            vanish_start=bool(flags & 1), vanish_end=bool(flags & 2))
+        motions.append(mo)
+        motion_specs.append((keys, t0, t1, flags))
+    acc = Accel(AccelOption(allow_update=allow_update))
+    for i in range(n_static):
+        acc.emplace_back(meshes[inst_mesh[i]], aff[i].reshape(3, 4))
+    for j, mo in enumerate(motions):
+        acc.emplace_back(mo)
+    acc.build()
+    torch.cuda.synchronize()
+    scene = S.Scene(datas, inst_mesh, aff, np.full(n_static + n_motion, 0xFF, np.uint32))
+    return scene, acc, meshes, motions, motion_specs
+
+
+def _rays_times(rng, n, seed):
+    rays = S.sphere_rays(n, [-1.5] * 3, [1.5] * 3, seed=seed)
+    times = rng.uniform(-0.3, 1.3, n).astype(np.float32)
+    times[:16] = np.nan
+    times[16:32] = [0.0, 1.0, 0.25, 0.75] * 4
+    return rays, times
+
+
+def test_motion_instances_match_oracle(lcx, oracle_mod):
+    import torch
+    from luisacompute_gb300.accel import hits_to_numpy, rays_to_device
+    rng = np.random.default_rng(51)
+    scene, acc, meshes, motions, specs = _setup(rng)
+    osc = oracle_mod.OracleScene(scene)
+    rays, times = _rays_times(rng, 60_000, 52)
+    want = osc.trace_motion(rays, times, specs)
+    want_any = osc.trace_motion(rays, times, specs, any_hit=True)
+    assert (want["inst"] >= 5).sum() > 500 and (want["inst"] < 5).sum() > 500  # moving and static hits
+    d_rays, d_times = rays_to_device(rays), torch.from_numpy(times).cuda()
+    for layout in (0, 1):
+        got = hits_to_numpy(acc.trace_closest_motion(d_rays, d_times, layout=layout))
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), layout
+        occ = acc.trace_any_motion(d_rays, d_times, layout=layout).cpu().numpy()
+        assert np.array_equal(occ, want_any), layout
+    # calls without times (and the plain trace calls) use time 0
+    zero = osc.trace_motion(rays, np.zeros(rays.shape[0], np.float32), specs)
+    for got in (acc.trace_closest_motion(d_rays), acc.trace_closest(d_rays)):
+        assert np.array_equal(hits_to_numpy(got).view(np.uint8), zero.view(np.uint8))
+    # a static-only result differs: the motion moved something
+    assert not np.array_equal(want.view(np.uint8), zero.view(np.uint8))
+    from luisacompute_gb300 import _capi
+    _capi.check(lcx.lcx_check_trace_errors(), "trace errors")
+
+
+def test_motion_keyframe_rebuild_refit_and_errors(lcx, oracle_mod):
+    import torch
+    from luisacompute_gb300 import _capi
+    from luisacompute_gb300.accel import REQUEST_PREFER_UPDATE, hits_to_numpy, rays_to_device
+    rng = np.random.default_rng(53)
+    scene, acc, meshes, motions, specs = _setup(rng, allow_update=True)
+    rays, times = _rays_times(rng, 30_000, 54)
+    d_rays, d_times = rays_to_device(rays), torch.from_numpy(times).cuda()
+    # new keyframes: traces of the accel fail until it is built again; a refit takes them
+    keys = _keyframes(rng, motions[2].keys.shape[0])
+    motions[2].set_keyframes(keys.reshape(-1, 3, 4))
+    motions[2].build()
+    specs[5 + 2] = (keys, specs[5 + 2][1], specs[5 + 2][2], specs[5 + 2][3])
+    with pytest.raises(_capi.LcxError):
+        acc.trace_closest_motion(d_rays, d_times)
+    acc.build(request=REQUEST_PREFER_UPDATE)
+    assert acc.stats().refits == 1
+    want = oracle_mod.OracleScene(scene).trace_motion(rays, times, specs)
+    got = hits_to_numpy(acc.trace_closest_motion(d_rays, d_times))
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    # what motion accels cannot do
+    v = _capi.LcxAccelView()
+    assert lcx.lcx_accel_device_view(acc.handle, ctypes.byref(v)) == _capi.LCX_ERR_INVALID_ARG
+    out = torch.empty((16, 6), dtype=torch.int32, device="cuda")
+    job = (_capi.LcxTraceJob * 1)(_capi.LcxTraceJob(acc.handle, d_rays.data_ptr(), out.data_ptr(), 16, 0xFF, 0, 0))
+    assert lcx.lcx_trace_jobs(job, 1, 1, None) == _capi.LCX_ERR_INVALID_ARG
+    h = ctypes.c_uint64(0)
+    for opt in (_capi.LcxMotionOption(1, 0.0, 1.0, 0, 0, 0, 0), _capi.LcxMotionOption(2, 1.0, 1.0, 0, 0, 0, 0),
+                _capi.LcxMotionOption(2, 0.0, 1.0, 0, 0, _capi.LCX_MOTION_SRT, 0)):
+        assert lcx.lcx_motion_instance_create(meshes[0].handle, ctypes.byref(opt), ctypes.byref(h)) == \
+            _capi.LCX_ERR_INVALID_ARG
+    assert lcx.lcx_motion_instance_set_keyframes(motions[0].handle, keys.ctypes.data, 99) == _capi.LCX_ERR_INVALID_ARG
+    # a destroyed motion instance: the accel's traces fail (its memory stays with the accel)
+    motions[1].destroy()
+    with pytest.raises(_capi.LcxError):
+        acc.trace_closest_motion(d_rays, d_times)
+    with pytest.raises(_capi.LcxError):
+        acc.build()
