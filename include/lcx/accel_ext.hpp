@@ -131,6 +131,22 @@ public:
         check(lcx_procedural_destroy(handle), "destroy_procedural_primitive");
     }
 
+    // device_interface.h create_motion_instance: a mesh moved by matrix keyframes (row-major 3x4 each)
+    [[nodiscard]] ResourceCreationInfo create_motion_instance(uint64_t mesh, const LcxMotionOption &option,
+                                                              const std::vector<std::array<float, 12>> &keyframes,
+                                                              void *stream) const {
+        ResourceCreationInfo info;
+        check(lcx_motion_instance_create(mesh, &option, &info.handle), "create_motion_instance");
+        check(lcx_motion_instance_set_keyframes(info.handle, keyframes.empty() ? nullptr : keyframes[0].data(),
+                                                uint32_t(keyframes.size())),
+              "MotionInstance::set_keyframes");
+        check(lcx_motion_instance_build(info.handle, stream), "MotionInstance::build");
+        return info;
+    }
+    void destroy_motion_instance(uint64_t handle) const {
+        check(lcx_motion_instance_destroy(handle), "destroy_motion_instance");
+    }
+
     [[nodiscard]] ResourceCreationInfo create_accel(const AccelOption &option) const {
         const LcxAccelOption o = option.c();
         ResourceCreationInfo info;
@@ -195,6 +211,15 @@ public:
     void trace_any_host(uint64_t accel, const Ray *rays, uint32_t n, uint32_t mask, uint8_t *occluded, void *stream,
                         uint32_t layout = LCX_NODES_QUANT8) const {
         check(lcx_trace_any_host(accel, rays, n, mask, occluded, layout, stream), "trace_any_host");
+    }
+    // Accel::intersect_motion / intersect_any_motion: a time per ray (device array, null = 0).
+    void trace_closest_motion(uint64_t accel, const Ray *rays, const float *times, uint32_t n, uint32_t mask,
+                              TriangleHit *hits, void *stream, uint32_t layout = LCX_NODES_QUANT8) const {
+        check(lcx_trace_closest_motion(accel, rays, times, n, mask, hits, layout, stream), "trace_closest_motion");
+    }
+    void trace_any_motion(uint64_t accel, const Ray *rays, const float *times, uint32_t n, uint32_t mask,
+                          uint8_t *occluded, void *stream, uint32_t layout = LCX_NODES_QUANT8) const {
+        check(lcx_trace_any_motion(accel, rays, times, n, mask, occluded, layout, stream), "trace_any_motion");
     }
     // Ray batches of many jobs (accels, closest or any) in one launch per kind.
     void trace_jobs(const std::vector<LcxTraceJob> &jobs, void *stream, uint32_t layout = LCX_NODES_QUANT8) const {
