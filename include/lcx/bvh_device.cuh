@@ -123,11 +123,16 @@ struct __align__(16) InstRec {
 };
 static_assert(sizeof(InstRec) == 80, "InstRec is 80 B");
 
-// Motion of a motion instance (matrix keyframes; AccelOption::Motion,
-// include/luisa/runtime/rhi/resource.h:105-117): `count` row-major 3x4
-// object-to-world matrices spaced evenly over [t0, t1], interpolated linearly
-// per element.  flags bit 0: the instance vanishes before t0 (else the time is
-// clamped), bit 1: after t1.
+// Motion of a motion instance (AccelOption::Motion,
+// include/luisa/runtime/rhi/resource.h:101-118): `count` keyframes spaced
+// evenly over [t0, t1].  Matrix mode: row-major 3x4 object-to-world matrices
+// (12 floats each), interpolated linearly per element.  SRT mode (flags bit
+// 2): the reference's MotionInstanceTransformSRT (16 floats: pivot xyz,
+// quaternion xyzw, scale xyz, shear xyz, translation xyz), every component
+// interpolated linearly and the quaternion normalised, composed as
+// M = T R S with S = [[sx, sh0, sh1, px], [0, sy, sh2, py], [0, 0, sz, pz]].
+// flags bit 0: the instance vanishes before t0 (else the time is clamped),
+// bit 1: after t1.
 struct __align__(16) MotionDesc {
     const float *keys;
     uint32_t count;
@@ -213,6 +218,41 @@ __device__ __forceinline__ void affine_inverse(const float *m, float *w) {
 // instance has vanished at that time.  Segment and fraction:
 // u = (time - t0) / (t1 - t0) clamped to [0, 1] (NaN -> 0), x = u (count - 1),
 // i = min(floor(x), count - 2), f = x - i; element k = fma(f, K1[k] - K0[k], K0[k]).
+// SRT mode: M = T R S from an interpolated SRT record (16 floats).  The
+// quaternion is normalised by 1 / sqrt(|q|^2); a zero quaternion gives NaN
+// (the instance is then missed), as an invalid rotation would anywhere.
+__device__ __forceinline__ void srt_matrix(const float *v, float m[12]) {
+    const float px = v[0], py = v[1], pz = v[2];
+    float qx = v[3], qy = v[4], qz = v[5], qw = v[6];
+    const float sx = v[7], sy = v[8], sz = v[9], a = v[10], b = v[11], c = v[12];
+    const float tx = v[13], ty = v[14], tz = v[15];
+    const float n2 = __fmaf_rn(qx, qx, __fmaf_rn(qy, qy, __fmaf_rn(qz, qz, __fmul_rn(qw, qw))));
+    const float rn = __fdiv_rn(1.0f, __fsqrt_rn(n2));
+    qx = __fmul_rn(qx, rn);
+    qy = __fmul_rn(qy, rn);
+    qz = __fmul_rn(qz, rn);
+    qw = __fmul_rn(qw, rn);
+    const float xx = __fmul_rn(qx, qx), yy = __fmul_rn(qy, qy), zz = __fmul_rn(qz, qz);
+    const float xy = __fmul_rn(qx, qy), xz = __fmul_rn(qx, qz), yz = __fmul_rn(qy, qz);
+    const float wx = __fmul_rn(qw, qx), wy = __fmul_rn(qw, qy), wz = __fmul_rn(qw, qz);
+    const float R[9] = {
+        __fsub_rn(1.0f, __fmul_rn(2.0f, __fadd_rn(yy, zz))), __fmul_rn(2.0f, __fsub_rn(xy, wz)),
+        __fmul_rn(2.0f, __fadd_rn(xz, wy)),
+        __fmul_rn(2.0f, __fadd_rn(xy, wz)), __fsub_rn(1.0f, __fmul_rn(2.0f, __fadd_rn(xx, zz))),
+        __fmul_rn(2.0f, __fsub_rn(yz, wx)),
+        __fmul_rn(2.0f, __fsub_rn(xz, wy)), __fmul_rn(2.0f, __fadd_rn(yz, wx)),
+        __fsub_rn(1.0f, __fmul_rn(2.0f, __fadd_rn(xx, yy)))};
+    // S columns: (sx, 0, 0), (a, sy, 0), (b, c, sz), (px, py, pz)
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        const float r0 = R[3 * r], r1 = R[3 * r + 1], r2 = R[3 * r + 2];
+        m[4 * r + 0] = __fmul_rn(r0, sx);
+        m[4 * r + 1] = __fmaf_rn(r0, a, __fmul_rn(r1, sy));
+        m[4 * r + 2] = __fmaf_rn(r0, b, __fmaf_rn(r1, c, __fmul_rn(r2, sz)));
+        m[4 * r + 3] = __fadd_rn(__fmaf_rn(r0, px, __fmaf_rn(r1, py, __fmul_rn(r2, pz))), r == 0 ? tx : (r == 1 ? ty : tz));
+    }
+}
+
 __device__ __forceinline__ bool motion_matrix(const MotionDesc &md, float time, float m[12]) {
     if ((md.flags & 1u) && time < md.t0) return false;
     if ((md.flags & 2u) && time > md.t1) return false;
@@ -221,6 +261,14 @@ __device__ __forceinline__ bool motion_matrix(const MotionDesc &md, float time, 
     const float x = __fmul_rn(u, float(md.count - 1u));
     const uint32_t i = min(uint32_t(floorf(x)), md.count - 2u);
     const float f = __fsub_rn(x, float(i));
+    if (md.flags & 4u) {  // SRT keyframes
+        const float *k0 = md.keys + 16ull * i, *k1 = k0 + 16;
+        float v[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) v[k] = __fmaf_rn(f, __fsub_rn(k1[k], k0[k]), k0[k]);
+        srt_matrix(v, m);
+        return true;
+    }
     const float *k0 = md.keys + 12ull * i, *k1 = k0 + 12;
 #pragma unroll
     for (int k = 0; k < 12; k++) m[k] = __fmaf_rn(f, __fsub_rn(k1[k], k0[k]), k0[k]);

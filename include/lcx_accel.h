@@ -256,8 +256,14 @@ LCX_API int lcx_accel_stats(uint64_t accel, LcxAccelStats *out);
  * keyframe_count >= 2 keyframes spaced evenly over [time_start, time_end]
  * (time_end > time_start); a ray time before time_start (after time_end)
  * makes the instance vanish if vanish_start (vanish_end) is set, else it is
- * clamped.  Only LCX_MOTION_MATRIX keyframes are supported (the reference's
- * SRT mode is not: interpolated rotations need swept bounds). */
+ * clamped.  LCX_MOTION_MATRIX keyframes are row-major 3x4 object-to-world
+ * matrices (12 floats), interpolated per element; LCX_MOTION_SRT keyframes
+ * are the reference's MotionInstanceTransformSRT (16 floats: pivot xyz,
+ * quaternion xyzw, scale xyz, shear xyz, translation xyz;
+ * include/luisa/runtime/rtx/motion_transform.h:13-19), every component
+ * interpolated linearly and the quaternion normalised, composed as
+ * T * R * S with S = [[sx, shear0, shear1, px], [0, sy, shear2, py],
+ * [0, 0, sz, pz]]. */
 enum { LCX_MOTION_MATRIX = 0, LCX_MOTION_SRT = 1 };
 typedef struct LcxMotionOption {
     uint32_t keyframe_count;
@@ -265,7 +271,7 @@ typedef struct LcxMotionOption {
     float time_end;
     uint8_t vanish_start;
     uint8_t vanish_end;
-    uint8_t mode;        /* LCX_MOTION_MATRIX */
+    uint8_t mode;        /* LCX_MOTION_MATRIX or LCX_MOTION_SRT */
     uint8_t _pad;
 } LcxMotionOption;
 
@@ -279,9 +285,10 @@ typedef struct LcxMotionOption {
  * fail until they are built again.  No CPU-backend counterpart. */
 LCX_API int lcx_motion_instance_create(uint64_t mesh, const LcxMotionOption *option, uint64_t *out_handle);
 LCX_API int lcx_motion_instance_destroy(uint64_t motion_instance);
-/* `count` (== keyframe_count) row-major 3x4 object-to-world matrices, host
- * memory (MotionInstance::set_keyframes with the reference's float4x4
- * matrices, packed as Modification::set_transform packs them). */
+/* `count` (== keyframe_count) keyframes in host memory: 12 floats each
+ * (LCX_MOTION_MATRIX: the reference's float4x4 matrices packed as
+ * Modification::set_transform packs them) or 16 (LCX_MOTION_SRT)
+ * (MotionInstance::set_keyframes). */
 LCX_API int lcx_motion_instance_set_keyframes(uint64_t motion_instance, const float *matrices, uint32_t count);
 /* Uploads the keyframes on `stream` (MotionInstance::build). */
 LCX_API int lcx_motion_instance_build(uint64_t motion_instance, void *stream);

@@ -364,12 +364,13 @@ class MotionInstance:
     (``trace_closest_motion``)."""
 
     def __init__(self, mesh: Mesh, keyframes, time_start: float = 0.0, time_end: float = 1.0,
-                 vanish_start: bool = False, vanish_end: bool = False, stream=None):
+                 vanish_start: bool = False, vanish_end: bool = False, stream=None, srt: bool = False):
         self.lib = _capi.load()
         self.mesh = mesh
-        keys = np.stack([_as_affine(k) for k in keyframes])
+        self.srt = srt  # keyframes are 16-float SRT records (pivot, quaternion, scale, shear, translation)
+        keys = self._pack(keyframes)
         opt = _capi.LcxMotionOption(keys.shape[0], time_start, time_end, int(vanish_start), int(vanish_end),
-                                    _capi.LCX_MOTION_MATRIX, 0)
+                                    _capi.LCX_MOTION_SRT if srt else _capi.LCX_MOTION_MATRIX, 0)
         h = ctypes.c_uint64(0)
         check(self.lib.lcx_motion_instance_create(mesh.handle, ctypes.byref(opt), ctypes.byref(h)),
               "lcx_motion_instance_create")
@@ -377,8 +378,13 @@ class MotionInstance:
         self.set_keyframes(keys)
         self.build(stream)
 
+    def _pack(self, keyframes) -> np.ndarray:
+        if self.srt:
+            return np.ascontiguousarray(np.asarray(keyframes, np.float32).reshape(-1, 16))
+        return np.ascontiguousarray(np.stack([_as_affine(k) for k in keyframes]), np.float32)
+
     def set_keyframes(self, keyframes):
-        keys = np.ascontiguousarray(np.stack([_as_affine(k) for k in keyframes]), np.float32)
+        keys = self._pack(keyframes)
         check(self.lib.lcx_motion_instance_set_keyframes(self.handle, keys.ctypes.data, keys.shape[0]),
               "lcx_motion_instance_set_keyframes")
         self.keys = keys

@@ -513,8 +513,12 @@ __global__ void __launch_bounds__(kPrepBlock) k_inst_prep(const InstState *inst,
         const InstState &s = inst[i];
         float m[12], w[12];
         const MotionDesc *md = s.motion;
+        const bool srt = md != nullptr && (md->flags & 4u);
         if (md != nullptr) {  // a motion instance: keyframe 0 stands in (its w2o is not used)
-            for (int k = 0; k < 12; k++) m[k] = md->keys[k];
+            if (srt)
+                srt_matrix(md->keys, m);
+            else
+                for (int k = 0; k < 12; k++) m[k] = md->keys[k];
         } else {
 #pragma unroll
             for (int k = 0; k < 12; k++) m[k] = s.o2w[k];
@@ -530,8 +534,44 @@ __global__ void __launch_bounds__(kPrepBlock) k_inst_prep(const InstState *inst,
             // a static instance: its matrix; a motion instance: the union over its keyframes,
             // which bounds the linear interpolation of the matrices (a point moves along the
             // segment between its keyframe positions), padded for the FP32 interpolation
-            const uint32_t nkey = md != nullptr ? md->count : 1u;
+            const uint32_t nkey = srt ? 0u : (md != nullptr ? md->count : 1u);
             const float rel = md != nullptr ? 0x1p-17f : 0x1p-20f;
+            // SRT keyframes, per segment: S (scale, shear, pivot; linear in the keyframe
+            // values) maps the BLAS box into the union of its two keyframe boxes; any
+            // rotation keeps that within the ball of its largest corner distance; the
+            // translation moves along the segment between its keyframe values
+            for (uint32_t seg = 0; srt && seg + 1 < md->count; seg++) {
+                float sl[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, sh[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+                float tl[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, th[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+                for (uint32_t e = 0; e < 2; e++) {
+                    const float *v = md->keys + 16ull * (seg + e);
+                    // rows of S: (sx, a, b | px), (0, sy, c | py), (0, 0, sz | pz)
+                    const float S[12] = {v[7], v[10], v[11], v[0], 0.0f, v[8], v[12], v[1], 0.0f, 0.0f, v[9], v[2]};
+                    for (int k = 0; k < 3; k++) {
+                        float a = S[4 * k + 3], b = S[4 * k + 3];
+                        for (int j = 0; j < 3; j++) {
+                            const float e0 = S[4 * k + j] * blo[j], e1 = S[4 * k + j] * bhi[j];
+                            a += fminf(e0, e1);
+                            b += fmaxf(e0, e1);
+                        }
+                        sl[k] = fminf(sl[k], a);
+                        sh[k] = fmaxf(sh[k], b);
+                        tl[k] = fminf(tl[k], v[13 + k]);
+                        th[k] = fmaxf(th[k], v[13 + k]);
+                    }
+                }
+                float r2 = 0.0f;
+                for (int k = 0; k < 3; k++) {
+                    const float c = fmaxf(fabsf(sl[k]), fabsf(sh[k]));
+                    r2 += c * c;
+                }
+                const float r = sqrtf(r2) * (1.0f + 0x1p-16f);
+                for (int k = 0; k < 3; k++) {
+                    const float pad = (r + fmaxf(fabsf(tl[k]), fabsf(th[k]))) * 0x1p-17f;
+                    wl[k] = fminf(wl[k], tl[k] - r - pad);
+                    wh[k] = fmaxf(wh[k], th[k] + r + pad);
+                }
+            }
             for (uint32_t key = 0; key < nkey; key++) {
                 if (md != nullptr)
                     for (int k = 0; k < 12; k++) m[k] = md->keys[12ull * key + k];

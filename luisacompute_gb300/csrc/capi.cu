@@ -1651,8 +1651,8 @@ int lcx_motion_instance_create(uint64_t mesh, const LcxMotionOption *option, uin
     if (o.keyframe_count > (1u << 16)) return fail(LCX_ERR_INVALID_ARG, "too many keyframes (%u)", o.keyframe_count);
     if (!(o.time_end > o.time_start) || !std::isfinite(o.time_start) || !std::isfinite(o.time_end))
         return fail(LCX_ERR_INVALID_ARG, "motion time range must be finite with time_end > time_start");
-    if (o.mode != LCX_MOTION_MATRIX)
-        return fail(LCX_ERR_INVALID_ARG, "only matrix keyframes are supported (SRT keyframes are not)");
+    if (o.mode != LCX_MOTION_MATRIX && o.mode != LCX_MOTION_SRT)
+        return fail(LCX_ERR_INVALID_ARG, "motion mode must be LCX_MOTION_MATRIX or LCX_MOTION_SRT");
     auto m = find_mesh(mesh);
     if (!m) return fail(LCX_ERR_INVALID_ARG, "lcx_motion_instance_create: unknown mesh handle %llu",
                         (unsigned long long)mesh);
@@ -1660,11 +1660,16 @@ int lcx_motion_instance_create(uint64_t mesh, const LcxMotionOption *option, uin
     auto mo = std::make_shared<MotionObj>();
     mo->child = mesh;
     mo->opt = o;
-    mo->keys.assign(size_t(o.keyframe_count) * 12, 0.0f);
+    const size_t per = o.mode == LCX_MOTION_SRT ? 16 : 12;
+    mo->keys.assign(size_t(o.keyframe_count) * per, 0.0f);
     for (uint32_t k = 0; k < o.keyframe_count; k++) {  // identity keyframes
-        mo->keys[12 * k + 0] = 1.0f;
-        mo->keys[12 * k + 5] = 1.0f;
-        mo->keys[12 * k + 10] = 1.0f;
+        float *v = &mo->keys[per * k];
+        if (per == 16) {  // pivot 0, quaternion (0,0,0,1), scale 1, shear 0, translation 0
+            v[6] = 1.0f;
+            v[7] = v[8] = v[9] = 1.0f;
+        } else {
+            v[0] = v[5] = v[10] = 1.0f;
+        }
     }
     LCX_CUDA(cudaMalloc(&mo->mem, sizeof(MotionDesc) + sizeof(float) * mo->keys.size()), "cudaMalloc(motion)");
     mo->d_md = static_cast<MotionDesc *>(mo->mem);
@@ -1702,7 +1707,7 @@ int lcx_motion_instance_set_keyframes(uint64_t handle, const float *matrices, ui
     if (!matrices || count != mo->opt.keyframe_count)
         return fail(LCX_ERR_INVALID_ARG, "expected %u keyframes", mo->opt.keyframe_count);
     std::lock_guard<std::mutex> lk(mo->mtx);
-    mo->keys.assign(matrices, matrices + size_t(count) * 12);
+    mo->keys.assign(matrices, matrices + size_t(count) * (mo->opt.mode == LCX_MOTION_SRT ? 16 : 12));
     return LCX_OK;
 }
 
@@ -1717,7 +1722,8 @@ int lcx_motion_instance_build(uint64_t handle, void *stream) {
     md.count = mo->opt.keyframe_count;
     md.t0 = mo->opt.time_start;
     md.t1 = mo->opt.time_end;
-    md.flags = (mo->opt.vanish_start ? 1u : 0u) | (mo->opt.vanish_end ? 2u : 0u);
+    md.flags = (mo->opt.vanish_start ? 1u : 0u) | (mo->opt.vanish_end ? 2u : 0u) |
+               (mo->opt.mode == LCX_MOTION_SRT ? 4u : 0u);
     // pageable sources: the calls return once the data has been staged
     LCX_CUDA(cudaMemcpyAsync(mo->mem, &md, sizeof(md), cudaMemcpyHostToDevice, st), "motion upload");
     LCX_CUDA(cudaMemcpyAsync(const_cast<float *>(md.keys), mo->keys.data(), sizeof(float) * mo->keys.size(),

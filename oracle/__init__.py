@@ -117,8 +117,9 @@ class OracleScene:
 
     def trace_motion(self, rays: np.ndarray, times: np.ndarray, motion: list, mask: int = 0xFF, any_hit: bool = False,
                      threads: int = 0):
-        """Rays with per-ray times over the scene whose instance i moves by motion[i] = (keys (k, 12)
-        float32, t0, t1, flags) or stays static (None); lcxo_trace_motion."""
+        """Rays with per-ray times over the scene whose instance i moves by motion[i] = (keys (k, 12),
+        or (k, 16) SRT records with flags bit 2, float32, t0, t1, flags) or stays static (None);
+        lcxo_trace_motion."""
         from luisacompute_gb300.scenes import HIT_DTYPE
         import ctypes
         rays = np.ascontiguousarray(rays)
@@ -128,7 +129,7 @@ class OracleScene:
         for i, mo in enumerate(motion):
             if mo is None:
                 continue
-            keys = np.ascontiguousarray(mo[0], np.float32).reshape(-1, 12)
+            keys = np.ascontiguousarray(mo[0], np.float32).reshape(-1, 16 if mo[3] & 4 else 12)
             keep.append(keys)
             arr[i] = LcxoMotion(keys.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), keys.shape[0], mo[1], mo[2], mo[3])
         hits = np.zeros(rays.shape[0], HIT_DTYPE)

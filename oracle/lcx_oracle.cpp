@@ -823,6 +823,33 @@ void lcxo_pathtrace(const void *accel, const float *const *albedo, const LcxoPtP
 
 void lcxo_affine_inverse(const float *o2w, float *w2o) { affine_inverse_f32(o2w, w2o); }
 
+// include/lcx/bvh_device.cuh srt_matrix, operation for operation
+static void srt_matrix_f32(const float *v, float m[12]) {
+    const float px = v[0], py = v[1], pz = v[2];
+    float qx = v[3], qy = v[4], qz = v[5], qw = v[6];
+    const float sx = v[7], sy = v[8], sz = v[9], a = v[10], b = v[11], c = v[12];
+    const float tx = v[13], ty = v[14], tz = v[15];
+    const float n2 = std::fma(qx, qx, std::fma(qy, qy, std::fma(qz, qz, qw * qw)));
+    const float rn = 1.0f / std::sqrt(n2);
+    qx = qx * rn;
+    qy = qy * rn;
+    qz = qz * rn;
+    qw = qw * rn;
+    const float xx = qx * qx, yy = qy * qy, zz = qz * qz;
+    const float xy = qx * qy, xz = qx * qz, yz = qy * qz;
+    const float wx = qw * qx, wy = qw * qy, wz = qw * qz;
+    const float R[9] = {1.0f - 2.0f * (yy + zz), 2.0f * (xy - wz), 2.0f * (xz + wy),
+                        2.0f * (xy + wz), 1.0f - 2.0f * (xx + zz), 2.0f * (yz - wx),
+                        2.0f * (xz - wy), 2.0f * (yz + wx), 1.0f - 2.0f * (xx + yy)};
+    for (int r = 0; r < 3; r++) {
+        const float r0 = R[3 * r], r1 = R[3 * r + 1], r2 = R[3 * r + 2];
+        m[4 * r + 0] = r0 * sx;
+        m[4 * r + 1] = std::fma(r0, a, r1 * sy);
+        m[4 * r + 2] = std::fma(r0, b, std::fma(r1, c, r2 * sz));
+        m[4 * r + 3] = std::fma(r0, px, std::fma(r1, py, r2 * pz)) + (r == 0 ? tx : (r == 1 ? ty : tz));
+    }
+}
+
 // include/lcx/bvh_device.cuh motion_matrix, operation for operation
 static bool motion_matrix_f32(const LcxoMotion &md, float time, float m[12]) {
     if ((md.flags & 1u) && time < md.t0) return false;
@@ -833,6 +860,13 @@ static bool motion_matrix_f32(const LcxoMotion &md, float time, float m[12]) {
     uint32_t i = uint32_t(std::floor(x));
     if (i > md.count - 2u) i = md.count - 2u;
     const float f = x - float(i);
+    if (md.flags & 4u) {  // SRT records
+        const float *k0 = md.keys + 16 * size_t(i), *k1 = k0 + 16;
+        float v[16];
+        for (int k = 0; k < 16; k++) v[k] = std::fma(f, k1[k] - k0[k], k0[k]);
+        srt_matrix_f32(v, m);
+        return true;
+    }
     const float *k0 = md.keys + 12 * size_t(i), *k1 = k0 + 12;
     for (int k = 0; k < 12; k++) m[k] = std::fma(f, k1[k] - k0[k], k0[k]);
     return true;

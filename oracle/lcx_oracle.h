@@ -105,9 +105,10 @@ void lcxo_affine_inverse(const float *o2w, float *w2o);
 
 /* Motion instances (the product's matrix keyframes): instance i moves when
  * motion[i].keys is non-null -- `count` row-major 3x4 object-to-world
- * matrices over [t0, t1]; flags bit 0 / 1: vanish before t0 / after t1.  The
- * interpolation restates motion_matrix of include/lcx/bvh_device.cuh with the
- * same FP32 sequence; the inverse is affine_inverse_f32.  Every instance is
+ * matrices over [t0, t1] (flags bit 2: SRT records of 16 floats instead);
+ * flags bit 0 / 1: vanish before t0 / after t1.  The interpolation restates
+ * motion_matrix and srt_matrix of include/lcx/bvh_device.cuh with the same
+ * FP32 sequence; the inverse is affine_inverse_f32.  Every instance is
  * tested (no TLAS), each through its mesh BVH.  times: one per ray. */
 typedef struct LcxoMotion {
     const float *keys;

@@ -4,7 +4,7 @@ intersect_motion / intersect_any_motion with a time per ray, include/luisa/dsl/r
 Matrix keyframes are interpolated per element at each ray's time and inverted with the static
 instances' FP32 sequence; the oracle restates both (lcxo_trace_motion), so the records must be the
 same bit for bit, for times inside, before and after the motion range (clamped, or vanished when
-the motion asks for it) and NaN times."""
+the motion asks for it) and NaN times, with matrix and SRT keyframes."""
 import ctypes
 
 import numpy as np
@@ -111,7 +111,7 @@ def test_motion_keyframe_rebuild_refit_and_errors(lcx, oracle_mod):
     assert lcx.lcx_trace_jobs(job, 1, 1, None) == _capi.LCX_ERR_INVALID_ARG
     h = ctypes.c_uint64(0)
     for opt in (_capi.LcxMotionOption(1, 0.0, 1.0, 0, 0, 0, 0), _capi.LcxMotionOption(2, 1.0, 1.0, 0, 0, 0, 0),
-                _capi.LcxMotionOption(2, 0.0, 1.0, 0, 0, _capi.LCX_MOTION_SRT, 0)):
+                _capi.LcxMotionOption(2, 0.0, 1.0, 0, 0, 2, 0)):
         assert lcx.lcx_motion_instance_create(meshes[0].handle, ctypes.byref(opt), ctypes.byref(h)) == \
             _capi.LCX_ERR_INVALID_ARG
     assert lcx.lcx_motion_instance_set_keyframes(motions[0].handle, keys.ctypes.data, 99) == _capi.LCX_ERR_INVALID_ARG
@@ -121,3 +121,51 @@ def test_motion_keyframe_rebuild_refit_and_errors(lcx, oracle_mod):
         acc.trace_closest_motion(d_rays, d_times)
     with pytest.raises(_capi.LcxError):
         acc.build()
+
+
+def _srt_keyframes(rng, k):
+    """k SRT records: pivot, unit-ish quaternion (not normalised: the product normalises), scale,
+    shear, translation."""
+    v = np.zeros((k, 16), np.float32)
+    v[:, 0:3] = rng.uniform(-0.2, 0.2, (k, 3))
+    q = rng.normal(0.0, 1.0, (k, 4))
+    v[:, 3:7] = q * rng.uniform(0.5, 2.0, (k, 1))
+    v[:, 7:10] = rng.uniform(0.15, 0.45, (k, 3))
+    v[:, 10:13] = rng.uniform(-0.1, 0.1, (k, 3))
+    v[:, 13:16] = rng.uniform(-1.0, 1.0, (k, 3))
+    return v
+
+
+def test_srt_motion_matches_oracle(lcx, oracle_mod):
+    import torch
+    from luisacompute_gb300.accel import Accel, MotionInstance, hits_to_numpy, mesh_from_data, rays_to_device
+    rng = np.random.default_rng(55)
+    datas = [S.icosphere(3), S.displaced_mesh(2_000, rng)]
+    meshes = [mesh_from_data(d).build() for d in datas]
+    n = 10
+    inst_mesh = np.arange(n) % 2
+    specs, motions = [], []
+    acc = Accel()
+    for j in range(n):
+        keys = _srt_keyframes(rng, 2 + j % 3)
+        t0, t1 = (0.0, 1.0) if j % 2 == 0 else (0.2, 0.9)
+        flags = (j % 4) | 4
+        mo = MotionInstance(meshes[inst_mesh[j]], keys, t0, t1, vanish_start=bool(flags & 1),
+                            vanish_end=bool(flags & 2), srt=True)
+        motions.append(mo)
+        specs.append((keys, t0, t1, flags))
+        acc.emplace_back(mo)
+    acc.build()
+    scene = S.Scene(datas, inst_mesh, np.tile(S.IDENTITY, (n, 1)), np.full(n, 0xFF, np.uint32))
+    osc = oracle_mod.OracleScene(scene)
+    rays, times = _rays_times(rng, 50_000, 56)
+    want = osc.trace_motion(rays, times, specs)
+    want_any = osc.trace_motion(rays, times, specs, any_hit=True)
+    assert (want["inst"] != S.MISS).sum() > 1000
+    d_rays, d_times = rays_to_device(rays), torch.from_numpy(times).cuda()
+    for layout in (0, 1):
+        got = hits_to_numpy(acc.trace_closest_motion(d_rays, d_times, layout=layout))
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), layout
+        assert np.array_equal(acc.trace_any_motion(d_rays, d_times, layout=layout).cpu().numpy(), want_any)
+    from luisacompute_gb300 import _capi
+    _capi.check(lcx.lcx_check_trace_errors(), "trace errors")
