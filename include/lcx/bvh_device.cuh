@@ -95,6 +95,28 @@ struct __align__(16) TriRec {
 };
 static_assert(sizeof(TriRec) == 48, "TriRec is 48 B");
 
+// Vertex motion of a mesh built with a motion option (the reference's
+// keyframed vertices: the vertex buffer holds `keys` copies of the
+// `vcount` vertices back to back, include/luisa/runtime/rtx/mesh.h:137-139).
+// Keyframes span [t0, t1] evenly; vertices are interpolated linearly per
+// component at the ray's time (flags as MotionDesc: bit 0 / 1 vanish before
+// t0 / after t1).
+struct __align__(16) MeshMotion {
+    const unsigned char *vbase;
+    const unsigned char *tbase;
+    uint64_t vstride;
+    uint32_t vcount;  // vertices per keyframe
+    uint32_t keys;
+    float t0, t1;
+    uint32_t flags;
+    uint32_t _pad;
+};
+static_assert(sizeof(MeshMotion) == 48, "MeshMotion is 48 B");
+
+// TriRec of a vertex-motion mesh: v0.w = prim id, v1.w = this marker, v2.xy =
+// the mesh's MeshMotion address; the motion kernels interpolate its vertices.
+constexpr uint32_t kTriMotion = 0xffffffffu;
+
 // Device descriptor of a built BLAS (one per mesh handle, fixed address).
 struct __align__(16) BlasDesc {
     const Node8Q *qnodes;
@@ -106,7 +128,10 @@ struct __align__(16) BlasDesc {
     uint32_t depth;
     float hi[3];
     uint32_t valid;  // bit 0: built with at least one item; bit 1: procedural (AABB items)
+    const MeshMotion *motion;  // vertex motion (null: static vertices)
+    uint64_t _pad;
 };
+static_assert(sizeof(BlasDesc) == 80, "BlasDesc is 80 B");
 // InstRec.mask of a procedural instance: its visibility mask in bits 8..15 and
 // bit 31 set, so the trace kernels' test (ray mask & mask), ray masks being
 // 8 bits, never enters it; lcx::ray_query decodes it.
@@ -253,14 +278,47 @@ __device__ __forceinline__ void srt_matrix(const float *v, float m[12]) {
     }
 }
 
-__device__ __forceinline__ bool motion_matrix(const MotionDesc &md, float time, float m[12]) {
-    if ((md.flags & 1u) && time < md.t0) return false;
-    if ((md.flags & 2u) && time > md.t1) return false;
-    float u = __fdiv_rn(__fsub_rn(time, md.t0), __fsub_rn(md.t1, md.t0));
+// Keyframe segment i and fraction f of `time` over `count` keyframes on
+// [t0, t1]; false when the motion has vanished at that time.
+__device__ __forceinline__ bool motion_segment(float t0, float t1, uint32_t count, uint32_t flags, float time,
+                                               uint32_t &i, float &f) {
+    if ((flags & 1u) && time < t0) return false;
+    if ((flags & 2u) && time > t1) return false;
+    float u = __fdiv_rn(__fsub_rn(time, t0), __fsub_rn(t1, t0));
     u = u >= 0.0f ? (u <= 1.0f ? u : 1.0f) : 0.0f;
-    const float x = __fmul_rn(u, float(md.count - 1u));
-    const uint32_t i = min(uint32_t(floorf(x)), md.count - 2u);
-    const float f = __fsub_rn(x, float(i));
+    const float x = __fmul_rn(u, float(count - 1u));
+    i = min(uint32_t(floorf(x)), count - 2u);
+    f = __fsub_rn(x, float(i));
+    return true;
+}
+
+// Vertices of triangle `prim` of a vertex-motion mesh at `time` (w = prim id
+// bits in a, 0 in b and c, as a TriRec); false when vanished.  Each component
+// is fma(f, K1 - K0, K0).
+__device__ __forceinline__ bool motion_triangle(const MeshMotion &mm, uint32_t prim, float time, float4 &a, float4 &b,
+                                                float4 &c) {
+    uint32_t i;
+    float f;
+    if (!motion_segment(mm.t0, mm.t1, mm.keys, mm.flags, time, i, f)) return false;
+    const uint32_t *t = reinterpret_cast<const uint32_t *>(mm.tbase + 12ull * prim);
+    float4 *out[3] = {&a, &b, &c};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const uint64_t v = t[k];
+        const float4 p0 = __ldg(reinterpret_cast<const float4 *>(mm.vbase + mm.vstride * (uint64_t(i) * mm.vcount + v)));
+        const float4 p1 =
+            __ldg(reinterpret_cast<const float4 *>(mm.vbase + mm.vstride * (uint64_t(i + 1u) * mm.vcount + v)));
+        *out[k] = make_float4(__fmaf_rn(f, __fsub_rn(p1.x, p0.x), p0.x), __fmaf_rn(f, __fsub_rn(p1.y, p0.y), p0.y),
+                              __fmaf_rn(f, __fsub_rn(p1.z, p0.z), p0.z), 0.0f);
+    }
+    a.w = __uint_as_float(prim);
+    return true;
+}
+
+__device__ __forceinline__ bool motion_matrix(const MotionDesc &md, float time, float m[12]) {
+    uint32_t i;
+    float f;
+    if (!motion_segment(md.t0, md.t1, md.count, md.flags, time, i, f)) return false;
     if (md.flags & 4u) {  // SRT keyframes
         const float *k0 = md.keys + 16ull * i, *k1 = k0 + 16;
         float v[16];

@@ -171,6 +171,7 @@ LCX_API uint32_t lcx_version(void);
 LCX_API int lcx_mesh_create(const LcxAccelOption *option, uint64_t *out_handle);
 LCX_API int lcx_mesh_destroy(uint64_t mesh);
 
+
 /* MeshBuildCommand visit (CPU: accel.rs:205-260; CUDA: cuda_mesh.cpp:31-69).
  * Builds the BLAS on `stream`: Morton-code LBVH, collapsed to 8-wide nodes in
  * both node layouts.  Returns after enqueueing; the mesh may be used by
@@ -292,6 +293,19 @@ LCX_API int lcx_motion_instance_destroy(uint64_t motion_instance);
 LCX_API int lcx_motion_instance_set_keyframes(uint64_t motion_instance, const float *matrices, uint32_t count);
 /* Uploads the keyframes on `stream` (MotionInstance::build). */
 LCX_API int lcx_motion_instance_build(uint64_t motion_instance, void *stream);
+
+/* A mesh with keyframed vertices (AccelOption::Motion on a mesh,
+ * include/luisa/runtime/rtx/mesh.h:85-86, 127-139; the CUDA backend's motion
+ * GAS, cuda_mesh.cpp:20-22): its build commands' vertex buffers hold
+ * motion->keyframe_count copies of the vertices back to back (the vertex
+ * count must be a whole multiple), indexed by the same triangles.  Traces
+ * interpolate the three vertices of a triangle linearly at the ray's time
+ * (lcx_trace_closest_motion / lcx_trace_any_motion; other calls use time 0);
+ * vanish_start / vanish_end and the time range behave as for motion
+ * instances; motion->mode is ignored.  The vertex buffer is borrowed and read
+ * by every later trace.  allow_update is rejected (no refit). */
+LCX_API int lcx_mesh_create_motion(const LcxAccelOption *option, const LcxMotionOption *motion,
+                                   uint64_t *out_handle);
 
 /* ----------------------------------------------------------------- queries */
 

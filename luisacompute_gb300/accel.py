@@ -62,7 +62,11 @@ def _as_affine(transform) -> np.ndarray:
 class Mesh:
     """A BLAS over borrowed device vertex/triangle buffers."""
 
-    def __init__(self, vertices, triangles, option: AccelOption | None = None, vertex_stride: int | None = None):
+    def __init__(self, vertices, triangles, option: AccelOption | None = None, vertex_stride: int | None = None,
+                 motion_keyframes: int = 0, time_start: float = 0.0, time_end: float = 1.0,
+                 vanish_start: bool = False, vanish_end: bool = False):
+        """motion_keyframes >= 2: keyframed vertices (lcx_mesh_create_motion); `vertices` then holds
+        that many copies of the vertex set back to back."""
         torch = _torch()
         self.lib = _capi.load()
         self.vertices, self.triangles = vertices, triangles
@@ -75,8 +79,13 @@ class Mesh:
         if triangles.dtype not in (torch.int32, torch.uint32) or triangles.numel() % 3 != 0:
             raise ValueError("triangles must be a (T, 3) int32/uint32 tensor")
         h = ctypes.c_uint64(0)
-        check(self.lib.lcx_mesh_create(ctypes.byref((option or AccelOption()).c()), ctypes.byref(h)),
-              "lcx_mesh_create")
+        if motion_keyframes >= 2:
+            mo = _capi.LcxMotionOption(motion_keyframes, time_start, time_end, int(vanish_start), int(vanish_end), 0, 0)
+            check(self.lib.lcx_mesh_create_motion(ctypes.byref((option or AccelOption()).c()), ctypes.byref(mo),
+                                                  ctypes.byref(h)), "lcx_mesh_create_motion")
+        else:
+            check(self.lib.lcx_mesh_create(ctypes.byref((option or AccelOption()).c()), ctypes.byref(h)),
+                  "lcx_mesh_create")
         self.handle = h.value
 
     def build(self, request: int = REQUEST_FORCE_BUILD, stream=None) -> "Mesh":

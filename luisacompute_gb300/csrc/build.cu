@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(kPrepBlock) k_tri_prep(const SegInput *segs, u
         float4 l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f), h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
         uint32_t i0 = 0, i1 = 0, i2 = 0;
         bool bad = false;
-        if (g.kind == kSegAabbs) {  // the item box is the AABB record (min xyz, max xyz)
+        if ((g.kind & 0xffu) == kSegAabbs) {  // the item box is the AABB record (min xyz, max xyz)
             const float *bx = reinterpret_cast<const float *>(g.vbase + 24ull * local);
             l.x = bx[0];
             l.y = bx[1];
@@ -152,16 +152,22 @@ __global__ void __launch_bounds__(kPrepBlock) k_tri_prep(const SegInput *segs, u
         if (bad) {
             atomicOr(&segctl[kSegWords * s + kSegErr], kErrBadIndex);
             atomicOr(&ctl[kCtlErr], kErrBadIndex);
-        } else if (g.kind != kSegAabbs) {
-            const float4 a = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i0));
-            const float4 b = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i1));
-            const float4 cc = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * i2));
-            l.x = fminf(fminf(l.x, a.x), fminf(b.x, cc.x));
-            l.y = fminf(fminf(l.y, a.y), fminf(b.y, cc.y));
-            l.z = fminf(fminf(l.z, a.z), fminf(b.z, cc.z));
-            h.x = fmaxf(fmaxf(h.x, a.x), fmaxf(b.x, cc.x));
-            h.y = fmaxf(fmaxf(h.y, a.y), fmaxf(b.y, cc.y));
-            h.z = fmaxf(fmaxf(h.z, a.z), fmaxf(b.z, cc.z));
+        } else if ((g.kind & 0xffu) != kSegAabbs) {
+            // vertex motion (kind >> 8 keyframes): the union over the keyframes bounds the
+            // linearly interpolated triangle at every time
+            const uint32_t keys = max(g.kind >> 8, 1u);
+            for (uint32_t key = 0; key < keys; key++) {
+                const uint64_t kb = uint64_t(key) * g.vcount;
+                const float4 a = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * (kb + i0)));
+                const float4 b = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * (kb + i1)));
+                const float4 cc = __ldg(reinterpret_cast<const float4 *>(g.vbase + g.vstride * (kb + i2)));
+                l.x = fminf(fminf(l.x, a.x), fminf(b.x, cc.x));
+                l.y = fminf(fminf(l.y, a.y), fminf(b.y, cc.y));
+                l.z = fminf(fminf(l.z, a.z), fminf(b.z, cc.z));
+                h.x = fmaxf(fmaxf(h.x, a.x), fmaxf(b.x, cc.x));
+                h.y = fmaxf(fmaxf(h.y, a.y), fmaxf(b.y, cc.y));
+                h.z = fmaxf(fmaxf(h.z, a.z), fmaxf(b.z, cc.z));
+            }
         }
         if (box_empty(l, h)) {
             l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f);
@@ -1070,10 +1076,18 @@ __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *d
             const SegInput &g = segs[s];
             // a reference of a split build names its triangle (local index of the mesh)
             const uint32_t prim = ref_prim != nullptr ? ref_prim[g.item_offset + item] : item;
-            if (g.kind == kSegAabbs) {
+            if ((g.kind & 0xffu) == kSegAabbs) {
                 const float *bx = reinterpret_cast<const float *>(g.vbase + 24ull * prim);
                 tris[pos] = TriRec{make_float4(bx[0], bx[1], bx[2], __uint_as_float(prim)),
                                    make_float4(bx[3], bx[4], bx[5], 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
+                return;
+            }
+            if (g.kind >> 8) {  // vertex motion: the motion kernels interpolate the vertices at the ray's time
+                const unsigned long long mp = reinterpret_cast<unsigned long long>(g.desc->motion);
+                tris[pos] = TriRec{make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(prim)),
+                                   make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kTriMotion)),
+                                   make_float4(__uint_as_float(uint32_t(mp)), __uint_as_float(uint32_t(mp >> 32)), 0.0f,
+                                               0.0f)};
                 return;
             }
             const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * prim);
@@ -1103,7 +1117,7 @@ __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *d
         bd->hi[1] = rh.y;
         bd->hi[2] = rh.z;
         bd->depth = sc[kSegDepth];
-        bd->valid = (empty ? 0u : 1u) | (g.kind == kSegAabbs ? 2u : 0u);
+        bd->valid = (empty ? 0u : 1u) | ((g.kind & 0xffu) == kSegAabbs ? 2u : 0u);
     }
 }
 
@@ -1439,7 +1453,7 @@ __global__ void k_refit(RefitArgs A) {
                             atomicOr(&A.ctl[kCtlErr], kErrBadIndex);
                             continue;
                         }
-                        if (g.kind == kSegAabbs) {
+                        if ((g.kind & 0xffu) == kSegAabbs) {
                             const float *bx = reinterpret_cast<const float *>(g.vbase + 24ull * prim);
                             for (int k = 0; k < 3; k++) {
                                 il[k] = bx[k];
@@ -1493,7 +1507,7 @@ __global__ void k_refit(RefitArgs A) {
                     bd->lo[k] = empty ? FLT_MAX : nl[k];
                     bd->hi[k] = empty ? -FLT_MAX : nh[k];
                 }
-                bd->valid = (empty ? 0u : 1u) | (g.kind == kSegAabbs ? 2u : 0u);
+                bd->valid = (empty ? 0u : 1u) | ((g.kind & 0xffu) == kSegAabbs ? 2u : 0u);
             }
             return;
         }

@@ -6,6 +6,7 @@
 // CPU: src/rust/luisa_compute_backend_impl/src/cpu/stream.rs:410-428), with
 // status codes in place of the reference's aborts.
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <unordered_set>
 #include <atomic>
@@ -151,6 +152,8 @@ struct MeshObj {
     uint32_t node_count = 0, tri_count = 0, depth = 0;
     uint32_t ref_count = 0;  // leaf items: tri_count, or more with triangle splitting
     uint32_t kind = kSegTriangles;  // or kSegAabbs: a procedural primitive (lcx_procedural_*)
+    LcxMotionOption motion{};       // keyframe_count >= 2: vertex motion (lcx_mesh_create_motion)
+    MeshMotion *d_motion = nullptr;  // after the BlasDesc in d_desc's allocation
     uint32_t seg = 0;  // segment (position in its build) within `block`
     uint64_t refits = 0;  // refits since the last full build
     bool built = false;
@@ -497,6 +500,13 @@ int mesh_segments(const std::vector<MeshObj *> &meshes, const LcxMeshBuildComman
             return fail(LCX_ERR_INVALID_ARG, "entry %zu: a procedural primitive takes lcx_procedural_build", i);
         uint64_t tri64 = 0, v64 = 0;
         if (int r = validate_mesh_command(&cmds[i], tri64, v64)) return r;
+        const uint32_t keys = meshes[i]->motion.keyframe_count;
+        if (keys >= 2) {  // mesh.cpp check_mesh_vert_buffer_motion_keyframe_count: whole keyframes
+            if (v64 % keys != 0)
+                return fail(LCX_ERR_INVALID_ARG, "entry %zu: %llu vertices are not %u whole keyframes", i,
+                            (unsigned long long)v64, keys);
+            v64 /= keys;
+        }
         SegInput &g = segs[i];
         g.vbase = reinterpret_cast<const unsigned char *>(cmds[i].vertex_buffer) + cmds[i].vertex_buffer_offset;
         g.vstride = cmds[i].vertex_stride;
@@ -504,7 +514,7 @@ int mesh_segments(const std::vector<MeshObj *> &meshes, const LcxMeshBuildComman
         g.vcount = uint32_t(v64);
         g.item_offset = uint32_t(total);
         g.item_count = uint32_t(tri64);
-        g.kind = kSegTriangles;
+        g.kind = kSegTriangles | (keys >= 2 ? keys << 8 : 0u);
         g.desc = meshes[i]->d_desc;
         requests[i] = cmds[i].request;
         total += tri64;
@@ -666,6 +676,21 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
             block->h_segs = segs;
         }
         LCX_CUDA(cudaMemsetAsync(wsah, 0, sah_bytes, st), "cudaMemset");
+        // vertex-motion meshes: their MeshMotion (this build's buffers) before the emit reads it
+        for (size_t i = 0; i < count; i++) {
+            MeshObj *m = meshes[i];
+            if (m->motion.keyframe_count < 2) continue;
+            MeshMotion mm{};
+            mm.vbase = segs[i].vbase;
+            mm.tbase = segs[i].tbase;
+            mm.vstride = segs[i].vstride;
+            mm.vcount = segs[i].vcount;
+            mm.keys = m->motion.keyframe_count;
+            mm.t0 = m->motion.time_start;
+            mm.t1 = m->motion.time_end;
+            mm.flags = (m->motion.vanish_start ? 1u : 0u) | (m->motion.vanish_end ? 2u : 0u);
+            LCX_CUDA(cudaMemcpyAsync(m->d_motion, &mm, sizeof(mm), cudaMemcpyHostToDevice, st), "motion upload");
+        }
         LCX_CUDA(emit_blas(s, bp, W, qn, fn, tr, wsah, rtab, st), "BLAS emit");
         for (size_t i = 0; i < count; i++) {
             MeshObj *m = meshes[i];
@@ -787,6 +812,38 @@ int lcx_mesh_create(const LcxAccelOption *option, uint64_t *out_handle) {
     m->device = ds->device;
     LCX_CUDA(cudaMalloc(&m->d_desc, sizeof(BlasDesc)), "cudaMalloc(BlasDesc)");
     LCX_CUDA(cudaMemset(m->d_desc, 0, sizeof(BlasDesc)), "cudaMemset(BlasDesc)");
+    const uint64_t h = g_next_handle.fetch_add(1);
+    {
+        std::lock_guard<std::mutex> lk(g_reg_mtx);
+        g_meshes[h] = m;
+    }
+    *out_handle = h;
+    return LCX_OK;
+}
+
+int lcx_mesh_create_motion(const LcxAccelOption *option, const LcxMotionOption *motion, uint64_t *out_handle) {
+    if (!out_handle || !motion) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_create_motion: null argument");
+    if (int r = check_option(option)) return r;
+    const LcxMotionOption &o = *motion;
+    if (o.keyframe_count < 2 || o.keyframe_count > (1u << 16))
+        return fail(LCX_ERR_INVALID_ARG, "a motion mesh needs 2..65536 keyframes");
+    if (!(o.time_end > o.time_start) || !std::isfinite(o.time_start) || !std::isfinite(o.time_end))
+        return fail(LCX_ERR_INVALID_ARG, "motion time range must be finite with time_end > time_start");
+    if (option && option->allow_update)
+        return fail(LCX_ERR_INVALID_ARG, "motion meshes cannot be refit (allow_update)");
+    DeviceState *ds = nullptr;
+    if (int r = current_device_state(&ds)) return r;
+    auto m = std::make_shared<MeshObj>();
+    if (option) m->opt = *option;
+    m->device = ds->device;
+    m->motion = o;
+    LCX_CUDA(cudaMalloc(&m->d_desc, sizeof(BlasDesc) + sizeof(MeshMotion)), "cudaMalloc(BlasDesc)");
+    LCX_CUDA(cudaMemset(m->d_desc, 0, sizeof(BlasDesc) + sizeof(MeshMotion)), "cudaMemset(BlasDesc)");
+    m->d_motion = reinterpret_cast<MeshMotion *>(m->d_desc + 1);
+    const MeshMotion *mp = m->d_motion;
+    LCX_CUDA(cudaMemcpy(reinterpret_cast<char *>(m->d_desc) + offsetof(BlasDesc, motion), &mp, sizeof(mp),
+                        cudaMemcpyHostToDevice),
+             "BlasDesc motion");
     const uint64_t h = g_next_handle.fetch_add(1);
     {
         std::lock_guard<std::mutex> lk(g_reg_mtx);
@@ -1052,10 +1109,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
             a->uniq_dirty = true;
             a->pending_rebuild = true;  // as cuda_accel.cpp:184-185: a primitive change forces a rebuild
         }
-    if (motion_changed) {
-        a->has_motion = false;
-        for (const auto &mo : a->inst_motion) a->has_motion = a->has_motion || mo != nullptr;
-    }
+    (void)motion_changed;  // has_motion describes the built TLAS: set by the build below
     if (mod_count) {
         ScratchHolder hold(st);
         ModRec *d_mods = nullptr;
@@ -1069,6 +1123,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     // every referenced mesh must exist and be built before a kernel reads its descriptor
     std::vector<std::pair<uint64_t, uint64_t>> gens;
     uint32_t max_blas_depth = 0;
+    bool mesh_motion = false;  // an instanced mesh has vertex motion
     {
         if (a->uniq_dirty) {
             std::vector<uint64_t> &uniq = a->uniq_mesh;
@@ -1084,11 +1139,15 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
             if (!m->built) return fail(LCX_ERR_NOT_BUILT, "Mesh not built");
             gens.emplace_back(h, m->generation);
             max_blas_depth = std::max(max_blas_depth, m->depth);
+            mesh_motion = mesh_motion || m->motion.keyframe_count >= 2;
         }
     }
     const uint32_t n = instance_count;
     std::vector<std::pair<std::shared_ptr<MotionObj>, uint64_t>> mgens;
-    if (a->has_motion) {
+    bool inst_motion = false;
+    for (const auto &mo : a->inst_motion) inst_motion = inst_motion || mo != nullptr;
+    a->has_motion = inst_motion || mesh_motion;
+    if (inst_motion) {
         std::unordered_set<MotionObj *> seen;
         for (const auto &mo : a->inst_motion) {
             if (!mo || !seen.insert(mo.get()).second) continue;

@@ -20,7 +20,8 @@ struct SegInput {
     uint32_t vcount;
     uint32_t item_offset;        // first item of this segment among all items of the build
     uint32_t item_count;
-    uint32_t kind;               // kSegTriangles (vbase, tbase) or kSegAabbs (vbase: 24-byte AABBs)
+    uint32_t kind;               // low byte: kSegTriangles (vbase, tbase) or kSegAabbs (vbase: 24-byte AABBs);
+                                 // bits 8+: vertex-motion keyframes (vbase holds them back to back, vcount each)
     BlasDesc *desc;              // BLAS descriptor the emit fills in (null for a TLAS)
 };
 enum : uint32_t { kSegTriangles = 0, kSegAabbs = 1 };

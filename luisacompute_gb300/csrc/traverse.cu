@@ -210,7 +210,14 @@ struct Walker {
             const uint32_t k = __ffs(Gt.y) - 1u;
             Gt.y &= Gt.y - 1u;
             const float4 *tp = reinterpret_cast<const float4 *>(blas_tris + Gt.x + k);
-            const float4 a = bvh_ld(tp), b = bvh_ld(tp + 1), c = bvh_ld(tp + 2);
+            float4 a = bvh_ld(tp), b = bvh_ld(tp + 1), c = bvh_ld(tp + 2);
+            if constexpr (kMotion) {
+                if (__float_as_uint(b.w) == kTriMotion) {  // a vertex-motion mesh: its triangle at the ray's time
+                    const MeshMotion *mm = reinterpret_cast<const MeshMotion *>(
+                        (unsigned long long)__float_as_uint(c.x) | ((unsigned long long)__float_as_uint(c.y) << 32));
+                    if (!motion_triangle(*mm, __float_as_uint(a.w), time, a, b, c)) continue;
+                }
+            }
             if (kCount) c_tris++;
             float t, u, v;
             if (wt_intersect(wt, tmin, best_t, a, b, c, t, u, v)) {

@@ -57,8 +57,8 @@ def load():
         lib.lcxo_fp64_closest.argtypes = [c_void_p, c_void_p, c_size_t, c_uint32, c_void_p, c_void_p, c_int]
         lib.lcxo_fp64_eval.argtypes = [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p]
         lib.lcxo_affine_inverse.argtypes = [c_void_p, c_void_p]
-        lib.lcxo_trace_motion.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_uint32, c_int,
-                                          c_void_p, c_void_p, c_int]
+        lib.lcxo_trace_motion.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_uint32,
+                                          c_int, c_void_p, c_void_p, c_int]
         lib.lcxo_pathtrace.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]
         lib.lcxo_intersect_triangle.restype = c_int
         lib.lcxo_intersect_triangle.argtypes = [c_void_p, c_void_p, c_float, c_float, c_void_p, c_void_p, c_void_p,
@@ -74,6 +74,13 @@ def _ptr(a: np.ndarray):
 class LcxoMotion(ctypes.Structure):
     _fields_ = [("keys", ctypes.POINTER(ctypes.c_float)), ("count", ctypes.c_uint32), ("t0", ctypes.c_float),
                 ("t1", ctypes.c_float), ("flags", ctypes.c_uint32)]
+
+
+class LcxoMeshMotion(ctypes.Structure):
+    _fields_ = [("verts", ctypes.POINTER(ctypes.c_float)), ("stride_floats", ctypes.c_size_t),
+                ("vcount", ctypes.c_uint32), ("keys", ctypes.c_uint32), ("tris", ctypes.POINTER(ctypes.c_uint32)),
+                ("tri_count", ctypes.c_uint32), ("t0", ctypes.c_float), ("t1", ctypes.c_float),
+                ("flags", ctypes.c_uint32)]
 
 
 class OracleScene:
@@ -116,7 +123,7 @@ class OracleScene:
         return hits
 
     def trace_motion(self, rays: np.ndarray, times: np.ndarray, motion: list, mask: int = 0xFF, any_hit: bool = False,
-                     threads: int = 0):
+                     threads: int = 0, mesh_motion: list | None = None):
         """Rays with per-ray times over the scene whose instance i moves by motion[i] = (keys (k, 12),
         or (k, 16) SRT records with flags bit 2, float32, t0, t1, flags) or stays static (None);
         lcxo_trace_motion."""
@@ -132,10 +139,23 @@ class OracleScene:
             keys = np.ascontiguousarray(mo[0], np.float32).reshape(-1, 16 if mo[3] & 4 else 12)
             keep.append(keys)
             arr[i] = LcxoMotion(keys.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), keys.shape[0], mo[1], mo[2], mo[3])
+        marr = None
+        if mesh_motion is not None:  # per instance: (vertices (keys*V, >=3) float32, keys, triangles, t0, t1, flags)
+            marr = (LcxoMeshMotion * len(mesh_motion))()
+            for i, mm in enumerate(mesh_motion):
+                if mm is None:
+                    continue
+                verts = np.ascontiguousarray(mm[0], np.float32)
+                tris = np.ascontiguousarray(mm[2], np.uint32).reshape(-1, 3)
+                keep += [verts, tris]
+                marr[i] = LcxoMeshMotion(verts.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), verts.shape[1],
+                                         verts.shape[0] // mm[1], mm[1],
+                                         tris.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), tris.shape[0],
+                                         mm[3], mm[4], mm[5])
         hits = np.zeros(rays.shape[0], HIT_DTYPE)
         occ = np.zeros(rays.shape[0], np.uint8)
-        self.lib.lcxo_trace_motion(self.accel, arr, _ptr(rays), _ptr(times), rays.shape[0], mask, int(any_hit),
-                                   _ptr(hits), _ptr(occ), threads)
+        self.lib.lcxo_trace_motion(self.accel, arr, marr, _ptr(rays), _ptr(times), rays.shape[0], mask,
+                                   int(any_hit), _ptr(hits), _ptr(occ), threads)
         return occ if any_hit else hits
 
     def trace_any(self, rays: np.ndarray, mask: int = 0xFF, threads: int = 0) -> np.ndarray:

@@ -850,16 +850,24 @@ static void srt_matrix_f32(const float *v, float m[12]) {
     }
 }
 
+// include/lcx/bvh_device.cuh motion_segment, operation for operation
+static bool motion_segment_f32(float t0, float t1, uint32_t count, uint32_t flags, float time, uint32_t &i, float &f) {
+    if ((flags & 1u) && time < t0) return false;
+    if ((flags & 2u) && time > t1) return false;
+    float u = (time - t0) / (t1 - t0);
+    u = u >= 0.0f ? (u <= 1.0f ? u : 1.0f) : 0.0f;
+    const float x = u * float(count - 1u);
+    i = uint32_t(std::floor(x));
+    if (i > count - 2u) i = count - 2u;
+    f = x - float(i);
+    return true;
+}
+
 // include/lcx/bvh_device.cuh motion_matrix, operation for operation
 static bool motion_matrix_f32(const LcxoMotion &md, float time, float m[12]) {
-    if ((md.flags & 1u) && time < md.t0) return false;
-    if ((md.flags & 2u) && time > md.t1) return false;
-    float u = (time - md.t0) / (md.t1 - md.t0);
-    u = u >= 0.0f ? (u <= 1.0f ? u : 1.0f) : 0.0f;
-    const float x = u * float(md.count - 1u);
-    uint32_t i = uint32_t(std::floor(x));
-    if (i > md.count - 2u) i = md.count - 2u;
-    const float f = x - float(i);
+    uint32_t i;
+    float f;
+    if (!motion_segment_f32(md.t0, md.t1, md.count, md.flags, time, i, f)) return false;
     if (md.flags & 4u) {  // SRT records
         const float *k0 = md.keys + 16 * size_t(i), *k1 = k0 + 16;
         float v[16];
@@ -872,8 +880,42 @@ static bool motion_matrix_f32(const LcxoMotion &md, float time, float m[12]) {
     return true;
 }
 
-void lcxo_trace_motion(const void *accel, const LcxoMotion *motion, const LcxoRay *rays, const float *times,
-                       size_t n, uint32_t mask, int any, LcxoHit *hits, uint8_t *occluded, int threads) {
+// Every triangle of a keyframed-vertex mesh at `time` (motion_triangle of
+// include/lcx/bvh_device.cuh, operation for operation), in object space.
+static bool trace_motion_mesh(bool kAny, const LcxoMeshMotion &mm, uint32_t inst, const float *o, const float *d,
+                              float tmin, float time, LcxoHit &best) {
+    uint32_t seg;
+    float f;
+    if (!motion_segment_f32(mm.t0, mm.t1, mm.keys, mm.flags, time, seg, f)) return false;
+    WtRay wr;
+    wt_setup(wr, o, d, tmin, best.t);
+    for (uint32_t p = 0; p < mm.tri_count; p++) {
+        float v[3][3];
+        bool ok = true;
+        for (int k = 0; k < 3 && ok; k++) {
+            const uint32_t idx = mm.tris[3 * size_t(p) + k];
+            if (idx >= mm.vcount) {
+                ok = false;
+                break;
+            }
+            const float *p0 = mm.verts + mm.stride_floats * (size_t(seg) * mm.vcount + idx);
+            const float *p1 = mm.verts + mm.stride_floats * (size_t(seg + 1u) * mm.vcount + idx);
+            for (int j = 0; j < 3; j++) v[k][j] = std::fma(f, p1[j] - p0[j], p0[j]);
+        }
+        if (!ok) continue;
+        float t, u, w;
+        wr.tmax = best.t;
+        if (wt_intersect(wr, v[0], v[1], v[2], t, u, w)) {
+            if (kAny) return true;
+            if (better(t, inst, p, best)) best = LcxoHit{inst, p, u, w, t, 0};
+        }
+    }
+    return false;
+}
+
+void lcxo_trace_motion(const void *accel, const LcxoMotion *motion, const LcxoMeshMotion *mesh_motion,
+                       const LcxoRay *rays, const float *times, size_t n, uint32_t mask, int any, LcxoHit *hits,
+                       uint8_t *occluded, int threads) {
     const Accel &a = *static_cast<const Accel *>(accel);
     parallel_rays(n, threads, [&](size_t r) {
         const LcxoRay &ray = rays[r];
@@ -892,7 +934,13 @@ void lcxo_trace_motion(const void *accel, const LcxoMotion *motion, const LcxoRa
             }
             float oo[3], od[3];
             transform_ray_f32(wp, ray.o, ray.d, oo, od);
-            if (any) {
+            if (mesh_motion != nullptr && mesh_motion[id].verts != nullptr) {
+                if (any) {
+                    if (trace_motion_mesh(true, mesh_motion[id], id, oo, od, ray.tmin, times[r], best)) occ = true;
+                } else {
+                    trace_motion_mesh(false, mesh_motion[id], id, oo, od, ray.tmin, times[r], best);
+                }
+            } else if (any) {
                 if (trace_mesh<true>(*m, id, oo, od, ray.tmin, best)) occ = true;
             } else {
                 trace_mesh<false>(*m, id, oo, od, ray.tmin, best);

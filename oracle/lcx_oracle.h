@@ -116,8 +116,22 @@ typedef struct LcxoMotion {
     float t0, t1;
     uint32_t flags;
 } LcxoMotion;
-void lcxo_trace_motion(const void *accel, const LcxoMotion *motion, const LcxoRay *rays, const float *times,
-                       size_t n, uint32_t mask, int any, LcxoHit *hits, uint8_t *occluded, int threads);
+/* Keyframed vertices of an instance's mesh (null verts: static): `keys`
+ * copies of `vcount` vertices (stride_floats apart, xyz used) over [t0, t1],
+ * interpolated per component (motion_triangle of bvh_device.cuh); such
+ * instances are tested triangle by triangle. */
+typedef struct LcxoMeshMotion {
+    const float *verts;
+    size_t stride_floats;
+    uint32_t vcount, keys;
+    const uint32_t *tris;
+    uint32_t tri_count;
+    float t0, t1;
+    uint32_t flags;
+} LcxoMeshMotion;
+void lcxo_trace_motion(const void *accel, const LcxoMotion *motion, const LcxoMeshMotion *mesh_motion,
+                       const LcxoRay *rays, const float *times, size_t n, uint32_t mask, int any, LcxoHit *hits,
+                       uint8_t *occluded, int threads);
 int lcxo_intersect_triangle(const float *o, const float *d, float tmin, float tmax,
                             const float *v0, const float *v1, const float *v2, float *t,
                             float *u, float *v);

@@ -169,3 +169,64 @@ def test_srt_motion_matches_oracle(lcx, oracle_mod):
         assert np.array_equal(acc.trace_any_motion(d_rays, d_times, layout=layout).cpu().numpy(), want_any)
     from luisacompute_gb300 import _capi
     _capi.check(lcx.lcx_check_trace_errors(), "trace errors")
+
+
+def test_keyframed_vertices_match_oracle(lcx, oracle_mod):
+    """A mesh with keyframed vertices (the vertex buffer holds 3 copies of the vertices), instanced
+    with static transforms and through a motion instance (both motions at once), next to a static
+    mesh: the oracle's records bit for bit, closest and any, both layouts; the plain calls use time 0."""
+    import torch
+    from luisacompute_gb300.accel import Accel, Mesh, MotionInstance, hits_to_numpy, mesh_from_data, rays_to_device
+    rng = np.random.default_rng(57)
+    base = S.icosphere(3)
+    keys = 3
+    frames = []
+    for k in range(keys):
+        v = base.vertices.copy()
+        v[:, :3] = v[:, :3] * np.float32(0.6 + 0.2 * k) + rng.normal(0.0, 0.02, (v.shape[0], 3)).astype(np.float32)
+        v[:, :3] += np.float32(0.3 * k)
+        frames.append(v)
+    stacked = np.ascontiguousarray(np.concatenate(frames), np.float32)
+    t0, t1, flags = 0.1, 0.9, 2  # vanishes after t1
+    mesh = Mesh(torch.from_numpy(stacked).cuda(), torch.from_numpy(base.triangles.astype(np.int32)).cuda(),
+                motion_keyframes=keys, time_start=t0, time_end=t1, vanish_end=True).build()
+    other = S.displaced_mesh(2_000, rng)
+    static = mesh_from_data(other).build()
+    aff = _keyframes(rng, 4, spread=0.8)
+    acc = Accel()
+    acc.emplace_back(mesh, aff[0].reshape(3, 4))
+    acc.emplace_back(mesh, aff[1].reshape(3, 4))
+    acc.emplace_back(static, aff[2].reshape(3, 4))
+    ikeys = _keyframes(rng, 2, spread=0.5)
+    mo = MotionInstance(mesh, ikeys.reshape(-1, 3, 4), 0.0, 1.0)
+    acc.emplace_back(mo)
+    acc.build()
+    first = S.MeshData(frames[0], base.triangles)
+    scene = S.Scene([first, other], np.array([0, 0, 1, 0]), np.concatenate([aff[:3], S.IDENTITY[None]]),
+                    np.full(4, 0xFF, np.uint32))
+    osc = oracle_mod.OracleScene(scene)
+    vm = (stacked, keys, base.triangles, t0, t1, flags)
+    mesh_motion = [vm, vm, None, vm]
+    specs = [None, None, None, (ikeys, 0.0, 1.0, 0)]
+    rays, times = _rays_times(rng, 40_000, 58)
+    want = osc.trace_motion(rays, times, specs, mesh_motion=mesh_motion)
+    want_any = osc.trace_motion(rays, times, specs, any_hit=True, mesh_motion=mesh_motion)
+    assert np.isin([0, 1, 2, 3], want["inst"]).all()
+    d_rays, d_times = rays_to_device(rays), torch.from_numpy(times).cuda()
+    for layout in (0, 1):
+        got = hits_to_numpy(acc.trace_closest_motion(d_rays, d_times, layout=layout))
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), layout
+        assert np.array_equal(acc.trace_any_motion(d_rays, d_times, layout=layout).cpu().numpy(), want_any)
+    zero = osc.trace_motion(rays, np.zeros(rays.shape[0], np.float32), specs, mesh_motion=mesh_motion)
+    assert np.array_equal(hits_to_numpy(acc.trace_closest(d_rays)).view(np.uint8), zero.view(np.uint8))
+    from luisacompute_gb300 import _capi
+    _capi.check(lcx.lcx_check_trace_errors(), "trace errors")
+    # a vertex buffer that is not whole keyframes, and refit, are refused
+    bad = Mesh(torch.from_numpy(stacked[:-1]).cuda(), torch.from_numpy(base.triangles.astype(np.int32)).cuda(),
+               motion_keyframes=keys)
+    with pytest.raises(_capi.LcxError):
+        bad.build()
+    from luisacompute_gb300.accel import AccelOption
+    with pytest.raises(_capi.LcxError):
+        Mesh(torch.from_numpy(stacked).cuda(), torch.from_numpy(base.triangles.astype(np.int32)).cuda(),
+             AccelOption(allow_update=True), motion_keyframes=keys)
