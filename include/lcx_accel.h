@@ -222,6 +222,22 @@ typedef struct LcxProceduralBuildCommand {
  * commits its own distance. */
 LCX_API int lcx_procedural_create(const LcxAccelOption *option, uint64_t *out_handle);
 LCX_API int lcx_procedural_destroy(uint64_t handle);
+/* Builds a batch like lcx_mesh_build_batch and reserves it for rebuilds
+ * captured in CUDA graphs: the batch's block gets room for any tree over the
+ * same triangles (wide nodes <= triangles + meshes) and keeps its segment
+ * table on the device.  A later lcx_mesh_build_batch (or a single-mesh batch's
+ * lcx_mesh_build) of the same meshes, in the same order, over the same
+ * buffers, sizes and strides -- the vertices may have moved -- rebuilds the
+ * BVHs in place with kernels only: no host synchronisation, no allocation
+ * outside stream-ordered scratch, so it can be captured.  Such rebuilds
+ * report errors through lcx_check_trace_errors, and lcx_mesh_stats keeps the
+ * reserving build's figures.  Splitting is off for reserved batches; meshes
+ * with allow_update or vertex motion are refused.  Synchronises the host
+ * once (as a batch build).  No counterpart in the reference, whose builds
+ * synchronise per mesh (cuda_primitive.cpp:74). */
+LCX_API int lcx_mesh_build_batch_reserve(const uint64_t *meshes, const LcxMeshBuildCommand *cmds,
+                                         uint32_t count, void *stream);
+
 /* Builds (PREFER_UPDATE with allow_update: refits) on `stream`, like
  * lcx_mesh_build.  Empty boxes (min > max on an axis) are never reported. */
 LCX_API int lcx_procedural_build(uint64_t handle, const LcxProceduralBuildCommand *command, void *stream);

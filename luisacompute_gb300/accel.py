@@ -428,6 +428,20 @@ def build_meshes(meshes, request: int = REQUEST_FORCE_BUILD, stream=None):
     return meshes
 
 
+def reserve_meshes(meshes, stream=None):
+    """lcx_mesh_build_batch_reserve: build the batch and keep room to rebuild it in place (later
+    ``build_meshes`` calls of the same meshes over the same buffers, capturable in CUDA graphs)."""
+    lib = _capi.load()
+    n = len(meshes)
+    handles = (ctypes.c_uint64 * n)(*[m.handle for m in meshes])
+    cmds = (LcxMeshBuildCommand * n)()
+    for i, m in enumerate(meshes):
+        cmds[i] = LcxMeshBuildCommand(REQUEST_FORCE_BUILD, 0, m.vertices.data_ptr(), 0, m.vertex_size,
+                                      m.vertex_stride, m.triangles.data_ptr(), 0, m.triangle_size)
+    check(lib.lcx_mesh_build_batch_reserve(handles, cmds, n, stream_handle(stream)), "lcx_mesh_build_batch_reserve")
+    return meshes
+
+
 def set_refit_sync(sync: bool):
     """Refit mode of later PREFER_UPDATE mesh builds: True synchronises once to report bad
     indices from the call; False only enqueues kernels (capturable in a CUDA graph) and leaves

@@ -1052,9 +1052,12 @@ __device__ void emit_node(const TreeView &tv, const SegInput *segs, const uint32
 
 __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *desc, uint32_t wide_count,
                             int leaf_max, Node8Q *qn, Node8F *fn, TriRec *tris, const uint32_t *segctl,
-                            uint32_t *ctl, double *sah, unsigned long long *rtab, const uint32_t *ref_prim) {
+                            uint32_t *ctl, double *sah, unsigned long long *rtab, const uint32_t *ref_prim,
+                            bool count_on_device) {
     const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= wide_count) return;
+    // a build that does not read its node count back: wide_count is the capacity
+    // of the output, the collapse's count (never above it) bounds the work
+    if (w >= wide_count || (count_on_device && w >= __ldcg(&ctl[kCtlWideCount]))) return;
     const uint32_t seg = desc[12ull * w + 3];
     if (segs[seg].item_count == 0) {  // root slot of an empty segment
         if (w == seg) {
@@ -1316,10 +1319,21 @@ cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const Build
 }
 
 cudaError_t emit_blas(const BuildScratch &s, const BuildParams &bp, uint32_t wide_count, Node8Q *qn, Node8F *fn,
-                      TriRec *tris, double *wide_sah, unsigned long long *rtab, cudaStream_t st) {
+                      TriRec *tris, double *wide_sah, unsigned long long *rtab, cudaStream_t st,
+                      bool count_on_device) {
     k_emit_blas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.segs, s.desc, wide_count, bp.leaf_max,
                                                               qn, fn, tris, s.segctl, s.ctl, wide_sah, rtab,
-                                                              s.ref_prim);
+                                                              s.ref_prim, count_on_device);
+    return cudaGetLastError();
+}
+
+__global__ void k_or_errors(const uint32_t *ctl, uint32_t *into) {
+    const uint32_t e = ctl[kCtlErr];
+    if (e) atomicOr(&into[kCtlErr], e);
+}
+
+cudaError_t report_build_errors(const uint32_t *ctl, uint32_t *into, cudaStream_t st) {
+    k_or_errors<<<1, 1, 0, st>>>(ctl, into);
     return cudaGetLastError();
 }
 

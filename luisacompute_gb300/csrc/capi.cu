@@ -107,6 +107,13 @@ struct DevBlock {
     float4 *ilo = nullptr, *ihi = nullptr;  // TLAS: instance boxes
     float *w2o = nullptr;             // TLAS: instance inverses
     uint32_t *segctl = nullptr;       // TLAS: kSegWords words
+    // reserved batches (lcx_mesh_build_batch_reserve): room for any tree over the
+    // same items (cap_wide nodes), the segment table (d_segs / h_segs) and the
+    // initial control words on the device, so a rebuild needs no host sync
+    bool reserved = false;
+    uint32_t items = 0, cap_wide = 0;
+    uint32_t *d_segctl_init = nullptr;
+    double *wsah = nullptr;
     ~DevBlock() {
         if (ptr) cudaFree(ptr);  // cudaFree waits for work still using it
     }
@@ -276,7 +283,8 @@ struct ScratchHolder {
 
 // Allocates the scratch of a build over n items in the given segments and
 // uploads the segment table and initial control words.
-int alloc_scratch(ScratchHolder &h, BuildScratch &s, const std::vector<SegInput> &segs, uint32_t n, bool tlas) {
+int alloc_scratch(ScratchHolder &h, BuildScratch &s, const std::vector<SegInput> &segs, uint32_t n, bool tlas,
+                  const SegInput *d_segs_src = nullptr, const uint32_t *d_segctl_src = nullptr) {
     const size_t nn = std::max<uint32_t>(n, 1);
     s.n = n;
     s.nseg = uint32_t(segs.size());
@@ -303,14 +311,24 @@ int alloc_scratch(ScratchHolder &h, BuildScratch &s, const std::vector<SegInput>
     LCX_CUDA(h.alloc((void **)&s.ctl, sizeof(uint32_t) * kCtlWords), "scratch");
     s.sort_tmp_bytes = sort_temp_bytes(uint32_t(nn));
     LCX_CUDA(h.alloc(&s.sort_tmp, s.sort_tmp_bytes), "scratch");
-    // uploads: segment table, control words (centroid minima start at the largest ordered value)
-    std::vector<uint32_t> segctl(size_t(kSegWords) * s.nseg, 0u);
-    for (uint32_t i = 0; i < s.nseg; i++)
-        for (int k = 0; k < 3; k++) segctl[size_t(kSegWords) * i + kSegCenLo + k] = 0xffffffffu;
-    LCX_CUDA(cudaMemcpyAsync(d_segs, segs.data(), sizeof(SegInput) * s.nseg, cudaMemcpyHostToDevice, h.st),
-             "segment upload");
-    LCX_CUDA(cudaMemcpyAsync(s.segctl, segctl.data(), sizeof(uint32_t) * segctl.size(), cudaMemcpyHostToDevice, h.st),
-             "segment upload");
+    // uploads: segment table, control words (centroid minima start at the largest ordered value);
+    // a reserved rebuild copies both from the device (no host data: capturable)
+    if (d_segs_src != nullptr) {
+        LCX_CUDA(cudaMemcpyAsync(d_segs, d_segs_src, sizeof(SegInput) * s.nseg, cudaMemcpyDeviceToDevice, h.st),
+                 "segment copy");
+        LCX_CUDA(cudaMemcpyAsync(s.segctl, d_segctl_src, sizeof(uint32_t) * kSegWords * s.nseg,
+                                 cudaMemcpyDeviceToDevice, h.st),
+                 "segment copy");
+    } else {
+        std::vector<uint32_t> segctl(size_t(kSegWords) * s.nseg, 0u);
+        for (uint32_t i = 0; i < s.nseg; i++)
+            for (int k = 0; k < 3; k++) segctl[size_t(kSegWords) * i + kSegCenLo + k] = 0xffffffffu;
+        LCX_CUDA(cudaMemcpyAsync(d_segs, segs.data(), sizeof(SegInput) * s.nseg, cudaMemcpyHostToDevice, h.st),
+                 "segment upload");
+        LCX_CUDA(cudaMemcpyAsync(s.segctl, segctl.data(), sizeof(uint32_t) * segctl.size(), cudaMemcpyHostToDevice,
+                                 h.st),
+                 "segment upload");
+    }
     LCX_CUDA(cudaMemsetAsync(s.bin_sah, 0, sizeof(double) * 2 * s.nseg, h.st), "scratch init");
     LCX_CUDA(cudaMemsetAsync(s.ctl, 0, sizeof(uint32_t) * kCtlWords, h.st), "scratch init");
     // (copies from pageable memory return once the source has been staged)
@@ -525,19 +543,52 @@ int mesh_segments(const std::vector<MeshObj *> &meshes, const LcxMeshBuildComman
 }
 
 // Builds (or refits) the BVHs of `meshes` from their segments in one pass.
+// A reserved batch rebuilt in place (the same meshes in the same order over the
+// same buffers): the build's kernels only, no host synchronisation and no
+// allocation outside the stream-ordered scratch, so it can be captured in a
+// CUDA graph.  Errors go to the device's asynchronous error word; the meshes'
+// statistics (node count, depth) keep the reserving build's values.
+// Otherwise kNoRefit.
+int try_reserved_rebuild(const std::vector<MeshObj *> &meshes, const std::vector<SegInput> &segs, cudaStream_t st) {
+    const size_t count = meshes.size();
+    DevBlock *blk = meshes[0]->block.get();
+    if (!blk || !blk->reserved || blk->nseg != count || blk->h_segs.size() != count) return kNoRefit;
+    for (size_t i = 0; i < count; i++)
+        if (meshes[i]->block.get() != blk || meshes[i]->seg != i) return kNoRefit;
+    if (std::memcmp(blk->h_segs.data(), segs.data(), sizeof(SegInput) * count) != 0) return kNoRefit;
+    DeviceState *ds = nullptr;
+    if (int r = current_device_state(&ds)) return r;
+    BuildParams bp = build_params_for(meshes[0]->opt);
+    bp.split = 0.0f;
+    ScratchHolder hold(st);
+    BuildScratch s;
+    if (int r = alloc_scratch(hold, s, blk->h_segs, blk->items, false, blk->d_segs, blk->d_segctl_init)) return r;
+    LCX_CUDA(build_tree_tris(s, bp, st), "BLAS rebuild");
+    LCX_CUDA(cudaMemsetAsync(blk->wsah, 0, 2 * sizeof(double) * count, st), "cudaMemset");
+    LCX_CUDA(emit_blas(s, bp, blk->cap_wide, blk->qn, blk->fn, blk->tris, blk->wsah, nullptr, st, true),
+             "BLAS rebuild emit");
+    LCX_CUDA(report_build_errors(s.ctl, ds->refit_ctl, st), "BLAS rebuild errors");
+    for (MeshObj *m : meshes) m->generation++;  // accels over these meshes must be built (or refit) again
+    bump_mesh_epoch();
+    return LCX_OK;
+}
+
 int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInput> &segs,
-                 const std::vector<uint32_t> &requests, cudaStream_t st, Retired &retired) {
+                 const std::vector<uint32_t> &requests, cudaStream_t st, Retired &retired, bool reserve = false) {
     const size_t count = meshes.size();
     uint64_t total = 0;
     for (const SegInput &g : segs) total += g.item_count;
-    {
-        const int r = try_refit(meshes, requests, segs, st);
+    if (!reserve) {
+        int r = try_refit(meshes, requests, segs, st);
+        if (r != kNoRefit) return r;
+        r = try_reserved_rebuild(meshes, segs, st);
         if (r != kNoRefit) return r;
     }
     if (capturing(st))  // a build sizes its block on the host
         return fail(LCX_ERR_INVALID_ARG,
                     "mesh build in a CUDA graph capture: only refits (PREFER_UPDATE, allow_update, every mesh of the "
-                    "block, same triangle counts, asynchronous refit mode) can be captured");
+                    "block, same triangle counts, asynchronous refit mode) and rebuilds of a reserved batch "
+                    "(lcx_mesh_build_batch_reserve, same meshes and buffers) can be captured");
     const BuildParams bp = build_params_for(meshes[0]->opt);
     if (total == 0) {
         LCX_CUDA(cudaStreamSynchronize(st), "sync");
@@ -564,7 +615,7 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
         ScratchHolder hold(st);
         BuildScratch s;
         // triangle splitting: FAST_TRACE triangle meshes, none of them kept for refits
-        bool split = bp.split > 0.0f && !want_rtab;
+        bool split = bp.split > 0.0f && !want_rtab && !reserve;
         for (const SegInput &g : segs) split = split && g.kind == kSegTriangles;
         std::vector<SegInput> rsegs;  // the segments in reference space
         uint32_t n_items = n;
@@ -644,15 +695,19 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
                 return fail(LCX_ERR_CUDA, "BLAS build placed %u of %u items of mesh %zu",
                             rb.segctl[kSegWords * i + kSegItems], isegs[i].item_count, i);
         const uint32_t W = rb.ctl[kCtlWideCount];
-        const size_t q_bytes = size_t(W) * sizeof(Node8Q), f_bytes = size_t(W) * sizeof(Node8F);
+        // a reserved batch has room for any tree over its items: every wide node opens a
+        // binary node or is a segment root, so there are at most items + segments of them
+        const uint32_t W_alloc = reserve ? uint32_t(std::max<uint64_t>(W, uint64_t(n_items) + count)) : W;
+        const size_t q_bytes = size_t(W_alloc) * sizeof(Node8Q), f_bytes = size_t(W_alloc) * sizeof(Node8F);
         const size_t t_bytes = size_t(n_items) * sizeof(TriRec), sah_bytes = 2 * sizeof(double) * count;
+        const size_t res_bytes = reserve ? sizeof(SegInput) * count + sizeof(uint32_t) * kSegWords * count : 0;
         // refit data: parent table, counters, segment table (16-byte aligned)
         const size_t r_bytes =
             want_rtab ? ((size_t(W) * (sizeof(unsigned long long) + sizeof(uint32_t)) + 15) & ~size_t(15)) +
                             sizeof(SegInput) * count
                       : 0;
         block = std::make_shared<DevBlock>();
-        block->bytes = q_bytes + f_bytes + t_bytes + sah_bytes + r_bytes;
+        block->bytes = q_bytes + f_bytes + t_bytes + sah_bytes + r_bytes + res_bytes;
         LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(BLAS)");
         Node8Q *qn = static_cast<Node8Q *>(block->ptr);
         Node8F *fn = reinterpret_cast<Node8F *>(reinterpret_cast<char *>(block->ptr) + q_bytes);
@@ -674,6 +729,24 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
             LCX_CUDA(cudaMemcpyAsync(block->d_segs, segs.data(), sizeof(SegInput) * count, cudaMemcpyHostToDevice, st),
                      "refit segment table");
             block->h_segs = segs;
+        }
+        if (reserve) {  // segment table and initial control words for the rebuilds
+            char *rp = reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes + t_bytes + sah_bytes + r_bytes;
+            block->reserved = true;
+            block->items = n_items;
+            block->cap_wide = W_alloc;
+            block->wsah = wsah;
+            block->d_segs = reinterpret_cast<SegInput *>(rp);
+            block->d_segctl_init = reinterpret_cast<uint32_t *>(rp + sizeof(SegInput) * count);
+            block->h_segs = segs;
+            std::vector<uint32_t> init(size_t(kSegWords) * count, 0u);
+            for (size_t i = 0; i < count; i++)
+                for (int k = 0; k < 3; k++) init[size_t(kSegWords) * i + kSegCenLo + k] = 0xffffffffu;
+            LCX_CUDA(cudaMemcpyAsync(block->d_segs, segs.data(), sizeof(SegInput) * count, cudaMemcpyHostToDevice, st),
+                     "reserve segment table");
+            LCX_CUDA(cudaMemcpyAsync(block->d_segctl_init, init.data(), sizeof(uint32_t) * init.size(),
+                                     cudaMemcpyHostToDevice, st),
+                     "reserve control words");
         }
         LCX_CUDA(cudaMemsetAsync(wsah, 0, sah_bytes, st), "cudaMemset");
         // vertex-motion meshes: their MeshMotion (this build's buffers) before the emit reads it
@@ -957,6 +1030,41 @@ int lcx_mesh_build_batch(const uint64_t *meshes, const LcxMeshBuildCommand *cmds
     std::vector<uint32_t> req;
     if (int r = mesh_segments(order, cmds, segs, req)) return r;
     return build_meshes(order, segs, req, static_cast<cudaStream_t>(stream), retired);
+}
+
+int lcx_mesh_build_batch_reserve(const uint64_t *meshes, const LcxMeshBuildCommand *cmds, uint32_t count,
+                                 void *stream) {
+    if (count == 0) return LCX_OK;
+    if (!meshes || !cmds) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build_batch_reserve: null arguments");
+    std::vector<std::shared_ptr<MeshObj>> objs(count);
+    for (uint32_t i = 0; i < count; i++) {
+        objs[i] = find_mesh(meshes[i]);
+        if (!objs[i]) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build_batch_reserve: unknown mesh handle %llu",
+                                  (unsigned long long)meshes[i]);
+        if (objs[i]->opt.allow_update)
+            return fail(LCX_ERR_INVALID_ARG, "a reserved batch is rebuilt, not refit (allow_update)");
+        if (objs[i]->motion.keyframe_count >= 2)
+            return fail(LCX_ERR_INVALID_ARG, "motion meshes cannot be reserved");
+    }
+    std::vector<MeshObj *> order(count);
+    for (uint32_t i = 0; i < count; i++) order[i] = objs[i].get();
+    std::vector<MeshObj *> sorted = order;
+    std::sort(sorted.begin(), sorted.end());
+    for (uint32_t i = 1; i < count; i++)
+        if (sorted[i] == sorted[i - 1]) return fail(LCX_ERR_INVALID_ARG, "a mesh appears twice");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (capturing(st)) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build_batch_reserve cannot be captured");
+    Retired retired;
+    std::vector<std::unique_lock<std::mutex>> locks;
+    locks.reserve(count);
+    for (MeshObj *m : sorted) locks.emplace_back(m->mtx);
+    std::vector<SegInput> segs;
+    std::vector<uint32_t> req;
+    if (int r = mesh_segments(order, cmds, segs, req)) return r;
+    uint64_t total = 0;
+    for (const SegInput &g : segs) total += g.item_count;
+    if (total == 0) return fail(LCX_ERR_INVALID_ARG, "a reserved batch needs triangles");
+    return build_meshes(order, segs, req, st, retired, true);
 }
 
 int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out) {
@@ -1514,7 +1622,8 @@ int lcx_check_trace_errors(void) {
     if (rerr) {
         LCX_CUDA(cudaMemset(ds->refit_ctl, 0, kCtlWords * sizeof(uint32_t)), "refit error reset");
         if (rerr & kErrTooDeep) return fail(LCX_ERR_DEPTH, "an asynchronous refit met a BVH deeper than expected");
-        return fail(LCX_ERR_INVALID_ARG, "an asynchronous refit failed (bad index or unquantisable coordinates)");
+        return fail(LCX_ERR_INVALID_ARG,
+                    "an asynchronous refit or reserved rebuild failed (bad index or unquantisable coordinates)");
     }
     if (flags & 2u) return fail(LCX_ERR_TIMEOUT, "a ray exceeded the traversal step bound (corrupt BVH?)");
     if (flags & 1u) return fail(LCX_ERR_DEPTH, "a ray overflowed the traversal stack");

@@ -119,8 +119,13 @@ cudaError_t split_emit(const SegInput *tsegs, uint32_t nseg, uint32_t n, const u
 
 // Phase 2: write both node layouts and the leaf items; wide_sah (2 nseg
 // doubles, zeroed by the caller, may be null) receives the per-segment wide SAH.
+// count_on_device: wide_count is the output's capacity and the collapse's own
+// count (in s.ctl) bounds the nodes written -- a build with no host readback.
 cudaError_t emit_blas(const BuildScratch &s, const BuildParams &bp, uint32_t wide_count, Node8Q *qn, Node8F *fn,
-                      TriRec *tris, double *wide_sah, unsigned long long *rtab, cudaStream_t st);
+                      TriRec *tris, double *wide_sah, unsigned long long *rtab, cudaStream_t st,
+                      bool count_on_device = false);
+// ORs a build's error bits into another control block (the asynchronous error word).
+cudaError_t report_build_errors(const uint32_t *ctl, uint32_t *into, cudaStream_t st);
 // Refit (build.cu): new triangle records and boxes for a BLAS block whose
 // topology is kept (rtab written by its build), from the segments' current
 // buffers; bottom-up over the W wide nodes, then both node layouts re-encoded.

@@ -327,3 +327,68 @@ def ctypes_pair(fn):
     a, b = ctypes.c_uint32(), ctypes.c_uint32()
     _ = fn(ctypes.byref(a), ctypes.byref(b))
     return a.value, b.value
+
+
+def test_reserved_batch_rebuild_in_cuda_graph(lcx, oracle_mod):
+    """lcx_mesh_build_batch_reserve, then full rebuilds of the batch in place (no host sync): first
+    uncaptured after the vertices moved, then captured in a CUDA graph with a torch kernel that
+    writes the vertices and a TLAS refit, replayed over several frames.  A rebuild gives a new
+    topology for the new vertices; every frame must match the oracle on that frame's vertices."""
+    import torch
+    from luisacompute_gb300 import _capi
+    from luisacompute_gb300.accel import (REQUEST_PREFER_UPDATE, Accel, AccelOption, build_meshes, hits_to_numpy,
+                                          rays_to_device, reserve_meshes)
+    rng = np.random.default_rng(61)
+    datas = [S.displaced_mesh(int(n), rng) for n in (500, 4_000, 20_000, 1_200)]
+    meshes = reserve_meshes(_device(datas, allow_update=False))
+    n = len(meshes)
+    aff = _placements(rng, n, spread=1.0)
+    acc = Accel(AccelOption(allow_update=True))
+    acc.emplace_back_many(meshes, aff)
+    acc.build()
+    rays = S.sphere_rays(50_000, [-2.0] * 3, [2.0] * 3, seed=62)
+    masks = np.full(n, 0xFF, np.uint32)
+    _check_scene(oracle_mod, acc, S.Scene(datas, np.arange(n), aff, masks), rays)
+    nodes_before = [int(m.stats().node_count) for m in meshes]
+    # an uncaptured in-place rebuild after large deformations
+    datas = [_deform(md, rng, 0.08, 1.4) for md in datas]
+    for m, md in zip(meshes, datas):
+        m.vertices.copy_(torch.from_numpy(md.vertices).cuda())
+    build_meshes(meshes)
+    acc.build(request=REQUEST_PREFER_UPDATE)
+    _check_scene(oracle_mod, acc, S.Scene(datas, np.arange(n), aff, masks), rays)
+    assert [int(m.stats().node_count) for m in meshes] == nodes_before  # the reserving build's figures
+    # captured: vertices from a device phase, rebuild, TLAS refit, trace
+    base = [m.vertices.clone() for m in meshes]
+    disp = []
+    for md in datas:
+        d = np.zeros_like(md.vertices)
+        d[:, :3] = rng.normal(0.0, 0.05, (md.vertices.shape[0], 3))
+        disp.append(torch.from_numpy(d).cuda())
+    phase = torch.zeros(1, device="cuda")
+    d_rays = rays_to_device(rays)
+    out = torch.empty((rays.shape[0], 6), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        for m, b, d in zip(meshes, base, disp):
+            m.vertices.copy_(b + d * phase)
+        build_meshes(meshes)
+        acc.build(request=REQUEST_PREFER_UPDATE)
+        acc.trace_closest(d_rays, out=out)
+    for p in (0.0, 1.0, -2.0, 3.0):
+        phase.fill_(p)
+        g.replay()
+        torch.cuda.synchronize()
+        frame = [S.MeshData(m.vertices.cpu().numpy(), md.triangles) for m, md in zip(meshes, datas)]
+        want = oracle_mod.OracleScene(S.Scene(frame, np.arange(n), aff, masks)).trace_closest(rays)
+        assert np.array_equal(hits_to_numpy(out).view(np.uint8), want.view(np.uint8)), p
+        _capi.check(lcx.lcx_check_trace_errors(), "rebuild / trace errors")
+    # other buffers: no longer the reserved batch, so an ordinary build
+    moved = [m.vertices.clone() for m in meshes]
+    for m, v in zip(meshes, moved):
+        m.vertices = v
+    build_meshes(meshes)
+    acc.build()
+    frame = [S.MeshData(v.cpu().numpy(), md.triangles) for v, md in zip(moved, datas)]
+    _check_scene(oracle_mod, acc, S.Scene(frame, np.arange(n), aff, masks), rays, layouts=(1,))
