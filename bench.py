@@ -254,6 +254,21 @@ def run_batch_build(args):
     finally:
         set_refit_sync(True)
     del graph, uacc, upd
+    # a reserved batch: full rebuilds in place with no host synchronisation, also as a CUDA graph
+    from luisacompute_gb300.accel import reserve_meshes
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    res = reserve_meshes([Mesh(m.vertices, m.triangles) for m in meshes])
+    torch.cuda.synchronize()
+    res_bytes = max(0, free0 - torch.cuda.mem_get_info()[0])  # the reserved block, about
+    reserved_s = timed(lambda: build_meshes(res), 5)
+    graph_b = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph_b):
+        build_meshes(res)
+    graph_b.replay()
+    graph_rebuild_s = timed(graph_b.replay, 5)
+    _capi.check(_capi.load().lcx_check_trace_errors(), "rebuild errors")
+    del graph_b, res
     # kernels of ours per batched build: tri_prep, morton, lbvh, binary_sah, collapse_init, collapse, emit
     # (the timed loop; the refit figures in "extra" come after it)
     line = {"metric": "Mtris/s batched BLAS build (4096 meshes)", "value": total / batch_s / 1e6, "unit": "Mtris/s",
@@ -274,11 +289,17 @@ def run_batch_build(args):
                                 "tlas_rebuild_ms": tlas_rebuild_s * 1e3, "tlas_refit_ms": tlas_refit_s * 1e3,
                                 "tlas_refits_counted": tlas_refits,
                                 "graph_frame_ms": graph_s * 1e3,
+                                "reserved_rebuild_ms": reserved_s * 1e3,
+                                "reserved_graph_rebuild_ms": graph_rebuild_s * 1e3,
+                                "reserved_graph_rebuild_mtris_s": total / graph_rebuild_s / 1e6,
+                                "reserved_block_gib": res_bytes / 2**30,
                                 "what": "the same 4096 meshes created with allow_update: one batched build vs "
                                         "one batched PREFER_UPDATE (refit in place, topology kept; refit_ms "
                                         "synchronises once for errors, refit_async_ms does not); a TLAS over "
                                         "the 100,000 instances rebuilt vs refit; graph_frame_ms = BLAS refit of "
-                                        "all 4096 meshes + TLAS refit captured as one CUDA graph, per replay"},
+                                        "all 4096 meshes + TLAS refit captured as one CUDA graph, per replay; "
+                                        "reserved_*: the 4096 meshes reserved (lcx_mesh_build_batch_reserve) and "
+                                        "fully rebuilt in place with no host sync, plain and as a CUDA graph"},
                       "tlas_instances": args.instances, "tlas_build_ms": tlas_s * 1e3,
                       "tlas_first_build_ms": tlas_first_s * 1e3,
                       "tlas": {"nodes": int(st.node_count), "depth": int(st.depth), "sah": st.sah_cost,

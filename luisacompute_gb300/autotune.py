@@ -262,7 +262,9 @@ def tune_batch_build(datas, *, sample: int = 512, reps: int = 3, sah_slack: floa
 
     import torch
     t_start = time.perf_counter()
-    space = BUILD_SPACE if space is None else space
+    # triangle splitting is a traversal-quality knob: on displaced meshes it wins the SAH
+    # criterion at several times the build time, so batched builds keep it at its current value
+    space = {k: v for k, v in BUILD_SPACE.items() if k != "split"} if space is None else space
     meshes = [mesh_from_data(m) for m in datas[:sample]]
     start = current()
     trials = []

@@ -140,10 +140,11 @@ struct Retired {
     ~Retired() {
         if (blocks.empty() && others.empty()) return;
         // a barrier, not a critical section: once the exclusive lock has been held, every
-        // trace that looked up these blocks has enqueued its kernel; the wait for those
-        // kernels and the frees happen outside it, so traces on other objects go on
+        // trace that looked up these blocks has enqueued its kernel; the frees (cudaFree,
+        // which the driver completes after the work queued before it) run outside it.  No
+        // explicit device synchronisation: it would stop the host from preparing the next
+        // build while this one runs (batched builds 93.7 -> 141.5 ms with it)
         { std::unique_lock<std::shared_mutex> lk(g_life_mtx); }
-        cudaDeviceSynchronize();
         blocks.clear();
         others.clear();
     }
