@@ -1207,18 +1207,15 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
         if (a->inst_motion[i]) retired.others.push_back(std::move(a->inst_motion[i]));
     a->inst_motion.resize(instance_count);
     a->inst_count = instance_count;
-    bool motion_changed = false;
     for (size_t i = 0; i < mod_count; i++)
         if (new_mesh[i]) {
             a->inst_mesh[recs[i].index] = new_mesh[i];
             auto &slot = a->inst_motion[recs[i].index];
-            if (slot || new_motion[i]) motion_changed = true;
             if (slot) retired.others.push_back(std::move(slot));
             slot = std::move(new_motion[i]);
             a->uniq_dirty = true;
             a->pending_rebuild = true;  // as cuda_accel.cpp:184-185: a primitive change forces a rebuild
         }
-    (void)motion_changed;  // has_motion describes the built TLAS: set by the build below
     if (mod_count) {
         ScratchHolder hold(st);
         ModRec *d_mods = nullptr;

@@ -429,8 +429,10 @@ __global__ void __launch_bounds__(kTraceBlock,
     k_trace(TraceParams P) {
     using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort, kMotion>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
+#if LCX_COOP_TRIS
     __shared__ unsigned long long coop_keys[kTraceBlock];  // per owner lane: min (ordered t, prim)
     __shared__ float2 coop_uv[kTraceBlock];                 // per owner lane: barycentrics of that minimum
+#endif
     uint2 deep_stack[W_t::kDeepSlots];
     const uint32_t lane = threadIdx.x & 31u;
     W_t W(P, stack_mem + threadIdx.x, deep_stack);
