@@ -97,6 +97,22 @@ struct ProceduralPrimitiveBuildCommand {
     size_t aabb_buffer_size;
 };
 
+// include/luisa/runtime/rhi/command.h:446-486; control points are float4
+// {x, y, z, radius} records cp_stride bytes apart, segments u32 first-point indices.
+enum class CurveBasis : uint32_t { PIECEWISE_LINEAR = 0, CUBIC_BSPLINE = 1, CATMULL_ROM = 2, BEZIER = 3 };
+struct CurveBuildCommand {
+    uint64_t handle;
+    AccelBuildRequest request;
+    CurveBasis basis;
+    size_t cp_count;
+    size_t seg_count;
+    uint64_t cp_buffer;
+    size_t cp_buffer_offset;
+    size_t cp_stride;
+    uint64_t seg_buffer;
+    size_t seg_buffer_offset;
+};
+
 struct AccelBuildCommand {
     uint64_t handle;
     uint32_t instance_count;
@@ -130,6 +146,15 @@ public:
     void destroy_procedural_primitive(uint64_t handle) const {
         check(lcx_procedural_destroy(handle), "destroy_procedural_primitive");
     }
+
+    // device_interface.h:177-178: a BLAS over curve segments, instanced like a mesh
+    [[nodiscard]] ResourceCreationInfo create_curve(const AccelOption &option) const {
+        const LcxAccelOption o = option.c();
+        ResourceCreationInfo info;
+        check(lcx_curve_create(&o, &info.handle), "create_curve");
+        return info;
+    }
+    void destroy_curve(uint64_t handle) const { check(lcx_curve_destroy(handle), "destroy_curve"); }
 
     // device_interface.h create_motion_instance: a mesh moved by matrix keyframes (row-major 3x4 each)
     [[nodiscard]] ResourceCreationInfo create_motion_instance(uint64_t mesh, const LcxMotionOption &option,
@@ -186,6 +211,12 @@ public:
         const LcxProceduralBuildCommand c{static_cast<uint32_t>(cmd.request), 0u, cmd.aabb_buffer,
                                           cmd.aabb_buffer_offset, cmd.aabb_buffer_size};
         check(lcx_procedural_build(cmd.handle, &c, stream), "ProceduralPrimitiveBuildCommand");
+    }
+    void dispatch(const CurveBuildCommand &cmd, void *stream) const {
+        const LcxCurveBuildCommand c{static_cast<uint32_t>(cmd.request), static_cast<uint32_t>(cmd.basis),
+                                     cmd.cp_buffer, cmd.cp_buffer_offset, cmd.cp_stride, cmd.cp_count,
+                                     cmd.seg_buffer, cmd.seg_buffer_offset, cmd.seg_count};
+        check(lcx_curve_build(cmd.handle, &c, stream), "CurveBuildCommand");
     }
     void dispatch(const AccelBuildCommand &cmd, void *stream) const {
         check(lcx_accel_build(cmd.handle, cmd.instance_count, static_cast<uint32_t>(cmd.request),
@@ -300,6 +331,35 @@ private:
     size_t size_;
 };
 
+class Curve {
+public:
+    // control_points: device array of `cp_count` float4 {x, y, z, radius}; segments: `seg_count` u32
+    Curve(const AccelGpuExt &ext, CurveBasis basis, uint64_t control_points, size_t cp_count, uint64_t segments,
+          size_t seg_count, const AccelOption &option = {})
+        : ext_(&ext), basis_(basis), cps_(control_points), cp_count_(cp_count), segs_(segments),
+          seg_count_(seg_count) {
+        handle_ = ext.create_curve(option).handle;
+    }
+    Curve(const Curve &) = delete;
+    Curve &operator=(const Curve &) = delete;
+    ~Curve() {
+        if (handle_) lcx_curve_destroy(handle_);
+    }
+    [[nodiscard]] CurveBuildCommand build(AccelBuildRequest request = AccelBuildRequest::FORCE_BUILD) const {
+        return CurveBuildCommand{handle_, request, basis_, cp_count_, seg_count_, cps_, 0, 16, segs_, 0};
+    }
+    [[nodiscard]] uint64_t handle() const noexcept { return handle_; }
+
+private:
+    const AccelGpuExt *ext_;
+    uint64_t handle_{0};
+    CurveBasis basis_;
+    uint64_t cps_;
+    size_t cp_count_;
+    uint64_t segs_;
+    size_t seg_count_;
+};
+
 class Accel {
 public:
     explicit Accel(const AccelGpuExt &ext, const AccelOption &option = {}) : ext_(&ext) {
@@ -319,6 +379,10 @@ public:
     void emplace_back(const ProceduralPrimitive &prim, const std::array<float, 12> &affine,
                       uint8_t visibility_mask = 0xffu, bool opaque = true, uint32_t user_id = 0) {
         emplace_handle(prim.handle(), affine, visibility_mask, opaque, user_id);
+    }
+    void emplace_back(const Curve &curve, const std::array<float, 12> &affine, uint8_t visibility_mask = 0xffu,
+                      bool opaque = true, uint32_t user_id = 0) {
+        emplace_handle(curve.handle(), affine, visibility_mask, opaque, user_id);
     }
     void emplace_handle(uint64_t primitive, const std::array<float, 12> &affine, uint8_t visibility_mask,
                         bool opaque, uint32_t user_id) {
@@ -407,6 +471,10 @@ public:
         return *this;
     }
     CommandStream &operator<<(const ProceduralPrimitiveBuildCommand &c) {
+        ext_->dispatch(c, stream_);
+        return *this;
+    }
+    CommandStream &operator<<(const CurveBuildCommand &c) {
         ext_->dispatch(c, stream_);
         return *this;
     }

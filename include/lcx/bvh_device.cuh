@@ -127,9 +127,9 @@ struct __align__(16) BlasDesc {
     float lo[3];
     uint32_t depth;
     float hi[3];
-    uint32_t valid;  // bit 0: built with at least one item; bit 1: procedural (AABB items)
+    uint32_t valid;  // bit 0: built with at least one item; bit 1: procedural (AABB items); bit 2: curve
     const MeshMotion *motion;  // vertex motion (null: static vertices)
-    uint64_t _pad;
+    const float4 *curve;       // curve BLAS: 4 Bezier control points per segment (else null)
 };
 static_assert(sizeof(BlasDesc) == 80, "BlasDesc is 80 B");
 // InstRec.mask of a procedural instance: its visibility mask in bits 8..15 and
@@ -183,6 +183,10 @@ static_assert(sizeof(InstState) == 80, "InstState is 80 B");
 // shifted up by 8 (like procedural ones), so the kernels without motion support
 // never enter them; the MotionDesc address sits in the first 8 bytes of w2o.
 constexpr uint32_t kInstMotion = 0x40000000u;
+// TLAS leaf records of curve instances carry this bit, with the visibility mask
+// shifted up by 8 as well (and kInstMotion too for a motion instance of a curve):
+// only the extended (motion and curve) kernels enter them.
+constexpr uint32_t kInstCurve = 0x20000000u;
 
 struct __align__(16) ModRec {  // == LcxModification with primitive translated
     uint32_t index, user_id, flags, vis_mask;
@@ -450,6 +454,281 @@ __host__ __device__ __forceinline__ float ordered_to_float(uint32_t u) {
     x.u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
     return x.f;
 #endif
+}
+
+// ---------------------------------------------------------------------------
+// Curves (the reference's Curve, include/luisa/runtime/rtx/curve.h, with the
+// bases of include/luisa/runtime/rhi/curve_basis.h:11-24).  A segment of a
+// curve is the union of the balls centred on its curve c(u), u in [0, 1],
+// with radius r(u); position and radius (x, y, z and w of the control points)
+// follow the segment's basis.  The build converts every segment to cubic
+// Bezier form (4 control points, 64 B, in the BLAS's `curve` array);
+// piecewise-linear segments keep their two points in slots 0 and 3 (slots 1
+// and 2 repeat them).
+//
+// A cubic segment is traced as `pieces` round cones, piece k being the convex
+// hull of the balls at u = k/pieces and (k+1)/pieces.  The build picks the
+// count so that the chords stay within 5 % of the curve's radius: with D the
+// larger of the two 4-D second differences of the Bezier points, a chord of
+// parameter length h deviates from the curve by at most 0.75 D h^2 (the
+// interpolation bound h^2/8 max|c''|, and |c''| <= 6 D), so
+// pieces = ceil(sqrt(0.75 D / eps)) with eps = 0.05 max(r_max, 1e-3 |P3 - P0|),
+// at most kCurveMaxPieces.
+//
+// Ends: piecewise-linear segments have spherical end caps (curve_basis.h:12-13).
+// Cubic segments are open (curve_basis.h:14-22) at an end where no segment of
+// the same curve goes on (the next segment of the buffer does not start where
+// this one ends): a ray whose entry point lies on that end's ball, behind the
+// end's tangent circle, enters the open tube and does not hit it.  Joints
+// between segments keep their balls, which close the small gaps that chords of
+// different directions leave.  Hits are entries only: a ray starting inside a
+// segment's volume does not hit that segment.  The hit record holds the curve
+// parameter u of the ball that touches the hit point, and bary.y = -1 (the
+// reference's curve-hit convention, include/luisa/runtime/rtx/hit.h:29-30 and
+// cpu/accel.rs:491-494).
+constexpr uint32_t kTriCurve = 0xfffffffeu;  // TriRec v1.w of a curve segment
+enum : uint32_t { kCurveLinear = 0, kCurveBSpline = 1, kCurveCatmullRom = 2, kCurveBezier = 3 };
+constexpr uint32_t kCurveMaxPieces = 32;
+// TriRec of a curve segment: v0.w = prim id, v1.w = kTriCurve, v2.xy = address
+// of its 4 Bezier points, v2.z = pieces, v2.w = flags (bit 0: open start,
+// bit 1: open end).
+
+__device__ __forceinline__ float4 f4_axpy(float a, float4 x, float4 y) {  // a x + y
+    return make_float4(__fmaf_rn(a, x.x, y.x), __fmaf_rn(a, x.y, y.y), __fmaf_rn(a, x.z, y.z), __fmaf_rn(a, x.w, y.w));
+}
+__device__ __forceinline__ float4 f4_scale(float a, float4 x) { return make_float4(a * x.x, a * x.y, a * x.z, a * x.w); }
+__device__ __forceinline__ float4 f4_add(float4 x, float4 y) {
+    return make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+}
+__device__ __forceinline__ float4 f4_sub(float4 x, float4 y) {
+    return make_float4(x.x - y.x, x.y - y.y, x.z - y.z, x.w - y.w);
+}
+
+// Control points q (2 for linear, else 4) of one segment to Bezier form p[4]
+// (the uniform cubic B-spline and Catmull-Rom (tension 1/2) basis changes).
+__device__ __forceinline__ void curve_to_bezier(uint32_t basis, const float4 *q, float4 p[4]) {
+    if (basis == kCurveLinear) {
+        p[0] = p[1] = q[0];
+        p[2] = p[3] = q[1];
+    } else if (basis == kCurveBSpline) {  // (q0 + 4 q1 + q2)/6, (2 q1 + q2)/3, (q1 + 2 q2)/3, (q1 + 4 q2 + q3)/6
+        p[0] = f4_scale(1.0f / 6.0f, f4_add(f4_axpy(4.0f, q[1], q[0]), q[2]));
+        p[1] = f4_scale(1.0f / 3.0f, f4_axpy(2.0f, q[1], q[2]));
+        p[2] = f4_scale(1.0f / 3.0f, f4_axpy(2.0f, q[2], q[1]));
+        p[3] = f4_scale(1.0f / 6.0f, f4_add(f4_axpy(4.0f, q[2], q[1]), q[3]));
+    } else if (basis == kCurveCatmullRom) {  // q1, q1 + (q2 - q0)/6, q2 - (q3 - q1)/6, q2
+        p[0] = q[1];
+        p[1] = f4_axpy(1.0f / 6.0f, f4_sub(q[2], q[0]), q[1]);
+        p[2] = f4_axpy(-1.0f / 6.0f, f4_sub(q[3], q[1]), q[2]);
+        p[3] = q[2];
+    } else {
+        p[0] = q[0];
+        p[1] = q[1];
+        p[2] = q[2];
+        p[3] = q[3];
+    }
+}
+
+__device__ __forceinline__ float f4_norm2(float4 x) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)),
+                     __fadd_rn(__fmul_rn(x.z, x.z), __fmul_rn(x.w, x.w)));
+}
+
+// Round cones a segment is traced as (see above).  Every operation is
+// separately rounded so that a CPU restatement gets the same count.
+__device__ __forceinline__ uint32_t curve_pieces(uint32_t basis, const float4 p[4]) {
+    if (basis == kCurveLinear) return 1u;
+    const float4 d0 = make_float4(__fadd_rn(__fsub_rn(p[0].x, __fmul_rn(2.0f, p[1].x)), p[2].x),
+                                  __fadd_rn(__fsub_rn(p[0].y, __fmul_rn(2.0f, p[1].y)), p[2].y),
+                                  __fadd_rn(__fsub_rn(p[0].z, __fmul_rn(2.0f, p[1].z)), p[2].z),
+                                  __fadd_rn(__fsub_rn(p[0].w, __fmul_rn(2.0f, p[1].w)), p[2].w));
+    const float4 d1 = make_float4(__fadd_rn(__fsub_rn(p[1].x, __fmul_rn(2.0f, p[2].x)), p[3].x),
+                                  __fadd_rn(__fsub_rn(p[1].y, __fmul_rn(2.0f, p[2].y)), p[3].y),
+                                  __fadd_rn(__fsub_rn(p[1].z, __fmul_rn(2.0f, p[2].z)), p[3].z),
+                                  __fadd_rn(__fsub_rn(p[1].w, __fmul_rn(2.0f, p[2].w)), p[3].w));
+    const float D = __fsqrt_rn(fmaxf(f4_norm2(d0), f4_norm2(d1)));
+    const float rmax = fmaxf(fmaxf(p[0].w, p[1].w), fmaxf(p[2].w, p[3].w));
+    const float4 ch = make_float4(__fsub_rn(p[3].x, p[0].x), __fsub_rn(p[3].y, p[0].y), __fsub_rn(p[3].z, p[0].z), 0.0f);
+    const float len = __fsqrt_rn(f4_norm2(ch));
+    const float eps = __fmul_rn(0.05f, fmaxf(rmax, __fmul_rn(1e-3f, len)));
+    if (!(D > 0.0f)) return 1u;  // a straight segment (or NaN input)
+    if (!(eps > 0.0f)) return kCurveMaxPieces;
+    const float n = ceilf(__fsqrt_rn(__fdiv_rn(__fmul_rn(0.75f, D), eps)));
+    if (!(n < float(kCurveMaxPieces))) return kCurveMaxPieces;
+    return n < 1.0f ? 1u : uint32_t(n);
+}
+
+// Point and radius of a Bezier segment at u (Bernstein form; exact at 0 and 1).
+__device__ __forceinline__ float4 bezier_at(const float4 p[4], float u) {
+    const float s = 1.0f - u;
+    const float b0 = s * s * s, b1 = 3.0f * u * s * s, b2 = 3.0f * u * u * s, b3 = u * u * u;
+    return f4_axpy(b3, p[3], f4_axpy(b2, p[2], f4_axpy(b1, p[1], f4_scale(b0, p[0]))));
+}
+
+// Entry of the ray o + t d into the round cone of balls (a.xyz, a.w) and
+// (b.xyz, b.w) (radii >= 0): the convex hull of the two balls, the union of
+// the balls along the segment with linearly interpolated radius.  A convex
+// body meets a line in one interval, whose start is the smallest start among
+// its parts (the two balls and the truncated cone between the circles where
+// the hull touches them).  Returns true if that start lies in [tmin, tmax],
+// with the ball parameter u in [0, 1] of the hit point and `part` 0 (start
+// ball, behind its tangent circle), 1 (the cone) or 2 (end ball).  The ray is
+// re-based at its point closest to the cone's middle, which keeps the
+// quadratics well conditioned for far-away origins.
+__device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, float4 b, float tmin, float tmax,
+                                                 float &t_out, float &u_out, int &part) {
+    const float kInf = __int_as_float(0x7f800000);
+    const float dd = d.x * d.x + d.y * d.y + d.z * d.z;
+    const float3 m = make_float3(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z));
+    const float tc = ((m.x - o.x) * d.x + (m.y - o.y) * d.y + (m.z - o.z) * d.z) / dd;
+    const float3 os = make_float3(__fmaf_rn(tc, d.x, o.x), __fmaf_rn(tc, d.y, o.y), __fmaf_rn(tc, d.z, o.z));
+    const float3 ba = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
+    const float L2 = ba.x * ba.x + ba.y * ba.y + ba.z * ba.z;
+    const float L = sqrtf(L2);
+    const float dr = a.w - b.w;
+    float best = kInf;
+    int bp = -1;
+    // balls: smaller root of |os + t d - c|^2 = r^2
+    auto ball = [&](float4 c, int which) {
+        const float3 oc = make_float3(os.x - c.x, os.y - c.y, os.z - c.z);
+        const float hb = oc.x * d.x + oc.y * d.y + oc.z * d.z;
+        const float cc = (oc.x * oc.x + oc.y * oc.y + oc.z * oc.z) - c.w * c.w;
+        const float disc = hb * hb - dd * cc;
+        if (disc < 0.0f) return;
+        const float t = (-hb - sqrtf(disc)) / dd;
+        if (t < best) {
+            best = t;
+            bp = which;
+        }
+    };
+    if (!(L > fabsf(dr))) {  // one ball holds the other: the larger ball alone
+        ball(a.w >= b.w ? a : b, 3);
+    } else {
+        ball(a, 0);
+        ball(b, 2);
+        // the truncated cone: s = axial coordinate from a, rho = distance from the axis;
+        // its side is rho cos + s sin = ra for s in [ra sin, L + rb sin]
+        const float inv = 1.0f / L;
+        const float3 w = make_float3(ba.x * inv, ba.y * inv, ba.z * inv);
+        const float sn = dr * inv;
+        const float c2 = fmaxf((1.0f - sn) * (1.0f + sn), 0.0f);
+        const float3 q0 = make_float3(os.x - a.x, os.y - a.y, os.z - a.z);
+        const float s0 = q0.x * w.x + q0.y * w.y + q0.z * w.z;
+        const float sd = d.x * w.x + d.y * w.y + d.z * w.z;
+        const float qd = q0.x * d.x + q0.y * d.y + q0.z * d.z;
+        const float qq = q0.x * q0.x + q0.y * q0.y + q0.z * q0.z;
+        const float s_lo = a.w * sn, s_hi = L + b.w * sn;
+        float lo = -kInf, hi = kInf;
+        if (sd != 0.0f) {
+            const float t1 = (s_lo - s0) / sd, t2 = (s_hi - s0) / sd;
+            lo = fminf(t1, t2);
+            hi = fmaxf(t1, t2);
+        } else if (!(s0 >= s_lo && s0 <= s_hi)) {
+            lo = kInf;
+        }
+        // f(t) = c2 |q|^2 - s^2 + 2 ra sn s - ra^2 <= 0 inside the (one-sheeted, within the slab) cone
+        const float A = c2 * dd - sd * sd;
+        const float hB = c2 * qd - s0 * sd + a.w * sn * sd;
+        const float C = c2 * qq - s0 * s0 + 2.0f * a.w * sn * s0 - a.w * a.w;
+        if (lo <= hi) {
+            if (A != 0.0f) {
+                const float disc = hB * hB - A * C;
+                if (disc >= 0.0f) {
+                    const float sq = sqrtf(disc);
+                    const float qv = -(hB + copysignf(sq, hB));
+                    float r1 = qv / A, r2 = (qv != 0.0f) ? C / qv : r1;
+                    if (r1 > r2) {
+                        const float tt = r1;
+                        r1 = r2;
+                        r2 = tt;
+                    }
+                    if (A > 0.0f) {
+                        lo = fmaxf(lo, r1);
+                        hi = fminf(hi, r2);
+                    } else if (lo <= fminf(hi, r1)) {  // f <= 0 outside [r1, r2]: one side lies in the slab
+                        hi = fminf(hi, r1);
+                    } else {
+                        lo = fmaxf(lo, r2);
+                    }
+                } else if (A > 0.0f) {
+                    lo = kInf;
+                }
+            } else if (hB != 0.0f) {
+                const float tr = -C / (2.0f * hB);
+                if (hB > 0.0f)
+                    hi = fminf(hi, tr);
+                else
+                    lo = fmaxf(lo, tr);
+            } else if (C > 0.0f) {
+                lo = kInf;
+            }
+            if (lo <= hi && lo < best) {
+                best = lo;
+                bp = 1;
+            }
+        }
+    }
+    if (bp < 0) return false;
+    const float t = tc + best;
+    if (!(t >= tmin && t <= tmax)) return false;
+    // the ball touching the hit point: on the cone side its centre sits rho tan below the point's s
+    float u;
+    if (bp == 0)
+        u = 0.0f;
+    else if (bp == 2)
+        u = 1.0f;
+    else if (bp == 3)
+        u = a.w >= b.w ? 0.0f : 1.0f;
+    else {
+        const float3 x = make_float3(os.x + best * d.x - a.x, os.y + best * d.y - a.y, os.z + best * d.z - a.z);
+        const float s = (x.x * ba.x + x.y * ba.y + x.z * ba.z) / L;
+        const float rho = sqrtf(fmaxf(x.x * x.x + x.y * x.y + x.z * x.z - s * s, 0.0f));
+        const float sn = dr / L;
+        const float cs = sqrtf(fmaxf((1.0f - sn) * (1.0f + sn), 0.0f));
+        u = fminf(fmaxf((s - rho * sn / cs) / L, 0.0f), 1.0f);
+    }
+    t_out = t;
+    u_out = u;
+    part = bp == 3 ? 1 : bp;  // a lone ball is never an open end's cap
+    return true;
+}
+
+// Closest entry into curve segment `cp` (4 Bezier points) with t in [tmin, tmax].
+__device__ __forceinline__ bool curve_intersect(const float4 *cp, uint32_t pieces, uint32_t flags, float3 o, float3 d,
+                                             float tmin, float tmax, float &t_out, float &u_out) {
+    float4 p[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) p[k] = bvh_ld(cp + k);
+    pieces = min(max(pieces, 1u), kCurveMaxPieces);
+    const float dd = d.x * d.x + d.y * d.y + d.z * d.z;
+    if (!(dd > 0.0f)) return false;
+    bool found = false;
+    float4 c0 = p[0];
+    c0.w = fmaxf(c0.w, 0.0f);
+    for (uint32_t k = 0; k < pieces; k++) {
+        float4 c1 = (k + 1 == pieces) ? p[3] : bezier_at(p, float(k + 1) / float(pieces));
+        c1.w = fmaxf(c1.w, 0.0f);
+        // cull by the piece's bounding sphere: distance from its middle to the ray's line
+        const float3 mc = make_float3(0.5f * (c0.x + c1.x) - o.x, 0.5f * (c0.y + c1.y) - o.y, 0.5f * (c0.z + c1.z) - o.z);
+        const float3 h = make_float3(0.5f * (c1.x - c0.x), 0.5f * (c1.y - c0.y), 0.5f * (c1.z - c0.z));
+        const float R = sqrtf(h.x * h.x + h.y * h.y + h.z * h.z) + fmaxf(c0.w, c1.w);
+        const float3 cr = make_float3(mc.y * d.z - mc.z * d.y, mc.z * d.x - mc.x * d.z, mc.x * d.y - mc.y * d.x);
+        const float dist2 = (cr.x * cr.x + cr.y * cr.y + cr.z * cr.z) / dd;
+        if (R > 0.0f && dist2 <= 1.0001f * R * R) {
+            float t, u;
+            int part;
+            if (round_cone_entry(o, d, c0, c1, tmin, tmax, t, u, part)) {
+                const bool open_cap = (part == 0 && k == 0 && (flags & 1u)) || (part == 2 && k + 1 == pieces && (flags & 2u));
+                if (!open_cap) {
+                    tmax = t;
+                    t_out = t;
+                    u_out = fminf((float(k) + u) / float(pieces), 1.0f);
+                    found = true;
+                }
+            }
+        }
+        c0 = c1;
+    }
+    return found;
 }
 
 }  // namespace lcx

@@ -242,6 +242,54 @@ LCX_API int lcx_mesh_build_batch_reserve(const uint64_t *meshes, const LcxMeshBu
  * lcx_mesh_build.  Empty boxes (min > max on an axis) are never reported. */
 LCX_API int lcx_procedural_build(uint64_t handle, const LcxProceduralBuildCommand *command, void *stream);
 
+/* ------------------------------------------------------------------ curve */
+
+/* CurveBasis (include/luisa/runtime/rhi/curve_basis.h:11-24): 2 control points
+ * per segment for PIECEWISE_LINEAR, 4 for the others. */
+#define LCX_CURVE_PIECEWISE_LINEAR 0u
+#define LCX_CURVE_CUBIC_BSPLINE 1u
+#define LCX_CURVE_CATMULL_ROM 2u
+#define LCX_CURVE_BEZIER 3u
+
+/* CurveBuildCommand (include/luisa/runtime/rhi/command.h:446-486; C ABI
+ * src/rust/luisa_compute_api_types/src/lib.rs:620-631).  Control points are
+ * float4 {x, y, z, radius} records `cp_stride` bytes apart (>= 16 and a multiple of 4, as the reference's
+ * Embree path requires, cpu/accel.rs:160); the segment buffer holds one u32 per
+ * segment, the index of its first control point. */
+typedef struct LcxCurveBuildCommand {
+    uint32_t request;  /* LCX_REQUEST_* */
+    uint32_t basis;    /* LCX_CURVE_* */
+    uint64_t cp_buffer;
+    size_t cp_buffer_offset;
+    size_t cp_stride;
+    size_t cp_count;
+    uint64_t seg_buffer;
+    size_t seg_buffer_offset;
+    size_t seg_count;
+} LcxCurveBuildCommand;
+
+/* DeviceInterface::create_curve / destroy_curve (device_interface.h:177-178).  A curve
+ * is a BLAS over its segments; an accel instances it like a mesh
+ * (Modification.primitive = its handle), with a transform, a mask and motion
+ * instances (lcx_motion_instance_create) as for meshes.  Segment i is the
+ * union of balls along its curve (position and radius from the basis); hits
+ * report prim = i, bary = (u, -1) with u the curve parameter of the hit, and
+ * the ray's t (hit.h:29-30).  Linear segments have spherical end caps; cubic
+ * segments are open where the next segment of the buffer does not continue
+ * them.  Cubic segments are traced as up to 32 round cones whose chords stay
+ * within 5 % of the radius of the exact curve; hits are entries only (a ray
+ * starting inside a segment does not hit it).  Accels holding curves trace with
+ * the extended kernels (those of motion), through lcx_trace_* and the
+ * *_motion / *_host / *_ex entry points; lcx_trace_jobs and lcx::ray_query do
+ * not take them. */
+LCX_API int lcx_curve_create(const LcxAccelOption *option, uint64_t *out_handle);
+LCX_API int lcx_curve_destroy(uint64_t handle);
+/* Builds on `stream` (every request rebuilds: the reference's PREFER_UPDATE
+ * refit of the control points gives the same hits as a rebuild).  Errors: a
+ * segment whose control points run past cp_count (LCX_ERR_INVALID_ARG); a
+ * build inside a CUDA graph capture. */
+LCX_API int lcx_curve_build(uint64_t handle, const LcxCurveBuildCommand *command, void *stream);
+
 /* ------------------------------------------------------------------ accel */
 
 /* DeviceInterface::create_accel / destroy_accel: device_interface.h:183-184. */

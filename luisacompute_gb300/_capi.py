@@ -63,6 +63,15 @@ class LcxProceduralBuildCommand(ctypes.Structure):
                 ("aabb_buffer_offset", c_size_t), ("aabb_buffer_size", c_size_t)]
 
 
+class LcxCurveBuildCommand(ctypes.Structure):
+    _fields_ = [("request", c_uint32), ("basis", c_uint32), ("cp_buffer", c_uint64), ("cp_buffer_offset", c_size_t),
+                ("cp_stride", c_size_t), ("cp_count", c_size_t), ("seg_buffer", c_uint64),
+                ("seg_buffer_offset", c_size_t), ("seg_count", c_size_t)]
+
+
+CURVE_PIECEWISE_LINEAR, CURVE_CUBIC_BSPLINE, CURVE_CATMULL_ROM, CURVE_BEZIER = 0, 1, 2, 3
+
+
 class LcxInstanceBuffer(ctypes.Structure):
     _fields_ = [("states", c_void_p), ("count", c_uint32), ("_pad", c_uint32)]
 
@@ -103,6 +112,9 @@ _SIGS = {
     "lcx_procedural_create": (c_int, [POINTER(LcxAccelOption), POINTER(c_uint64)]),
     "lcx_procedural_destroy": (c_int, [c_uint64]),
     "lcx_procedural_build": (c_int, [c_uint64, POINTER(LcxProceduralBuildCommand), c_void_p]),
+    "lcx_curve_create": (c_int, [POINTER(LcxAccelOption), POINTER(c_uint64)]),
+    "lcx_curve_destroy": (c_int, [c_uint64]),
+    "lcx_curve_build": (c_int, [c_uint64, POINTER(LcxCurveBuildCommand), c_void_p]),
     "lcx_get_build_morton": (c_int, [POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
     "lcx_set_trace_reorder": (c_int, [c_uint32, c_uint32]),
     "lcx_set_trace_stack": (c_int, [c_uint32]),

@@ -18,13 +18,15 @@ import ctypes
 import numpy as np
 
 from . import _capi
-from ._capi import (HINT_FAST_BUILD, HINT_FAST_TRACE, MOD_OPAQUE_OFF, MOD_OPAQUE_ON, MOD_PRIMITIVE, MOD_TRANSFORM,
-                    MOD_USER_ID, MOD_VISIBILITY, NODES_FP32, NODES_QUANT8, REQUEST_FORCE_BUILD,
-                    REQUEST_PREFER_UPDATE, LcxAccelOption, LcxAccelStats, LcxMeshBuildCommand, check)
+from ._capi import (CURVE_BEZIER, CURVE_CATMULL_ROM, CURVE_CUBIC_BSPLINE, CURVE_PIECEWISE_LINEAR, HINT_FAST_BUILD,
+                    HINT_FAST_TRACE, MOD_OPAQUE_OFF, MOD_OPAQUE_ON, MOD_PRIMITIVE, MOD_TRANSFORM, MOD_USER_ID,
+                    MOD_VISIBILITY, NODES_FP32, NODES_QUANT8, REQUEST_FORCE_BUILD, REQUEST_PREFER_UPDATE,
+                    LcxAccelOption, LcxAccelStats, LcxMeshBuildCommand, check)
 from .scenes import MOD_DTYPE
 
-__all__ = ["AccelOption", "Mesh", "ProceduralPrimitive", "Accel", "HINT_FAST_TRACE", "HINT_FAST_BUILD", "REQUEST_FORCE_BUILD",
-           "REQUEST_PREFER_UPDATE", "NODES_FP32", "NODES_QUANT8", "stream_handle"]
+__all__ = ["AccelOption", "Mesh", "ProceduralPrimitive", "Curve", "Accel", "HINT_FAST_TRACE", "HINT_FAST_BUILD",
+           "REQUEST_FORCE_BUILD", "REQUEST_PREFER_UPDATE", "NODES_FP32", "NODES_QUANT8", "CURVE_PIECEWISE_LINEAR",
+           "CURVE_CUBIC_BSPLINE", "CURVE_CATMULL_ROM", "CURVE_BEZIER", "stream_handle"]
 
 
 def _torch():
@@ -142,6 +144,54 @@ class ProceduralPrimitive:
     def destroy(self):
         if getattr(self, "handle", 0):
             check(self.lib.lcx_procedural_destroy(self.handle), "lcx_procedural_destroy")
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Curve:
+    """A BLAS over curve segments (include/luisa/runtime/rtx/curve.h): ``control_points`` is an (N, 4)
+    float32 CUDA tensor of (x, y, z, radius) records, ``segments`` a uint32 / int32 CUDA tensor with the
+    first control point of each segment; ``basis`` is one of CURVE_PIECEWISE_LINEAR, CURVE_CUBIC_BSPLINE,
+    CURVE_CATMULL_ROM, CURVE_BEZIER.  Both buffers are borrowed like a mesh's.  Instanced by an Accel like
+    a Mesh; hits on it report prim = segment, bary = (u, -1)."""
+
+    def __init__(self, basis: int, control_points, segments, option: AccelOption | None = None):
+        torch = _torch()
+        self.lib = _capi.load()
+        if not control_points.is_cuda or control_points.dtype != torch.float32 or control_points.dim() != 2 \
+                or control_points.shape[1] != 4 or not control_points.is_contiguous():
+            raise ValueError("control_points must be a contiguous (N, 4) float32 CUDA tensor")
+        if not segments.is_cuda or segments.dtype not in (torch.int32, torch.uint32) or segments.dim() != 1 \
+                or not segments.is_contiguous():
+            raise ValueError("segments must be a contiguous 1-D int32 / uint32 CUDA tensor")
+        self.basis = int(basis)
+        self.control_points = control_points
+        self.segments = segments
+        h = ctypes.c_uint64(0)
+        check(self.lib.lcx_curve_create(ctypes.byref((option or AccelOption()).c()), ctypes.byref(h)),
+              "lcx_curve_create")
+        self.handle = h.value
+
+    def build(self, request: int = REQUEST_FORCE_BUILD, stream=None) -> "Curve":
+        cmd = _capi.LcxCurveBuildCommand(request, self.basis, self.control_points.data_ptr(), 0, 16,
+                                         self.control_points.shape[0], self.segments.data_ptr(), 0,
+                                         self.segments.numel())
+        check(self.lib.lcx_curve_build(self.handle, ctypes.byref(cmd), stream_handle(stream)), "lcx_curve_build")
+        return self
+
+    def stats(self) -> LcxAccelStats:
+        s = LcxAccelStats()
+        check(self.lib.lcx_mesh_stats(self.handle, ctypes.byref(s)), "lcx_mesh_stats")
+        return s
+
+    def destroy(self):
+        if getattr(self, "handle", 0):
+            check(self.lib.lcx_curve_destroy(self.handle), "lcx_curve_destroy")
             self.handle = 0
 
     def __del__(self):

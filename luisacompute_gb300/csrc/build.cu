@@ -142,6 +142,40 @@ __global__ void __launch_bounds__(kPrepBlock) k_tri_prep(const SegInput *segs, u
             h.x = bx[3];
             h.y = bx[4];
             h.z = bx[5];
+        } else if ((g.kind & 0xffu) == kSegCurves) {
+            // a curve segment: its control points to Bezier form (kept in the BLAS's curve
+            // array); the box holds the Bezier hull grown by the largest control radius,
+            // which bounds every ball the tracer places along the segment
+            const uint32_t basis = g.kind >> 8;
+            const uint32_t need = basis == kCurveLinear ? 2u : 4u;
+            const uint32_t first = reinterpret_cast<const uint32_t *>(g.tbase)[local];
+            bad = first > g.vcount || g.vcount - first < need;
+            if (!bad) {
+                float4 q[4], p[4];
+                for (uint32_t k = 0; k < 4; k++) {
+                    const float *cp = reinterpret_cast<const float *>(g.vbase + g.vstride * (first + min(k, need - 1)));
+                    q[k] = make_float4(cp[0], cp[1], cp[2], cp[3]);
+                }
+                curve_to_bezier(basis, q, p);
+                float4 *out = const_cast<float4 *>(g.desc->curve) + 4ull * local;  // the build owns the array
+                float pad = 0.0f;
+                for (int k = 0; k < 4; k++) {
+                    out[k] = p[k];
+                    l.x = fminf(l.x, p[k].x);
+                    l.y = fminf(l.y, p[k].y);
+                    l.z = fminf(l.z, p[k].z);
+                    h.x = fmaxf(h.x, p[k].x);
+                    h.y = fmaxf(h.y, p[k].y);
+                    h.z = fmaxf(h.z, p[k].z);
+                    pad = fmaxf(pad, p[k].w);
+                }
+                l.x -= pad;
+                l.y -= pad;
+                l.z -= pad;
+                h.x += pad;
+                h.y += pad;
+                h.z += pad;
+            }
         } else {
             const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * local);
             i0 = t[0];
@@ -152,7 +186,7 @@ __global__ void __launch_bounds__(kPrepBlock) k_tri_prep(const SegInput *segs, u
         if (bad) {
             atomicOr(&segctl[kSegWords * s + kSegErr], kErrBadIndex);
             atomicOr(&ctl[kCtlErr], kErrBadIndex);
-        } else if ((g.kind & 0xffu) != kSegAabbs) {
+        } else if ((g.kind & 0xffu) == kSegTriangles) {
             // vertex motion (kind >> 8 keyframes): the union over the keyframes bounds the
             // linearly interpolated triangle at every time
             const uint32_t keys = max(g.kind >> 8, 1u);
@@ -1085,6 +1119,27 @@ __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *d
                                    make_float4(bx[3], bx[4], bx[5], 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
                 return;
             }
+            if ((g.kind & 0xffu) == kSegCurves) {  // the segment's Bezier points, piece count and open ends
+                const uint32_t basis = g.kind >> 8;
+                const float4 *cp = g.desc->curve + 4ull * prim;
+                float4 p[4];
+                for (int k = 0; k < 4; k++) p[k] = cp[k];
+                const uint32_t pieces = curve_pieces(basis, p);
+                uint32_t flags = 0;
+                if (basis != kCurveLinear) {  // a cubic curve goes on where the next segment starts at this one's end
+                    const uint32_t *sg = reinterpret_cast<const uint32_t *>(g.tbase);
+                    const uint32_t step = basis == kCurveBezier ? 3u : 1u;
+                    const uint32_t first = sg[prim];
+                    if (!(prim > 0 && sg[prim - 1] + step == first)) flags |= 1u;
+                    if (!(prim + 1 < g.item_count && sg[prim + 1] == first + step)) flags |= 2u;
+                }
+                const unsigned long long a = reinterpret_cast<unsigned long long>(cp);
+                tris[pos] = TriRec{make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(prim)),
+                                   make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kTriCurve)),
+                                   make_float4(__uint_as_float(uint32_t(a)), __uint_as_float(uint32_t(a >> 32)),
+                                               __uint_as_float(pieces), __uint_as_float(flags))};
+                return;
+            }
             if (g.kind >> 8) {  // vertex motion: the motion kernels interpolate the vertices at the ray's time
                 const unsigned long long mp = reinterpret_cast<unsigned long long>(g.desc->motion);
                 tris[pos] = TriRec{make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(prim)),
@@ -1120,7 +1175,8 @@ __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *d
         bd->hi[1] = rh.y;
         bd->hi[2] = rh.z;
         bd->depth = sc[kSegDepth];
-        bd->valid = (empty ? 0u : 1u) | ((g.kind & 0xffu) == kSegAabbs ? 2u : 0u);
+        bd->valid = (empty ? 0u : 1u) | ((g.kind & 0xffu) == kSegAabbs ? 2u : 0u) |
+                    ((g.kind & 0xffu) == kSegCurves ? 4u : 0u);
     }
 }
 
@@ -1138,6 +1194,7 @@ __device__ __forceinline__ InstRec make_inst_rec(uint32_t id, const InstState *i
     r.inst_id = id;
     r.mask = !ok                ? 0u
              : (d->valid & 2u)  ? (((s.mask & 0xffu) << 8) | kInstProcedural)
+             : (d->valid & 4u)  ? (((s.mask & 0xffu) << 8) | kInstCurve | (s.motion != nullptr ? kInstMotion : 0u))
              : s.motion != nullptr ? (((s.mask & 0xffu) << 8) | kInstMotion)
                                    : (s.mask & 0xffu);
     if (ok && s.motion != nullptr) {  // the MotionDesc address instead of an inverse
@@ -1521,7 +1578,8 @@ __global__ void k_refit(RefitArgs A) {
                     bd->lo[k] = empty ? FLT_MAX : nl[k];
                     bd->hi[k] = empty ? -FLT_MAX : nh[k];
                 }
-                bd->valid = (empty ? 0u : 1u) | ((g.kind & 0xffu) == kSegAabbs ? 2u : 0u);
+                bd->valid = (empty ? 0u : 1u) | ((g.kind & 0xffu) == kSegAabbs ? 2u : 0u) |
+                            ((g.kind & 0xffu) == kSegCurves ? 4u : 0u);
             }
             return;
         }

@@ -159,7 +159,9 @@ struct MeshObj {
     size_t mem_bytes = 0;             // this mesh's share of the block
     uint32_t node_count = 0, tri_count = 0, depth = 0;
     uint32_t ref_count = 0;  // leaf items: tri_count, or more with triangle splitting
-    uint32_t kind = kSegTriangles;  // or kSegAabbs: a procedural primitive (lcx_procedural_*)
+    uint32_t kind = kSegTriangles;  // or kSegAabbs: a procedural primitive (lcx_procedural_*),
+                                    // kSegCurves: a curve (lcx_curve_*)
+    std::shared_ptr<DevBlock> curve_block;  // curves: the segments' Bezier points (64 B each)
     LcxMotionOption motion{};       // keyframe_count >= 2: vertex motion (lcx_mesh_create_motion)
     MeshMotion *d_motion = nullptr;  // after the BlasDesc in d_desc's allocation
     uint32_t seg = 0;  // segment (position in its build) within `block`
@@ -199,6 +201,7 @@ struct AccelObj {
     std::vector<std::shared_ptr<MotionObj>> inst_motion;  // motion instance per instance (null = static)
     std::vector<std::pair<std::shared_ptr<MotionObj>, uint64_t>> motion_gens;  // at the TLAS build
     bool has_motion = false;
+    bool has_curves = false;  // an instanced BLAS is a curve: traced by the extended kernels
     std::vector<uint64_t> uniq_mesh;  // the distinct nonzero handles of inst_mesh
     bool uniq_dirty = true;           // inst_mesh changed since uniq_mesh was made
     std::shared_ptr<DevBlock> block;
@@ -686,7 +689,10 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
         if (rb.ctl[kCtlErr] & kErrBadIndex) {
             for (size_t i = 0; i < count; i++)
                 if (rb.segctl[kSegWords * i + kSegErr] & kErrBadIndex)
-                    return fail(LCX_ERR_INVALID_ARG, "mesh %zu of the build: triangle index out of range (vertex count %u)",
+                    return fail(LCX_ERR_INVALID_ARG,
+                                (segs[i].kind & 0xffu) == kSegCurves
+                                    ? "curve %zu of the build: a segment's control points run past the %u given"
+                                    : "mesh %zu of the build: triangle index out of range (vertex count %u)",
                                 i, segs[i].vcount);
             return fail(LCX_ERR_INVALID_ARG, "triangle index out of range");
         }
@@ -845,7 +851,7 @@ int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, u
     p.tlas_q = a->qn;
     p.tlas_f = a->fn;
     p.insts = a->recs;
-    p.motion = a->has_motion;
+    p.motion = a->has_motion || a->has_curves;
     p.rays = reinterpret_cast<const Ray *>(d_rays);
     p.hits = reinterpret_cast<Hit *>(d_hits);
     p.ray_count = ray_count;
@@ -945,6 +951,7 @@ int lcx_mesh_destroy(uint64_t mesh) {
     std::lock_guard<std::mutex> lk(m->mtx);
     cudaDeviceSynchronize();
     m->block.reset();
+    m->curve_block.reset();
     if (m->d_desc) cudaFree(m->d_desc);
     m->d_desc = nullptr;
     return LCX_OK;
@@ -992,6 +999,71 @@ int lcx_procedural_build(uint64_t handle, const LcxProceduralBuildCommand *cmd, 
     std::vector<SegInput> segs{g};
     std::vector<uint32_t> req{cmd->request};
     return build_meshes(ms, segs, req, static_cast<cudaStream_t>(stream), retired);
+}
+
+int lcx_curve_create(const LcxAccelOption *option, uint64_t *out_handle) {
+    if (int r = lcx_mesh_create(option, out_handle)) return r;
+    auto m = find_mesh(*out_handle);
+    m->kind = kSegCurves;
+    return LCX_OK;
+}
+
+int lcx_curve_destroy(uint64_t handle) {
+    auto m = find_mesh(handle);
+    if (m && m->kind != kSegCurves) return fail(LCX_ERR_INVALID_ARG, "lcx_curve_destroy: handle is not a curve");
+    return lcx_mesh_destroy(handle);
+}
+
+// Curve builds (the reference's CurveBuildCommand visit, cpu/accel.rs:142-204;
+// CUDA: cuda_curve.cpp:37-70).  The build converts the segments to Bezier form
+// in a fresh array (the previous one stays alive for traces already queued on
+// the old tree, like a replaced BVH block) and builds the BLAS over the
+// segments' boxes; the emit writes one curve record per segment.
+int lcx_curve_build(uint64_t handle, const LcxCurveBuildCommand *cmd, void *stream) {
+    auto m = find_mesh(handle);
+    if (!m || m->kind != kSegCurves)
+        return fail(LCX_ERR_INVALID_ARG, "lcx_curve_build: unknown curve handle %llu", (unsigned long long)handle);
+    if (!cmd) return fail(LCX_ERR_INVALID_ARG, "lcx_curve_build: command is null");
+    if (cmd->request > LCX_REQUEST_FORCE_BUILD) return fail(LCX_ERR_INVALID_ARG, "invalid build request %u", cmd->request);
+    if (cmd->basis > LCX_CURVE_BEZIER) return fail(LCX_ERR_INVALID_ARG, "invalid curve basis %u", cmd->basis);
+    if (cmd->cp_stride < 16 || cmd->cp_stride % 4 != 0)
+        return fail(LCX_ERR_INVALID_ARG, "control point stride %zu must be >= 16 and a multiple of 4", cmd->cp_stride);
+    if (cmd->seg_count >= (1ull << 31) || cmd->cp_count >= (1ull << 32))
+        return fail(LCX_ERR_INVALID_ARG, "too many curve segments (%zu) or control points (%zu)", cmd->seg_count,
+                    cmd->cp_count);
+    if (cmd->seg_count && (!cmd->cp_buffer || !cmd->seg_buffer))
+        return fail(LCX_ERR_INVALID_ARG, "null control point or segment buffer");
+    if ((cmd->cp_buffer + cmd->cp_buffer_offset) % 4 != 0 || (cmd->seg_buffer + cmd->seg_buffer_offset) % 4 != 0)
+        return fail(LCX_ERR_INVALID_ARG, "control point and segment buffers must be 4-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (capturing(st)) return fail(LCX_ERR_INVALID_ARG, "curve build in a CUDA graph capture");
+    Retired retired;  // released after the mutex below
+    std::lock_guard<std::mutex> lk(m->mtx);
+    auto cblock = std::make_shared<DevBlock>();
+    cblock->bytes = 4 * sizeof(float4) * std::max<size_t>(cmd->seg_count, 1);
+    LCX_CUDA(cudaMalloc(&cblock->ptr, cblock->bytes), "cudaMalloc(curve points)");
+    const float4 *cptr = static_cast<const float4 *>(cblock->ptr);
+    LCX_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(m->d_desc) + offsetof(BlasDesc, curve), &cptr, sizeof(cptr),
+                             cudaMemcpyHostToDevice, st),
+             "curve descriptor");
+    LCX_CUDA(cudaStreamSynchronize(st), "sync");  // `cptr` is a host local
+    std::vector<MeshObj *> ms{m.get()};
+    SegInput g{};
+    g.vbase = reinterpret_cast<const unsigned char *>(cmd->cp_buffer) + cmd->cp_buffer_offset;
+    g.vstride = cmd->cp_stride;
+    g.tbase = reinterpret_cast<const unsigned char *>(cmd->seg_buffer) + cmd->seg_buffer_offset;
+    g.vcount = uint32_t(cmd->cp_count);
+    g.item_offset = 0;
+    g.item_count = uint32_t(cmd->seg_count);
+    g.kind = kSegCurves | (cmd->basis << 8);
+    g.desc = m->d_desc;
+    std::vector<SegInput> segs{g};
+    std::vector<uint32_t> req{LCX_REQUEST_FORCE_BUILD};
+    const int r = build_meshes(ms, segs, req, st, retired);
+    if (r != LCX_OK) return r;  // the old tree keeps its own points
+    if (m->curve_block) retired.blocks.push_back(std::move(m->curve_block));
+    m->curve_block = std::move(cblock);
+    return LCX_OK;
 }
 
 int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *cmd, void *stream) {
@@ -1230,6 +1302,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     std::vector<std::pair<uint64_t, uint64_t>> gens;
     uint32_t max_blas_depth = 0;
     bool mesh_motion = false;  // an instanced mesh has vertex motion
+    bool curves = false;       // an instanced BLAS is a curve
     {
         if (a->uniq_dirty) {
             std::vector<uint64_t> &uniq = a->uniq_mesh;
@@ -1246,6 +1319,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
             gens.emplace_back(h, m->generation);
             max_blas_depth = std::max(max_blas_depth, m->depth);
             mesh_motion = mesh_motion || m->motion.keyframe_count >= 2;
+            curves = curves || m->kind == kSegCurves;
         }
     }
     const uint32_t n = instance_count;
@@ -1253,6 +1327,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     bool inst_motion = false;
     for (const auto &mo : a->inst_motion) inst_motion = inst_motion || mo != nullptr;
     a->has_motion = inst_motion || mesh_motion;
+    a->has_curves = curves;
     if (inst_motion) {
         std::unordered_set<MotionObj *> seen;
         for (const auto &mo : a->inst_motion) {
@@ -1468,7 +1543,7 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
         p.tlas_q = a->qn;
         p.tlas_f = a->fn;
         p.insts = a->recs;
-        p.motion = a->has_motion;
+        p.motion = a->has_motion || a->has_curves;
     }
     p.times = d_times;
     if (d_times && reinterpret_cast<uintptr_t>(d_times) % 4 != 0)
@@ -1525,6 +1600,7 @@ int lcx_accel_device_view(uint64_t accel, LcxAccelView *out) {
         return fail(LCX_ERR_NOT_BUILT, "a mesh of the accel was destroyed, rebuilt or refit; rebuild the accel");
     if (a->has_motion)
         return fail(LCX_ERR_INVALID_ARG, "lcx::ray_query does not trace motion instances");
+    if (a->has_curves) return fail(LCX_ERR_INVALID_ARG, "lcx::ray_query does not trace curves");
     const uint32_t need = a->depth + a->max_blas_depth + 3;
     if (int(need) > kStackSize)
         return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the query stack (%d)", a->depth,
@@ -1560,6 +1636,8 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
         if (a->has_motion)
             return fail(LCX_ERR_INVALID_ARG, "job %u: accels with motion instances are traced with "
                                              "lcx_trace_closest_motion / lcx_trace_any_motion", i);
+        if (a->has_curves)
+            return fail(LCX_ERR_INVALID_ARG, "job %u: accels with curves are traced with lcx_trace_*", i);
         const uint32_t need = a->depth + a->max_blas_depth + 3;
         if (int(need) > kStackSize) return fail(LCX_ERR_DEPTH, "job %u: BVH too deep for the traversal stack", i);
         depth_need = std::max(depth_need, need);
@@ -1822,7 +1900,7 @@ int lcx_motion_instance_create(uint64_t mesh, const LcxMotionOption *option, uin
     auto m = find_mesh(mesh);
     if (!m) return fail(LCX_ERR_INVALID_ARG, "lcx_motion_instance_create: unknown mesh handle %llu",
                         (unsigned long long)mesh);
-    if (m->kind != kSegTriangles) return fail(LCX_ERR_INVALID_ARG, "motion instances of procedural primitives are not supported");
+    if (m->kind == kSegAabbs) return fail(LCX_ERR_INVALID_ARG, "motion instances of procedural primitives are not supported");
     auto mo = std::make_shared<MotionObj>();
     mo->child = mesh;
     mo->opt = o;

@@ -20,11 +20,14 @@ struct SegInput {
     uint32_t vcount;
     uint32_t item_offset;        // first item of this segment among all items of the build
     uint32_t item_count;
-    uint32_t kind;               // low byte: kSegTriangles (vbase, tbase) or kSegAabbs (vbase: 24-byte AABBs);
-                                 // bits 8+: vertex-motion keyframes (vbase holds them back to back, vcount each)
+    uint32_t kind;               // low byte: kSegTriangles (vbase, tbase) or kSegAabbs (vbase: 24-byte AABBs)
+                                 // or kSegCurves (vbase: control points, vcount of them; tbase: u32 segment
+                                 // starts; the Bezier form goes to desc->curve);
+                                 // bits 8+: triangles: vertex-motion keyframes (vbase holds them back to back,
+                                 // vcount each); curves: the basis (kCurve*)
     BlasDesc *desc;              // BLAS descriptor the emit fills in (null for a TLAS)
 };
-enum : uint32_t { kSegTriangles = 0, kSegAabbs = 1 };
+enum : uint32_t { kSegTriangles = 0, kSegAabbs = 1, kSegCurves = 2 };
 static_assert(sizeof(SegInput) == 48, "SegInput is 48 B");
 
 // Per-segment control words.
@@ -181,7 +184,7 @@ struct TraceParams {
     uint32_t job_count;
     const uint32_t *order;  // non-null: the k-th ray taken is rays[order[k]] (single-job launches)
     uint32_t short_stack;   // shared-memory stack entries per thread: 8, 16 or 24 (single-job, mode 0)
-    bool motion;            // the accel has motion instances: the motion kernels (mode 0) run the call
+    bool motion;            // the accel has motion or curves: the extended kernels (mode 0) run the call
     const float *times;     // motion launches: per-ray times (null: time 0)
 };
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st);

@@ -39,6 +39,11 @@ constexpr int kTraceBlock = 128;
 #ifndef LCX_TRACE_MIN_BLOCKS_F
 #define LCX_TRACE_MIN_BLOCKS_F 7
 #endif
+// The extended kernels (motion, curves) carry the curve test and the motion
+// interpolation: a larger register budget keeps them from spilling.
+#ifndef LCX_TRACE_MIN_BLOCKS_EXT
+#define LCX_TRACE_MIN_BLOCKS_EXT 4
+#endif
 // Stack entries kept in shared memory per thread (the rest of the kStackSize
 // entries go to local memory): a launch-time choice among 8, 16 (default) and
 // 24 for the single-job closest / any kernels; 16 for the others.
@@ -60,6 +65,8 @@ constexpr uint32_t kMaxRaySteps = 1u << 22;  // per-ray bound: a corrupt tree en
 // Per-lane traversal state and the operations both loop structures share.
 // kMulti: the launch serves several jobs (scenes); each lane takes its job's
 // TLAS, instance table, mask and buffers when it takes a ray.
+// kMotion: the extended kernels, for accels with motion instances, vertex-motion
+// meshes or curves (each ray has a time; curve segments get the curve test).
 template <int kLayout, bool kAny, bool kCount, bool kMulti, int kShort, bool kMotion = false>
 struct Walker {
     static constexpr int kShortStack = kShort < kStackSize ? kShort : kStackSize;
@@ -81,6 +88,7 @@ struct Walker {
     uint32_t best_inst = kInvalid, best_prim = kInvalid;
     // current-space ray (world at the TLAS level, object inside a BLAS)
     float ox = 0, oy = 0, oz = 0, ix = 1, iy = 1, iz = 1;
+    float rdx = 0, rdy = 0, rdz = 1;  // current-space direction (read by the curve test only)
     uint32_t octinv = 0;
     WtRay wt{};
     uint2 G = make_uint2(0, 0);
@@ -173,6 +181,11 @@ struct Walker {
         iy = slab_rcp(wdy);
         iz = slab_rcp(wdz);
         octinv = octant_inv(wdx, wdy, wdz);
+        if (kMotion) {
+            rdx = wdx;
+            rdy = wdy;
+            rdz = wdz;
+        }
     }
 
     // Take the front child of node group G, push the rest, intersect it.
@@ -212,6 +225,28 @@ struct Walker {
             const float4 *tp = reinterpret_cast<const float4 *>(blas_tris + Gt.x + k);
             float4 a = bvh_ld(tp), b = bvh_ld(tp + 1), c = bvh_ld(tp + 2);
             if constexpr (kMotion) {
+                if (__float_as_uint(b.w) == kTriCurve) {  // a curve segment
+                    if (kCount) c_tris++;
+                    const float4 *cp = reinterpret_cast<const float4 *>(
+                        (unsigned long long)__float_as_uint(c.x) | ((unsigned long long)__float_as_uint(c.y) << 32));
+                    float t, u;
+                    if (curve_intersect(cp, __float_as_uint(c.z), __float_as_uint(c.w), make_float3(ox, oy, oz),
+                                        make_float3(rdx, rdy, rdz), tmin, best_t, t, u)) {
+                        if (kAny) {
+                            occluded = true;
+                            return true;
+                        }
+                        const uint32_t prim = __float_as_uint(a.w);
+                        if (t < best_t || cur_inst < best_inst || (cur_inst == best_inst && prim < best_prim)) {
+                            best_t = t;
+                            best_u = u;
+                            best_v = -1.0f;
+                            best_inst = cur_inst;
+                            best_prim = prim;
+                        }
+                    }
+                    continue;
+                }
                 if (__float_as_uint(b.w) == kTriMotion) {  // a vertex-motion mesh: its triangle at the ray's time
                     const MeshMotion *mm = reinterpret_cast<const MeshMotion *>(
                         (unsigned long long)__float_as_uint(c.x) | ((unsigned long long)__float_as_uint(c.y) << 32));
@@ -347,8 +382,11 @@ struct Walker {
                 w[8] = r2.x, w[9] = r2.y, w[10] = r2.z, w[11] = r2.w;
             } else {  // a motion instance: the matrix at the ray's time, inverted as a static one is
                 uint32_t vis = m4.w;
-                const bool moving = (vis & (kInstMotion | kInstProcedural)) == kInstMotion;
-                if (moving) vis = (vis >> 8) & 0xffu;
+                // motion and curve instances hold their mask in bits 8..15; procedural ones stay
+                // unreachable (bit 31 and a shifted mask)
+                const bool shifted = (vis & kInstProcedural) == 0u && (vis & (kInstMotion | kInstCurve)) != 0u;
+                const bool moving = shifted && (vis & kInstMotion) != 0u;
+                if (shifted) vis = (vis >> 8) & 0xffu;
                 if ((vis & (kMulti ? mask : P.mask)) == 0u) continue;
                 const float4 r0 = bvh_ld(reinterpret_cast<const float4 *>(ip));
                 const float4 r1 = bvh_ld(reinterpret_cast<const float4 *>(ip + 1));
@@ -376,6 +414,11 @@ struct Walker {
             iz = slab_rcp(dz);
             octinv = octant_inv(dx, dy, dz);
             wt = wt_setup(ox, oy, oz, dx, dy, dz);
+            if (kMotion) {
+                rdx = dx;
+                rdy = dy;
+                rdz = dz;
+            }
             const unsigned long long qptr = (unsigned long long)pp.x | ((unsigned long long)pp.y << 32);
             const unsigned long long fptr = (unsigned long long)m4.x | ((unsigned long long)m4.y << 32);
             const unsigned long long tptr = (unsigned long long)pp.z | ((unsigned long long)pp.w << 32);
@@ -424,8 +467,9 @@ struct Walker {
 // together; a lane that finds items keeps walking (holding them in Gp) while
 // any lane of the warp is still searching, then all lanes handle items.
 template <int kLayout, bool kAny, bool kCount, int kMode, bool kMulti, int kShort, bool kMotion = false>
-__global__ void __launch_bounds__(kTraceBlock,
-                                  kLayout == LCX_NODES_QUANT8 ? LCX_TRACE_MIN_BLOCKS_Q : LCX_TRACE_MIN_BLOCKS_F)
+__global__ void __launch_bounds__(kTraceBlock, kMotion                       ? LCX_TRACE_MIN_BLOCKS_EXT
+                                               : kLayout == LCX_NODES_QUANT8 ? LCX_TRACE_MIN_BLOCKS_Q
+                                                                             : LCX_TRACE_MIN_BLOCKS_F)
     k_trace(TraceParams P) {
     using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort, kMotion>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
@@ -954,7 +998,7 @@ cudaError_t launch_mode(const TraceParams &p, int layout, bool any, bool countin
 }  // namespace
 
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
-    if (p.motion) {  // accels with motion instances: loop mode 0 with per-ray times
+    if (p.motion) {  // accels with motion or curves: the extended kernels, loop mode 0
         if (layout == LCX_NODES_QUANT8) {
             if (counting) return launch_one<LCX_NODES_QUANT8, false, true, 0, false, kDefaultShortStack, true>(p, st);
             return any ? launch_one<LCX_NODES_QUANT8, true, false, 0, false, kDefaultShortStack, true>(p, st)

@@ -304,3 +304,36 @@ def batch_meshes(count: int = 4096, lo: int = 64, hi: int = 262144, seed: int = 
     rng = np.random.default_rng(seed)
     targets = np.exp(rng.uniform(np.log(lo), np.log(hi), count)).astype(np.int64)
     return [displaced_mesh(int(t), rng) for t in targets]
+
+
+# ---------------------------------------------------------------- curves
+CURVE_STEP = {0: 1, 1: 1, 2: 1, 3: 3}  # control points between segment starts, per basis
+CURVE_POINTS = {0: 2, 1: 4, 2: 4, 3: 4}  # control points per segment
+
+
+def curve_segments(n_curves: int, n_cp: int, basis: int) -> np.ndarray:
+    """Segment starts of ``n_curves`` curves of ``n_cp`` consecutive control points each: every
+    segment a basis allows along each curve (Bezier segments share their end points)."""
+    step, need = CURVE_STEP[basis], CURVE_POINTS[basis]
+    per = (n_cp - need) // step + 1
+    starts = np.arange(per, dtype=np.uint32) * step
+    return (np.arange(n_curves, dtype=np.uint32)[:, None] * n_cp + starts[None, :]).reshape(-1)
+
+
+def hair_curves(n_curves: int, n_cp: int, rng: np.random.Generator, step: float = 0.12,
+                radius=(0.03, 0.004), lo=(-1.0, -1.0, -1.0), hi=(1.0, 1.0, 1.0)) -> np.ndarray:
+    """Control points (n_curves * n_cp, 4) of random smooth strands: roots uniform in [lo, hi], a
+    direction that wanders a little per step, radius tapering from ``radius[0]`` to ``radius[1]``."""
+    lo, hi = np.asarray(lo, np.float64), np.asarray(hi, np.float64)
+    p = lo + rng.random((n_curves, 3)) * (hi - lo)
+    d = rng.standard_normal((n_curves, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    out = np.zeros((n_curves, n_cp, 4), np.float32)
+    taper = np.linspace(radius[0], radius[1], n_cp)
+    for k in range(n_cp):
+        out[:, k, :3] = p
+        out[:, k, 3] = taper[k]
+        d = d + 0.35 * rng.standard_normal((n_curves, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        p = p + step * d
+    return out.reshape(-1, 4)

@@ -60,6 +60,13 @@ def load():
         lib.lcxo_trace_motion.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_uint32,
                                           c_int, c_void_p, c_void_p, c_int]
         lib.lcxo_pathtrace.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]
+        lib.lcxo_curve_create.restype = c_void_p
+        lib.lcxo_curve_create.argtypes = [c_void_p, c_size_t, c_size_t, c_void_p, c_size_t, c_uint32]
+        lib.lcxo_curve_destroy.argtypes = [c_void_p]
+        lib.lcxo_curve_pieces.restype = c_uint32
+        lib.lcxo_curve_pieces.argtypes = [c_void_p, c_size_t]
+        lib.lcxo_trace_curves.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, c_uint32, c_int,
+                                          c_void_p, c_void_p, c_int]
         lib.lcxo_intersect_triangle.restype = c_int
         lib.lcxo_intersect_triangle.argtypes = [c_void_p, c_void_p, c_float, c_float, c_void_p, c_void_p, c_void_p,
                                                 POINTER(c_float), POINTER(c_float), POINTER(c_float)]
@@ -204,6 +211,51 @@ class OracleScene:
             self.close()
         except Exception:
             pass
+
+
+class OracleCurve:
+    """One curve (lcxo_curve_create): control points (N, 4) float32, segment starts (uint32), basis 0..3."""
+
+    def __init__(self, control_points: np.ndarray, segments: np.ndarray, basis: int):
+        self.lib = load()
+        self.cps = np.ascontiguousarray(control_points, np.float32).reshape(-1, 4)
+        self.segs = np.ascontiguousarray(segments, np.uint32).reshape(-1)
+        self.handle = self.lib.lcxo_curve_create(_ptr(self.cps), 4, self.cps.shape[0], _ptr(self.segs),
+                                                 self.segs.size, int(basis))
+        if not self.handle:
+            raise ValueError("a curve segment runs past the control points")
+
+    def pieces(self) -> np.ndarray:
+        return np.array([self.lib.lcxo_curve_pieces(self.handle, i) for i in range(self.segs.size)], np.uint32)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.lcxo_curve_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def trace_curves(instances: list, o2w: np.ndarray, masks, rays: np.ndarray, mask: int = 0xFF, any_hit: bool = False,
+                 threads: int = 0):
+    """Brute-force closest / any hit over the curve instances (entries of ``instances`` that are None are
+    skipped: a mixed scene's mesh instances are traced with OracleScene and merged by the caller)."""
+    from luisacompute_gb300.scenes import HIT_DTYPE
+    lib = load()
+    n_inst = len(instances)
+    handles = (c_void_p * n_inst)(*[c.handle if c is not None else None for c in instances])
+    o2w = np.ascontiguousarray(o2w, np.float32).reshape(n_inst, 12)
+    masks = np.ascontiguousarray(np.broadcast_to(np.asarray(masks, np.uint32), (n_inst,)))
+    rays = np.ascontiguousarray(rays)
+    hits = np.zeros(rays.shape[0], HIT_DTYPE)
+    occ = np.zeros(rays.shape[0], np.uint8)
+    lib.lcxo_trace_curves(handles, _ptr(o2w), _ptr(masks), n_inst, _ptr(rays), rays.shape[0], mask, int(any_hit),
+                          _ptr(hits), _ptr(occ), threads)
+    return occ if any_hit else hits
 
 
 def affine_inverse(o2w: np.ndarray) -> np.ndarray:

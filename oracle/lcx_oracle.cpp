@@ -576,6 +576,216 @@ void parallel_rays(size_t n, int threads, F &&f) {
     for (auto &t : pool) t.join();
 }
 
+
+// ------------------------------------------------------------------ curves
+// Curves (the reference's Curve, include/luisa/runtime/rtx/curve.h; bases
+// include/luisa/runtime/rhi/curve_basis.h:11-24).  The reference hands curves
+// to Embree's round curves (cpu/accel.rs:142-204) and OptiX's round curves
+// (cuda_curve.cpp:37-70), neither of which is vendored, so what is restated is
+// the geometric definition the product documents (lcx_accel.h, curve section):
+// a segment is the union of balls along its curve; cubic segments are traced
+// as `pieces` round cones between the balls at u = k/pieces; linear segments
+// have end caps, cubic ones are open at ends no segment continues; hits are
+// entries only, reporting the touching ball's parameter u and bary.y = -1.
+// The basis change to Bezier form and the piece count use the same FP32
+// operation sequence as the kernels (so both pick the same pieces); the
+// intersection itself is computed here in FP64, independently of the kernels'
+// FP32 arithmetic.
+
+// Uniform cubic B-spline and Catmull-Rom (tension 1/2) to Bezier: the standard
+// basis-change matrices; linear segments keep their points in slots 0 and 3.
+void curve_to_bezier_f32(uint32_t basis, const float q[4][4], float p[4][4]) {
+    for (int c = 0; c < 4; c++) {
+        if (basis == 0) {
+            p[0][c] = p[1][c] = q[0][c];
+            p[2][c] = p[3][c] = q[1][c];
+        } else if (basis == 1) {
+            p[0][c] = (1.0f / 6.0f) * (std::fma(4.0f, q[1][c], q[0][c]) + q[2][c]);
+            p[1][c] = (1.0f / 3.0f) * std::fma(2.0f, q[1][c], q[2][c]);
+            p[2][c] = (1.0f / 3.0f) * std::fma(2.0f, q[2][c], q[1][c]);
+            p[3][c] = (1.0f / 6.0f) * (std::fma(4.0f, q[2][c], q[1][c]) + q[3][c]);
+        } else if (basis == 2) {
+            p[0][c] = q[1][c];
+            p[1][c] = std::fma(1.0f / 6.0f, q[2][c] - q[0][c], q[1][c]);
+            p[2][c] = std::fma(-1.0f / 6.0f, q[3][c] - q[1][c], q[2][c]);
+            p[3][c] = q[2][c];
+        } else {
+            p[0][c] = q[0][c];
+            p[1][c] = q[1][c];
+            p[2][c] = q[2][c];
+            p[3][c] = q[3][c];
+        }
+    }
+}
+
+float norm2_4(const float *x) { return (x[0] * x[0] + x[1] * x[1]) + (x[2] * x[2] + x[3] * x[3]); }
+
+// Chord count: eps = 0.05 max(r_max, 1e-3 |P3 - P0|), D = larger 4-D second
+// difference, pieces = ceil(sqrt(0.75 D / eps)) in [1, 32] (chord deviation
+// bound 0.75 D h^2).
+uint32_t curve_pieces_f32(uint32_t basis, const float p[4][4]) {
+    if (basis == 0) return 1u;
+    float d0[4], d1[4];
+    for (int c = 0; c < 4; c++) {
+        d0[c] = (p[0][c] - 2.0f * p[1][c]) + p[2][c];
+        d1[c] = (p[1][c] - 2.0f * p[2][c]) + p[3][c];
+    }
+    const float D = std::sqrt(std::max(norm2_4(d0), norm2_4(d1)));
+    const float rmax = std::max(std::max(p[0][3], p[1][3]), std::max(p[2][3], p[3][3]));
+    const float ch[4] = {p[3][0] - p[0][0], p[3][1] - p[0][1], p[3][2] - p[0][2], 0.0f};
+    const float len = std::sqrt(norm2_4(ch));
+    const float eps = 0.05f * std::max(rmax, 1e-3f * len);
+    if (!(D > 0.0f)) return 1u;
+    if (!(eps > 0.0f)) return 32u;
+    const float n = std::ceil(std::sqrt((0.75f * D) / eps));
+    if (!(n < 32.0f)) return 32u;
+    return n < 1.0f ? 1u : uint32_t(n);
+}
+
+struct CurveSeg {
+    double p[4][4];  // Bezier points (x, y, z, radius)
+    double lo[3], hi[3];
+    uint32_t pieces, flags;
+};
+
+double dot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// Interval of the line o + t d inside the convex hull of balls a and b
+// (radius in [3]); false if the line misses it.  `part_in`: 0 / 1 / 2 for an
+// entry on ball a, the cone between the tangent circles, ball b.
+bool round_cone_interval_f64(const double *o, const double *d, const double *a, const double *b, double &t_in,
+                             int &part_in) {
+    double ba[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+    const double L = std::sqrt(dot3(ba, ba));
+    const double ra = a[3], rb = b[3];
+    const double dd = dot3(d, d);
+    t_in = HUGE_VAL;
+    part_in = -1;
+    auto ball = [&](const double *c, double r, int which) {
+        const double oc[3] = {o[0] - c[0], o[1] - c[1], o[2] - c[2]};
+        const double hb = dot3(oc, d), cc = dot3(oc, oc) - r * r;
+        const double disc = hb * hb - dd * cc;
+        if (disc < 0.0) return;
+        const double t = (-hb - std::sqrt(disc)) / dd;
+        if (t < t_in) {
+            t_in = t;
+            part_in = which;
+        }
+    };
+    if (!(L > std::fabs(ra - rb))) {  // one ball holds the other
+        if (ra >= rb)
+            ball(a, ra, 3);
+        else
+            ball(b, rb, 3);
+        return part_in >= 0;
+    }
+    ball(a, ra, 0);
+    ball(b, rb, 2);
+    const double w[3] = {ba[0] / L, ba[1] / L, ba[2] / L};
+    const double sn = (ra - rb) / L, c2 = 1.0 - sn * sn;
+    const double q0[3] = {o[0] - a[0], o[1] - a[1], o[2] - a[2]};
+    const double s0 = dot3(q0, w), sd = dot3(d, w);
+    const double s_lo = ra * sn, s_hi = L + rb * sn;
+    double lo = -HUGE_VAL, hi = HUGE_VAL;
+    if (sd != 0.0) {
+        const double t1 = (s_lo - s0) / sd, t2 = (s_hi - s0) / sd;
+        lo = std::min(t1, t2);
+        hi = std::max(t1, t2);
+    } else if (!(s0 >= s_lo && s0 <= s_hi)) {
+        return part_in >= 0;
+    }
+    // inside the cone: c2 (|q|^2 - s^2) <= (ra - s sn)^2, i.e. A t^2 + 2 hB t + C <= 0
+    const double A = c2 * dd - sd * sd;
+    const double hB = c2 * dot3(q0, d) - s0 * sd + ra * sn * sd;
+    const double C = c2 * dot3(q0, q0) - s0 * s0 + 2.0 * ra * sn * s0 - ra * ra;
+    bool ok = true;
+    if (A != 0.0) {
+        const double disc = hB * hB - A * C;
+        if (disc >= 0.0) {
+            const double sq = std::sqrt(disc);
+            double r1 = (-hB - sq) / A, r2 = (-hB + sq) / A;
+            if (r1 > r2) std::swap(r1, r2);
+            if (A > 0.0) {
+                lo = std::max(lo, r1);
+                hi = std::min(hi, r2);
+            } else if (lo <= std::min(hi, r1)) {
+                hi = std::min(hi, r1);
+            } else {
+                lo = std::max(lo, r2);
+            }
+        } else if (A > 0.0) {
+            ok = false;
+        }
+    } else if (hB != 0.0) {
+        const double tr = -C / (2.0 * hB);
+        if (hB > 0.0)
+            hi = std::min(hi, tr);
+        else
+            lo = std::max(lo, tr);
+    } else if (C > 0.0) {
+        ok = false;
+    }
+    if (ok && lo <= hi && lo < t_in) {
+        t_in = lo;
+        part_in = 1;
+    }
+    return part_in >= 0;
+}
+
+// Closest entry (t in [tmin, tmax]) into a curve segment; u = curve parameter.
+bool curve_hit_f64(const CurveSeg &sg, const double *o, const double *d, double tmin, double tmax, double &t_out,
+                   double &u_out) {
+    bool found = false;
+    const uint32_t n = sg.pieces;
+    auto at = [&](uint32_t k, double *c) {
+        if (k == 0) {
+            for (int j = 0; j < 4; j++) c[j] = sg.p[0][j];
+        } else if (k == n) {
+            for (int j = 0; j < 4; j++) c[j] = sg.p[3][j];
+        } else {
+            const double u = double(k) / double(n), s = 1.0 - u;
+            const double b0 = s * s * s, b1 = 3.0 * u * s * s, b2 = 3.0 * u * u * s, b3 = u * u * u;
+            for (int j = 0; j < 4; j++) c[j] = b0 * sg.p[0][j] + b1 * sg.p[1][j] + b2 * sg.p[2][j] + b3 * sg.p[3][j];
+        }
+        c[3] = std::max(c[3], 0.0);
+    };
+    double c0[4], c1[4];
+    at(0, c0);
+    for (uint32_t k = 0; k < n; k++) {
+        at(k + 1, c1);
+        double t;
+        int part;
+        if ((c0[3] > 0.0 || c1[3] > 0.0) && round_cone_interval_f64(o, d, c0, c1, t, part) && t >= tmin &&
+            t <= tmax) {
+            const bool open_cap = (part == 0 && k == 0 && (sg.flags & 1u)) || (part == 2 && k + 1 == n && (sg.flags & 2u));
+            if (!open_cap) {
+                double ul;
+                if (part == 0)
+                    ul = 0.0;
+                else if (part == 2)
+                    ul = 1.0;
+                else if (part == 3)
+                    ul = c0[3] >= c1[3] ? 0.0 : 1.0;
+                else {  // cone side: the touching ball's centre lies rho tan(theta) before the point along the axis
+                    double ba[3] = {c1[0] - c0[0], c1[1] - c0[1], c1[2] - c0[2]};
+                    const double L = std::sqrt(dot3(ba, ba));
+                    const double x[3] = {o[0] + t * d[0] - c0[0], o[1] + t * d[1] - c0[1], o[2] + t * d[2] - c0[2]};
+                    const double s = dot3(x, ba) / L;
+                    const double rho = std::sqrt(std::max(dot3(x, x) - s * s, 0.0));
+                    const double sn = (c0[3] - c1[3]) / L;
+                    ul = std::min(std::max((s - rho * sn / std::sqrt(1.0 - sn * sn)) / L, 0.0), 1.0);
+                }
+                tmax = t;
+                t_out = t;
+                u_out = std::min((double(k) + ul) / double(n), 1.0);
+                found = true;
+            }
+        }
+        std::memcpy(c0, c1, sizeof(c0));
+    }
+    return found;
+}
+
 }  // namespace
 
 extern "C" {
@@ -960,6 +1170,100 @@ int lcxo_intersect_triangle(const float *o, const float *d, float tmin, float tm
     WtRay wr;
     wt_setup(wr, o, d, tmin, tmax);
     return wt_intersect(wr, v0, v1, v2, *t, *u, *v) ? 1 : 0;
+}
+
+
+void *lcxo_curve_create(const float *control_points, size_t cp_stride_floats, size_t cp_count,
+                        const uint32_t *segments, size_t seg_count, uint32_t basis) {
+    auto *segs = new std::vector<CurveSeg>(seg_count);
+    const uint32_t need = basis == 0 ? 2u : 4u;
+    for (size_t i = 0; i < seg_count; i++) {
+        CurveSeg &sg = (*segs)[i];
+        const uint32_t first = segments[i];
+        if (first > cp_count || cp_count - first < need) {  // the product reports this as an error
+            delete segs;
+            return nullptr;
+        }
+        float q[4][4], p[4][4];
+        for (uint32_t k = 0; k < 4; k++)
+            for (int c = 0; c < 4; c++) q[k][c] = control_points[(first + std::min(k, need - 1)) * cp_stride_floats + c];
+        curve_to_bezier_f32(basis, q, p);
+        sg.pieces = curve_pieces_f32(basis, p);
+        sg.flags = 0;
+        if (basis != 0) {
+            const uint32_t step = basis == 3 ? 3u : 1u;
+            if (!(i > 0 && segments[i - 1] + step == first)) sg.flags |= 1u;
+            if (!(i + 1 < seg_count && segments[i + 1] == first + step)) sg.flags |= 2u;
+        }
+        double pad = 0.0;
+        for (int k = 0; k < 4; k++) {
+            for (int c = 0; c < 4; c++) sg.p[k][c] = p[k][c];
+            pad = std::max(pad, sg.p[k][3]);
+        }
+        for (int c = 0; c < 3; c++) {
+            sg.lo[c] = std::min(std::min(sg.p[0][c], sg.p[1][c]), std::min(sg.p[2][c], sg.p[3][c])) - pad;
+            sg.hi[c] = std::max(std::max(sg.p[0][c], sg.p[1][c]), std::max(sg.p[2][c], sg.p[3][c])) + pad;
+        }
+    }
+    return segs;
+}
+
+void lcxo_curve_destroy(void *curve) { delete static_cast<std::vector<CurveSeg> *>(curve); }
+
+uint32_t lcxo_curve_pieces(const void *curve, size_t segment) {
+    return (*static_cast<const std::vector<CurveSeg> *>(curve))[segment].pieces;
+}
+
+void lcxo_trace_curves(void *const *inst_curve, const float *o2w, const uint32_t *inst_mask, size_t instance_count,
+                       const LcxoRay *rays, size_t n, uint32_t mask, int any, LcxoHit *hits, uint8_t *occluded,
+                       int threads) {
+    std::vector<float> w2o(12 * instance_count);
+    for (size_t i = 0; i < instance_count; i++) affine_inverse_f32(&o2w[12 * i], &w2o[12 * i]);
+    parallel_rays(n, threads, [&](size_t r) {
+        const LcxoRay &ray = rays[r];
+        LcxoHit best{kInvalid, kInvalid, 0.0f, 0.0f, ray.tmax, 0};
+        double best_t = ray.tmax;
+        bool occ = false;
+        for (uint32_t id = 0; id < instance_count && !occ; id++) {
+            const auto *segs = static_cast<const std::vector<CurveSeg> *>(inst_curve[id]);
+            if (!segs || (inst_mask[id] & mask) == 0u) continue;
+            float oo[3], od[3];
+            transform_ray_f32(&w2o[12 * size_t(id)], ray.o, ray.d, oo, od);
+            const double o[3] = {oo[0], oo[1], oo[2]}, d[3] = {od[0], od[1], od[2]};
+            for (uint32_t k = 0; k < segs->size() && !occ; k++) {
+                const CurveSeg &sg = (*segs)[k];
+                double tn = ray.tmin, tf = best_t;  // slab test against the segment's box
+                bool in = true;
+                for (int c = 0; c < 3 && in; c++) {
+                    if (d[c] == 0.0) {
+                        in = o[c] >= sg.lo[c] && o[c] <= sg.hi[c];
+                    } else {
+                        double t0 = (sg.lo[c] - o[c]) / d[c], t1 = (sg.hi[c] - o[c]) / d[c];
+                        if (t0 > t1) std::swap(t0, t1);
+                        tn = std::max(tn, t0);
+                        tf = std::min(tf, t1);
+                        in = tn <= tf * (1.0 + 1e-9) + 1e-12;
+                    }
+                }
+                if (!in) continue;
+                double t, u;
+                if (!curve_hit_f64(sg, o, d, ray.tmin, best_t, t, u)) continue;
+                if (any) {
+                    occ = true;
+                    break;
+                }
+                // t <= best_t; equal t goes to the smaller (inst, prim)
+                if (t < best_t || id < best.inst || (id == best.inst && k < best.prim)) {
+                    best_t = t;
+                    best = LcxoHit{id, k, float(u), -1.0f, float(t), 0};
+                }
+            }
+        }
+        if (any)
+            occluded[r] = occ ? 1 : 0;
+        else
+            hits[r] = best;
+    });
 }
 
 }  // extern "C"

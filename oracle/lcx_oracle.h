@@ -132,6 +132,19 @@ typedef struct LcxoMeshMotion {
 void lcxo_trace_motion(const void *accel, const LcxoMotion *motion, const LcxoMeshMotion *mesh_motion,
                        const LcxoRay *rays, const float *times, size_t n, uint32_t mask, int any, LcxoHit *hits,
                        uint8_t *occluded, int threads);
+/* Curves (bases 0..3 as LuisaCompute's CurveBasis): control point i at
+ * control_points + i*cp_stride_floats (x, y, z, radius); one u32 per segment
+ * (its first control point).  Returns null if a segment runs past cp_count.
+ * lcxo_trace_curves tests every segment of every instance whose
+ * inst_curve[i] is non-null (a curve from lcxo_curve_create; null instances are
+ * skipped), brute force, in FP64 (see lcx_oracle.cpp for the definition). */
+void *lcxo_curve_create(const float *control_points, size_t cp_stride_floats, size_t cp_count,
+                        const uint32_t *segments, size_t seg_count, uint32_t basis);
+void lcxo_curve_destroy(void *curve);
+uint32_t lcxo_curve_pieces(const void *curve, size_t segment);
+void lcxo_trace_curves(void *const *inst_curve, const float *o2w, const uint32_t *inst_mask, size_t instance_count,
+                       const LcxoRay *rays, size_t n, uint32_t mask, int any, LcxoHit *hits, uint8_t *occluded,
+                       int threads);
 int lcxo_intersect_triangle(const float *o, const float *d, float tmin, float tmax,
                             const float *v0, const float *v1, const float *v2, float *t,
                             float *u, float *v);

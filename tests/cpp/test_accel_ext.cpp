@@ -108,6 +108,30 @@ int main() {
         cudaMemcpy(hits2.data(), dh, sizeof(lcx::TriangleHit) * 4, cudaMemcpyDeviceToHost);
         REQUIRE(std::memcmp(hits2.data(), hits.data(), sizeof(lcx::TriangleHit) * 4) == 0);
         cudaFree(dbox);
+        // a curve: one linear strand of radius 0.1 along x at y = 0.25, z = 1, above the quad
+        const float cps[2][4] = {{0.0f, 0.25f, 1.0f, 0.1f}, {1.0f, 0.25f, 1.0f, 0.1f}};
+        const uint32_t seg0 = 0;
+        void *dcp = nullptr, *dseg = nullptr;
+        REQUIRE(cudaMalloc(&dcp, sizeof(cps)) == cudaSuccess && cudaMalloc(&dseg, sizeof(seg0)) == cudaSuccess);
+        cudaMemcpy(dcp, cps, sizeof(cps), cudaMemcpyHostToDevice);
+        cudaMemcpy(dseg, &seg0, sizeof(seg0), cudaMemcpyHostToDevice);
+        {
+            lcx::Curve strand{ext, lcx::CurveBasis::PIECEWISE_LINEAR, reinterpret_cast<uint64_t>(dcp), 2,
+                              reinterpret_cast<uint64_t>(dseg), 1};
+            lcx::Accel hair{ext};
+            hair.emplace_back(ma, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0});
+            hair.emplace_back(strand, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0});
+            stream << strand.build() << hair.build();
+            ext.trace_closest(hair.handle(), static_cast<lcx::Ray *>(dr), 4, 0xffu,
+                              static_cast<lcx::TriangleHit *>(dh), nullptr);
+            cudaMemcpy(hits.data(), dh, sizeof(lcx::TriangleHit) * 4, cudaMemcpyDeviceToHost);
+            // ray 0 meets the strand's top at z = 1.1 (t = 3.9, u = 0.25); ray 1 passes it by
+            REQUIRE(hits[0].inst == 1 && hits[0].prim == 0 && hits[0].bary[1] == -1.0f);
+            REQUIRE(std::fabs(hits[0].committed_ray_t - 3.9f) < 1e-5f && std::fabs(hits[0].bary[0] - 0.25f) < 1e-5f);
+            REQUIRE(hits[1].inst == 0 && hits[1].committed_ray_t == 5.0f);
+        }
+        cudaFree(dcp);
+        cudaFree(dseg);
         // errors surface as exceptions with the library's status code
         bool threw = false;
         try {

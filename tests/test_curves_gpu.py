@@ -1,0 +1,230 @@
+"""Curves (Curve, include/luisa/runtime/rtx/curve.h; CurveBasis, include/luisa/runtime/rhi/curve_basis.h:11-24;
+CurveBuildCommand, include/luisa/runtime/rhi/command.h:446-486).
+
+A segment is the union of balls along its curve (round curves, as the reference's Embree and OptiX
+paths use, cpu/accel.rs:150-156 and cuda_curve.cpp:45-51); cubic segments are traced as the round
+cones between the balls at u = k/pieces.  The oracle (lcxo_trace_curves) picks the same pieces with
+the kernels' FP32 sequence and intersects them in FP64, so records agree except on rays that graze
+a silhouette within FP32 rounding: the tests bound the share of such rays and the t / u errors.
+Hit records follow the reference's curve convention: prim = segment, bary = (u, -1)
+(include/luisa/runtime/rtx/hit.h:29-30, cpu/accel.rs:491-494)."""
+import numpy as np
+import pytest
+
+from luisacompute_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+INV = 0xFFFFFFFF
+BASES = (0, 1, 2, 3)
+
+
+def _aimed_rays(rng, targets, n, centre, radius=3.0, jitter=0.03):
+    """Rays from a sphere around ``centre`` toward jittered points of ``targets`` (many hits and
+    many near misses), plus a quarter of incoherent rays starting inside the scene's box."""
+    k = n - n // 4
+    tgt = targets[rng.integers(0, targets.shape[0], k)] + rng.normal(0.0, jitter, (k, 3))
+    o = rng.standard_normal((k, 3))
+    o = centre + radius * o / np.linalg.norm(o, axis=1, keepdims=True)
+    d = tgt - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros(n, S.RAY_DTYPE)
+    rays["o"][:k] = o
+    rays["d"][:k] = d
+    rays["tmax"][:k] = 1e30
+    lo, hi = targets.min(0), targets.max(0)
+    rays[k:] = S.sphere_rays(n - k, lo, hi, seed=int(rng.integers(1 << 30)))
+    return rays
+
+
+def _check(got, want, min_hits=0.15, max_mismatch=2e-3, curve_inst=None):
+    hg, hw = got["inst"] != INV, want["inst"] != INV
+    n = got.shape[0]
+    assert hw.mean() >= min_hits, hw.mean()
+    mism = hg != hw
+    assert mism.mean() <= max_mismatch, (int(mism.sum()), n)
+    both = hg & hw
+    tg, tw = got["t"][both].astype(np.float64), want["t"][both].astype(np.float64)
+    terr = np.abs(tg - tw) / (1e-4 + 1e-5 * np.abs(tw))
+    assert np.quantile(terr, 0.999) <= 1.0 and terr.max() <= 50.0, (np.quantile(terr, 0.999), terr.max())
+    same = (got["inst"][both] == want["inst"][both]) & (got["prim"][both] == want["prim"][both])
+    assert same.mean() >= 0.995, same.mean()
+    assert np.all(terr[~same] <= 50.0)  # another segment only at a near-tie
+    du = np.abs(got["bary"][both, 0][same] - want["bary"][both, 0][same])
+    assert np.quantile(du, 0.999) <= 2e-3 and du.max() <= 5e-2, (np.quantile(du, 0.999), du.max())
+    on_curve = hg if curve_inst is None else hg & np.isin(got["inst"], curve_inst)
+    assert np.all(got["bary"][on_curve, 1] == -1.0)
+    miss = ~hg
+    assert np.all(got["prim"][miss] == INV) and np.all(got["bary"][miss] == 0.0)
+
+
+def _curve_scene(rng, basis, n_curves=96, n_cp=10):
+    import torch
+    from luisacompute_gb300.accel import Accel, Curve
+    cps = S.hair_curves(n_curves, n_cp, rng)
+    segs = S.curve_segments(n_curves, n_cp, basis)
+    cv = Curve(basis, torch.from_numpy(cps).cuda(), torch.from_numpy(segs.astype(np.int32)).cuda()).build()
+    aff = np.stack([np.eye(3, 4, dtype=np.float32).reshape(12),
+                    S.affine_rows(S.random_rotations(1, rng), np.array([0.7]), np.array([[2.5, 0.0, 0.0]]))[0],
+                    S.affine_rows(S.random_rotations(1, rng), np.array([1.3]), np.array([[0.0, -2.5, 0.5]]))[0]])
+    masks = np.array([0xFF, 0x0F, 0xF0], np.uint32)
+    acc = Accel()
+    for i in range(3):
+        acc.emplace_back(cv, aff[i].reshape(3, 4), visibility_mask=int(masks[i]))
+    acc.build()
+    torch.cuda.synchronize()
+    world = np.concatenate([cps[:, :3] @ aff[i].reshape(3, 4)[:, :3].T + aff[i].reshape(3, 4)[:, 3]
+                            for i in range(3)])
+    return cps, segs, cv, acc, aff, masks, world
+
+
+@pytest.mark.parametrize("basis", BASES)
+def test_curve_bases_match_oracle(lcx, oracle_mod, basis):
+    from luisacompute_gb300.accel import hits_to_numpy, rays_to_device
+    rng = np.random.default_rng(700 + basis)
+    cps, segs, cv, acc, aff, masks, world = _curve_scene(rng, basis)
+    oc = oracle_mod.OracleCurve(cps, segs, basis)
+    if basis != 0:
+        assert oc.pieces().max() > 1  # bent strands are traced as several cones
+    rays = _aimed_rays(rng, world, 120_000, world.mean(0))
+    d_rays = rays_to_device(rays)
+    for mask in (0xFF, 0x0F):
+        want = oracle_mod.trace_curves([oc] * 3, aff, masks, rays, mask=mask)
+        want_any = oracle_mod.trace_curves([oc] * 3, aff, masks, rays, mask=mask, any_hit=True)
+        for layout in (0, 1):
+            got = hits_to_numpy(acc.trace_closest(d_rays, mask=mask, layout=layout))
+            _check(got, want, min_hits=0.1)
+            occ = acc.trace_any(d_rays, mask=mask, layout=layout).cpu().numpy()
+            assert (occ != want_any).mean() <= 2e-3
+            assert np.array_equal(occ.astype(bool), got["inst"] != INV) or (
+                (occ.astype(bool) != (got["inst"] != INV)).mean() <= 1e-3)
+    if mask == 0x0F:
+        assert not np.any(got["inst"] == 2)  # instance 2's mask 0xF0 never meets ray mask 0x0F
+
+
+def test_curve_open_ends_and_caps(lcx, oracle_mod):
+    """One straight strand along x (radius 0.1) per basis: rays straight down at x = 0.5 hit the side
+    (t = 0.9, u = 0.5); at x = 1.05 and x = -0.05 only the end balls lie below them, which linear
+    segments have (spherical caps) and open cubic ones do not; a ray starting inside misses."""
+    import torch
+    from luisacompute_gb300.accel import Accel, Curve, hits_to_numpy, rays_to_device
+    rays = np.zeros(4, S.RAY_DTYPE)
+    rays["o"] = [[0.5, 1, 0], [1.05, 1, 0], [-0.05, 1, 0], [0.5, 0, 0]]
+    rays["d"] = [0, -1, 0]
+    rays["tmax"] = 1e30
+    pts = {0: [[0, 0, 0, 0.1], [1, 0, 0, 0.1]],
+           3: [[0, 0, 0, 0.1], [1 / 3, 0, 0, 0.1], [2 / 3, 0, 0, 0.1], [1, 0, 0, 0.1]],
+           1: [[-1, 0, 0, 0.1], [0, 0, 0, 0.1], [1, 0, 0, 0.1], [2, 0, 0, 0.1]],  # B-spline: x runs 0..1
+           2: [[-1, 0, 0, 0.1], [0, 0, 0, 0.1], [1, 0, 0, 0.1], [2, 0, 0, 0.1]]}
+    for basis, p in pts.items():
+        cps = np.array(p, np.float32)
+        cv = Curve(basis, torch.from_numpy(cps).cuda(), torch.zeros(1, dtype=torch.int32).cuda()).build()
+        acc = Accel()
+        acc.emplace_back(cv)
+        acc.build()
+        got = hits_to_numpy(acc.trace_closest(rays_to_device(rays)))
+        want = oracle_mod.trace_curves([oracle_mod.OracleCurve(cps, np.zeros(1), basis)],
+                                       np.eye(3, 4, dtype=np.float32).reshape(1, 12), 0xFF, rays)
+        assert np.array_equal(got["inst"], want["inst"]), basis
+        assert got["inst"][0] == 0 and abs(got["t"][0] - 0.9) < 1e-5 and abs(got["bary"][0, 0] - 0.5) < 1e-4
+        assert got["bary"][0, 1] == -1.0
+        capped = basis == 0
+        assert (got["inst"][1] == 0) == capped and (got["inst"][2] == 0) == capped, basis
+        if capped:
+            assert abs(got["t"][1] - (1 - np.sqrt(0.01 - 0.0025))) < 1e-5 and got["bary"][1, 0] == 1.0
+            assert got["bary"][2, 0] == 0.0
+        assert got["inst"][3] == INV  # starts inside the strand
+
+
+def test_curves_with_meshes_and_errors(lcx, oracle_mod):
+    import torch
+    from luisacompute_gb300 import LcxError
+    from luisacompute_gb300._capi import LcxAccelView
+    from luisacompute_gb300.accel import Accel, Curve, hits_to_numpy, mesh_from_data, rays_to_device
+    import ctypes
+    rng = np.random.default_rng(711)
+    basis = 2
+    cps = S.hair_curves(64, 8, rng, lo=(-1.2, -1.2, -1.2), hi=(1.2, 1.2, 1.2))
+    segs = S.curve_segments(64, 8, basis)
+    d_cps = torch.from_numpy(cps).cuda()
+    cv = Curve(basis, d_cps, torch.from_numpy(segs.astype(np.int32)).cuda()).build()
+    sphere = S.icosphere(4, radius=0.8)
+    mesh = mesh_from_data(sphere).build()
+    acc = Accel()
+    acc.emplace_back(mesh)
+    acc.emplace_back(cv)
+    ident = np.eye(3, 4, dtype=np.float32).reshape(12)
+    shifted = ident.copy()
+    shifted[3] = 0.4
+    acc.emplace_back(cv, shifted.reshape(3, 4))
+    acc.build()
+    rays = _aimed_rays(rng, np.concatenate([cps[:, :3], sphere.vertices[:, :3]]), 80_000, np.zeros(3))
+    d_rays = rays_to_device(rays)
+    got = hits_to_numpy(acc.trace_closest(d_rays))
+    # oracle: the mesh instance alone (curve slots masked off), the curve instances alone, then the
+    # closest of the two with ties to the smaller instance id
+    osc = oracle_mod.OracleScene(S.Scene([sphere], np.zeros(3, np.int64), np.stack([ident, ident, shifted]),
+                                         np.array([0xFF, 0, 0], np.uint32)))
+    wm = osc.trace_closest(rays)
+    oc = oracle_mod.OracleCurve(cps, segs, basis)
+    wc = oracle_mod.trace_curves([None, oc, oc], np.stack([ident, ident, shifted]), 0xFF, rays)
+    take_c = (wc["t"] < wm["t"]) | ((wc["t"] == wm["t"]) & (wc["inst"] < wm["inst"]))
+    want = np.where(take_c, wc, wm)
+    _check(got, want, min_hits=0.3, curve_inst=[1, 2])
+    assert (got["inst"] == 0).sum() > 1000 and (got["inst"] >= 1).sum() > 1000
+    tri = got["inst"] == 0
+    assert np.all(got["bary"][tri, 1] >= 0.0)  # triangle hits keep their barycentrics
+    # the plain trace entry points take curve accels; the multi-job path and ray_query do not
+    with pytest.raises(LcxError):
+        view = LcxAccelView()
+        from luisacompute_gb300._capi import check
+        check(acc.lib.lcx_accel_device_view(acc.handle, ctypes.byref(view)), "lcx_accel_device_view")
+    # a rebuild with moved control points: the accel must be rebuilt, then it sees them
+    d_cps[:, 0] += 0.25
+    cv.build()
+    with pytest.raises(LcxError):
+        acc.trace_closest(d_rays)
+    acc.build()
+    got2 = hits_to_numpy(acc.trace_closest(d_rays))
+    cps2 = d_cps.cpu().numpy()
+    wc2 = oracle_mod.trace_curves([None, oracle_mod.OracleCurve(cps2, segs, basis)] * 1 +
+                                  [oracle_mod.OracleCurve(cps2, segs, basis)], np.stack([ident, ident, shifted]),
+                                  0xFF, rays)
+    take_c = (wc2["t"] < wm["t"]) | ((wc2["t"] == wm["t"]) & (wc2["inst"] < wm["inst"]))
+    _check(got2, np.where(take_c, wc2, wm), min_hits=0.3, curve_inst=[1, 2])
+    # a segment whose control points run past the buffer is an error, and the old tree stays usable
+    bad = torch.from_numpy(np.array([0, cps.shape[0] - 2], np.int32)).cuda()
+    cv_bad = Curve(basis, d_cps, bad)
+    with pytest.raises(LcxError):
+        cv_bad.build()
+    bad_lin = Curve(0, d_cps, torch.from_numpy(np.array([cps.shape[0] - 1], np.int32)).cuda())
+    with pytest.raises(LcxError):
+        bad_lin.build()
+    assert np.array_equal(hits_to_numpy(acc.trace_closest(d_rays)).view(np.uint8), got2.view(np.uint8))
+
+
+def test_curve_motion_instance(lcx, oracle_mod):
+    """A motion instance of a curve: at time tau the matrix is the per-element interpolation of its
+    keyframes, so the oracle traces the curve with that matrix."""
+    import torch
+    from luisacompute_gb300.accel import Accel, Curve, MotionInstance, hits_to_numpy, rays_to_device
+    rng = np.random.default_rng(731)
+    basis = 1
+    cps = S.hair_curves(48, 9, rng)
+    segs = S.curve_segments(48, 9, basis)
+    cv = Curve(basis, torch.from_numpy(cps).cuda(), torch.from_numpy(segs.astype(np.int32)).cuda()).build()
+    k0 = np.eye(3, 4, dtype=np.float32)
+    k1 = k0.copy()
+    k1[:, 3] = [0.6, -0.2, 0.1]
+    mo = MotionInstance(cv, np.stack([k0, k1]), 0.0, 1.0)
+    acc = Accel()
+    acc.emplace_back(mo)
+    acc.build()
+    tau = 0.25
+    m = (k0 + np.float32(tau) * (k1 - k0)).reshape(12)
+    world = cps[:, :3] + m.reshape(3, 4)[:, 3]
+    rays = _aimed_rays(rng, world, 60_000, world.mean(0))
+    times = torch.full((rays.shape[0],), tau, dtype=torch.float32, device="cuda")
+    got = hits_to_numpy(acc.trace_closest_motion(rays_to_device(rays), times))
+    want = oracle_mod.trace_curves([oracle_mod.OracleCurve(cps, segs, basis)], m.reshape(1, 12), 0xFF, rays)
+    _check(got, want, min_hits=0.1)
