@@ -496,12 +496,14 @@ constexpr uint32_t kCurveMaxPieces = 32;
 __device__ __forceinline__ float4 f4_axpy(float a, float4 x, float4 y) {  // a x + y
     return make_float4(__fmaf_rn(a, x.x, y.x), __fmaf_rn(a, x.y, y.y), __fmaf_rn(a, x.z, y.z), __fmaf_rn(a, x.w, y.w));
 }
-__device__ __forceinline__ float4 f4_scale(float a, float4 x) { return make_float4(a * x.x, a * x.y, a * x.z, a * x.w); }
+__device__ __forceinline__ float4 f4_scale(float a, float4 x) {
+    return make_float4(__fmul_rn(a, x.x), __fmul_rn(a, x.y), __fmul_rn(a, x.z), __fmul_rn(a, x.w));
+}
 __device__ __forceinline__ float4 f4_add(float4 x, float4 y) {
-    return make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+    return make_float4(__fadd_rn(x.x, y.x), __fadd_rn(x.y, y.y), __fadd_rn(x.z, y.z), __fadd_rn(x.w, y.w));
 }
 __device__ __forceinline__ float4 f4_sub(float4 x, float4 y) {
-    return make_float4(x.x - y.x, x.y - y.y, x.z - y.z, x.w - y.w);
+    return make_float4(__fsub_rn(x.x, y.x), __fsub_rn(x.y, y.y), __fsub_rn(x.z, y.z), __fsub_rn(x.w, y.w));
 }
 
 // Control points q (2 for linear, else 4) of one segment to Bezier form p[4]
@@ -558,10 +560,20 @@ __device__ __forceinline__ uint32_t curve_pieces(uint32_t basis, const float4 p[
 }
 
 // Point and radius of a Bezier segment at u (Bernstein form; exact at 0 and 1).
+// The curve arithmetic below rounds every operation explicitly (no contraction),
+// so every kernel that inlines it -- the trace kernels and lcx::ray_query in a
+// user's kernel -- computes the same bits.
 __device__ __forceinline__ float4 bezier_at(const float4 p[4], float u) {
-    const float s = 1.0f - u;
-    const float b0 = s * s * s, b1 = 3.0f * u * s * s, b2 = 3.0f * u * u * s, b3 = u * u * u;
-    return f4_axpy(b3, p[3], f4_axpy(b2, p[2], f4_axpy(b1, p[1], f4_scale(b0, p[0]))));
+    const float s = __fsub_rn(1.0f, u);
+    const float b0 = __fmul_rn(__fmul_rn(s, s), s), b1 = __fmul_rn(__fmul_rn(__fmul_rn(3.0f, u), s), s);
+    const float b2 = __fmul_rn(__fmul_rn(__fmul_rn(3.0f, u), u), s), b3 = __fmul_rn(__fmul_rn(u, u), u);
+    const float4 q = make_float4(__fmul_rn(b0, p[0].x), __fmul_rn(b0, p[0].y), __fmul_rn(b0, p[0].z),
+                                 __fmul_rn(b0, p[0].w));
+    return f4_axpy(b3, p[3], f4_axpy(b2, p[2], f4_axpy(b1, p[1], q)));
+}
+
+__device__ __forceinline__ float dot3_rn(float ax, float ay, float az, float bx, float by, float bz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
 }
 
 // Entry of the ray o + t d into the round cone of balls (a.xyz, a.w) and
@@ -577,29 +589,30 @@ __device__ __forceinline__ float4 bezier_at(const float4 p[4], float u) {
 __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, float4 b, float tmin, float tmax,
                                                  float &t_out, float &u_out, int &part) {
     const float kInf = __int_as_float(0x7f800000);
-    const float dd = d.x * d.x + d.y * d.y + d.z * d.z;
-    const float3 m = make_float3(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z));
-    const float tc = ((m.x - o.x) * d.x + (m.y - o.y) * d.y + (m.z - o.z) * d.z) / dd;
+    const float dd = dot3_rn(d.x, d.y, d.z, d.x, d.y, d.z);
+    const float mx = __fmul_rn(0.5f, __fadd_rn(a.x, b.x)), my = __fmul_rn(0.5f, __fadd_rn(a.y, b.y)),
+                mz = __fmul_rn(0.5f, __fadd_rn(a.z, b.z));
+    const float tc = __fdiv_rn(dot3_rn(__fsub_rn(mx, o.x), __fsub_rn(my, o.y), __fsub_rn(mz, o.z), d.x, d.y, d.z), dd);
     const float3 os = make_float3(__fmaf_rn(tc, d.x, o.x), __fmaf_rn(tc, d.y, o.y), __fmaf_rn(tc, d.z, o.z));
-    const float3 ba = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
-    const float L2 = ba.x * ba.x + ba.y * ba.y + ba.z * ba.z;
-    const float L = sqrtf(L2);
-    const float dr = a.w - b.w;
+    const float3 ba = make_float3(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y), __fsub_rn(b.z, a.z));
+    const float L = __fsqrt_rn(dot3_rn(ba.x, ba.y, ba.z, ba.x, ba.y, ba.z));
+    const float dr = __fsub_rn(a.w, b.w);
     float best = kInf;
     int bp = -1;
     // balls: smaller root of |os + t d - c|^2 = r^2
     auto ball = [&](float4 c, int which) {
-        const float3 oc = make_float3(os.x - c.x, os.y - c.y, os.z - c.z);
-        const float hb = oc.x * d.x + oc.y * d.y + oc.z * d.z;
-        const float cc = (oc.x * oc.x + oc.y * oc.y + oc.z * oc.z) - c.w * c.w;
-        const float disc = hb * hb - dd * cc;
+        const float ocx = __fsub_rn(os.x, c.x), ocy = __fsub_rn(os.y, c.y), ocz = __fsub_rn(os.z, c.z);
+        const float hb = dot3_rn(ocx, ocy, ocz, d.x, d.y, d.z);
+        const float cc = __fsub_rn(dot3_rn(ocx, ocy, ocz, ocx, ocy, ocz), __fmul_rn(c.w, c.w));
+        const float disc = __fsub_rn(__fmul_rn(hb, hb), __fmul_rn(dd, cc));
         if (disc < 0.0f) return;
-        const float t = (-hb - sqrtf(disc)) / dd;
+        const float t = __fdiv_rn(__fsub_rn(-hb, __fsqrt_rn(disc)), dd);
         if (t < best) {
             best = t;
             bp = which;
         }
     };
+    float sn = 0.0f, cs = 1.0f;
     if (!(L > fabsf(dr))) {  // one ball holds the other: the larger ball alone
         ball(a.w >= b.w ? a : b, 3);
     } else {
@@ -607,35 +620,38 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
         ball(b, 2);
         // the truncated cone: s = axial coordinate from a, rho = distance from the axis;
         // its side is rho cos + s sin = ra for s in [ra sin, L + rb sin]
-        const float inv = 1.0f / L;
-        const float3 w = make_float3(ba.x * inv, ba.y * inv, ba.z * inv);
-        const float sn = dr * inv;
-        const float c2 = fmaxf((1.0f - sn) * (1.0f + sn), 0.0f);
-        const float3 q0 = make_float3(os.x - a.x, os.y - a.y, os.z - a.z);
-        const float s0 = q0.x * w.x + q0.y * w.y + q0.z * w.z;
-        const float sd = d.x * w.x + d.y * w.y + d.z * w.z;
-        const float qd = q0.x * d.x + q0.y * d.y + q0.z * d.z;
-        const float qq = q0.x * q0.x + q0.y * q0.y + q0.z * q0.z;
-        const float s_lo = a.w * sn, s_hi = L + b.w * sn;
+        const float wx = __fdiv_rn(ba.x, L), wy = __fdiv_rn(ba.y, L), wz = __fdiv_rn(ba.z, L);
+        sn = __fdiv_rn(dr, L);
+        const float c2 = fmaxf(__fmul_rn(__fsub_rn(1.0f, sn), __fadd_rn(1.0f, sn)), 0.0f);
+        cs = __fsqrt_rn(c2);
+        const float q0x = __fsub_rn(os.x, a.x), q0y = __fsub_rn(os.y, a.y), q0z = __fsub_rn(os.z, a.z);
+        const float s0 = dot3_rn(q0x, q0y, q0z, wx, wy, wz);
+        const float sd = dot3_rn(d.x, d.y, d.z, wx, wy, wz);
+        const float qd = dot3_rn(q0x, q0y, q0z, d.x, d.y, d.z);
+        const float qq = dot3_rn(q0x, q0y, q0z, q0x, q0y, q0z);
+        const float ras = __fmul_rn(a.w, sn);
+        const float s_lo = ras, s_hi = __fadd_rn(L, __fmul_rn(b.w, sn));
         float lo = -kInf, hi = kInf;
         if (sd != 0.0f) {
-            const float t1 = (s_lo - s0) / sd, t2 = (s_hi - s0) / sd;
+            const float t1 = __fdiv_rn(__fsub_rn(s_lo, s0), sd), t2 = __fdiv_rn(__fsub_rn(s_hi, s0), sd);
             lo = fminf(t1, t2);
             hi = fmaxf(t1, t2);
         } else if (!(s0 >= s_lo && s0 <= s_hi)) {
             lo = kInf;
         }
         // f(t) = c2 |q|^2 - s^2 + 2 ra sn s - ra^2 <= 0 inside the (one-sheeted, within the slab) cone
-        const float A = c2 * dd - sd * sd;
-        const float hB = c2 * qd - s0 * sd + a.w * sn * sd;
-        const float C = c2 * qq - s0 * s0 + 2.0f * a.w * sn * s0 - a.w * a.w;
+        const float A = __fsub_rn(__fmul_rn(c2, dd), __fmul_rn(sd, sd));
+        const float hB = __fadd_rn(__fsub_rn(__fmul_rn(c2, qd), __fmul_rn(s0, sd)), __fmul_rn(ras, sd));
+        const float C = __fsub_rn(__fadd_rn(__fsub_rn(__fmul_rn(c2, qq), __fmul_rn(s0, s0)),
+                                            __fmul_rn(__fmul_rn(2.0f, ras), s0)),
+                                  __fmul_rn(a.w, a.w));
         if (lo <= hi) {
             if (A != 0.0f) {
-                const float disc = hB * hB - A * C;
+                const float disc = __fsub_rn(__fmul_rn(hB, hB), __fmul_rn(A, C));
                 if (disc >= 0.0f) {
-                    const float sq = sqrtf(disc);
-                    const float qv = -(hB + copysignf(sq, hB));
-                    float r1 = qv / A, r2 = (qv != 0.0f) ? C / qv : r1;
+                    const float sq = __fsqrt_rn(disc);
+                    const float qv = -__fadd_rn(hB, copysignf(sq, hB));
+                    float r1 = __fdiv_rn(qv, A), r2 = (qv != 0.0f) ? __fdiv_rn(C, qv) : r1;
                     if (r1 > r2) {
                         const float tt = r1;
                         r1 = r2;
@@ -653,7 +669,7 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
                     lo = kInf;
                 }
             } else if (hB != 0.0f) {
-                const float tr = -C / (2.0f * hB);
+                const float tr = __fdiv_rn(-C, __fmul_rn(2.0f, hB));
                 if (hB > 0.0f)
                     hi = fminf(hi, tr);
                 else
@@ -668,7 +684,7 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
         }
     }
     if (bp < 0) return false;
-    const float t = tc + best;
+    const float t = __fadd_rn(tc, best);
     if (!(t >= tmin && t <= tmax)) return false;
     // the ball touching the hit point: on the cone side its centre sits rho tan below the point's s
     float u;
@@ -679,12 +695,11 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
     else if (bp == 3)
         u = a.w >= b.w ? 0.0f : 1.0f;
     else {
-        const float3 x = make_float3(os.x + best * d.x - a.x, os.y + best * d.y - a.y, os.z + best * d.z - a.z);
-        const float s = (x.x * ba.x + x.y * ba.y + x.z * ba.z) / L;
-        const float rho = sqrtf(fmaxf(x.x * x.x + x.y * x.y + x.z * x.z - s * s, 0.0f));
-        const float sn = dr / L;
-        const float cs = sqrtf(fmaxf((1.0f - sn) * (1.0f + sn), 0.0f));
-        u = fminf(fmaxf((s - rho * sn / cs) / L, 0.0f), 1.0f);
+        const float xx = __fsub_rn(__fmaf_rn(best, d.x, os.x), a.x), xy = __fsub_rn(__fmaf_rn(best, d.y, os.y), a.y),
+                    xz = __fsub_rn(__fmaf_rn(best, d.z, os.z), a.z);
+        const float s = __fdiv_rn(dot3_rn(xx, xy, xz, ba.x, ba.y, ba.z), L);
+        const float rho = __fsqrt_rn(fmaxf(__fsub_rn(dot3_rn(xx, xy, xz, xx, xy, xz), __fmul_rn(s, s)), 0.0f));
+        u = fminf(fmaxf(__fdiv_rn(__fsub_rn(s, __fdiv_rn(__fmul_rn(rho, sn), cs)), L), 0.0f), 1.0f);
     }
     t_out = t;
     u_out = u;
@@ -694,34 +709,40 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
 
 // Closest entry into curve segment `cp` (4 Bezier points) with t in [tmin, tmax].
 __device__ __forceinline__ bool curve_intersect(const float4 *cp, uint32_t pieces, uint32_t flags, float3 o, float3 d,
-                                             float tmin, float tmax, float &t_out, float &u_out) {
+                                                float tmin, float tmax, float &t_out, float &u_out) {
     float4 p[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) p[k] = bvh_ld(cp + k);
     pieces = min(max(pieces, 1u), kCurveMaxPieces);
-    const float dd = d.x * d.x + d.y * d.y + d.z * d.z;
+    const float dd = dot3_rn(d.x, d.y, d.z, d.x, d.y, d.z);
     if (!(dd > 0.0f)) return false;
     bool found = false;
     float4 c0 = p[0];
     c0.w = fmaxf(c0.w, 0.0f);
     for (uint32_t k = 0; k < pieces; k++) {
-        float4 c1 = (k + 1 == pieces) ? p[3] : bezier_at(p, float(k + 1) / float(pieces));
+        float4 c1 = (k + 1 == pieces) ? p[3] : bezier_at(p, __fdiv_rn(float(k + 1), float(pieces)));
         c1.w = fmaxf(c1.w, 0.0f);
         // cull by the piece's bounding sphere: distance from its middle to the ray's line
-        const float3 mc = make_float3(0.5f * (c0.x + c1.x) - o.x, 0.5f * (c0.y + c1.y) - o.y, 0.5f * (c0.z + c1.z) - o.z);
-        const float3 h = make_float3(0.5f * (c1.x - c0.x), 0.5f * (c1.y - c0.y), 0.5f * (c1.z - c0.z));
-        const float R = sqrtf(h.x * h.x + h.y * h.y + h.z * h.z) + fmaxf(c0.w, c1.w);
-        const float3 cr = make_float3(mc.y * d.z - mc.z * d.y, mc.z * d.x - mc.x * d.z, mc.x * d.y - mc.y * d.x);
-        const float dist2 = (cr.x * cr.x + cr.y * cr.y + cr.z * cr.z) / dd;
-        if (R > 0.0f && dist2 <= 1.0001f * R * R) {
+        const float mx = __fsub_rn(__fmul_rn(0.5f, __fadd_rn(c0.x, c1.x)), o.x);
+        const float my = __fsub_rn(__fmul_rn(0.5f, __fadd_rn(c0.y, c1.y)), o.y);
+        const float mz = __fsub_rn(__fmul_rn(0.5f, __fadd_rn(c0.z, c1.z)), o.z);
+        const float hx = __fmul_rn(0.5f, __fsub_rn(c1.x, c0.x)), hy = __fmul_rn(0.5f, __fsub_rn(c1.y, c0.y)),
+                    hz = __fmul_rn(0.5f, __fsub_rn(c1.z, c0.z));
+        const float R = __fadd_rn(__fsqrt_rn(dot3_rn(hx, hy, hz, hx, hy, hz)), fmaxf(c0.w, c1.w));
+        const float crx = __fsub_rn(__fmul_rn(my, d.z), __fmul_rn(mz, d.y));
+        const float cry = __fsub_rn(__fmul_rn(mz, d.x), __fmul_rn(mx, d.z));
+        const float crz = __fsub_rn(__fmul_rn(mx, d.y), __fmul_rn(my, d.x));
+        const float dist2 = __fdiv_rn(dot3_rn(crx, cry, crz, crx, cry, crz), dd);
+        if (R > 0.0f && dist2 <= __fmul_rn(__fmul_rn(1.0001f, R), R)) {
             float t, u;
             int part;
             if (round_cone_entry(o, d, c0, c1, tmin, tmax, t, u, part)) {
-                const bool open_cap = (part == 0 && k == 0 && (flags & 1u)) || (part == 2 && k + 1 == pieces && (flags & 2u));
+                const bool open_cap =
+                    (part == 0 && k == 0 && (flags & 1u)) || (part == 2 && k + 1 == pieces && (flags & 2u));
                 if (!open_cap) {
                     tmax = t;
                     t_out = t;
-                    u_out = fminf((float(k) + u) / float(pieces), 1.0f);
+                    u_out = fminf(__fdiv_rn(__fadd_rn(float(k), u), float(pieces)), 1.0f);
                     found = true;
                 }
             }

@@ -159,10 +159,11 @@ __device__ __forceinline__ void intersect_f(const Node8F *nodes, uint32_t idx, f
         const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
         const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
         const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};
+#if !LCX_META_BYTEPAR
         const uint32_t mw = half ? hdr.w : hdr.z;
+#endif
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            const int s = half * 4 + k;
             const float tnx = (nx ? HX[k] : LX[k]) - ox, tfx = (nx ? LX[k] : HX[k]) - ox;
             const float tny = (ny ? HY[k] : LY[k]) - oy, tfy = (ny ? LY[k] : HY[k]) - oy;
             const float tnz = (nz ? HZ[k] : LZ[k]) - oz, tfz = (nz ? LZ[k] : HZ[k]) - oz;
@@ -173,7 +174,7 @@ __device__ __forceinline__ void intersect_f(const Node8F *nodes, uint32_t idx, f
             if (slab_accept(tn, tf)) bits |= cb << idx;
 #else
             const uint32_t meta = (mw >> (8 * k)) & 0xffu;
-            if (meta_internal(meta)) imask |= 1u << s;
+            if (meta_internal(meta)) imask |= 1u << (half * 4 + k);
             if (slab_accept(tn, tf)) bits |= slot_bits(meta, octinv);
 #endif
         }

@@ -20,8 +20,8 @@
 // valid until the accel is built again or destroyed.  The walk is one ray per
 // thread with a 32-entry local stack, over the 8-bit quantised nodes, with the
 // node test, instance transform and watertight triangle test of the trace
-// kernels: committing every candidate gives lcx_trace_closest's records bit
-// for bit.  Candidates arrive in traversal order, but the committed result is
+// kernels (and their curve test for curve instances): committing every
+// candidate gives lcx_trace_closest's records bit for bit.  Candidates arrive in traversal order, but the committed result is
 // the minimum over committed candidates of (t, inst, prim), so it does not
 // depend on that order when the decision depends only on the candidate.
 #pragma once
@@ -31,9 +31,11 @@
 
 namespace lcx {
 
+// A surface candidate: a triangle, or a curve segment (bary_v = -1, bary_u =
+// the curve parameter; the reference's curve convention, hit.h:29-30).
 struct TriangleCandidate {
     uint32_t inst;  // TLAS slot of the instance
-    uint32_t prim;  // triangle index in its mesh
+    uint32_t prim;  // triangle (segment) index in its mesh (curve)
     float bary_u, bary_v;
     float t;        // distance along the ray (world ray parameter)
 };
@@ -159,7 +161,16 @@ __device__ CommittedHit ray_query(const LcxAccelView &view, const LcxRay &ray, u
                 const float4 *tp = reinterpret_cast<const float4 *>(tris + Gt.x + k);
                 const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
                 float t, u, v;
-                if (!wt_intersect(wt, tmin, best_t, a, b, c, t, u, v)) continue;
+                if (__float_as_uint(b.w) == kTriCurve) {  // a curve segment: the curve test of the trace kernels
+                    const float4 *cp = reinterpret_cast<const float4 *>(
+                        (unsigned long long)__float_as_uint(c.x) | ((unsigned long long)__float_as_uint(c.y) << 32));
+                    if (!curve_intersect(cp, __float_as_uint(c.z), __float_as_uint(c.w), make_float3(ox, oy, oz),
+                                         make_float3(odx, ody, odz), tmin, best_t, t, u))
+                        continue;
+                    v = -1.0f;
+                } else if (!wt_intersect(wt, tmin, best_t, a, b, c, t, u, v)) {
+                    continue;
+                }
                 const uint32_t prim = __float_as_uint(a.w);
                 const int act = on_candidate(TriangleCandidate{cur_inst, prim, u, v, t});
                 if (act == kCommit || act == kCommitAndTerminate) {
@@ -181,7 +192,8 @@ __device__ CommittedHit ray_query(const LcxAccelView &view, const LcxRay &ray, u
                 const uint4 *ip = reinterpret_cast<const uint4 *>(insts + Gt.x + k);
                 const uint4 m4 = __ldg(ip + 4);  // fnodes (x,y), inst id (z), mask (w)
                 const bool proc = (m4.w & kInstProcedural) != 0u;
-                if ((((proc ? m4.w >> 8 : m4.w) & 0xffu) & mask) == 0u) continue;
+                const bool shifted = (m4.w & (kInstProcedural | kInstCurve)) != 0u;  // mask in bits 8..15
+                if ((((shifted ? m4.w >> 8 : m4.w) & 0xffu) & mask) == 0u) continue;
                 const float4 r0 = __ldg(reinterpret_cast<const float4 *>(ip));
                 const float4 r1 = __ldg(reinterpret_cast<const float4 *>(ip + 1));
                 const float4 r2 = __ldg(reinterpret_cast<const float4 *>(ip + 2));

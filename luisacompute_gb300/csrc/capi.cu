@@ -1600,7 +1600,6 @@ int lcx_accel_device_view(uint64_t accel, LcxAccelView *out) {
         return fail(LCX_ERR_NOT_BUILT, "a mesh of the accel was destroyed, rebuilt or refit; rebuild the accel");
     if (a->has_motion)
         return fail(LCX_ERR_INVALID_ARG, "lcx::ray_query does not trace motion instances");
-    if (a->has_curves) return fail(LCX_ERR_INVALID_ARG, "lcx::ray_query does not trace curves");
     const uint32_t need = a->depth + a->max_blas_depth + 3;
     if (int(need) > kStackSize)
         return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the query stack (%d)", a->depth,

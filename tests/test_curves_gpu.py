@@ -139,7 +139,6 @@ def test_curve_open_ends_and_caps(lcx, oracle_mod):
 def test_curves_with_meshes_and_errors(lcx, oracle_mod):
     import torch
     from luisacompute_gb300 import LcxError
-    from luisacompute_gb300._capi import LcxAccelView
     from luisacompute_gb300.accel import Accel, Curve, hits_to_numpy, mesh_from_data, rays_to_device
     import ctypes
     rng = np.random.default_rng(711)
@@ -174,11 +173,12 @@ def test_curves_with_meshes_and_errors(lcx, oracle_mod):
     assert (got["inst"] == 0).sum() > 1000 and (got["inst"] >= 1).sum() > 1000
     tri = got["inst"] == 0
     assert np.all(got["bary"][tri, 1] >= 0.0)  # triangle hits keep their barycentrics
-    # the plain trace entry points take curve accels; the multi-job path and ray_query do not
+    # the multi-job path does not take curve accels
+    from luisacompute_gb300._capi import LcxTraceJob, check
+    job_out = torch.empty((rays.shape[0], 6), dtype=torch.int32, device="cuda")
+    job = LcxTraceJob(acc.handle, d_rays.data_ptr(), job_out.data_ptr(), rays.shape[0], 0xFF, 0, 0)
     with pytest.raises(LcxError):
-        view = LcxAccelView()
-        from luisacompute_gb300._capi import check
-        check(acc.lib.lcx_accel_device_view(acc.handle, ctypes.byref(view)), "lcx_accel_device_view")
+        check(acc.lib.lcx_trace_jobs(ctypes.byref(job), 1, 1, None), "lcx_trace_jobs")
     # a rebuild with moved control points: the accel must be rebuilt, then it sees them
     d_cps[:, 0] += 0.25
     cv.build()

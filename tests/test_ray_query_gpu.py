@@ -189,3 +189,31 @@ def test_procedural_primitives(lcx, oracle_mod, rq):
     tri_sel = clear & ~sphere_first & np.isfinite(tt) & (kind == 1)
     for f in ("inst", "prim", "t"):
         assert np.array_equal(got[f][tri_sel], tri_hits[f][tri_sel])
+
+
+def test_curves_as_surface_candidates(lcx, rq):
+    """Curve segments reach the candidate callback as surface candidates (bary_v = -1); committing
+    every candidate gives lcx_trace_closest's records bit for bit, curve and triangle hits alike,
+    and a cutout of every curve segment leaves only the triangles."""
+    import torch
+    from luisacompute_gb300.accel import Accel, Curve, hits_to_numpy, mesh_from_data, rays_to_device
+    rng = np.random.default_rng(77)
+    cps = S.hair_curves(80, 10, rng)
+    segs = S.curve_segments(80, 10, 2)
+    cv = Curve(2, torch.from_numpy(cps).cuda(), torch.from_numpy(segs.astype(np.int32)).cuda()).build()
+    mesh = mesh_from_data(S.icosphere(3, radius=0.7)).build()
+    acc = Accel()
+    acc.emplace_back(cv)
+    acc.emplace_back(mesh)
+    acc.build()
+    rays = S.sphere_rays(60_000, [-1.5] * 3, [1.5] * 3, seed=78)
+    d = rays_to_device(rays)
+    n = rays.shape[0]
+    hits = torch.empty((n, 6), dtype=torch.int32, device="cuda")
+    assert rq.rq_run(ctypes.byref(_view(acc)), d.data_ptr(), n, 0, CUT, hits.data_ptr(), None) == 0
+    got = hits_to_numpy(hits)
+    want = hits_to_numpy(acc.trace_closest(d))
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    on_curve = got["inst"] == 0
+    assert on_curve.sum() > 500 and (got["inst"] == 1).sum() > 500
+    assert np.all(got["bary"][on_curve, 1] == -1.0)
