@@ -852,6 +852,7 @@ int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, u
     p.tlas_f = a->fn;
     p.insts = a->recs;
     p.motion = a->has_motion || a->has_curves;
+    p.curves = a->has_curves;
     p.rays = reinterpret_cast<const Ray *>(d_rays);
     p.hits = reinterpret_cast<Hit *>(d_hits);
     p.ray_count = ray_count;
@@ -1544,6 +1545,7 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
         p.tlas_f = a->fn;
         p.insts = a->recs;
         p.motion = a->has_motion || a->has_curves;
+        p.curves = a->has_curves;
     }
     p.times = d_times;
     if (d_times && reinterpret_cast<uintptr_t>(d_times) % 4 != 0)

@@ -185,6 +185,7 @@ struct TraceParams {
     const uint32_t *order;  // non-null: the k-th ray taken is rays[order[k]] (single-job launches)
     uint32_t short_stack;   // shared-memory stack entries per thread: 8, 16 or 24 (single-job, mode 0)
     bool motion;            // the accel has motion or curves: the extended kernels (mode 0) run the call
+    bool curves;            // with `motion`: the accel has curves (the extended kernels with the curve test)
     const float *times;     // motion launches: per-ray times (null: time 0)
 };
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st);

@@ -65,9 +65,10 @@ constexpr uint32_t kMaxRaySteps = 1u << 22;  // per-ray bound: a corrupt tree en
 // Per-lane traversal state and the operations both loop structures share.
 // kMulti: the launch serves several jobs (scenes); each lane takes its job's
 // TLAS, instance table, mask and buffers when it takes a ray.
-// kMotion: the extended kernels, for accels with motion instances, vertex-motion
-// meshes or curves (each ray has a time; curve segments get the curve test).
-template <int kLayout, bool kAny, bool kCount, bool kMulti, int kShort, bool kMotion = false>
+// kExt: the extended kernels.  1: accels with motion instances or vertex-motion
+// meshes (each ray has a time); 2: also curves (curve segments get the curve test,
+// with a larger register budget).
+template <int kLayout, bool kAny, bool kCount, bool kMulti, int kShort, int kExt = 0>
 struct Walker {
     static constexpr int kShortStack = kShort < kStackSize ? kShort : kStackSize;
     static constexpr int kDeep = kStackSize - kShortStack;    // entries in local memory
@@ -161,7 +162,7 @@ struct Walker {
         wdy = r1.y;
         wdz = r1.z;
         best_t = r1.w;
-        if (kMotion) time = P.times != nullptr ? __ldg(P.times + slot) : 0.0f;
+        if (kExt) time = P.times != nullptr ? __ldg(P.times + slot) : 0.0f;
         best_u = best_v = 0.0f;
         best_inst = best_prim = kInvalid;
         to_world();
@@ -181,7 +182,7 @@ struct Walker {
         iy = slab_rcp(wdy);
         iz = slab_rcp(wdz);
         octinv = octant_inv(wdx, wdy, wdz);
-        if (kMotion) {
+        if (kExt >= 2) {
             rdx = wdx;
             rdy = wdy;
             rdz = wdz;
@@ -224,7 +225,7 @@ struct Walker {
             Gt.y &= Gt.y - 1u;
             const float4 *tp = reinterpret_cast<const float4 *>(blas_tris + Gt.x + k);
             float4 a = bvh_ld(tp), b = bvh_ld(tp + 1), c = bvh_ld(tp + 2);
-            if constexpr (kMotion) {
+            if constexpr (kExt >= 2) {
                 if (__float_as_uint(b.w) == kTriCurve) {  // a curve segment
                     if (kCount) c_tris++;
                     const float4 *cp = reinterpret_cast<const float4 *>(
@@ -247,6 +248,8 @@ struct Walker {
                     }
                     continue;
                 }
+            }
+            if constexpr (kExt >= 1) {
                 if (__float_as_uint(b.w) == kTriMotion) {  // a vertex-motion mesh: its triangle at the ray's time
                     const MeshMotion *mm = reinterpret_cast<const MeshMotion *>(
                         (unsigned long long)__float_as_uint(c.x) | ((unsigned long long)__float_as_uint(c.y) << 32));
@@ -372,7 +375,7 @@ struct Walker {
             const uint4 *ip = reinterpret_cast<const uint4 *>((kMulti ? insts : P.insts) + Gt.x + k);
             const uint4 m4 = bvh_ld(ip + 4);  // fnodes (x,y), inst_id (z), mask (w)
             float w[12];
-            if constexpr (!kMotion) {
+            if constexpr (!kExt) {
                 if ((m4.w & (kMulti ? mask : P.mask)) == 0u) continue;
                 const float4 r0 = bvh_ld(reinterpret_cast<const float4 *>(ip));
                 const float4 r1 = bvh_ld(reinterpret_cast<const float4 *>(ip + 1));
@@ -414,7 +417,7 @@ struct Walker {
             iz = slab_rcp(dz);
             octinv = octant_inv(dx, dy, dz);
             wt = wt_setup(ox, oy, oz, dx, dy, dz);
-            if (kMotion) {
+            if (kExt >= 2) {
                 rdx = dx;
                 rdy = dy;
                 rdz = dz;
@@ -466,12 +469,12 @@ struct Walker {
 // kMode 1: speculative while-while (Aila & Laine 2009): lanes walk nodes
 // together; a lane that finds items keeps walking (holding them in Gp) while
 // any lane of the warp is still searching, then all lanes handle items.
-template <int kLayout, bool kAny, bool kCount, int kMode, bool kMulti, int kShort, bool kMotion = false>
-__global__ void __launch_bounds__(kTraceBlock, kMotion                       ? LCX_TRACE_MIN_BLOCKS_EXT
+template <int kLayout, bool kAny, bool kCount, int kMode, bool kMulti, int kShort, int kExt = 0>
+__global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? LCX_TRACE_MIN_BLOCKS_EXT
                                                : kLayout == LCX_NODES_QUANT8 ? LCX_TRACE_MIN_BLOCKS_Q
                                                                              : LCX_TRACE_MIN_BLOCKS_F)
     k_trace(TraceParams P) {
-    using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort, kMotion>;
+    using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort, kExt>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
 #if LCX_COOP_TRIS
     __shared__ unsigned long long coop_keys[kTraceBlock];  // per owner lane: min (ordered t, prim)
@@ -923,7 +926,7 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
     }
 }
 
-template <int L, bool A, bool C, int M, bool X, int S, bool Mo = false>
+template <int L, bool A, bool C, int M, bool X, int S, int Mo = 0>
 int blocks_per_sm() {
     static int v = 0;
     if (v == 0) {
@@ -945,7 +948,7 @@ int sm_count() {
     return v;
 }
 
-template <int L, bool A, bool C, int M, bool X = false, int S = kDefaultShortStack, bool Mo = false>
+template <int L, bool A, bool C, int M, bool X = false, int S = kDefaultShortStack, int Mo = 0>
 cudaError_t launch_one(const TraceParams &p, cudaStream_t st) {
     const uint64_t warps_needed = (uint64_t(p.ray_count) + 31) / 32;
     uint64_t grid = uint64_t(sm_count()) * blocks_per_sm<L, A, C, M, X, S, Mo>();
@@ -995,18 +998,24 @@ cudaError_t launch_mode(const TraceParams &p, int layout, bool any, bool countin
     return launch_one<LCX_NODES_FP32, false, false, M>(p, st);
 }
 
+// The extended kernels (kExt 1: motion; 2: motion and curves), loop mode 0 with per-ray times.
+template <int E>
+cudaError_t launch_ext(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
+    if (layout == LCX_NODES_QUANT8) {
+        if (counting) return launch_one<LCX_NODES_QUANT8, false, true, 0, false, kDefaultShortStack, E>(p, st);
+        return any ? launch_one<LCX_NODES_QUANT8, true, false, 0, false, kDefaultShortStack, E>(p, st)
+                   : launch_one<LCX_NODES_QUANT8, false, false, 0, false, kDefaultShortStack, E>(p, st);
+    }
+    if (counting) return launch_one<LCX_NODES_FP32, false, true, 0, false, kDefaultShortStack, E>(p, st);
+    return any ? launch_one<LCX_NODES_FP32, true, false, 0, false, kDefaultShortStack, E>(p, st)
+               : launch_one<LCX_NODES_FP32, false, false, 0, false, kDefaultShortStack, E>(p, st);
+}
+
 }  // namespace
 
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
     if (p.motion) {  // accels with motion or curves: the extended kernels, loop mode 0
-        if (layout == LCX_NODES_QUANT8) {
-            if (counting) return launch_one<LCX_NODES_QUANT8, false, true, 0, false, kDefaultShortStack, true>(p, st);
-            return any ? launch_one<LCX_NODES_QUANT8, true, false, 0, false, kDefaultShortStack, true>(p, st)
-                       : launch_one<LCX_NODES_QUANT8, false, false, 0, false, kDefaultShortStack, true>(p, st);
-        }
-        if (counting) return launch_one<LCX_NODES_FP32, false, true, 0, false, kDefaultShortStack, true>(p, st);
-        return any ? launch_one<LCX_NODES_FP32, true, false, 0, false, kDefaultShortStack, true>(p, st)
-                   : launch_one<LCX_NODES_FP32, false, false, 0, false, kDefaultShortStack, true>(p, st);
+        return p.curves ? launch_ext<2>(p, layout, any, counting, st) : launch_ext<1>(p, layout, any, counting, st);
     }
     if (p.jobs != nullptr) {  // multi-job launches: no counting; mode 2 with quantised nodes, else mode 0
         if (p.mode == 2 && layout == LCX_NODES_QUANT8)
