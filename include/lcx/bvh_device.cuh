@@ -129,7 +129,7 @@ struct __align__(16) BlasDesc {
     float hi[3];
     uint32_t valid;  // bit 0: built with at least one item; bit 1: procedural (AABB items); bit 2: curve
     const MeshMotion *motion;  // vertex motion (null: static vertices)
-    const float4 *curve;       // curve BLAS: 4 Bezier control points per segment (else null)
+    uint64_t _pad;
 };
 static_assert(sizeof(BlasDesc) == 80, "BlasDesc is 80 B");
 // InstRec.mask of a procedural instance: its visibility mask in bits 8..15 and
@@ -462,9 +462,8 @@ __host__ __device__ __forceinline__ float ordered_to_float(uint32_t u) {
 // curve is the union of the balls centred on its curve c(u), u in [0, 1],
 // with radius r(u); position and radius (x, y, z and w of the control points)
 // follow the segment's basis.  The build converts every segment to cubic
-// Bezier form (4 control points, 64 B, in the BLAS's `curve` array);
-// piecewise-linear segments keep their two points in slots 0 and 3 (slots 1
-// and 2 repeat them).
+// Bezier form (4 control points, 64 B, in a build-time array); piecewise-linear
+// segments keep their two points in slots 0 and 3 (slots 1 and 2 repeat them).
 //
 // A cubic segment is traced as `pieces` round cones, piece k being the convex
 // hull of the balls at u = k/pieces and (k+1)/pieces.  The build picks the
@@ -489,9 +488,10 @@ __host__ __device__ __forceinline__ float ordered_to_float(uint32_t u) {
 constexpr uint32_t kTriCurve = 0xfffffffeu;  // TriRec v1.w of a curve segment
 enum : uint32_t { kCurveLinear = 0, kCurveBSpline = 1, kCurveCatmullRom = 2, kCurveBezier = 3 };
 constexpr uint32_t kCurveMaxPieces = 32;
-// TriRec of a curve segment: v0.w = prim id, v1.w = kTriCurve, v2.xy = address
-// of its 4 Bezier points, v2.z = pieces, v2.w = flags (bit 0: open start,
-// bit 1: open end).
+// Leaf record of cone k of a curve segment (each cone is its own BVH item, so
+// traversal culls cones with their own tight boxes): v0 = (start ball centre,
+// segment id), v1 = (end ball centre, kTriCurve), v2 = (start radius, end
+// radius, k | pieces << 16, flags: bit 0 open start, bit 1 open end).
 
 __device__ __forceinline__ float4 f4_axpy(float a, float4 x, float4 y) {  // a x + y
     return make_float4(__fmaf_rn(a, x.x, y.x), __fmaf_rn(a, x.y, y.y), __fmaf_rn(a, x.z, y.z), __fmaf_rn(a, x.w, y.w));
@@ -707,49 +707,27 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
     return true;
 }
 
-// Closest entry into curve segment `cp` (4 Bezier points) with t in [tmin, tmax].
-__device__ __forceinline__ bool curve_intersect(const float4 *cp, uint32_t pieces, uint32_t flags, float3 o, float3 d,
-                                                float tmin, float tmax, float &t_out, float &u_out) {
-    float4 p[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) p[k] = bvh_ld(cp + k);
-    pieces = min(max(pieces, 1u), kCurveMaxPieces);
-    const float dd = dot3_rn(d.x, d.y, d.z, d.x, d.y, d.z);
-    if (!(dd > 0.0f)) return false;
-    bool found = false;
-    float4 c0 = p[0];
-    c0.w = fmaxf(c0.w, 0.0f);
-    for (uint32_t k = 0; k < pieces; k++) {
-        float4 c1 = (k + 1 == pieces) ? p[3] : bezier_at(p, __fdiv_rn(float(k + 1), float(pieces)));
-        c1.w = fmaxf(c1.w, 0.0f);
-        // cull by the piece's bounding sphere: distance from its middle to the ray's line
-        const float mx = __fsub_rn(__fmul_rn(0.5f, __fadd_rn(c0.x, c1.x)), o.x);
-        const float my = __fsub_rn(__fmul_rn(0.5f, __fadd_rn(c0.y, c1.y)), o.y);
-        const float mz = __fsub_rn(__fmul_rn(0.5f, __fadd_rn(c0.z, c1.z)), o.z);
-        const float hx = __fmul_rn(0.5f, __fsub_rn(c1.x, c0.x)), hy = __fmul_rn(0.5f, __fsub_rn(c1.y, c0.y)),
-                    hz = __fmul_rn(0.5f, __fsub_rn(c1.z, c0.z));
-        const float R = __fadd_rn(__fsqrt_rn(dot3_rn(hx, hy, hz, hx, hy, hz)), fmaxf(c0.w, c1.w));
-        const float crx = __fsub_rn(__fmul_rn(my, d.z), __fmul_rn(mz, d.y));
-        const float cry = __fsub_rn(__fmul_rn(mz, d.x), __fmul_rn(mx, d.z));
-        const float crz = __fsub_rn(__fmul_rn(mx, d.y), __fmul_rn(my, d.x));
-        const float dist2 = __fdiv_rn(dot3_rn(crx, cry, crz, crx, cry, crz), dd);
-        if (R > 0.0f && dist2 <= __fmul_rn(__fmul_rn(1.0001f, R), R)) {
-            float t, u;
-            int part;
-            if (round_cone_entry(o, d, c0, c1, tmin, tmax, t, u, part)) {
-                const bool open_cap =
-                    (part == 0 && k == 0 && (flags & 1u)) || (part == 2 && k + 1 == pieces && (flags & 2u));
-                if (!open_cap) {
-                    tmax = t;
-                    t_out = t;
-                    u_out = fminf(__fdiv_rn(__fadd_rn(float(k), u), float(pieces)), 1.0f);
-                    found = true;
-                }
-            }
-        }
-        c0 = c1;
-    }
-    return found;
+// Ball k of `pieces` along a Bezier segment: centre and radius (>= 0) at u = k / pieces.
+__device__ __forceinline__ float4 curve_piece_point(const float4 p[4], uint32_t k, uint32_t pieces) {
+    float4 c = k == 0 ? p[0] : k >= pieces ? p[3] : bezier_at(p, __fdiv_rn(float(k), float(pieces)));
+    c.w = fmaxf(c.w, 0.0f);
+    return c;
+}
+
+// Entry into cone k of a curve segment's `pieces` (balls c0, c1; `flags` as in
+// the leaf record) with t in [tmin, tmax]; u = the curve parameter of the hit.
+__device__ __forceinline__ bool curve_piece_entry(float3 o, float3 d, float4 c0, float4 c1, uint32_t k,
+                                                  uint32_t pieces, uint32_t flags, float tmin, float tmax,
+                                                  float &t_out, float &u_out) {
+    if (!(c0.w > 0.0f || c1.w > 0.0f)) return false;
+    float t, u;
+    int part;
+    if (!round_cone_entry(o, d, c0, c1, tmin, tmax, t, u, part)) return false;
+    if ((part == 0 && k == 0 && (flags & 1u)) || (part == 2 && k + 1 >= pieces && (flags & 2u)))
+        return false;  // the open end of a cubic curve
+    t_out = t;
+    u_out = fminf(__fdiv_rn(__fadd_rn(float(k), u), float(pieces)), 1.0f);
+    return true;
 }
 
 }  // namespace lcx

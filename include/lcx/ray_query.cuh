@@ -161,11 +161,11 @@ __device__ CommittedHit ray_query(const LcxAccelView &view, const LcxRay &ray, u
                 const float4 *tp = reinterpret_cast<const float4 *>(tris + Gt.x + k);
                 const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
                 float t, u, v;
-                if (__float_as_uint(b.w) == kTriCurve) {  // a curve segment: the curve test of the trace kernels
-                    const float4 *cp = reinterpret_cast<const float4 *>(
-                        (unsigned long long)__float_as_uint(c.x) | ((unsigned long long)__float_as_uint(c.y) << 32));
-                    if (!curve_intersect(cp, __float_as_uint(c.z), __float_as_uint(c.w), make_float3(ox, oy, oz),
-                                         make_float3(odx, ody, odz), tmin, best_t, t, u))
+                if (__float_as_uint(b.w) == kTriCurve) {  // a cone of a curve segment: the trace kernels' test
+                    const uint32_t kn = __float_as_uint(c.z);
+                    if (!curve_piece_entry(make_float3(ox, oy, oz), make_float3(odx, ody, odz),
+                                           make_float4(a.x, a.y, a.z, c.x), make_float4(b.x, b.y, b.z, c.y),
+                                           kn & 0xffffu, kn >> 16, __float_as_uint(c.w), tmin, best_t, t, u))
                         continue;
                     v = -1.0f;
                 } else if (!wt_intersect(wt, tmin, best_t, a, b, c, t, u, v)) {

@@ -277,8 +277,9 @@ typedef struct LcxCurveBuildCommand {
  * the ray's t (hit.h:29-30).  Linear segments have spherical end caps; cubic
  * segments are open where the next segment of the buffer does not continue
  * them.  Cubic segments are traced as up to 32 round cones whose chords stay
- * within 5 % of the radius of the exact curve; hits are entries only (a ray
- * starting inside a segment does not hit it).  Accels holding curves trace with
+ * within 5 % of the radius of the exact curve (the BLAS items are the cones:
+ * lcx_mesh_stats counts them); hits are entries only (a ray starting inside a
+ * segment does not hit it).  Accels holding curves trace with
  * the extended kernels (those of motion), through lcx_trace_* and the
  * *_motion / *_host / *_ex entry points; lcx::ray_query offers curve segments
  * as surface candidates with bary_v = -1; lcx_trace_jobs does not take them. */

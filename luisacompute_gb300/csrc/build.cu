@@ -121,6 +121,74 @@ __device__ __forceinline__ void add_centroid(uint32_t seg, bool valid, const flo
     }
 }
 
+// Curve builds.  The BLAS items are the cones of the segments (a linear segment
+// is one cone, a cubic one `pieces` cones, see bvh_device.cuh), so traversal
+// culls cones by their own tight boxes.  k_curve_prep converts each segment to
+// Bezier form, picks its cone count and open ends; after an exclusive scan of
+// the counts, k_curve_fill names the segment of every cone.  The build's
+// SegInput then has vbase = the Bezier array (4 float4 per segment) followed by
+// vcount u32 cone offsets and vcount u32 metas (cones | flags << 8), and
+// tbase = the u32 segment of each cone.
+struct CurveCone {
+    float4 c0, c1;  // balls: centre xyz, radius w
+    uint32_t seg, k, pieces, flags;
+};
+
+__device__ __forceinline__ CurveCone curve_cone(const SegInput &g, uint32_t item) {
+    const float4 *bez = reinterpret_cast<const float4 *>(g.vbase);
+    const uint32_t nseg = g.vcount;
+    const uint32_t *off = reinterpret_cast<const uint32_t *>(bez + 4ull * nseg);
+    const uint32_t *meta = off + nseg;
+    const uint32_t s = min(reinterpret_cast<const uint32_t *>(g.tbase)[item], nseg - 1u);
+    CurveCone c;
+    c.seg = s;
+    c.pieces = max(meta[s] & 0xffu, 1u);
+    c.flags = meta[s] >> 8;
+    c.k = min(item - off[s], c.pieces - 1u);
+    float4 p[4];
+    for (int k = 0; k < 4; k++) p[k] = bez[4ull * s + k];
+    c.c0 = curve_piece_point(p, c.k, c.pieces);
+    c.c1 = curve_piece_point(p, c.k + 1, c.pieces);
+    return c;
+}
+
+__global__ void k_curve_prep(const unsigned char *cps, uint64_t stride, uint32_t cp_count, const uint32_t *seg,
+                             uint32_t nseg, uint32_t basis, float4 *bez, uint32_t *count, uint32_t *meta,
+                             uint32_t *err) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg) return;
+    const uint32_t need = basis == kCurveLinear ? 2u : 4u;
+    const uint32_t first = seg[s];
+    float4 p[4] = {make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
+    uint32_t pieces = 0, flags = 0;
+    if (first > cp_count || cp_count - first < need) {
+        atomicOr(err, 1u);
+    } else {
+        float4 q[4];
+        for (uint32_t k = 0; k < 4; k++) {
+            const float *cp = reinterpret_cast<const float *>(cps + stride * (uint64_t(first) + min(k, need - 1)));
+            q[k] = make_float4(cp[0], cp[1], cp[2], cp[3]);
+        }
+        curve_to_bezier(basis, q, p);
+        pieces = curve_pieces(basis, p);
+        if (basis != kCurveLinear) {  // a cubic curve goes on where the next segment starts at this one's end
+            const uint32_t step = basis == kCurveBezier ? 3u : 1u;
+            if (!(s > 0 && seg[s - 1] + step == first)) flags |= 1u;
+            if (!(s + 1 < nseg && seg[s + 1] == first + step)) flags |= 2u;
+        }
+    }
+    for (int k = 0; k < 4; k++) bez[4ull * s + k] = p[k];
+    count[s] = pieces;
+    meta[s] = pieces | (flags << 8);
+}
+
+__global__ void k_curve_fill(const uint32_t *off, const uint32_t *count, uint32_t nseg, uint32_t *cone_seg) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg) return;
+    const uint32_t o = off[s];
+    for (uint32_t k = 0; k < count[s]; k++) cone_seg[o + k] = s;
+}
+
 __global__ void __launch_bounds__(kPrepBlock) k_tri_prep(const SegInput *segs, uint32_t nseg, uint32_t n, float4 *lo,
                                                          float4 *hi, uint32_t *segctl, uint32_t *ctl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -142,40 +210,14 @@ __global__ void __launch_bounds__(kPrepBlock) k_tri_prep(const SegInput *segs, u
             h.x = bx[3];
             h.y = bx[4];
             h.z = bx[5];
-        } else if ((g.kind & 0xffu) == kSegCurves) {
-            // a curve segment: its control points to Bezier form (kept in the BLAS's curve
-            // array); the box holds the Bezier hull grown by the largest control radius,
-            // which bounds every ball the tracer places along the segment
-            const uint32_t basis = g.kind >> 8;
-            const uint32_t need = basis == kCurveLinear ? 2u : 4u;
-            const uint32_t first = reinterpret_cast<const uint32_t *>(g.tbase)[local];
-            bad = first > g.vcount || g.vcount - first < need;
-            if (!bad) {
-                float4 q[4], p[4];
-                for (uint32_t k = 0; k < 4; k++) {
-                    const float *cp = reinterpret_cast<const float *>(g.vbase + g.vstride * (first + min(k, need - 1)));
-                    q[k] = make_float4(cp[0], cp[1], cp[2], cp[3]);
-                }
-                curve_to_bezier(basis, q, p);
-                float4 *out = const_cast<float4 *>(g.desc->curve) + 4ull * local;  // the build owns the array
-                float pad = 0.0f;
-                for (int k = 0; k < 4; k++) {
-                    out[k] = p[k];
-                    l.x = fminf(l.x, p[k].x);
-                    l.y = fminf(l.y, p[k].y);
-                    l.z = fminf(l.z, p[k].z);
-                    h.x = fmaxf(h.x, p[k].x);
-                    h.y = fmaxf(h.y, p[k].y);
-                    h.z = fmaxf(h.z, p[k].z);
-                    pad = fmaxf(pad, p[k].w);
-                }
-                l.x -= pad;
-                l.y -= pad;
-                l.z -= pad;
-                h.x += pad;
-                h.y += pad;
-                h.z += pad;
-            }
+        } else if ((g.kind & 0xffu) == kSegCurves) {  // one cone of a curve segment: the box of its two balls
+            const CurveCone cc = curve_cone(g, local);
+            l.x = fminf(cc.c0.x - cc.c0.w, cc.c1.x - cc.c1.w);
+            l.y = fminf(cc.c0.y - cc.c0.w, cc.c1.y - cc.c1.w);
+            l.z = fminf(cc.c0.z - cc.c0.w, cc.c1.z - cc.c1.w);
+            h.x = fmaxf(cc.c0.x + cc.c0.w, cc.c1.x + cc.c1.w);
+            h.y = fmaxf(cc.c0.y + cc.c0.w, cc.c1.y + cc.c1.w);
+            h.z = fmaxf(cc.c0.z + cc.c0.w, cc.c1.z + cc.c1.w);
         } else {
             const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * local);
             i0 = t[0];
@@ -1119,25 +1161,12 @@ __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *d
                                    make_float4(bx[3], bx[4], bx[5], 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
                 return;
             }
-            if ((g.kind & 0xffu) == kSegCurves) {  // the segment's Bezier points, piece count and open ends
-                const uint32_t basis = g.kind >> 8;
-                const float4 *cp = g.desc->curve + 4ull * prim;
-                float4 p[4];
-                for (int k = 0; k < 4; k++) p[k] = cp[k];
-                const uint32_t pieces = curve_pieces(basis, p);
-                uint32_t flags = 0;
-                if (basis != kCurveLinear) {  // a cubic curve goes on where the next segment starts at this one's end
-                    const uint32_t *sg = reinterpret_cast<const uint32_t *>(g.tbase);
-                    const uint32_t step = basis == kCurveBezier ? 3u : 1u;
-                    const uint32_t first = sg[prim];
-                    if (!(prim > 0 && sg[prim - 1] + step == first)) flags |= 1u;
-                    if (!(prim + 1 < g.item_count && sg[prim + 1] == first + step)) flags |= 2u;
-                }
-                const unsigned long long a = reinterpret_cast<unsigned long long>(cp);
-                tris[pos] = TriRec{make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(prim)),
-                                   make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kTriCurve)),
-                                   make_float4(__uint_as_float(uint32_t(a)), __uint_as_float(uint32_t(a >> 32)),
-                                               __uint_as_float(pieces), __uint_as_float(flags))};
+            if ((g.kind & 0xffu) == kSegCurves) {  // a cone: its balls, its place along the segment, open ends
+                const CurveCone cc = curve_cone(g, prim);
+                tris[pos] = TriRec{make_float4(cc.c0.x, cc.c0.y, cc.c0.z, __uint_as_float(cc.seg)),
+                                   make_float4(cc.c1.x, cc.c1.y, cc.c1.z, __uint_as_float(kTriCurve)),
+                                   make_float4(cc.c0.w, cc.c1.w, __uint_as_float(cc.k | (cc.pieces << 16)),
+                                               __uint_as_float(cc.flags))};
                 return;
             }
             if (g.kind >> 8) {  // vertex motion: the motion kernels interpolate the vertices at the ray's time
@@ -1360,6 +1389,22 @@ cudaError_t split_count(const SegInput *tsegs, uint32_t nseg, uint32_t n, float 
 cudaError_t exclusive_sum(void *tmp, size_t *tmp_bytes, const uint32_t *in, uint32_t *out, uint32_t n,
                           cudaStream_t st) {
     return cub::DeviceScan::ExclusiveSum(tmp, *tmp_bytes, in, out, int(n), st);
+}
+
+cudaError_t curve_prepare(const unsigned char *cps, uint64_t stride, uint32_t cp_count, const uint32_t *seg,
+                          uint32_t nseg, uint32_t basis, float4 *bez, uint32_t *count, uint32_t *meta, uint32_t *err,
+                          cudaStream_t st) {
+    if (nseg == 0) return cudaSuccess;
+    k_curve_prep<<<blocks_for(nseg, kPrepBlock), kPrepBlock, 0, st>>>(cps, stride, cp_count, seg, nseg, basis, bez,
+                                                                       count, meta, err);
+    return cudaGetLastError();
+}
+
+cudaError_t curve_fill(const uint32_t *off, const uint32_t *count, uint32_t nseg, uint32_t *cone_seg,
+                       cudaStream_t st) {
+    if (nseg == 0) return cudaSuccess;
+    k_curve_fill<<<blocks_for(nseg, kPrepBlock), kPrepBlock, 0, st>>>(off, count, nseg, cone_seg);
+    return cudaGetLastError();
 }
 
 cudaError_t split_emit(const SegInput *tsegs, uint32_t nseg, uint32_t n, const uint32_t *refs, const uint32_t *ref_off,

@@ -160,8 +160,7 @@ struct MeshObj {
     uint32_t node_count = 0, tri_count = 0, depth = 0;
     uint32_t ref_count = 0;  // leaf items: tri_count, or more with triangle splitting
     uint32_t kind = kSegTriangles;  // or kSegAabbs: a procedural primitive (lcx_procedural_*),
-                                    // kSegCurves: a curve (lcx_curve_*)
-    std::shared_ptr<DevBlock> curve_block;  // curves: the segments' Bezier points (64 B each)
+                                    // kSegCurves: a curve (lcx_curve_*; items are its cones)
     LcxMotionOption motion{};       // keyframe_count >= 2: vertex motion (lcx_mesh_create_motion)
     MeshMotion *d_motion = nullptr;  // after the BlasDesc in d_desc's allocation
     uint32_t seg = 0;  // segment (position in its build) within `block`
@@ -689,10 +688,7 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
         if (rb.ctl[kCtlErr] & kErrBadIndex) {
             for (size_t i = 0; i < count; i++)
                 if (rb.segctl[kSegWords * i + kSegErr] & kErrBadIndex)
-                    return fail(LCX_ERR_INVALID_ARG,
-                                (segs[i].kind & 0xffu) == kSegCurves
-                                    ? "curve %zu of the build: a segment's control points run past the %u given"
-                                    : "mesh %zu of the build: triangle index out of range (vertex count %u)",
+                    return fail(LCX_ERR_INVALID_ARG, "mesh %zu of the build: triangle index out of range (vertex count %u)",
                                 i, segs[i].vcount);
             return fail(LCX_ERR_INVALID_ARG, "triangle index out of range");
         }
@@ -952,7 +948,6 @@ int lcx_mesh_destroy(uint64_t mesh) {
     std::lock_guard<std::mutex> lk(m->mtx);
     cudaDeviceSynchronize();
     m->block.reset();
-    m->curve_block.reset();
     if (m->d_desc) cudaFree(m->d_desc);
     m->d_desc = nullptr;
     return LCX_OK;
@@ -1016,10 +1011,10 @@ int lcx_curve_destroy(uint64_t handle) {
 }
 
 // Curve builds (the reference's CurveBuildCommand visit, cpu/accel.rs:142-204;
-// CUDA: cuda_curve.cpp:37-70).  The build converts the segments to Bezier form
-// in a fresh array (the previous one stays alive for traces already queued on
-// the old tree, like a replaced BVH block) and builds the BLAS over the
-// segments' boxes; the emit writes one curve record per segment.
+// CUDA: cuda_curve.cpp:37-70).  The segments go to Bezier form and are cut into
+// cones (one host read-back for the cone count), and the BLAS is built over the
+// cones; their leaf records hold everything a trace needs, so the build-time
+// arrays are released with the build.
 int lcx_curve_build(uint64_t handle, const LcxCurveBuildCommand *cmd, void *stream) {
     auto m = find_mesh(handle);
     if (!m || m->kind != kSegCurves)
@@ -1029,7 +1024,7 @@ int lcx_curve_build(uint64_t handle, const LcxCurveBuildCommand *cmd, void *stre
     if (cmd->basis > LCX_CURVE_BEZIER) return fail(LCX_ERR_INVALID_ARG, "invalid curve basis %u", cmd->basis);
     if (cmd->cp_stride < 16 || cmd->cp_stride % 4 != 0)
         return fail(LCX_ERR_INVALID_ARG, "control point stride %zu must be >= 16 and a multiple of 4", cmd->cp_stride);
-    if (cmd->seg_count >= (1ull << 31) || cmd->cp_count >= (1ull << 32))
+    if (cmd->seg_count >= (1ull << 26) || cmd->cp_count >= (1ull << 32))
         return fail(LCX_ERR_INVALID_ARG, "too many curve segments (%zu) or control points (%zu)", cmd->seg_count,
                     cmd->cp_count);
     if (cmd->seg_count && (!cmd->cp_buffer || !cmd->seg_buffer))
@@ -1038,33 +1033,62 @@ int lcx_curve_build(uint64_t handle, const LcxCurveBuildCommand *cmd, void *stre
         return fail(LCX_ERR_INVALID_ARG, "control point and segment buffers must be 4-byte aligned");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (capturing(st)) return fail(LCX_ERR_INVALID_ARG, "curve build in a CUDA graph capture");
-    Retired retired;  // released after the mutex below
+    Retired retired;  // released after the mutex below (the build-time arrays go with it)
     std::lock_guard<std::mutex> lk(m->mtx);
+    const uint32_t nseg = uint32_t(cmd->seg_count);
+    // [Bezier points 64 B | cone offsets | metas | counts] per segment, an error word, the scan's scratch
+    size_t scan_bytes = 0;
+    LCX_CUDA(exclusive_sum(nullptr, &scan_bytes, nullptr, nullptr, std::max(nseg, 1u), st), "scan size");
+    const size_t nbytes = size_t(std::max(nseg, 1u));
+    const size_t scan_at = (nbytes * 76 + 4 + 255) / 256 * 256;
     auto cblock = std::make_shared<DevBlock>();
-    cblock->bytes = 4 * sizeof(float4) * std::max<size_t>(cmd->seg_count, 1);
-    LCX_CUDA(cudaMalloc(&cblock->ptr, cblock->bytes), "cudaMalloc(curve points)");
-    const float4 *cptr = static_cast<const float4 *>(cblock->ptr);
-    LCX_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(m->d_desc) + offsetof(BlasDesc, curve), &cptr, sizeof(cptr),
-                             cudaMemcpyHostToDevice, st),
-             "curve descriptor");
-    LCX_CUDA(cudaStreamSynchronize(st), "sync");  // `cptr` is a host local
+    cblock->bytes = scan_at + scan_bytes;
+    LCX_CUDA(cudaMalloc(&cblock->ptr, cblock->bytes), "cudaMalloc(curve build)");
+    retired.blocks.push_back(cblock);
+    char *base = static_cast<char *>(cblock->ptr);
+    float4 *bez = reinterpret_cast<float4 *>(base);
+    uint32_t *off = reinterpret_cast<uint32_t *>(base + 64 * nbytes);
+    uint32_t *meta = off + nbytes;
+    uint32_t *count = meta + nbytes;
+    uint32_t *err = count + nbytes;
+    const auto *cps = reinterpret_cast<const unsigned char *>(cmd->cp_buffer) + cmd->cp_buffer_offset;
+    const auto *seg = reinterpret_cast<const uint32_t *>(reinterpret_cast<const unsigned char *>(cmd->seg_buffer) +
+                                                         cmd->seg_buffer_offset);
+    uint32_t cones = 0;
+    uint32_t *cone_seg = nullptr;
+    if (nseg) {
+        LCX_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st), "curve error word");
+        LCX_CUDA(curve_prepare(cps, cmd->cp_stride, uint32_t(cmd->cp_count), seg, nseg, cmd->basis, bez, count, meta,
+                               err, st),
+                 "curve prepare");
+        LCX_CUDA(exclusive_sum(base + scan_at, &scan_bytes, count, off, nseg, st), "curve cone scan");
+        uint32_t h[3] = {0, 0, 0};  // last offset, last count, error
+        LCX_CUDA(cudaMemcpyAsync(&h[0], off + nseg - 1, 4, cudaMemcpyDeviceToHost, st), "cone count");
+        LCX_CUDA(cudaMemcpyAsync(&h[1], count + nseg - 1, 4, cudaMemcpyDeviceToHost, st), "cone count");
+        LCX_CUDA(cudaMemcpyAsync(&h[2], err, 4, cudaMemcpyDeviceToHost, st), "curve errors");
+        LCX_CUDA(cudaStreamSynchronize(st), "sync");
+        if (h[2]) return fail(LCX_ERR_INVALID_ARG, "curve segment control points run past the %zu given", cmd->cp_count);
+        cones = h[0] + h[1];  // at most 32 per segment: below 2^31
+        auto pblock = std::make_shared<DevBlock>();
+        pblock->bytes = sizeof(uint32_t) * std::max(cones, 1u);
+        LCX_CUDA(cudaMalloc(&pblock->ptr, pblock->bytes), "cudaMalloc(curve cones)");
+        retired.blocks.push_back(pblock);
+        cone_seg = static_cast<uint32_t *>(pblock->ptr);
+        LCX_CUDA(curve_fill(off, count, nseg, cone_seg, st), "curve fill");
+    }
     std::vector<MeshObj *> ms{m.get()};
     SegInput g{};
-    g.vbase = reinterpret_cast<const unsigned char *>(cmd->cp_buffer) + cmd->cp_buffer_offset;
-    g.vstride = cmd->cp_stride;
-    g.tbase = reinterpret_cast<const unsigned char *>(cmd->seg_buffer) + cmd->seg_buffer_offset;
-    g.vcount = uint32_t(cmd->cp_count);
+    g.vbase = reinterpret_cast<const unsigned char *>(bez);
+    g.vstride = 0;
+    g.tbase = reinterpret_cast<const unsigned char *>(cone_seg);
+    g.vcount = nseg;
     g.item_offset = 0;
-    g.item_count = uint32_t(cmd->seg_count);
+    g.item_count = cones;
     g.kind = kSegCurves | (cmd->basis << 8);
     g.desc = m->d_desc;
     std::vector<SegInput> segs{g};
     std::vector<uint32_t> req{LCX_REQUEST_FORCE_BUILD};
-    const int r = build_meshes(ms, segs, req, st, retired);
-    if (r != LCX_OK) return r;  // the old tree keeps its own points
-    if (m->curve_block) retired.blocks.push_back(std::move(m->curve_block));
-    m->curve_block = std::move(cblock);
-    return LCX_OK;
+    return build_meshes(ms, segs, req, st, retired);
 }
 
 int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *cmd, void *stream) {

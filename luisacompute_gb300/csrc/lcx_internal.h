@@ -21,8 +21,8 @@ struct SegInput {
     uint32_t item_offset;        // first item of this segment among all items of the build
     uint32_t item_count;
     uint32_t kind;               // low byte: kSegTriangles (vbase, tbase) or kSegAabbs (vbase: 24-byte AABBs)
-                                 // or kSegCurves (vbase: control points, vcount of them; tbase: u32 segment
-                                 // starts; the Bezier form goes to desc->curve);
+                                 // or kSegCurves (vbase: Bezier points, cone offsets and metas of vcount
+                                 // segments; tbase: u32 segment per cone; see build.cu);
                                  // bits 8+: triangles: vertex-motion keyframes (vbase holds them back to back,
                                  // vcount each); curves: the basis (kCurve*)
     BlasDesc *desc;              // BLAS descriptor the emit fills in (null for a TLAS)
@@ -117,6 +117,13 @@ cudaError_t split_count(const SegInput *tsegs, uint32_t nseg, uint32_t n, float 
                         cudaStream_t st);
 cudaError_t exclusive_sum(void *tmp, size_t *tmp_bytes, const uint32_t *in, uint32_t *out, uint32_t n,
                           cudaStream_t st);
+// Curve builds (see build.cu): per-segment Bezier form, cone counts and metas,
+// then the segment of every cone once the counts are scanned.
+cudaError_t curve_prepare(const unsigned char *cps, uint64_t stride, uint32_t cp_count, const uint32_t *seg,
+                          uint32_t nseg, uint32_t basis, float4 *bez, uint32_t *count, uint32_t *meta, uint32_t *err,
+                          cudaStream_t st);
+cudaError_t curve_fill(const uint32_t *off, const uint32_t *count, uint32_t nseg, uint32_t *cone_seg,
+                       cudaStream_t st);
 cudaError_t split_emit(const SegInput *tsegs, uint32_t nseg, uint32_t n, const uint32_t *refs, const uint32_t *ref_off,
                        BuildScratch &s, uint32_t *ref_prim, cudaStream_t st);
 
