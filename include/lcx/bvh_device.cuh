@@ -485,13 +485,22 @@ __host__ __device__ __forceinline__ float ordered_to_float(uint32_t u) {
 // parameter u of the ball that touches the hit point, and bary.y = -1 (the
 // reference's curve-hit convention, include/luisa/runtime/rtx/hit.h:29-30 and
 // cpu/accel.rs:491-494).
-constexpr uint32_t kTriCurve = 0xfffffffeu;  // TriRec v1.w of a curve segment
+constexpr uint32_t kTriCurve = 0xfffffffeu;        // TriRec v1.w of a cone of a curve
+constexpr uint32_t kTriCurveMotion = 0xfffffffdu;  // ... of a curve with keyframed control points
 enum : uint32_t { kCurveLinear = 0, kCurveBSpline = 1, kCurveCatmullRom = 2, kCurveBezier = 3 };
 constexpr uint32_t kCurveMaxPieces = 32;
 // Leaf record of cone k of a curve segment (each cone is its own BVH item, so
 // traversal culls cones with their own tight boxes): v0 = (start ball centre,
 // segment id), v1 = (end ball centre, kTriCurve), v2 = (start radius, end
 // radius, k | pieces << 16, flags: bit 0 open start, bit 1 open end).
+// A curve with keyframed control points (the reference's curve motion,
+// include/luisa/runtime/rtx/curve.h:10): its Bezier points interpolate linearly
+// between keyframes, and so do the balls (they are linear in the points), so a
+// cone keeps per keyframe its two balls and is interpolated at the ray's time.
+// Its record: v0 = (t0, t1, vanish flags, segment id), v1 = (keyframes, 0, 0,
+// kTriCurveMotion), v2 = (address of the keyframes' balls (2 float4 each),
+// k | pieces << 16, open-end flags).  The cone count of a segment is the
+// largest over its keyframes.
 
 __device__ __forceinline__ float4 f4_axpy(float a, float4 x, float4 y) {  // a x + y
     return make_float4(__fmaf_rn(a, x.x, y.x), __fmaf_rn(a, x.y, y.y), __fmaf_rn(a, x.z, y.z), __fmaf_rn(a, x.w, y.w));
@@ -712,6 +721,24 @@ __device__ __forceinline__ float4 curve_piece_point(const float4 p[4], uint32_t 
     float4 c = k == 0 ? p[0] : k >= pieces ? p[3] : bezier_at(p, __fdiv_rn(float(k), float(pieces)));
     c.w = fmaxf(c.w, 0.0f);
     return c;
+}
+
+// The two balls of a keyframed cone at `time` (one FMA per component, as
+// motion_triangle); false when the curve has vanished at that time.
+__device__ __forceinline__ bool curve_motion_cone(const float4 &a, const float4 &b, const float4 &c, float time,
+                                                  float4 &c0, float4 &c1) {
+    uint32_t i;
+    float f;
+    if (!motion_segment(a.x, a.y, __float_as_uint(b.x), __float_as_uint(a.z), time, i, f)) return false;
+    const float4 *kd = reinterpret_cast<const float4 *>(
+                           (unsigned long long)__float_as_uint(c.x) | ((unsigned long long)__float_as_uint(c.y) << 32)) +
+                       2ull * i;
+    const float4 p0 = bvh_ld(kd), p1 = bvh_ld(kd + 1), q0 = bvh_ld(kd + 2), q1 = bvh_ld(kd + 3);
+    c0 = make_float4(__fmaf_rn(f, __fsub_rn(q0.x, p0.x), p0.x), __fmaf_rn(f, __fsub_rn(q0.y, p0.y), p0.y),
+                     __fmaf_rn(f, __fsub_rn(q0.z, p0.z), p0.z), __fmaf_rn(f, __fsub_rn(q0.w, p0.w), p0.w));
+    c1 = make_float4(__fmaf_rn(f, __fsub_rn(q1.x, p1.x), p1.x), __fmaf_rn(f, __fsub_rn(q1.y, p1.y), p1.y),
+                     __fmaf_rn(f, __fsub_rn(q1.z, p1.z), p1.z), __fmaf_rn(f, __fsub_rn(q1.w, p1.w), p1.w));
+    return true;
 }
 
 // Entry into cone k of a curve segment's `pieces` (balls c0, c1; `flags` as in

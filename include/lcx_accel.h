@@ -371,6 +371,16 @@ LCX_API int lcx_motion_instance_build(uint64_t motion_instance, void *stream);
  * by every later trace.  allow_update is rejected (no refit). */
 LCX_API int lcx_mesh_create_motion(const LcxAccelOption *option, const LcxMotionOption *motion,
                                    uint64_t *out_handle);
+/* A curve with keyframed control points (the reference's curve motion,
+ * AccelOption::motion with Curve, include/luisa/runtime/rtx/curve.h:10-11):
+ * the build command's control point buffer holds keyframe_count copies of
+ * cp_count / keyframe_count points back to back, and segment indices address
+ * one copy.  The points interpolate linearly between keyframes spaced evenly over
+ * [time_start, time_end] (clamped, or vanishing with vanish_start / vanish_end);
+ * traces take the ray's time through the *_motion entry points, as for
+ * lcx_mesh_create_motion. */
+LCX_API int lcx_curve_create_motion(const LcxAccelOption *option, const LcxMotionOption *motion,
+                                    uint64_t *out_handle);
 
 /* ----------------------------------------------------------------- queries */
 

@@ -126,6 +126,7 @@ _SIGS = {
     "lcx_get_build_split": (c_int, [POINTER(ctypes.c_float)]),
     "lcx_mesh_build_batch_reserve": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
     "lcx_mesh_create_motion": (c_int, [c_void_p, c_void_p, POINTER(c_uint64)]),
+    "lcx_curve_create_motion": (c_int, [c_void_p, c_void_p, POINTER(c_uint64)]),
     "lcx_motion_instance_create": (c_int, [c_uint64, c_void_p, POINTER(c_uint64)]),
     "lcx_motion_instance_destroy": (c_int, [c_uint64]),
     "lcx_motion_instance_set_keyframes": (c_int, [c_uint64, c_void_p, c_uint32]),

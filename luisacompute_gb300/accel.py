@@ -158,9 +158,13 @@ class Curve:
     float32 CUDA tensor of (x, y, z, radius) records, ``segments`` a uint32 / int32 CUDA tensor with the
     first control point of each segment; ``basis`` is one of CURVE_PIECEWISE_LINEAR, CURVE_CUBIC_BSPLINE,
     CURVE_CATMULL_ROM, CURVE_BEZIER.  Both buffers are borrowed like a mesh's.  Instanced by an Accel like
-    a Mesh; hits on it report prim = segment, bary = (u, -1)."""
+    a Mesh; hits on it report prim = segment, bary = (u, -1).  motion_keyframes >= 2: keyframed control
+    points (lcx_curve_create_motion); ``control_points`` then holds that many copies back to back and
+    ``segments`` index one copy."""
 
-    def __init__(self, basis: int, control_points, segments, option: AccelOption | None = None):
+    def __init__(self, basis: int, control_points, segments, option: AccelOption | None = None,
+                 motion_keyframes: int = 0, time_start: float = 0.0, time_end: float = 1.0,
+                 vanish_start: bool = False, vanish_end: bool = False):
         torch = _torch()
         self.lib = _capi.load()
         if not control_points.is_cuda or control_points.dtype != torch.float32 or control_points.dim() != 2 \
@@ -173,8 +177,13 @@ class Curve:
         self.control_points = control_points
         self.segments = segments
         h = ctypes.c_uint64(0)
-        check(self.lib.lcx_curve_create(ctypes.byref((option or AccelOption()).c()), ctypes.byref(h)),
-              "lcx_curve_create")
+        if motion_keyframes >= 2:
+            mo = _capi.LcxMotionOption(motion_keyframes, time_start, time_end, int(vanish_start), int(vanish_end), 0, 0)
+            check(self.lib.lcx_curve_create_motion(ctypes.byref((option or AccelOption()).c()), ctypes.byref(mo),
+                                                   ctypes.byref(h)), "lcx_curve_create_motion")
+        else:
+            check(self.lib.lcx_curve_create(ctypes.byref((option or AccelOption()).c()), ctypes.byref(h)),
+                  "lcx_curve_create")
         self.handle = h.value
 
     def build(self, request: int = REQUEST_FORCE_BUILD, stream=None) -> "Curve":

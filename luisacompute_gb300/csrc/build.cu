@@ -126,18 +126,23 @@ __device__ __forceinline__ void add_centroid(uint32_t seg, bool valid, const flo
 // culls cones by their own tight boxes.  k_curve_prep converts each segment to
 // Bezier form, picks its cone count and open ends; after an exclusive scan of
 // the counts, k_curve_fill names the segment of every cone.  The build's
-// SegInput then has vbase = the Bezier array (4 float4 per segment) followed by
-// vcount u32 cone offsets and vcount u32 metas (cones | flags << 8), and
-// tbase = the u32 segment of each cone.
+// SegInput then has vbase = the Bezier array (4 float4 per segment and
+// keyframe) followed by vcount u32 cone offsets and vcount u32 metas (cones |
+// flags << 8), tbase = the u32 segment of each cone, kind bits 16+ = the
+// keyframes (0 or 1: static) and, for keyframed curves, vstride = the address
+// of the cones' keyframe balls that the emit fills (2 float4 per cone and
+// keyframe).
 struct CurveCone {
     float4 c0, c1;  // balls: centre xyz, radius w
     uint32_t seg, k, pieces, flags;
 };
 
-__device__ __forceinline__ CurveCone curve_cone(const SegInput &g, uint32_t item) {
+__device__ __forceinline__ uint32_t curve_keys(const SegInput &g) { return max(g.kind >> 16, 1u); }
+
+__device__ __forceinline__ CurveCone curve_cone(const SegInput &g, uint32_t item, uint32_t key = 0) {
     const float4 *bez = reinterpret_cast<const float4 *>(g.vbase);
-    const uint32_t nseg = g.vcount;
-    const uint32_t *off = reinterpret_cast<const uint32_t *>(bez + 4ull * nseg);
+    const uint32_t nseg = g.vcount, keys = curve_keys(g);
+    const uint32_t *off = reinterpret_cast<const uint32_t *>(bez + 4ull * keys * nseg);
     const uint32_t *meta = off + nseg;
     const uint32_t s = min(reinterpret_cast<const uint32_t *>(g.tbase)[item], nseg - 1u);
     CurveCone c;
@@ -146,38 +151,43 @@ __device__ __forceinline__ CurveCone curve_cone(const SegInput &g, uint32_t item
     c.flags = meta[s] >> 8;
     c.k = min(item - off[s], c.pieces - 1u);
     float4 p[4];
-    for (int k = 0; k < 4; k++) p[k] = bez[4ull * s + k];
+    for (int k = 0; k < 4; k++) p[k] = bez[4ull * (uint64_t(s) * keys + min(key, keys - 1u)) + k];
     c.c0 = curve_piece_point(p, c.k, c.pieces);
     c.c1 = curve_piece_point(p, c.k + 1, c.pieces);
     return c;
 }
 
-__global__ void k_curve_prep(const unsigned char *cps, uint64_t stride, uint32_t cp_count, const uint32_t *seg,
-                             uint32_t nseg, uint32_t basis, float4 *bez, uint32_t *count, uint32_t *meta,
-                             uint32_t *err) {
+// cp_count: control points per keyframe; keyframe j's points follow keyframe j-1's.
+__global__ void k_curve_prep(const unsigned char *cps, uint64_t stride, uint32_t cp_count, uint32_t keys,
+                             const uint32_t *seg, uint32_t nseg, uint32_t basis, float4 *bez, uint32_t *count,
+                             uint32_t *meta, uint32_t *err) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nseg) return;
     const uint32_t need = basis == kCurveLinear ? 2u : 4u;
     const uint32_t first = seg[s];
-    float4 p[4] = {make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
+    const bool bad = first > cp_count || cp_count - first < need;
+    if (bad) atomicOr(err, 1u);
     uint32_t pieces = 0, flags = 0;
-    if (first > cp_count || cp_count - first < need) {
-        atomicOr(err, 1u);
-    } else {
-        float4 q[4];
-        for (uint32_t k = 0; k < 4; k++) {
-            const float *cp = reinterpret_cast<const float *>(cps + stride * (uint64_t(first) + min(k, need - 1)));
-            q[k] = make_float4(cp[0], cp[1], cp[2], cp[3]);
+    for (uint32_t key = 0; key < keys; key++) {
+        float4 p[4] = {make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0),
+                       make_float4(0, 0, 0, 0)};
+        if (!bad) {
+            float4 q[4];
+            for (uint32_t k = 0; k < 4; k++) {
+                const uint64_t at = uint64_t(key) * cp_count + first + min(k, need - 1);
+                const float *cp = reinterpret_cast<const float *>(cps + stride * at);
+                q[k] = make_float4(cp[0], cp[1], cp[2], cp[3]);
+            }
+            curve_to_bezier(basis, q, p);
+            pieces = max(pieces, curve_pieces(basis, p));
         }
-        curve_to_bezier(basis, q, p);
-        pieces = curve_pieces(basis, p);
-        if (basis != kCurveLinear) {  // a cubic curve goes on where the next segment starts at this one's end
-            const uint32_t step = basis == kCurveBezier ? 3u : 1u;
-            if (!(s > 0 && seg[s - 1] + step == first)) flags |= 1u;
-            if (!(s + 1 < nseg && seg[s + 1] == first + step)) flags |= 2u;
-        }
+        for (int k = 0; k < 4; k++) bez[4ull * (uint64_t(s) * keys + key) + k] = p[k];
     }
-    for (int k = 0; k < 4; k++) bez[4ull * s + k] = p[k];
+    if (!bad && basis != kCurveLinear) {  // a cubic curve goes on where the next segment starts at this one's end
+        const uint32_t step = basis == kCurveBezier ? 3u : 1u;
+        if (!(s > 0 && seg[s - 1] + step == first)) flags |= 1u;
+        if (!(s + 1 < nseg && seg[s + 1] == first + step)) flags |= 2u;
+    }
     count[s] = pieces;
     meta[s] = pieces | (flags << 8);
 }
@@ -210,14 +220,18 @@ __global__ void __launch_bounds__(kPrepBlock) k_tri_prep(const SegInput *segs, u
             h.x = bx[3];
             h.y = bx[4];
             h.z = bx[5];
-        } else if ((g.kind & 0xffu) == kSegCurves) {  // one cone of a curve segment: the box of its two balls
-            const CurveCone cc = curve_cone(g, local);
-            l.x = fminf(cc.c0.x - cc.c0.w, cc.c1.x - cc.c1.w);
-            l.y = fminf(cc.c0.y - cc.c0.w, cc.c1.y - cc.c1.w);
-            l.z = fminf(cc.c0.z - cc.c0.w, cc.c1.z - cc.c1.w);
-            h.x = fmaxf(cc.c0.x + cc.c0.w, cc.c1.x + cc.c1.w);
-            h.y = fmaxf(cc.c0.y + cc.c0.w, cc.c1.y + cc.c1.w);
-            h.z = fmaxf(cc.c0.z + cc.c0.w, cc.c1.z + cc.c1.w);
+        } else if ((g.kind & 0xffu) == kSegCurves) {
+            // one cone of a curve segment: the box of its two balls, over the keyframes (a ball
+            // interpolated between two keyframes stays inside the union of their boxes)
+            for (uint32_t key = 0; key < curve_keys(g); key++) {
+                const CurveCone cc = curve_cone(g, local, key);
+                l.x = fminf(l.x, fminf(cc.c0.x - cc.c0.w, cc.c1.x - cc.c1.w));
+                l.y = fminf(l.y, fminf(cc.c0.y - cc.c0.w, cc.c1.y - cc.c1.w));
+                l.z = fminf(l.z, fminf(cc.c0.z - cc.c0.w, cc.c1.z - cc.c1.w));
+                h.x = fmaxf(h.x, fmaxf(cc.c0.x + cc.c0.w, cc.c1.x + cc.c1.w));
+                h.y = fmaxf(h.y, fmaxf(cc.c0.y + cc.c0.w, cc.c1.y + cc.c1.w));
+                h.z = fmaxf(h.z, fmaxf(cc.c0.z + cc.c0.w, cc.c1.z + cc.c1.w));
+            }
         } else {
             const uint32_t *t = reinterpret_cast<const uint32_t *>(g.tbase + 12ull * local);
             i0 = t[0];
@@ -1161,6 +1175,23 @@ __global__ void k_emit_blas(TreeView tv, const SegInput *segs, const uint32_t *d
                                    make_float4(bx[3], bx[4], bx[5], 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
                 return;
             }
+            if ((g.kind & 0xffu) == kSegCurves && curve_keys(g) > 1) {  // a keyframed cone
+                const uint32_t keys = curve_keys(g);
+                float4 *kd = reinterpret_cast<float4 *>(g.vstride) + 2ull * keys * prim;
+                CurveCone cc{};
+                for (uint32_t key = 0; key < keys; key++) {
+                    cc = curve_cone(g, prim, key);
+                    kd[2 * key] = cc.c0;
+                    kd[2 * key + 1] = cc.c1;
+                }
+                const MeshMotion *mm = g.desc->motion;
+                const unsigned long long ka = reinterpret_cast<unsigned long long>(kd);
+                tris[pos] = TriRec{make_float4(mm->t0, mm->t1, __uint_as_float(mm->flags), __uint_as_float(cc.seg)),
+                                   make_float4(__uint_as_float(keys), 0.0f, 0.0f, __uint_as_float(kTriCurveMotion)),
+                                   make_float4(__uint_as_float(uint32_t(ka)), __uint_as_float(uint32_t(ka >> 32)),
+                                               __uint_as_float(cc.k | (cc.pieces << 16)), __uint_as_float(cc.flags))};
+                return;
+            }
             if ((g.kind & 0xffu) == kSegCurves) {  // a cone: its balls, its place along the segment, open ends
                 const CurveCone cc = curve_cone(g, prim);
                 tris[pos] = TriRec{make_float4(cc.c0.x, cc.c0.y, cc.c0.z, __uint_as_float(cc.seg)),
@@ -1391,12 +1422,12 @@ cudaError_t exclusive_sum(void *tmp, size_t *tmp_bytes, const uint32_t *in, uint
     return cub::DeviceScan::ExclusiveSum(tmp, *tmp_bytes, in, out, int(n), st);
 }
 
-cudaError_t curve_prepare(const unsigned char *cps, uint64_t stride, uint32_t cp_count, const uint32_t *seg,
-                          uint32_t nseg, uint32_t basis, float4 *bez, uint32_t *count, uint32_t *meta, uint32_t *err,
-                          cudaStream_t st) {
+cudaError_t curve_prepare(const unsigned char *cps, uint64_t stride, uint32_t cp_count, uint32_t keys,
+                          const uint32_t *seg, uint32_t nseg, uint32_t basis, float4 *bez, uint32_t *count,
+                          uint32_t *meta, uint32_t *err, cudaStream_t st) {
     if (nseg == 0) return cudaSuccess;
-    k_curve_prep<<<blocks_for(nseg, kPrepBlock), kPrepBlock, 0, st>>>(cps, stride, cp_count, seg, nseg, basis, bez,
-                                                                       count, meta, err);
+    k_curve_prep<<<blocks_for(nseg, kPrepBlock), kPrepBlock, 0, st>>>(cps, stride, cp_count, keys, seg, nseg, basis,
+                                                                       bez, count, meta, err);
     return cudaGetLastError();
 }
 

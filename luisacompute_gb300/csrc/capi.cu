@@ -161,6 +161,7 @@ struct MeshObj {
     uint32_t ref_count = 0;  // leaf items: tri_count, or more with triangle splitting
     uint32_t kind = kSegTriangles;  // or kSegAabbs: a procedural primitive (lcx_procedural_*),
                                     // kSegCurves: a curve (lcx_curve_*; items are its cones)
+    std::shared_ptr<DevBlock> curve_keys;  // keyframed curves: the cones' balls per keyframe
     LcxMotionOption motion{};       // keyframe_count >= 2: vertex motion (lcx_mesh_create_motion)
     MeshMotion *d_motion = nullptr;  // after the BlasDesc in d_desc's allocation
     uint32_t seg = 0;  // segment (position in its build) within `block`
@@ -948,6 +949,7 @@ int lcx_mesh_destroy(uint64_t mesh) {
     std::lock_guard<std::mutex> lk(m->mtx);
     cudaDeviceSynchronize();
     m->block.reset();
+    m->curve_keys.reset();
     if (m->d_desc) cudaFree(m->d_desc);
     m->d_desc = nullptr;
     return LCX_OK;
@@ -1004,6 +1006,15 @@ int lcx_curve_create(const LcxAccelOption *option, uint64_t *out_handle) {
     return LCX_OK;
 }
 
+int lcx_curve_create_motion(const LcxAccelOption *option, const LcxMotionOption *motion, uint64_t *out_handle) {
+    if (motion && motion->keyframe_count >= (1u << 16))
+        return fail(LCX_ERR_INVALID_ARG, "a motion curve takes at most 65535 keyframes");
+    if (int r = lcx_mesh_create_motion(option, motion, out_handle)) return r;
+    auto m = find_mesh(*out_handle);
+    m->kind = kSegCurves;
+    return LCX_OK;
+}
+
 int lcx_curve_destroy(uint64_t handle) {
     auto m = find_mesh(handle);
     if (m && m->kind != kSegCurves) return fail(LCX_ERR_INVALID_ARG, "lcx_curve_destroy: handle is not a curve");
@@ -1036,18 +1047,24 @@ int lcx_curve_build(uint64_t handle, const LcxCurveBuildCommand *cmd, void *stre
     Retired retired;  // released after the mutex below (the build-time arrays go with it)
     std::lock_guard<std::mutex> lk(m->mtx);
     const uint32_t nseg = uint32_t(cmd->seg_count);
-    // [Bezier points 64 B | cone offsets | metas | counts] per segment, an error word, the scan's scratch
+    const uint32_t keys = m->motion.keyframe_count >= 2 ? m->motion.keyframe_count : 1u;
+    if (cmd->cp_count % keys != 0)
+        return fail(LCX_ERR_INVALID_ARG, "control point count %zu is not a multiple of the %u keyframes", cmd->cp_count,
+                    keys);
+    const uint32_t cp_per_key = uint32_t(cmd->cp_count / keys);
+    // [Bezier points 64 B per keyframe | cone offsets | metas | counts] per segment, an error word,
+    // the scan's scratch
     size_t scan_bytes = 0;
     LCX_CUDA(exclusive_sum(nullptr, &scan_bytes, nullptr, nullptr, std::max(nseg, 1u), st), "scan size");
     const size_t nbytes = size_t(std::max(nseg, 1u));
-    const size_t scan_at = (nbytes * 76 + 4 + 255) / 256 * 256;
+    const size_t scan_at = (nbytes * (64 * size_t(keys) + 12) + 4 + 255) / 256 * 256;
     auto cblock = std::make_shared<DevBlock>();
     cblock->bytes = scan_at + scan_bytes;
     LCX_CUDA(cudaMalloc(&cblock->ptr, cblock->bytes), "cudaMalloc(curve build)");
     retired.blocks.push_back(cblock);
     char *base = static_cast<char *>(cblock->ptr);
     float4 *bez = reinterpret_cast<float4 *>(base);
-    uint32_t *off = reinterpret_cast<uint32_t *>(base + 64 * nbytes);
+    uint32_t *off = reinterpret_cast<uint32_t *>(base + 64 * size_t(keys) * nbytes);
     uint32_t *meta = off + nbytes;
     uint32_t *count = meta + nbytes;
     uint32_t *err = count + nbytes;
@@ -1058,8 +1075,8 @@ int lcx_curve_build(uint64_t handle, const LcxCurveBuildCommand *cmd, void *stre
     uint32_t *cone_seg = nullptr;
     if (nseg) {
         LCX_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st), "curve error word");
-        LCX_CUDA(curve_prepare(cps, cmd->cp_stride, uint32_t(cmd->cp_count), seg, nseg, cmd->basis, bez, count, meta,
-                               err, st),
+        LCX_CUDA(curve_prepare(cps, cmd->cp_stride, cp_per_key, keys, seg, nseg, cmd->basis, bez, count, meta, err,
+                               st),
                  "curve prepare");
         LCX_CUDA(exclusive_sum(base + scan_at, &scan_bytes, count, off, nseg, st), "curve cone scan");
         uint32_t h[3] = {0, 0, 0};  // last offset, last count, error
@@ -1067,7 +1084,7 @@ int lcx_curve_build(uint64_t handle, const LcxCurveBuildCommand *cmd, void *stre
         LCX_CUDA(cudaMemcpyAsync(&h[1], count + nseg - 1, 4, cudaMemcpyDeviceToHost, st), "cone count");
         LCX_CUDA(cudaMemcpyAsync(&h[2], err, 4, cudaMemcpyDeviceToHost, st), "curve errors");
         LCX_CUDA(cudaStreamSynchronize(st), "sync");
-        if (h[2]) return fail(LCX_ERR_INVALID_ARG, "curve segment control points run past the %zu given", cmd->cp_count);
+        if (h[2]) return fail(LCX_ERR_INVALID_ARG, "curve segment control points run past the %u given", cp_per_key);
         cones = h[0] + h[1];  // at most 32 per segment: below 2^31
         auto pblock = std::make_shared<DevBlock>();
         pblock->bytes = sizeof(uint32_t) * std::max(cones, 1u);
@@ -1076,19 +1093,36 @@ int lcx_curve_build(uint64_t handle, const LcxCurveBuildCommand *cmd, void *stre
         cone_seg = static_cast<uint32_t *>(pblock->ptr);
         LCX_CUDA(curve_fill(off, count, nseg, cone_seg, st), "curve fill");
     }
+    std::shared_ptr<DevBlock> kblock;  // keyframed curves: the cones' balls per keyframe, kept with the tree
+    if (keys > 1) {
+        kblock = std::make_shared<DevBlock>();
+        kblock->bytes = 2 * sizeof(float4) * size_t(keys) * std::max(cones, 1u);
+        LCX_CUDA(cudaMalloc(&kblock->ptr, kblock->bytes), "cudaMalloc(curve keyframes)");
+        MeshMotion mm{};
+        mm.keys = keys;
+        mm.t0 = m->motion.time_start;
+        mm.t1 = m->motion.time_end;
+        mm.flags = (m->motion.vanish_start ? 1u : 0u) | (m->motion.vanish_end ? 2u : 0u);
+        LCX_CUDA(cudaMemcpyAsync(m->d_motion, &mm, sizeof(mm), cudaMemcpyHostToDevice, st), "motion upload");
+        LCX_CUDA(cudaStreamSynchronize(st), "sync");  // `mm` is a host local
+    }
     std::vector<MeshObj *> ms{m.get()};
     SegInput g{};
     g.vbase = reinterpret_cast<const unsigned char *>(bez);
-    g.vstride = 0;
+    g.vstride = kblock ? reinterpret_cast<uint64_t>(kblock->ptr) : 0;
     g.tbase = reinterpret_cast<const unsigned char *>(cone_seg);
     g.vcount = nseg;
     g.item_offset = 0;
     g.item_count = cones;
-    g.kind = kSegCurves | (cmd->basis << 8);
+    g.kind = kSegCurves | (cmd->basis << 8) | (keys > 1 ? keys << 16 : 0u);
     g.desc = m->d_desc;
     std::vector<SegInput> segs{g};
     std::vector<uint32_t> req{LCX_REQUEST_FORCE_BUILD};
-    return build_meshes(ms, segs, req, st, retired);
+    const int r = build_meshes(ms, segs, req, st, retired);
+    if (r != LCX_OK) return r;  // the old tree keeps its keyframe balls
+    if (m->curve_keys) retired.blocks.push_back(std::move(m->curve_keys));
+    m->curve_keys = std::move(kblock);
+    return LCX_OK;
 }
 
 int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *cmd, void *stream) {

@@ -22,7 +22,8 @@ struct SegInput {
     uint32_t item_count;
     uint32_t kind;               // low byte: kSegTriangles (vbase, tbase) or kSegAabbs (vbase: 24-byte AABBs)
                                  // or kSegCurves (vbase: Bezier points, cone offsets and metas of vcount
-                                 // segments; tbase: u32 segment per cone; see build.cu);
+                                 // segments; tbase: u32 segment per cone; bits 16+: keyframes; vstride:
+                                 // keyframed cones' balls; see build.cu);
                                  // bits 8+: triangles: vertex-motion keyframes (vbase holds them back to back,
                                  // vcount each); curves: the basis (kCurve*)
     BlasDesc *desc;              // BLAS descriptor the emit fills in (null for a TLAS)
@@ -119,9 +120,9 @@ cudaError_t exclusive_sum(void *tmp, size_t *tmp_bytes, const uint32_t *in, uint
                           cudaStream_t st);
 // Curve builds (see build.cu): per-segment Bezier form, cone counts and metas,
 // then the segment of every cone once the counts are scanned.
-cudaError_t curve_prepare(const unsigned char *cps, uint64_t stride, uint32_t cp_count, const uint32_t *seg,
-                          uint32_t nseg, uint32_t basis, float4 *bez, uint32_t *count, uint32_t *meta, uint32_t *err,
-                          cudaStream_t st);
+cudaError_t curve_prepare(const unsigned char *cps, uint64_t stride, uint32_t cp_count, uint32_t keys,
+                          const uint32_t *seg, uint32_t nseg, uint32_t basis, float4 *bez, uint32_t *count,
+                          uint32_t *meta, uint32_t *err, cudaStream_t st);
 cudaError_t curve_fill(const uint32_t *off, const uint32_t *count, uint32_t nseg, uint32_t *cone_seg,
                        cudaStream_t st);
 cudaError_t split_emit(const SegInput *tsegs, uint32_t nseg, uint32_t n, const uint32_t *refs, const uint32_t *ref_off,

@@ -226,13 +226,15 @@ struct Walker {
             const float4 *tp = reinterpret_cast<const float4 *>(blas_tris + Gt.x + k);
             float4 a = bvh_ld(tp), b = bvh_ld(tp + 1), c = bvh_ld(tp + 2);
             if constexpr (kExt >= 2) {
-                if (__float_as_uint(b.w) == kTriCurve) {  // a cone of a curve segment
+                const uint32_t marker = __float_as_uint(b.w);
+                if (marker == kTriCurve || marker == kTriCurveMotion) {  // a cone of a curve segment
                     if (kCount) c_tris++;
+                    float4 c0 = make_float4(a.x, a.y, a.z, c.x), c1 = make_float4(b.x, b.y, b.z, c.y);
+                    if (marker == kTriCurveMotion && !curve_motion_cone(a, b, c, time, c0, c1)) continue;
                     const uint32_t kn = __float_as_uint(c.z);
                     float t, u;
-                    if (curve_piece_entry(make_float3(ox, oy, oz), make_float3(rdx, rdy, rdz),
-                                          make_float4(a.x, a.y, a.z, c.x), make_float4(b.x, b.y, b.z, c.y),
-                                          kn & 0xffffu, kn >> 16, __float_as_uint(c.w), tmin, best_t, t, u)) {
+                    if (curve_piece_entry(make_float3(ox, oy, oz), make_float3(rdx, rdy, rdz), c0, c1, kn & 0xffffu,
+                                          kn >> 16, __float_as_uint(c.w), tmin, best_t, t, u)) {
                         if (kAny) {
                             occluded = true;
                             return true;

@@ -67,6 +67,11 @@ def load():
         lib.lcxo_curve_pieces.argtypes = [c_void_p, c_size_t]
         lib.lcxo_trace_curves.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, c_uint32, c_int,
                                           c_void_p, c_void_p, c_int]
+        lib.lcxo_curve_create_motion.restype = c_void_p
+        lib.lcxo_curve_create_motion.argtypes = [c_void_p, c_size_t, c_size_t, c_uint32, c_void_p, c_size_t, c_uint32,
+                                                 c_float, c_float, c_uint32]
+        lib.lcxo_trace_curves_t.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t,
+                                            c_uint32, c_int, c_void_p, c_void_p, c_int]
         lib.lcxo_intersect_triangle.restype = c_int
         lib.lcxo_intersect_triangle.argtypes = [c_void_p, c_void_p, c_float, c_float, c_void_p, c_void_p, c_void_p,
                                                 POINTER(c_float), POINTER(c_float), POINTER(c_float)]
@@ -216,12 +221,16 @@ class OracleScene:
 class OracleCurve:
     """One curve (lcxo_curve_create): control points (N, 4) float32, segment starts (uint32), basis 0..3."""
 
-    def __init__(self, control_points: np.ndarray, segments: np.ndarray, basis: int):
+    def __init__(self, control_points: np.ndarray, segments: np.ndarray, basis: int, keyframes: int = 1,
+                 time_start: float = 0.0, time_end: float = 1.0, vanish_start: bool = False, vanish_end: bool = False):
         self.lib = load()
         self.cps = np.ascontiguousarray(control_points, np.float32).reshape(-1, 4)
         self.segs = np.ascontiguousarray(segments, np.uint32).reshape(-1)
-        self.handle = self.lib.lcxo_curve_create(_ptr(self.cps), 4, self.cps.shape[0], _ptr(self.segs),
-                                                 self.segs.size, int(basis))
+        keys = max(int(keyframes), 1)
+        flags = (1 if vanish_start else 0) | (2 if vanish_end else 0)
+        self.handle = self.lib.lcxo_curve_create_motion(_ptr(self.cps), 4, self.cps.shape[0] // keys, keys,
+                                                        _ptr(self.segs), self.segs.size, int(basis), time_start,
+                                                        time_end, flags)
         if not self.handle:
             raise ValueError("a curve segment runs past the control points")
 
@@ -241,7 +250,7 @@ class OracleCurve:
 
 
 def trace_curves(instances: list, o2w: np.ndarray, masks, rays: np.ndarray, mask: int = 0xFF, any_hit: bool = False,
-                 threads: int = 0):
+                 threads: int = 0, times: np.ndarray | None = None):
     """Brute-force closest / any hit over the curve instances (entries of ``instances`` that are None are
     skipped: a mixed scene's mesh instances are traced with OracleScene and merged by the caller)."""
     from luisacompute_gb300.scenes import HIT_DTYPE
@@ -253,8 +262,12 @@ def trace_curves(instances: list, o2w: np.ndarray, masks, rays: np.ndarray, mask
     rays = np.ascontiguousarray(rays)
     hits = np.zeros(rays.shape[0], HIT_DTYPE)
     occ = np.zeros(rays.shape[0], np.uint8)
-    lib.lcxo_trace_curves(handles, _ptr(o2w), _ptr(masks), n_inst, _ptr(rays), rays.shape[0], mask, int(any_hit),
-                          _ptr(hits), _ptr(occ), threads)
+    tp = None
+    if times is not None:
+        times = np.ascontiguousarray(times, np.float32)
+        tp = _ptr(times)
+    lib.lcxo_trace_curves_t(handles, _ptr(o2w), _ptr(masks), n_inst, _ptr(rays), tp, rays.shape[0], mask,
+                            int(any_hit), _ptr(hits), _ptr(occ), threads)
     return occ if any_hit else hits
 
 

@@ -1173,65 +1173,110 @@ int lcxo_intersect_triangle(const float *o, const float *d, float tmin, float tm
 }
 
 
-void *lcxo_curve_create(const float *control_points, size_t cp_stride_floats, size_t cp_count,
-                        const uint32_t *segments, size_t seg_count, uint32_t basis) {
-    auto *segs = new std::vector<CurveSeg>(seg_count);
+
+
+// Curves: segs holds keys x nseg segments, keyframe-major.  The cone count of a
+// segment is the largest over its keyframes (the kernels' choice).
+struct CurveObj {
+    uint32_t keys = 1;
+    float t0 = 0.0f, t1 = 1.0f;
+    uint32_t mflags = 0;
+    size_t nseg = 0;
+    std::vector<CurveSeg> segs;
+};
+
+void *lcxo_curve_create_motion(const float *control_points, size_t cp_stride_floats, size_t cp_per_key, uint32_t keys,
+                               const uint32_t *segments, size_t seg_count, uint32_t basis, float t0, float t1,
+                               uint32_t flags) {
+    auto *cv = new CurveObj();
+    cv->keys = keys < 1 ? 1 : keys;
+    cv->t0 = t0;
+    cv->t1 = t1;
+    cv->mflags = flags;
+    cv->nseg = seg_count;
+    cv->segs.resize(size_t(cv->keys) * seg_count);
     const uint32_t need = basis == 0 ? 2u : 4u;
     for (size_t i = 0; i < seg_count; i++) {
-        CurveSeg &sg = (*segs)[i];
         const uint32_t first = segments[i];
-        if (first > cp_count || cp_count - first < need) {  // the product reports this as an error
-            delete segs;
+        if (first > cp_per_key || cp_per_key - first < need) {  // the product reports this as an error
+            delete cv;
             return nullptr;
         }
-        float q[4][4], p[4][4];
-        for (uint32_t k = 0; k < 4; k++)
-            for (int c = 0; c < 4; c++) q[k][c] = control_points[(first + std::min(k, need - 1)) * cp_stride_floats + c];
-        curve_to_bezier_f32(basis, q, p);
-        sg.pieces = curve_pieces_f32(basis, p);
-        sg.flags = 0;
+        uint32_t pieces = 1, flags_i = 0;
         if (basis != 0) {
             const uint32_t step = basis == 3 ? 3u : 1u;
-            if (!(i > 0 && segments[i - 1] + step == first)) sg.flags |= 1u;
-            if (!(i + 1 < seg_count && segments[i + 1] == first + step)) sg.flags |= 2u;
+            if (!(i > 0 && segments[i - 1] + step == first)) flags_i |= 1u;
+            if (!(i + 1 < seg_count && segments[i + 1] == first + step)) flags_i |= 2u;
         }
-        double pad = 0.0;
-        for (int k = 0; k < 4; k++) {
-            for (int c = 0; c < 4; c++) sg.p[k][c] = p[k][c];
-            pad = std::max(pad, sg.p[k][3]);
+        for (uint32_t key = 0; key < cv->keys; key++) {
+            CurveSeg &sg = cv->segs[size_t(key) * seg_count + i];
+            float q[4][4], p[4][4];
+            for (uint32_t k = 0; k < 4; k++)
+                for (int c = 0; c < 4; c++)
+                    q[k][c] = control_points[(size_t(key) * cp_per_key + first + std::min(k, need - 1)) *
+                                                 cp_stride_floats + c];
+            curve_to_bezier_f32(basis, q, p);
+            pieces = std::max(pieces, curve_pieces_f32(basis, p));
+            sg.flags = flags_i;
+            double pad = 0.0;
+            for (int k = 0; k < 4; k++) {
+                for (int c = 0; c < 4; c++) sg.p[k][c] = p[k][c];
+                pad = std::max(pad, sg.p[k][3]);
+            }
+            for (int c = 0; c < 3; c++) {
+                sg.lo[c] = std::min(std::min(sg.p[0][c], sg.p[1][c]), std::min(sg.p[2][c], sg.p[3][c])) - pad;
+                sg.hi[c] = std::max(std::max(sg.p[0][c], sg.p[1][c]), std::max(sg.p[2][c], sg.p[3][c])) + pad;
+            }
         }
-        for (int c = 0; c < 3; c++) {
-            sg.lo[c] = std::min(std::min(sg.p[0][c], sg.p[1][c]), std::min(sg.p[2][c], sg.p[3][c])) - pad;
-            sg.hi[c] = std::max(std::max(sg.p[0][c], sg.p[1][c]), std::max(sg.p[2][c], sg.p[3][c])) + pad;
-        }
+        for (uint32_t key = 0; key < cv->keys; key++) cv->segs[size_t(key) * seg_count + i].pieces = pieces;
     }
-    return segs;
+    return cv;
 }
 
-void lcxo_curve_destroy(void *curve) { delete static_cast<std::vector<CurveSeg> *>(curve); }
+void *lcxo_curve_create(const float *control_points, size_t cp_stride_floats, size_t cp_count,
+                        const uint32_t *segments, size_t seg_count, uint32_t basis) {
+    return lcxo_curve_create_motion(control_points, cp_stride_floats, cp_count, 1, segments, seg_count, basis, 0.0f,
+                                    1.0f, 0u);
+}
+
+void lcxo_curve_destroy(void *curve) { delete static_cast<CurveObj *>(curve); }
 
 uint32_t lcxo_curve_pieces(const void *curve, size_t segment) {
-    return (*static_cast<const std::vector<CurveSeg> *>(curve))[segment].pieces;
+    return static_cast<const CurveObj *>(curve)->segs[segment].pieces;
 }
 
-void lcxo_trace_curves(void *const *inst_curve, const float *o2w, const uint32_t *inst_mask, size_t instance_count,
-                       const LcxoRay *rays, size_t n, uint32_t mask, int any, LcxoHit *hits, uint8_t *occluded,
-                       int threads) {
+void lcxo_trace_curves_t(void *const *inst_curve, const float *o2w, const uint32_t *inst_mask, size_t instance_count,
+                         const LcxoRay *rays, const float *times, size_t n, uint32_t mask, int any, LcxoHit *hits,
+                         uint8_t *occluded, int threads) {
     std::vector<float> w2o(12 * instance_count);
     for (size_t i = 0; i < instance_count; i++) affine_inverse_f32(&o2w[12 * i], &w2o[12 * i]);
     parallel_rays(n, threads, [&](size_t r) {
         const LcxoRay &ray = rays[r];
+        const float time = times != nullptr ? times[r] : 0.0f;
         LcxoHit best{kInvalid, kInvalid, 0.0f, 0.0f, ray.tmax, 0};
         double best_t = ray.tmax;
         bool occ = false;
         for (uint32_t id = 0; id < instance_count && !occ; id++) {
-            const auto *segs = static_cast<const std::vector<CurveSeg> *>(inst_curve[id]);
-            if (!segs || (inst_mask[id] & mask) == 0u) continue;
+            const auto *cv = static_cast<const CurveObj *>(inst_curve[id]);
+            if (!cv || (inst_mask[id] & mask) == 0u) continue;
+            uint32_t key = 0;
+            float f = 0.0f;
+            if (cv->keys > 1 && !motion_segment_f32(cv->t0, cv->t1, cv->keys, cv->mflags, time, key, f)) continue;
             float oo[3], od[3];
             transform_ray_f32(&w2o[12 * size_t(id)], ray.o, ray.d, oo, od);
             const double o[3] = {oo[0], oo[1], oo[2]}, d[3] = {od[0], od[1], od[2]};
-            for (uint32_t k = 0; k < segs->size() && !occ; k++) {
-                const CurveSeg &sg = (*segs)[k];
+            for (uint32_t k = 0; k < cv->nseg && !occ; k++) {
+                const CurveSeg &s0 = cv->segs[size_t(key) * cv->nseg + k];
+                CurveSeg sg = s0;
+                if (cv->keys > 1) {  // the Bezier points at the ray's time; the box covers both keyframes
+                    const CurveSeg &s1 = cv->segs[size_t(key + 1) * cv->nseg + k];
+                    for (int j = 0; j < 4; j++)
+                        for (int c = 0; c < 4; c++) sg.p[j][c] = s0.p[j][c] + double(f) * (s1.p[j][c] - s0.p[j][c]);
+                    for (int c = 0; c < 3; c++) {
+                        sg.lo[c] = std::min(s0.lo[c], s1.lo[c]);
+                        sg.hi[c] = std::max(s0.hi[c], s1.hi[c]);
+                    }
+                }
                 double tn = ray.tmin, tf = best_t;  // slab test against the segment's box
                 bool in = true;
                 for (int c = 0; c < 3 && in; c++) {
@@ -1264,6 +1309,13 @@ void lcxo_trace_curves(void *const *inst_curve, const float *o2w, const uint32_t
         else
             hits[r] = best;
     });
+}
+
+void lcxo_trace_curves(void *const *inst_curve, const float *o2w, const uint32_t *inst_mask, size_t instance_count,
+                       const LcxoRay *rays, size_t n, uint32_t mask, int any, LcxoHit *hits, uint8_t *occluded,
+                       int threads) {
+    lcxo_trace_curves_t(inst_curve, o2w, inst_mask, instance_count, rays, nullptr, n, mask, any, hits, occluded,
+                        threads);
 }
 
 }  // extern "C"

@@ -145,6 +145,15 @@ uint32_t lcxo_curve_pieces(const void *curve, size_t segment);
 void lcxo_trace_curves(void *const *inst_curve, const float *o2w, const uint32_t *inst_mask, size_t instance_count,
                        const LcxoRay *rays, size_t n, uint32_t mask, int any, LcxoHit *hits, uint8_t *occluded,
                        int threads);
+/* Keyframed control points: `keys` copies of cp_per_key points back to back
+ * over [t0, t1] (flags bit 0 / 1: vanish before / after); the Bezier points
+ * interpolate linearly at each ray's time (times: one per ray, null = 0). */
+void *lcxo_curve_create_motion(const float *control_points, size_t cp_stride_floats, size_t cp_per_key, uint32_t keys,
+                               const uint32_t *segments, size_t seg_count, uint32_t basis, float t0, float t1,
+                               uint32_t flags);
+void lcxo_trace_curves_t(void *const *inst_curve, const float *o2w, const uint32_t *inst_mask, size_t instance_count,
+                         const LcxoRay *rays, const float *times, size_t n, uint32_t mask, int any, LcxoHit *hits,
+                         uint8_t *occluded, int threads);
 int lcxo_intersect_triangle(const float *o, const float *d, float tmin, float tmax,
                             const float *v0, const float *v1, const float *v2, float *t,
                             float *u, float *v);

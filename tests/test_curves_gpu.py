@@ -228,3 +228,51 @@ def test_curve_motion_instance(lcx, oracle_mod):
     got = hits_to_numpy(acc.trace_closest_motion(rays_to_device(rays), times))
     want = oracle_mod.trace_curves([oracle_mod.OracleCurve(cps, segs, basis)], m.reshape(1, 12), 0xFF, rays)
     _check(got, want, min_hits=0.1)
+
+
+def test_keyframed_curves_match_oracle(lcx, oracle_mod):
+    """Curves with keyframed control points (three keyframes, each a perturbed copy of the strands):
+    traced at times inside, before and after the range and NaN, with and without vanishing, under an
+    instance transform, against the oracle's interpolation of the Bezier points."""
+    import torch
+    from luisacompute_gb300.accel import Accel, Curve, hits_to_numpy, rays_to_device
+    rng = np.random.default_rng(741)
+    basis, n_curves, n_cp, keys = 2, 48, 9, 3
+    base = S.hair_curves(n_curves, n_cp, rng)
+    frames = [base]
+    for _ in range(keys - 1):  # each later keyframe moves every control point a little (radii kept)
+        jitter = np.zeros_like(base)
+        jitter[:, :3] = rng.normal(0.0, 0.05, (base.shape[0], 3))
+        frames.append(base + jitter)
+    cps = np.concatenate(frames).astype(np.float32)
+    segs = S.curve_segments(n_curves, n_cp, basis)
+    d_cps = torch.from_numpy(cps).cuda()
+    d_segs = torch.from_numpy(segs.astype(np.int32)).cuda()
+    aff = S.affine_rows(S.random_rotations(1, rng), np.array([1.1]), np.array([[0.2, -0.1, 0.3]]))[0]
+    rays = _aimed_rays(rng, base[:, :3] @ aff.reshape(3, 4)[:, :3].T + aff.reshape(3, 4)[:, 3], 60_000,
+                       aff.reshape(3, 4)[:, 3])
+    times = rng.uniform(-0.3, 1.3, rays.shape[0]).astype(np.float32)
+    times[:16] = np.nan
+    d_rays, d_times = rays_to_device(rays), torch.from_numpy(times).cuda()
+    for vanish in (False, True):
+        cv = Curve(basis, d_cps, d_segs, motion_keyframes=keys, time_start=0.0, time_end=1.0,
+                   vanish_start=vanish, vanish_end=vanish).build()
+        acc = Accel()
+        acc.emplace_back(cv, aff.reshape(3, 4))
+        acc.build()
+        oc = oracle_mod.OracleCurve(cps, segs, basis, keyframes=keys, vanish_start=vanish, vanish_end=vanish)
+        want = oracle_mod.trace_curves([oc], aff.reshape(1, 12), 0xFF, rays, times=times)
+        got = hits_to_numpy(acc.trace_closest_motion(d_rays, d_times))
+        _check(got, want, min_hits=0.05)
+        occ = acc.trace_any_motion(d_rays, d_times).cpu().numpy()
+        want_any = oracle_mod.trace_curves([oc], aff.reshape(1, 12), 0xFF, rays, times=times, any_hit=True)
+        assert (occ != want_any).mean() <= 2e-3
+        outside = (times < 0.0) | (times > 1.0)
+        if vanish:
+            assert np.all(got["inst"][outside] == INV)
+        else:
+            assert np.any(got["inst"][outside] != INV)
+    # the control point count must be a whole number of keyframes
+    from luisacompute_gb300 import LcxError
+    with pytest.raises(LcxError):
+        Curve(basis, d_cps[:-1], d_segs, motion_keyframes=keys).build()

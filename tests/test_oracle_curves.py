@@ -95,3 +95,17 @@ def test_curve_segment_tables():
     assert list(S.curve_segments(1, 7, 3)) == [0, 3]
     cps = S.hair_curves(3, 6, np.random.default_rng(1))
     assert cps.shape == (18, 4) and cps.dtype == np.float32 and np.all(cps[:, 3] > 0)
+
+
+def test_keyframed_strand_moves_and_vanishes(oracle_mod):
+    """Two keyframes one unit apart in y: at time tau the strand's top lies at y = tau + r; with
+    vanish_end the strand is gone after the range, without it the last keyframe holds."""
+    cps = np.array([[0, 0, 0, 0.1], [1, 0, 0, 0.1], [0, 1, 0, 0.1], [1, 1, 0, 0.1]], np.float32)
+    times = np.array([0.0, 0.5, 1.5, -1.0], np.float32)
+    rays = _rays([[0.5, 3, 0]] * 4)
+    gone = oracle_mod.OracleCurve(cps, np.array([0]), 0, keyframes=2, vanish_end=True)
+    h = oracle_mod.trace_curves([gone], IDENT, 0xFF, rays, times=times)
+    assert list(h["inst"]) == [0, 0, INV, 0]
+    assert np.allclose(h["t"][[0, 1, 3]], [2.9, 2.4, 2.9], atol=1e-6)
+    held = oracle_mod.OracleCurve(cps, np.array([0]), 0, keyframes=2)
+    assert abs(oracle_mod.trace_curves([held], IDENT, 0xFF, rays, times=times)["t"][2] - 1.9) < 1e-6
