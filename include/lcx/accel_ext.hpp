@@ -154,6 +154,13 @@ public:
         check(lcx_curve_create(&o, &info.handle), "create_curve");
         return info;
     }
+    // AccelOption::motion with >= 2 keyframes: the control-point buffer holds the keyframes back to back
+    [[nodiscard]] ResourceCreationInfo create_curve(const AccelOption &option, const LcxMotionOption &motion) const {
+        const LcxAccelOption o = option.c();
+        ResourceCreationInfo info;
+        check(lcx_curve_create_motion(&o, &motion, &info.handle), "create_curve");
+        return info;
+    }
     void destroy_curve(uint64_t handle) const { check(lcx_curve_destroy(handle), "destroy_curve"); }
 
     // device_interface.h create_motion_instance: a mesh moved by matrix keyframes (row-major 3x4 each)
