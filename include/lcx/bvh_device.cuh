@@ -581,6 +581,20 @@ __device__ __forceinline__ float4 bezier_at(const float4 p[4], float u) {
     return f4_axpy(b3, p[3], f4_axpy(b2, p[2], f4_axpy(b1, p[1], q)));
 }
 
+// Reciprocal and square root from the MUFU approximations (about 1 ulp): the
+// curve test needs neither correctly rounded, only the same bits in every
+// kernel, which one fixed instruction gives.
+__device__ __forceinline__ float rcp_fast(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sqrt_fast(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 __device__ __forceinline__ float dot3_rn(float ax, float ay, float az, float bx, float by, float bz) {
     return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
 }
@@ -601,10 +615,11 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
     const float dd = dot3_rn(d.x, d.y, d.z, d.x, d.y, d.z);
     const float mx = __fmul_rn(0.5f, __fadd_rn(a.x, b.x)), my = __fmul_rn(0.5f, __fadd_rn(a.y, b.y)),
                 mz = __fmul_rn(0.5f, __fadd_rn(a.z, b.z));
-    const float tc = __fdiv_rn(dot3_rn(__fsub_rn(mx, o.x), __fsub_rn(my, o.y), __fsub_rn(mz, o.z), d.x, d.y, d.z), dd);
+    const float idd = rcp_fast(dd);
+    const float tc = __fmul_rn(dot3_rn(__fsub_rn(mx, o.x), __fsub_rn(my, o.y), __fsub_rn(mz, o.z), d.x, d.y, d.z), idd);
     const float3 os = make_float3(__fmaf_rn(tc, d.x, o.x), __fmaf_rn(tc, d.y, o.y), __fmaf_rn(tc, d.z, o.z));
     const float3 ba = make_float3(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y), __fsub_rn(b.z, a.z));
-    const float L = __fsqrt_rn(dot3_rn(ba.x, ba.y, ba.z, ba.x, ba.y, ba.z));
+    const float L = sqrt_fast(dot3_rn(ba.x, ba.y, ba.z, ba.x, ba.y, ba.z));
     const float dr = __fsub_rn(a.w, b.w);
     float best = kInf;
     int bp = -1;
@@ -615,7 +630,7 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
         const float cc = __fsub_rn(dot3_rn(ocx, ocy, ocz, ocx, ocy, ocz), __fmul_rn(c.w, c.w));
         const float disc = __fsub_rn(__fmul_rn(hb, hb), __fmul_rn(dd, cc));
         if (disc < 0.0f) return;
-        const float t = __fdiv_rn(__fsub_rn(-hb, __fsqrt_rn(disc)), dd);
+        const float t = __fmul_rn(__fsub_rn(-hb, sqrt_fast(disc)), idd);
         if (t < best) {
             best = t;
             bp = which;
@@ -629,10 +644,11 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
         ball(b, 2);
         // the truncated cone: s = axial coordinate from a, rho = distance from the axis;
         // its side is rho cos + s sin = ra for s in [ra sin, L + rb sin]
-        const float wx = __fdiv_rn(ba.x, L), wy = __fdiv_rn(ba.y, L), wz = __fdiv_rn(ba.z, L);
-        sn = __fdiv_rn(dr, L);
+        const float iL = rcp_fast(L);
+        const float wx = __fmul_rn(ba.x, iL), wy = __fmul_rn(ba.y, iL), wz = __fmul_rn(ba.z, iL);
+        sn = __fmul_rn(dr, iL);
         const float c2 = fmaxf(__fmul_rn(__fsub_rn(1.0f, sn), __fadd_rn(1.0f, sn)), 0.0f);
-        cs = __fsqrt_rn(c2);
+        cs = sqrt_fast(c2);
         const float q0x = __fsub_rn(os.x, a.x), q0y = __fsub_rn(os.y, a.y), q0z = __fsub_rn(os.z, a.z);
         const float s0 = dot3_rn(q0x, q0y, q0z, wx, wy, wz);
         const float sd = dot3_rn(d.x, d.y, d.z, wx, wy, wz);
@@ -642,7 +658,8 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
         const float s_lo = ras, s_hi = __fadd_rn(L, __fmul_rn(b.w, sn));
         float lo = -kInf, hi = kInf;
         if (sd != 0.0f) {
-            const float t1 = __fdiv_rn(__fsub_rn(s_lo, s0), sd), t2 = __fdiv_rn(__fsub_rn(s_hi, s0), sd);
+            const float isd = rcp_fast(sd);
+            const float t1 = __fmul_rn(__fsub_rn(s_lo, s0), isd), t2 = __fmul_rn(__fsub_rn(s_hi, s0), isd);
             lo = fminf(t1, t2);
             hi = fmaxf(t1, t2);
         } else if (!(s0 >= s_lo && s0 <= s_hi)) {
@@ -658,9 +675,9 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
             if (A != 0.0f) {
                 const float disc = __fsub_rn(__fmul_rn(hB, hB), __fmul_rn(A, C));
                 if (disc >= 0.0f) {
-                    const float sq = __fsqrt_rn(disc);
+                    const float sq = sqrt_fast(disc);
                     const float qv = -__fadd_rn(hB, copysignf(sq, hB));
-                    float r1 = __fdiv_rn(qv, A), r2 = (qv != 0.0f) ? __fdiv_rn(C, qv) : r1;
+                    float r1 = __fmul_rn(qv, rcp_fast(A)), r2 = (qv != 0.0f) ? __fmul_rn(C, rcp_fast(qv)) : r1;
                     if (r1 > r2) {
                         const float tt = r1;
                         r1 = r2;
@@ -678,7 +695,7 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
                     lo = kInf;
                 }
             } else if (hB != 0.0f) {
-                const float tr = __fdiv_rn(-C, __fmul_rn(2.0f, hB));
+                const float tr = __fmul_rn(-C, rcp_fast(__fmul_rn(2.0f, hB)));
                 if (hB > 0.0f)
                     hi = fminf(hi, tr);
                 else
@@ -706,9 +723,10 @@ __device__ __forceinline__ bool round_cone_entry(float3 o, float3 d, float4 a, f
     else {
         const float xx = __fsub_rn(__fmaf_rn(best, d.x, os.x), a.x), xy = __fsub_rn(__fmaf_rn(best, d.y, os.y), a.y),
                     xz = __fsub_rn(__fmaf_rn(best, d.z, os.z), a.z);
-        const float s = __fdiv_rn(dot3_rn(xx, xy, xz, ba.x, ba.y, ba.z), L);
-        const float rho = __fsqrt_rn(fmaxf(__fsub_rn(dot3_rn(xx, xy, xz, xx, xy, xz), __fmul_rn(s, s)), 0.0f));
-        u = fminf(fmaxf(__fdiv_rn(__fsub_rn(s, __fdiv_rn(__fmul_rn(rho, sn), cs)), L), 0.0f), 1.0f);
+        const float iL = rcp_fast(L);
+        const float s = __fmul_rn(dot3_rn(xx, xy, xz, ba.x, ba.y, ba.z), iL);
+        const float rho = sqrt_fast(fmaxf(__fsub_rn(dot3_rn(xx, xy, xz, xx, xy, xz), __fmul_rn(s, s)), 0.0f));
+        u = fminf(fmaxf(__fmul_rn(__fsub_rn(s, __fmul_rn(__fmul_rn(rho, sn), rcp_fast(cs))), iL), 0.0f), 1.0f);
     }
     t_out = t;
     u_out = u;

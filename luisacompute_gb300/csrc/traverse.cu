@@ -39,10 +39,12 @@ constexpr int kTraceBlock = 128;
 #ifndef LCX_TRACE_MIN_BLOCKS_F
 #define LCX_TRACE_MIN_BLOCKS_F 7
 #endif
-// The extended kernels (motion, curves) carry the curve test and the motion
-// interpolation: a larger register budget keeps them from spilling.
+// The curve kernels carry the curve test and the motion interpolation: 5 blocks
+// per SM (96 registers) keeps the quantised-node ones from spilling; measured
+// on the hair workload (Catmull-Rom, camera rays): 5 blocks 0.902, 6 blocks
+// (8 bytes spilled) 0.911, 7 blocks 0.893 Grays/s; 4 blocks were 11 % slower.
 #ifndef LCX_TRACE_MIN_BLOCKS_EXT
-#define LCX_TRACE_MIN_BLOCKS_EXT 4
+#define LCX_TRACE_MIN_BLOCKS_EXT 5
 #endif
 // Stack entries kept in shared memory per thread (the rest of the kStackSize
 // entries go to local memory): a launch-time choice among 8, 16 (default) and
