@@ -72,12 +72,17 @@ struct CommittedHit {
     float t;               // t_max of the ray for a miss
 };
 
-// One ray against `view`, triangles and procedural primitives.  `mask`:
+// One ray against `view`, triangles, curves and procedural primitives.  `mask`:
 // instances with (mask & instance mask) == 0 are skipped.  Returns the closest
-// committed hit; a miss is {~0u, ~0u, (0,0), kHitMiss, t_max}.
-template <class OnCandidate, class OnProcedural>
-__device__ CommittedHit ray_query(const LcxAccelView &view, const LcxRay &ray, uint32_t mask,
-                                  OnCandidate &&on_candidate, OnProcedural &&on_procedural) {
+// committed hit; a miss is {~0u, ~0u, (0,0), kHitMiss, t_max}.  kMotion: the
+// ray has a time (the reference's traverse_motion, include/luisa/dsl/rtx/accel.h:49-50):
+// motion instances move, keyframed vertices and control points interpolate, with
+// the trace kernels' motion arithmetic.  Without it, motion instances and
+// keyframed meshes and curves are passed over (view.motion says whether the
+// accel has any).
+template <bool kMotion, class OnCandidate, class OnProcedural>
+__device__ CommittedHit ray_query_core(const LcxAccelView &view, const LcxRay &ray, float time, uint32_t mask,
+                                       OnCandidate &&on_candidate, OnProcedural &&on_procedural) {
     const Node8Q *tlas = static_cast<const Node8Q *>(view.tlas_nodes);
     const InstRec *insts = static_cast<const InstRec *>(view.instances);
     const float wox = ray.origin[0], woy = ray.origin[1], woz = ray.origin[2];
@@ -159,17 +164,25 @@ __device__ CommittedHit ray_query(const LcxAccelView &view, const LcxRay &ray, u
                 const uint32_t k = __ffs(Gt.y) - 1u;
                 Gt.y &= Gt.y - 1u;
                 const float4 *tp = reinterpret_cast<const float4 *>(tris + Gt.x + k);
-                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
                 float t, u, v;
-                if (__float_as_uint(b.w) == kTriCurve) {  // a cone of a curve segment: the trace kernels' test
+                const uint32_t marker = __float_as_uint(b.w);
+                if (marker == kTriCurve || marker == kTriCurveMotion) {  // a cone of a curve: the trace kernels' test
+                    float4 c0 = make_float4(a.x, a.y, a.z, c.x), c1 = make_float4(b.x, b.y, b.z, c.y);
+                    if (marker == kTriCurveMotion && (!kMotion || !curve_motion_cone(a, b, c, time, c0, c1))) continue;
                     const uint32_t kn = __float_as_uint(c.z);
-                    if (!curve_piece_entry(make_float3(ox, oy, oz), make_float3(odx, ody, odz),
-                                           make_float4(a.x, a.y, a.z, c.x), make_float4(b.x, b.y, b.z, c.y),
-                                           kn & 0xffffu, kn >> 16, __float_as_uint(c.w), tmin, best_t, t, u))
+                    if (!curve_piece_entry(make_float3(ox, oy, oz), make_float3(odx, ody, odz), c0, c1, kn & 0xffffu,
+                                           kn >> 16, __float_as_uint(c.w), tmin, best_t, t, u))
                         continue;
                     v = -1.0f;
-                } else if (!wt_intersect(wt, tmin, best_t, a, b, c, t, u, v)) {
-                    continue;
+                } else {
+                    if (marker == kTriMotion) {  // keyframed vertices: the triangle at the ray's time
+                        if (!kMotion) continue;
+                        const MeshMotion *mm = reinterpret_cast<const MeshMotion *>(
+                            (unsigned long long)__float_as_uint(c.x) | ((unsigned long long)__float_as_uint(c.y) << 32));
+                        if (!motion_triangle(*mm, __float_as_uint(a.w), time, a, b, c)) continue;
+                    }
+                    if (!wt_intersect(wt, tmin, best_t, a, b, c, t, u, v)) continue;
                 }
                 const uint32_t prim = __float_as_uint(a.w);
                 const int act = on_candidate(TriangleCandidate{cur_inst, prim, u, v, t});
@@ -192,15 +205,25 @@ __device__ CommittedHit ray_query(const LcxAccelView &view, const LcxRay &ray, u
                 const uint4 *ip = reinterpret_cast<const uint4 *>(insts + Gt.x + k);
                 const uint4 m4 = __ldg(ip + 4);  // fnodes (x,y), inst id (z), mask (w)
                 const bool proc = (m4.w & kInstProcedural) != 0u;
-                const bool shifted = (m4.w & (kInstProcedural | kInstCurve)) != 0u;  // mask in bits 8..15
+                // mask in bits 8..15
+                const bool shifted = (m4.w & (kInstProcedural | kInstCurve | kInstMotion)) != 0u;
+                const bool moving = !proc && (m4.w & kInstMotion) != 0u;
                 if ((((shifted ? m4.w >> 8 : m4.w) & 0xffu) & mask) == 0u) continue;
+                if (moving && !kMotion) continue;
                 const float4 r0 = __ldg(reinterpret_cast<const float4 *>(ip));
                 const float4 r1 = __ldg(reinterpret_cast<const float4 *>(ip + 1));
                 const float4 r2 = __ldg(reinterpret_cast<const float4 *>(ip + 2));
+                float w[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
+                if (kMotion && moving) {  // the matrix at the ray's time, inverted as a static one is
+                    const MotionDesc *md = reinterpret_cast<const MotionDesc *>(
+                        (unsigned long long)__float_as_uint(r0.x) | ((unsigned long long)__float_as_uint(r0.y) << 32));
+                    float m[12];
+                    if (!motion_matrix(*md, time, m)) continue;  // vanished at this time
+                    affine_inverse(m, w);
+                }
                 const uint4 pp = __ldg(ip + 3);  // qnodes (x,y), tris (z,w)
                 if (Gt.y && sp < kStackSize) stk[sp++] = Gt;
                 if (G.y && sp < kStackSize) stk[sp++] = G;
-                const float w[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
                 float dx, dy, dz;
                 transform_point(w, wox, woy, woz, ox, oy, oz);
                 transform_dir(w, wdx, wdy, wdz, dx, dy, dz);
@@ -247,14 +270,22 @@ __device__ CommittedHit ray_query(const LcxAccelView &view, const LcxRay &ray, u
     return h;
 }
 
-// Triangles only (procedural instances are passed over): the TriangleHit
-// record of the closest committed triangle.
-template <class OnCandidate>
-__device__ LcxTriangleHit ray_query(const LcxAccelView &view, const LcxRay &ray, uint32_t mask,
-                                    OnCandidate &&on_candidate) {
-    const CommittedHit c = ray_query(view, ray, mask, on_candidate, [](const ProceduralCandidate &) {
-        return ProceduralDecision{kSkip, 0.0f};
-    });
+template <class OnCandidate, class OnProcedural>
+__device__ CommittedHit ray_query(const LcxAccelView &view, const LcxRay &ray, uint32_t mask,
+                                  OnCandidate &&on_candidate, OnProcedural &&on_procedural) {
+    return ray_query_core<false>(view, ray, 0.0f, mask, on_candidate, on_procedural);
+}
+
+// With a time per ray (motion blur): moving instances and keyframed meshes and
+// curves at `time`, as lcx_trace_closest_motion traces them.
+template <class OnCandidate, class OnProcedural>
+__device__ CommittedHit ray_query_motion(const LcxAccelView &view, const LcxRay &ray, float time, uint32_t mask,
+                                         OnCandidate &&on_candidate, OnProcedural &&on_procedural) {
+    return ray_query_core<true>(view, ray, time, mask, on_candidate, on_procedural);
+}
+
+namespace detail {
+inline __device__ LcxTriangleHit surface_hit(const CommittedHit &c) {
     LcxTriangleHit h;
     h.inst = c.inst;
     h.prim = c.prim;
@@ -263,6 +294,24 @@ __device__ LcxTriangleHit ray_query(const LcxAccelView &view, const LcxRay &ray,
     h.committed_ray_t = c.t;
     h._pad = 0u;
     return h;
+}
+}  // namespace detail
+
+// Surfaces only (procedural instances are passed over): the TriangleHit
+// record of the closest committed triangle or curve.
+template <class OnCandidate>
+__device__ LcxTriangleHit ray_query(const LcxAccelView &view, const LcxRay &ray, uint32_t mask,
+                                    OnCandidate &&on_candidate) {
+    return detail::surface_hit(ray_query(view, ray, mask, on_candidate, [](const ProceduralCandidate &) {
+        return ProceduralDecision{kSkip, 0.0f};
+    }));
+}
+template <class OnCandidate>
+__device__ LcxTriangleHit ray_query_motion(const LcxAccelView &view, const LcxRay &ray, float time, uint32_t mask,
+                                           OnCandidate &&on_candidate) {
+    return detail::surface_hit(ray_query_motion(view, ray, time, mask, on_candidate, [](const ProceduralCandidate &) {
+        return ProceduralDecision{kSkip, 0.0f};
+    }));
 }
 
 }  // namespace lcx

@@ -395,7 +395,7 @@ typedef struct LcxAccelView {
     const void *tlas_nodes;  /* the TLAS's 8-bit quantised nodes (device) */
     const void *instances;   /* its leaf instance records (device) */
     uint32_t stack_need;     /* stack entries a query needs (<= 32) */
-    uint32_t _pad;
+    uint32_t motion;         /* 1: motion instances or keyframed meshes / curves (lcx::ray_query_motion) */
 } LcxAccelView;
 LCX_API int lcx_accel_device_view(uint64_t accel, LcxAccelView *out);
 

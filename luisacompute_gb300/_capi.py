@@ -82,7 +82,7 @@ class LcxMotionOption(ctypes.Structure):
 
 
 class LcxAccelView(ctypes.Structure):
-    _fields_ = [("tlas_nodes", c_void_p), ("instances", c_void_p), ("stack_need", c_uint32), ("_pad", c_uint32)]
+    _fields_ = [("tlas_nodes", c_void_p), ("instances", c_void_p), ("stack_need", c_uint32), ("motion", c_uint32)]
 
 
 class LcxPtStats(ctypes.Structure):

@@ -1658,8 +1658,6 @@ int lcx_accel_device_view(uint64_t accel, LcxAccelView *out) {
     if (!a->built) return fail(LCX_ERR_NOT_BUILT, "accel not built");
     if (!meshes_current(a.get()))
         return fail(LCX_ERR_NOT_BUILT, "a mesh of the accel was destroyed, rebuilt or refit; rebuild the accel");
-    if (a->has_motion)
-        return fail(LCX_ERR_INVALID_ARG, "lcx::ray_query does not trace motion instances");
     const uint32_t need = a->depth + a->max_blas_depth + 3;
     if (int(need) > kStackSize)
         return fail(LCX_ERR_DEPTH, "TLAS depth %u + BLAS depth %u exceeds the query stack (%d)", a->depth,
@@ -1667,7 +1665,7 @@ int lcx_accel_device_view(uint64_t accel, LcxAccelView *out) {
     out->tlas_nodes = a->qn;
     out->instances = a->recs;
     out->stack_need = need;
-    out->_pad = 0;
+    out->motion = a->has_motion ? 1u : 0u;
     return LCX_OK;
 }
 

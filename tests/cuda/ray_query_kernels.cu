@@ -57,7 +57,26 @@ __global__ void k_query(LcxAccelView view, const LcxRay *rays, uint32_t n, uint3
         hits[i] = h;
 }
 
+// commit every candidate of a motion query at times[i] (= lcx_trace_closest_motion)
+__global__ void k_query_motion(LcxAccelView view, const LcxRay *rays, const float *times, uint32_t n,
+                               LcxTriangleHit *hits) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    hits[i] = lcx::ray_query_motion(view, rays[i], times[i], 0xffu,
+                                    [](const lcx::TriangleCandidate &) { return int(lcx::kCommit); });
+}
+
 }  // namespace
+
+extern "C" __attribute__((visibility("default"))) int rq_run_motion(const LcxAccelView *view, const LcxRay *rays,
+                                                                    const float *times, uint32_t n,
+                                                                    LcxTriangleHit *hits) {
+    if (n == 0) return 0;
+    if (!view || !rays || !times || !hits) return -1;
+    k_query_motion<<<(n + 127) / 128, 128>>>(*view, rays, times, n, hits);
+    if (cudaGetLastError() != cudaSuccess) return -5;
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : -5;
+}
 
 extern "C" __attribute__((visibility("default"))) int rq_run(const LcxAccelView *view, const LcxRay *rays, uint32_t n,
                                                              uint32_t mode, uint32_t cut, LcxTriangleHit *hits,

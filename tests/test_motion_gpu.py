@@ -103,9 +103,9 @@ def test_motion_keyframe_rebuild_refit_and_errors(lcx, oracle_mod):
     want = oracle_mod.OracleScene(scene).trace_motion(rays, times, specs)
     got = hits_to_numpy(acc.trace_closest_motion(d_rays, d_times))
     assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
-    # what motion accels cannot do
+    # what motion accels cannot do (lcx::ray_query_motion takes their device view: test_ray_query_gpu.py)
     v = _capi.LcxAccelView()
-    assert lcx.lcx_accel_device_view(acc.handle, ctypes.byref(v)) == _capi.LCX_ERR_INVALID_ARG
+    assert lcx.lcx_accel_device_view(acc.handle, ctypes.byref(v)) == _capi.LCX_OK and v.motion == 1
     out = torch.empty((16, 6), dtype=torch.int32, device="cuda")
     job = (_capi.LcxTraceJob * 1)(_capi.LcxTraceJob(acc.handle, d_rays.data_ptr(), out.data_ptr(), 16, 0xFF, 0, 0))
     assert lcx.lcx_trace_jobs(job, 1, 1, None) == _capi.LCX_ERR_INVALID_ARG

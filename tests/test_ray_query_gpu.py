@@ -31,6 +31,9 @@ def rq(tmp_path_factory):
     lib.rq_run.restype = ctypes.c_int
     lib.rq_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                            ctypes.c_void_p, ctypes.c_void_p]
+    lib.rq_run_motion.restype = ctypes.c_int
+    lib.rq_run_motion.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                  ctypes.c_void_p]
     return lib
 
 
@@ -217,3 +220,53 @@ def test_curves_as_surface_candidates(lcx, rq):
     on_curve = got["inst"] == 0
     assert on_curve.sum() > 500 and (got["inst"] == 1).sum() > 500
     assert np.all(got["bary"][on_curve, 1] == -1.0)
+
+
+def test_ray_query_motion(lcx, rq):
+    """lcx::ray_query_motion (the reference's traverse_motion, include/luisa/dsl/rtx/accel.h:49-50):
+    committing every candidate at each ray's time gives lcx_trace_closest_motion's records bit for
+    bit, on an accel with static and moving instances, a keyframed mesh and a keyframed curve; the
+    plain query on the same view passes over everything that moves."""
+    import torch
+    from luisacompute_gb300.accel import (Accel, Curve, Mesh, MotionInstance, hits_to_numpy, mesh_from_data,
+                                          rays_to_device)
+    rng = np.random.default_rng(91)
+    sphere = S.icosphere(3, radius=0.4)
+    mesh = mesh_from_data(sphere).build()
+    keys = S.affine_rows(S.random_rotations(3, rng), np.array([1.0, 1.2, 0.8]),
+                         rng.uniform(-0.6, 0.6, (3, 3))).reshape(3, 3, 4)
+    mo = MotionInstance(mesh, keys, 0.0, 1.0, vanish_end=True)
+    v0 = sphere.vertices.copy()
+    v1 = v0.copy()
+    v1[:, 1] += 0.5
+    kv = torch.from_numpy(np.concatenate([v0, v1])).cuda()
+    kt = torch.from_numpy(sphere.triangles.astype(np.int32)).cuda()
+    kmesh = Mesh(kv, kt, motion_keyframes=2).build()
+    cps = S.hair_curves(32, 8, rng)
+    moved = cps.copy()
+    moved[:, 0] += 0.3
+    kc = Curve(2, torch.from_numpy(np.concatenate([cps, moved])).cuda(),
+               torch.from_numpy(S.curve_segments(32, 8, 2).astype(np.int32)).cuda(), motion_keyframes=2).build()
+    acc = Accel()
+    acc.emplace_back(mesh, np.array([[1, 0, 0, 0.8], [0, 1, 0, 0], [0, 0, 1, 0]], np.float32))
+    acc.emplace_back(mo)
+    acc.emplace_back(kmesh, np.array([[1, 0, 0, -0.8], [0, 1, 0, 0], [0, 0, 1, 0]], np.float32))
+    acc.emplace_back(kc)
+    acc.build()
+    view = _view(acc)
+    assert view.motion == 1
+    rays = S.sphere_rays(60_000, [-1.5] * 3, [1.5] * 3, seed=92)
+    times = rng.uniform(-0.2, 1.2, rays.shape[0]).astype(np.float32)
+    d, dt = rays_to_device(rays), torch.from_numpy(times).cuda()
+    n = rays.shape[0]
+    hits = torch.empty((n, 6), dtype=torch.int32, device="cuda")
+    assert rq.rq_run_motion(ctypes.byref(view), d.data_ptr(), dt.data_ptr(), n, hits.data_ptr()) == 0
+    got = hits_to_numpy(hits)
+    want = hits_to_numpy(acc.trace_closest_motion(d, dt))
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    for inst in range(4):
+        assert (got["inst"] == inst).sum() > 200, inst
+    # the plain query sees the static instance only
+    assert rq.rq_run(ctypes.byref(view), d.data_ptr(), n, 0, CUT, hits.data_ptr(), None) == 0
+    plain = hits_to_numpy(hits)
+    assert set(np.unique(plain["inst"])) <= {0, 0xFFFFFFFF} and (plain["inst"] == 0).sum() > 200
