@@ -78,4 +78,56 @@ __device__ __forceinline__ void set_instance_opacity(const InstanceBuffer &b, ui
     b.states[i].opaque = opaque ? 1u : 0u;
 }
 
+// Keyframes of a motion instance (the reference's instance_motion_matrix /
+// set_instance_motion_matrix / instance_motion_srt / set_instance_motion_srt,
+// include/luisa/dsl/rtx/accel.h:69-110).  Matrix keyframes are row-major 3x4
+// (12 floats); SRT keyframes the 16-float MotionInstanceTransformSRT records
+// (pivot, quaternion, scale, shear, translation).  The getters return false and
+// leave `out` alone, and the setters do nothing, when instance i is out of range,
+// is not a motion instance, holds the other kind of keyframe, or `key` is past
+// its keyframe count.  As with the other edits, the next lcx_accel_build of the
+// accel (a refit or a rebuild) takes the new keyframes into its bounds; traces
+// before it see new keyframes inside old bounds.  The keyframes belong to the
+// motion instance: every instance of it, in any accel, moves with them, and a
+// later lcx_motion_instance_build uploads the host's keyframes over them.
+__device__ __forceinline__ const MotionDesc *instance_motion(const InstanceBuffer &b, uint32_t i, bool srt,
+                                                             uint32_t key) {
+    if (i >= b.count) return nullptr;
+    const MotionDesc *md = b.states[i].motion;
+    if (md == nullptr || key >= md->count || ((md->flags & 4u) != 0u) != srt) return nullptr;
+    return md;
+}
+
+__device__ __forceinline__ bool instance_motion_matrix(const InstanceBuffer &b, uint32_t i, uint32_t key,
+                                                       float out[12]) {
+    const MotionDesc *md = instance_motion(b, i, false, key);
+    if (md == nullptr) return false;
+    for (int k = 0; k < 12; k++) out[k] = md->keys[12ull * key + k];
+    return true;
+}
+
+__device__ __forceinline__ void set_instance_motion_matrix(const InstanceBuffer &b, uint32_t i, uint32_t key,
+                                                           const float m[12]) {
+    const MotionDesc *md = instance_motion(b, i, false, key);
+    if (md == nullptr) return;
+    float *k0 = const_cast<float *>(md->keys) + 12ull * key;  // device memory of the motion instance
+    for (int k = 0; k < 12; k++) k0[k] = m[k];
+}
+
+__device__ __forceinline__ bool instance_motion_srt(const InstanceBuffer &b, uint32_t i, uint32_t key,
+                                                    float out[16]) {
+    const MotionDesc *md = instance_motion(b, i, true, key);
+    if (md == nullptr) return false;
+    for (int k = 0; k < 16; k++) out[k] = md->keys[16ull * key + k];
+    return true;
+}
+
+__device__ __forceinline__ void set_instance_motion_srt(const InstanceBuffer &b, uint32_t i, uint32_t key,
+                                                        const float v[16]) {
+    const MotionDesc *md = instance_motion(b, i, true, key);
+    if (md == nullptr) return;
+    float *k0 = const_cast<float *>(md->keys) + 16ull * key;
+    for (int k = 0; k < 16; k++) k0[k] = v[k];
+}
+
 }  // namespace lcx

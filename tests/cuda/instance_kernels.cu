@@ -40,6 +40,16 @@ __global__ void k_read(lcx::InstanceBuffer b, uint32_t n, float *affines, uint32
     opaque[i] = lcx::instance_opaque(b, i) ? 1u : 0u;
 }
 
+// Motion keyframe `key` of instances 0..n-1: read the old one into `old` (12 floats; untouched when
+// the instance has no such keyframe), write `m` + 12 i, and report which reads succeeded.
+__global__ void k_motion_key(lcx::InstanceBuffer b, uint32_t n, uint32_t key, const float *m, float *old,
+                             uint32_t *found) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    found[i] = lcx::instance_motion_matrix(b, i, key, old + 12ull * i) ? 1u : 0u;
+    lcx::set_instance_motion_matrix(b, i, key, m + 12ull * i);
+}
+
 lcx::InstanceBuffer as_buffer(const LcxInstanceBuffer *b) {
     return lcx::InstanceBuffer{static_cast<lcx::InstState *>(b->states), b->count, 0u};
 }
@@ -59,5 +69,14 @@ extern "C" __attribute__((visibility("default"))) int inst_read(const LcxInstanc
     if (!b || !affines || !masks || !user_ids || !opaque) return -1;
     if (n == 0) return 0;
     k_read<<<(n + 127) / 128, 128>>>(as_buffer(b), n, affines, masks, user_ids, opaque);
+    return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
+
+extern "C" __attribute__((visibility("default"))) int inst_motion_key(const LcxInstanceBuffer *b, uint32_t n,
+                                                                      uint32_t key, const float *m, float *old,
+                                                                      uint32_t *found) {
+    if (!b || !m || !old || !found) return -1;
+    if (n == 0) return 0;
+    k_motion_key<<<(n + 127) / 128, 128>>>(as_buffer(b), n, key, m, old, found);
     return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }

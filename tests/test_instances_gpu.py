@@ -30,6 +30,8 @@ def ik(tmp_path_factory):
     lib.inst_edit.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
     lib.inst_read.restype = ctypes.c_int
     lib.inst_read.argtypes = [ctypes.c_void_p, ctypes.c_uint32] + [ctypes.c_void_p] * 4
+    lib.inst_motion_key.restype = ctypes.c_int
+    lib.inst_motion_key.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32] + [ctypes.c_void_p] * 3
     return lib
 
 
@@ -134,3 +136,61 @@ def test_instance_edits_in_cuda_graph(lcx, oracle_mod, ik):
         want = oracle_mod.OracleScene(S.Scene(scene.meshes, scene.inst_mesh, aff, scene.inst_mask)).trace_closest(rays)
         assert np.array_equal(hits_to_numpy(out).view(np.uint8), want.view(np.uint8)), frame
     _capi.check(lcx.lcx_check_trace_errors(), "trace errors")
+
+
+def test_device_motion_keyframe_edits(lcx, oracle_mod, ik):
+    """instance_motion_matrix / set_instance_motion_matrix (include/luisa/dsl/rtx/accel.h:69-110) from
+    a user kernel: keyframe 1 of every matrix motion instance is read and replaced; static instances
+    and the SRT one report no matrix keyframe and keep theirs.  After a TLAS refit the traces match
+    the oracle with the new keyframes, bit for bit."""
+    import torch
+    from luisacompute_gb300.accel import (REQUEST_PREFER_UPDATE, Accel, AccelOption, MotionInstance, hits_to_numpy,
+                                          mesh_from_data, rays_to_device)
+    rng = np.random.default_rng(61)
+    data = S.icosphere(3, radius=0.5)
+    mesh = mesh_from_data(data).build()
+    n_static, n_motion = 2, 3
+    static_aff = S.affine_rows(S.random_rotations(n_static, rng), np.ones(n_static), rng.uniform(-1, 1, (n_static, 3)))
+    keys = [S.affine_rows(S.random_rotations(2, rng), np.ones(2), rng.uniform(-1, 1, (2, 3))) for _ in range(n_motion)]
+    motions = [MotionInstance(mesh, k.reshape(-1, 3, 4), 0.0, 1.0) for k in keys]
+    srt = np.zeros((2, 16), np.float32)
+    srt[:, 6] = 1.0      # identity quaternion (x, y, z, w at 3..6)
+    srt[:, 7:10] = 1.0   # unit scale
+    srt[1, 13:16] = [0.5, 0.0, 0.0]
+    srt_mo = MotionInstance(mesh, srt, 0.0, 1.0, srt=True)
+    acc = Accel(AccelOption(allow_update=True))
+    for i in range(n_static):
+        acc.emplace_back(mesh, static_aff[i].reshape(3, 4))
+    for mo in motions:
+        acc.emplace_back(mo)
+    acc.emplace_back(srt_mo)
+    acc.build()
+    n = n_static + n_motion + 1
+    new = S.affine_rows(S.random_rotations(n, rng), np.ones(n), rng.uniform(-1, 1, (n, 3)))
+    d_new = torch.from_numpy(new).cuda()
+    old = torch.full((n, 12), -7.0, dtype=torch.float32, device="cuda")
+    found = torch.zeros(n, dtype=torch.int32, device="cuda")
+    buf = _buffer(acc)
+    assert ik.inst_motion_key(ctypes.byref(buf), n, 1, d_new.data_ptr(), old.data_ptr(), found.data_ptr()) == 0
+    torch.cuda.synchronize()
+    assert list(found.cpu().numpy()) == [0, 0, 1, 1, 1, 0]
+    old_np = old.cpu().numpy()
+    for j in range(n_motion):
+        assert np.array_equal(old_np[n_static + j], keys[j][1])
+    assert np.all(old_np[[0, 1, n - 1]] == -7.0)
+    # a key past the count changes nothing
+    assert ik.inst_motion_key(ctypes.byref(buf), n, 2, d_new.data_ptr(), old.data_ptr(), found.data_ptr()) == 0
+    torch.cuda.synchronize()
+    assert not found.cpu().numpy().any()
+    acc.build(request=REQUEST_PREFER_UPDATE)
+    specs = [None] * n_static + [(np.stack([keys[j][0], new[n_static + j]]), 0.0, 1.0, 0) for j in range(n_motion)]
+    specs.append((srt, 0.0, 1.0, 4))
+    scene = S.Scene([data], np.zeros(n, np.int64),
+                    np.concatenate([static_aff, np.tile(np.eye(3, 4, dtype=np.float32).reshape(1, 12), (n - n_static, 1))]),
+                    np.full(n, 0xFF, np.uint32))
+    rays = S.sphere_rays(50_000, [-1.6] * 3, [1.6] * 3, seed=62)
+    times = rng.uniform(0.0, 1.0, rays.shape[0]).astype(np.float32)
+    want = oracle_mod.OracleScene(scene).trace_motion(rays, times, specs)
+    got = hits_to_numpy(acc.trace_closest_motion(rays_to_device(rays), torch.from_numpy(times).cuda()))
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    assert np.isin(np.arange(n_static, n_static + n_motion), got["inst"]).all()
