@@ -367,6 +367,24 @@ private:
     size_t seg_count_;
 };
 
+// include/luisa/runtime/rtx/motion_instance.h: a built mesh (or curve) moved by keyframes.
+class MotionInstance {
+public:
+    MotionInstance(const AccelGpuExt &ext, uint64_t child, const LcxMotionOption &option,
+                   const std::vector<std::array<float, 12>> &keyframes, void *stream = nullptr) {
+        handle_ = ext.create_motion_instance(child, option, keyframes, stream).handle;
+    }
+    MotionInstance(const MotionInstance &) = delete;
+    MotionInstance &operator=(const MotionInstance &) = delete;
+    ~MotionInstance() {
+        if (handle_) lcx_motion_instance_destroy(handle_);
+    }
+    [[nodiscard]] uint64_t handle() const noexcept { return handle_; }
+
+private:
+    uint64_t handle_{0};
+};
+
 class Accel {
 public:
     explicit Accel(const AccelGpuExt &ext, const AccelOption &option = {}) : ext_(&ext) {
@@ -390,6 +408,53 @@ public:
     void emplace_back(const Curve &curve, const std::array<float, 12> &affine, uint8_t visibility_mask = 0xffu,
                       bool opaque = true, uint32_t user_id = 0) {
         emplace_handle(curve.handle(), affine, visibility_mask, opaque, user_id);
+    }
+    // a motion instance moves by its own keyframes, so it takes no transform here
+    void emplace_back(const MotionInstance &instance, uint8_t visibility_mask = 0xffu, bool opaque = true,
+                      uint32_t user_id = 0) {
+        emplace_handle(instance.handle(), {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0}, visibility_mask, opaque, user_id);
+    }
+    // src/runtime/rtx/accel.cpp:114-131, 163-193: replace instance `index` (primitive, transform, mask,
+    // opacity, user id), or only its primitive
+    void set(uint32_t index, const Mesh &mesh, const std::array<float, 12> &affine, uint8_t visibility_mask = 0xffu,
+             bool opaque = true, uint32_t user_id = 0) {
+        set_handle(index, mesh.handle(), affine, visibility_mask, opaque, user_id);
+    }
+    void set(uint32_t index, const Curve &curve, const std::array<float, 12> &affine, uint8_t visibility_mask = 0xffu,
+             bool opaque = true, uint32_t user_id = 0) {
+        set_handle(index, curve.handle(), affine, visibility_mask, opaque, user_id);
+    }
+    void set(uint32_t index, const ProceduralPrimitive &prim, const std::array<float, 12> &affine,
+             uint8_t visibility_mask = 0xffu, bool opaque = true, uint32_t user_id = 0) {
+        set_handle(index, prim.handle(), affine, visibility_mask, opaque, user_id);
+    }
+    void set(uint32_t index, const MotionInstance &instance, uint8_t visibility_mask = 0xffu, bool opaque = true,
+             uint32_t user_id = 0) {
+        set_handle(index, instance.handle(), {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0}, visibility_mask, opaque, user_id);
+    }
+    // set_mesh / set_curve / set_procedural_primitive / set_motion_instance: the primitive only
+    void set_mesh(uint32_t index, const Mesh &mesh) { set_prim_handle(index, mesh.handle()); }
+    void set_curve(uint32_t index, const Curve &curve) { set_prim_handle(index, curve.handle()); }
+    void set_procedural_primitive(uint32_t index, const ProceduralPrimitive &prim) {
+        set_prim_handle(index, prim.handle());
+    }
+    void set_motion_instance(uint32_t index, const MotionInstance &instance) {
+        set_prim_handle(index, instance.handle());
+    }
+    void set_prim_handle(uint32_t index, uint64_t primitive) {
+        Modification &m = checked_mod(index);
+        m.primitive = primitive;
+        m.flags |= LCX_MOD_PRIMITIVE;
+    }
+    void set_handle(uint32_t index, uint64_t primitive, const std::array<float, 12> &affine, uint8_t visibility_mask,
+                    bool opaque, uint32_t user_id) {
+        Modification &m = checked_mod(index);
+        m.primitive = primitive;
+        std::memcpy(m.affine, affine.data(), sizeof(m.affine));
+        m.vis_mask = visibility_mask;
+        m.user_id = user_id;
+        m.flags = LCX_MOD_PRIMITIVE | LCX_MOD_TRANSFORM | LCX_MOD_VISIBILITY | LCX_MOD_USER_ID |
+                  (opaque ? LCX_MOD_OPAQUE_ON : LCX_MOD_OPAQUE_OFF);
     }
     void emplace_handle(uint64_t primitive, const std::array<float, 12> &affine, uint8_t visibility_mask,
                         bool opaque, uint32_t user_id) {

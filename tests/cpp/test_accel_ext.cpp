@@ -132,6 +132,35 @@ int main() {
         }
         cudaFree(dcp);
         cudaFree(dseg);
+        // set / set_mesh replace an instance; a motion instance moves the quad from z = 0 to z = -1
+        {
+            lcx::Accel swap{ext};
+            swap.emplace_back(ma, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0});
+            stream << swap.build();
+            swap.set(0, mb, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, -3});
+            stream << swap.build();
+            ext.trace_closest(swap.handle(), static_cast<lcx::Ray *>(dr), 4, 0xffu,
+                              static_cast<lcx::TriangleHit *>(dh), nullptr);
+            cudaMemcpy(hits.data(), dh, sizeof(lcx::TriangleHit) * 4, cudaMemcpyDeviceToHost);
+            REQUIRE(hits[0].inst == 0 && hits[0].committed_ray_t == 8.0f);
+            swap.set_mesh(0, ma);
+            stream << swap.build();
+            LcxMotionOption mo{2, 0.0f, 1.0f, 0, 0, LCX_MOTION_MATRIX, 0};
+            lcx::MotionInstance moving{ext, ma.handle(), mo,
+                                       {{1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0}, {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, -1}}};
+            lcx::Accel blur{ext};
+            blur.emplace_back(moving);
+            stream << blur.build();
+            std::vector<float> times{1.0f, 0.5f, 0.0f, 0.0f};
+            void *dtimes = nullptr;
+            REQUIRE(cudaMalloc(&dtimes, sizeof(float) * 4) == cudaSuccess);
+            cudaMemcpy(dtimes, times.data(), sizeof(float) * 4, cudaMemcpyHostToDevice);
+            ext.trace_closest_motion(blur.handle(), static_cast<lcx::Ray *>(dr), static_cast<const float *>(dtimes), 4,
+                                     0xffu, static_cast<lcx::TriangleHit *>(dh), nullptr);
+            cudaMemcpy(hits.data(), dh, sizeof(lcx::TriangleHit) * 4, cudaMemcpyDeviceToHost);
+            REQUIRE(hits[0].committed_ray_t == 6.0f && hits[1].committed_ray_t == 5.5f);
+            cudaFree(dtimes);
+        }
         // errors surface as exceptions with the library's status code
         bool threw = false;
         try {
