@@ -269,12 +269,30 @@ class Accel:
         self._mods.pop(self._count, None)
         self._meshes.pop(self._count, None)
 
+    def set(self, index: int, mesh, transform=None, visibility_mask: int = 0xFF, opaque: bool = True,
+            user_id: int = 0):
+        """Replace instance ``index`` (src/runtime/rtx/accel.cpp:114-131, 163-178): its primitive (a Mesh,
+        Curve, ProceduralPrimitive or MotionInstance), transform, mask, opacity and user id."""
+        self._check_index(index)
+        m = self._mod(index)
+        m["primitive"] = mesh.handle
+        m["affine"] = _as_affine(np.eye(4) if transform is None else transform)
+        m["vis_mask"] = visibility_mask & 0xFF
+        m["user_id"] = user_id
+        m["flags"] = (MOD_PRIMITIVE | MOD_TRANSFORM | MOD_VISIBILITY | MOD_USER_ID |
+                      (MOD_OPAQUE_ON if opaque else MOD_OPAQUE_OFF))
+        self._meshes[index] = mesh
+
     def set_mesh_on_update(self, index: int, mesh: Mesh):
+        """Replace only the primitive of instance ``index`` (the reference's set_mesh / set_curve /
+        set_procedural_primitive / set_motion_instance, accel.cpp:179-193)."""
         self._check_index(index)
         m = self._mod(index)
         m["primitive"] = mesh.handle
         m["flags"] |= MOD_PRIMITIVE
         self._meshes[index] = mesh
+
+    set_mesh = set_curve = set_procedural_primitive = set_motion_instance = set_mesh_on_update
 
     def set_transform_on_update(self, index: int, transform):
         self._check_index(index)
