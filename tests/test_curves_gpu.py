@@ -201,13 +201,16 @@ def test_curves_with_meshes_and_errors(lcx, oracle_mod):
     with pytest.raises(LcxError):
         bad_lin.build()
     assert np.array_equal(hits_to_numpy(acc.trace_closest(d_rays)).view(np.uint8), got2.view(np.uint8))
-    # Accel.set swaps instance 1 from the curve to the sphere mesh: its hits become triangle hits
-    acc.set(1, mesh)
+    # Accel.set swaps instance 1 from the curve to a moved copy of the sphere: its hits become triangle hits
+    away = ident.copy()
+    away[3] = 1.5
+    acc.set(1, mesh, away.reshape(3, 4))
     acc.build()
     got3 = hits_to_numpy(acc.trace_closest(d_rays))
     on1 = got3["inst"] == 1
     assert on1.sum() > 100 and np.all(got3["bary"][on1, 1] >= 0.0)
     acc.set_curve(1, cv)
+    acc.set_transform_on_update(1, ident.reshape(3, 4))
     acc.build()
     assert np.array_equal(hits_to_numpy(acc.trace_closest(d_rays)).view(np.uint8), got2.view(np.uint8))
 
