@@ -281,8 +281,9 @@ typedef struct LcxCurveBuildCommand {
  * lcx_mesh_stats counts them); hits are entries only (a ray starting inside a
  * segment does not hit it).  Accels holding curves trace with
  * the extended kernels (those of motion), through lcx_trace_* and the
- * *_motion / *_host / *_ex entry points; lcx::ray_query offers curve segments
- * as surface candidates with bary_v = -1; lcx_trace_jobs does not take them. */
+ * *_motion / *_host / *_ex entry points and lcx_trace_jobs (a group with a
+ * curve job runs the curve kernel); lcx::ray_query offers curve segments as
+ * surface candidates with bary_v = -1. */
 LCX_API int lcx_curve_create(const LcxAccelOption *option, uint64_t *out_handle);
 LCX_API int lcx_curve_destroy(uint64_t handle);
 /* Builds on `stream` (every request rebuilds: the reference's PREFER_UPDATE

@@ -1675,6 +1675,7 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
     if (node_layout > LCX_NODES_QUANT8) return fail(LCX_ERR_INVALID_ARG, "invalid node layout %u", node_layout);
     std::shared_lock<std::shared_mutex> life(g_life_mtx);  // until the kernels are enqueued
     std::vector<DevJob> groups[2];  // [0] closest, [1] any
+    bool curves[2] = {false, false};  // a job of the group traces curves: the curve kernel runs the group
     uint64_t totals[2] = {0, 0};
     uint32_t depth_need = 0;
     for (uint32_t i = 0; i < count; i++) {
@@ -1693,12 +1694,11 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
         if (a->has_motion)
             return fail(LCX_ERR_INVALID_ARG, "job %u: accels with motion instances are traced with "
                                              "lcx_trace_closest_motion / lcx_trace_any_motion", i);
-        if (a->has_curves)
-            return fail(LCX_ERR_INVALID_ARG, "job %u: accels with curves are traced with lcx_trace_*", i);
         const uint32_t need = a->depth + a->max_blas_depth + 3;
         if (int(need) > kStackSize) return fail(LCX_ERR_DEPTH, "job %u: BVH too deep for the traversal stack", i);
         depth_need = std::max(depth_need, need);
         const int g = j.any ? 1 : 0;
+        curves[g] = curves[g] || a->has_curves;
         DevJob d{};
         d.tlas_q = a->qn;
         d.tlas_f = a->fn;
@@ -1732,6 +1732,7 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
         p.postpone_sp = kStackSize - int(depth_need);
         p.jobs = d_jobs;
         p.job_count = uint32_t(groups[g].size());
+        p.motion = p.curves = curves[g];
         LCX_CUDA(cudaMemsetAsync(p.pool, 0, 4 * sizeof(uint32_t), st), "trace counter reset");
         LCX_CUDA(launch_trace(p, int(node_layout), g == 1, false, st), "multi-job trace launch");
     }

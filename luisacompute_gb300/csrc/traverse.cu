@@ -1005,6 +1005,13 @@ cudaError_t launch_mode(const TraceParams &p, int layout, bool any, bool countin
 // The extended kernels (kExt 1: motion; 2: motion and curves), loop mode 0 with per-ray times.
 template <int E>
 cudaError_t launch_ext(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
+    if (E == 2 && p.jobs != nullptr) {  // multi-job launches with curves (time 0: jobs carry no times)
+        if (layout == LCX_NODES_QUANT8)
+            return any ? launch_one<LCX_NODES_QUANT8, true, false, 0, true, kDefaultShortStack, E>(p, st)
+                       : launch_one<LCX_NODES_QUANT8, false, false, 0, true, kDefaultShortStack, E>(p, st);
+        return any ? launch_one<LCX_NODES_FP32, true, false, 0, true, kDefaultShortStack, E>(p, st)
+                   : launch_one<LCX_NODES_FP32, false, false, 0, true, kDefaultShortStack, E>(p, st);
+    }
     if (layout == LCX_NODES_QUANT8) {
         if (counting) return launch_one<LCX_NODES_QUANT8, false, true, 0, false, kDefaultShortStack, E>(p, st);
         return any ? launch_one<LCX_NODES_QUANT8, true, false, 0, false, kDefaultShortStack, E>(p, st)

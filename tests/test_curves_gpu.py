@@ -173,12 +173,6 @@ def test_curves_with_meshes_and_errors(lcx, oracle_mod):
     assert (got["inst"] == 0).sum() > 1000 and (got["inst"] >= 1).sum() > 1000
     tri = got["inst"] == 0
     assert np.all(got["bary"][tri, 1] >= 0.0)  # triangle hits keep their barycentrics
-    # the multi-job path does not take curve accels
-    from luisacompute_gb300._capi import LcxTraceJob, check
-    job_out = torch.empty((rays.shape[0], 6), dtype=torch.int32, device="cuda")
-    job = LcxTraceJob(acc.handle, d_rays.data_ptr(), job_out.data_ptr(), rays.shape[0], 0xFF, 0, 0)
-    with pytest.raises(LcxError):
-        check(acc.lib.lcx_trace_jobs(ctypes.byref(job), 1, 1, None), "lcx_trace_jobs")
     # a rebuild with moved control points: the accel must be rebuilt, then it sees them
     d_cps[:, 0] += 0.25
     cv.build()
@@ -288,3 +282,38 @@ def test_keyframed_curves_match_oracle(lcx, oracle_mod):
     from luisacompute_gb300 import LcxError
     with pytest.raises(LcxError):
         Curve(basis, d_cps[:-1], d_segs, motion_keyframes=keys).build()
+
+
+def test_curves_in_multi_job_launches(lcx):
+    """lcx_trace_jobs with a curve accel among its jobs: the group runs the curve kernel, and every
+    job's records equal its own lcx_trace_closest / lcx_trace_any call, bit for bit."""
+    import ctypes
+    import torch
+    from luisacompute_gb300 import _capi
+    from luisacompute_gb300.accel import Accel, Curve, hits_to_numpy, mesh_from_data, rays_to_device
+    rng = np.random.default_rng(751)
+    cps = S.hair_curves(64, 9, rng)
+    cv = Curve(1, torch.from_numpy(cps).cuda(),
+               torch.from_numpy(S.curve_segments(64, 9, 1).astype(np.int32)).cuda()).build()
+    curves = Accel()
+    curves.emplace_back(cv)
+    curves.build()
+    mesh = mesh_from_data(S.icosphere(4, radius=0.9)).build()
+    tris = Accel()
+    tris.emplace_back(mesh)
+    tris.build()
+    rays = [rays_to_device(_aimed_rays(rng, cps[:, :3], 40_000, np.zeros(3))) for _ in range(2)]
+    outs = [torch.empty((40_000, 6), dtype=torch.int32, device="cuda") for _ in range(2)]
+    occ = torch.empty(40_000, dtype=torch.uint8, device="cuda")
+    jobs = (_capi.LcxTraceJob * 3)(
+        _capi.LcxTraceJob(curves.handle, rays[0].data_ptr(), outs[0].data_ptr(), 40_000, 0xFF, 0, 0),
+        _capi.LcxTraceJob(tris.handle, rays[1].data_ptr(), outs[1].data_ptr(), 40_000, 0xFF, 0, 0),
+        _capi.LcxTraceJob(curves.handle, rays[1].data_ptr(), occ.data_ptr(), 40_000, 0xFF, 1, 0))
+    for layout in (0, 1):
+        _capi.check(_capi.load().lcx_trace_jobs(jobs, 3, layout, None), "lcx_trace_jobs")
+        torch.cuda.synchronize()
+        for k, acc in enumerate((curves, tris)):
+            want = hits_to_numpy(acc.trace_closest(rays[k], layout=layout))
+            assert np.array_equal(hits_to_numpy(outs[k]).view(np.uint8), want.view(np.uint8)), (layout, k)
+        assert torch.equal(occ, curves.trace_any(rays[1], layout=layout))
+    assert (hits_to_numpy(outs[0])["inst"] == 0).mean() > 0.1
