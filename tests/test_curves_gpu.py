@@ -317,3 +317,29 @@ def test_curves_in_multi_job_launches(lcx):
             assert np.array_equal(hits_to_numpy(outs[k]).view(np.uint8), want.view(np.uint8)), (layout, k)
         assert torch.equal(occ, curves.trace_any(rays[1], layout=layout))
     assert (hits_to_numpy(outs[0])["inst"] == 0).mean() > 0.1
+
+
+def test_curve_edge_cases(lcx, oracle_mod):
+    """A curve with no segments (its instance is empty), a strand of zero radius (never hit), and a
+    segment with NaN control points (never hit; the other segments of the same curve still are)."""
+    import torch
+    from luisacompute_gb300.accel import Accel, Curve, hits_to_numpy, rays_to_device
+    empty = Curve(0, torch.zeros((2, 4), dtype=torch.float32, device="cuda"),
+                  torch.zeros(0, dtype=torch.int32, device="cuda")).build()
+    assert empty.stats().leaf_prim_count == 0
+    thin = np.array([[0, 0, 0, 0.0], [1, 0, 0, 0.0]], np.float32)
+    thin_cv = Curve(0, torch.from_numpy(thin).cuda(), torch.zeros(1, dtype=torch.int32, device="cuda")).build()
+    pts = np.array([[0, 0, 0, 0.1], [1, 0, 0, 0.1], [np.nan, 0, 0, 0.1], [3, 0, 0, 0.1]], np.float32)
+    nan_cv = Curve(0, torch.from_numpy(pts).cuda(), torch.arange(3, dtype=torch.int32, device="cuda")).build()
+    acc = Accel()
+    acc.emplace_back(empty)
+    acc.emplace_back(thin_cv, np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 2]], np.float32))
+    acc.emplace_back(nan_cv)
+    acc.build()
+    rays = np.zeros(4, S.RAY_DTYPE)
+    rays["o"] = [[0.5, 1, 0], [1.5, 1, 0], [2.5, 1, 0], [0.5, 1, 2]]
+    rays["d"] = [0, -1, 0]
+    rays["tmax"] = 1e30
+    got = hits_to_numpy(acc.trace_closest(rays_to_device(rays)))
+    assert got["inst"][0] == 2 and got["prim"][0] == 0 and abs(got["t"][0] - 0.9) < 1e-5
+    assert list(got["inst"][1:]) == [0xFFFFFFFF] * 3  # NaN segments, and the zero-radius strand
