@@ -15,6 +15,7 @@ itself, Rust + Embree, cannot be built here).
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import re
@@ -681,8 +682,13 @@ def main():
         acc.trace_closest(d_rays, out=d_hits, layout=args.layout)
         h_hits.copy_(d_hits, non_blocking=True)
 
-    def host_step():  # lcx_trace_closest_host: chunked, copies overlapped with the traversal
+    def host_step():  # lcx_trace_closest_host: direct host access or chunked staged copies (auto)
         acc.trace_closest_host(h_rays, h_hits, layout=args.layout)
+
+    from luisacompute_gb300 import _capi as C
+    lib = C.load()
+    mode, coherent = ctypes.c_uint32(0), ctypes.c_uint32(0)
+    C.check(lib.lcx_get_host_access(ctypes.byref(mode), ctypes.byref(coherent)), "host access")
 
     def time_e2e(step):
         for _ in range(3):
@@ -698,6 +704,9 @@ def main():
         return e0.elapsed_time(e1)
 
     e2e_serial_ms = time_e2e(serial_step)
+    C.check(lib.lcx_set_host_access(C.HOST_STAGED), "host access")  # the staged path, for comparison
+    e2e_staged_ms = time_e2e(host_step)
+    C.check(lib.lcx_set_host_access(mode.value), "host access")
     e2e_ms = time_e2e(host_step)
     if world > 1:
         import torch.distributed as dist
@@ -718,8 +727,12 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n * 32),
                     "d2h_bytes_per_step": int(n * 24),
-                    "path": "lcx_trace_closest_host via ctypes: pinned host rays and hits, 2^21-ray chunks "
-                            "through device staging, copies in the timed region overlapped with the traversal",
+                    "path": ("lcx_trace_closest_host via ctypes, pinned host rays and hits: the traversal kernel "
+                             "reads the rays from and writes the hits to host memory over the coherent CPU-GPU "
+                             "link (NVLink-C2C), no staging copies" if coherent.value and mode.value != C.HOST_STAGED
+                             else "lcx_trace_closest_host via ctypes: pinned host rays and hits, 2^21-ray chunks "
+                                  "through device staging, copies in the timed region overlapped with the traversal"),
+                    "staged_copies_value": n * e2e_steps / (e2e_staged_ms / 1e3) / 1e9,
                     "serial_copies_value": n * e2e_steps / (e2e_serial_ms / 1e3) / 1e9},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_src,

@@ -475,10 +475,18 @@ LCX_API int lcx_trace_any_motion(uint64_t accel, const LcxRay *d_rays, const flo
 /* The same queries over HOST buffers, for callers whose rays and results live
  * in host memory -- the form of the reference's CPU backend, whose
  * trace_closest / trace_any read and write host arrays
- * (src/rust/luisa_compute_backend_impl/src/cpu/accel.rs:449-535).  The rays
- * stream through device staging in chunks (lcx_set_host_chunk, default 2^21
- * rays; a ring of 4 chunks of staging, 56 B per ray, kept in a memory pool): the copy in of one chunk, the traversal of the previous one and the
- * copy out of the one before run at once.  Stream-ordered like the device
+ * (src/rust/luisa_compute_backend_impl/src/cpu/accel.rs:449-535).  Two
+ * paths (lcx_set_host_access):
+ *   - direct: when both buffers are pinned (page-locked, each one allocation)
+ *     and the device reads host memory through a coherent link (NVLink-C2C on
+ *     Grace systems; the default there), the traversal kernel itself reads
+ *     the rays from and writes the results to host memory, with no staging
+ *     and no copies;
+ *   - staged: otherwise the rays stream through device staging in chunks
+ *     (lcx_set_host_chunk, default 2^21 rays; a ring of 4 chunks of staging,
+ *     56 B per ray, kept in a memory pool): the copy in of one chunk, the
+ *     traversal of the previous one and the copy out of the one before run at
+ *     once.  Stream-ordered like the device
  * forms: the work starts after `stream`'s earlier work and `stream` waits for
  * the last result copy, so h_hits / h_occluded are complete once `stream` is
  * synchronised.  Results equal the device forms'.  Pinned host memory
@@ -494,6 +502,15 @@ LCX_API int lcx_trace_any_host(uint64_t accel, const LcxRay *h_rays, uint32_t ra
 /* Rays per chunk of the host-buffer traces (2^14..2^26).  A tuning knob with
  * no reference counterpart. */
 LCX_API int lcx_set_host_chunk(uint32_t rays);
+/* Host-buffer trace path: LCX_HOST_AUTO (direct when the device has a
+ * coherent host link and the buffers are pinned, else staged), LCX_HOST_STAGED,
+ * LCX_HOST_DIRECT (direct whenever the buffers are pinned: on a device without
+ * a coherent link the kernel's host accesses cross PCIe one by one).
+ * lcx_get_host_access reports the mode and whether the current device has the
+ * coherent link.  Tuning knobs with no reference counterpart. */
+enum { LCX_HOST_AUTO = 0, LCX_HOST_STAGED = 1, LCX_HOST_DIRECT = 2 };
+LCX_API int lcx_set_host_access(uint32_t mode);
+LCX_API int lcx_get_host_access(uint32_t *mode, uint32_t *coherent_link);
 
 /* Counting build of the closest-hit traversal: per-ray visit counts
  * d_counts[3*i + {0,1,2}] = {wide nodes fetched, triangles tested, instances

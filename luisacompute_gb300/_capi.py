@@ -26,6 +26,7 @@ ERROR_NAMES = {0: "LCX_OK", -1: "LCX_ERR_INVALID_ARG", -2: "LCX_ERR_OOM", -3: "L
 HINT_FAST_TRACE, HINT_FAST_BUILD = 0, 1
 REQUEST_PREFER_UPDATE, REQUEST_FORCE_BUILD = 0, 1
 NODES_FP32, NODES_QUANT8 = 0, 1
+HOST_AUTO, HOST_STAGED, HOST_DIRECT = 0, 1, 2
 MOD_PRIMITIVE, MOD_TRANSFORM, MOD_OPAQUE_ON, MOD_OPAQUE_OFF, MOD_VISIBILITY, MOD_USER_ID = 1, 2, 4, 8, 16, 32
 
 
@@ -120,6 +121,8 @@ _SIGS = {
     "lcx_set_trace_stack": (c_int, [c_uint32]),
     "lcx_trace_closest_host": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
     "lcx_trace_any_host": (c_int, [c_uint64, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
+    "lcx_set_host_access": (c_int, [c_uint32]),
+    "lcx_get_host_access": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),
     "lcx_set_host_chunk": (c_int, [c_uint32]),
     "lcx_accel_instance_buffer": (c_int, [c_uint64, POINTER(LcxInstanceBuffer)]),
     "lcx_set_build_split": (c_int, [ctypes.c_float]),

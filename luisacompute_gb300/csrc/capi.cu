@@ -1833,6 +1833,39 @@ int lcx_trace_any(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint
 // device's copy-in, trace and copy-out streams.  Everything stays ordered
 // after `stream`'s earlier work, and `stream` waits for the last copy out.
 uint32_t g_host_chunk = 1u << 21;  // lcx_set_host_chunk (2^20: 5.65 ms, 2^21: 5.39, 2^22: 5.33 per 8.4M rays)
+uint32_t g_host_access = LCX_HOST_AUTO;  // lcx_set_host_access
+
+// Whether the device reads host memory through the host's page tables: a
+// coherent CPU-GPU link (NVLink-C2C on Grace systems), where a kernel's own
+// loads and stores of host memory run at link speed.
+bool host_link_coherent(int device) {
+    static int cached[64];
+    static bool known[64];
+    if (device < 0 || device >= 64) return false;
+    if (!known[device]) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess) v = 0;
+        cached[device] = v;
+        known[device] = true;
+    }
+    return cached[device] != 0;
+}
+
+// The device address of `bytes` bytes of pinned host memory at `p` (both ends
+// inside page-locked host allocations), else null.
+const void *pinned_device_address(const void *p, size_t bytes) {
+    cudaPointerAttributes a{}, b{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    const void *last = static_cast<const char *>(p) + (bytes ? bytes - 1 : 0);
+    if (cudaPointerGetAttributes(&b, last) != cudaSuccess || b.type != cudaMemoryTypeHost) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.devicePointer;
+}
 constexpr uint32_t kHostRing = 4;
 
 static int trace_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *h_hits,
@@ -1844,6 +1877,19 @@ static int trace_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count, 
     if (capturing(st)) return fail(LCX_ERR_INVALID_ARG, "host-buffer traces cannot be captured in a CUDA graph");
     DeviceState *ds = nullptr;
     if (int r = current_device_state(&ds)) return r;
+    // direct access: the traversal reads the rays from and writes the results to the pinned host
+    // buffers itself, with no staging and no copies (on GB300 over NVLink-C2C: 4.62 ms per 8.4M
+    // rays, against 5.09 ms through staged chunks and 4.29 ms on device buffers)
+    if (g_host_access == LCX_HOST_DIRECT || (g_host_access == LCX_HOST_AUTO && host_link_coherent(ds->device))) {
+        const size_t out_bytes = size_t(ray_count) * (h_hits ? sizeof(LcxTriangleHit) : 1);
+        const void *dr = pinned_device_address(h_rays, size_t(ray_count) * sizeof(LcxRay));
+        const void *dout = pinned_device_address(h_hits ? static_cast<const void *>(h_hits) : h_occ, out_bytes);
+        if (dr && dout)
+            return trace_common(accel, static_cast<const LcxRay *>(dr), ray_count, mask,
+                                h_hits ? static_cast<LcxTriangleHit *>(const_cast<void *>(dout)) : nullptr,
+                                h_hits ? nullptr : static_cast<uint8_t *>(const_cast<void *>(dout)), nullptr, layout,
+                                stream);
+    }
     // chunk sizes: a short ramp up (the first copy in is not overlapped), full
     // chunks, and a ramp down (nor is the last copy out)
     const uint32_t chunk = g_host_chunk;
@@ -2047,6 +2093,20 @@ int lcx_trace_any_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count,
                        uint32_t node_layout, void *stream) {
     if (!h_occluded && ray_count) return fail(LCX_ERR_INVALID_ARG, "occluded buffer is null");
     return trace_host(accel, h_rays, ray_count, mask, nullptr, h_occluded, node_layout, stream);
+}
+
+int lcx_set_host_access(uint32_t mode) {
+    if (mode > LCX_HOST_DIRECT) return fail(LCX_ERR_INVALID_ARG, "invalid host access mode %u", mode);
+    g_host_access = mode;
+    return LCX_OK;
+}
+
+int lcx_get_host_access(uint32_t *mode, uint32_t *coherent_link) {
+    DeviceState *ds = nullptr;
+    if (int r = current_device_state(&ds)) return r;
+    if (mode) *mode = g_host_access;
+    if (coherent_link) *coherent_link = host_link_coherent(ds->device) ? 1u : 0u;
+    return LCX_OK;
 }
 
 int lcx_set_host_chunk(uint32_t rays) {

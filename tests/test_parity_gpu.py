@@ -354,14 +354,16 @@ def test_ray_reorder_does_not_change_results(torch_cuda, lcx, oracle_mod, bits):
     no_kernel_errors()
 
 
-@pytest.mark.parametrize("chunk", [1 << 14, 1 << 20])
-def test_host_buffer_traces(torch_cuda, lcx, oracle_mod, chunk):
-    """lcx_trace_closest_host / lcx_trace_any_host (rays and results in host memory, chunked
-    through device staging with copies overlapped): the oracle's records bit for bit, for pinned
-    and pageable buffers, a ray count that is not a multiple of the chunk (with 2^14: 13 chunks
-    through the 4-slot staging ring), both layouts, on a side stream; the empty call is a no-op."""
+@pytest.mark.parametrize("chunk,access", [(1 << 14, 1), (1 << 20, 1), (1 << 20, 0), (1 << 20, 2)])
+def test_host_buffer_traces(torch_cuda, lcx, oracle_mod, chunk, access):
+    """lcx_trace_closest_host / lcx_trace_any_host (rays and results in host memory): the oracle's
+    records bit for bit, for pinned and pageable buffers, both layouts, on a side stream, in every
+    host access mode: staged (chunked through device staging with copies overlapped; a ray count
+    that is not a multiple of the chunk, with 2^14 13 chunks through the 4-slot ring), direct (the
+    kernel reads and writes the pinned host buffers itself) and auto; the empty call is a no-op."""
     from luisacompute_gb300 import _capi
     lib = _capi.load()
+    _capi.check(lib.lcx_set_host_access(access), "host access")
     scene = small_terrain()
     rays = np.concatenate([S.terrain_rays(scene, 150_000, seed=17), S.terrain_shadow_rays(scene, 50_003, seed=18)])
     osc = oracle_mod.OracleScene(scene)
@@ -397,8 +399,10 @@ def test_host_buffer_traces(torch_cuda, lcx, oracle_mod, chunk):
         assert lib.lcx_trace_closest_host(acc.handle, rays.ctypes.data, 16, 0xFF, None, 1, None) \
             == _capi.LCX_ERR_INVALID_ARG
         assert lib.lcx_set_host_chunk(100) == _capi.LCX_ERR_INVALID_ARG
+        assert lib.lcx_set_host_access(3) == _capi.LCX_ERR_INVALID_ARG
     finally:
         _capi.check(lib.lcx_set_host_chunk(1 << 21), "chunk")
+        _capi.check(lib.lcx_set_host_access(_capi.HOST_AUTO), "host access")
     no_kernel_errors()
 
 
