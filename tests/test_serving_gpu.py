@@ -6,10 +6,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("max_batch_rays,min_chunk", [(60_000, 1 << 16), (16_384, 1_024)])
-def test_mix_equals_alone(lcx, oracle_mod, max_batch_rays, min_chunk):
+@pytest.mark.parametrize("max_batch_rays,min_chunk,direct", [(60_000, 1 << 16, None), (16_384, 1_024, None),
+                                                              (16_384, 1_024, False)])
+def test_mix_equals_alone(lcx, oracle_mod, max_batch_rays, min_chunk, direct):
     """With the small cap, requests of up to 40k rays are split into chunks across launches
-    and streams; every result must still equal the request served alone."""
+    and streams; every result must still equal the request served alone, with the kernels reading
+    and writing the requests' pinned buffers directly (the default on a coherent host link) and
+    through device copies (direct=False)."""
     from luisacompute_gb300 import scenes as S
     from luisacompute_gb300 import serving as V
     scenes, reqs = V.make_workload(n_scenes=6, n_requests=60, rate_hz=3000.0, tri_lo=2_000, tri_hi=60_000,
@@ -18,7 +21,7 @@ def test_mix_equals_alone(lcx, oracle_mod, max_batch_rays, min_chunk):
     # a small budget forces evictions and rebuilds on demand
     budget = 12 << 20
     mix = V.ContinuousServer(V.SceneStore(scenes, budget), slots=3, max_batch_rays=max_batch_rays,
-                             min_chunk=min_chunk)
+                             min_chunk=min_chunk, direct_host=direct)
     got = V.results(mix.run([V.Request(r.rid, r.arrival, r.scene, r.rays, r.any_hit, r.new_scene) for r in reqs]))
     assert mix.store.evictions > 0
     if max_batch_rays >= 40_000:
