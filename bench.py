@@ -59,6 +59,9 @@ def parse():
                          "pathtrace: wavefront path tracing 1920x1080x4spp; curves: hair strands as round curves")
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--rate", type=float, default=800.0, help="serving: Poisson arrival rate (requests/s)")
+    ap.add_argument("--warm-split", type=float, default=3.0,
+                    help="serving: triangle-splitting fraction for the scenes built before requests arrive "
+                         "(0: none; 3.0 measured p99 4.5-4.7 ms against 10.1 ms without)")
     ap.add_argument("--budget-gb", type=float, default=8.0, help="serving: HBM budget for scenes")
     ap.add_argument("--meshes", type=int, default=4096)
     ap.add_argument("--instances", type=int, default=100_000)
@@ -364,13 +367,13 @@ def run_serving(args):
         V.PlainServer(V.SceneStore(scenes, budget)).run(clone()[:8])
         torch.cuda.synchronize()
         store_c = V.SceneStore(scenes, budget)
-        store_c.warm(sorted(scenes))  # the 64 scenes are resident before requests arrive
+        store_c.warm(sorted(scenes), split=args.warm_split)  # the 64 scenes are resident before requests arrive
         cont = V.ContinuousServer(store_c, slots=4)
         with ClockSampler(0) as clocks:
             rc = cont.run(clone())
         torch.cuda.synchronize()
         store_p = V.SceneStore(scenes, budget)
-        store_p.warm(sorted(scenes))
+        store_p.warm(sorted(scenes), split=args.warm_split)
         rp = V.PlainServer(store_p).run(clone())
         runs[rate] = {"rate_hz": rate, "generation_s": gen_s,
                       "continuous": {**V.latency_stats(rc), "batches": cont.batches, "chunks": cont.chunks,
@@ -388,7 +391,9 @@ def run_serving(args):
             "config": {"workload": f"64 resident scenes log-uniform 10k..4M tris, {args.requests} Poisson requests, "
                                    "1k..4M rays (half camera, half incoherent; half closest, half any), "
                                    f"8% upload a new scene, HBM budget {args.budget_gb:g} GiB, 4 stream slots, "
-                                   "<= 1M rays per launch, <= 2M rays in flight, fewest-remaining-rays first"},
+                                   "<= 1M rays per launch, <= 2M rays in flight, fewest-remaining-rays first",
+                       "resident_scene_split": args.warm_split,
+                       "host_buffers": "pinned; read and written by the kernels directly on a coherent host link"},
             "runs": list(runs.values()), "clocks": base["clocks"],
             "gpu_launches": base["continuous"]["trace_launches"]}
     print(json.dumps(line), flush=True)

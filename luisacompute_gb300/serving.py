@@ -71,13 +71,23 @@ class SceneStore:
         self.builds = 0
         self.evictions = 0
 
-    def warm(self, ids, stream=None) -> None:
-        """Build scenes `ids` (as many as the budget holds) before serving starts."""
+    def warm(self, ids, stream=None, split: float = 0.0) -> None:
+        """Build scenes `ids` (as many as the budget holds) before serving starts.  split > 0: with
+        triangle splitting at that fraction (lcx_set_build_split): slower builds, faster traces on
+        scenes of long overlapping triangles; builds during serving (uploads, rebuilds after an
+        eviction) keep the process's setting."""
         import torch
         stream = stream or torch.cuda.current_stream()
-        for sid in ids:
-            self.build(sid, None, stream)
-        torch.cuda.synchronize()
+        lib = _capi.load()
+        old = ctypes.c_float(0.0)
+        _capi.check(lib.lcx_get_build_split(ctypes.byref(old)), "lcx_get_build_split")
+        _capi.check(lib.lcx_set_build_split(ctypes.c_float(split)), "lcx_set_build_split")
+        try:
+            for sid in ids:
+                self.build(sid, None, stream)
+            torch.cuda.synchronize()
+        finally:
+            _capi.check(lib.lcx_set_build_split(old), "lcx_set_build_split")
 
     def resident(self, sid: int) -> bool:
         with self.lock:
