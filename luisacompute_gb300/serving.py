@@ -14,7 +14,11 @@ scene that must be built before their rays run.  Two servers process the same ar
   chunk.  Batches on different streams overlap on the device; the query streams have a higher
   priority than the build stream.  Scene builds run on their own thread and stream, so an
   upload never blocks admission.  Scenes live in an HBM budget with LRU eviction of scenes no
-  queued or in-flight request needs; an evicted scene is rebuilt on demand.
+  queued or in-flight request needs; an evicted scene is rebuilt on demand.  Scenes resident before
+  requests arrive may be built with triangle splitting (``SceneStore.warm(split=...)``), which
+  traces scenes of long overlapping triangles faster without putting its build cost on any
+  request.  On a coherent CPU-GPU link the kernels read each request's pinned rays and write its
+  pinned results directly (``direct_host``), with no copies.
 * ``PlainServer`` — one request at a time: build if needed, copy in, one trace call, copy out,
   wait, next.
 
