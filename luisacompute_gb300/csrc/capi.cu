@@ -1833,22 +1833,25 @@ int lcx_trace_any(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint
 // device's copy-in, trace and copy-out streams.  Everything stays ordered
 // after `stream`'s earlier work, and `stream` waits for the last copy out.
 uint32_t g_host_chunk = 1u << 21;  // lcx_set_host_chunk (2^20: 5.65 ms, 2^21: 5.39, 2^22: 5.33 per 8.4M rays)
-uint32_t g_host_access = LCX_HOST_AUTO;  // lcx_set_host_access
+std::atomic<uint32_t> g_host_access{LCX_HOST_AUTO};  // lcx_set_host_access
 
 // Whether the device reads host memory through the host's page tables: a
 // coherent CPU-GPU link (NVLink-C2C on Grace systems), where a kernel's own
 // loads and stores of host memory run at link speed.
 bool host_link_coherent(int device) {
-    static int cached[64];
-    static bool known[64];
+    static std::atomic<int> cached[64];  // 0: not asked yet, 1: no, 2: yes
     if (device < 0 || device >= 64) return false;
-    if (!known[device]) {
+    int c = cached[device].load(std::memory_order_relaxed);
+    if (c == 0) {
         int v = 0;
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess) v = 0;
-        cached[device] = v;
-        known[device] = true;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess) {
+            cudaGetLastError();
+            v = 0;
+        }
+        c = v ? 2 : 1;
+        cached[device].store(c, std::memory_order_relaxed);
     }
-    return cached[device] != 0;
+    return c == 2;
 }
 
 // The device address of `bytes` bytes of pinned host memory at `p` (both ends
@@ -1880,7 +1883,8 @@ static int trace_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count, 
     // direct access: the traversal reads the rays from and writes the results to the pinned host
     // buffers itself, with no staging and no copies (on GB300 over NVLink-C2C: 4.62 ms per 8.4M
     // rays, against 5.09 ms through staged chunks and 4.29 ms on device buffers)
-    if (g_host_access == LCX_HOST_DIRECT || (g_host_access == LCX_HOST_AUTO && host_link_coherent(ds->device))) {
+    const uint32_t access = g_host_access.load();
+    if (access == LCX_HOST_DIRECT || (access == LCX_HOST_AUTO && host_link_coherent(ds->device))) {
         const size_t out_bytes = size_t(ray_count) * (h_hits ? sizeof(LcxTriangleHit) : 1);
         const void *dr = pinned_device_address(h_rays, size_t(ray_count) * sizeof(LcxRay));
         const void *dout = pinned_device_address(h_hits ? static_cast<const void *>(h_hits) : h_occ, out_bytes);
