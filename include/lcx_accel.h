@@ -390,8 +390,11 @@ LCX_API int lcx_curve_create_motion(const LcxAccelOption *option, const LcxMotio
  * include/luisa/dsl/rtx/ray_query.h:17-240).  The reference hands the accel
  * to kernels through its DSL binding; this is that handle as plain pointers.
  * Valid until the accel is rebuilt (a refit keeps it valid) or destroyed, or
- * a mesh it instances is rebuilt or refit without the accel being built again.  Fails like a trace call on an accel that is not
- * ready (LCX_ERR_NOT_BUILT, LCX_ERR_DEPTH). */
+ * a mesh it instances is rebuilt or refit without the accel being built
+ * again.  Fails like a trace call on an accel that is not ready
+ * (LCX_ERR_NOT_BUILT, LCX_ERR_DEPTH).  `motion` = 1: the accel has motion
+ * instances or keyframed meshes or curves, which lcx::ray_query_motion traces
+ * and the plain lcx::ray_query passes over. */
 typedef struct LcxAccelView {
     const void *tlas_nodes;  /* the TLAS's 8-bit quantised nodes (device) */
     const void *instances;   /* its leaf instance records (device) */
@@ -463,8 +466,8 @@ LCX_API int lcx_trace_any_ex(uint64_t accel, const LcxRay *d_rays, uint32_t ray_
  * intersect_any_motion, include/luisa/dsl/rtx/accel.h:47-48): d_times holds
  * ray_count floats (null: time 0).  Static instances ignore the time.  Any
  * trace of an accel that instances a motion instance runs the motion kernels
- * (time 0 for the calls without times); lcx_trace_jobs and
- * lcx_accel_device_view reject such accels. */
+ * (time 0 for the calls without times); lcx_trace_jobs rejects such accels,
+ * and user kernels trace them with lcx::ray_query_motion. */
 LCX_API int lcx_trace_closest_motion(uint64_t accel, const LcxRay *d_rays, const float *d_times,
                                      uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
                                      uint32_t node_layout, void *stream);
