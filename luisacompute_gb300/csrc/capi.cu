@@ -1888,7 +1888,9 @@ static int trace_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count, 
         const size_t out_bytes = size_t(ray_count) * (h_hits ? sizeof(LcxTriangleHit) : 1);
         const void *dr = pinned_device_address(h_rays, size_t(ray_count) * sizeof(LcxRay));
         const void *dout = pinned_device_address(h_hits ? static_cast<const void *>(h_hits) : h_occ, out_bytes);
-        if (dr && dout)
+        const bool aligned = reinterpret_cast<uintptr_t>(dr) % 16 == 0 &&
+                             (!h_hits || reinterpret_cast<uintptr_t>(dout) % 8 == 0);  // else staged, which takes any
+        if (dr && dout && aligned)
             return trace_common(accel, static_cast<const LcxRay *>(dr), ray_count, mask,
                                 h_hits ? static_cast<LcxTriangleHit *>(const_cast<void *>(dout)) : nullptr,
                                 h_hits ? nullptr : static_cast<uint8_t *>(const_cast<void *>(dout)), nullptr, layout,

@@ -392,6 +392,14 @@ def test_host_buffer_traces(torch_cuda, lcx, oracle_mod, chunk, access):
             torch_cuda.cuda.synchronize()
             assert np.array_equal(got2.view(np.uint8), want.view(np.uint8))
             assert np.array_equal(occ2, want_any)
+        # pinned buffers at odd offsets: the direct path steps aside for the staged one
+        raw_rays = torch_cuda.empty(rays.nbytes + 8, dtype=torch_cuda.uint8).pin_memory()
+        raw_rays[8:] = torch_cuda.from_numpy(rays.view(np.uint8).reshape(-1))
+        raw_hits = torch_cuda.zeros(want.nbytes + 4, dtype=torch_cuda.uint8).pin_memory()
+        _capi.check(lib.lcx_trace_closest_host(acc.handle, raw_rays.data_ptr() + 8, rays.shape[0], 0xFF,
+                                               raw_hits.data_ptr() + 4, 1, None), "odd offsets")
+        torch_cuda.cuda.synchronize()
+        assert np.array_equal(raw_hits.numpy()[4:], want.view(np.uint8).reshape(-1))
         empty = np.zeros(0, rays.dtype)
         acc.trace_closest_host(empty, np.zeros(0, want.dtype))
         with pytest.raises(ValueError):
