@@ -452,6 +452,12 @@ typedef struct LcxTraceJob {
  * share the GPU.  Results equal one lcx_trace_closest / lcx_trace_any call
  * per job.  At most 2^31 rays per kind. */
 LCX_API int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout, void *stream);
+/* The same with a time per ray for accels with motion (times[i]: job i's
+ * ray_count floats, device-accessible, or null for time 0; `times` null: all
+ * time 0, as lcx_trace_jobs).  Results equal one lcx_trace_closest_motion /
+ * lcx_trace_any_motion call per job. */
+LCX_API int lcx_trace_jobs_motion(const LcxTraceJob *jobs, const float *const *times, uint32_t count,
+                                  uint32_t node_layout, void *stream);
 
 /* Same queries with an explicit node layout (LCX_NODES_FP32 or
  * LCX_NODES_QUANT8); lcx_trace_closest/any use LCX_NODES_QUANT8. */
@@ -466,8 +472,9 @@ LCX_API int lcx_trace_any_ex(uint64_t accel, const LcxRay *d_rays, uint32_t ray_
  * intersect_any_motion, include/luisa/dsl/rtx/accel.h:47-48): d_times holds
  * ray_count floats (null: time 0).  Static instances ignore the time.  Any
  * trace of an accel that instances a motion instance runs the motion kernels
- * (time 0 for the calls without times); lcx_trace_jobs rejects such accels,
- * and user kernels trace them with lcx::ray_query_motion. */
+ * (time 0 for the calls without times; lcx_trace_jobs_motion takes a time
+ * per ray of each job), and user kernels trace them with
+ * lcx::ray_query_motion. */
 LCX_API int lcx_trace_closest_motion(uint64_t accel, const LcxRay *d_rays, const float *d_times,
                                      uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
                                      uint32_t node_layout, void *stream);

@@ -1669,13 +1669,15 @@ int lcx_accel_device_view(uint64_t accel, LcxAccelView *out) {
     return LCX_OK;
 }
 
-int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout, void *stream) {
+static int trace_jobs(const LcxTraceJob *jobs, const float *const *times, uint32_t count, uint32_t node_layout,
+                      void *stream) {
     if (count == 0) return LCX_OK;
     if (!jobs) return fail(LCX_ERR_INVALID_ARG, "lcx_trace_jobs: jobs is null");
     if (node_layout > LCX_NODES_QUANT8) return fail(LCX_ERR_INVALID_ARG, "invalid node layout %u", node_layout);
     std::shared_lock<std::shared_mutex> life(g_life_mtx);  // until the kernels are enqueued
     std::vector<DevJob> groups[2];  // [0] closest, [1] any
     bool curves[2] = {false, false};  // a job of the group traces curves: the curve kernel runs the group
+    bool motion[2] = {false, false};  // ... motion: the motion kernel (or the curve kernel) runs it
     uint64_t totals[2] = {0, 0};
     uint32_t depth_need = 0;
     for (uint32_t i = 0; i < count; i++) {
@@ -1691,14 +1693,15 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
         if (!meshes_current(a.get()))
             return fail(LCX_ERR_NOT_BUILT, "job %u: a mesh of the accel was destroyed or rebuilt; rebuild the accel",
                         i);
-        if (a->has_motion)
-            return fail(LCX_ERR_INVALID_ARG, "job %u: accels with motion instances are traced with "
-                                             "lcx_trace_closest_motion / lcx_trace_any_motion", i);
+        const float *jt = times ? times[i] : nullptr;
+        if (jt && reinterpret_cast<uintptr_t>(jt) % 4 != 0)
+            return fail(LCX_ERR_INVALID_ARG, "job %u: times must be 4-byte aligned", i);
         const uint32_t need = a->depth + a->max_blas_depth + 3;
         if (int(need) > kStackSize) return fail(LCX_ERR_DEPTH, "job %u: BVH too deep for the traversal stack", i);
         depth_need = std::max(depth_need, need);
         const int g = j.any ? 1 : 0;
         curves[g] = curves[g] || a->has_curves;
+        motion[g] = motion[g] || a->has_motion;
         DevJob d{};
         d.tlas_q = a->qn;
         d.tlas_f = a->fn;
@@ -1708,6 +1711,7 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
         d.first = uint32_t(totals[g]);
         d.count = j.ray_count;
         d.mask = j.mask & 0xffu;
+        d.times = jt;
         totals[g] += j.ray_count;
         if (totals[g] > kMaxTraceRays) return fail(LCX_ERR_INVALID_ARG, "lcx_trace_jobs: more than 2^31 rays");
         groups[g].push_back(d);
@@ -1732,11 +1736,21 @@ int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout
         p.postpone_sp = kStackSize - int(depth_need);
         p.jobs = d_jobs;
         p.job_count = uint32_t(groups[g].size());
-        p.motion = p.curves = curves[g];
+        p.motion = curves[g] || motion[g];
+        p.curves = curves[g];
         LCX_CUDA(cudaMemsetAsync(p.pool, 0, 4 * sizeof(uint32_t), st), "trace counter reset");
         LCX_CUDA(launch_trace(p, int(node_layout), g == 1, false, st), "multi-job trace launch");
     }
     return LCX_OK;
+}
+
+int lcx_trace_jobs(const LcxTraceJob *jobs, uint32_t count, uint32_t node_layout, void *stream) {
+    return trace_jobs(jobs, nullptr, count, node_layout, stream);
+}
+
+int lcx_trace_jobs_motion(const LcxTraceJob *jobs, const float *const *times, uint32_t count, uint32_t node_layout,
+                          void *stream) {
+    return trace_jobs(jobs, times, count, node_layout, stream);
 }
 
 int lcx_check_trace_errors(void) {

@@ -170,8 +170,9 @@ struct __align__(16) DevJob {
     uint32_t count;
     uint32_t mask;
     uint32_t _pad;
+    const float *times;  // per-ray times of the extended kernels (null: time 0)
 };
-static_assert(sizeof(DevJob) == 56 || sizeof(DevJob) == 64, "DevJob size");
+static_assert(sizeof(DevJob) == 64, "DevJob size");
 
 struct TraceParams {
     const Node8Q *tlas_q;

@@ -133,6 +133,7 @@ struct Walker {
 
     __device__ __forceinline__ void start(uint32_t rid) {
         slot = rid;
+        const float *times = P.times;
         if (kMulti) {  // job of global ray rid: last job whose first ray is <= rid
             uint32_t lo = 0, hi = P.job_count - 1;
             while (lo < hi) {
@@ -149,6 +150,7 @@ struct Walker {
             rays = j.rays;
             out = j.out;
             mask = j.mask;
+            times = j.times;
             slot = rid - j.first;
         }
         else if (P.order != nullptr) {
@@ -164,7 +166,7 @@ struct Walker {
         wdy = r1.y;
         wdz = r1.z;
         best_t = r1.w;
-        if (kExt) time = P.times != nullptr ? __ldg(P.times + slot) : 0.0f;
+        if (kExt) time = times != nullptr ? __ldg(times + slot) : 0.0f;
         best_u = best_v = 0.0f;
         best_inst = best_prim = kInvalid;
         to_world();
@@ -1005,7 +1007,7 @@ cudaError_t launch_mode(const TraceParams &p, int layout, bool any, bool countin
 // The extended kernels (kExt 1: motion; 2: motion and curves), loop mode 0 with per-ray times.
 template <int E>
 cudaError_t launch_ext(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
-    if (E == 2 && p.jobs != nullptr) {  // multi-job launches with curves (time 0: jobs carry no times)
+    if (p.jobs != nullptr) {  // multi-job launches with motion or curves (each job's times, or time 0)
         if (layout == LCX_NODES_QUANT8)
             return any ? launch_one<LCX_NODES_QUANT8, true, false, 0, true, kDefaultShortStack, E>(p, st)
                        : launch_one<LCX_NODES_QUANT8, false, false, 0, true, kDefaultShortStack, E>(p, st);

@@ -103,12 +103,12 @@ def test_motion_keyframe_rebuild_refit_and_errors(lcx, oracle_mod):
     want = oracle_mod.OracleScene(scene).trace_motion(rays, times, specs)
     got = hits_to_numpy(acc.trace_closest_motion(d_rays, d_times))
     assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
-    # what motion accels cannot do (lcx::ray_query_motion takes their device view: test_ray_query_gpu.py)
+    # device views and multi-job launches take motion accels (lcx::ray_query_motion: test_ray_query_gpu.py)
     v = _capi.LcxAccelView()
     assert lcx.lcx_accel_device_view(acc.handle, ctypes.byref(v)) == _capi.LCX_OK and v.motion == 1
     out = torch.empty((16, 6), dtype=torch.int32, device="cuda")
     job = (_capi.LcxTraceJob * 1)(_capi.LcxTraceJob(acc.handle, d_rays.data_ptr(), out.data_ptr(), 16, 0xFF, 0, 0))
-    assert lcx.lcx_trace_jobs(job, 1, 1, None) == _capi.LCX_ERR_INVALID_ARG
+    assert lcx.lcx_trace_jobs(job, 1, 1, None) == _capi.LCX_OK  # time 0 (lcx_trace_jobs_motion takes times)
     h = ctypes.c_uint64(0)
     for opt in (_capi.LcxMotionOption(1, 0.0, 1.0, 0, 0, 0, 0), _capi.LcxMotionOption(2, 1.0, 1.0, 0, 0, 0, 0),
                 _capi.LcxMotionOption(2, 0.0, 1.0, 0, 0, 2, 0)):
@@ -230,3 +230,41 @@ def test_keyframed_vertices_match_oracle(lcx, oracle_mod):
     with pytest.raises(_capi.LcxError):
         Mesh(torch.from_numpy(stacked).cuda(), torch.from_numpy(base.triangles.astype(np.int32)).cuda(),
              AccelOption(allow_update=True), motion_keyframes=keys)
+
+
+def test_motion_in_multi_job_launches(lcx, oracle_mod):
+    """lcx_trace_jobs_motion: jobs on a motion accel (each with its own ray times) and on a static
+    accel share one launch per kind; every job equals its own lcx_trace_closest_motion /
+    lcx_trace_any_motion call bit for bit, and plain lcx_trace_jobs traces the motion accel at
+    time 0."""
+    import torch
+    from luisacompute_gb300 import _capi
+    from luisacompute_gb300.accel import Accel, hits_to_numpy, mesh_from_data, rays_to_device
+    rng = np.random.default_rng(57)
+    scene, acc, meshes, motions, specs = _setup(rng)
+    static = Accel()
+    static.emplace_back(mesh_from_data(S.icosphere(3)).build())
+    static.build()
+    lib = _capi.load()
+    n = 30_000
+    rays = [rays_to_device(_rays_times(rng, n, 60 + k)[0]) for k in range(3)]
+    times = [torch.from_numpy(_rays_times(rng, n, 70 + k)[1]).cuda() for k in range(3)]
+    outs = [torch.empty((n, 6), dtype=torch.int32, device="cuda") for _ in range(2)]
+    occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+    jobs = (_capi.LcxTraceJob * 3)(
+        _capi.LcxTraceJob(acc.handle, rays[0].data_ptr(), outs[0].data_ptr(), n, 0xFF, 0, 0),
+        _capi.LcxTraceJob(static.handle, rays[1].data_ptr(), outs[1].data_ptr(), n, 0xFF, 0, 0),
+        _capi.LcxTraceJob(acc.handle, rays[2].data_ptr(), occ.data_ptr(), n, 0xFF, 1, 0))
+    tptr = (ctypes.c_void_p * 3)(times[0].data_ptr(), None, times[2].data_ptr())
+    for layout in (0, 1):
+        _capi.check(lib.lcx_trace_jobs_motion(jobs, tptr, 3, layout, None), "lcx_trace_jobs_motion")
+        torch.cuda.synchronize()
+        want0 = hits_to_numpy(acc.trace_closest_motion(rays[0], times[0], layout=layout))
+        assert np.array_equal(hits_to_numpy(outs[0]).view(np.uint8), want0.view(np.uint8))
+        want1 = hits_to_numpy(static.trace_closest(rays[1], layout=layout))
+        assert np.array_equal(hits_to_numpy(outs[1]).view(np.uint8), want1.view(np.uint8))
+        assert torch.equal(occ, acc.trace_any_motion(rays[2], times[2], layout=layout))
+    _capi.check(lib.lcx_trace_jobs(jobs, 3, 1, None), "lcx_trace_jobs")
+    torch.cuda.synchronize()
+    want0 = hits_to_numpy(acc.trace_closest_motion(rays[0], layout=1))  # time 0
+    assert np.array_equal(hits_to_numpy(outs[0]).view(np.uint8), want0.view(np.uint8))
