@@ -263,6 +263,13 @@ public:
     void trace_jobs(const std::vector<LcxTraceJob> &jobs, void *stream, uint32_t layout = LCX_NODES_QUANT8) const {
         check(lcx_trace_jobs(jobs.data(), uint32_t(jobs.size()), layout, stream), "trace_jobs");
     }
+    // times[i]: job i's per-ray times (device-accessible) or null for time 0
+    void trace_jobs_motion(const std::vector<LcxTraceJob> &jobs, const std::vector<const float *> &times,
+                           void *stream, uint32_t layout = LCX_NODES_QUANT8) const {
+        if (times.size() != jobs.size()) throw Error(LCX_ERR_INVALID_ARG, "trace_jobs_motion: one time array per job");
+        check(lcx_trace_jobs_motion(jobs.data(), times.data(), uint32_t(jobs.size()), layout, stream),
+              "trace_jobs_motion");
+    }
     // The accel for lcx::ray_query in the backend's own kernels (include/lcx/ray_query.cuh).
     [[nodiscard]] LcxAccelView device_view(uint64_t accel) const {
         LcxAccelView v{};
