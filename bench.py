@@ -149,13 +149,9 @@ def ncu_traffic_per_ray(layout):
     return float(m.group(1)) if m else None
 
 
-def cpu_baseline(scene, rays, budget_s=12.0, threads=0):
-    """The oracle (CPU restatement, all host threads) on a bounded sample of the same rays."""
-    import oracle
-    oracle.build()
-    t0 = time.perf_counter()
-    osc = oracle.OracleScene(scene)
-    build_s = time.perf_counter() - t0
+def cpu_baseline(osc, rays, build_s, budget_s=12.0, threads=0):
+    """The oracle (CPU restatement, all host threads) on a bounded sample of the same rays.
+    Returns the baseline record and the oracle's hits for the first ``n`` rays (the sample)."""
     cores = threads or os.cpu_count()
     pilot = rays[:65536]
     t0 = time.perf_counter()
@@ -164,12 +160,214 @@ def cpu_baseline(scene, rays, budget_s=12.0, threads=0):
     n = int(min(rays.shape[0], max(65536, 65536 * budget_s / max(dt, 1e-6))))
     sample = rays[:n]
     t0 = time.perf_counter()
-    osc.trace_closest(sample, threads=cores)
+    hits = osc.trace_closest(sample, threads=cores)
     dt = time.perf_counter() - t0
-    osc.close()
     return {"value": n / dt / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"first {n} of the {rays.shape[0]} incoherent rays, oracle BVH build excluded "
-                      f"({build_s:.1f} s)"}
+                      f"({build_s:.1f} s)"}, hits
+
+
+def closest_parity(oracle_mod, osc, rays, got, want):
+    """Every record of ``got`` (GPU) against ``want`` (oracle, same rays): bit-exact records, and
+    the (inst, prim) disagreements classified in FP64 as near-ties or grazing hits."""
+    g = got.view(np.uint32).reshape(-1, 6)[:, :5]
+    w = want.view(np.uint32).reshape(-1, 6)[:, :5]
+    exact = np.all(g == w, axis=1)
+    rep = oracle_mod.adjudicate(osc, rays, got, want)
+    same_id = (got["inst"] == want["inst"]) & (got["prim"] == want["prim"])
+    other = same_id & ~exact  # same triangle, different t or barycentric bits
+    t_rel = 0.0
+    if other.any():
+        tg, tw = got["t"][other].astype(np.float64), want["t"][other].astype(np.float64)
+        t_rel = float(np.max(np.abs(tg - tw) / np.maximum(np.abs(tw), 1e-30)))
+    return {"rays": int(rays.shape[0]), "bit_exact": float(exact.mean()), "bit_exact_rays": int(exact.sum()),
+            "id_agreement": float(same_id.mean()), "disagree": rep["disagree"], "near_tie": rep["near_tie"],
+            "grazing": rep["grazing"], "unexplained": len(rep["unexplained"]),
+            "same_id_other_bits": int(other.sum()), "same_id_t_rel_max": t_rel}
+
+
+def headline_parity(osc, rays, dev_hits, host_hits, baseline_hits, shadow=None, occ=None, fp32_equal=None):
+    """Parity of the bench's own outputs at the full headline size, against the oracle: the
+    device-resident run (`value`), the host-buffer run (`e2e`) and, when given, the any-hit run on
+    the shadow rays.  The oracle's hits of the timed cpu_baseline sample are reused; the rest of
+    the rays are traced here, untimed."""
+    import oracle as oracle_mod
+    t0 = time.perf_counter()
+    n0 = baseline_hits.shape[0]
+    want = baseline_hits
+    if n0 < rays.shape[0]:
+        want = np.concatenate([baseline_hits, osc.trace_closest(rays[n0:])])
+    out = {"oracle": "oracle/lcx_oracle.cpp (FP32 restatement of accel.rs:449-535, binned-SAH BVH); "
+                     "mismatches classified by its FP64 evaluator",
+           "closest": closest_parity(oracle_mod, osc, rays, dev_hits, want),
+           "closest_e2e": closest_parity(oracle_mod, osc, rays, host_hits, want)}
+    if shadow is not None and occ is not None:
+        want_occ = osc.trace_any(shadow)
+        agree = occ.astype(bool) == want_occ.astype(bool)
+        out["any"] = {"rays": int(shadow.shape[0]), "bit_exact": float(agree.mean()),
+                      "disagree": int((~agree).sum()), "occluded_frac": float(want_occ.mean())}
+    if fp32_equal is not None:
+        out["fp32_nodes_records_equal_quant8"] = bool(fp32_equal)
+    out["check_s"] = time.perf_counter() - t0
+    return out
+
+
+def _event_ms(fn, reps, stream):
+    """Mean ms per call of fn() by CUDA events on `stream` (synchronised on both sides)."""
+    import torch
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def leg_per_thread(acc, d_rays, d_hits, n, stream, reps=5):
+    """Loop mode 3 on the headline rays: one ray per thread through lcx::trace_closest, the
+    per-ray device call a user megakernel makes (include/lcx/trace.cuh)."""
+    import ctypes
+    from luisacompute_gb300 import _capi
+    lib = _capi.load()
+    k = [ctypes.c_uint32(0) for _ in range(3)]
+    _capi.check(lib.lcx_get_trace_tuning(*[ctypes.byref(x) for x in k]), "lcx_get_trace_tuning")
+    _capi.check(lib.lcx_set_trace_tuning(k[0].value, k[1].value, 3), "lcx_set_trace_tuning")
+    try:
+        for _ in range(3):
+            acc.trace_closest(d_rays, out=d_hits)
+        ms = _event_ms(lambda: acc.trace_closest(d_rays, out=d_hits), reps, stream)
+    finally:
+        _capi.check(lib.lcx_set_trace_tuning(k[0].value, k[1].value, k[2].value), "lcx_set_trace_tuning")
+    return {"grays_per_s": n / (ms * 1e-3) / 1e9, "ms": ms,
+            "what": "loop mode 3: one ray per thread, each calling lcx::trace_closest (include/lcx/trace.cuh) with "
+                    "a 16-entry shared short stack, as a user megakernel does; same rays and records as `value`"}
+
+
+def leg_multi_job(scene_acc, stream, jobs=2048, lo=256, hi=8192, seed=23):
+    """Many small closest-hit jobs against several resident scenes: one lcx_trace_jobs launch
+    (the batched form) against one lcx_trace_closest per job in sequence (the plain
+    one-job-at-a-time path, each job on the best single kernel, loop mode 2), the latter captured
+    in a CUDA graph and replayed so that host overhead is not counted against it."""
+    import torch
+    from luisacompute_gb300 import _capi
+    from luisacompute_gb300.accel import accel_from_scene, rays_to_device, stream_handle
+    lib = _capi.load()
+    rng = np.random.default_rng(seed)
+    scenes = [S.icosphere_scene(k) for k in (3, 4, 5)] + [S.terrain_scene(n=256, sphere_count=16, sphere_subdiv=3)]
+    built = [accel_from_scene(s) for s in scenes]
+    accs = [scene_acc] + [a for a, _ in built]
+    counts = np.exp(rng.uniform(np.log(lo), np.log(hi), jobs)).astype(np.int64)
+    first = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    total = int(counts.sum())
+    d_rays = rays_to_device(S.sphere_rays(total, [-1.5] * 3, [1.5] * 3, seed=seed + 1))
+    hits_a = torch.empty((total, 6), dtype=torch.int32, device="cuda")
+    hits_b = torch.empty_like(hits_a)
+    pick = rng.integers(0, len(accs), jobs)
+    table = (_capi.LcxTraceJob * jobs)()
+    for j in range(jobs):
+        table[j] = _capi.LcxTraceJob(accs[pick[j]].handle, d_rays.data_ptr() + int(first[j]) * 32,
+                                     hits_a.data_ptr() + int(first[j]) * 24, int(counts[j]), 0xFF, 0, 0)
+    sh = stream_handle(stream)
+
+    def batched():
+        _capi.check(lib.lcx_trace_jobs(table, jobs, 1, sh), "lcx_trace_jobs")
+
+    def one_at_a_time(h):
+        for j in range(jobs):
+            _capi.check(lib.lcx_trace_closest(accs[pick[j]].handle, d_rays.data_ptr() + int(first[j]) * 32,
+                                              int(counts[j]), 0xFF, hits_b.data_ptr() + int(first[j]) * 24, h),
+                        "lcx_trace_closest")
+
+    for _ in range(3):
+        batched()
+    batched_ms = _event_ms(batched, 5, stream)
+    one_at_a_time(sh)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):  # captured on torch's capture stream
+        one_at_a_time(stream_handle(torch.cuda.current_stream()))
+    for _ in range(2):
+        graph.replay()
+    plain_ms = _event_ms(graph.replay, 5, stream)
+    equal = bool(torch.equal(hits_a, hits_b))
+    del graph
+    return {"jobs": jobs, "rays": total, "scenes": len(accs), "batched_ms": batched_ms, "one_at_a_time_ms": plain_ms,
+            "batched_grays_per_s": total / (batched_ms * 1e-3) / 1e9,
+            "one_at_a_time_grays_per_s": total / (plain_ms * 1e-3) / 1e9,
+            "ratio": plain_ms / batched_ms, "records_equal": equal,
+            "what": f"{jobs} closest-hit jobs of {lo}..{hi} rays (log-uniform) against {len(accs)} resident scenes "
+                    "(the headline scene, icospheres of 1,280 / 5,120 / 20,480 triangles, a small terrain): one "
+                    "lcx_trace_jobs launch (host preparation included) vs one lcx_trace_closest per job in "
+                    "sequence, replayed from a CUDA graph (no host overhead counted against it)"}
+
+
+def leg_batch_build(stream, count=512):
+    """Batched BLAS build of a 512-mesh sample of the batched-build workload (log-uniform
+    64..262,144 triangles, 1 % Gaussian displacement): Mtris/s of one lcx_mesh_build_batch."""
+    from luisacompute_gb300.accel import build_meshes, mesh_from_data
+    datas = S.batch_meshes(count, seed=6)
+    meshes = [mesh_from_data(m) for m in datas]
+    total = sum(m.tri_count for m in datas)
+    for _ in range(3):
+        build_meshes(meshes)
+    ms = _event_ms(lambda: build_meshes(meshes), 5, stream)
+    return {"meshes": count, "triangles": int(total), "ms": ms, "mtris_per_s": total / (ms * 1e-3) / 1e6,
+            "what": "one lcx_mesh_build_batch over the sample per step (its host sync for the node count included), "
+                    "default build knobs"}
+
+
+def leg_pathtrace(scene, acc, meshes, stream, steps=5):
+    """Wavefront path tracing of the headline scene, 1920x1080, 4 spp, <= 8 bounces."""
+    import torch
+    from luisacompute_gb300 import pathtrace as PT
+    alb = PT.albedos_to_device(PT.albedos(scene))
+    prm = PT.params(width=1920, height=1080, spp=4, max_bounces=8, rr_start=3, eye=(0.0, 0.8, 2.4))
+    for _ in range(3):
+        PT.render(scene, acc, meshes, alb, prm)
+    times, st = [], None
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, _, st = PT.render(scene, acc, meshes, alb, prm, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = float(np.median(times))
+    return {"ms_per_frame": ms, "rays_closest": int(st.closest_rays), "rays_any": int(st.any_rays),
+            "grays_per_s": (st.closest_rays + st.any_rays) / (ms * 1e-3) / 1e9,
+            "what": "lcx_pt_render, 1920x1080x4 spp, <= 8 bounces, RR from 3, per-bounce host syncs included"}
+
+
+def leg_serving(requests=300, rate=800.0, n_scenes=16):
+    """A short serving mix: continuous batching against one request at a time on the same trace."""
+    import torch
+    from luisacompute_gb300 import serving as V
+    scenes, reqs = V.make_workload(n_scenes=n_scenes, n_requests=requests, rate_hz=rate, tri_hi=1_000_000,
+                                   ray_pool=12)
+    budget = 8 << 30
+
+    def clone():
+        return [V.Request(r.rid, r.arrival, r.scene, r.rays, r.any_hit, r.new_scene) for r in reqs]
+
+    V.ContinuousServer(V.SceneStore(scenes, budget), slots=4).run(clone()[:8])  # warm pools and modules
+    torch.cuda.synchronize()
+    store = V.SceneStore(scenes, budget)
+    store.warm(sorted(scenes), split=3.0)
+    cont = V.ContinuousServer(store, slots=4)
+    rc = cont.run(clone())
+    torch.cuda.synchronize()
+    store_p = V.SceneStore(scenes, budget)
+    store_p.warm(sorted(scenes), split=3.0)
+    rp = V.PlainServer(store_p).run(clone())
+    c, p = V.latency_stats(rc), V.latency_stats(rp)
+    return {"continuous": {"p50_ms": c["p50_ms"], "p99_ms": c["p99_ms"], "grays_per_s": c["grays_per_s"],
+                           "queries_0.5M_to_2M_rays": c["queries_0.5M_to_2M_rays"]},
+            "one_at_a_time": {"p50_ms": p["p50_ms"], "p99_ms": p["p99_ms"], "grays_per_s": p["grays_per_s"],
+                              "queries_0.5M_to_2M_rays": p["queries_0.5M_to_2M_rays"]},
+            "what": f"{requests} Poisson requests at {rate:g}/s, {n_scenes} resident scenes of 10k..1M triangles "
+                    "(split-built), 1k..4M rays, half camera half incoherent, half closest half any, 8% uploads"}
 
 
 def run_batch_build(args):
@@ -676,6 +874,8 @@ def main():
         ms = float(t.item())
     ms_per_step = ms / args.steps
     value = n * world * args.steps / (ms / 1e3) / 1e9
+    from luisacompute_gb300.accel import hits_to_numpy
+    dev_hits = hits_to_numpy(d_hits) if rank == 0 else None  # the timed run's records, for the parity check
 
     # end to end: pinned host rays -> device -> trace -> hits -> pinned host
     h_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8)).pin_memory()
@@ -742,15 +942,22 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_src,
                          "traffic": None if traffic_pr is None else traffic_pr * n,
+                         "traffic_source": None if traffic_pr is None else
+                         ("profiles/trace_closest_quant8_terrain.md: ncu dram__bytes_read.sum + dram__bytes_write.sum "
+                          "of one full-size launch of this kernel in an earlier capture (per ray, times the rays "
+                          "of this run); not measured in this run"),
                          "algorithmic_bytes_per_ray": bytes_per_ray,
                          "visits_per_ray": {"nodes": c[0], "triangles": c[1], "instances": c[2]},
                          "kernel": kernel_name,
-                         "visits_from": "the counting pass (loop mode 0); mode 2 visits ~5 % more nodes"},
+                         "visits_from": (f"the counting build of the timed loop structure (loop mode {knobs[2].value}"
+                                         f"{', quantised nodes' if args.layout == 1 else ''}) on the same rays, "
+                                         "before the timed region")},
             "clocks": clocks.summary(),
             "gpu_launches": args.steps}
     if tuned is not None:
         line["config"]["autotune"] = tuned
 
+    shadow_np = occ_np = fp32_equal = None
     if rank == 0 and not args.no_extra:
         extra = {"build_wall_s_all_meshes_and_tlas": build_wall_s}
         try:
@@ -765,7 +972,9 @@ def main():
             x1.record(stream)
             torch.cuda.synchronize()
             extra["closest_grays_" + ("fp32" if other == 0 else "quant8")] = n * 5 / (x0.elapsed_time(x1) / 1e3) / 1e9
-            sh = rays_to_device(S.terrain_shadow_rays(scene, n, seed=5))
+            fp32_equal = np.array_equal(hits_to_numpy(d_hits).view(np.uint8), dev_hits.view(np.uint8))
+            shadow_np = S.terrain_shadow_rays(scene, n, seed=5)
+            sh = rays_to_device(shadow_np)
             occ = torch.empty(n, dtype=torch.uint8, device="cuda")
             for _ in range(3):
                 acc.trace_any(sh, out=occ, layout=args.layout)
@@ -777,6 +986,7 @@ def main():
             torch.cuda.synchronize()
             extra["any_shadow_grays"] = n * 5 / (x0.elapsed_time(x1) / 1e3) / 1e9
             extra["shadow_occluded_frac"] = float(occ.float().mean().item())
+            occ_np = occ.cpu().numpy()
             st = acc.stats()
             extra["tlas"] = {"nodes": int(st.node_count), "depth": int(st.depth), "max_blas_depth": int(st.max_blas_depth)}
             ms0 = meshes[0].stats()
@@ -786,10 +996,30 @@ def main():
             del sh, occ
         except Exception as e:  # extras never fail the bench
             extra["error"] = repr(e)
+        # the other forms, each a bounded leg (a failing leg records its error)
+        for name, leg in (("per_thread_device_calls", lambda: leg_per_thread(acc, d_rays, d_hits, n, stream)),
+                          ("multi_job_vs_one_at_a_time", lambda: leg_multi_job(acc, stream)),
+                          ("batched_build_512_meshes", lambda: leg_batch_build(stream)),
+                          ("pathtrace_1080p_4spp", lambda: leg_pathtrace(scene, acc, meshes, stream)),
+                          ("serving_short_mix", leg_serving)):
+            t0 = time.perf_counter()
+            try:
+                extra[name] = leg()
+            except Exception as e:
+                extra[name] = {"error": repr(e)}
+            extra[name]["leg_wall_s"] = time.perf_counter() - t0
         line["extra"] = extra
 
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(scene, rays)
+        import oracle
+        oracle.build()
+        t0 = time.perf_counter()
+        osc = oracle.OracleScene(scene)
+        build_s = time.perf_counter() - t0
+        line["cpu_baseline"], base_hits = cpu_baseline(osc, rays, build_s)
+        host_hits = h_hits.numpy().view(S.HIT_DTYPE).reshape(-1)
+        line["parity"] = headline_parity(osc, rays, dev_hits, host_hits, base_hits, shadow_np, occ_np, fp32_equal)
+        osc.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

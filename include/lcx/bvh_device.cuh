@@ -26,6 +26,7 @@ constexpr int kWide = 8;
 constexpr int kMaxLeafItems = 3;    // items per leaf slot (meta holds a 2-bit count)
 constexpr int kStackSize = 32;      // traversal stack entries per thread
 constexpr int kMaxLevels = 64;      // wide-tree depth limit of the collapse
+constexpr uint32_t kMaxRaySteps = 1u << 22;  // default per-ray step bound: a corrupt tree ends the ray, never hangs
 
 #ifndef LCX_L2_KEEP
 #define LCX_L2_KEEP 0

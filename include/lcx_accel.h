@@ -524,7 +524,9 @@ LCX_API int lcx_get_host_access(uint32_t *mode, uint32_t *coherent_link);
 
 /* Counting build of the closest-hit traversal: per-ray visit counts
  * d_counts[3*i + {0,1,2}] = {wide nodes fetched, triangles tested, instances
- * entered}.  Used to compute algorithmic bytes per ray. */
+ * entered}.  Used to compute algorithmic bytes per ray.  The counts are those
+ * of the loop structure the plain call would run (lcx_set_trace_tuning's
+ * mode: loop mode 2 for quantised nodes by default). */
 LCX_API int lcx_trace_closest_counts(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count,
                              uint32_t mask, LcxTriangleHit *d_hits, uint32_t *d_counts,
                              uint32_t node_layout, void *stream);
@@ -541,7 +543,10 @@ LCX_API int lcx_trace_closest_counts(uint64_t accel, const LcxRay *d_rays, uint3
  * call before any stream capture.  All calls share the array (it is cleared at
  * the start of each call): calls that overlap on the GPU race and must be
  * ordered by the caller.  ray_count <= 2^31; larger counts return
- * LCX_ERR_INVALID_ARG. */
+ * LCX_ERR_INVALID_ARG.  Kernel-side bounds (stack overflow, step bound) are
+ * reported by lcx_check_trace_errors like those of the other trace calls.  The
+ * array's device address is kept for the life of the process: do not call this
+ * entry point again after a cudaDeviceReset. */
 LCX_API int lcx_trace_closest_noalloc(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask,
                                       LcxTriangleHit *d_hits, void *stream);
 
@@ -634,7 +639,10 @@ LCX_API int lcx_get_build_split(float *fraction);
  * structure -- 2 (default) = deferred triangle batches: each warp queues the
  * triangles its lanes find and tests them 32 at a time (quantised-node,
  * single-job, non-counting calls; the others run mode 0); 0 = each step
- * visits one node and tests its triangles; 1 = speculative while-while.
+ * visits one node and tests its triangles; 1 = speculative while-while;
+ * 3 = one ray per thread through lcx::trace_closest / lcx::trace_any
+ * (include/lcx/trace.cuh), the form a user kernel's per-ray calls take
+ * (quantised-node single-job calls; the others run mode 0).
  * postpone: in mode 2, the queue size that starts a batch (1..32; 0 = 24 for
  * closest, 16 for any hit); in modes 0 and 1, a lane defers its triangle tests
  * while fewer than this many lanes would run them (0 = never).  Results do
@@ -655,6 +663,14 @@ LCX_API int lcx_set_trace_reorder(uint32_t bits, uint32_t min_rays);
 LCX_API int lcx_set_trace_stack(uint32_t short_entries);
 LCX_API int lcx_get_trace_stack(uint32_t *short_entries);
 LCX_API int lcx_get_trace_reorder(uint32_t *bits, uint32_t *min_rays);
+/* Per-ray step bound of later trace calls (every form): a ray that takes more
+ * traversal steps ends with the record it has and flags LCX_ERR_TIMEOUT for
+ * lcx_check_trace_errors.  0 restores the default, 2^22 steps, which no valid
+ * BVH reaches; a small bound lets a caller (or a test) check the timeout path
+ * on a valid scene without a hang.  A guard with no reference counterpart:
+ * the reference's OptiX and Embree traversals have no step bound. */
+LCX_API int lcx_set_trace_step_bound(uint32_t steps);
+LCX_API int lcx_get_trace_step_bound(uint32_t *steps);
 
 #ifdef __cplusplus
 }

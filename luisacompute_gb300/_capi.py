@@ -140,6 +140,8 @@ _SIGS = {
     "lcx_trace_any_motion": (c_int, [c_uint64, c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
     "lcx_set_refit_sync": (c_int, [c_uint32]),
     "lcx_get_trace_stack": (c_int, [POINTER(c_uint32)]),
+    "lcx_set_trace_step_bound": (c_int, [c_uint32]),
+    "lcx_get_trace_step_bound": (c_int, [POINTER(c_uint32)]),
     "lcx_get_trace_reorder": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),
     "lcx_accel_create": (c_int, [POINTER(LcxAccelOption), POINTER(c_uint64)]),
     "lcx_accel_destroy": (c_int, [c_uint64]),

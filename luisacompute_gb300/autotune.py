@@ -11,8 +11,8 @@ It measures, on the caller's own scene and rays, and picks:
 * traversal knobs (``lcx_set_trace_tuning`` / ``lcx_set_trace_stack`` / ``lcx_set_trace_reorder``):
   - ray-pool refill threshold: the number of idle lanes at which a warp takes new rays, 1..32;
   - shared-memory stack depth: 8, 16 or 24 entries per thread;
-  - loop structure: 2 (deferred triangle batches, the default), 0 (node + its items per step) or
-    1 (speculative while-while);
+  - loop structure: 2 (deferred triangle batches, the default), 0 (node + its items per step),
+    1 (speculative while-while) or 3 (one ray per thread through the device-side trace functions);
   - mode 2's flush size (``postpone``): 0 (24 closest / 16 any), 12 or 32 queued tests;
   - ray reordering: off, or sorted by octant and 7-bit origin Morton cell.
 
@@ -41,7 +41,7 @@ from . import _capi
 from .accel import NODES_QUANT8, Accel, build_meshes, mesh_from_data
 
 BUILD_SPACE = {"leaf_max": [1, 2, 3], "width": [8, 6, 4], "blas_cube": [1, 0], "split": [0.0, 1.0, 3.0]}
-TRACE_SPACE = {"refill": [1, 2, 4, 8, 16, 32], "short_stack": [8, 16, 24], "mode": [2, 0, 1], "postpone": [0, 12, 32],
+TRACE_SPACE = {"refill": [1, 2, 4, 8, 16, 32], "short_stack": [8, 16, 24], "mode": [2, 0, 1, 3], "postpone": [0, 12, 32],
                "reorder_bits": [0, 7]}
 
 

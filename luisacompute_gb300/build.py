@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "liblcx_accel.so"
 SOURCES = ["build.cu", "traverse.cu", "capi.cu", "sort.cu", "noalloc.cu", "pathtrace.cu", "reorder.cu"]
-HEADERS = ["lcx_device.cuh", "lcx_internal.h", "pt_math.cuh"]
+HEADERS = ["lcx_internal.h", "pt_math.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               f"-I{ROOT / 'include'}", f"-I{CSRC}"]

@@ -567,7 +567,10 @@ int try_reserved_rebuild(const std::vector<MeshObj *> &meshes, const std::vector
     ScratchHolder hold(st);
     BuildScratch s;
     if (int r = alloc_scratch(hold, s, blk->h_segs, blk->items, false, blk->d_segs, blk->d_segctl_init)) return r;
-    LCX_CUDA(build_tree_tris(s, bp, st), "BLAS rebuild");
+    {
+        NvtxRange nr("reserved rebuild: boxes, sort, LBVH, collapse");
+        LCX_CUDA(build_tree_tris(s, bp, st), "BLAS rebuild");
+    }
     LCX_CUDA(cudaMemsetAsync(blk->wsah, 0, 2 * sizeof(double) * count, st), "cudaMemset");
     LCX_CUDA(emit_blas(s, bp, blk->cap_wide, blk->qn, blk->fn, blk->tris, blk->wsah, nullptr, st, true),
              "BLAS rebuild emit");
@@ -684,7 +687,10 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
             LCX_CUDA(hold.alloc((void **)&ref_prim, sizeof(uint32_t) * n_items), "split scratch");
             LCX_CUDA(split_emit(d_tsegs, uint32_t(count), n, d_refs, d_ref_off, s, ref_prim, st), "triangle split");
         }
-        LCX_CUDA(build_tree_tris(s, bp, st), "BLAS build");
+        {
+            NvtxRange nr("BLAS build: boxes, sort, LBVH, collapse");
+            LCX_CUDA(build_tree_tris(s, bp, st), "BLAS build");
+        }
         if (int r = read_back(s, st, rb)) return r;
         if (rb.ctl[kCtlErr] & kErrBadIndex) {
             for (size_t i = 0; i < count; i++)
@@ -768,7 +774,10 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
             mm.flags = (m->motion.vanish_start ? 1u : 0u) | (m->motion.vanish_end ? 2u : 0u);
             LCX_CUDA(cudaMemcpyAsync(m->d_motion, &mm, sizeof(mm), cudaMemcpyHostToDevice, st), "motion upload");
         }
-        LCX_CUDA(emit_blas(s, bp, W, qn, fn, tr, wsah, rtab, st), "BLAS emit");
+        {
+            NvtxRange nr("BLAS build: emit nodes and triangles");
+            LCX_CUDA(emit_blas(s, bp, W, qn, fn, tr, wsah, rtab, st), "BLAS emit");
+        }
         for (size_t i = 0; i < count; i++) {
             MeshObj *m = meshes[i];
             const uint32_t *sc = &rb.segctl[kSegWords * i];
@@ -804,6 +813,7 @@ struct TraceTuning {
     uint32_t postpone = 0;  // modes 0 / 1: postponing did not pay (sweep 0..24); mode 2: 0 = per-kind flush size
     uint32_t mode = 2;      // traversal loop structure: deferred triangle batches (quantised nodes; FP32 runs mode 0)
     uint32_t short_stack = 16;  // shared-memory stack entries per thread (8, 16, 24)
+    uint32_t max_steps = kMaxRaySteps;  // per-ray step bound (lcx_set_trace_step_bound)
 };
 TraceTuning g_tune;
 
@@ -857,6 +867,8 @@ int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, u
     p.refill = g_tune.refill;
     p.postpone = g_tune.postpone;
     p.mode = g_tune.mode;
+    p.short_stack = g_tune.short_stack;
+    p.max_steps = g_tune.max_steps;
     p.postpone_sp = kStackSize - int(depth_need);
     return LCX_OK;
 }
@@ -1126,6 +1138,7 @@ int lcx_curve_build(uint64_t handle, const LcxCurveBuildCommand *cmd, void *stre
 }
 
 int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *cmd, void *stream) {
+    NvtxRange nr("lcx_mesh_build");
     auto m = find_mesh(mesh);
     if (!m) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build: unknown mesh handle %llu", (unsigned long long)mesh);
     if (!cmd) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build: command is null");
@@ -1139,6 +1152,7 @@ int lcx_mesh_build(uint64_t mesh, const LcxMeshBuildCommand *cmd, void *stream) 
 }
 
 int lcx_mesh_build_batch(const uint64_t *meshes, const LcxMeshBuildCommand *cmds, uint32_t count, void *stream) {
+    NvtxRange nr("lcx_mesh_build_batch");
     if (count == 0) return LCX_OK;
     if (!meshes || !cmds) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_build_batch: null arguments");
     std::vector<std::shared_ptr<MeshObj>> objs(count);
@@ -1259,6 +1273,7 @@ int lcx_accel_destroy(uint64_t accel) {
 
 int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, const LcxModification *mods,
                     size_t mod_count, int update_instance_buffer_only, void *stream) {
+    NvtxRange nr("lcx_accel_build");
     auto a = find_accel(accel);
     if (!a) return fail(LCX_ERR_INVALID_ARG, "lcx_accel_build: unknown accel handle %llu", (unsigned long long)accel);
     if (request > LCX_REQUEST_FORCE_BUILD) return fail(LCX_ERR_INVALID_ARG, "invalid build request %u", request);
@@ -1429,7 +1444,10 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
         std::vector<SegInput> segs(1);
         segs[0] = SegInput{nullptr, 0, nullptr, 0, 0, n, 0, nullptr};
         if (int r = alloc_scratch(hold, s, segs, n, true)) return r;
-        LCX_CUDA(build_tree_insts(a->d_inst, s, bp, st), "TLAS build");
+        {
+            NvtxRange nr("TLAS build: boxes, sort, LBVH, collapse");
+            LCX_CUDA(build_tree_insts(a->d_inst, s, bp, st), "TLAS build");
+        }
         if (int r = read_back(s, st, rb)) return r;
         if (rb.ctl[kCtlErr] & kErrTooDeep) return fail(LCX_ERR_DEPTH, "TLAS deeper than %d levels", kMaxLevels);
         if (rb.segctl[kSegItems] != n)
@@ -1466,7 +1484,10 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
             block->fn = fn;
         }
         LCX_CUDA(cudaMemsetAsync(wsah, 0, 2 * sizeof(double), st), "cudaMemset");
-        LCX_CUDA(emit_tlas(a->d_inst, s, bp, W, qn, fn, ir, wsah, rtab, st), "TLAS emit");
+        {
+            NvtxRange nr("TLAS build: emit nodes and instances");
+            LCX_CUDA(emit_tlas(a->d_inst, s, bp, W, qn, fn, ir, wsah, rtab, st), "TLAS emit");
+        }
         a->qn = qn;
         a->fn = fn;
         a->recs = ir;
@@ -1622,6 +1643,7 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     p.postpone = g_tune.postpone;
     p.mode = g_tune.mode;
     p.short_stack = g_tune.short_stack;
+    p.max_steps = g_tune.max_steps;
     // regular pushes need at most tlas_depth + blas_depth + 3 entries; postponed
     // triangle groups may use what is left
     p.postpone_sp = kStackSize - int(depth_need);
@@ -1631,6 +1653,7 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
         if (int r = reorder_begin(p.rays, ray_count, p.tlas_f, rbits, st, &rs)) return r;
         p.order = rs.order;
     }
+    NvtxRange nr(d_occ ? "trace_any" : "trace_closest");
     cudaError_t e = cudaMemsetAsync(p.pool, 0, 4 * sizeof(uint32_t), st);
     if (e == cudaSuccess) e = launch_trace(p, int(layout), d_occ != nullptr, d_counts != nullptr, st);
     const int released = reorder_end(&rs, st);
@@ -1719,6 +1742,7 @@ static int trace_jobs(const LcxTraceJob *jobs, const float *const *times, uint32
     DeviceState *ds = nullptr;
     if (int r = current_device_state(&ds)) return r;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    NvtxRange nr("trace_jobs");
     for (int g = 0; g < 2; g++) {
         if (groups[g].empty()) continue;
         ScratchHolder hold(st);
@@ -1733,6 +1757,7 @@ static int trace_jobs(const LcxTraceJob *jobs, const float *const *times, uint32
         p.refill = g_tune.refill;
         p.mode = g_tune.mode == 2 ? 2u : 0u;  // multi-job kernels: mode 2 (quantised nodes) or 0
         p.postpone = p.mode == 2 ? g_tune.postpone : 0u;
+        p.max_steps = g_tune.max_steps;
         p.postpone_sp = kStackSize - int(depth_need);
         p.jobs = d_jobs;
         p.job_count = uint32_t(groups[g].size());
@@ -1760,6 +1785,7 @@ int lcx_check_trace_errors(void) {
     std::vector<uint32_t> h(kPoolSlots * 4);
     LCX_CUDA(cudaMemcpy(h.data(), ds->pool, h.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost), "pool readback");
     uint32_t flags = 0;
+    if (int r = noalloc_take_errors(&flags)) return r;  // lcx_trace_closest_noalloc's own error word
     for (uint32_t i = 0; i < kPoolSlots; i++) flags |= h[4 * i + 1];
     if (flags) {
         for (uint32_t i = 0; i < kPoolSlots; i++) h[4 * i + 1] = 0;
@@ -1773,17 +1799,33 @@ int lcx_check_trace_errors(void) {
         return fail(LCX_ERR_INVALID_ARG,
                     "an asynchronous refit or reserved rebuild failed (bad index or unquantisable coordinates)");
     }
-    if (flags & 2u) return fail(LCX_ERR_TIMEOUT, "a ray exceeded the traversal step bound (corrupt BVH?)");
+    if (flags & 2u)
+        return fail(LCX_ERR_TIMEOUT, "a ray exceeded the traversal step bound (lcx_set_trace_step_bound; the "
+                                     "default bound is reached only on a corrupt BVH)");
     if (flags & 1u) return fail(LCX_ERR_DEPTH, "a ray overflowed the traversal stack");
     return LCX_OK;
 }
 
 int lcx_set_trace_tuning(uint32_t refill, uint32_t postpone, uint32_t mode) {
-    if (refill < 1 || refill > 32 || postpone > 32 || mode > 2)
-        return fail(LCX_ERR_INVALID_ARG, "tuning out of range (refill 1..32, postpone 0..32, mode 0..2)");
+    if (refill < 1 || refill > 32 || postpone > 32 || mode > 3)
+        return fail(LCX_ERR_INVALID_ARG, "tuning out of range (refill 1..32, postpone 0..32, mode 0..3)");
     g_tune.refill = refill;
     g_tune.postpone = postpone;
     g_tune.mode = mode;
+    return LCX_OK;
+}
+
+int lcx_set_trace_step_bound(uint32_t steps) {
+    if (steps > kMaxRaySteps)
+        return fail(LCX_ERR_INVALID_ARG, "step bound %u out of range (0 = default %u, 1..%u)", steps, kMaxRaySteps,
+                    kMaxRaySteps);
+    g_tune.max_steps = steps == 0 ? kMaxRaySteps : steps;
+    return LCX_OK;
+}
+
+int lcx_get_trace_step_bound(uint32_t *steps) {
+    if (!steps) return fail(LCX_ERR_INVALID_ARG, "null output");
+    *steps = g_tune.max_steps;
     return LCX_OK;
 }
 
@@ -1892,6 +1934,7 @@ static int trace_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count, 
                             layout, stream);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (capturing(st)) return fail(LCX_ERR_INVALID_ARG, "host-buffer traces cannot be captured in a CUDA graph");
+    NvtxRange nr(h_occ ? "trace_any_host" : "trace_closest_host");
     DeviceState *ds = nullptr;
     if (int r = current_device_state(&ds)) return r;
     // direct access: the traversal reads the rays from and writes the results to the pinned host

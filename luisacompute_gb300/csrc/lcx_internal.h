@@ -7,10 +7,35 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "lcx_accel.h"
-#include "lcx_device.cuh"
+#include "lcx/bvh_device.cuh"  // device-side layouts and arithmetic, shared with user kernels
 
 namespace lcx {
+
+// NVTX range over a build phase or a trace call, in the library's own domain
+// "lcx_accel" (header-only NVTX v3: without a profiler attached a push / pop
+// costs a function-pointer check).  The names are the entry points and phases:
+// nsys / ncu --nvtx show where a build's or a frame's time goes, as the
+// reference's named OptiX builds do (src/backends/cuda/cuda_accel.cpp:28,68).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) {
+        nvtxEventAttributes_t a{};
+        a.version = NVTX_VERSION;
+        a.size = NVTX_EVENT_ATTRIB_STRUCT_SIZE;
+        a.messageType = NVTX_MESSAGE_TYPE_ASCII;
+        a.message.ascii = name;
+        nvtxDomainRangePushEx(domain(), &a);
+    }
+    ~NvtxRange() { nvtxDomainRangePop(domain()); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+    static nvtxDomainHandle_t domain() {
+        static nvtxDomainHandle_t d = nvtxDomainCreateA("lcx_accel");
+        return d;
+    }
+};
 
 // One BVH of a build: a mesh's triangles (BLAS) or a TLAS's instances.
 struct SegInput {
@@ -196,6 +221,7 @@ struct TraceParams {
     bool motion;            // the accel has motion or curves: the extended kernels (mode 0) run the call
     bool curves;            // with `motion`: the accel has curves (the extended kernels with the curve test)
     const float *times;     // motion launches: per-ray times (null: time 0)
+    uint32_t max_steps = kMaxRaySteps;  // per-ray step bound; a ray that exceeds it ends and flags LCX_ERR_TIMEOUT
 };
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st);
 
@@ -220,6 +246,8 @@ int scratch_pool(cudaMemPool_t *out);
 int trace_params_for(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
                      uint32_t max_rays, TraceParams &p);
 int record_error(int code, const char *msg);
+// Error flags of lcx_trace_closest_noalloc on the current device (noalloc.cu), read and cleared.
+int noalloc_take_errors(uint32_t *flags);
 
 // BVH lifetime lock (capi.cu): a trace holds it shared from validating its
 // accel until its kernel is enqueued; freeing BVH memory holds it exclusively.

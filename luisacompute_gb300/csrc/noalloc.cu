@@ -31,7 +31,9 @@ uint32_t *g_scratch_addr[kMaxDevices] = {};
 
 // Device address of g_noalloc_scratch on the current device.  In host code the
 // symbol's name is only a host-side stand-in, never a device address, so it is
-// looked up once per device with that device current.
+// looked up once per device with that device current.  The address is kept for
+// the life of the process: after cudaDeviceReset (a new primary context) the
+// entry point must not be called again in that process.
 int scratch_address(uint32_t **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -53,6 +55,35 @@ int scratch_address(uint32_t **out) {
 }
 
 }  // namespace
+
+namespace lcx {
+
+// The kernel-side error flags (stack overflow, step bound) the allocation-free
+// trace left in its scratch on the current device, cleared as they are read;
+// 0 when it never ran there.  lcx_check_trace_errors calls it after its device
+// synchronisation, so no call of the entry point is in flight.
+int noalloc_take_errors(uint32_t *flags) {
+    *flags = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return record_error(LCX_ERR_CUDA, cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return LCX_OK;
+    uint32_t *addr = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_setup_mtx);
+        addr = g_scratch_addr[dev];
+    }
+    if (addr == nullptr) return LCX_OK;
+    e = cudaMemcpy(flags, addr + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && *flags != 0u) e = cudaMemset(addr + 1, 0, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return record_error(LCX_ERR_CUDA, cudaGetErrorString(e));
+    }
+    return LCX_OK;
+}
+
+}  // namespace lcx
 
 extern "C" int lcx_trace_closest_noalloc(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask,
                                          LcxTriangleHit *d_hits, void *stream) {

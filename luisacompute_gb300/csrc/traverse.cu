@@ -16,7 +16,7 @@
 //     short stack: the top kShortStack entries (8 B each) per thread in shared
 //     memory, deeper ones in local memory;
 //   * two levels: a TLAS leaf item is an instance; the ray is moved to object
-//     space with the exact FP32 sequence of lcx_device.cuh and the same loop
+//     space with the exact FP32 sequence of lcx/bvh_device.cuh and the same loop
 //     runs over the BLAS; when the stack unwinds to the entry depth the world
 //     ray is restored;
 //   * 128-bit read-only loads of nodes (5 for Node8Q, 13 for Node8F) and
@@ -25,6 +25,7 @@
 //     of traversal order; any hit stops at the first accepted triangle.
 #include "lcx_internal.h"
 #include "lcx/node_test.cuh"
+#include "lcx/trace.cuh"
 
 namespace lcx {
 namespace {
@@ -50,7 +51,6 @@ constexpr int kTraceBlock = 128;
 // entries go to local memory): a launch-time choice among 8, 16 (default) and
 // 24 for the single-job closest / any kernels; 16 for the others.
 constexpr int kDefaultShortStack = 16;
-constexpr uint32_t kMaxRaySteps = 1u << 22;  // per-ray bound: a corrupt tree ends the ray, never hangs
 
 // Loop mode 0 with the triangle tests spread over the warp (coop_triangles):
 // results identical, but measured slower on GB300 (terrain workload, closest
@@ -463,10 +463,15 @@ struct Walker {
             __stcs(hp + 1, make_uint2(__float_as_uint(best_u), __float_as_uint(best_v)));
             __stcs(hp + 2, make_uint2(__float_as_uint(best_t), 0u));
         }
+        store_counts();
+    }
+
+    // Visit counters of the counting build (per ray: nodes, triangles tested, instances entered).
+    __device__ __forceinline__ void store_counts() {
         if (kCount) {
-            P.counts[3ull * rid + 0] = c_nodes;
-            P.counts[3ull * rid + 1] = c_tris;
-            P.counts[3ull * rid + 2] = c_insts;
+            P.counts[3ull * slot + 0] = c_nodes;
+            P.counts[3ull * slot + 1] = c_tris;
+            P.counts[3ull * slot + 2] = c_insts;
         }
     }
 };
@@ -527,7 +532,7 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
             uint2 Gt = make_uint2(0, 0);
             bool tri = false;
             if (active) {
-                if (++ray_steps > kMaxRaySteps) {
+                if (++ray_steps > P.max_steps) {
                     atomicOr(P.pool + 1, 2u);
                     done = true;
                 } else {
@@ -547,7 +552,7 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
             if (active && !done && W.G.y == 0u) done = W.pop_or_done();
 #else
             if (!active) continue;
-            if (++ray_steps > kMaxRaySteps) {
+            if (++ray_steps > P.max_steps) {
                 atomicOr(P.pool + 1, 2u);
                 done = true;
             } else {
@@ -583,7 +588,7 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
                 const bool searching = has_node && Gt.y == 0u;
                 if (!__any_sync(~0u, searching)) break;
                 if (has_node && (Gt.y == 0u || Gp.y == 0u)) {
-                    if (++ray_steps > kMaxRaySteps) {
+                    if (++ray_steps > P.max_steps) {
                         atomicOr(P.pool + 1, 2u);
                         W.G = make_uint2(0, 0);
                         Gt = Gp = make_uint2(0, 0);
@@ -659,6 +664,9 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
 #ifndef LCX_DEFER_STACK
 #define LCX_DEFER_STACK 8
 #endif
+#ifndef LCX_DEFER_VISITS
+#define LCX_DEFER_VISITS 1  // node visits per step while a visit finds no items
+#endif
 constexpr int kDeferCap = LCX_DEFER_CAP;  // queued triangle tests per warp
 
 struct DeferQueue {
@@ -673,9 +681,11 @@ struct DeferQueue {
     void *ret_out[32];             // multi-job launches: the retired ray's output buffer
 };
 
-template <int kLayout, bool kAny, int kShort, bool kMulti>
+// kCount: the counting build (single-job closest hit), for the algorithmic bytes of this loop's own
+// visits: nodes visited, triangles queued (each is tested once), instances entered.
+template <int kLayout, bool kAny, int kShort, bool kMulti, bool kCount = false>
 __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_deferred(TraceParams P) {
-    using W_t = Walker<kLayout, kAny, false, kMulti, kShort>;
+    using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
     __shared__ DeferQueue queues[kTraceBlock / 32];
     uint2 deep_stack[W_t::kDeepSlots];
@@ -831,13 +841,26 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
                 W.G = make_uint2(0, 0);
                 W.sp = 0;
                 W.blas_sp = 0;
-            } else if (++ray_steps > kMaxRaySteps) {
+            } else if (++ray_steps > P.max_steps) {
                 atomicOr(P.pool + 1, 2u);
                 W.G = make_uint2(0, 0);
                 W.sp = 0;
                 W.blas_sp = 0;
             } else if (W.G.y >= 0x01000000u) {
                 W.visit(Gt);
+#if LCX_DEFER_VISITS > 1
+                // while a visit finds only internal children, take the next one in the same step
+                for (int v = 1; v < LCX_DEFER_VISITS && Gt.y == 0u && W.G.y >= 0x01000000u; v++) {
+                    if (++ray_steps > P.max_steps) {
+                        atomicOr(P.pool + 1, 2u);
+                        W.G = make_uint2(0, 0);
+                        W.sp = 0;
+                        W.blas_sp = 0;
+                        break;
+                    }
+                    W.visit(Gt);
+                }
+#endif
             } else {
                 Gt = W.G;
                 W.G = make_uint2(0, 0);
@@ -846,6 +869,7 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
 
         // 2. queue the triangles found inside a BLAS (warp-wide prefix over the lanes' counts)
         const bool has_tris = active && W.in_blas && Gt.y != 0u;
+        if (kCount && has_tris) W.c_tris += __popc(Gt.y);
         if (__any_sync(~0u, has_tris)) {
             uint32_t bits = has_tris ? Gt.y : 0u;
             const TriRec *tbase = has_tris ? W.blas_tris + Gt.x : nullptr;
@@ -914,6 +938,7 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
                         Q.ret_prim[lane] = W.best_prim;
                         Q.ret_rid[lane] = W.slot;
                         if (kMulti) Q.ret_out[lane] = W.out;
+                        W.store_counts();  // complete: its triangles were counted when queued
                         ret_occ = W.occluded;
                         retired = true;
                         mine = 0;
@@ -930,6 +955,59 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
         // 5. test the queue once it is full enough, or a finished ray is waiting on it
         if (qn >= flush_at || __any_sync(~0u, blocked)) flush();
     }
+}
+
+// ---------------------------------------------------------------------------
+// Loop mode 3: one ray per thread, each thread calling lcx::trace_closest /
+// lcx::trace_any (include/lcx/trace.cuh) with a 16-entry shared short stack --
+// exactly what a user megakernel's per-ray calls run, as a launch form of the
+// plain entry points (so the per-ray device functions are measured and
+// parity-tested through the C ABI).  No persistent warps: a warp holds its
+// lanes until its slowest ray ends.  Motion accels are traced by the same walk
+// (at each ray's time).
+template <bool kAny>
+__global__ void __launch_bounds__(kTraceBlock, LCX_TRACE_MIN_BLOCKS_Q) k_trace_per_thread(TraceParams P) {
+    constexpr int kShort = 16;
+    __shared__ uint2 sstack[kShort * kTraceBlock];
+    const uint32_t k = blockIdx.x * kTraceBlock + threadIdx.x;
+    if (k >= P.ray_count) return;
+    const uint32_t i = P.order != nullptr ? __ldg(P.order + k) : k;  // reordered calls: the k-th ray taken
+    LcxAccelView view;
+    view.tlas_nodes = P.tlas_q;
+    view.instances = P.insts;
+    view.stack_need = 0u;
+    view.motion = P.motion ? 1u : 0u;
+    const float4 *rp = reinterpret_cast<const float4 *>(P.rays + i);
+    const float4 r0 = __ldcs(rp), r1 = __ldcs(rp + 1);
+    LcxRay ray;
+    ray.origin[0] = r0.x;
+    ray.origin[1] = r0.y;
+    ray.origin[2] = r0.z;
+    ray.t_min = r0.w;
+    ray.direction[0] = r1.x;
+    ray.direction[1] = r1.y;
+    ray.direction[2] = r1.z;
+    ray.t_max = r1.w;
+    const float time = P.times != nullptr ? __ldg(P.times + i) : 0.0f;
+    LcxTriangleHit h;
+    bool occ;
+    detail::trace_walk<kAny, kShort>(view, ray, time, P.mask, ShortStack{sstack + threadIdx.x, kTraceBlock}, h, occ,
+                                     P.max_steps, P.pool + 1);
+    if (kAny) {
+        P.occluded[i] = occ ? 1 : 0;
+    } else {
+        uint2 *hp = reinterpret_cast<uint2 *>(P.hits + i);
+        __stcs(hp, make_uint2(h.inst, h.prim));
+        __stcs(hp + 1, make_uint2(__float_as_uint(h.bary[0]), __float_as_uint(h.bary[1])));
+        __stcs(hp + 2, make_uint2(__float_as_uint(h.committed_ray_t), 0u));
+    }
+}
+
+template <bool A>
+cudaError_t launch_per_thread(const TraceParams &p, cudaStream_t st) {
+    const uint64_t grid = (uint64_t(p.ray_count) + kTraceBlock - 1) / kTraceBlock;
+    k_trace_per_thread<A><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
+    return cudaGetLastError();
 }
 
 template <int L, bool A, bool C, int M, bool X, int S, int Mo = 0>
@@ -973,12 +1051,12 @@ cudaError_t launch_stack(const TraceParams &p, cudaStream_t st) {
     return launch_one<L, A, false, 0, false, kDefaultShortStack>(p, st);
 }
 
-template <int L, bool A, int S, bool X = false>
+template <int L, bool A, int S, bool X = false, bool C = false>
 cudaError_t launch_deferred(const TraceParams &p, cudaStream_t st) {
     static int per_sm = 0;
     if (per_sm == 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_deferred<L, A, S, X>, kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_deferred<L, A, S, X, C>, kTraceBlock, 0);
         per_sm = b > 0 ? b : 1;
     }
     const uint64_t warps_needed = (uint64_t(p.ray_count) + 31) / 32;
@@ -986,7 +1064,7 @@ cudaError_t launch_deferred(const TraceParams &p, cudaStream_t st) {
     const uint64_t grid_need = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
     if (grid_need < grid) grid = grid_need;
     if (grid == 0) grid = 1;
-    k_trace_deferred<L, A, S, X><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
+    k_trace_deferred<L, A, S, X, C><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -1027,6 +1105,10 @@ cudaError_t launch_ext(const TraceParams &p, int layout, bool any, bool counting
 }  // namespace
 
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
+    // loop mode 3 (one ray per thread through the device-side trace functions): single-job,
+    // quantised-node, non-counting calls, static or moving; the others run mode 0
+    if (p.mode == 3 && p.jobs == nullptr && !counting && layout == LCX_NODES_QUANT8)
+        return any ? launch_per_thread<true>(p, st) : launch_per_thread<false>(p, st);
     if (p.motion) {  // accels with motion or curves: the extended kernels, loop mode 0
         return p.curves ? launch_ext<2>(p, layout, any, counting, st) : launch_ext<1>(p, layout, any, counting, st);
     }
@@ -1040,12 +1122,15 @@ cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counti
         return any ? launch_one<LCX_NODES_FP32, true, false, 0, true>(p, st)
                    : launch_one<LCX_NODES_FP32, false, false, 0, true>(p, st);
     }
-    // deferred triangle batches: single-job quantised-node launches without counting (with FP32
-    // nodes mode 2 measured slower than mode 0, 1.06-1.10 vs 1.62 Grays/s, so those run mode 0)
-    if (p.mode == 2 && !counting && layout == LCX_NODES_QUANT8)
+    // deferred triangle batches: single-job quantised-node launches (with FP32 nodes mode 2
+    // measured slower than mode 0, 1.06-1.10 vs 1.62 Grays/s, so those run mode 0); the counting
+    // build of mode 2 counts this loop's own visits
+    if (p.mode == 2 && layout == LCX_NODES_QUANT8) {
+        if (counting) return launch_deferred<LCX_NODES_QUANT8, false, LCX_DEFER_STACK, false, true>(p, st);
         return any ? launch_deferred<LCX_NODES_QUANT8, true, LCX_DEFER_STACK>(p, st)
                    : launch_deferred<LCX_NODES_QUANT8, false, LCX_DEFER_STACK>(p, st);
-    if (p.mode == 2) return launch_mode<0>(p, layout, any, counting, st);
+    }
+    if (p.mode >= 2) return launch_mode<0>(p, layout, any, counting, st);
     return p.mode == 1 ? launch_mode<1>(p, layout, any, counting, st) : launch_mode<0>(p, layout, any, counting, st);
 }
 

@@ -53,6 +53,8 @@ class Request:
     dispatched: float = -1.0  # first launch of any of its rays (seconds after the start)
     done: float = -1.0
     result: np.ndarray | None = None
+    error: str | None = None  # the request failed (its scene could not be admitted or built)
+    cancelled: bool = False   # cancelled before all of its rays ran; its results are incomplete
 
 
 @dataclass
@@ -63,8 +65,13 @@ class _Resident:
     pins: int = 0
 
 
+class BudgetError(RuntimeError):
+    """A scene does not fit the HBM budget even with every unpinned scene evicted."""
+
+
 class SceneStore:
-    """Scenes by id: host data always, device BVHs within `budget_bytes` (LRU eviction)."""
+    """Scenes by id: host data always, device BVHs within `budget_bytes` (LRU eviction).  A scene
+    larger than the whole budget is refused (BudgetError) instead of overrunning it."""
 
     def __init__(self, scenes: dict, budget_bytes: int):
         self.host = dict(scenes)         # id -> MeshData
@@ -92,6 +99,12 @@ class SceneStore:
             torch.cuda.synchronize()
         finally:
             _capi.check(lib.lcx_set_build_split(old), "lcx_set_build_split")
+
+    @staticmethod
+    def estimate(md: S.MeshData) -> int:
+        """Device bytes of a resident scene: uploaded buffers + BVH (~0.36 wide nodes x 288 B +
+        48 B per triangle at leaf size 1)."""
+        return md.vertices.nbytes + md.triangles.nbytes + md.tri_count * 160 + (1 << 16)
 
     def resident(self, sid: int) -> bool:
         with self.lock:
@@ -151,8 +164,9 @@ class SceneStore:
                     raise ValueError(f"scene id {sid} already exists")
                 self.host[sid] = data
         md = self.host[sid]
-        # uploaded buffers + BVH (~0.36 wide nodes x 288 B + 48 B per triangle at leaf size 1)
-        est = md.vertices.nbytes + md.triangles.nbytes + md.tri_count * 160 + (1 << 16)
+        est = self.estimate(md)
+        if est > self.budget:
+            raise BudgetError(f"scene {sid} needs about {est} bytes of HBM; the budget is {self.budget}")
         with self.lock:
             victims = self._evict_for(est)
         self._destroy(victims)
@@ -224,8 +238,15 @@ class ContinuousServer:
     def __init__(self, store: SceneStore, slots: int = 4, max_batch_rays: int = 1 << 20, layout: int = 1,
                  max_wait_s: float = 0.05, min_chunk: int = 1 << 16, max_inflight_rays: int | None = 2 << 20,
                  build_priority: int = 0, max_concurrent_kernels: int | None = None,
-                 max_batch_ms: float | None = None, direct_host: bool | None = None):
+                 max_batch_ms: float | None = None, direct_host: bool | None = None, on_launch=None):
         self.store = store
+        # on_launch(server, batch): called by the serving loop after each launch, with the batch's
+        # (request, first ray, rays) pieces (progress reporting, or cancelling from the loop itself)
+        self.on_launch = on_launch
+        self._cancel = set()
+        self._cancel_lock = threading.Lock()
+        self.failed = 0
+        self.cancelled = 0
         # direct host access: on a coherent CPU-GPU link (NVLink-C2C) the trace kernel reads each
         # request's pinned rays and writes its pinned results itself, with no copies in or out;
         # None = when the device has such a link (lcx_get_host_access)
@@ -264,6 +285,13 @@ class ContinuousServer:
         self.trace_launches = 0  # lcx_trace_jobs launches one kernel per query kind in a batch
         # per batch: (launch time, completion time seen by the loop, [(request id, first ray, rays)])
         self.timeline = []
+
+    def cancel(self, rid: int) -> None:
+        """Cancel request `rid` (from any thread, before or while it runs).  Rays not yet launched
+        are dropped; launched chunks finish (a kernel is not interrupted), then the request
+        completes with ``cancelled`` set and incomplete results.  Other requests are unaffected."""
+        with self._cancel_lock:
+            self._cancel.add(rid)
 
     def _builder(self):
         import torch
@@ -333,10 +361,33 @@ class ContinuousServer:
             while done < len(reqs):
                 progressed = False
                 now = time.perf_counter() - t0
+                # cancellations: drop the unlaunched rays of cancelled requests
+                with self._cancel_lock:
+                    cancel = set(self._cancel)
+                if cancel:
+                    keep = []
+                    for r in pending:
+                        if r.rid in cancel and not r.cancelled:
+                            r.cancelled = True
+                            self.cancelled += 1
+                            r._next = r.rays.shape[0]
+                            if r._out == 0:  # nothing in flight: done now
+                                r.done = now
+                                done += 1
+                            progressed = True
+                        else:
+                            keep.append(r)
+                    pending = keep
                 # arrivals
                 while nxt < len(reqs) and reqs[nxt].arrival <= now:
                     r = reqs[nxt]
                     nxt += 1
+                    if r.rid in cancel:  # cancelled before it arrived
+                        r.cancelled = True
+                        self.cancelled += 1
+                        r.done = now
+                        done += 1
+                        continue
                     if r.new_scene is not None:
                         waiting_new.setdefault(r.scene, []).append(r)
                         if r.scene not in building:
@@ -350,10 +401,20 @@ class ContinuousServer:
                         sid, err = self.built.get_nowait()
                     except queue.Empty:
                         break
-                    if err is not None:
-                        raise err
                     progressed = True
                     building.discard(sid)
+                    if err is not None:
+                        if not isinstance(err, BudgetError):
+                            raise err
+                        # the scene cannot be admitted: its requests fail, the others go on
+                        failed = waiting_new.pop(sid, []) + [r for r in pending if r.scene == sid]
+                        pending = [r for r in pending if r.scene != sid]
+                        for r in failed:
+                            r.error = str(err)
+                            r.done = time.perf_counter() - t0
+                            self.failed += 1
+                            done += 1
+                        continue
                     pending.extend(waiting_new.pop(sid, []))
                 # completed batches
                 for sl in self.slots:
@@ -395,6 +456,8 @@ class ContinuousServer:
                     self.batches += 1
                     self.chunks += len(batch)
                     progressed = True
+                    if self.on_launch is not None:
+                        self.on_launch(self, batch)
                 if not progressed:
                     time.sleep(20e-6)  # let the builder thread run (GIL) while waiting
         finally:
@@ -471,7 +534,12 @@ class PlainServer:
             while time.perf_counter() - t0 < r.arrival:
                 pass
             if r.new_scene is not None or not self.store.resident(r.scene):
-                self.store.build(r.scene, r.new_scene, stream)
+                try:
+                    self.store.build(r.scene, r.new_scene, stream)
+                except BudgetError as e:  # the request fails; the next one goes on
+                    r.error = str(e)
+                    r.done = time.perf_counter() - t0
+                    continue
             pin = self.store.pin(r.scene)
             acc = pin.accel
             with torch.cuda.stream(stream):
@@ -500,7 +568,9 @@ def results(reqs: list) -> list:
 
 def latency_stats(reqs: list) -> dict:
     """p50/p99 latency (ms) overall, for queries on resident scenes, for requests that upload a
-    scene, and for 0.5M..2M-ray queries; aggregate Grays/s over the run."""
+    scene, and for 0.5M..2M-ray queries; aggregate Grays/s over the run.  Failed and cancelled
+    requests are left out."""
+    reqs = [r for r in reqs if r.error is None and not r.cancelled]
     lat = np.array([r.done - r.arrival for r in reqs]) * 1e3
     rays = np.array([r.rays.shape[0] for r in reqs])
     up = np.array([r.new_scene is not None for r in reqs])

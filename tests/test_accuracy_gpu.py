@@ -76,7 +76,9 @@ def _stats(oracle_mod, scene, rays, got, name):
            "steep_point_rel_max": float(dp[steep].max()), "scene_extent": ext}
     print("ACCURACY " + json.dumps(out))
     assert out["unexplained"] == 0
-    assert out["id_agreement"] >= 0.99999 or rep["disagree"] == rep["near_tie"] + rep["grazing"]
+    # both conditions: at least 99.999 % of rays agree, and every disagreement is explained
+    assert out["id_agreement"] >= 0.99999
+    assert rep["disagree"] == rep["near_tie"] + rep["grazing"]
     assert out["steep_t_rel_floored_max"] <= 1e-5
     assert out["steep_point_rel_max"] <= 1e-5
     return out

@@ -45,9 +45,24 @@ def test_tuning_knobs_round_trip_and_range_checks(lcx):
         assert lcx.lcx_set_build_tuning(2, 9) == _capi.LCX_ERR_INVALID_ARG
         assert lcx.lcx_set_build_morton(2, 0, 0) == _capi.LCX_ERR_INVALID_ARG
         assert lcx.lcx_set_trace_tuning(0, 0, 0) == _capi.LCX_ERR_INVALID_ARG
-        assert lcx.lcx_set_trace_tuning(4, 0, 3) == _capi.LCX_ERR_INVALID_ARG
+        assert lcx.lcx_set_trace_tuning(4, 0, 4) == _capi.LCX_ERR_INVALID_ARG
         assert lcx.lcx_set_build_split(ctypes.c_float(-1.0)) == _capi.LCX_ERR_INVALID_ARG
         assert A.current() == cfg  # rejected calls change nothing
     finally:
         A.apply(old)
     assert A.current() == old
+
+
+def test_step_bound_knob(lcx):
+    """The per-ray step bound is host state: default 2^22, settable, 0 restores the default,
+    larger values are rejected."""
+    v = ctypes.c_uint32(0)
+    assert lcx.lcx_get_trace_step_bound(ctypes.byref(v)) == 0 and v.value == 1 << 22
+    try:
+        assert lcx.lcx_set_trace_step_bound(5) == 0
+        assert lcx.lcx_get_trace_step_bound(ctypes.byref(v)) == 0 and v.value == 5
+        assert lcx.lcx_set_trace_step_bound((1 << 22) + 1) == _capi.LCX_ERR_INVALID_ARG
+        assert lcx.lcx_get_trace_step_bound(ctypes.byref(v)) == 0 and v.value == 5
+    finally:
+        assert lcx.lcx_set_trace_step_bound(0) == 0
+    assert lcx.lcx_get_trace_step_bound(ctypes.byref(v)) == 0 and v.value == 1 << 22

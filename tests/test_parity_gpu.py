@@ -102,6 +102,31 @@ def test_terrain_shadow_any(torch_cuda, lcx, oracle_mod, layout):
     assert 0.05 < want.mean() < 0.95
 
 
+@pytest.fixture(scope="module")
+def full_terrain(oracle_mod):
+    """The headline scene at full size: the 1024x1024 heightfield (2,093,058 triangles) and 256
+    instances of a 20,480-triangle icosphere, with its oracle."""
+    scene = S.terrain_scene()
+    return scene, oracle_mod.OracleScene(scene)
+
+
+@pytest.mark.parametrize("layout", [1, 0])
+def test_full_terrain_closest_and_any(torch_cuda, lcx, oracle_mod, full_terrain, layout):
+    """The full headline scene, 2^20 incoherent rays of the headline distribution (closest hit)
+    and 2^20 shadow rays (any hit), both node layouts, bit for bit against the oracle."""
+    scene, osc = full_terrain
+    acc, _ = gpu_scene(scene)
+    rays = S.terrain_rays(scene, 1 << 20, seed=4)
+    got = trace(acc, rays, layout)
+    assert_bit_exact(oracle_mod, osc, rays, got, osc.trace_closest(rays))
+    assert (got["inst"] > 0).sum() > 1000  # the instanced spheres are hit
+    shadow = S.terrain_shadow_rays(scene, 1 << 20, seed=5)
+    occ = trace_any(acc, shadow, layout)
+    want = osc.trace_any(shadow)
+    assert np.array_equal(occ, want)
+    assert 0.05 < want.mean() < 0.95
+
+
 def test_masks(torch_cuda, lcx, oracle_mod):
     scene = small_terrain()
     scene.inst_mask = np.array([0x01] + [0x02, 0x04] * 32, np.uint32)
@@ -296,7 +321,8 @@ def test_axis_aligned_exact_ties(torch_cuda, lcx, oracle_mod, layout):
 
 @pytest.mark.parametrize("refill,postpone,mode", [(1, 0, 0), (8, 8, 0), (16, 12, 0), (32, 32, 0), (4, 20, 0),
                                                   (4, 0, 1), (16, 0, 1), (1, 8, 1),
-                                                  (4, 0, 2), (1, 1, 2), (8, 16, 2), (32, 32, 2), (2, 5, 2)])
+                                                  (4, 0, 2), (1, 1, 2), (8, 16, 2), (32, 32, 2), (2, 5, 2),
+                                                  (4, 0, 3)])
 def test_tuning_does_not_change_results(torch_cuda, lcx, oracle_mod, refill, postpone, mode):
     import ctypes
     from luisacompute_gb300 import _capi
@@ -325,7 +351,7 @@ def test_ray_reorder_does_not_change_results(torch_cuda, lcx, oracle_mod, bits):
     for closest, any, both layouts, the counting kernel and a call below min_rays."""
     import ctypes
     from luisacompute_gb300 import _capi
-    from luisacompute_gb300.accel import rays_to_device
+    from luisacompute_gb300.accel import hits_to_numpy, rays_to_device
     lib = _capi.load()
     scene = small_terrain()
     rays = np.concatenate([S.terrain_rays(scene, 100_000, seed=15), S.terrain_shadow_rays(scene, 50_000, seed=16)])
@@ -333,8 +359,21 @@ def test_ray_reorder_does_not_change_results(torch_cuda, lcx, oracle_mod, bits):
     want = osc.trace_closest(rays)
     want_any = osc.trace_any(rays)
     acc, _ = gpu_scene(scene)
-    plain_counts = torch_cuda.zeros((rays.shape[0], 3), dtype=torch_cuda.int32, device="cuda")
-    acc.trace_closest(rays_to_device(rays), layout=1, counts=plain_counts)
+    tune = [ctypes.c_uint32(0) for _ in range(3)]
+    _capi.check(lib.lcx_get_trace_tuning(*tune), "get")
+
+    def counts_mode0():
+        # loop mode 0: a ray's walk does not depend on its neighbours (in mode 2 the queued
+        # triangle tests, and so the best t that culls nodes, depend on the warp's other rays)
+        _capi.check(lib.lcx_set_trace_tuning(tune[0].value, 0, 0), "set")
+        try:
+            c = torch_cuda.zeros((rays.shape[0], 3), dtype=torch_cuda.int32, device="cuda")
+            acc.trace_closest(rays_to_device(rays), layout=1, counts=c)
+            return c
+        finally:
+            _capi.check(lib.lcx_set_trace_tuning(tune[0].value, tune[1].value, tune[2].value), "set")
+
+    plain_counts = counts_mode0()
     old = [ctypes.c_uint32(0) for _ in range(2)]
     _capi.check(lib.lcx_get_trace_reorder(*old), "get")
     try:
@@ -343,9 +382,12 @@ def test_ray_reorder_does_not_change_results(torch_cuda, lcx, oracle_mod, bits):
             got = trace(acc, rays, layout)
             assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
             assert np.array_equal(trace_any(acc, rays, layout), want_any)
+        assert torch_cuda.equal(counts_mode0(), plain_counts)
+        # the default loop structure's counting build gives the oracle's records
         counts = torch_cuda.zeros_like(plain_counts)
-        acc.trace_closest(rays_to_device(rays), layout=1, counts=counts)
-        assert torch_cuda.equal(counts, plain_counts)  # a ray's walk does not depend on its neighbours
+        got = hits_to_numpy(acc.trace_closest(rays_to_device(rays), layout=1, counts=counts))
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+        assert counts[:, 0].min() >= 1
         _capi.check(lib.lcx_set_trace_reorder(bits, rays.shape[0] + 1), "set")  # below min_rays: not reordered
         assert np.array_equal(trace(acc, rays, 1).view(np.uint8), want.view(np.uint8))
         assert lib.lcx_set_trace_reorder(10, 0) == _capi.LCX_ERR_INVALID_ARG
