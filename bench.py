@@ -313,9 +313,24 @@ def leg_batch_build(stream, count=512):
     for _ in range(3):
         build_meshes(meshes)
     ms = _event_ms(lambda: build_meshes(meshes), 5, stream)
+    # the same meshes reserved without a build (lcx_mesh_reserve_batch): their first build captured in a
+    # CUDA graph, replayed
+    import torch
+    from luisacompute_gb300.accel import Mesh, reserve_meshes
+    res = reserve_meshes([Mesh(m.vertices, m.triangles) for m in meshes], build=False)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        build_meshes(res)
+    for _ in range(2):
+        graph.replay()
+    gms = _event_ms(graph.replay, 5, stream)
+    del graph, res
     return {"meshes": count, "triangles": int(total), "ms": ms, "mtris_per_s": total / (ms * 1e-3) / 1e6,
+            "graph_first_build_ms": gms, "graph_first_build_mtris_per_s": total / (gms * 1e-3) / 1e6,
             "what": "one lcx_mesh_build_batch over the sample per step (its host sync for the node count included), "
-                    "default build knobs"}
+                    "default build knobs; graph_first_build: the sample reserved without a build and its first "
+                    "build captured in a CUDA graph (no host sync), per replay"}
 
 
 def leg_pathtrace(scene, acc, meshes, stream, steps=5):
@@ -362,8 +377,13 @@ def leg_serving(requests=300, rate=800.0, n_scenes=16):
     store_p.warm(sorted(scenes), split=3.0)
     rp = V.PlainServer(store_p).run(clone())
     c, p = V.latency_stats(rc), V.latency_stats(rp)
+    slow = sorted(rc, key=lambda r: r.arrival - r.done)[:3]  # the slowest requests, for the tail
+    worst = [{"rid": r.rid, "rays": int(r.rays.shape[0]), "any": bool(r.any_hit), "upload": r.new_scene is not None,
+              "arrival_ms": r.arrival * 1e3, "wait_ms": (r.dispatched - r.arrival) * 1e3,
+              "run_ms": (r.done - r.dispatched) * 1e3} for r in slow]
     return {"continuous": {"p50_ms": c["p50_ms"], "p99_ms": c["p99_ms"], "grays_per_s": c["grays_per_s"],
-                           "queries_0.5M_to_2M_rays": c["queries_0.5M_to_2M_rays"]},
+                           "queries_0.5M_to_2M_rays": c["queries_0.5M_to_2M_rays"], "slowest": worst,
+                           "batches": cont.batches, "builds": store.builds, "evictions": store.evictions},
             "one_at_a_time": {"p50_ms": p["p50_ms"], "p99_ms": p["p99_ms"], "grays_per_s": p["grays_per_s"],
                               "queries_0.5M_to_2M_rays": p["queries_0.5M_to_2M_rays"]},
             "what": f"{requests} Poisson requests at {rate:g}/s, {n_scenes} resident scenes of 10k..1M triangles "

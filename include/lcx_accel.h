@@ -28,6 +28,7 @@
 #ifndef LCX_ACCEL_H
 #define LCX_ACCEL_H
 
+#include <stdbool.h>
 #include <stddef.h>
 #include <stdint.h>
 
@@ -237,6 +238,20 @@ LCX_API int lcx_procedural_destroy(uint64_t handle);
  * synchronise per mesh (cuda_primitive.cpp:74). */
 LCX_API int lcx_mesh_build_batch_reserve(const uint64_t *meshes, const LcxMeshBuildCommand *cmds,
                                          uint32_t count, void *stream);
+/* Reserves a batch without building it: the same block lcx_mesh_build_batch_reserve keeps (room
+ * for any tree over the batch's triangles: triangles + meshes wide nodes, the segment table and
+ * the initial control words on the device), allocated and uploaded with one synchronisation, and
+ * no build.  The batch's first build is then the next lcx_mesh_build_batch of the same meshes, in
+ * the same order, over the same buffers: it runs the reserved-rebuild kernels only, with no host
+ * synchronisation and no allocation of its own (stream-ordered scratch), so it can be captured in
+ * a CUDA graph together with what follows it.  Until that build has run on the stream the meshes
+ * are empty to a TLAS build.  Their statistics stay zero (node count, depth, SAH) until a
+ * synchronising build; a tree deeper than the traversal stack is reported by
+ * lcx_check_trace_errors.  Errors of the in-graph build (bad indices) go to the same asynchronous
+ * error word.  Triangle meshes without allow_update or motion.  Replaces the reference's per-mesh
+ * build with a host sync each (cuda_primitive.cpp:20-113, sync at :74). */
+LCX_API int lcx_mesh_reserve_batch(const uint64_t *meshes, const LcxMeshBuildCommand *cmds, uint32_t count,
+                                   void *stream);
 
 /* Builds (PREFER_UPDATE with allow_update: refits) on `stream`, like
  * lcx_mesh_build.  Empty boxes (min > max on an axis) are never reported. */
@@ -549,6 +564,67 @@ LCX_API int lcx_trace_closest_counts(uint64_t accel, const LcxRay *d_rays, uint3
  * entry point again after a cudaDeviceReset. */
 LCX_API int lcx_trace_closest_noalloc(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask,
                                       LcxTriangleHit *d_hits, void *stream);
+
+/* ------------------------------------------- the CPU backend's per-ray table */
+
+/* The accel table that kernels of the reference's CPU backend call per ray
+ * (defs::Accel, src/rust/luisa_compute_cpu_kernel_defs/src/lib.rs:111-125,
+ * filled per binding in src/rust/luisa_compute_backend_impl/src/cpu/stream.rs:546-560
+ * and called by the generated code, src/rust/luisa_compute_backend_impl/src/cpu/codegen/cpp.rs:1334-1350),
+ * with the same layout, field order and calling convention. */
+typedef struct __attribute__((aligned(16))) LcxMat4 {
+    float m[16]; /* column-major: m[4 * column + row] */
+} LcxMat4;
+typedef struct __attribute__((aligned(8))) LcxCpuCommittedHit {
+    uint32_t inst, prim;
+    float bary[2];
+    uint32_t hit_type; /* 0 miss, 1 triangle, 2 procedural */
+    float committed_ray_t;
+} LcxCpuCommittedHit;
+typedef struct LcxCpuProceduralHit {
+    uint32_t inst, prim;
+} LcxCpuProceduralHit;
+struct LcxCpuAccel;
+/* defs::RayQuery (lib.rs:127-141), 128 B. */
+typedef struct __attribute__((aligned(16))) LcxCpuRayQuery {
+    LcxCpuCommittedHit hit;
+    LcxRay ray;
+    uint32_t mask;
+    float cur_committed_ray_t;
+    LcxTriangleHit cur_triangle_hit;
+    LcxCpuProceduralHit cur_procedural_hit;
+    bool cur_commited;
+    bool terminate_on_first;
+    bool terminated;
+    void *user_data;
+    const struct LcxCpuAccel *accel;
+} LcxCpuRayQuery;
+typedef void (*LcxCpuHitCallback)(LcxCpuRayQuery *);
+typedef struct LcxCpuAccel {
+    const void *handle;
+    LcxTriangleHit (*trace_closest)(const void *handle, const LcxRay *ray, uint32_t mask);
+    bool (*trace_any)(const void *handle, const LcxRay *ray, uint32_t mask);
+    void (*set_instance_visibility)(const void *handle, uint32_t instance, uint32_t mask);
+    void (*set_instance_transform)(const void *handle, uint32_t instance, const LcxMat4 *transform);
+    void (*set_instance_user_id)(const void *handle, uint32_t instance, uint32_t user_id);
+    LcxMat4 (*instance_transform)(const void *handle, uint32_t instance);
+    uint32_t (*instance_user_id)(const void *handle, uint32_t instance);
+    uint32_t (*instance_visibility_mask)(const void *handle, uint32_t instance);
+    void (*ray_query)(const void *handle, LcxCpuRayQuery *rq, LcxCpuHitCallback on_triangle,
+                      LcxCpuHitCallback on_procedural);
+} LcxCpuAccel;
+/* Fills `out` for a built accel (its handle field is `accel`).  Each function
+ * is one host round trip to the GPU (tens of microseconds per ray): a
+ * compatibility form for generated code that keeps the per-ray calls; the
+ * batched entry points are the fast form.  The functions cannot return a status: on an error trace_closest
+ * returns the miss record, trace_any false, the getters their defaults, and
+ * lcx_last_error_string says why.  Instance edits take effect at the next
+ * lcx_accel_build (as the reference's CPU backend marks instances dirty);
+ * the getters read the current instance state.  ray_query runs the host
+ * callbacks on the candidates of the ray found on the GPU (at most 4096),
+ * in increasing t, with the reference's commit / terminate protocol; motion
+ * is traced at time 0, as the reference's CPU backend does. */
+LCX_API int lcx_accel_cpu_table(uint64_t accel, LcxCpuAccel *out);
 
 /* ------------------------------------------------------ wavefront path tracer */
 

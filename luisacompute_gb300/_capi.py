@@ -86,6 +86,54 @@ class LcxAccelView(ctypes.Structure):
     _fields_ = [("tlas_nodes", c_void_p), ("instances", c_void_p), ("stack_need", c_uint32), ("motion", c_uint32)]
 
 
+class LcxRay(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_float * 3), ("t_min", ctypes.c_float), ("direction", ctypes.c_float * 3),
+                ("t_max", ctypes.c_float)]
+
+
+class LcxTriangleHit(ctypes.Structure):
+    _fields_ = [("inst", c_uint32), ("prim", c_uint32), ("bary", ctypes.c_float * 2), ("committed_ray_t", ctypes.c_float),
+                ("_pad", c_uint32)]
+
+
+class LcxMat4(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_float * 16)]
+
+
+class LcxCpuCommittedHit(ctypes.Structure):
+    _fields_ = [("inst", c_uint32), ("prim", c_uint32), ("bary", ctypes.c_float * 2), ("hit_type", c_uint32),
+                ("committed_ray_t", ctypes.c_float)]
+
+
+class LcxCpuRayQuery(ctypes.Structure):
+    """defs::RayQuery (the reference's cpu_kernel_defs/src/lib.rs:127-141), 128 B."""
+    _fields_ = [("hit", LcxCpuCommittedHit), ("_a", ctypes.c_uint8 * 8), ("ray", LcxRay), ("mask", c_uint32),
+                ("cur_committed_ray_t", ctypes.c_float), ("cur_triangle_hit", LcxTriangleHit),
+                ("cur_procedural_inst", c_uint32), ("cur_procedural_prim", c_uint32), ("cur_commited", ctypes.c_bool),
+                ("terminate_on_first", ctypes.c_bool), ("terminated", ctypes.c_bool), ("_b", ctypes.c_uint8 * 5),
+                ("user_data", c_void_p), ("accel", c_void_p)]
+
+
+LcxCpuHitCallback = ctypes.CFUNCTYPE(None, ctypes.POINTER(LcxCpuRayQuery))
+CpuTraceClosest = ctypes.CFUNCTYPE(LcxTriangleHit, c_void_p, ctypes.POINTER(LcxRay), c_uint32)
+CpuTraceAny = ctypes.CFUNCTYPE(ctypes.c_bool, c_void_p, ctypes.POINTER(LcxRay), c_uint32)
+CpuSetU32 = ctypes.CFUNCTYPE(None, c_void_p, c_uint32, c_uint32)
+CpuSetTransform = ctypes.CFUNCTYPE(None, c_void_p, c_uint32, ctypes.POINTER(LcxMat4))
+CpuGetTransform = ctypes.CFUNCTYPE(LcxMat4, c_void_p, c_uint32)
+CpuGetU32 = ctypes.CFUNCTYPE(c_uint32, c_void_p, c_uint32)
+CpuRayQueryFn = ctypes.CFUNCTYPE(None, c_void_p, ctypes.POINTER(LcxCpuRayQuery), LcxCpuHitCallback,
+                                 LcxCpuHitCallback)
+
+
+class LcxCpuAccel(ctypes.Structure):
+    """The CPU backend's per-ray accel table (defs::Accel, cpu_kernel_defs/src/lib.rs:111-125)."""
+    _fields_ = [("handle", c_void_p), ("trace_closest", CpuTraceClosest), ("trace_any", CpuTraceAny),
+                ("set_instance_visibility", CpuSetU32), ("set_instance_transform", CpuSetTransform),
+                ("set_instance_user_id", CpuSetU32), ("instance_transform", CpuGetTransform),
+                ("instance_user_id", CpuGetU32), ("instance_visibility_mask", CpuGetU32),
+                ("ray_query", CpuRayQueryFn)]
+
+
 class LcxPtStats(ctypes.Structure):
     _fields_ = [("closest_rays", c_uint64), ("any_rays", c_uint64), ("bounces", c_uint32), ("ms", ctypes.c_float),
                 ("launches", c_uint32), ("_pad", c_uint32)]
@@ -129,6 +177,7 @@ _SIGS = {
     "lcx_set_build_split": (c_int, [ctypes.c_float]),
     "lcx_get_build_split": (c_int, [POINTER(ctypes.c_float)]),
     "lcx_mesh_build_batch_reserve": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
+    "lcx_mesh_reserve_batch": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
     "lcx_mesh_create_motion": (c_int, [c_void_p, c_void_p, POINTER(c_uint64)]),
     "lcx_curve_create_motion": (c_int, [c_void_p, c_void_p, POINTER(c_uint64)]),
     "lcx_motion_instance_create": (c_int, [c_uint64, c_void_p, POINTER(c_uint64)]),
@@ -140,6 +189,7 @@ _SIGS = {
     "lcx_trace_any_motion": (c_int, [c_uint64, c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, c_void_p]),
     "lcx_set_refit_sync": (c_int, [c_uint32]),
     "lcx_get_trace_stack": (c_int, [POINTER(c_uint32)]),
+    "lcx_accel_cpu_table": (c_int, [c_uint64, POINTER(LcxCpuAccel)]),
     "lcx_set_trace_step_bound": (c_int, [c_uint32]),
     "lcx_get_trace_step_bound": (c_int, [POINTER(c_uint32)]),
     "lcx_get_trace_reorder": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),

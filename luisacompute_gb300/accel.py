@@ -505,9 +505,11 @@ def build_meshes(meshes, request: int = REQUEST_FORCE_BUILD, stream=None):
     return meshes
 
 
-def reserve_meshes(meshes, stream=None):
+def reserve_meshes(meshes, stream=None, build: bool = True):
     """lcx_mesh_build_batch_reserve: build the batch and keep room to rebuild it in place (later
-    ``build_meshes`` calls of the same meshes over the same buffers, capturable in CUDA graphs)."""
+    ``build_meshes`` calls of the same meshes over the same buffers, capturable in CUDA graphs).
+    build=False: lcx_mesh_reserve_batch, the room only; the first ``build_meshes`` of the batch is
+    then already the in-place build and can itself be captured."""
     lib = _capi.load()
     n = len(meshes)
     handles = (ctypes.c_uint64 * n)(*[m.handle for m in meshes])
@@ -515,7 +517,8 @@ def reserve_meshes(meshes, stream=None):
     for i, m in enumerate(meshes):
         cmds[i] = LcxMeshBuildCommand(REQUEST_FORCE_BUILD, 0, m.vertices.data_ptr(), 0, m.vertex_size,
                                       m.vertex_stride, m.triangles.data_ptr(), 0, m.triangle_size)
-    check(lib.lcx_mesh_build_batch_reserve(handles, cmds, n, stream_handle(stream)), "lcx_mesh_build_batch_reserve")
+    fn = lib.lcx_mesh_build_batch_reserve if build else lib.lcx_mesh_reserve_batch
+    check(fn(handles, cmds, n, stream_handle(stream)), fn.__name__)
     return meshes
 
 

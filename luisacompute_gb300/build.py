@@ -18,7 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "liblcx_accel.so"
-SOURCES = ["build.cu", "traverse.cu", "capi.cu", "sort.cu", "noalloc.cu", "pathtrace.cu", "reorder.cu"]
+SOURCES = ["build.cu", "traverse.cu", "capi.cu", "sort.cu", "noalloc.cu", "pathtrace.cu", "reorder.cu", "cpu_table.cu"]
 HEADERS = ["lcx_internal.h", "pt_math.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
@@ -32,7 +32,8 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblcx_accel.so")
 
 
-PUBLIC_HEADERS = ["lcx_accel.h", "lcx/bvh_device.cuh", "lcx/node_test.cuh", "lcx/accel_instances.cuh"]
+PUBLIC_HEADERS = ["lcx_accel.h", "lcx/bvh_device.cuh", "lcx/node_test.cuh", "lcx/accel_instances.cuh", "lcx/trace.cuh",
+                  "lcx/ray_query.cuh"]
 
 
 def _stamp() -> str:

@@ -580,6 +580,73 @@ int try_reserved_rebuild(const std::vector<MeshObj *> &meshes, const std::vector
     return LCX_OK;
 }
 
+// Reserves a batch without building it: the block a reserved batch has (room for any tree over the
+// items, the segment table and the initial control words on the device) and nothing else, so the
+// batch's first build -- the next lcx_mesh_build_batch of the same meshes over the same buffers,
+// which takes the reserved-rebuild path -- needs no host synchronisation and can be captured in a
+// CUDA graph.  The meshes count as built (their descriptors are zero, i.e. empty, until that build
+// runs); their statistics stay zero until a synchronising build.
+int reserve_only(const std::vector<MeshObj *> &meshes, const std::vector<SegInput> &segs, cudaStream_t st,
+                 Retired &retired) {
+    const size_t count = meshes.size();
+    uint64_t total = 0;
+    for (const SegInput &g : segs) total += g.item_count;
+    if (total == 0) return fail(LCX_ERR_INVALID_ARG, "a reserved batch needs triangles");
+    if (total + count >= (1ull << 31)) return fail(LCX_ERR_INVALID_ARG, "too many triangles in one batch");
+    const uint32_t n_items = uint32_t(total);
+    // every wide node opens a binary node or is a segment root: at most items + segments of them
+    const uint32_t W_alloc = uint32_t(uint64_t(n_items) + count);
+    const size_t q_bytes = size_t(W_alloc) * sizeof(Node8Q), f_bytes = size_t(W_alloc) * sizeof(Node8F);
+    const size_t t_bytes = size_t(n_items) * sizeof(TriRec), sah_bytes = 2 * sizeof(double) * count;
+    const size_t res_bytes = sizeof(SegInput) * count + sizeof(uint32_t) * kSegWords * count;
+    auto block = std::make_shared<DevBlock>();
+    block->bytes = q_bytes + f_bytes + t_bytes + sah_bytes + res_bytes;
+    LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(reserved BLAS block)");
+    char *base = static_cast<char *>(block->ptr);
+    block->qn = reinterpret_cast<Node8Q *>(base);
+    block->fn = reinterpret_cast<Node8F *>(base + q_bytes);
+    block->tris = reinterpret_cast<TriRec *>(base + q_bytes + f_bytes);
+    block->wsah = reinterpret_cast<double *>(base + q_bytes + f_bytes + t_bytes);
+    char *rp = base + q_bytes + f_bytes + t_bytes + sah_bytes;
+    block->d_segs = reinterpret_cast<SegInput *>(rp);
+    block->d_segctl_init = reinterpret_cast<uint32_t *>(rp + sizeof(SegInput) * count);
+    block->h_segs = segs;
+    block->reserved = true;
+    block->items = n_items;
+    block->cap_wide = W_alloc;
+    block->wide = 0;
+    block->nseg = uint32_t(count);
+    std::vector<uint32_t> init(size_t(kSegWords) * count, 0u);
+    for (size_t i = 0; i < count; i++)
+        for (int k = 0; k < 3; k++) init[size_t(kSegWords) * i + kSegCenLo + k] = 0xffffffffu;
+    LCX_CUDA(cudaMemcpyAsync(block->d_segs, segs.data(), sizeof(SegInput) * count, cudaMemcpyHostToDevice, st),
+             "reserve segment table");
+    LCX_CUDA(cudaMemcpyAsync(block->d_segctl_init, init.data(), sizeof(uint32_t) * init.size(), cudaMemcpyHostToDevice,
+                             st),
+             "reserve control words");
+    LCX_CUDA(cudaMemsetAsync(block->wsah, 0, sah_bytes, st), "cudaMemset");
+    // the host vectors above are read by the copies: wait for them (one sync at reservation, none later)
+    LCX_CUDA(cudaStreamSynchronize(st), "reserve sync");
+    for (size_t i = 0; i < count; i++) {
+        MeshObj *m = meshes[i];
+        LCX_CUDA(cudaMemset(m->d_desc, 0, sizeof(BlasDesc)), "cudaMemset(BlasDesc)");
+        if (m->block) retired.blocks.push_back(std::move(m->block));
+        m->block = block;
+        m->seg = uint32_t(i);
+        m->wide_sah = block->wsah + 2 * i;
+        m->refits = 0;
+        m->node_count = 0;
+        m->depth = 0;  // unknown until a synchronising build; the traversal flags a stack overflow
+        m->tri_count = m->ref_count = segs[i].item_count;
+        m->mem_bytes = size_t(m->tri_count) * sizeof(TriRec);
+        m->sah = 0.0;
+        m->built = true;
+        m->generation++;
+    }
+    bump_mesh_epoch();
+    return LCX_OK;
+}
+
 int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInput> &segs,
                  const std::vector<uint32_t> &requests, cudaStream_t st, Retired &retired, bool reserve = false) {
     const size_t count = meshes.size();
@@ -1211,6 +1278,39 @@ int lcx_mesh_build_batch_reserve(const uint64_t *meshes, const LcxMeshBuildComma
     for (const SegInput &g : segs) total += g.item_count;
     if (total == 0) return fail(LCX_ERR_INVALID_ARG, "a reserved batch needs triangles");
     return build_meshes(order, segs, req, st, retired, true);
+}
+
+int lcx_mesh_reserve_batch(const uint64_t *meshes, const LcxMeshBuildCommand *cmds, uint32_t count, void *stream) {
+    if (count == 0) return LCX_OK;
+    if (!meshes || !cmds) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_reserve_batch: null arguments");
+    std::vector<std::shared_ptr<MeshObj>> objs(count);
+    for (uint32_t i = 0; i < count; i++) {
+        objs[i] = find_mesh(meshes[i]);
+        if (!objs[i]) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_reserve_batch: unknown mesh handle %llu",
+                                  (unsigned long long)meshes[i]);
+        if (objs[i]->opt.allow_update)
+            return fail(LCX_ERR_INVALID_ARG, "a reserved batch is rebuilt, not refit (allow_update)");
+        if (objs[i]->motion.keyframe_count >= 2) return fail(LCX_ERR_INVALID_ARG, "motion meshes cannot be reserved");
+    }
+    std::vector<MeshObj *> order(count);
+    for (uint32_t i = 0; i < count; i++) order[i] = objs[i].get();
+    std::vector<MeshObj *> sorted = order;
+    std::sort(sorted.begin(), sorted.end());
+    for (uint32_t i = 1; i < count; i++)
+        if (sorted[i] == sorted[i - 1]) return fail(LCX_ERR_INVALID_ARG, "a mesh appears twice");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (capturing(st)) return fail(LCX_ERR_INVALID_ARG, "lcx_mesh_reserve_batch cannot be captured (it allocates)");
+    NvtxRange nr("lcx_mesh_reserve_batch");
+    Retired retired;
+    std::vector<std::unique_lock<std::mutex>> locks;
+    locks.reserve(count);
+    for (MeshObj *m : sorted) locks.emplace_back(m->mtx);
+    std::vector<SegInput> segs;
+    std::vector<uint32_t> req;
+    if (int r = mesh_segments(order, cmds, segs, req)) return r;
+    for (const SegInput &g : segs)
+        if (g.kind != kSegTriangles) return fail(LCX_ERR_INVALID_ARG, "a reserved batch holds triangle meshes");
+    return reserve_only(order, segs, st, retired);
 }
 
 int lcx_mesh_stats(uint64_t mesh, LcxAccelStats *out) {

@@ -669,6 +669,7 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
 #endif
 constexpr int kDeferCap = LCX_DEFER_CAP;  // queued triangle tests per warp
 
+template <bool kMulti>
 struct DeferQueue {
     const TriRec *tri[kDeferCap];
     uint32_t rec[kDeferCap];       // ray record: lane | slot << 5
@@ -678,7 +679,7 @@ struct DeferQueue {
     float tmax[64];                // per record: the owner's best t at the flush
     float ret_t[32], ret_u[32], ret_v[32];
     uint32_t ret_inst[32], ret_prim[32], ret_rid[32];
-    void *ret_out[32];             // multi-job launches: the retired ray's output buffer
+    void *ret_out[kMulti ? 32 : 1];  // multi-job launches: the retired ray's output buffer
 };
 
 // kCount: the counting build (single-job closest hit), for the algorithmic bytes of this loop's own
@@ -687,10 +688,10 @@ template <int kLayout, bool kAny, int kShort, bool kMulti, bool kCount = false>
 __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_deferred(TraceParams P) {
     using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
-    __shared__ DeferQueue queues[kTraceBlock / 32];
+    __shared__ DeferQueue<kMulti> queues[kTraceBlock / 32];
     uint2 deep_stack[W_t::kDeepSlots];
     const uint32_t lane = threadIdx.x & 31u;
-    DeferQueue &Q = queues[threadIdx.x >> 5];
+    DeferQueue<kMulti> &Q = queues[threadIdx.x >> 5];
     W_t W(P, stack_mem + threadIdx.x, deep_stack);
     const int refill = int(P.refill);
     // queue size that starts a flush: P.postpone, or 24 for closest / 16 for any hit (measured on the

@@ -392,3 +392,39 @@ def test_reserved_batch_rebuild_in_cuda_graph(lcx, oracle_mod):
     acc.build()
     frame = [S.MeshData(v.cpu().numpy(), md.triangles) for v, md in zip(moved, datas)]
     _check_scene(oracle_mod, acc, S.Scene(frame, np.arange(n), aff, masks), rays, layouts=(1,))
+
+
+def test_first_build_in_cuda_graph(lcx, oracle_mod):
+    """lcx_mesh_reserve_batch allocates the room of a reserved batch and builds nothing; the
+    batch's first build is then captured in a CUDA graph (no host sync, no allocation of its own)
+    and replayed.  The TLAS built afterwards traces the oracle's records; a replay after the
+    vertices moved rebuilds the trees in place, and a TLAS rebuild traces the new vertices."""
+    import torch
+    from luisacompute_gb300 import _capi
+    from luisacompute_gb300.accel import Accel, build_meshes, reserve_meshes
+    rng = np.random.default_rng(71)
+    datas = [S.displaced_mesh(int(n), rng) for n in (700, 9_000, 30_000, 2_500, 64)]
+    meshes = reserve_meshes(_device(datas, allow_update=False), build=False)
+    assert all(int(m.stats().node_count) == 0 for m in meshes)  # reserved, not built
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        build_meshes(meshes)  # the first build of these meshes, inside the capture
+    g.replay()
+    torch.cuda.synchronize()
+    _capi.check(lcx.lcx_check_trace_errors(), "in-graph build errors")
+    n = len(meshes)
+    aff = _placements(rng, n, spread=1.0)
+    masks = np.full(n, 0xFF, np.uint32)
+    acc = Accel()
+    acc.emplace_back_many(meshes, aff)
+    acc.build()
+    rays = S.sphere_rays(40_000, [-2.0] * 3, [2.0] * 3, seed=72)
+    _check_scene(oracle_mod, acc, S.Scene(datas, np.arange(n), aff, masks), rays)
+    # move the vertices, replay the same graph, rebuild the TLAS: the new geometry
+    datas = [_deform(md, rng, 0.08, 1.3) for md in datas]
+    for m, md in zip(meshes, datas):
+        m.vertices.copy_(torch.from_numpy(md.vertices).cuda())
+    g.replay()
+    acc.build()
+    _check_scene(oracle_mod, acc, S.Scene(datas, np.arange(n), aff, masks), rays)
