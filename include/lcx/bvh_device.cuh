@@ -223,7 +223,7 @@ __device__ __forceinline__ void affine_inverse(const float *m, float *w) {
     const float c01 = __fmaf_rn(f, g, -__fmul_rn(d, i));
     const float c02 = __fmaf_rn(d, h, -__fmul_rn(e, g));
     const float det = __fmaf_rn(a, c00, __fmaf_rn(b, c01, __fmul_rn(c, c02)));
-    const float r = __fdiv_rn(1.0f, det);
+    const float r = __frcp_rn(det);  // the correctly rounded 1 / det
     float R[9];
     R[0] = __fmul_rn(c00, r);
     R[1] = __fmul_rn(__fmaf_rn(c, h, -__fmul_rn(b, i)), r);
@@ -257,7 +257,7 @@ __device__ __forceinline__ void srt_matrix(const float *v, float m[12]) {
     const float sx = v[7], sy = v[8], sz = v[9], a = v[10], b = v[11], c = v[12];
     const float tx = v[13], ty = v[14], tz = v[15];
     const float n2 = __fmaf_rn(qx, qx, __fmaf_rn(qy, qy, __fmaf_rn(qz, qz, __fmul_rn(qw, qw))));
-    const float rn = __fdiv_rn(1.0f, __fsqrt_rn(n2));
+    const float rn = __frcp_rn(__fsqrt_rn(n2));
     qx = __fmul_rn(qx, rn);
     qy = __fmul_rn(qy, rn);
     qz = __fmul_rn(qz, rn);
@@ -379,7 +379,7 @@ __device__ __forceinline__ WtRay wt_setup(float ox, float oy, float oz, float dx
         ky = t;
     }
     const float dkx = pick3(kx, dx, dy, dz), dky = pick3(ky, dx, dy, dz);
-    r.Sz = __fdiv_rn(1.0f, dkz);
+    r.Sz = __frcp_rn(dkz);  // the correctly rounded 1 / dkz (IEEE reciprocal)
     r.Sx = __fmul_rn(dkx, r.Sz);
     r.Sy = __fmul_rn(dky, r.Sz);
     r.perm = kx | (ky << 2) | (kz << 4);

@@ -82,8 +82,9 @@ typedef struct LcxTriangle {
     uint32_t i0, i1, i2;
 } LcxTriangle;
 
-/* AccelOption: include/luisa/runtime/rhi/resource.h:94-125 (motion omitted:
- * motion blur is not on this path). */
+/* AccelOption: include/luisa/runtime/rhi/resource.h:94-125.  Its motion part
+ * is LcxMotionOption, taken by lcx_mesh_create_motion, lcx_curve_create_motion
+ * and lcx_motion_instance_create. */
 enum { LCX_HINT_FAST_TRACE = 0, LCX_HINT_FAST_BUILD = 1 };
 typedef struct LcxAccelOption {
     uint32_t hint;            /* LCX_HINT_FAST_TRACE | LCX_HINT_FAST_BUILD */
@@ -708,6 +709,13 @@ LCX_API int lcx_get_build_morton(uint32_t *blas_cube, uint32_t *tlas_cube, uint3
  * reference's OptiX and Embree builders). */
 LCX_API int lcx_set_build_split(float fraction);
 LCX_API int lcx_get_build_split(float *fraction);
+/* Leaf-slot filling for later BLAS builds (0 or 1): once no child of a wide
+ * node can become a wide node itself, its free slots are filled by splitting
+ * leaf slots (largest area first) into slots of fewer triangles.  The node
+ * count and the cost of a node test stay the same; a ray tests fewer
+ * triangles.  Default 1.  Results do not depend on it. */
+LCX_API int lcx_set_build_fill(uint32_t fill);
+LCX_API int lcx_get_build_fill(uint32_t *fill);
 
 /* Traversal knobs, process-wide (no counterpart in the reference: OptiX and
  * Embree pick theirs internally).  refill: a warp takes new rays once at

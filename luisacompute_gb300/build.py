@@ -79,14 +79,5 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
-def build_oracle() -> Path:
-    """Build the CPU oracle (test infrastructure) with its own Makefile."""
-    r = subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    return ROOT / "oracle" / "liblcx_oracle.so"
-
-
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))
-    print(build_oracle())

@@ -848,9 +848,12 @@ struct TreeView {
 // Open up to `width` children of binary node b, assign them to octant slots
 // and allocate their wide-node / item ranges.  desc: 12 words per wide node
 // (binary node, child base, item base, segment, 8 slot children).
+// fill: slots still free once no child can become a wide node are filled by
+// splitting leaf slots (largest area first) into finer ones -- no new wide
+// node, the node test costs the same, and a ray tests fewer triangles.
 __device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t b, uint32_t w, uint32_t seg,
-                              int leaf_max, int width, uint32_t *desc, uint2 *qout, uint32_t *ctl, uint32_t *segctl,
-                              int level) {
+                              int leaf_max, int width, int fill, uint32_t *desc, uint2 *qout, uint32_t *ctl,
+                              uint32_t *segctl, int level) {
     uint32_t C[8];
     float A[8];
     int nC;
@@ -872,6 +875,26 @@ __device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t
         float best_a = -1.0f;
         for (int k = 0; k < nC; k++) {
             if (!tv.leaf(C[k]) && tv.count(C[k]) > uint32_t(leaf_max) && A[k] > best_a) {
+                best_a = A[k];
+                best = k;
+            }
+        }
+        if (best < 0) break;
+        const uint32_t x = C[best];
+        C[best] = tv.child[2 * x];
+        C[nC] = tv.child[2 * x + 1];
+        float4 l, h;
+        tv.box(C[best], l, h);
+        A[best] = box_area(l, h);
+        tv.box(C[nC], l, h);
+        A[nC] = box_area(l, h);
+        nC++;
+    }
+    while (fill && nC < width) {  // every child is a leaf slot now: split the largest splittable one
+        int best = -1;
+        float best_a = -1.0f;
+        for (int k = 0; k < nC; k++) {
+            if (!tv.leaf(C[k]) && A[k] > best_a) {
                 best_a = A[k];
                 best = k;
             }
@@ -972,8 +995,8 @@ __global__ void k_collapse_init(const SegInput *segs, uint32_t nseg, uint32_t *s
     segctl[kSegWords * s + kSegNodes] = 1u;
 }
 
-__global__ void k_collapse(TreeView tv, const SegInput *segs, int leaf_max, int width, uint32_t *desc, uint2 *q0,
-                           uint2 *q1, uint32_t *ctl, uint32_t *segctl) {
+__global__ void k_collapse(TreeView tv, const SegInput *segs, int leaf_max, int width, int fill, uint32_t *desc,
+                           uint2 *q0, uint2 *q1, uint32_t *ctl, uint32_t *segctl) {
     cg::grid_group grid = cg::this_grid();
     int level = 0;
     for (; level < kMaxLevels; level++) {
@@ -984,7 +1007,7 @@ __global__ void k_collapse(TreeView tv, const SegInput *segs, int leaf_max, int 
         for (unsigned long long t = grid.thread_rank(); t < cnt; t += grid.size()) {
             const uint2 task = qin[t];
             const uint32_t seg = tv.segment(task.x);
-            collapse_node(tv, segs, task.x, task.y, seg, leaf_max, width, desc, qout, ctl, segctl, level);
+            collapse_node(tv, segs, task.x, task.y, seg, leaf_max, width, fill, desc, qout, ctl, segctl, level);
         }
         grid.sync();
     }
@@ -1377,11 +1400,11 @@ cudaError_t build_common(BuildScratch &s, const BuildParams &bp, cudaStream_t st
     k_collapse_init<<<blocks_for(s.nseg, 256), 256, 0, st>>>(s.segs, s.nseg, s.segctl, s.queue, s.desc, s.ctl);
     TreeView tv = make_view(s);
     const SegInput *segs = s.segs;
-    int lm = bp.leaf_max, width = bp.width;
+    int lm = bp.leaf_max, width = bp.width, fill = bp.fill ? 1 : 0;
     uint32_t *desc = s.desc;
     uint2 *q0 = s.queue, *q1 = s.queue + s.queue_len;
     uint32_t *ctl = s.ctl, *segctl = s.segctl;
-    void *args[] = {&tv, &segs, &lm, &width, &desc, &q0, &q1, &ctl, &segctl};
+    void *args[] = {&tv, &segs, &lm, &width, &fill, &desc, &q0, &q1, &ctl, &segctl};
     return cudaLaunchCooperativeKernel(reinterpret_cast<void *>(k_collapse), dim3(collapse_grid()), dim3(128), args, 0,
                                        st);
 }

@@ -388,6 +388,10 @@ struct BuildTuning {
     // it takes 0.61 -> 0.68 / 1.00 Grays/s (nodes per ray 27.7 -> 13.0 at 3).  The
     // autotuner and callers with such meshes turn it on.
     float split = 0.0f;
+    // leaf-slot filling (lcx_set_build_fill), on: on the terrain workload triangle tests per ray fall
+    // 3.00 -> 2.64 with the same 343k wide nodes (closest 2.020 -> 2.030 Grays/s in loop mode 2,
+    // 1.660 -> 1.716 in mode 0)
+    uint32_t fill = 1;
 };
 BuildTuning g_build_tune;
 
@@ -397,6 +401,7 @@ BuildParams build_params_for(const LcxAccelOption &o) {
     bp.width = g_build_tune.width;
     bp.cube = g_build_tune.blas_cube;
     bp.split = (o.hint == LCX_HINT_FAST_TRACE && !o.allow_update) ? g_build_tune.split : 0.0f;
+    bp.fill = g_build_tune.fill;
     return bp;
 }
 
@@ -1628,6 +1633,18 @@ int lcx_accel_stats(uint64_t accel, LcxAccelStats *out) {
         LCX_CUDA(cudaMemcpy(h, a->wide_sah, sizeof(h), cudaMemcpyDeviceToHost), "wide SAH readback");
         out->wide_sah_cost = h[1] > 0.0 ? h[0] / h[1] : 0.0;
     }
+    return LCX_OK;
+}
+
+int lcx_set_build_fill(uint32_t fill) {
+    if (fill > 1) return fail(LCX_ERR_INVALID_ARG, "lcx_set_build_fill: 0 or 1");
+    g_build_tune.fill = fill;
+    return LCX_OK;
+}
+
+int lcx_get_build_fill(uint32_t *fill) {
+    if (!fill) return fail(LCX_ERR_INVALID_ARG, "null output");
+    *fill = g_build_tune.fill;
     return LCX_OK;
 }
 

@@ -89,6 +89,7 @@ struct BuildParams {
     uint32_t size_bits = 0;  // extended-Morton size-class bits (TLAS builds)
     uint32_t cube = 1;       // normalise centroids by the largest extent on every axis (else per axis)
     float split = 0.0f;      // triangle splitting: extra references, as a fraction of the triangles (0 = off)
+    uint32_t fill = 0;       // BLAS collapse: split leaf slots into finer ones while slots are free
 };
 
 // Per-build device scratch, sized for n items in nseg segments.

@@ -60,6 +60,22 @@ constexpr int kDefaultShortStack = 16;
 #ifndef LCX_COOP_TRIS
 #define LCX_COOP_TRIS 0
 #endif
+// Measured without effect on the terrain workload, so off: loading an instance record's rows before
+// its mask test (one round trip instead of two: 1.975 -> 1.965 Grays/s) and the triangle-queue
+// prefix from one ballot per bit instead of a shuffle scan (1.975 -> 1.961).
+#ifndef LCX_INST_LOADS_FIRST
+#define LCX_INST_LOADS_FIRST 0
+#endif
+#ifndef LCX_QUEUE_BALLOT
+#define LCX_QUEUE_BALLOT 0
+#endif
+// Deferred kernel: ray ids a warp takes from the global counter at a time (0 = just its idle lanes'
+// count), the chunk's rays prefetched into L2 when it is taken.  Measured on the terrain workload
+// (closest / any Grays/s): 0: 1.975 / 3.34; 32: 2.023 / 3.45; 64: 2.025 / 3.47; 128: 1.996 / 3.45
+// (the end of the launch waits on the larger chunks).
+#ifndef LCX_RAY_CHUNK
+#define LCX_RAY_CHUNK 64
+#endif
 #ifndef LCX_PREFETCH
 #define LCX_PREFETCH 0  // 1: prefetch the next node into L1 (measured: 1.77 -> 1.66 Grays/s, so off)
 #endif
@@ -382,10 +398,18 @@ struct Walker {
             const uint4 m4 = bvh_ld(ip + 4);  // fnodes (x,y), inst_id (z), mask (w)
             float w[12];
             if constexpr (!kExt) {
+#if LCX_INST_LOADS_FIRST
+                // the whole record in one round trip, before the mask test (a masked-out instance wastes it)
+                const float4 r0 = bvh_ld(reinterpret_cast<const float4 *>(ip));
+                const float4 r1 = bvh_ld(reinterpret_cast<const float4 *>(ip + 1));
+                const float4 r2 = bvh_ld(reinterpret_cast<const float4 *>(ip + 2));
+                if ((m4.w & (kMulti ? mask : P.mask)) == 0u) continue;
+#else
                 if ((m4.w & (kMulti ? mask : P.mask)) == 0u) continue;
                 const float4 r0 = bvh_ld(reinterpret_cast<const float4 *>(ip));
                 const float4 r1 = bvh_ld(reinterpret_cast<const float4 *>(ip + 1));
                 const float4 r2 = bvh_ld(reinterpret_cast<const float4 *>(ip + 2));
+#endif
                 w[0] = r0.x, w[1] = r0.y, w[2] = r0.z, w[3] = r0.w;
                 w[4] = r1.x, w[5] = r1.y, w[6] = r1.z, w[7] = r1.w;
                 w[8] = r2.x, w[9] = r2.y, w[10] = r2.z, w[11] = r2.w;
@@ -664,8 +688,10 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
 #ifndef LCX_DEFER_STACK
 #define LCX_DEFER_STACK 8
 #endif
+// Node visits per step while a visit finds no items: 2 and 3 measured slower (1.975 -> 1.765 /
+// 1.531 Grays/s; 1.898 at 6 blocks per SM): the extra visits run with few lanes and cost registers.
 #ifndef LCX_DEFER_VISITS
-#define LCX_DEFER_VISITS 1  // node visits per step while a visit finds no items
+#define LCX_DEFER_VISITS 1
 #endif
 constexpr int kDeferCap = LCX_DEFER_CAP;  // queued triangle tests per warp
 
@@ -701,6 +727,9 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
 
     bool active = false, exhausted = false;
     uint32_t rid = 0, ray_steps = 0;
+#if LCX_RAY_CHUNK
+    uint32_t chunk_next = 0, chunk_end = 0;  // warp-uniform: ray ids this warp has taken and not yet started
+#endif
     uint32_t qn = 0;        // queued entries (warp-uniform)
     uint32_t pend = 0;      // bit s: a queued entry uses this lane's record s
     uint32_t mine = 0;      // bit s: record s belongs to the lane's current ray (else to the retired one)
@@ -814,6 +843,36 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
         const uint32_t idle = __ballot_sync(~0u, !active);
         const int n_idle = __popc(idle);
         if (!exhausted && n_idle >= refill) {
+#if LCX_RAY_CHUNK
+            // the warp takes LCX_RAY_CHUNK ids at a time from the global counter and serves its idle
+            // lanes from them: one atomic per chunk, and the chunk's rays prefetched into L2 at once
+            if (chunk_next >= chunk_end) {
+                uint32_t base = 0;
+                if (lane == 0) base = atomicAdd(P.pool, uint32_t(LCX_RAY_CHUNK));
+                base = __shfl_sync(~0u, base, 0);
+                chunk_next = base;
+                chunk_end = uint32_t(min(uint64_t(base) + LCX_RAY_CHUNK, uint64_t(P.ray_count)));
+                if (chunk_next > chunk_end) chunk_next = chunk_end;
+                if (!kMulti && P.order == nullptr) {
+                    for (uint32_t r = base + lane; r < chunk_end; r += 32u)
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(P.rays + r));
+                }
+            }
+            const uint32_t base = chunk_next;
+            const uint32_t take = min(uint32_t(n_idle), chunk_end - chunk_next);
+            chunk_next += take;
+            if (chunk_next >= chunk_end && chunk_end >= P.ray_count) exhausted = true;
+            if (!active) {
+                const uint32_t k = __popc(idle & ((1u << lane) - 1u));
+                if (k < take) {
+                    rid = base + k;
+                    active = true;
+                    ray_steps = 0;
+                    mine = 0;
+                    W.start(rid);
+                }
+            }
+#else
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(P.pool, uint32_t(n_idle));
             base = __shfl_sync(~0u, base, 0);
@@ -828,6 +887,7 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
                     W.start(rid);
                 }
             }
+#endif
         }
         if (__ballot_sync(~0u, active) == 0u) {
             if (qn != 0u || __any_sync(~0u, retired)) flush();
@@ -876,6 +936,21 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
             const TriRec *tbase = has_tris ? W.blas_tris + Gt.x : nullptr;
             for (;;) {
                 const uint32_t cnt = __popc(bits);
+#if LCX_QUEUE_BALLOT
+                // exclusive prefix and total of the lanes' counts (< 32) from one ballot per bit:
+                // independent votes instead of a chain of dependent shuffles
+                uint32_t excl = 0u, total = 0u;
+                const uint32_t below = (1u << lane) - 1u;
+#pragma unroll
+                for (int b = 0; b < 5; b++) {
+                    const uint32_t m = __ballot_sync(~0u, (cnt >> b) & 1u);
+                    excl += uint32_t(__popc(m & below)) << b;
+                    total += uint32_t(__popc(m)) << b;
+                }
+                if (total == 0u) break;
+                const uint32_t space = uint32_t(kDeferCap) - qn;
+                uint32_t pos = qn + excl;
+#else
                 uint32_t incl = cnt;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -886,6 +961,7 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
                 if (total == 0u) break;
                 const uint32_t space = uint32_t(kDeferCap) - qn;
                 uint32_t pos = qn + incl - cnt;
+#endif
                 while (bits != 0u && pos < uint32_t(kDeferCap)) {
                     const uint32_t k = __ffs(bits) - 1u;
                     bits &= bits - 1u;

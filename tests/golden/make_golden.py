@@ -1,9 +1,9 @@
 """Generates tests/golden/cornell_box.npz: seeded inputs and the oracle's outputs on the
 Cornell box of the reference's own tests.
 
-Run from the repository root, in a checkout that has the reference next to it:
+Run from the repository root, with the path of a LuisaCompute checkout (required):
 
-    python tests/golden/make_golden.py [path/to/LuisaCompute]
+    python tests/golden/make_golden.py path/to/LuisaCompute
 
 Scene.  The geometry is the OBJ text that LuisaCompute's path-tracing tests embed
 (src/tests/common/cornell_box.h; "Released into the Public Domain" by its authors,
@@ -129,4 +129,6 @@ def load():
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the LuisaCompute checkout>")
+    main(Path(sys.argv[1]))
