@@ -25,6 +25,7 @@
 //             shared pools; a segment's root is wide node s, its indices are
 //             stored relative to it, its items relative to its item offset
 #include <cooperative_groups.h>
+#include <cooperative_groups/scan.h>
 
 #include <cfloat>
 
@@ -36,6 +37,19 @@ namespace cg = cooperative_groups;
 
 namespace lcx {
 namespace {
+
+#ifndef LCX_OCTANT_FAST
+#define LCX_OCTANT_FAST 1
+#endif
+#ifndef LCX_COLLAPSE_AGG
+#define LCX_COLLAPSE_AGG 1
+#endif
+#ifndef LCX_QUANT_MUL
+#define LCX_QUANT_MUL 1
+#endif
+#ifndef LCX_COLLAPSE_BLOCKS
+#define LCX_COLLAPSE_BLOCKS 2  // resident blocks per SM of the cooperative collapse
+#endif
 
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr int kPrepBlock = 256;
@@ -928,27 +942,47 @@ __device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t
     }
     uint32_t slot_child[8];
     for (int s = 0; s < 8; s++) slot_child[s] = kInvalid;
-    uint32_t used_slots = 0, used_children = 0;
-    for (int it = 0; it < nC; it++) {
-        float best = -INFINITY;
-        int bk = -1, bs = -1;
-        for (int k = 0; k < nC; k++) {
-            if (used_children >> k & 1u) continue;
+    // Each child's best slot is the octant of its offset's signs (it maximises the dot product with
+    // the octant diagonal).  When those octants are distinct, the greedy assignment below gives
+    // exactly them, so it is skipped: nearly every node, at a fraction of the greedy's cost.
+    uint32_t pref[8], pref_used = 0;
+    bool distinct = LCX_OCTANT_FAST != 0;
+    for (int k = 0; k < nC; k++) {
+        pref[k] = (off[k][0] < 0.0f ? 1u : 0u) | (off[k][1] < 0.0f ? 2u : 0u) | (off[k][2] < 0.0f ? 4u : 0u);
+        // a zero or NaN component ties two slots: leave those nodes to the greedy
+        const bool clear = fabsf(off[k][0]) > 0.0f && fabsf(off[k][1]) > 0.0f && fabsf(off[k][2]) > 0.0f;
+        distinct = distinct && clear && !(pref_used >> pref[k] & 1u);
+        pref_used |= 1u << pref[k];
+    }
+    if (distinct) {
+        for (int k = 0; k < nC; k++) slot_child[pref[k]] = C[k];
+    } else {
+        float cost[8][8];  // dot(offset, octant diagonal) per child and slot
+        for (int k = 0; k < nC; k++)
             for (int s = 0; s < 8; s++) {
-                if (used_slots >> s & 1u) continue;
-                float sc = ((s & 1) ? -off[k][0] : off[k][0]) + ((s & 2) ? -off[k][1] : off[k][1]) +
-                           ((s & 4) ? -off[k][2] : off[k][2]);
-                if (!(sc == sc)) sc = -FLT_MAX;  // NaN never blocks an assignment
-                if (bk < 0 || sc > best) {
-                    best = sc;
-                    bk = k;
-                    bs = s;
+                const float sc = ((s & 1) ? -off[k][0] : off[k][0]) + ((s & 2) ? -off[k][1] : off[k][1]) +
+                                 ((s & 4) ? -off[k][2] : off[k][2]);
+                cost[k][s] = sc == sc ? sc : -FLT_MAX;  // NaN never blocks an assignment
+            }
+        uint32_t used_slots = 0, used_children = 0;
+        for (int it = 0; it < nC; it++) {
+            float best = -INFINITY;
+            int bk = -1, bs = -1;
+            for (int k = 0; k < nC; k++) {
+                if (used_children >> k & 1u) continue;
+                for (int s = 0; s < 8; s++) {
+                    if (used_slots >> s & 1u) continue;
+                    if (bk < 0 || cost[k][s] > best) {
+                        best = cost[k][s];
+                        bk = k;
+                        bs = s;
+                    }
                 }
             }
+            used_children |= 1u << bk;
+            used_slots |= 1u << bs;
+            slot_child[bs] = C[bk];
         }
-        used_children |= 1u << bk;
-        used_slots |= 1u << bs;
-        slot_child[bs] = C[bk];
     }
     uint32_t n_int = 0, n_items = 0;
     for (int s = 0; s < 8; s++) {
@@ -961,9 +995,27 @@ __device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t
             n_items += cnt;
     }
     uint32_t *sc = segctl + kSegWords * seg;
+    // The global counters take every node of the level: one atomic per group of lanes that reach
+    // this point together (a prefix over their counts gives each lane its range), instead of one
+    // per lane on the same two addresses.
+#if LCX_COLLAPSE_AGG
+    cg::coalesced_group g = cg::coalesced_threads();
+    const uint32_t incl = cg::inclusive_scan(g, n_int);
+    const uint32_t total = g.shfl(incl, g.size() - 1);
+    uint32_t wbase = 0, qb = 0;
+    if (g.thread_rank() == g.size() - 1 && total) {
+        wbase = atomicAdd(&ctl[kCtlWideCount], total);
+        qb = atomicAdd(&ctl[kCtlLevel + level + 1], total);
+    }
+    wbase = g.shfl(wbase, g.size() - 1);
+    qb = g.shfl(qb, g.size() - 1);
+    const uint32_t child_base = n_int ? wbase + incl - n_int : 0u;
+    const uint32_t qbase = n_int ? qb + incl - n_int : 0u;
+#else
     const uint32_t child_base = n_int ? atomicAdd(&ctl[kCtlWideCount], n_int) : 0u;
-    const uint32_t item_base = n_items ? segs[seg].item_offset + atomicAdd(&sc[kSegItems], n_items) : 0u;
     const uint32_t qbase = n_int ? atomicAdd(&ctl[kCtlLevel + level + 1], n_int) : 0u;
+#endif
+    const uint32_t item_base = n_items ? segs[seg].item_offset + atomicAdd(&sc[kSegItems], n_items) : 0u;
     if (n_int) atomicAdd(&sc[kSegNodes], n_int);
     atomicMax(&sc[kSegDepth], uint32_t(level + 1));
     uint32_t *d = desc + 12ull * w;
@@ -1045,9 +1097,18 @@ __device__ __forceinline__ void quant_child(const float cl[3], const float ch[3]
                                             uint32_t ql[3], uint32_t qh[3], uint32_t *ctl) {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
+        // e is a power of two, so 1 / e is exact (2^-127 included, as a subnormal) and x * (1 / e)
+        // has the exact value of x / e: with the same directed rounding the two give the same bits,
+        // and the multiplication is far cheaper than a directed division
+#if LCX_QUANT_MUL
+        const float inv_e = __frcp_rn(__uint_as_float(ex[k] << 23));
+        float a = floorf(__fmul_rd(__fsub_rd(cl[k], p[k]), inv_e)) - 1.0f;
+        float z = ceilf(__fmul_ru(__fsub_ru(ch[k], p[k]), inv_e)) + 1.0f;
+#else
         const float e = __uint_as_float(ex[k] << 23);
         float a = floorf(__fdiv_rd(__fsub_rd(cl[k], p[k]), e)) - 1.0f;
         float z = ceilf(__fdiv_ru(__fsub_ru(ch[k], p[k]), e)) + 1.0f;
+#endif
         if (!(a >= -1.0f) || !(z <= 255.0f)) atomicOr(&ctl[kCtlErr], kErrQuant);
         ql[k] = uint32_t(fminf(fmaxf(a, 0.0f), 255.0f));
         qh[k] = uint32_t(fminf(fmaxf(z, 0.0f), 255.0f));
@@ -1376,7 +1437,8 @@ int collapse_grid() {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse, 128, 0);
-        grid = sms * (per_sm > 2 ? 2 : (per_sm > 0 ? per_sm : 1));
+        const int want = LCX_COLLAPSE_BLOCKS;
+        grid = sms * (per_sm > want ? want : (per_sm > 0 ? per_sm : 1));
     }
     return grid;
 }
