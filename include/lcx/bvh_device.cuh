@@ -130,7 +130,10 @@ struct __align__(16) BlasDesc {
     float hi[3];
     uint32_t valid;  // bit 0: built with at least one item; bit 1: procedural (AABB items); bit 2: curve
     const MeshMotion *motion;  // vertex motion (null: static vertices)
-    uint64_t _pad;
+    // Bounding sphere around the centre of [lo, hi]: every item lies within bs_r of it.  0 or not
+    // finite: none (a refit, or a descriptor not written by a build), the box alone bounds the BLAS.
+    float bs_r;
+    uint32_t _pad;
 };
 static_assert(sizeof(BlasDesc) == 80, "BlasDesc is 80 B");
 // InstRec.mask of a procedural instance: its visibility mask in bits 8..15 and

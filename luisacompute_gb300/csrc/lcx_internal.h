@@ -65,6 +65,7 @@ enum : int {
     kSegNodes = 8,
     kSegDepth = 9,
     kSegErr = 10,
+    kSegRad2 = 11,  // max squared distance of an item box corner from the root box centre (float bits)
     kSegWords = 12,
 };
 

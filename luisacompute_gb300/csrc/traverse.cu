@@ -73,6 +73,13 @@ constexpr int kDefaultShortStack = 16;
 // count), the chunk's rays prefetched into L2 when it is taken.  Measured on the terrain workload
 // (closest / any Grays/s): 0: 1.975 / 3.34; 32: 2.023 / 3.45; 64: 2.025 / 3.47; 128: 1.996 / 3.45
 // (the end of the launch waits on the larger chunks).
+// Deferred kernel: an instance entry records the object-space ray and the flush sets up the
+// watertight test per queued entry (1), or the entry sets it up and records it (0).  The entry runs
+// with a few lanes in nearly every step, the flush with all of them: 2.035 -> 2.12 Grays/s on the
+// terrain workload (any hit 3.48 -> 3.55), same records.
+#ifndef LCX_WT_AT_FLUSH
+#define LCX_WT_AT_FLUSH 1
+#endif
 #ifndef LCX_RAY_CHUNK
 #define LCX_RAY_CHUNK 64
 #endif
@@ -86,7 +93,9 @@ constexpr int kDefaultShortStack = 16;
 // kExt: the extended kernels.  1: accels with motion instances or vertex-motion
 // meshes (each ray has a time); 2: also curves (curve segments get the curve test,
 // with a larger register budget).
-template <int kLayout, bool kAny, bool kCount, bool kMulti, int kShort, int kExt = 0>
+// kNoWt: the caller tests triangles from its own ray records (the deferred kernel): an instance
+// entry keeps the object-space direction instead of setting up the watertight test.
+template <int kLayout, bool kAny, bool kCount, bool kMulti, int kShort, int kExt = 0, bool kNoWt = false>
 struct Walker {
     static constexpr int kShortStack = kShort < kStackSize ? kShort : kStackSize;
     static constexpr int kDeep = kStackSize - kShortStack;    // entries in local memory
@@ -446,8 +455,8 @@ struct Walker {
             iy = slab_rcp(dy);
             iz = slab_rcp(dz);
             octinv = octant_inv(dx, dy, dz);
-            wt = wt_setup(ox, oy, oz, dx, dy, dz);
-            if (kExt >= 2) {
+            if constexpr (!kNoWt) wt = wt_setup(ox, oy, oz, dx, dy, dz);
+            if (kExt >= 2 || kNoWt) {
                 rdx = dx;
                 rdy = dy;
                 rdz = dz;
@@ -712,7 +721,7 @@ struct DeferQueue {
 // visits: nodes visited, triangles queued (each is tested once), instances entered.
 template <int kLayout, bool kAny, int kShort, bool kMulti, bool kCount = false>
 __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_deferred(TraceParams P) {
-    using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort>;
+    using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort, 0, LCX_WT_AT_FLUSH != 0>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
     __shared__ DeferQueue<kMulti> queues[kTraceBlock / 32];
     uint2 deep_stack[W_t::kDeepSlots];
@@ -758,6 +767,11 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
             if (j < qn) {
                 r = Q.rec[j];
                 WtRay ray;
+#if LCX_WT_AT_FLUSH
+                // the record holds the object-space ray; the test's setup is the same function of it
+                // that an entry would have computed, so the bits are the same
+                ray = wt_setup(Q.rr[0][r], Q.rr[1][r], Q.rr[2][r], Q.rr[3][r], Q.rr[4][r], Q.rr[5][r]);
+#else
                 ray.ox = Q.rr[0][r];
                 ray.oy = Q.rr[1][r];
                 ray.oz = Q.rr[2][r];
@@ -765,6 +779,7 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
                 ray.Sy = Q.rr[4][r];
                 ray.Sz = Q.rr[5][r];
                 ray.perm = __float_as_uint(Q.rr[6][r]);
+#endif
                 const float lo = Q.rr[7][r], hi = Q.tmax[r];
                 const float4 *tp = reinterpret_cast<const float4 *>(Q.tri[j]);
                 const float4 a = bvh_ld(tp), b = bvh_ld(tp + 1), c = bvh_ld(tp + 2);
@@ -987,6 +1002,14 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
             if (W.in_blas) {
                 cur ^= 1u;
                 const uint32_t r = lane + 32u * cur;
+#if LCX_WT_AT_FLUSH
+                Q.rr[0][r] = W.ox;
+                Q.rr[1][r] = W.oy;
+                Q.rr[2][r] = W.oz;
+                Q.rr[3][r] = W.rdx;
+                Q.rr[4][r] = W.rdy;
+                Q.rr[5][r] = W.rdz;
+#else
                 Q.rr[0][r] = W.wt.ox;
                 Q.rr[1][r] = W.wt.oy;
                 Q.rr[2][r] = W.wt.oz;
@@ -994,6 +1017,7 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
                 Q.rr[4][r] = W.wt.Sy;
                 Q.rr[5][r] = W.wt.Sz;
                 Q.rr[6][r] = __uint_as_float(W.wt.perm);
+#endif
                 Q.rr[7][r] = W.tmin;
                 Q.rr[8][r] = __uint_as_float(W.cur_inst);
                 mine |= 1u << cur;
