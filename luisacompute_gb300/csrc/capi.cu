@@ -392,6 +392,10 @@ struct BuildTuning {
     // 3.00 -> 2.64 with the same 343k wide nodes (closest 2.020 -> 2.030 Grays/s in loop mode 2,
     // 1.660 -> 1.716 in mode 0)
     uint32_t fill = 1;
+    // binned-SAH TLAS up to 2048 instances (lcx_set_build_tlas_sah), on: on the terrain workload (a
+    // heightfield and 256 small spheres) TLAS SAH 20.0 -> 15.2, node visits per ray 15.19 -> 13.99,
+    // closest 2.358 -> 2.492 Grays/s, any hit 3.89 -> 4.12
+    uint32_t tlas_sah = 1;
 };
 BuildTuning g_build_tune;
 
@@ -1541,6 +1545,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
     bp.leaf_max = 1;
     bp.size_bits = g_build_tune.tlas_size_bits;
     bp.cube = g_build_tune.tlas_cube;
+    bp.tlas_sah = g_build_tune.tlas_sah;
     BuildReadback rb;
     std::shared_ptr<DevBlock> block;
     {
@@ -1633,6 +1638,18 @@ int lcx_accel_stats(uint64_t accel, LcxAccelStats *out) {
         LCX_CUDA(cudaMemcpy(h, a->wide_sah, sizeof(h), cudaMemcpyDeviceToHost), "wide SAH readback");
         out->wide_sah_cost = h[1] > 0.0 ? h[0] / h[1] : 0.0;
     }
+    return LCX_OK;
+}
+
+int lcx_set_build_tlas_sah(uint32_t sah) {
+    if (sah > 1) return fail(LCX_ERR_INVALID_ARG, "lcx_set_build_tlas_sah: 0 or 1");
+    g_build_tune.tlas_sah = sah;
+    return LCX_OK;
+}
+
+int lcx_get_build_tlas_sah(uint32_t *sah) {
+    if (!sah) return fail(LCX_ERR_INVALID_ARG, "null output");
+    *sah = g_build_tune.tlas_sah;
     return LCX_OK;
 }
 

@@ -91,6 +91,7 @@ struct BuildParams {
     uint32_t cube = 1;       // normalise centroids by the largest extent on every axis (else per axis)
     float split = 0.0f;      // triangle splitting: extra references, as a fraction of the triangles (0 = off)
     uint32_t fill = 0;       // BLAS collapse: split leaf slots into finer ones while slots are free
+    uint32_t tlas_sah = 0;   // TLAS of up to 2048 instances: a binned-SAH binary tree instead of the LBVH
 };
 
 // Per-build device scratch, sized for n items in nseg segments.
