@@ -716,14 +716,21 @@ LCX_API int lcx_get_build_split(float *fraction);
  * triangles.  Default 1.  Results do not depend on it. */
 LCX_API int lcx_set_build_fill(uint32_t fill);
 LCX_API int lcx_get_build_fill(uint32_t *fill);
-/* TLAS builds of up to 2048 instances (0 or 1): 1 builds the binary tree by
- * binned SAH (16 bins per axis, top-down, on the GPU) instead of the Morton
- * LBVH, before the same collapse to wide nodes.  Instance sets mixing a few
- * large objects with many small ones trace faster through it; the build takes
- * longer (0.8 ms at 257 instances, about 2 ms at 1024, against 0.4 ms).  Default 1.
- * Results do not depend on it. */
+/* TLAS builds (0 or 1): 1 builds the binary tree by binned SAH (16 bins per
+ * axis, top-down, on the GPU) instead of the Morton LBVH, before the same
+ * collapse to wide nodes.  Instance sets mixing a few large objects with many
+ * small ones trace faster through it.  Default 1.  Results do not depend on it. */
 LCX_API int lcx_set_build_tlas_sah(uint32_t sah);
 LCX_API int lcx_get_build_tlas_sah(uint32_t *sah);
+/* BLAS builds of FAST_TRACE meshes (0 or 1): 1 builds the binary tree by the
+ * same binned SAH instead of the Morton LBVH (the reference's FAST_TRACE builds
+ * are SAH builds too: Embree's high-quality builder, OptiX's PREFER_FAST_TRACE).
+ * The build synchronises the stream once per level of node ranges above 1024
+ * triangles, so it takes longer than the LBVH; FAST_BUILD meshes, reserved
+ * batches (lcx_mesh_build_batch_reserve, lcx_mesh_reserve_batch) and their
+ * rebuilds keep the LBVH.  Default 1.  Results do not depend on it. */
+LCX_API int lcx_set_build_blas_sah(uint32_t sah);
+LCX_API int lcx_get_build_blas_sah(uint32_t *sah);
 
 /* Traversal knobs, process-wide (no counterpart in the reference: OptiX and
  * Embree pick theirs internally).  refill: a warp takes new rays once at

@@ -179,6 +179,8 @@ _SIGS = {
     "lcx_set_build_fill": (c_int, [c_uint32]),
     "lcx_set_build_tlas_sah": (c_int, [c_uint32]),
     "lcx_get_build_tlas_sah": (c_int, [POINTER(c_uint32)]),
+    "lcx_set_build_blas_sah": (c_int, [c_uint32]),
+    "lcx_get_build_blas_sah": (c_int, [POINTER(c_uint32)]),
     "lcx_get_build_fill": (c_int, [POINTER(c_uint32)]),
     "lcx_mesh_build_batch_reserve": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
     "lcx_mesh_reserve_batch": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),

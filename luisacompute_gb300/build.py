@@ -18,8 +18,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "liblcx_accel.so"
-SOURCES = ["build.cu", "traverse.cu", "capi.cu", "sort.cu", "noalloc.cu", "pathtrace.cu", "reorder.cu", "cpu_table.cu"]
-HEADERS = ["lcx_internal.h", "pt_math.cuh"]
+SOURCES = ["build.cu", "sah.cu", "traverse.cu", "capi.cu", "sort.cu", "noalloc.cu", "pathtrace.cu", "reorder.cu", "cpu_table.cu"]
+HEADERS = ["lcx_internal.h", "build_util.cuh", "pt_math.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               f"-I{ROOT / 'include'}", f"-I{CSRC}"]

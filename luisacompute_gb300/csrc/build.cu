@@ -31,6 +31,7 @@
 
 #include <cub/device/device_scan.cuh>
 
+#include "build_util.cuh"
 #include "lcx_internal.h"
 
 namespace cg = cooperative_groups;
@@ -56,7 +57,6 @@ namespace {
 #define LCX_COLLAPSE_BLOCKS 8
 #endif
 
-constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr int kPrepBlock = 256;
 
 __device__ __forceinline__ unsigned long long spread21(uint32_t v) {
@@ -67,16 +67,6 @@ __device__ __forceinline__ unsigned long long spread21(uint32_t v) {
     x = (x | x << 4) & 0x10c30c30c30c30c3ull;
     x = (x | x << 2) & 0x1249249249249249ull;
     return x;
-}
-
-__device__ __forceinline__ bool box_empty(const float4 &lo, const float4 &hi) {
-    return !(lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z);
-}
-
-__device__ __forceinline__ float box_area(const float4 &lo, const float4 &hi) {
-    if (box_empty(lo, hi)) return 0.0f;
-    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
-    return 2.0f * (dx * dy + dy * dz + dz * dx);
 }
 
 __device__ __forceinline__ double box_area_d(float lx, float ly, float lz, float hx, float hy, float hz) {
@@ -97,19 +87,6 @@ __device__ __forceinline__ void seg_sum(double *out, uint32_t seg, double v) {
     } else {
         atomicAdd(&out[2 * seg], v);
     }
-}
-
-// Segment of global item i: binary search over the segment table.
-__device__ __forceinline__ uint32_t segment_of(const SegInput *segs, uint32_t nseg, uint32_t i) {
-    uint32_t lo = 0, hi = nseg - 1;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi + 1) >> 1;
-        if (segs[mid].item_offset <= i)
-            lo = mid;
-        else
-            hi = mid - 1;
-    }
-    return lo;
 }
 
 // Centroid bounds into the per-segment control words; warps whose lanes share
@@ -1470,8 +1447,6 @@ __global__ void k_binary_sah(uint32_t n, uint32_t seg_shift, const unsigned long
     }
 }
 
-inline unsigned blocks_for(uint64_t n, unsigned bs) { return unsigned((n + bs - 1) / bs); }
-
 TreeView make_view(const BuildScratch &s) {
     TreeView tv;
     tv.child = s.bin_child;
@@ -1549,8 +1524,12 @@ cudaError_t build_tree_tris(BuildScratch &s, const BuildParams &bp, cudaStream_t
     if (s.ref_prim == nullptr)  // with triangle splitting split_emit has written the item boxes
         k_tri_prep<<<blocks_for(s.n, kPrepBlock), kPrepBlock, 0, st>>>(s.segs, s.nseg, s.n, s.box_lo, s.box_hi,
                                                                        s.segctl, s.ctl);
-    return build_common(s, bp, st);
+    return bp.blas_sah ? build_tree_sah(s, bp, st) : build_common(s, bp, st);
 }
+
+cudaError_t build_tree_lbvh(BuildScratch &s, const BuildParams &bp, cudaStream_t st) { return build_common(s, bp, st); }
+
+cudaError_t build_tree_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st) { return build_rest(s, bp, st); }
 
 cudaError_t split_count(const SegInput *tsegs, uint32_t nseg, uint32_t n, float fraction, float *wts,
                         unsigned long long *sums, uint32_t *refs, uint32_t *seg_refs, uint32_t *segctl, uint32_t *ctl,
@@ -1595,176 +1574,9 @@ cudaError_t split_emit(const SegInput *tsegs, uint32_t nseg, uint32_t n, const u
     return cudaGetLastError();
 }
 
-// Binned-SAH binary tree over the n items of a single segment (a TLAS of up to kSahMaxItems
-// instances), in the layout k_lbvh writes: items reordered in vals so every node covers a
-// contiguous range, the internal node splitting [a, m) | [m, b) stored at index m - 1, the root in
-// segctl[kSegRoot].  One block, level-synchronous; each range is split by one thread: centroid
-// bounds, 16 bins on each axis, the split of least cost A_L N_L + A_R N_R, then an in-place
-// partition (a median split when all centroids coincide).  Ranges of one item are leaves.  The
-// collapse and emit downstream see no difference from an LBVH.  ranges: 8 n words of scratch.
-// Each range is split by one thread, so the top levels are serial: TLAS builds measured 0.83 / 1.95 /
-// 6.7 / 20.5 ms at 257 / 1,024 / 4,096 / 8,192 instances, against 0.42 / 0.44 / 0.56 / 0.71 ms for
-// the LBVH; above 2,048 instances the LBVH is used.
-constexpr uint32_t kSahMaxItems = 2048;
-constexpr int kSahBins = 16;
-
-__device__ __forceinline__ float3 centroid_of(const float4 &l, const float4 &h) {
-    if (box_empty(l, h)) return make_float3(0.0f, 0.0f, 0.0f);
-    return make_float3(0.5f * (l.x + h.x), 0.5f * (l.y + h.y), 0.5f * (l.z + h.z));
-}
-__device__ __forceinline__ float axis_of(const float3 &c, int k) { return k == 0 ? c.x : (k == 1 ? c.y : c.z); }
-__device__ __forceinline__ float area3(const float3 &l, const float3 &h) {
-    if (!(l.x <= h.x && l.y <= h.y && l.z <= h.z)) return 0.0f;
-    const float dx = h.x - l.x, dy = h.y - l.y, dz = h.z - l.z;
-    return 2.0f * (dx * dy + dy * dz + dz * dx);
-}
-
-__global__ void __launch_bounds__(256) k_sah_tree(uint32_t n, const float4 *lo, const float4 *hi, uint32_t *vals,
-                                                   uint32_t *bin_child, float4 *bin_lo, float4 *bin_hi,
-                                                   uint32_t *ranges, uint32_t *segctl) {
-    __shared__ uint32_t count[2];
-    if (threadIdx.x == 0) {
-        count[0] = 0u;
-        count[1] = 0u;
-    }
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) vals[i] = i;
-    __syncthreads();
-    if (n == 1) {
-        if (threadIdx.x == 0) segctl[kSegRoot] = kLeafBit | 0u;
-        return;
-    }
-    // a range: (first, end, parent node + 1 or 0 for the root, side)
-    if (threadIdx.x == 0) {
-        ranges[0] = 0u;
-        ranges[1] = n;
-        ranges[2] = 0u;
-        ranges[3] = 0u;
-        count[0] = 1u;
-    }
-    __syncthreads();
-    for (uint32_t level = 0; level < n; level++) {
-        const uint32_t cur = level & 1u, nxt = cur ^ 1u;
-        const uint32_t todo = count[cur];
-        if (todo == 0u) break;
-        const uint32_t *in = ranges + 4ull * n * cur;
-        uint32_t *out = ranges + 4ull * n * nxt;
-        for (uint32_t t = threadIdx.x; t < todo; t += blockDim.x) {
-            const uint32_t a = in[4 * t], b = in[4 * t + 1], parent1 = in[4 * t + 2], side = in[4 * t + 3];
-            float3 cl = make_float3(FLT_MAX, FLT_MAX, FLT_MAX), ch = make_float3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
-            float3 bl = cl, bh = ch;  // the node's box
-            for (uint32_t i = a; i < b; i++) {
-                const float4 l = lo[vals[i]], h = hi[vals[i]];
-                const float3 c = centroid_of(l, h);
-                cl = make_float3(fminf(cl.x, c.x), fminf(cl.y, c.y), fminf(cl.z, c.z));
-                ch = make_float3(fmaxf(ch.x, c.x), fmaxf(ch.y, c.y), fmaxf(ch.z, c.z));
-                bl = make_float3(fminf(bl.x, l.x), fminf(bl.y, l.y), fminf(bl.z, l.z));
-                bh = make_float3(fmaxf(bh.x, h.x), fmaxf(bh.y, h.y), fmaxf(bh.z, h.z));
-            }
-            // best split over 3 axes x (kSahBins - 1) bin boundaries
-            float best = FLT_MAX;
-            int best_axis = -1, best_bin = 0;
-            for (int k = 0; k < 3; k++) {
-                const float c0 = axis_of(cl, k), ext = axis_of(ch, k) - c0;
-                if (!(ext > 0.0f)) continue;
-                uint32_t bn[kSahBins];
-                float3 bbl[kSahBins], bbh[kSahBins];
-                for (int j = 0; j < kSahBins; j++) {
-                    bn[j] = 0u;
-                    bbl[j] = make_float3(FLT_MAX, FLT_MAX, FLT_MAX);
-                    bbh[j] = make_float3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
-                }
-                for (uint32_t i = a; i < b; i++) {
-                    const float4 l = lo[vals[i]], h = hi[vals[i]];
-                    const int j = min(kSahBins - 1, int(float(kSahBins) * (axis_of(centroid_of(l, h), k) - c0) / ext));
-                    bn[j]++;
-                    bbl[j] = make_float3(fminf(bbl[j].x, l.x), fminf(bbl[j].y, l.y), fminf(bbl[j].z, l.z));
-                    bbh[j] = make_float3(fmaxf(bbh[j].x, h.x), fmaxf(bbh[j].y, h.y), fmaxf(bbh[j].z, h.z));
-                }
-                float right_area[kSahBins];
-                uint32_t right_n[kSahBins];
-                float3 rl = make_float3(FLT_MAX, FLT_MAX, FLT_MAX), rh = make_float3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
-                uint32_t rn = 0u;
-                for (int j = kSahBins - 1; j > 0; j--) {
-                    rl = make_float3(fminf(rl.x, bbl[j].x), fminf(rl.y, bbl[j].y), fminf(rl.z, bbl[j].z));
-                    rh = make_float3(fmaxf(rh.x, bbh[j].x), fmaxf(rh.y, bbh[j].y), fmaxf(rh.z, bbh[j].z));
-                    rn += bn[j];
-                    right_area[j] = area3(rl, rh);
-                    right_n[j] = rn;
-                }
-                float3 ll = make_float3(FLT_MAX, FLT_MAX, FLT_MAX), lh = make_float3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
-                uint32_t ln = 0u;
-                for (int j = 0; j < kSahBins - 1; j++) {  // split between bins j and j + 1
-                    ll = make_float3(fminf(ll.x, bbl[j].x), fminf(ll.y, bbl[j].y), fminf(ll.z, bbl[j].z));
-                    lh = make_float3(fmaxf(lh.x, bbh[j].x), fmaxf(lh.y, bbh[j].y), fmaxf(lh.z, bbh[j].z));
-                    ln += bn[j];
-                    if (ln == 0u || right_n[j + 1] == 0u) continue;
-                    const float cost = area3(ll, lh) * float(ln) + right_area[j + 1] * float(right_n[j + 1]);
-                    if (cost < best) {
-                        best = cost;
-                        best_axis = k;
-                        best_bin = j;
-                    }
-                }
-            }
-            uint32_t m = a + (b - a) / 2;  // a median split when no binned split separates the items
-            if (best_axis >= 0) {
-                const float c0 = axis_of(cl, best_axis), ext = axis_of(ch, best_axis) - c0;
-                uint32_t i = a, j = b;
-                while (i < j) {  // in-place partition: bins <= best_bin to the left
-                    const float4 l = lo[vals[i]], h = hi[vals[i]];
-                    const int bi =
-                        min(kSahBins - 1, int(float(kSahBins) * (axis_of(centroid_of(l, h), best_axis) - c0) / ext));
-                    if (bi <= best_bin) {
-                        i++;
-                    } else {
-                        j--;
-                        const uint32_t tmp = vals[i];
-                        vals[i] = vals[j];
-                        vals[j] = tmp;
-                    }
-                }
-                if (i > a && i < b) m = i;
-            }
-            const uint32_t node = m - 1u;  // the internal node of this range
-            bin_lo[node] = make_float4(bl.x, bl.y, bl.z, __uint_as_float(b - a));
-            bin_hi[node] = make_float4(bh.x, bh.y, bh.z, __uint_as_float(a));
-            if (parent1 == 0u)
-                segctl[kSegRoot] = node;
-            else
-                bin_child[2 * (parent1 - 1u) + side] = node;
-            // children: a one-item range is a leaf, a longer one waits for the next level
-            if (m - a == 1u) {
-                bin_child[2 * node] = kLeafBit | a;
-            } else {
-                const uint32_t k = atomicAdd(&count[nxt], 1u);
-                out[4 * k] = a;
-                out[4 * k + 1] = m;
-                out[4 * k + 2] = node + 1u;
-                out[4 * k + 3] = 0u;
-            }
-            if (b - m == 1u) {
-                bin_child[2 * node + 1] = kLeafBit | m;
-            } else {
-                const uint32_t k = atomicAdd(&count[nxt], 1u);
-                out[4 * k] = m;
-                out[4 * k + 1] = b;
-                out[4 * k + 2] = node + 1u;
-                out[4 * k + 3] = 1u;
-            }
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) count[cur] = 0u;
-        __syncthreads();
-    }
-}
-
 cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
     k_inst_prep<<<blocks_for(s.n, kPrepBlock), kPrepBlock, 0, st>>>(inst, s.n, s.box_lo, s.box_hi, s.w2o, s.segctl);
-    if (!(bp.tlas_sah && s.nseg == 1 && s.n >= 1 && s.n <= kSahMaxItems)) return build_common(s, bp, st);
-    // a TLAS of up to kSahMaxItems instances: a binned-SAH binary tree in place of the Morton LBVH
-    k_sah_tree<<<1, 256, 0, st>>>(s.n, s.box_lo, s.box_hi, s.vals_sorted, s.bin_child, s.bin_lo, s.bin_hi, s.desc,
-                                  s.segctl);
-    return build_rest(s, bp, st);
+    return bp.tlas_sah ? build_tree_sah(s, bp, st) : build_common(s, bp, st);
 }
 
 cudaError_t emit_blas(const BuildScratch &s, const BuildParams &bp, uint32_t wide_count, Node8Q *qn, Node8F *fn,

@@ -313,7 +313,7 @@ int alloc_scratch(ScratchHolder &h, BuildScratch &s, const std::vector<SegInput>
     LCX_CUDA(h.alloc((void **)&s.queue, sizeof(uint2) * 2 * s.queue_len), "scratch");
     if (tlas) LCX_CUDA(h.alloc((void **)&s.w2o, sizeof(float) * 12 * nn), "scratch");
     LCX_CUDA(h.alloc((void **)&s.ctl, sizeof(uint32_t) * kCtlWords), "scratch");
-    s.sort_tmp_bytes = sort_temp_bytes(uint32_t(nn));
+    s.sort_tmp_bytes = std::max(sort_temp_bytes(uint32_t(nn)), sah_scan_temp_bytes(uint32_t(nn)));
     LCX_CUDA(h.alloc(&s.sort_tmp, s.sort_tmp_bytes), "scratch");
     // uploads: segment table, control words (centroid minima start at the largest ordered value);
     // a reserved rebuild copies both from the device (no host data: capturable)
@@ -392,10 +392,12 @@ struct BuildTuning {
     // 3.00 -> 2.64 with the same 343k wide nodes (closest 2.020 -> 2.030 Grays/s in loop mode 2,
     // 1.660 -> 1.716 in mode 0)
     uint32_t fill = 1;
-    // binned-SAH TLAS up to 2048 instances (lcx_set_build_tlas_sah), on: on the terrain workload (a
-    // heightfield and 256 small spheres) TLAS SAH 20.0 -> 15.2, node visits per ray 15.19 -> 13.99,
-    // closest 2.358 -> 2.492 Grays/s, any hit 3.89 -> 4.12
+    // binned-SAH TLAS (lcx_set_build_tlas_sah), on: on the terrain workload (a heightfield and 256
+    // small spheres) TLAS SAH 20.0 -> 15.2, node visits per ray 15.19 -> 13.99, closest 2.358 ->
+    // 2.492 Grays/s, any hit 3.89 -> 4.12
     uint32_t tlas_sah = 1;
+    // binned-SAH BLAS of FAST_TRACE meshes (lcx_set_build_blas_sah), on
+    uint32_t blas_sah = 1;
 };
 BuildTuning g_build_tune;
 
@@ -406,6 +408,7 @@ BuildParams build_params_for(const LcxAccelOption &o) {
     bp.cube = g_build_tune.blas_cube;
     bp.split = (o.hint == LCX_HINT_FAST_TRACE && !o.allow_update) ? g_build_tune.split : 0.0f;
     bp.fill = g_build_tune.fill;
+    bp.blas_sah = o.hint == LCX_HINT_FAST_TRACE ? g_build_tune.blas_sah : 0u;
     return bp;
 }
 
@@ -573,6 +576,7 @@ int try_reserved_rebuild(const std::vector<MeshObj *> &meshes, const std::vector
     if (int r = current_device_state(&ds)) return r;
     BuildParams bp = build_params_for(meshes[0]->opt);
     bp.split = 0.0f;
+    bp.blas_sah = 0u;  // capturable: no host synchronisation
     ScratchHolder hold(st);
     BuildScratch s;
     if (int r = alloc_scratch(hold, s, blk->h_segs, blk->items, false, blk->d_segs, blk->d_segctl_init)) return r;
@@ -672,7 +676,8 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
                     "mesh build in a CUDA graph capture: only refits (PREFER_UPDATE, allow_update, every mesh of the "
                     "block, same triangle counts, asynchronous refit mode) and rebuilds of a reserved batch "
                     "(lcx_mesh_build_batch_reserve, same meshes and buffers) can be captured");
-    const BuildParams bp = build_params_for(meshes[0]->opt);
+    BuildParams bp = build_params_for(meshes[0]->opt);
+    if (reserve) bp.blas_sah = 0u;  // its rebuilds are capturable LBVH builds: keep the first one alike
     if (total == 0) {
         LCX_CUDA(cudaStreamSynchronize(st), "sync");
         for (MeshObj *m : meshes) {
@@ -1650,6 +1655,18 @@ int lcx_set_build_tlas_sah(uint32_t sah) {
 int lcx_get_build_tlas_sah(uint32_t *sah) {
     if (!sah) return fail(LCX_ERR_INVALID_ARG, "null output");
     *sah = g_build_tune.tlas_sah;
+    return LCX_OK;
+}
+
+int lcx_set_build_blas_sah(uint32_t sah) {
+    if (sah > 1) return fail(LCX_ERR_INVALID_ARG, "lcx_set_build_blas_sah: 0 or 1");
+    g_build_tune.blas_sah = sah;
+    return LCX_OK;
+}
+
+int lcx_get_build_blas_sah(uint32_t *sah) {
+    if (!sah) return fail(LCX_ERR_INVALID_ARG, "null output");
+    *sah = g_build_tune.blas_sah;
     return LCX_OK;
 }
 

@@ -91,7 +91,8 @@ struct BuildParams {
     uint32_t cube = 1;       // normalise centroids by the largest extent on every axis (else per axis)
     float split = 0.0f;      // triangle splitting: extra references, as a fraction of the triangles (0 = off)
     uint32_t fill = 0;       // BLAS collapse: split leaf slots into finer ones while slots are free
-    uint32_t tlas_sah = 0;   // TLAS of up to 2048 instances: a binned-SAH binary tree instead of the LBVH
+    uint32_t tlas_sah = 0;   // TLAS: a binned-SAH binary tree instead of the LBVH
+    uint32_t blas_sah = 0;   // BLAS: a binned-SAH binary tree instead of the LBVH (never in a capturable rebuild)
 };
 
 // Per-build device scratch, sized for n items in nseg segments.
@@ -132,6 +133,14 @@ uint32_t morton_axis_bits(uint32_t nseg, uint32_t *seg_bits);
 // caller reads ctl (wide node count, errors) and segctl back.
 cudaError_t build_tree_tris(BuildScratch &s, const BuildParams &bp, cudaStream_t st);
 cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const BuildParams &bp, cudaStream_t st);
+// The pieces after the item boxes: Morton codes + sort + LBVH (then the rest); the binned-SAH
+// binary tree (sah.cu; synchronises the stream once per level of ranges above 1024 items, and
+// falls back to the LBVH under stream capture); the rest = binary SAH, bounding spheres, collapse.
+cudaError_t build_tree_lbvh(BuildScratch &s, const BuildParams &bp, cudaStream_t st);
+cudaError_t build_tree_sah(BuildScratch &s, const BuildParams &bp, cudaStream_t st);
+cudaError_t build_tree_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st);
+// Temporary bytes of the SAH build's scan over n items (it shares the sort's scratch).
+size_t sah_scan_temp_bytes(uint32_t n);
 
 // Triangle splitting (split builds).  split_count: per triangle 1 + its extra
 // references (refs; at most fraction x the segment's triangles extra per
