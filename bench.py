@@ -313,6 +313,19 @@ def leg_batch_build(stream, count=512):
     for _ in range(3):
         build_meshes(meshes)
     ms = _event_ms(lambda: build_meshes(meshes), 5, stream)
+    sah = float(np.mean([m.stats().wide_sah_cost for m in meshes]))
+    # the same build with the Morton LBVH in place of the binned-SAH builder
+    from luisacompute_gb300 import _capi
+    lib = _capi.load()
+    old = ctypes.c_uint32(0)
+    _capi.check(lib.lcx_get_build_blas_sah(ctypes.byref(old)), "blas_sah")
+    _capi.check(lib.lcx_set_build_blas_sah(1 - old.value), "blas_sah")
+    try:
+        build_meshes(meshes)
+        ms_other = _event_ms(lambda: build_meshes(meshes), 5, stream)
+        sah_other = float(np.mean([m.stats().wide_sah_cost for m in meshes]))
+    finally:
+        _capi.check(lib.lcx_set_build_blas_sah(old.value), "blas_sah")
     # the same meshes reserved without a build (lcx_mesh_reserve_batch): their first build captured in a
     # CUDA graph, replayed
     import torch
@@ -326,11 +339,14 @@ def leg_batch_build(stream, count=512):
         graph.replay()
     gms = _event_ms(graph.replay, 5, stream)
     del graph, res
+    names = ("sah", "lbvh") if old.value else ("lbvh", "sah")
     return {"meshes": count, "triangles": int(total), "ms": ms, "mtris_per_s": total / (ms * 1e-3) / 1e6,
+            "builder": names[0], "mean_wide_sah": sah,
+            f"{names[1]}_ms": ms_other, f"{names[1]}_mean_wide_sah": sah_other,
             "graph_first_build_ms": gms, "graph_first_build_mtris_per_s": total / (gms * 1e-3) / 1e6,
             "what": "one lcx_mesh_build_batch over the sample per step (its host sync for the node count included), "
                     "default build knobs; graph_first_build: the sample reserved without a build and its first "
-                    "build captured in a CUDA graph (no host sync), per replay"}
+                    "build captured in a CUDA graph (no host sync, Morton LBVH), per replay"}
 
 
 def leg_pathtrace(scene, acc, meshes, stream, steps=5):
@@ -425,8 +441,15 @@ def run_batch_build(args):
 
     for _ in range(max(3, args.warmup)):
         build_meshes(meshes)
+    from luisacompute_gb300 import _capi
+    lib = _capi.load()
+    launches0 = ctypes.c_uint64(0)
+    _capi.check(lib.lcx_get_build_kernel_launches(ctypes.byref(launches0)), "launch count")
     with ClockSampler(0) as clocks:
         batch_s = timed(lambda: build_meshes(meshes), args.steps)
+    launches1 = ctypes.c_uint64(0)
+    _capi.check(lib.lcx_get_build_kernel_launches(ctypes.byref(launches1)), "launch count")
+    launches = int(launches1.value - launches0.value)
     # one-by-one on the first 256 meshes (each lcx_mesh_build synchronises once)
     sub = meshes[:256]
     sub_tris = sum(m.triangles.shape[0] for m in sub)
@@ -492,8 +515,10 @@ def run_batch_build(args):
     graph_rebuild_s = timed(graph_b.replay, 5)
     _capi.check(_capi.load().lcx_check_trace_errors(), "rebuild errors")
     del graph_b, res
-    # kernels of ours per batched build: tri_prep, morton, lbvh, binary_sah, collapse_init, collapse, emit
-    # (the timed loop; the refit figures in "extra" come after it)
+    # gpu_launches: our kernels in the timed loop, from the library's build-launch counter (the
+    # LBVH: tri_prep, morton, lbvh, binary_sah, collapse_init, collapse, emit; the SAH builder: its
+    # seed and mark, four kernels per level of ranges above 1,024 items, the per-range blocks and
+    # the segment keys in place of morton and lbvh; CUB's sort and scan are library kernels)
     line = {"metric": "Mtris/s batched BLAS build (4096 meshes)", "value": total / batch_s / 1e6, "unit": "Mtris/s",
             "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": batch_s * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -502,7 +527,7 @@ def run_batch_build(args):
                                    "icosphere or grid with 1% Gaussian displacement; one lcx_mesh_build_batch per step",
                        "generation_s": gen_s,
                        "l2": "inputs (vertices + indices, ~2.6 GB) and outputs exceed the 129 MB L2"},
-            "clocks": clocks.summary(), "gpu_launches": 7 * args.steps,
+            "clocks": clocks.summary(), "gpu_launches": launches,
             "extra": {"one_by_one_mtris_s_first_256": sub_tris / single_s / 1e6,
                       "batched_mtris_s_first_256": sub_tris / batch_sub_s / 1e6,
                       "mean_wide_sah": float(np.mean(wide)),
@@ -553,12 +578,13 @@ def cpu_baseline_build(datas, meshes, rng, count=16):
         tris += md.tri_count
         ms = meshes[i].stats()
         sah.append({"tris": int(md.tri_count), "oracle_binned_sah": float(lib.lcxo_mesh_sah(om)),
-                    "ours_binary_lbvh": ms.sah_cost, "ours_wide": ms.wide_sah_cost, "ours_depth": int(ms.depth)})
+                    "ours_binary": ms.sah_cost, "ours_wide": ms.wide_sah_cost, "ours_depth": int(ms.depth)})
         lib.lcxo_mesh_destroy(om)
-    ratio = float(np.median([x["ours_binary_lbvh"] / x["oracle_binned_sah"] for x in sah]))
+    ratio = float(np.median([x["ours_binary"] / x["oracle_binned_sah"] for x in sah]))
     return {"value": tris / secs / 1e6, "unit": "Mtris/s", "cores": 1, "kind": "port",
             "sample": f"{count} meshes of the batch ({tris} triangles), oracle binned-SAH build",
-            "sah_sample": sah, "median_sah_ratio_ours_lbvh_to_oracle_binned": ratio}
+            "sah_sample": sah, "median_sah_ratio_ours_to_oracle_binned": ratio,
+            "ours_builder": "the timed build's (autotuned: binned SAH or Morton LBVH)"}
 
 
 def run_serving(args):

@@ -731,6 +731,11 @@ LCX_API int lcx_get_build_tlas_sah(uint32_t *sah);
  * rebuilds keep the LBVH.  Default 1.  Results do not depend on it. */
 LCX_API int lcx_set_build_blas_sah(uint32_t sah);
 LCX_API int lcx_get_build_blas_sah(uint32_t *sah);
+/* Kernels of this library launched by builds, refits and instance updates
+ * since it was loaded (a host-side counter for launch accounting; the CUB
+ * sort and scan kernels a build also runs are library kernels and are not
+ * counted).  No counterpart in the reference. */
+LCX_API int lcx_get_build_kernel_launches(uint64_t *count);
 
 /* Traversal knobs, process-wide (no counterpart in the reference: OptiX and
  * Embree pick theirs internally).  refill: a warp takes new rays once at

@@ -181,6 +181,7 @@ _SIGS = {
     "lcx_get_build_tlas_sah": (c_int, [POINTER(c_uint32)]),
     "lcx_set_build_blas_sah": (c_int, [c_uint32]),
     "lcx_get_build_blas_sah": (c_int, [POINTER(c_uint32)]),
+    "lcx_get_build_kernel_launches": (c_int, [POINTER(c_uint64)]),
     "lcx_get_build_fill": (c_int, [POINTER(c_uint32)]),
     "lcx_mesh_build_batch_reserve": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
     "lcx_mesh_reserve_batch": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),

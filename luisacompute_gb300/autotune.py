@@ -6,7 +6,8 @@ It measures, on the caller's own scene and rays, and picks:
   - node width: children per wide node, 2..8;
   - leaf size: items per leaf slot, 1..3 (the collapse schedule: subtrees of at most this many
     triangles become leaf slots, everything larger is opened);
-  - Morton normalisation of BLAS centroids: by the largest extent ("cube") or per axis;
+  - BLAS builder of FAST_TRACE meshes: binned SAH or Morton LBVH (``lcx_set_build_blas_sah``);
+  - Morton normalisation of BLAS centroids (LBVH builds): by the largest extent ("cube") or per axis;
   - triangle splitting of FAST_TRACE meshes: extra references as a fraction of the triangles.
 * traversal knobs (``lcx_set_trace_tuning`` / ``lcx_set_trace_stack`` / ``lcx_set_trace_reorder``):
   - ray-pool refill threshold: the number of idle lanes at which a warp takes new rays, 1..32;
@@ -40,7 +41,8 @@ from pathlib import Path
 from . import _capi
 from .accel import NODES_QUANT8, Accel, build_meshes, mesh_from_data
 
-BUILD_SPACE = {"leaf_max": [1, 2, 3], "width": [8, 6, 4], "blas_cube": [1, 0], "split": [0.0, 1.0, 3.0]}
+BUILD_SPACE = {"blas_sah": [1, 0], "leaf_max": [1, 2, 3], "width": [8, 6, 4], "blas_cube": [1, 0],
+               "split": [0.0, 1.0, 3.0]}
 TRACE_SPACE = {"refill": [1, 2, 4, 8, 16, 32], "short_stack": [8, 16, 24], "mode": [2, 0, 1, 3], "postpone": [0, 12, 32],
                "reorder_bits": [0, 7]}
 
@@ -56,6 +58,7 @@ class Config:
     reorder_bits: int = 0
     postpone: int = 0
     split: float = 0.0
+    blas_sah: int = 1
 
 
 @dataclass
@@ -91,8 +94,10 @@ def current() -> Config:
     _capi.check(lib.lcx_get_trace_reorder(rb, rm), "lcx_get_trace_reorder")
     sp = ctypes.c_float(0.0)
     _capi.check(lib.lcx_get_build_split(ctypes.byref(sp)), "lcx_get_build_split")
+    (bs,) = _u32(1)
+    _capi.check(lib.lcx_get_build_blas_sah(bs), "lcx_get_build_blas_sah")
     return Config(lm.value, w.value, bc.value, rf.value, ss.value, md.value, rb.value, pp.value,
-                  round(sp.value, 6))
+                  round(sp.value, 6), bs.value)
 
 
 def apply(cfg: Config):
@@ -105,6 +110,7 @@ def apply(cfg: Config):
     _capi.check(lib.lcx_set_build_tuning(cfg.leaf_max, cfg.width), "lcx_set_build_tuning")
     _capi.check(lib.lcx_set_build_morton(cfg.blas_cube, tc.value, sb.value), "lcx_set_build_morton")
     _capi.check(lib.lcx_set_build_split(ctypes.c_float(cfg.split)), "lcx_set_build_split")
+    _capi.check(lib.lcx_set_build_blas_sah(cfg.blas_sah), "lcx_set_build_blas_sah")
     _capi.check(lib.lcx_set_trace_tuning(cfg.refill, cfg.postpone, cfg.mode), "lcx_set_trace_tuning")
     _capi.check(lib.lcx_set_trace_stack(cfg.short_stack), "lcx_set_trace_stack")
     _capi.check(lib.lcx_set_trace_reorder(cfg.reorder_bits, rm.value), "lcx_set_trace_reorder")
@@ -254,7 +260,7 @@ def tune_batch_build(datas, *, sample: int = 512, reps: int = 3, sah_slack: floa
                      space: dict | None = None, log=None) -> TuneResult:
     """Tunes the build knobs for batched BLAS builds (``lcx_mesh_build_batch``) on the first
     ``sample`` meshes of ``datas`` (scenes.MeshData): among every point of the grid ``space``
-    (leaf size x node width x Morton normalisation) whose mean wide-BVH SAH is within
+    (BLAS builder x leaf size x node width x Morton normalisation) whose mean wide-BVH SAH is within
     ``sah_slack`` of the best one, the fastest build wins.  Build time is the median of
     ``reps`` CUDA-event timings.  Leaves the winner applied; ``default_ms`` / ``tuned_ms`` are
     the build times of the starting and the chosen configuration."""

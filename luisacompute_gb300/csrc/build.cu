@@ -27,6 +27,7 @@
 #include <cooperative_groups.h>
 #include <cooperative_groups/scan.h>
 
+#include <atomic>
 #include <cfloat>
 
 #include <cub/device/device_scan.cuh>
@@ -1477,6 +1478,7 @@ cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st);
 
 cudaError_t build_common(BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
     const uint32_t n = s.n;
+    note_build_launches(1);
     k_morton<<<blocks_for(n, 256), 256, 0, st>>>(s.segs, s.nseg, n, s.axis_bits, bp.size_bits, bp.cube, s.box_lo,
                                                   s.box_hi, s.segctl, s.keys, s.vals);
     cudaError_t e = sort_pairs(s.sort_tmp, s.sort_tmp_bytes, s.keys, s.keys_sorted, s.vals, s.vals_sorted, n,
@@ -1487,6 +1489,7 @@ cudaError_t build_common(BuildScratch &s, const BuildParams &bp, cudaStream_t st
         if (e != cudaSuccess) return e;
     }
     const uint32_t shift = s.nseg > 1 ? 3 * s.axis_bits : 64;
+    note_build_launches(1);
     k_lbvh<<<blocks_for(n, 256), 256, 0, st>>>(s.segs, n, shift, s.keys_sorted, s.vals_sorted, s.box_lo, s.box_hi,
                                                  s.bin_child, s.bin_lo, s.bin_hi, s.other, s.segctl);
     return build_rest(s, bp, st);
@@ -1496,8 +1499,10 @@ cudaError_t build_common(BuildScratch &s, const BuildParams &bp, cudaStream_t st
 cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
     const uint32_t n = s.n;
     const uint32_t shift = s.nseg > 1 ? 3 * s.axis_bits : 64;
+    note_build_launches(1);
     k_binary_sah<<<blocks_for(n, 256), 256, 0, st>>>(n, shift, s.keys_sorted, s.vals_sorted, s.bin_lo, s.bin_hi,
                                                        s.box_lo, s.box_hi, s.segs, s.segctl, s.bin_sah);
+    note_build_launches(1);
     k_collapse_init<<<blocks_for(s.nseg, 256), 256, 0, st>>>(s.segs, s.nseg, s.segctl, s.queue, s.desc, s.ctl);
     TreeView tv = make_view(s);
     const SegInput *segs = s.segs;
@@ -1506,6 +1511,7 @@ cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st) 
     uint2 *q0 = s.queue, *q1 = s.queue + s.queue_len;
     uint32_t *ctl = s.ctl, *segctl = s.segctl;
     void *args[] = {&tv, &segs, &lm, &width, &fill, &desc, &q0, &q1, &ctl, &segctl};
+    note_build_launches(1);
     return cudaLaunchCooperativeKernel(reinterpret_cast<void *>(k_collapse), dim3(collapse_grid()), dim3(128), args, 0,
                                        st);
 }
@@ -1520,10 +1526,19 @@ uint32_t morton_axis_bits(uint32_t nseg, uint32_t *seg_bits) {
     return ab > 21 ? 21 : ab;
 }
 
+namespace {
+std::atomic<uint64_t> g_build_launches{0};
+}
+
+void note_build_launches(uint32_t k) { g_build_launches.fetch_add(k, std::memory_order_relaxed); }
+uint64_t build_launches() { return g_build_launches.load(std::memory_order_relaxed); }
+
 cudaError_t build_tree_tris(BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
-    if (s.ref_prim == nullptr)  // with triangle splitting split_emit has written the item boxes
+    if (s.ref_prim == nullptr) {  // with triangle splitting split_emit has written the item boxes
+        note_build_launches(1);
         k_tri_prep<<<blocks_for(s.n, kPrepBlock), kPrepBlock, 0, st>>>(s.segs, s.nseg, s.n, s.box_lo, s.box_hi,
                                                                        s.segctl, s.ctl);
+    }
     return bp.blas_sah ? build_tree_sah(s, bp, st) : build_common(s, bp, st);
 }
 
@@ -1538,8 +1553,11 @@ cudaError_t split_count(const SegInput *tsegs, uint32_t nseg, uint32_t n, float 
     cudaError_t e = cudaMemsetAsync(sums, 0, sizeof(unsigned long long) * nseg + sizeof(uint32_t) * nseg, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(seg_refs, 0, sizeof(uint32_t) * nseg, st);
     if (e != cudaSuccess) return e;
+    note_build_launches(1);
     k_split_weight<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(tsegs, nseg, n, wts, wmax, segctl, ctl);
+    note_build_launches(1);
     k_split_quant<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(tsegs, nseg, n, wts, wmax, sums);
+    note_build_launches(1);
     k_split_assign<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(
         tsegs, nseg, n, reinterpret_cast<const uint32_t *>(wts), sums, fraction, refs, seg_refs);
     return cudaGetLastError();
@@ -1554,6 +1572,7 @@ cudaError_t curve_prepare(const unsigned char *cps, uint64_t stride, uint32_t cp
                           const uint32_t *seg, uint32_t nseg, uint32_t basis, float4 *bez, uint32_t *count,
                           uint32_t *meta, uint32_t *err, cudaStream_t st) {
     if (nseg == 0) return cudaSuccess;
+    note_build_launches(1);
     k_curve_prep<<<blocks_for(nseg, kPrepBlock), kPrepBlock, 0, st>>>(cps, stride, cp_count, keys, seg, nseg, basis,
                                                                        bez, count, meta, err);
     return cudaGetLastError();
@@ -1562,12 +1581,14 @@ cudaError_t curve_prepare(const unsigned char *cps, uint64_t stride, uint32_t cp
 cudaError_t curve_fill(const uint32_t *off, const uint32_t *count, uint32_t nseg, uint32_t *cone_seg,
                        cudaStream_t st) {
     if (nseg == 0) return cudaSuccess;
+    note_build_launches(1);
     k_curve_fill<<<blocks_for(nseg, kPrepBlock), kPrepBlock, 0, st>>>(off, count, nseg, cone_seg);
     return cudaGetLastError();
 }
 
 cudaError_t split_emit(const SegInput *tsegs, uint32_t nseg, uint32_t n, const uint32_t *refs, const uint32_t *ref_off,
                        BuildScratch &s, uint32_t *ref_prim, cudaStream_t st) {
+    note_build_launches(1);
     k_split_emit<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(tsegs, nseg, n, refs, ref_off, s.box_lo, s.box_hi,
                                                                    ref_prim, s.segctl);
     s.ref_prim = ref_prim;
@@ -1575,6 +1596,7 @@ cudaError_t split_emit(const SegInput *tsegs, uint32_t nseg, uint32_t n, const u
 }
 
 cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
+    note_build_launches(1);
     k_inst_prep<<<blocks_for(s.n, kPrepBlock), kPrepBlock, 0, st>>>(inst, s.n, s.box_lo, s.box_hi, s.w2o, s.segctl);
     return bp.tlas_sah ? build_tree_sah(s, bp, st) : build_common(s, bp, st);
 }
@@ -1582,6 +1604,7 @@ cudaError_t build_tree_insts(const InstState *inst, BuildScratch &s, const Build
 cudaError_t emit_blas(const BuildScratch &s, const BuildParams &bp, uint32_t wide_count, Node8Q *qn, Node8F *fn,
                       TriRec *tris, double *wide_sah, unsigned long long *rtab, cudaStream_t st,
                       bool count_on_device) {
+    note_build_launches(1);
     k_emit_blas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.segs, s.desc, wide_count, bp.leaf_max,
                                                               qn, fn, tris, s.segctl, s.ctl, wide_sah, rtab,
                                                               s.ref_prim, count_on_device);
@@ -1594,6 +1617,7 @@ __global__ void k_or_errors(const uint32_t *ctl, uint32_t *into) {
 }
 
 cudaError_t report_build_errors(const uint32_t *ctl, uint32_t *into, cudaStream_t st) {
+    note_build_launches(1);
     k_or_errors<<<1, 1, 0, st>>>(ctl, into);
     return cudaGetLastError();
 }
@@ -1601,6 +1625,7 @@ cudaError_t report_build_errors(const uint32_t *ctl, uint32_t *into, cudaStream_
 cudaError_t emit_tlas(const InstState *inst, const BuildScratch &s, const BuildParams &bp, uint32_t wide_count,
                       Node8Q *qn, Node8F *fn, InstRec *recs, double *wide_sah, unsigned long long *rtab,
                       cudaStream_t st) {
+    note_build_launches(1);
     k_emit_tlas<<<blocks_for(wide_count, 128), 128, 0, st>>>(make_view(s), s.segs, s.desc, wide_count, bp.leaf_max,
                                                               inst, s.w2o, qn, fn, recs, s.ctl, wide_sah, rtab);
     return cudaGetLastError();
@@ -1609,12 +1634,14 @@ cudaError_t emit_tlas(const InstState *inst, const BuildScratch &s, const BuildP
 cudaError_t apply_modifications(const ModRec *mods, uint32_t count, InstState *inst, uint32_t instance_count,
                                 cudaStream_t st) {
     if (count == 0) return cudaSuccess;
+    note_build_launches(1);
     k_apply_mods<<<blocks_for(count, 256), 256, 0, st>>>(mods, count, inst, instance_count);
     return cudaGetLastError();
 }
 
 cudaError_t init_instances(InstState *inst, uint32_t begin, uint32_t end, cudaStream_t st) {
     if (end <= begin) return cudaSuccess;
+    note_build_launches(1);
     k_init_instances<<<blocks_for(end - begin, 256), 256, 0, st>>>(inst, begin, end);
     return cudaGetLastError();
 }
@@ -1871,7 +1898,9 @@ cudaError_t refit_blas(const SegInput *segs, uint32_t nseg, uint32_t W, const un
     A.segs = segs;
     A.nseg = nseg;
     A.tris = tris;
+    note_build_launches(1);
     k_refit<false><<<blocks_for(W, 128), 128, 0, st>>>(A);
+    note_build_launches(1);
     k_requantize<<<blocks_for(W, 128), 128, 0, st>>>(W, qn, fn, ctl);
     return cudaGetLastError();
 }
@@ -1883,6 +1912,7 @@ cudaError_t refit_tlas(const InstState *inst, uint32_t n, float4 *ilo, float4 *i
     cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(uint32_t) * W, st);
     if (e != cudaSuccess) return e;
     // instance world boxes and inverses, as a build computes them (segctl: scratch)
+    note_build_launches(1);
     k_inst_prep<<<blocks_for(n, kPrepBlock), kPrepBlock, 0, st>>>(inst, n, ilo, ihi, w2o, segctl);
     RefitArgs A{};
     A.W = W;
@@ -1897,7 +1927,9 @@ cudaError_t refit_tlas(const InstState *inst, uint32_t n, float4 *ilo, float4 *i
     A.w2o = w2o;
     A.recs = recs;
     A.ninst = n;
+    note_build_launches(1);
     k_refit<true><<<blocks_for(W, 128), 128, 0, st>>>(A);
+    note_build_launches(1);
     k_requantize<<<blocks_for(W, 128), 128, 0, st>>>(W, qn, fn, ctl);
     return cudaGetLastError();
 }

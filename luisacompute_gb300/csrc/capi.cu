@@ -1658,6 +1658,12 @@ int lcx_get_build_tlas_sah(uint32_t *sah) {
     return LCX_OK;
 }
 
+int lcx_get_build_kernel_launches(uint64_t *count) {
+    if (!count) return fail(LCX_ERR_INVALID_ARG, "null output");
+    *count = build_launches();
+    return LCX_OK;
+}
+
 int lcx_set_build_blas_sah(uint32_t sah) {
     if (sah > 1) return fail(LCX_ERR_INVALID_ARG, "lcx_set_build_blas_sah: 0 or 1");
     g_build_tune.blas_sah = sah;

@@ -141,6 +141,10 @@ cudaError_t build_tree_sah(BuildScratch &s, const BuildParams &bp, cudaStream_t 
 cudaError_t build_tree_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st);
 // Temporary bytes of the SAH build's scan over n items (it shares the sort's scratch).
 size_t sah_scan_temp_bytes(uint32_t n);
+// Kernels of this library launched by builds, refits and instance updates: a host counter
+// (library kernels, CUB's sort and scan, are not counted).
+void note_build_launches(uint32_t k);
+uint64_t build_launches();
 
 // Triangle splitting (split builds).  split_count: per triangle 1 + its extra
 // references (refs; at most fraction x the segment's triangles extra per

@@ -54,6 +54,13 @@ constexpr uint32_t kSahMaxLevels = kSahMedianLevel + 40;
 constexpr uint32_t kSahSmallMedian = 24;
 constexpr uint32_t kBinThreads = 256, kBinWarps = kBinThreads / 32;
 constexpr uint32_t kSmallThreads = 128, kSmallWarps = kSmallThreads / 32;
+#ifndef LCX_SAH_THREAD_RANGE
+#define LCX_SAH_THREAD_RANGE 16
+#endif
+constexpr uint32_t kThreadRange = LCX_SAH_THREAD_RANGE;  // ranges of at most this many items: one thread
+// bins per axis in the small ranges' warps: 8 built the terrain BLAS 3 % faster but made the
+// 257-instance TLAS SAH 15.2 -> 15.8 and traversal 1.5 % slower
+constexpr int kSmallBins = kSahBins;
 
 // control words: small-range count, large-range counts of the two level parities, error bits
 enum : uint32_t { kCtrSmall = 0, kCtrLarge = 1, kCtrErr = 3, kCtrWords = 8 };
@@ -123,26 +130,37 @@ __device__ __forceinline__ float bin_hi_of(uint32_t v) { return v == 0u ? -FLT_M
 
 // Bins per unit length over [lo, hi]; 0 (every item in bin 0) for an empty, degenerate or
 // non-finite extent.
+template <int B = kSahBins>
 __device__ __forceinline__ float sah_scale(float lo, float hi) {
     const float e = hi - lo;
-    const float s = e > 0.0f ? float(kSahBins) / e : 0.0f;
+    const float s = e > 0.0f ? float(B) / e : 0.0f;
     return isfinite(s) ? s : 0.0f;
 }
-// The bin of centroid coordinate c: clamped to [0, kSahBins - 1]; NaN goes to bin 0.
+// The bin of centroid coordinate c: clamped to [0, B - 1]; NaN goes to bin 0.
+template <int B = kSahBins>
 __device__ __forceinline__ int sah_bin(float c, float lo, float scale) {
-    return int(fminf(fmaxf((c - lo) * scale, 0.0f), float(kSahBins - 1)));
+    return int(fminf(fmaxf((c - lo) * scale, 0.0f), float(B - 1)));
 }
 
-// Adds one item per valid lane to bin `key` of `bins` (every lane of the warp calls).  When the
-// valid lanes share the key, one lane adds the warp's count and box; else each adds its own.
-__device__ __forceinline__ void bin_add(uint32_t *bins, uint32_t key, bool valid, const float4 &l, const float4 &h) {
+// Adds one item per valid lane to three bins of `bins` (keys[q]: its bin key on axis q; every lane
+// of the warp calls).  For each axis whose key the valid lanes share, one lane adds the warp's count
+// and box (reduced once for all such axes); on the other axes each valid lane adds its own.
+__device__ __forceinline__ void bin_add3(uint32_t *bins, const uint32_t keys[3], bool valid, const float4 &l,
+                                         const float4 &h) {
     const unsigned vm = __ballot_sync(~0u, valid);
     if (vm == 0u) return;
     const uint32_t first = __ffs(vm) - 1u;
-    const uint32_t k0 = __shfl_sync(~0u, key, first);
-    if (__all_sync(~0u, !valid || key == k0)) {
-        float v[6] = {valid ? l.x : FLT_MAX,  valid ? l.y : FLT_MAX,  valid ? l.z : FLT_MAX,
-                      valid ? h.x : -FLT_MAX, valid ? h.y : -FLT_MAX, valid ? h.z : -FLT_MAX};
+    bool uni[3];
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const uint32_t k0 = __shfl_sync(~0u, keys[q], first);
+        uni[q] = __all_sync(~0u, !valid || keys[q] == k0);
+        any = any || uni[q];
+    }
+    float v[6] = {valid ? l.x : FLT_MAX,  valid ? l.y : FLT_MAX,  valid ? l.z : FLT_MAX,
+                  valid ? h.x : -FLT_MAX, valid ? h.y : -FLT_MAX, valid ? h.z : -FLT_MAX};
+    if (any) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
@@ -150,23 +168,20 @@ __device__ __forceinline__ void bin_add(uint32_t *bins, uint32_t key, bool valid
 #pragma unroll
             for (int q = 3; q < 6; q++) v[q] = fmaxf(v[q], __shfl_xor_sync(~0u, v[q], o));
         }
-        if ((threadIdx.x & 31u) == first) {
-            uint32_t *b = bins + size_t(k0) * kBinWords;
-            atomicAdd(b, uint32_t(__popc(vm)));
+    }
+    const bool leader = (threadIdx.x & 31u) == first;
 #pragma unroll
-            for (int q = 0; q < 3; q++) atomicMin(b + 1 + q, float_to_ordered(v[q]));
-#pragma unroll
-            for (int q = 3; q < 6; q++) atomicMax(b + 1 + q, float_to_ordered(v[q]));
+    for (int q = 0; q < 3; q++) {
+        if (uni[q] ? leader : valid) {
+            uint32_t *b = bins + size_t(keys[q]) * kBinWords;
+            atomicAdd(b, uni[q] ? uint32_t(__popc(vm)) : 1u);
+            atomicMin(b + 1, float_to_ordered(uni[q] ? v[0] : l.x));
+            atomicMin(b + 2, float_to_ordered(uni[q] ? v[1] : l.y));
+            atomicMin(b + 3, float_to_ordered(uni[q] ? v[2] : l.z));
+            atomicMax(b + 4, float_to_ordered(uni[q] ? v[3] : h.x));
+            atomicMax(b + 5, float_to_ordered(uni[q] ? v[4] : h.y));
+            atomicMax(b + 6, float_to_ordered(uni[q] ? v[5] : h.z));
         }
-    } else if (valid) {
-        uint32_t *b = bins + size_t(key) * kBinWords;
-        atomicAdd(b, 1u);
-        atomicMin(b + 1, float_to_ordered(l.x));
-        atomicMin(b + 2, float_to_ordered(l.y));
-        atomicMin(b + 3, float_to_ordered(l.z));
-        atomicMax(b + 4, float_to_ordered(h.x));
-        atomicMax(b + 5, float_to_ordered(h.y));
-        atomicMax(b + 6, float_to_ordered(h.z));
     }
 }
 
@@ -226,28 +241,29 @@ struct SahSplit {
 // The split of least cost from a range's bins (3 axes x kSahBins bins x kBinWords words); every
 // lane of the warp calls and gets the result.  Ties go to the lower axis, then the lower bin.
 __device__ SahSplit best_split(const uint32_t *bins) {
-    const uint32_t j = threadIdx.x & 15u;
+    const uint32_t lane = threadIdx.x & 31u, j = lane & 15u, half = lane >> 4;
     SahSplit r;
     float best = FLT_MAX;
     uint32_t best_key = kInvalid;
-    for (int k = 0; k < 3; k++) {
-        uint32_t pn, sn;
-        float3 pl, ph, sl, sh;
-        sweep_axis(bins + size_t(k) * kSahBins * kBinWords, pn, pl, ph, sn, sl, sh);
-        if (k == 0) {  // all bins: the range's box
-            r.box_l = shfl3(pl, 15, 16);
-            r.box_h = shfl3(ph, 15, 16);
-        }
+    // two sweeps: axis 0 in lanes 0-15 and axis 1 in lanes 16-31, then axis 2 in both halves
+    uint32_t pn[2], sn[2];
+    float3 pl[2], ph[2], sl[2], sh[2];
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const uint32_t k = it == 0 ? half : 2u;
+        sweep_axis(bins + size_t(k) * kSahBins * kBinWords, pn[it], pl[it], ph[it], sn[it], sl[it], sh[it]);
         // split between bins j and j + 1: the suffix from bin j + 1
-        const uint32_t rn = __shfl_down_sync(~0u, sn, 1, 16);
-        const float3 rl = shfl_down3(sl, 1), rh = shfl_down3(sh, 1);
-        const bool ok = j + 1u < uint32_t(kSahBins) && pn > 0u && rn > 0u;
-        const float cost = area3(pl, ph) * float(pn) + area3(rl, rh) * float(rn);
+        const uint32_t rn = __shfl_down_sync(~0u, sn[it], 1, 16);
+        const float3 rl = shfl_down3(sl[it], 1), rh = shfl_down3(sh[it], 1);
+        const bool ok = j + 1u < uint32_t(kSahBins) && pn[it] > 0u && rn > 0u;
+        const float cost = area3(pl[it], ph[it]) * float(pn[it]) + area3(rl, rh) * float(rn);
         if (ok && cost < best) {
             best = cost;
-            best_key = uint32_t(k) * kSahBins + j;
+            best_key = k * kSahBins + j;
         }
     }
+    r.box_l = shfl3(pl[0], 15);  // axis 0 over all bins: the range's box
+    r.box_h = shfl3(ph[0], 15);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float oc = __shfl_xor_sync(~0u, best, o);
@@ -267,14 +283,16 @@ __device__ SahSplit best_split(const uint32_t *bins) {
     }
     r.axis = int(best_key / kSahBins);
     r.bin = int(best_key % kSahBins);
-    uint32_t pn, sn;
-    float3 pl, ph, sl, sh;
-    sweep_axis(bins + size_t(r.axis) * kSahBins * kBinWords, pn, pl, ph, sn, sl, sh);
-    r.nl = __shfl_sync(~0u, pn, r.bin);
-    r.left_l = shfl3(pl, r.bin);
-    r.left_h = shfl3(ph, r.bin);
-    r.right_l = shfl3(sl, r.bin + 1);
-    r.right_h = shfl3(sh, r.bin + 1);
+    const bool second = r.axis == 2;                           // warp-uniform
+    const int src = (r.axis == 1 ? 16 : 0) + r.bin;            // the lane that swept the best split
+    const uint32_t p_n = second ? pn[1] : pn[0];
+    const float3 p_l = second ? pl[1] : pl[0], p_h = second ? ph[1] : ph[0];
+    const float3 s_l = second ? sl[1] : sl[0], s_h = second ? sh[1] : sh[0];
+    r.nl = __shfl_sync(~0u, p_n, src);
+    r.left_l = shfl3(p_l, src);
+    r.left_h = shfl3(p_h, src);
+    r.right_l = shfl3(s_l, src + 1);
+    r.right_h = shfl3(s_h, src + 1);
     return r;
 }
 
@@ -349,14 +367,21 @@ __global__ void __launch_bounds__(kBinThreads) k_sah_bin(uint32_t n, const uint3
     }
     __syncthreads();
     uint32_t t[kPer];
+    uint32_t lo_t = kInvalid, hi_t = 0u;
 #pragma unroll
     for (uint32_t j = 0; j < kPer; j++) {
         const uint32_t i = base + j * kBinThreads + threadIdx.x;
         t[j] = i < n ? pos_task[i] : kInvalid;
         if (t[j] != kInvalid) {
-            atomicMin(&t_min, t[j]);
-            atomicMax(&t_max, t[j]);
+            lo_t = min(lo_t, t[j]);
+            hi_t = max(hi_t, t[j]);
         }
+    }
+    lo_t = __reduce_min_sync(~0u, lo_t);
+    hi_t = __reduce_max_sync(~0u, hi_t);
+    if ((threadIdx.x & 31u) == 0u && lo_t != kInvalid) {
+        atomicMin(&t_min, lo_t);
+        atomicMax(&t_max, hi_t);
     }
     __syncthreads();
     const uint32_t t0 = t_min, t1 = t_max;  // the chunk meets at most two large ranges
@@ -378,12 +403,14 @@ __global__ void __launch_bounds__(kBinThreads) k_sah_bin(uint32_t n, const uint3
             slot = t[j] == t0 ? 0u : 1u;
             rec = task + size_t(kTaskWords) * t[j];
         }
+        uint32_t keys[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const int b =
                 valid ? sah_bin(axis_of(c, k), __uint_as_float(rec[kTLo + k]), __uint_as_float(rec[kTScale + k])) : 0;
-            bin_add(mine, slot * 3u * kSahBins + uint32_t(k) * kSahBins + uint32_t(b), valid, l, h);
+            keys[k] = slot * 3u * kSahBins + uint32_t(k) * kSahBins + uint32_t(b);
         }
+        bin_add3(mine, keys, valid, l, h);
     }
     __syncthreads();
     for (uint32_t w = threadIdx.x; w < 2 * kTaskBinWords; w += kBinThreads) {
@@ -536,20 +563,133 @@ __global__ void k_sah_scatter(uint32_t n, const uint32_t *pos_task, uint32_t *po
     pos_task_out[dst] = left ? rec[kTLeft] : rec[kTRight];
 }
 
+__device__ __forceinline__ float4 sbox_lo(const float *box, uint32_t p) {
+    return make_float4(box[p], box[kSahChunk + p], box[2 * kSahChunk + p], 0.0f);
+}
+__device__ __forceinline__ float4 sbox_hi(const float *box, uint32_t p) {
+    return make_float4(box[3 * kSahChunk + p], box[4 * kSahChunk + p], box[5 * kSahChunk + p], 0.0f);
+}
+
+// Sort key of item p on an axis: its box midpoint (the sort only orders the candidates of a
+// split, so it needs no agreement with the bins).
+__device__ __forceinline__ float sort_key(const float *box, uint32_t p, int axis) {
+#if LCX_SAH_SORT_KEY_FULL
+    return axis_of(centroid_of(sbox_lo(box, p), sbox_hi(box, p)), axis);
+#else
+    return 0.5f * (box[axis * kSahChunk + p] + box[(axis + 3) * kSahChunk + p]);
+#endif
+}
+
+// The subtree of a range of at most kThreadRange items, built by the calling thread alone with the
+// exact SAH of every split position: at each node the items are sorted by centroid on each axis
+// (a stable insertion sort of the range's order) and swept from both ends.  box: the block's item
+// boxes (6 x kSahChunk floats), perm: its order; nodes and links as in the warp levels.
+__device__ void thread_subtree(uint32_t ra0, uint32_t rb0, uint32_t up0, uint32_t a, uint32_t ss, uint16_t *perm,
+                               const float *box, float4 *bin_lo, float4 *bin_hi, uint32_t *bin_child,
+                               uint32_t *segctl) {
+    uint32_t st_r[kThreadRange], st_up[kThreadRange];
+    float rarea[kThreadRange];
+    int sp = 0;
+    st_r[sp] = ra0 | (rb0 << 16);
+    st_up[sp++] = up0;
+    while (sp > 0) {
+        --sp;
+        const uint32_t ra = st_r[sp] & 0xffffu, rb = st_r[sp] >> 16, up = st_up[sp], k = rb - ra;
+        float4 nl = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f), nh = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
+        for (uint32_t i = ra; i < rb; i++) {
+            const float4 l = sbox_lo(box, perm[i]), h = sbox_hi(box, perm[i]);
+            nl = make_float4(fminf(nl.x, l.x), fminf(nl.y, l.y), fminf(nl.z, l.z), 0.0f);
+            nh = make_float4(fmaxf(nh.x, h.x), fmaxf(nh.y, h.y), fmaxf(nh.z, h.z), 0.0f);
+        }
+        float best = FLT_MAX;
+        int best_axis = -1;
+        uint32_t best_pos = k / 2u;
+        for (int axis = 0; axis < 3; axis++) {
+            auto key = [&](uint32_t p) { return sort_key(box, p, axis); };
+            for (uint32_t i = ra + 1u; i < rb; i++) {  // stable insertion sort by centroid
+                const uint16_t p = perm[i];
+                const float kp = key(p);
+                uint32_t j = i;
+                while (j > ra && key(perm[j - 1u]) > kp) {
+                    perm[j] = perm[j - 1u];
+                    j--;
+                }
+                perm[j] = p;
+            }
+            float3 l = make_float3(FLT_MAX, FLT_MAX, FLT_MAX), h = make_float3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+            for (uint32_t i = rb - 1u; i > ra; i--) {  // rarea[j]: items j.. of the range
+                const float4 bl = sbox_lo(box, perm[i]), bh = sbox_hi(box, perm[i]);
+                l = fmin3(l, make_float3(bl.x, bl.y, bl.z));
+                h = fmax3(h, make_float3(bh.x, bh.y, bh.z));
+                rarea[i - ra] = area3(l, h);
+            }
+            l = make_float3(FLT_MAX, FLT_MAX, FLT_MAX);
+            h = make_float3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+            for (uint32_t i = ra; i + 1u < rb; i++) {  // split after item i
+                const float4 bl = sbox_lo(box, perm[i]), bh = sbox_hi(box, perm[i]);
+                l = fmin3(l, make_float3(bl.x, bl.y, bl.z));
+                h = fmax3(h, make_float3(bh.x, bh.y, bh.z));
+                const uint32_t nleft = i - ra + 1u;
+                const float cost = area3(l, h) * float(nleft) + rarea[nleft] * float(k - nleft);
+                if (cost < best) {
+                    best = cost;
+                    best_axis = axis;
+                    best_pos = nleft;
+                }
+            }
+        }
+        if (best_axis >= 0 && best_axis != 2) {  // back to the order of the best axis
+            const int axis = best_axis;
+            auto key = [&](uint32_t p) { return sort_key(box, p, axis); };
+            for (uint32_t i = ra + 1u; i < rb; i++) {
+                const uint16_t p = perm[i];
+                const float kp = key(p);
+                uint32_t j = i;
+                while (j > ra && key(perm[j - 1u]) > kp) {
+                    perm[j] = perm[j - 1u];
+                    j--;
+                }
+                perm[j] = p;
+            }
+        }
+        const uint32_t m = ra + best_pos;
+        const uint32_t node = a + m - 1u;
+        bin_lo[node] = make_float4(nl.x, nl.y, nl.z, __uint_as_float(k));
+        bin_hi[node] = make_float4(nh.x, nh.y, nh.z, __uint_as_float(a + ra));
+        link_child(up, ss, node, bin_child, segctl);
+        if (m - ra == 1u) {
+            link_child(node + 1u, ss, kLeafBit | (a + ra), bin_child, segctl);
+        } else {
+            st_r[sp] = ra | (m << 16);
+            st_up[sp++] = node + 1u;
+        }
+        if (rb - m == 1u) {
+            link_child((node + 1u) | (1u << 31), ss, kLeafBit | (a + m), bin_child, segctl);
+        } else {
+            st_r[sp] = m | (rb << 16);
+            st_up[sp++] = (node + 1u) | (1u << 31);
+        }
+    }
+}
+
 // One block per small range (at most kSahChunk items): the item boxes in shared memory, then
-// level by level one warp per open range: exact node box and centroid bounds, 16 bins per axis,
-// the split of least cost (the median when none separates the items), a stable partition of the
-// range's order, the internal node and the links; one-item children become leaves.
+// level by level one warp per open range of more than kThreadRange items: exact centroid bounds,
+// 16 bins per axis (their union is the node box), the split of least cost (the median when none
+// separates the items, and from level kSahSmallMedian on), a stable ballot partition of the
+// range's order, the internal node and the links; one-item children become leaves, children of
+// 2..kThreadRange items go to a list (in tlist at the range's offset: at most one entry of two
+// words per two items) that the block's threads then build one per thread (thread_subtree).
 __global__ void __launch_bounds__(kSmallThreads) k_sah_small(uint32_t n, uint32_t *ctr, const uint32_t *small,
                                                              const uint32_t *vals_in, uint32_t *vals_out,
                                                              const float4 *lo, const float4 *hi, float4 *bin_lo,
-                                                             float4 *bin_hi, uint32_t *bin_child, uint32_t *segctl) {
+                                                             float4 *bin_hi, uint32_t *bin_child, uint32_t *segctl,
+                                                             uint32_t *tlist) {
     __shared__ float s_box[6][kSahChunk];
     __shared__ uint32_t s_id[kSahChunk];
     __shared__ uint16_t s_perm[2][kSahChunk];      // the order, and each range's partition buffer
     __shared__ uint2 s_rng[2][kSahChunk / 2];      // open ranges: (a | b << 16, up) of this level and the next
     __shared__ uint32_t s_bins[kSmallWarps][kTaskBinWords];
-    __shared__ uint32_t s_cnt[2];
+    __shared__ uint32_t s_cnt[2], s_tcnt;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const unsigned below = (1u << lane) - 1u;
     const uint32_t total = min(ctr[kCtrSmall], n);
@@ -581,12 +721,37 @@ __global__ void __launch_bounds__(kSmallThreads) k_sah_small(uint32_t n, uint32_
             s_box[5][k] = h.z;
             s_perm[0][k] = uint16_t(k);
         }
+        uint32_t *tl = tlist + a;
         if (threadIdx.x == 0) {
-            s_rng[0][0] = make_uint2(nt << 16, root_up);
-            s_cnt[0] = 1u;
-            s_cnt[1] = 0u;
+            s_cnt[0] = s_cnt[1] = s_tcnt = 0u;
+            if (nt > kThreadRange) {
+                s_rng[0][0] = make_uint2(nt << 16, root_up);
+                s_cnt[0] = 1u;
+            } else {
+                tl[0] = nt << 16;
+                tl[1] = root_up;
+                s_tcnt = 1u;
+            }
         }
         __syncthreads();
+        // a child of 2..kThreadRange items to the thread list, a larger one to the next level
+        auto push = [&](uint32_t cur_next, uint32_t ra, uint32_t rb, uint32_t up) {
+            if (rb - ra <= kThreadRange) {
+                const uint32_t q = atomicAdd(&s_tcnt, 1u);
+                if (2u * q + 1u < nt) {
+                    tl[2u * q] = ra | (rb << 16);
+                    tl[2u * q + 1u] = up;
+                } else {
+                    atomicOr(&ctr[kCtrErr], kSahErrSmall);
+                }
+            } else {
+                const uint32_t q = atomicAdd(&s_cnt[cur_next], 1u);
+                if (q < kSahChunk / 2)
+                    s_rng[cur_next][q] = make_uint2(ra | (rb << 16), up);
+                else
+                    atomicOr(&ctr[kCtrErr], kSahErrSmall);
+            }
+        };
         uint32_t cur = 0u;
         for (uint32_t level = 0; level < kSahChunk; level++) {
             const uint32_t open = s_cnt[cur];
@@ -594,86 +759,68 @@ __global__ void __launch_bounds__(kSmallThreads) k_sah_small(uint32_t n, uint32_
             for (uint32_t r = warp; r < open; r += kSmallWarps) {
                 const uint2 R = s_rng[cur][r];
                 const uint32_t ra = R.x & 0xffffu, rb = R.x >> 16, up = R.y, cnt = rb - ra;
-                // node box and centroid bounds
-                float v[12];
+                // centroid bounds (the node box comes from the bins)
+                float v[6];
 #pragma unroll
                 for (int q = 0; q < 3; q++) {
-                    v[q] = v[6 + q] = FLT_MAX;
-                    v[3 + q] = v[9 + q] = -FLT_MAX;
+                    v[q] = FLT_MAX;
+                    v[3 + q] = -FLT_MAX;
                 }
                 for (uint32_t k = ra + lane; k < rb; k += 32u) {
                     const uint32_t p = s_perm[0][k];
-                    const float4 l = make_float4(s_box[0][p], s_box[1][p], s_box[2][p], 0.0f);
-                    const float4 h = make_float4(s_box[3][p], s_box[4][p], s_box[5][p], 0.0f);
-                    const float3 c = centroid_of(l, h);
-                    v[0] = fminf(v[0], l.x);
-                    v[1] = fminf(v[1], l.y);
-                    v[2] = fminf(v[2], l.z);
-                    v[3] = fmaxf(v[3], h.x);
-                    v[4] = fmaxf(v[4], h.y);
-                    v[5] = fmaxf(v[5], h.z);
-                    v[6] = fminf(v[6], c.x);
-                    v[7] = fminf(v[7], c.y);
-                    v[8] = fminf(v[8], c.z);
-                    v[9] = fmaxf(v[9], c.x);
-                    v[10] = fmaxf(v[10], c.y);
-                    v[11] = fmaxf(v[11], c.z);
+                    const float3 c = centroid_of(sbox_lo(&s_box[0][0], p), sbox_hi(&s_box[0][0], p));
+                    v[0] = fminf(v[0], c.x);
+                    v[1] = fminf(v[1], c.y);
+                    v[2] = fminf(v[2], c.z);
+                    v[3] = fmaxf(v[3], c.x);
+                    v[4] = fmaxf(v[4], c.y);
+                    v[5] = fmaxf(v[5], c.z);
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
-                    for (int q = 0; q < 12; q++) {
+                    for (int q = 0; q < 6; q++) {
                         const float x = __shfl_xor_sync(~0u, v[q], o);
-                        v[q] = (q % 6) < 3 ? fminf(v[q], x) : fmaxf(v[q], x);
+                        v[q] = q < 3 ? fminf(v[q], x) : fmaxf(v[q], x);
                     }
                 }
-                const float cl[3] = {v[6], v[7], v[8]};
-                const float sc[3] = {sah_scale(v[6], v[9]), sah_scale(v[7], v[10]), sah_scale(v[8], v[11])};
-                int axis = -1, bin = 0;
-                if (cnt > 2u && level < kSahSmallMedian) {
-                    uint32_t *wb = s_bins[warp];
-                    for (uint32_t q = lane; q < kTaskBinWords; q += 32u) wb[q] = bin_init(q);
-                    __syncwarp();
-                    for (uint32_t k0 = ra; k0 < rb; k0 += 32u) {
-                        const uint32_t k = k0 + lane;
-                        const bool valid = k < rb;
-                        float4 l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f);
-                        float4 h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
-                        if (valid) {
-                            const uint32_t p = s_perm[0][k];
-                            l = make_float4(s_box[0][p], s_box[1][p], s_box[2][p], 0.0f);
-                            h = make_float4(s_box[3][p], s_box[4][p], s_box[5][p], 0.0f);
-                        }
-                        const float3 c = centroid_of(l, h);
+                const float cl[3] = {v[0], v[1], v[2]};
+                const float sc[3] = {sah_scale<kSmallBins>(v[0], v[3]), sah_scale<kSmallBins>(v[1], v[4]),
+                                     sah_scale<kSmallBins>(v[2], v[5])};
+                uint32_t *wb = s_bins[warp];
+                for (uint32_t q = lane; q < 3u * kSmallBins * kBinWords; q += 32u) wb[q] = bin_init(q);
+                __syncwarp();
+                for (uint32_t k0 = ra; k0 < rb; k0 += 32u) {
+                    const uint32_t k = k0 + lane;
+                    const bool valid = k < rb;
+                    float4 l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f);
+                    float4 h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
+                    if (valid) {
+                        const uint32_t p = s_perm[0][k];
+                        l = sbox_lo(&s_box[0][0], p);
+                        h = sbox_hi(&s_box[0][0], p);
+                    }
+                    const float3 c = centroid_of(l, h);
+                    uint32_t keys[3];
 #pragma unroll
-                        for (int q = 0; q < 3; q++) {
-                            const int bq = sah_bin(axis_of(c, q), cl[q], sc[q]);
-                            bin_add(wb, uint32_t(q) * kSahBins + uint32_t(bq), valid, l, h);
-                        }
-                    }
-                    __syncwarp();
-                    const SahSplit sp = best_split(wb);
-                    axis = sp.axis;
-                    bin = sp.bin;
-                    __syncwarp();
+                    for (int q = 0; q < 3; q++)
+                        keys[q] = uint32_t(q) * kSmallBins + uint32_t(sah_bin<kSmallBins>(axis_of(c, q), cl[q], sc[q]));
+                    bin_add3(wb, keys, valid, l, h);
                 }
-                // left count with this rule; a split that separates nothing falls back to the median
+                __syncwarp();
+                const SahSplit sp = best_split(wb);
+                __syncwarp();
+                // the split's left count is the bins' (the partition below bins by the same function);
+                // deep levels, and ranges no bin boundary separates, split at the median
+                const int axis = level < kSahSmallMedian ? sp.axis : -1;
+                const int bin = sp.bin;
+                const uint32_t nl = axis >= 0 ? sp.nl : cnt / 2u;
                 auto goes_left = [&](uint32_t k) -> bool {
                     if (axis < 0) return k < ra + cnt / 2u;
                     const uint32_t p = s_perm[0][k];
-                    const float4 l = make_float4(s_box[0][p], s_box[1][p], s_box[2][p], 0.0f);
-                    const float4 h = make_float4(s_box[3][p], s_box[4][p], s_box[5][p], 0.0f);
-                    return sah_bin(axis_of(centroid_of(l, h), axis), cl[axis], sc[axis]) <= bin;
+                    const float3 c = centroid_of(sbox_lo(&s_box[0][0], p), sbox_hi(&s_box[0][0], p));
+                    return sah_bin<kSmallBins>(axis_of(c, axis), cl[axis], sc[axis]) <= bin;
                 };
-                uint32_t nl = 0u;
-                for (uint32_t k0 = ra; k0 < rb; k0 += 32u) {
-                    const uint32_t k = k0 + lane;
-                    nl += __popc(__ballot_sync(~0u, k < rb && goes_left(k)));
-                }
-                if (nl == 0u || nl == cnt) {
-                    axis = -1;
-                    nl = cnt / 2u;
-                }
                 const uint32_t m = ra + nl;
                 uint32_t L = 0u, Rn = 0u;
                 for (uint32_t k0 = ra; k0 < rb; k0 += 32u) {
@@ -683,37 +830,29 @@ __global__ void __launch_bounds__(kSmallThreads) k_sah_small(uint32_t n, uint32_
                     const unsigned bl = __ballot_sync(~0u, f), br = __ballot_sync(~0u, valid && !f);
                     if (valid) {
                         const uint32_t dst = f ? ra + L + __popc(bl & below) : m + Rn + __popc(br & below);
-                        s_perm[1][dst] = s_perm[0][k];
+                        if (f ? dst < m : dst < rb) s_perm[1][dst] = s_perm[0][k];
                     }
                     L += __popc(bl);
                     Rn += __popc(br);
                 }
+                if (L != nl && lane == 0) atomicOr(&ctr[kCtrErr], kSahErrSmall);
                 __syncwarp();
                 for (uint32_t k = ra + lane; k < rb; k += 32u) s_perm[0][k] = s_perm[1][k];
                 __syncwarp();
+                const float v_box[6] = {sp.box_l.x, sp.box_l.y, sp.box_l.z, sp.box_h.x, sp.box_h.y, sp.box_h.z};
                 if (lane == 0) {
                     const uint32_t node = a + m - 1u;
-                    bin_lo[node] = make_float4(v[0], v[1], v[2], __uint_as_float(cnt));
-                    bin_hi[node] = make_float4(v[3], v[4], v[5], __uint_as_float(a + ra));
+                    bin_lo[node] = make_float4(v_box[0], v_box[1], v_box[2], __uint_as_float(cnt));
+                    bin_hi[node] = make_float4(v_box[3], v_box[4], v_box[5], __uint_as_float(a + ra));
                     link_child(up, ss, node, bin_child, segctl);
-                    if (m - ra == 1u) {
+                    if (m - ra == 1u)
                         link_child(node + 1u, ss, kLeafBit | (a + ra), bin_child, segctl);
-                    } else {
-                        const uint32_t q = atomicAdd(&s_cnt[cur ^ 1u], 1u);
-                        if (q < kSahChunk / 2)
-                            s_rng[cur ^ 1u][q] = make_uint2(ra | (m << 16), node + 1u);
-                        else
-                            atomicOr(&ctr[kCtrErr], kSahErrSmall);
-                    }
-                    if (rb - m == 1u) {
+                    else
+                        push(cur ^ 1u, ra, m, node + 1u);
+                    if (rb - m == 1u)
                         link_child((node + 1u) | (1u << 31), ss, kLeafBit | (a + m), bin_child, segctl);
-                    } else {
-                        const uint32_t q = atomicAdd(&s_cnt[cur ^ 1u], 1u);
-                        if (q < kSahChunk / 2)
-                            s_rng[cur ^ 1u][q] = make_uint2(m | (rb << 16), (node + 1u) | (1u << 31));
-                        else
-                            atomicOr(&ctr[kCtrErr], kSahErrSmall);
-                    }
+                    else
+                        push(cur ^ 1u, m, rb, (node + 1u) | (1u << 31));
                 }
             }
             __syncthreads();
@@ -721,6 +860,13 @@ __global__ void __launch_bounds__(kSmallThreads) k_sah_small(uint32_t n, uint32_
             cur ^= 1u;
             __syncthreads();
         }
+        const uint32_t tc = min(s_tcnt, nt / 2u);
+        for (uint32_t j = threadIdx.x; j < tc; j += kSmallThreads) {
+            const uint32_t R = tl[2u * j], up = tl[2u * j + 1u];
+            thread_subtree(R & 0xffffu, R >> 16, up, a, ss, s_perm[0], &s_box[0][0], bin_lo, bin_hi, bin_child,
+                           segctl);
+        }
+        __syncthreads();
         for (uint32_t k = threadIdx.x; k < nt; k += kSmallThreads) vals_out[a + k] = s_id[s_perm[0][k]];
     }
 }
@@ -754,6 +900,7 @@ cudaError_t sah_tree(BuildScratch &s, cudaStream_t st, bool *ok) {
     SahLayout L = sah_layout(s);
     cudaError_t e = cudaMemsetAsync(L.ctr, 0, sizeof(uint32_t) * kCtrWords, st);
     if (e != cudaSuccess) return e;
+    note_build_launches(2);
     k_sah_seed<<<blocks_for(s.nseg, 128), 128, 0, st>>>(s.segs, s.nseg, L.cap, s.segctl, L.ctr, L.small, L.task[0],
                                                        L.bins[0], L.seg_task);
     k_sah_mark<<<blocks_for(n, 256), 256, 0, st>>>(s.segs, s.nseg, n, L.seg_task, L.pos_task[0], s.vals);
@@ -766,6 +913,7 @@ cudaError_t sah_tree(BuildScratch &s, cudaStream_t st, bool *ok) {
     for (uint32_t level = 0; h[kCtrErr] == 0u && h[kCtrLarge + par] > 0u; level++) {
         if (level >= kSahMaxLevels) return cudaSuccess;  // cannot happen: median splits from kSahMedianLevel
         const uint32_t large = std::min(h[kCtrLarge + par], L.cap);
+        note_build_launches(4);
         k_sah_bin<<<blocks_for(n, kSahChunk), kBinThreads, 0, st>>>(n, L.pos_task[par], vin, s.box_lo, s.box_hi,
                                                                     L.task[par], L.bins[par]);
         k_sah_split<<<blocks_for(uint64_t(large) * 32u, 128), 128, 0, st>>>(
@@ -788,11 +936,15 @@ cudaError_t sah_tree(BuildScratch &s, cudaStream_t st, bool *ok) {
     const uint32_t nsmall = h[kCtrSmall];
     if (nsmall > 0u) {
         const uint32_t grid = std::min<uint32_t>(nsmall, uint32_t(small_grid()));
+        note_build_launches(1);
         k_sah_small<<<grid, kSmallThreads, 0, st>>>(n, L.ctr, L.small, vin, s.vals_sorted, s.box_lo, s.box_hi, s.bin_lo,
-                                                    s.bin_hi, s.bin_child, s.segctl);
+                                                    s.bin_hi, s.bin_child, s.segctl,
+                                                    reinterpret_cast<uint32_t *>(s.other));
     }
-    if (s.nseg > 1)
+    if (s.nseg > 1) {
+        note_build_launches(1);
         k_sah_keys<<<blocks_for(n, 256), 256, 0, st>>>(s.segs, s.nseg, n, 3 * s.axis_bits, s.keys_sorted);
+    }
     e = cudaMemcpyAsync(h, L.ctr, sizeof(h), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;

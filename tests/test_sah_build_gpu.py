@@ -69,13 +69,24 @@ def _trace(scene, rays, batch):
 
 
 def _aimed(scene, n, seed):
-    """Rays from a box around the scene aimed at random points inside it."""
+    """Rays from random points of the scene's box, each aimed at the centroid of a random triangle
+    of a random instance."""
     lo, hi = scene.bounds()
     rng = np.random.default_rng(seed)
     rays = S.sphere_rays(n, lo, hi, seed=seed)
-    tgt = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    inst = np.array([i for i in range(scene.instance_count) if scene.meshes[scene.inst_mesh[i]].tri_count > 0])
+    pick = inst[rng.integers(0, inst.size, n)]
+    tgt = np.zeros((n, 3))
+    for i in np.unique(pick):
+        sel = pick == i
+        m = scene.meshes[scene.inst_mesh[i]]
+        t = rng.integers(0, m.tri_count, int(sel.sum()))
+        v = m.vertices[:, :3].astype(np.float64)
+        c = v[m.triangles[t].astype(np.int64)].mean(axis=1)
+        a = scene.inst_affine[i].astype(np.float64).reshape(3, 4)
+        tgt[sel] = c @ a[:, :3].T + a[:, 3]
     d = tgt - rays["o"]
-    rays["d"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays["d"] = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
     return rays
 
 
@@ -98,7 +109,7 @@ def test_sah_blas_sizes_and_degenerates(lcx, oracle_mod, batch):
         assert np.array_equal(occ, want_occ), f"blas_sah {sah}"
         for md, m in zip(meshes, meshes_d):
             assert int(m.stats().leaf_prim_count) == md.triangles.shape[0]
-    assert (want["inst"] != S.MISS).mean() > 0.2
+    assert (want["inst"] != S.MISS).mean() > 0.5
 
 
 def test_sah_blas_invalid_triangles(lcx):
@@ -108,8 +119,9 @@ def test_sah_blas_invalid_triangles(lcx):
     good = _strip(2500, rng)
     bad = S.MeshData(good.vertices.copy(), good.triangles.copy())
     bad.vertices[0:3 * 2500:15, 0] = np.nan
-    scene = _scene([bad], rng)
-    rays = _aimed(_scene([good], np.random.default_rng(26)), 50_000, seed=27)
+    good_scene = _scene([good], rng)
+    scene = S.Scene([bad], good_scene.inst_mesh, good_scene.inst_affine, good_scene.inst_mask)
+    rays = _aimed(good_scene, 50_000, seed=27)
     res = []
     for sah in (1, 0):
         with _Knob("blas_sah", sah):
@@ -118,7 +130,7 @@ def test_sah_blas_invalid_triangles(lcx):
         res.append((got, occ))
     assert np.array_equal(res[0][0].view(np.uint8), res[1][0].view(np.uint8))
     assert np.array_equal(res[0][1], res[1][1])
-    assert (res[0][0]["inst"] != S.MISS).mean() > 0.05
+    assert (res[0][0]["inst"] != S.MISS).mean() > 0.3
 
 
 def test_sah_lowers_the_heightfield_sah(lcx, oracle_mod):
@@ -187,4 +199,4 @@ def test_sah_tlas_many_instances(lcx, oracle_mod, count):
         torch.cuda.synchronize()
         assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), f"tlas_sah {on}"
         assert int(acc.stats().leaf_prim_count) == count
-    assert (want["inst"] != S.MISS).mean() > 0.1
+    assert (want["inst"] != S.MISS).mean() > 0.5
