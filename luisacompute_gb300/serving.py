@@ -15,9 +15,10 @@ scene that must be built before their rays run.  Two servers process the same ar
   priority than the build stream.  Scene builds run on their own thread and stream, so an
   upload never blocks admission.  Scenes live in an HBM budget with LRU eviction of scenes no
   queued or in-flight request needs; an evicted scene is rebuilt on demand.  Scenes resident before
-  requests arrive may be built with triangle splitting (``SceneStore.warm(split=...)``), which
-  traces scenes of long overlapping triangles faster without putting its build cost on any
-  request.  On a coherent CPU-GPU link the kernels read each request's pinned rays and write its
+  requests arrive are FAST_TRACE builds (binned SAH) and may use triangle splitting
+  (``SceneStore.warm(split=...)``), which traces scenes of long overlapping triangles faster
+  without putting its build cost on any request; builds on a request's path (uploads, rebuilds
+  after an eviction) are FAST_BUILD builds (Morton LBVH, about half the build time).  On a coherent CPU-GPU link the kernels read each request's pinned rays and write its
   pinned results directly (``direct_host``), with no copies.
 * ``PlainServer`` — one request at a time: build if needed, copy in, one trace call, copy out,
   wait, next.
@@ -38,7 +39,7 @@ import numpy as np
 
 from . import _capi
 from . import scenes as S
-from .accel import Accel, Mesh, stream_handle
+from .accel import HINT_FAST_BUILD, HINT_FAST_TRACE, Accel, AccelOption, Mesh, stream_handle
 
 
 @dataclass
@@ -73,9 +74,10 @@ class SceneStore:
     """Scenes by id: host data always, device BVHs within `budget_bytes` (LRU eviction).  A scene
     larger than the whole budget is refused (BudgetError) instead of overrunning it."""
 
-    def __init__(self, scenes: dict, budget_bytes: int):
+    def __init__(self, scenes: dict, budget_bytes: int, request_hint: int = HINT_FAST_BUILD):
         self.host = dict(scenes)         # id -> MeshData
         self.budget = budget_bytes
+        self.request_hint = request_hint  # AccelOption hint of builds on a request's path
         self.res: OrderedDict = OrderedDict()  # id -> _Resident, most recent last
         self.used = 0
         self.lock = threading.Lock()
@@ -95,7 +97,7 @@ class SceneStore:
         _capi.check(lib.lcx_set_build_split(ctypes.c_float(split)), "lcx_set_build_split")
         try:
             for sid in ids:
-                self.build(sid, None, stream)
+                self.build(sid, None, stream, hint=HINT_FAST_TRACE)
             torch.cuda.synchronize()
         finally:
             _capi.check(lib.lcx_set_build_split(old), "lcx_set_build_split")
@@ -154,9 +156,10 @@ class SceneStore:
             r.accel.destroy()
             r.mesh.destroy()
 
-    def build(self, sid: int, data: S.MeshData | None, stream) -> None:
+    def build(self, sid: int, data: S.MeshData | None, stream, hint: int | None = None) -> None:
         """Upload and build scene `sid` on `stream`; `data` registers a new scene under a new id
-        (scene ids are never reused, so no request races a replacement)."""
+        (scene ids are never reused, so no request races a replacement).  hint: the AccelOption
+        hint of the build (None: the store's request_hint)."""
         import torch
         if data is not None:
             with self.lock:
@@ -176,7 +179,7 @@ class SceneStore:
             v.copy_(hv, non_blocking=True)
             t = torch.empty(ht.shape, dtype=torch.int32, device="cuda")
             t.copy_(ht, non_blocking=True)
-        mesh = Mesh(v, t)
+        mesh = Mesh(v, t, AccelOption(hint=self.request_hint if hint is None else hint))
         mesh.build(stream=stream)
         acc = Accel()
         acc.emplace_back(mesh)
