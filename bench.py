@@ -955,9 +955,11 @@ def main():
         return e0.elapsed_time(e1)
 
     e2e_serial_ms = time_e2e(serial_step)
-    C.check(lib.lcx_set_host_access(C.HOST_STAGED), "host access")  # the staged path, for comparison
-    e2e_staged_ms = time_e2e(host_step)
-    C.check(lib.lcx_set_host_access(mode.value), "host access")
+    direct_value = None
+    if coherent.value:  # the direct path, for comparison
+        C.check(lib.lcx_set_host_access(C.HOST_DIRECT), "host access")
+        direct_value = n * e2e_steps / (time_e2e(host_step) / 1e3) / 1e9
+        C.check(lib.lcx_set_host_access(mode.value), "host access")
     e2e_ms = time_e2e(host_step)
     if world > 1:
         import torch.distributed as dist
@@ -980,10 +982,10 @@ def main():
                     "d2h_bytes_per_step": int(n * 24),
                     "path": ("lcx_trace_closest_host via ctypes, pinned host rays and hits: the traversal kernel "
                              "reads the rays from and writes the hits to host memory over the coherent CPU-GPU "
-                             "link (NVLink-C2C), no staging copies" if coherent.value and mode.value != C.HOST_STAGED
-                             else "lcx_trace_closest_host via ctypes: pinned host rays and hits, 2^21-ray chunks "
+                             "link (NVLink-C2C), no staging copies" if coherent.value and mode.value == C.HOST_DIRECT
+                             else "lcx_trace_closest_host via ctypes: pinned host rays and hits, 2^22-ray chunks "
                                   "through device staging, copies in the timed region overlapped with the traversal"),
-                    "staged_copies_value": n * e2e_steps / (e2e_staged_ms / 1e3) / 1e9,
+                    "direct_host_access_value": direct_value,
                     "serial_copies_value": n * e2e_steps / (e2e_serial_ms / 1e3) / 1e9},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_src,

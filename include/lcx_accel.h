@@ -505,11 +505,11 @@ LCX_API int lcx_trace_any_motion(uint64_t accel, const LcxRay *d_rays, const flo
  * paths (lcx_set_host_access):
  *   - direct: when both buffers are pinned (page-locked, each one allocation)
  *     and the device reads host memory through a coherent link (NVLink-C2C on
- *     Grace systems; the default there), the traversal kernel itself reads
- *     the rays from and writes the results to host memory, with no staging
- *     and no copies;
+ *     Grace systems; the default there for calls of at most 2^18 rays), the
+ *     traversal kernel itself reads the rays from and writes the results to
+ *     host memory, with no staging and no copies;
  *   - staged: otherwise the rays stream through device staging in chunks
- *     (lcx_set_host_chunk, default 2^21 rays; a ring of 4 chunks of staging,
+ *     (lcx_set_host_chunk, default 2^22 rays; a ring of 4 chunks of staging,
  *     56 B per ray, kept in a memory pool): the copy in of one chunk, the
  *     traversal of the previous one and the copy out of the one before run at
  *     once.  Stream-ordered like the device
@@ -529,7 +529,8 @@ LCX_API int lcx_trace_any_host(uint64_t accel, const LcxRay *h_rays, uint32_t ra
  * no reference counterpart. */
 LCX_API int lcx_set_host_chunk(uint32_t rays);
 /* Host-buffer trace path: LCX_HOST_AUTO (direct when the device has a
- * coherent host link and the buffers are pinned, else staged), LCX_HOST_STAGED,
+ * coherent host link, the buffers are pinned and the call has at most 2^18
+ * rays, else staged), LCX_HOST_STAGED,
  * LCX_HOST_DIRECT (direct whenever the buffers are pinned: on a device without
  * a coherent link the kernel's host accesses cross PCIe one by one).
  * lcx_get_host_access reports the mode and whether the current device has the

@@ -2045,7 +2045,9 @@ int lcx_trace_any(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint
 // the traversal of chunk i and the copy out of chunk i-1 run at once on the
 // device's copy-in, trace and copy-out streams.  Everything stays ordered
 // after `stream`'s earlier work, and `stream` waits for the last copy out.
-uint32_t g_host_chunk = 1u << 21;  // lcx_set_host_chunk (2^20: 5.65 ms, 2^21: 5.39, 2^22: 5.33 per 8.4M rays)
+// lcx_set_host_chunk: 8.4M rays at 2.00 / 2.13 / 2.17 / 2.17 Grays/s with 2^20 / 2^21 / 2^22 / 2^23
+// (4M rays: 1.80 / 1.85 / 1.97 / 1.93)
+uint32_t g_host_chunk = 1u << 22;
 std::atomic<uint32_t> g_host_access{LCX_HOST_AUTO};  // lcx_set_host_access
 
 // Whether the device reads host memory through the host's page tables: a
@@ -2095,10 +2097,15 @@ static int trace_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count, 
     DeviceState *ds = nullptr;
     if (int r = current_device_state(&ds)) return r;
     // direct access: the traversal reads the rays from and writes the results to the pinned host
-    // buffers itself, with no staging and no copies (on GB300 over NVLink-C2C: 4.62 ms per 8.4M
-    // rays, against 5.09 ms through staged chunks and 4.29 ms on device buffers)
+    // buffers itself, with no staging and no copies.  On GB300 over NVLink-C2C it traced 8.4M rays
+    // at 1.11-1.84 Grays/s from box to box, against 2.13-2.18 through staged 2^21..2^22-ray chunks
+    // (2.62 on device buffers; 4M rays: 1.11-1.78 against 1.85-1.98; 1M rays: 1.05-1.46 against
+    // 1.29-1.30), so the automatic choice takes it only for calls of at most kDirectAutoRays rays,
+    // where the staging's fixed costs weigh most.
+    constexpr uint32_t kDirectAutoRays = 1u << 18;
     const uint32_t access = g_host_access.load();
-    if (access == LCX_HOST_DIRECT || (access == LCX_HOST_AUTO && host_link_coherent(ds->device))) {
+    if (access == LCX_HOST_DIRECT ||
+        (access == LCX_HOST_AUTO && ray_count <= kDirectAutoRays && host_link_coherent(ds->device))) {
         const size_t out_bytes = size_t(ray_count) * (h_hits ? sizeof(LcxTriangleHit) : 1);
         const void *dr = pinned_device_address(h_rays, size_t(ray_count) * sizeof(LcxRay));
         const void *dout = pinned_device_address(h_hits ? static_cast<const void *>(h_hits) : h_occ, out_bytes);

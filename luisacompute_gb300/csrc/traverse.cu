@@ -688,6 +688,9 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
 // nodes and without counting; 1.77 -> 1.90 Grays/s on the terrain workload (visits per
 // ray 16.95 -> 17.76 nodes, 2.17 -> 2.42 triangle tests: the lagging best t
 // culls less; 31.7 tests per flush on average).
+#ifndef LCX_TRI_PREFETCH
+#define LCX_TRI_PREFETCH 0
+#endif
 #ifndef LCX_DEFER_CAP
 #define LCX_DEFER_CAP 64
 #endif
@@ -980,6 +983,13 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
                 while (bits != 0u && pos < uint32_t(kDeferCap)) {
                     const uint32_t k = __ffs(bits) - 1u;
                     bits &= bits - 1u;
+#if LCX_TRI_PREFETCH
+                    {  // the record's two 128-byte lines into L1 now, for the flush's loads
+                        const char *tp = reinterpret_cast<const char *>(tbase + k);
+                        asm volatile("prefetch.global.L1 [%0];" ::"l"(tp));
+                        asm volatile("prefetch.global.L1 [%0];" ::"l"(tp + 47));
+                    }
+#endif
                     Q.tri[pos] = tbase + k;
                     Q.rec[pos] = lane | (cur << 5);
                     pend |= 1u << cur;

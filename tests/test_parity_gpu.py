@@ -402,7 +402,8 @@ def test_host_buffer_traces(torch_cuda, lcx, oracle_mod, chunk, access):
     records bit for bit, for pinned and pageable buffers, both layouts, on a side stream, in every
     host access mode: staged (chunked through device staging with copies overlapped; a ray count
     that is not a multiple of the chunk, with 2^14 13 chunks through the 4-slot ring), direct (the
-    kernel reads and writes the pinned host buffers itself) and auto; the empty call is a no-op."""
+    kernel reads and writes the pinned host buffers itself) and auto (staged above 2^18 rays, as
+    here); the empty call is a no-op."""
     from luisacompute_gb300 import _capi
     lib = _capi.load()
     _capi.check(lib.lcx_set_host_access(access), "host access")
@@ -451,7 +452,7 @@ def test_host_buffer_traces(torch_cuda, lcx, oracle_mod, chunk, access):
         assert lib.lcx_set_host_chunk(100) == _capi.LCX_ERR_INVALID_ARG
         assert lib.lcx_set_host_access(3) == _capi.LCX_ERR_INVALID_ARG
     finally:
-        _capi.check(lib.lcx_set_host_chunk(1 << 21), "chunk")
+        _capi.check(lib.lcx_set_host_chunk(1 << 22), "chunk")
         _capi.check(lib.lcx_set_host_access(_capi.HOST_AUTO), "host access")
     no_kernel_errors()
 
