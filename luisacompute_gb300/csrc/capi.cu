@@ -2045,6 +2045,12 @@ int lcx_trace_any(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint
 // the traversal of chunk i and the copy out of chunk i-1 run at once on the
 // device's copy-in, trace and copy-out streams.  Everything stays ordered
 // after `stream`'s earlier work, and `stream` waits for the last copy out.
+#ifndef LCX_HOST_RAMP_SHIFT
+#define LCX_HOST_RAMP_SHIFT 3  // the first and last chunks: chunk >> this, doubling up to the chunk
+#endif
+#ifndef LCX_HOST_RING
+#define LCX_HOST_RING 4  // staging slots
+#endif
 // lcx_set_host_chunk: 8.4M rays at 2.00 / 2.13 / 2.17 / 2.17 Grays/s with 2^20 / 2^21 / 2^22 / 2^23
 // (4M rays: 1.80 / 1.85 / 1.97 / 1.93)
 uint32_t g_host_chunk = 1u << 22;
@@ -2084,7 +2090,7 @@ const void *pinned_device_address(const void *p, size_t bytes) {
     }
     return a.devicePointer;
 }
-constexpr uint32_t kHostRing = 4;
+constexpr uint32_t kHostRing = LCX_HOST_RING;
 
 static int trace_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *h_hits,
                       uint8_t *h_occ, uint32_t layout, void *stream) {
@@ -2131,7 +2137,7 @@ static int trace_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count, 
             off += c;
             left -= c;
         };
-        const uint64_t ramp0 = std::max<uint64_t>(chunk >> 3, 1u << 14);
+        const uint64_t ramp0 = std::max<uint64_t>(chunk >> LCX_HOST_RAMP_SHIFT, 1u << 14);
         for (uint64_t c = ramp0; c < chunk && left; c <<= 1) take(c);
         uint64_t down = 0;
         for (uint64_t c = chunk >> 1; c >= ramp0; c >>= 1) down += c;

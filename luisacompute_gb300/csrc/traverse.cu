@@ -689,6 +689,8 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
 // ray 16.95 -> 17.76 nodes, 2.17 -> 2.42 triangle tests: the lagging best t
 // culls less; 31.7 tests per flush on average).
 #ifndef LCX_TRI_PREFETCH
+// 1: prefetch each queued triangle record into L1 at queue time (terrain workload: 2.619 against
+// 2.606 Grays/s, within noise, so off)
 #define LCX_TRI_PREFETCH 0
 #endif
 #ifndef LCX_DEFER_CAP
