@@ -699,6 +699,11 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
 #ifndef LCX_DEFER_MIN_BLOCKS
 #define LCX_DEFER_MIN_BLOCKS 7
 #endif
+#ifndef LCX_DEFER_MIN_BLOCKS_EXT
+// motion launches (kExt 1): terrain workload with moving spheres 1.45 / 1.60 / 1.33 / 1.04 Grays/s
+// at 4 / 5 / 6 / 7 blocks per SM (6 and 7 spill)
+#define LCX_DEFER_MIN_BLOCKS_EXT 5
+#endif
 #ifndef LCX_DEFER_STACK
 #define LCX_DEFER_STACK 8
 #endif
@@ -709,11 +714,12 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
 #endif
 constexpr int kDeferCap = LCX_DEFER_CAP;  // queued triangle tests per warp
 
-template <bool kMulti>
+template <bool kMulti, int kExt = 0>
 struct DeferQueue {
     const TriRec *tri[kDeferCap];
     uint32_t rec[kDeferCap];       // ray record: lane | slot << 5
     float rr[9][64];               // per record: ox oy oz Sx Sy Sz perm tmin inst (perm, inst as bits)
+    float rtime[kExt ? 64 : 1];    // motion launches: per record, its ray's time
     unsigned long long key[64];    // per record: min (ordered t << 32 | prim)
     float2 uv[64];                 // per record: barycentrics of that minimum
     float tmax[64];                // per record: the owner's best t at the flush
@@ -724,14 +730,19 @@ struct DeferQueue {
 
 // kCount: the counting build (single-job closest hit), for the algorithmic bytes of this loop's own
 // visits: nodes visited, triangles queued (each is tested once), instances entered.
-template <int kLayout, bool kAny, int kShort, bool kMulti, bool kCount = false>
-__global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_deferred(TraceParams P) {
-    using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort, 0, LCX_WT_AT_FLUSH != 0>;
+// kExt 1: accels with motion instances or vertex-motion meshes (each ray has a time; an instance
+// entry takes the instance's matrix at that time, and the flush interpolates a moving triangle at
+// its ray's time); accels with curves stay on loop mode 0.
+template <int kLayout, bool kAny, int kShort, bool kMulti, bool kCount = false, int kExt = 0>
+__global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT : LCX_DEFER_MIN_BLOCKS)
+    k_trace_deferred(TraceParams P) {
+    static_assert(kExt <= 1, "curves take loop mode 0");
+    using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort, kExt, LCX_WT_AT_FLUSH != 0>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
-    __shared__ DeferQueue<kMulti> queues[kTraceBlock / 32];
+    __shared__ DeferQueue<kMulti, kExt> queues[kTraceBlock / 32];
     uint2 deep_stack[W_t::kDeepSlots];
     const uint32_t lane = threadIdx.x & 31u;
-    DeferQueue<kMulti> &Q = queues[threadIdx.x >> 5];
+    DeferQueue<kMulti, kExt> &Q = queues[threadIdx.x >> 5];
     W_t W(P, stack_mem + threadIdx.x, deep_stack);
     const int refill = int(P.refill);
     // queue size that starts a flush: P.postpone, or 24 for closest / 16 for any hit (measured on the
@@ -787,8 +798,17 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
 #endif
                 const float lo = Q.rr[7][r], hi = Q.tmax[r];
                 const float4 *tp = reinterpret_cast<const float4 *>(Q.tri[j]);
-                const float4 a = bvh_ld(tp), b = bvh_ld(tp + 1), c = bvh_ld(tp + 2);
-                if (wt_intersect(ray, lo, hi, a, b, c, t, u, v)) {
+                float4 a = bvh_ld(tp), b = bvh_ld(tp + 1), c = bvh_ld(tp + 2);
+                bool live = true;
+                if constexpr (kExt >= 1) {
+                    if (__float_as_uint(b.w) == kTriMotion) {  // a vertex-motion mesh: its triangle at the ray's time
+                        const MeshMotion *mm = reinterpret_cast<const MeshMotion *>(
+                            (unsigned long long)__float_as_uint(c.x) |
+                            ((unsigned long long)__float_as_uint(c.y) << 32));
+                        live = motion_triangle(*mm, __float_as_uint(a.w), Q.rtime[r], a, b, c);
+                    }
+                }
+                if (live && wt_intersect(ray, lo, hi, a, b, c, t, u, v)) {
                     hit = true;
                     key = kAny ? 0ull
                                : (static_cast<unsigned long long>(float_to_ordered(t)) << 32) | __float_as_uint(a.w);
@@ -1032,6 +1052,7 @@ __global__ void __launch_bounds__(kTraceBlock, LCX_DEFER_MIN_BLOCKS) k_trace_def
 #endif
                 Q.rr[7][r] = W.tmin;
                 Q.rr[8][r] = __uint_as_float(W.cur_inst);
+                if constexpr (kExt >= 1) Q.rtime[r] = W.time;
                 mine |= 1u << cur;
             }
         }
@@ -1164,12 +1185,12 @@ cudaError_t launch_stack(const TraceParams &p, cudaStream_t st) {
     return launch_one<L, A, false, 0, false, kDefaultShortStack>(p, st);
 }
 
-template <int L, bool A, int S, bool X = false, bool C = false>
+template <int L, bool A, int S, bool X = false, bool C = false, int E = 0>
 cudaError_t launch_deferred(const TraceParams &p, cudaStream_t st) {
     static int per_sm = 0;
     if (per_sm == 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_deferred<L, A, S, X, C>, kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_deferred<L, A, S, X, C, E>, kTraceBlock, 0);
         per_sm = b > 0 ? b : 1;
     }
     const uint64_t warps_needed = (uint64_t(p.ray_count) + 31) / 32;
@@ -1177,7 +1198,7 @@ cudaError_t launch_deferred(const TraceParams &p, cudaStream_t st) {
     const uint64_t grid_need = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
     if (grid_need < grid) grid = grid_need;
     if (grid == 0) grid = 1;
-    k_trace_deferred<L, A, S, X, C><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
+    k_trace_deferred<L, A, S, X, C, E><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -1222,7 +1243,17 @@ cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counti
     // quantised-node, non-counting calls, static or moving; the others run mode 0
     if (p.mode == 3 && p.jobs == nullptr && !counting && layout == LCX_NODES_QUANT8)
         return any ? launch_per_thread<true>(p, st) : launch_per_thread<false>(p, st);
-    if (p.motion) {  // accels with motion or curves: the extended kernels, loop mode 0
+    if (p.motion) {
+        // accels with motion instances or vertex-motion meshes: loop mode 2 (deferred triangle batches
+        // at each ray's time) with quantised nodes; curves, FP32 nodes, the counting build and the
+        // other loop modes: the extended kernels of loop mode 0
+        if (!p.curves && p.mode == 2 && layout == LCX_NODES_QUANT8 && !counting) {
+            if (p.jobs != nullptr)
+                return any ? launch_deferred<LCX_NODES_QUANT8, true, LCX_DEFER_STACK, true, false, 1>(p, st)
+                           : launch_deferred<LCX_NODES_QUANT8, false, LCX_DEFER_STACK, true, false, 1>(p, st);
+            return any ? launch_deferred<LCX_NODES_QUANT8, true, LCX_DEFER_STACK, false, false, 1>(p, st)
+                       : launch_deferred<LCX_NODES_QUANT8, false, LCX_DEFER_STACK, false, false, 1>(p, st);
+        }
         return p.curves ? launch_ext<2>(p, layout, any, counting, st) : launch_ext<1>(p, layout, any, counting, st);
     }
     if (p.jobs != nullptr) {  // multi-job launches: no counting; mode 2 with quantised nodes, else mode 0
