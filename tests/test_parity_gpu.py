@@ -319,6 +319,37 @@ def test_axis_aligned_exact_ties(torch_cuda, lcx, oracle_mod, layout):
     assert (got["inst"][:2 * m] != S.MISS).sum() >= 2 * 15 * 15
 
 
+@pytest.mark.parametrize("layout", [0, 1])
+def test_identity_instances(torch_cuda, lcx, oracle_mod, layout):
+    """Identity and translated instances of a mesh whose vertices include -0 and exact zeros,
+    against rays with +0 / -0 direction components and zero origins (signed zeros through the
+    instance transform, the slab reciprocals and the watertight test): the oracle's records bit
+    for bit."""
+    rng = np.random.default_rng(71)
+    grid = S.grid_mesh(24, 24)
+    v = grid.vertices.copy()
+    v[::7, 0] = -0.0
+    v[::5, 2] = 0.0
+    mesh = S.MeshData(v, grid.triangles)
+    aff = np.stack([S.IDENTITY, S.IDENTITY.copy()])
+    aff[1, 3] = 3.0  # a translated copy
+    scene = S.Scene([mesh, S.icosphere(2)], np.array([0, 0, 1]), np.concatenate([aff, S.IDENTITY[None]]),
+                    np.full(3, 0xFF, np.uint32))
+    lo, hi = scene.bounds()
+    rays = S.sphere_rays(60_000, lo, hi, seed=72)
+    k = rays.shape[0] // 4
+    rays["d"][:k, 0] = 0.0                       # +0 direction components
+    rays["d"][k:2 * k, 2] = -0.0                 # -0 direction components
+    rays["o"][2 * k:3 * k, 1] = rng.choice([0.0, -0.0], k).astype(np.float32)  # zero origins
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_closest(rays)
+    acc, _ = gpu_scene(scene)
+    got = trace(acc, rays, layout)
+    assert_bit_exact(oracle_mod, osc, rays, got, want)
+    assert (want["inst"] != S.MISS).mean() > 0.2
+    no_kernel_errors()
+
+
 @pytest.mark.parametrize("refill,postpone,mode", [(1, 0, 0), (8, 8, 0), (16, 12, 0), (32, 32, 0), (4, 20, 0),
                                                   (4, 0, 1), (16, 0, 1), (1, 8, 1),
                                                   (4, 0, 2), (1, 1, 2), (8, 16, 2), (32, 32, 2), (2, 5, 2),
