@@ -1477,6 +1477,7 @@ int collapse_grid() {
 cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st);
 
 cudaError_t build_common(BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
+    NvtxRange nr("LBVH: Morton codes, sort, radix tree");
     const uint32_t n = s.n;
     note_build_launches(1);
     k_morton<<<blocks_for(n, 256), 256, 0, st>>>(s.segs, s.nseg, n, s.axis_bits, bp.size_bits, bp.cube, s.box_lo,
@@ -1497,6 +1498,7 @@ cudaError_t build_common(BuildScratch &s, const BuildParams &bp, cudaStream_t st
 
 // After the binary tree: its SAH (and the BLAS bounding spheres), then the collapse.
 cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
+    NvtxRange nr("binary SAH, bounding spheres, collapse");
     const uint32_t n = s.n;
     const uint32_t shift = s.nseg > 1 ? 3 * s.axis_bits : 64;
     note_build_launches(1);

@@ -581,7 +581,7 @@ int try_reserved_rebuild(const std::vector<MeshObj *> &meshes, const std::vector
     BuildScratch s;
     if (int r = alloc_scratch(hold, s, blk->h_segs, blk->items, false, blk->d_segs, blk->d_segctl_init)) return r;
     {
-        NvtxRange nr("reserved rebuild: boxes, sort, LBVH, collapse");
+        NvtxRange nr("reserved rebuild: boxes, tree, collapse");
         LCX_CUDA(build_tree_tris(s, bp, st), "BLAS rebuild");
     }
     LCX_CUDA(cudaMemsetAsync(blk->wsah, 0, 2 * sizeof(double) * count, st), "cudaMemset");
@@ -769,7 +769,7 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
             LCX_CUDA(split_emit(d_tsegs, uint32_t(count), n, d_refs, d_ref_off, s, ref_prim, st), "triangle split");
         }
         {
-            NvtxRange nr("BLAS build: boxes, sort, LBVH, collapse");
+            NvtxRange nr("BLAS build: boxes, tree, collapse");
             LCX_CUDA(build_tree_tris(s, bp, st), "BLAS build");
         }
         if (int r = read_back(s, st, rb)) return r;
@@ -1560,7 +1560,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
         segs[0] = SegInput{nullptr, 0, nullptr, 0, 0, n, 0, nullptr};
         if (int r = alloc_scratch(hold, s, segs, n, true)) return r;
         {
-            NvtxRange nr("TLAS build: boxes, sort, LBVH, collapse");
+            NvtxRange nr("TLAS build: boxes, tree, collapse");
             LCX_CUDA(build_tree_insts(a->d_inst, s, bp, st), "TLAS build");
         }
         if (int r = read_back(s, st, rb)) return r;

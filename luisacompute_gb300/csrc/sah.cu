@@ -895,6 +895,7 @@ int small_grid() {
 // The binary tree; false in *ok when the device flagged an inconsistency (the caller rebuilds
 // with the LBVH).
 cudaError_t sah_tree(BuildScratch &s, cudaStream_t st, bool *ok) {
+    NvtxRange nr("binned-SAH tree");
     *ok = false;
     const uint32_t n = s.n;
     SahLayout L = sah_layout(s);
@@ -912,6 +913,7 @@ cudaError_t sah_tree(BuildScratch &s, cudaStream_t st, bool *ok) {
     uint32_t par = 0u;
     for (uint32_t level = 0; h[kCtrErr] == 0u && h[kCtrLarge + par] > 0u; level++) {
         if (level >= kSahMaxLevels) return cudaSuccess;  // cannot happen: median splits from kSahMedianLevel
+        NvtxRange lr("SAH level: ranges above 1024 items");
         const uint32_t large = std::min(h[kCtrLarge + par], L.cap);
         note_build_launches(4);
         k_sah_bin<<<blocks_for(n, kSahChunk), kBinThreads, 0, st>>>(n, L.pos_task[par], vin, s.box_lo, s.box_hi,
@@ -934,6 +936,7 @@ cudaError_t sah_tree(BuildScratch &s, cudaStream_t st, bool *ok) {
     }
     if (h[kCtrErr] != 0u) return cudaSuccess;
     const uint32_t nsmall = h[kCtrSmall];
+    NvtxRange sr("SAH: one block per range of at most 1024 items");
     if (nsmall > 0u) {
         const uint32_t grid = std::min<uint32_t>(nsmall, uint32_t(small_grid()));
         note_build_launches(1);
