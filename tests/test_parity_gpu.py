@@ -321,15 +321,20 @@ def test_axis_aligned_exact_ties(torch_cuda, lcx, oracle_mod, layout):
 
 @pytest.mark.parametrize("layout", [0, 1])
 def test_identity_instances(torch_cuda, lcx, oracle_mod, layout):
-    """Identity and translated instances of a mesh whose vertices include -0 and exact zeros,
-    against rays with +0 / -0 direction components and zero origins (signed zeros through the
-    instance transform, the slab reciprocals and the watertight test): the oracle's records bit
-    for bit."""
+    """Identity and translated instances of a flat grid whose zero coordinates are partly -0 (the
+    same geometry, signed zeros), against rays with +0 / -0 direction components and with origins
+    on the grid's plane (signed zeros through the instance transform, the slab reciprocals and the
+    watertight test): the oracle's records bit for bit.  (A grid folded by moving vertices onto
+    zero coordinates is not a fit: its overlapping coplanar triangles meet a ray at t values that
+    differ by rounding, and the oracle's own BVH then disagrees with its brute-force answer.)"""
     rng = np.random.default_rng(71)
-    grid = S.grid_mesh(24, 24)
+    grid = S.grid_mesh(25, 25)
     v = grid.vertices.copy()
-    v[::7, 0] = -0.0
-    v[::5, 2] = 0.0
+    v[::3, 1] = -0.0                                          # y = 0 everywhere: -0 on a third
+    zx = np.nonzero(v[:, 0] == 0.0)[0]
+    v[zx[::2], 0] = -0.0                                      # half of the x = 0 column
+    zz = np.nonzero(v[:, 2] == 0.0)[0]
+    v[zz[1::2], 2] = -0.0                                     # half of the z = 0 row
     mesh = S.MeshData(v, grid.triangles)
     aff = np.stack([S.IDENTITY, S.IDENTITY.copy()])
     aff[1, 3] = 3.0  # a translated copy
@@ -340,13 +345,14 @@ def test_identity_instances(torch_cuda, lcx, oracle_mod, layout):
     k = rays.shape[0] // 4
     rays["d"][:k, 0] = 0.0                       # +0 direction components
     rays["d"][k:2 * k, 2] = -0.0                 # -0 direction components
-    rays["o"][2 * k:3 * k, 1] = rng.choice([0.0, -0.0], k).astype(np.float32)  # zero origins
+    rays["o"][2 * k:3 * k, 1] = rng.choice([0.0, -0.0], k).astype(np.float32)  # origins on the plane
     osc = oracle_mod.OracleScene(scene)
     want = osc.trace_closest(rays)
+    assert np.array_equal(want.view(np.uint8), osc.brute_closest(rays).view(np.uint8))
     acc, _ = gpu_scene(scene)
     got = trace(acc, rays, layout)
     assert_bit_exact(oracle_mod, osc, rays, got, want)
-    assert (want["inst"] != S.MISS).mean() > 0.2
+    assert (want["inst"] != S.MISS).mean() > 0.3
     no_kernel_errors()
 
 
