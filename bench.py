@@ -64,6 +64,9 @@ def parse():
                          "(0: none; 3.0 measured p99 4.5-4.7 ms against 10.1 ms without)")
     ap.add_argument("--budget-gb", type=float, default=8.0, help="serving: HBM budget for scenes")
     ap.add_argument("--meshes", type=int, default=4096)
+    ap.add_argument("--builder", default="auto", choices=["auto", "sah", "lbvh"],
+                    help="batch_build: the BLAS builder of the FAST_TRACE meshes (auto: the autotuner's "
+                         "choice, or the library default with --no-autotune)")
     ap.add_argument("--instances", type=int, default=100_000)
     return ap.parse_args()
 
@@ -420,9 +423,15 @@ def run_batch_build(args):
     gen_s = time.perf_counter() - t0
     total = sum(m.tri_count for m in datas)
     tuned = None
+    from luisacompute_gb300 import _capi
+    if args.builder != "auto":  # a fixed builder, and the autotuner's other knobs
+        _capi.check(_capi.load().lcx_set_build_blas_sah(1 if args.builder == "sah" else 0), "builder")
     if not args.no_autotune:
         from luisacompute_gb300 import autotune
-        tuned = autotune.tune_batch_build(datas, sample=512).to_json()
+        space = None
+        if args.builder != "auto":
+            space = {k: v for k, v in autotune.BUILD_SPACE.items() if k not in ("split", "blas_sah")}
+        tuned = autotune.tune_batch_build(datas, sample=512, space=space).to_json()
     meshes = [mesh_from_data(m) for m in datas]
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
@@ -441,8 +450,10 @@ def run_batch_build(args):
 
     for _ in range(max(3, args.warmup)):
         build_meshes(meshes)
-    from luisacompute_gb300 import _capi
     lib = _capi.load()
+    sah_on = ctypes.c_uint32(0)
+    _capi.check(lib.lcx_get_build_blas_sah(ctypes.byref(sah_on)), "builder")
+    builder_name = "binned SAH" if sah_on.value else "Morton LBVH"
     launches0 = ctypes.c_uint64(0)
     _capi.check(lib.lcx_get_build_kernel_launches(ctypes.byref(launches0)), "launch count")
     with ClockSampler(0) as clocks:
@@ -525,7 +536,7 @@ def run_batch_build(args):
             "data": "synthetic (seeded)",
             "config": {"workload": f"{len(meshes)} meshes, {total} triangles, counts log-uniform [64, 262144], "
                                    "icosphere or grid with 1% Gaussian displacement; one lcx_mesh_build_batch per step",
-                       "generation_s": gen_s,
+                       "generation_s": gen_s, "blas_builder": builder_name,
                        "l2": "inputs (vertices + indices, ~2.6 GB) and outputs exceed the 129 MB L2"},
             "clocks": clocks.summary(), "gpu_launches": launches,
             "extra": {"one_by_one_mtris_s_first_256": sub_tris / single_s / 1e6,
