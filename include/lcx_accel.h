@@ -730,6 +730,14 @@ LCX_API int lcx_get_build_tlas_sah(uint32_t *sah);
  * triangles, so it takes longer than the LBVH; FAST_BUILD meshes, reserved
  * batches (lcx_mesh_build_batch_reserve, lcx_mesh_reserve_batch) and their
  * rebuilds keep the LBVH.  Default 1.  Results do not depend on it. */
+/* The collapse of FAST_TRACE BLASes and TLASes to wide nodes (0 or 1): 0
+ * opens the largest-area children greedily (then fills free slots by
+ * splitting leaf slots); 1 follows a dynamic program over the binary tree that
+ * minimises the wide tree's cost (Ylitie, Karras and Laine 2017).  Default 1.
+ * FAST_BUILD meshes and reserved batches keep the greedy collapse.  Results do
+ * not depend on it. */
+LCX_API int lcx_set_build_collapse(uint32_t mode);
+LCX_API int lcx_get_build_collapse(uint32_t *mode);
 LCX_API int lcx_set_build_blas_sah(uint32_t sah);
 LCX_API int lcx_get_build_blas_sah(uint32_t *sah);
 /* Kernels of this library launched by builds, refits and instance updates

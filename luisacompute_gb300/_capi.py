@@ -179,6 +179,8 @@ _SIGS = {
     "lcx_set_build_fill": (c_int, [c_uint32]),
     "lcx_set_build_tlas_sah": (c_int, [c_uint32]),
     "lcx_get_build_tlas_sah": (c_int, [POINTER(c_uint32)]),
+    "lcx_set_build_collapse": (c_int, [c_uint32]),
+    "lcx_get_build_collapse": (c_int, [POINTER(c_uint32)]),
     "lcx_set_build_blas_sah": (c_int, [c_uint32]),
     "lcx_get_build_blas_sah": (c_int, [POINTER(c_uint32)]),
     "lcx_get_build_kernel_launches": (c_int, [POINTER(c_uint64)]),

@@ -7,6 +7,7 @@ It measures, on the caller's own scene and rays, and picks:
   - leaf size: items per leaf slot, 1..3 (the collapse schedule: subtrees of at most this many
     triangles become leaf slots, everything larger is opened);
   - BLAS builder of FAST_TRACE meshes: binned SAH or Morton LBVH (``lcx_set_build_blas_sah``);
+  - collapse to wide nodes: dynamic program or greedy (``lcx_set_build_collapse``);
   - Morton normalisation of BLAS centroids (LBVH builds): by the largest extent ("cube") or per axis;
   - triangle splitting of FAST_TRACE meshes: extra references as a fraction of the triangles.
 * traversal knobs (``lcx_set_trace_tuning`` / ``lcx_set_trace_stack`` / ``lcx_set_trace_reorder``):
@@ -41,8 +42,8 @@ from pathlib import Path
 from . import _capi
 from .accel import NODES_QUANT8, Accel, build_meshes, mesh_from_data
 
-BUILD_SPACE = {"blas_sah": [1, 0], "leaf_max": [1, 2, 3], "width": [8, 6, 4], "blas_cube": [1, 0],
-               "split": [0.0, 1.0, 3.0]}
+BUILD_SPACE = {"blas_sah": [1, 0], "collapse": [1, 0], "leaf_max": [1, 2, 3], "width": [8, 6, 4],
+               "blas_cube": [1, 0], "split": [0.0, 1.0, 3.0]}
 TRACE_SPACE = {"refill": [1, 2, 4, 8, 16, 32], "short_stack": [8, 16, 24], "mode": [2, 0, 1, 3], "postpone": [0, 12, 32],
                "reorder_bits": [0, 7]}
 
@@ -59,6 +60,7 @@ class Config:
     postpone: int = 0
     split: float = 0.0
     blas_sah: int = 1
+    collapse: int = 1
 
 
 @dataclass
@@ -96,8 +98,10 @@ def current() -> Config:
     _capi.check(lib.lcx_get_build_split(ctypes.byref(sp)), "lcx_get_build_split")
     (bs,) = _u32(1)
     _capi.check(lib.lcx_get_build_blas_sah(bs), "lcx_get_build_blas_sah")
+    (cm,) = _u32(1)
+    _capi.check(lib.lcx_get_build_collapse(cm), "lcx_get_build_collapse")
     return Config(lm.value, w.value, bc.value, rf.value, ss.value, md.value, rb.value, pp.value,
-                  round(sp.value, 6), bs.value)
+                  round(sp.value, 6), bs.value, cm.value)
 
 
 def apply(cfg: Config):
@@ -111,6 +115,7 @@ def apply(cfg: Config):
     _capi.check(lib.lcx_set_build_morton(cfg.blas_cube, tc.value, sb.value), "lcx_set_build_morton")
     _capi.check(lib.lcx_set_build_split(ctypes.c_float(cfg.split)), "lcx_set_build_split")
     _capi.check(lib.lcx_set_build_blas_sah(cfg.blas_sah), "lcx_set_build_blas_sah")
+    _capi.check(lib.lcx_set_build_collapse(cfg.collapse), "lcx_set_build_collapse")
     _capi.check(lib.lcx_set_trace_tuning(cfg.refill, cfg.postpone, cfg.mode), "lcx_set_trace_tuning")
     _capi.check(lib.lcx_set_trace_stack(cfg.short_stack), "lcx_set_trace_stack")
     _capi.check(lib.lcx_set_trace_reorder(cfg.reorder_bits, rm.value), "lcx_set_trace_reorder")

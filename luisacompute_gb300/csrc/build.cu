@@ -843,6 +843,7 @@ struct TreeView {
     const uint32_t *vals;   // sorted item ids
     const unsigned long long *keys;
     uint32_t seg_shift;     // segment = key >> seg_shift (64: a single segment)
+    const uint32_t *dp_dec = nullptr;  // collapse by dynamic program: decisions per binary node (else greedy)
     __device__ __forceinline__ bool leaf(uint32_t id) const { return (id & kLeafBit) != 0; }
     __device__ __forceinline__ uint32_t count(uint32_t id) const {
         return leaf(id) ? 1u : __float_as_uint(blo[id].w);
@@ -885,12 +886,46 @@ __device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t
         C[1] = tv.child[2 * b + 1];
         nC = 2;
     }
+    const uint32_t kw = (tv.dp_dec != nullptr && !tv.leaf(b)) ? (tv.dp_dec[b] & 7u) : 0u;
+    if (kw != 0u) {
+        // the dynamic program's choice: `width` slots split kw | width - kw between b's children, each
+        // side expanded by its own decisions (a subtree given i slots either takes i - 1, or splits
+        // i = k + (i - k) between its children)
+        nC = 0;
+        uint32_t sn[8], si[8];
+        int sp = 0;
+        sn[sp] = C[1];
+        si[sp++] = uint32_t(width) - kw;
+        sn[sp] = C[0];
+        si[sp++] = kw;
+        while (sp > 0 && nC < 8) {
+            --sp;
+            uint32_t nd = sn[sp], i = si[sp];
+            for (int guard = 0; guard < 16; guard++) {
+                if (tv.leaf(nd) || i <= 1u) {
+                    C[nC++] = nd;
+                    break;
+                }
+                const uint32_t d = (tv.dp_dec[nd] >> (3u * (i - 1u))) & 7u;
+                if (d == 0u || d >= i) {
+                    i--;  // fewer slots serve this subtree as well
+                    continue;
+                }
+                if (sp < 8) {
+                    sn[sp] = tv.child[2 * nd + 1];
+                    si[sp++] = i - d;
+                }
+                nd = tv.child[2 * nd];
+                i = d;
+            }
+        }
+    }
     for (int k = 0; k < nC; k++) {
         float4 l, h;
         tv.box(C[k], l, h);
         A[k] = box_area(l, h);
     }
-    while (nC < width) {
+    while (kw == 0u && nC < width) {
         int best = -1;
         float best_a = -1.0f;
         for (int k = 0; k < nC; k++) {
@@ -910,7 +945,7 @@ __device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t
         A[nC] = box_area(l, h);
         nC++;
     }
-    while (fill && nC < width) {  // every child is a leaf slot now: split the largest splittable one
+    while (kw == 0u && fill && nC < width) {  // every child is a leaf slot now: split the largest splittable one
         int best = -1;
         float best_a = -1.0f;
         for (int k = 0; k < nC; k++) {
@@ -1037,6 +1072,105 @@ __device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t
             qout[qbase + rank] = make_uint2(c, child_base + rank);
             rank++;
         }
+    }
+}
+
+// ---- collapse by dynamic program (Ylitie, Karras & Laine 2017, "Efficient Incoherent Ray
+// Traversal on GPUs Through Compressed Wide BVHs"): bottom-up over the binary tree, the cost of
+// each subtree given i = 1..width slots of its wide parent -- a leaf slot (at most leaf_max items,
+// cost dp_prim x area x items), a wide node of its own (cost area + the best split of `width` slots
+// between its children), or for i > 1 the best split of i slots between its children -- and the
+// decisions that reach it, which the collapse then follows instead of opening the largest child.
+// Costs are in units of the root-independent box area; a node test costs 1.
+
+// Parent of every item and internal binary node (kInvalid: none, a segment root).
+__global__ void k_dp_parents(TreeView tv, const SegInput *segs, uint32_t nseg, uint32_t n, uint32_t *parent_item,
+                             uint32_t *parent_node) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j + 1u >= n) return;
+    const uint32_t s = segment_of(segs, nseg, j);
+    if (j + 1u >= segs[s].item_offset + segs[s].item_count) return;  // not an internal node
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+        const uint32_t c = tv.child[2ull * j + side];
+        if (c & kLeafBit) {
+            if ((c & ~kLeafBit) < n) parent_item[c & ~kLeafBit] = j;
+        } else if (c < n) {
+            parent_node[c] = j;
+        }
+    }
+}
+
+__device__ __forceinline__ void dp_child_costs(const TreeView &tv, uint32_t c, int width, float cp, const float *cost,
+                                               float out[8]) {
+    if (tv.leaf(c)) {
+        float4 l, h;
+        tv.box(c, l, h);
+        const float v = cp * box_area(l, h);
+        for (int i = 0; i < 8; i++) out[i] = v;
+    } else {
+        for (int i = 0; i < 8; i++) out[i] = i < width ? __ldcg(cost + 8ull * c + i) : FLT_MAX;
+    }
+}
+
+// The costs and decisions of internal node nd from its children's.  dec word: bits 0..2 the split
+// of `width` slots when nd is a wide node; bits 3(i-1)..3(i-1)+2 for i = 2..width: 0 = take i - 1
+// slots, else k = the left child's share of i slots.
+__device__ void dp_node(const TreeView &tv, uint32_t nd, int width, int leaf_max, float cp, float *cost,
+                        uint32_t *dec) {
+    float cl[8], cr[8];
+    dp_child_costs(tv, tv.child[2ull * nd], width, cp, cost, cl);
+    dp_child_costs(tv, tv.child[2ull * nd + 1], width, cp, cost, cr);
+    float dist[9];
+    uint32_t dk[9];
+    for (int j = 0; j <= 8; j++) {
+        dist[j] = FLT_MAX;
+        dk[j] = 0u;
+    }
+    for (int j = 2; j <= width; j++)
+        for (int k = 1; k < j; k++) {
+            const float v = cl[k - 1] + cr[j - k - 1];
+            if (v < dist[j]) {
+                dist[j] = v;
+                dk[j] = uint32_t(k);
+            }
+        }
+    float4 l, h;
+    tv.box(nd, l, h);
+    const float a = box_area(l, h);
+    const uint32_t cnt = tv.count(nd);
+    uint32_t word = 0u;
+    float prev;
+    if (cnt <= uint32_t(leaf_max)) {
+        prev = cp * a * float(cnt);
+    } else {
+        prev = a + dist[width];
+        word = dk[width];
+    }
+    cost[8ull * nd] = prev;
+    for (int i = 2; i <= width; i++) {
+        if (dist[i] < prev) {
+            prev = dist[i];
+            word |= dk[i] << (3 * (i - 1));
+        }
+        cost[8ull * nd + i - 1] = prev;
+    }
+    for (int i = width + 1; i <= 8; i++) cost[8ull * nd + i - 1] = prev;
+    dec[nd] = word;
+}
+
+// One thread per item walks up; the second arrival at a node computes it (its other subtree is done).
+__global__ void k_dp_up(TreeView tv, uint32_t n, int width, int leaf_max, float cp, const uint32_t *parent_item,
+                        const uint32_t *parent_node, uint32_t *arrivals, float *cost, uint32_t *dec) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    uint32_t nd = parent_item[p];
+    for (uint32_t guard = 0; guard < n && nd < n; guard++) {
+        __threadfence();
+        if (atomicAdd(&arrivals[nd], 1u) == 0u) return;
+        __threadfence();
+        dp_node(tv, nd, width, leaf_max, cp, cost, dec);
+        nd = parent_node[nd];
     }
 }
 
@@ -1504,9 +1638,23 @@ cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st) 
     note_build_launches(1);
     k_binary_sah<<<blocks_for(n, 256), 256, 0, st>>>(n, shift, s.keys_sorted, s.vals_sorted, s.bin_lo, s.bin_hi,
                                                        s.box_lo, s.box_hi, s.segs, s.segctl, s.bin_sah);
+    TreeView tv = make_view(s);
+    if (s.dp_cost != nullptr && n > 1) {
+        // scratch the tree no longer needs: the Morton keys hold the parents, the unsorted ids the
+        // arrival counters, the LBVH's sibling words the decisions
+        uint32_t *parent_item = reinterpret_cast<uint32_t *>(s.keys), *parent_node = parent_item + n;
+        uint32_t *arrivals = s.vals, *dec = reinterpret_cast<uint32_t *>(s.other);
+        cudaError_t e = cudaMemsetAsync(parent_item, 0xff, sizeof(uint32_t) * 2ull * n, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(arrivals, 0, sizeof(uint32_t) * n, st);
+        if (e != cudaSuccess) return e;
+        note_build_launches(2);
+        k_dp_parents<<<blocks_for(n, 256), 256, 0, st>>>(tv, s.segs, s.nseg, n, parent_item, parent_node);
+        k_dp_up<<<blocks_for(n, 256), 256, 0, st>>>(tv, n, bp.width, bp.leaf_max, bp.dp_prim, parent_item,
+                                                     parent_node, arrivals, s.dp_cost, dec);
+        tv.dp_dec = dec;
+    }
     note_build_launches(1);
     k_collapse_init<<<blocks_for(s.nseg, 256), 256, 0, st>>>(s.segs, s.nseg, s.segctl, s.queue, s.desc, s.ctl);
-    TreeView tv = make_view(s);
     const SegInput *segs = s.segs;
     int lm = bp.leaf_max, width = bp.width, fill = bp.fill ? 1 : 0;
     uint32_t *desc = s.desc;

@@ -93,6 +93,8 @@ struct BuildParams {
     uint32_t fill = 0;       // BLAS collapse: split leaf slots into finer ones while slots are free
     uint32_t tlas_sah = 0;   // TLAS: a binned-SAH binary tree instead of the LBVH
     uint32_t blas_sah = 0;   // BLAS: a binned-SAH binary tree instead of the LBVH (never in a capturable rebuild)
+    uint32_t dp = 0;         // collapse by the dynamic program over the binary tree (else greedy)
+    float dp_prim = 0.3f;    // the dynamic program's cost of an item test against a node test of 1
 };
 
 // Per-build device scratch, sized for n items in nseg segments.
@@ -120,6 +122,7 @@ struct BuildScratch {
     void *sort_tmp = nullptr;
     size_t sort_tmp_bytes = 0;
     const uint32_t *ref_prim = nullptr;  // split builds: triangle (local index) of each item (reference)
+    float *dp_cost = nullptr;            // collapse by dynamic program: 8 costs per binary node (else null)
 };
 
 size_t sort_temp_bytes(uint32_t n);

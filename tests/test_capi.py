@@ -36,7 +36,7 @@ def test_tuning_knobs_round_trip_and_range_checks(lcx):
     old = A.current()
     try:
         cfg = A.Config(leaf_max=3, width=4, blas_cube=0, refill=16, short_stack=24, mode=1, reorder_bits=7,
-                       postpone=12, split=1.0, blas_sah=0)
+                       postpone=12, split=1.0, blas_sah=0, collapse=0)
         A.apply(cfg)
         assert A.current() == cfg
         assert lcx.lcx_set_trace_stack(12) == _capi.LCX_ERR_INVALID_ARG
@@ -48,6 +48,7 @@ def test_tuning_knobs_round_trip_and_range_checks(lcx):
         assert lcx.lcx_set_trace_tuning(4, 0, 4) == _capi.LCX_ERR_INVALID_ARG
         assert lcx.lcx_set_build_split(ctypes.c_float(-1.0)) == _capi.LCX_ERR_INVALID_ARG
         assert lcx.lcx_set_build_blas_sah(2) == _capi.LCX_ERR_INVALID_ARG
+        assert lcx.lcx_set_build_collapse(2) == _capi.LCX_ERR_INVALID_ARG
         assert lcx.lcx_set_build_tlas_sah(2) == _capi.LCX_ERR_INVALID_ARG
         assert A.current() == cfg  # rejected calls change nothing
     finally:

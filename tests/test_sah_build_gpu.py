@@ -200,3 +200,34 @@ def test_sah_tlas_many_instances(lcx, oracle_mod, count):
         assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), f"tlas_sah {on}"
         assert int(acc.stats().leaf_prim_count) == count
     assert (want["inst"] != S.MISS).mean() > 0.5
+
+
+@pytest.mark.parametrize("batch", [False, True])
+def test_dp_collapse(lcx, oracle_mod, batch):
+    """The collapse by dynamic program (lcx_set_build_collapse 1, the default) against the greedy one
+    (0): the oracle's records bit for bit either way, on uneven meshes alone and in one batch, and
+    fewer wide nodes on a heightfield, whose wide-tree SAH is no higher."""
+    import torch
+    from luisacompute_gb300.accel import Accel, mesh_from_data
+    rng = np.random.default_rng(31)
+    meshes = [_strip(n, rng) for n in (2, 17, 700, 3000)] + [S.heightfield(64, seed=4), S.icosphere(3)]
+    scene = _scene(meshes, rng)
+    rays = _aimed(scene, 80_000, seed=32)
+    osc = oracle_mod.OracleScene(scene)
+    want, want_occ = osc.trace_closest(rays), osc.trace_any(rays)
+    for mode in (1, 0):
+        with _Knob("collapse", mode):
+            got, occ, _, _ = _trace(scene, rays, batch)
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), f"collapse {mode}"
+        assert np.array_equal(occ, want_occ), f"collapse {mode}"
+    md = S.heightfield(192, seed=5)
+    stats = {}
+    for mode in (1, 0):
+        with _Knob("collapse", mode):
+            m = mesh_from_data(md).build()
+        torch.cuda.synchronize()
+        st = m.stats()
+        assert int(st.leaf_prim_count) == md.triangles.shape[0]
+        stats[mode] = (int(st.node_count), st.wide_sah_cost)
+    assert stats[1][0] < 0.9 * stats[0][0], stats
+    assert stats[1][1] <= stats[0][1] * 1.01, stats
