@@ -781,14 +781,82 @@ __device__ __forceinline__ bool delta_less(const unsigned long long *k, uint32_t
     return (a ^ (a + 1)) < (b ^ (b + 1));
 }
 
+// ---- collapse by dynamic program (Ylitie, Karras & Laine 2017, "Efficient Incoherent Ray
+// Traversal on GPUs Through Compressed Wide BVHs"): bottom-up over the binary tree, the cost of
+// each subtree given i = 1..width slots of its wide parent -- a leaf slot (at most leaf_max items,
+// cost dp_prim x area x items), a wide node of its own (cost area + the best split of `width` slots
+// between its children), or for i > 1 the best split of i slots between its children -- and the
+// decisions that reach it, which the collapse then follows instead of opening the largest child.
+// Costs are in units of the root-independent box area; a node test costs 1.  The LBVH's own
+// bottom-up walk runs it for 8-wide nodes (k_lbvh<8>); other trees and widths take a pass of
+// their own (k_dp_parents, k_dp_up).
+
+// The costs out[0..W) of a node of box area a over cnt items for 1..W slots, from its children's
+// (cl, cr), and its decision word: bits 0..2 the split of W slots when the node is a wide node;
+// bits 3(i-1)..3(i-1)+2 for i = 2..W: 0 = take i - 1 slots, else k = the left child's share of
+// i slots.  W is a template argument so that every cost stays in registers; out may alias cl or cr.
+template <int W>
+__device__ __forceinline__ uint32_t dp_up_node(const float *cl, const float *cr, float a, uint32_t cnt, int leaf_max,
+                                               float cp, float *out) {
+    float dist[W + 1];
+    uint32_t dk[W + 1];
+#pragma unroll
+    for (int j = 2; j <= W; j++) {
+        dist[j] = FLT_MAX;
+        dk[j] = 0u;
+#pragma unroll
+        for (int k = 1; k < j; k++) {
+            const float v = cl[k - 1] + cr[j - k - 1];
+            if (v < dist[j]) {
+                dist[j] = v;
+                dk[j] = uint32_t(k);
+            }
+        }
+    }
+    uint32_t word = 0u;
+    float prev;
+    if (cnt <= uint32_t(leaf_max)) {
+        prev = cp * a * float(cnt);
+    } else {
+        prev = a + dist[W];
+        word = dk[W];
+    }
+    out[0] = prev;
+#pragma unroll
+    for (int i = 2; i <= W; i++) {
+        if (dist[i] < prev) {
+            prev = dist[i];
+            word |= dk[i] << (3 * (i - 1));
+        }
+        out[i - 1] = prev;
+    }
+    return word;
+}
+
+// A node's 8 cost words (slots beyond W repeat the W-slot cost).
+template <int W>
+__device__ __forceinline__ void dp_store_costs(float *dst, const float *c) {
+    float o[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) o[i] = c[i < W ? i : W - 1];
+    float4 *d4 = reinterpret_cast<float4 *>(dst);
+    d4[0] = make_float4(o[0], o[1], o[2], o[3]);
+    d4[1] = make_float4(o[4], o[5], o[6], o[7]);
+}
+
 // Binary node j (0 <= j < n-1) covers sorted items [first, first + count);
 // bin_lo.w / bin_hi.w hold count / first as bits.  A segment's keys differ
 // from its neighbours' in the segment bits, so its boundary deltas are larger
 // than every inner one and the merges stay inside it; the thread that
 // completes the node spanning the whole segment records it as the root.
+// W > 0: the same walk also runs the collapse's dynamic program for W-wide nodes (dp_up_node): the
+// completing thread holds its own subtree's costs in registers, reads the sibling's, writes the
+// node's costs and, over the node's arrival word (which nothing reads after the second arrival),
+// its decision word.
+template <int W>
 __global__ void k_lbvh(const SegInput *segs, uint32_t n, uint32_t seg_shift, const unsigned long long *keys,
                        const uint32_t *vals, const float4 *lo, const float4 *hi, uint32_t *bin_child, float4 *bin_lo,
-                       float4 *bin_hi, int32_t *other, uint32_t *segctl) {
+                       float4 *bin_hi, int32_t *other, uint32_t *segctl, int leaf_max, float cp, float *cost) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t s = seg_shift < 64 ? uint32_t(keys[i] >> seg_shift) : 0u;
@@ -802,14 +870,23 @@ __global__ void k_lbvh(const SegInput *segs, uint32_t n, uint32_t seg_shift, con
     }
     const uint32_t item = vals[i];
     float4 clo = lo[item], chi = hi[item];
+    float ccost[W > 0 ? W : 1];
+    if constexpr (W > 0) {
+        const float v = cp * box_area(clo, chi);
+#pragma unroll
+        for (int k = 0; k < W; k++) ccost[k] = v;
+    }
     for (uint32_t guard = 0; guard < n; guard++) {
         const bool left = (l == 0) || (r != n - 1 && delta_less(keys, r, l - 1));
         const uint32_t parent = left ? r : l - 1;
         bin_child[2 * parent + (left ? 0 : 1)] = cur;
-        __threadfence();
-        const int32_t prev = atomicExch(&other[parent], left ? int32_t(l) : int32_t(r));
+        // acquire-release: publishes this subtree's node (and costs), sees the sibling's
+        int32_t prev;
+        asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;"
+                     : "=r"(prev)
+                     : "l"(other + parent), "r"(left ? int32_t(l) : int32_t(r))
+                     : "memory");
         if (prev < 0) return;  // the sibling finishes the parent
-        __threadfence();
         if (left)
             r = uint32_t(prev);
         else
@@ -828,6 +905,21 @@ __global__ void k_lbvh(const SegInput *segs, uint32_t n, uint32_t seg_shift, con
         chi = make_float4(fmaxf(chi.x, shi.x), fmaxf(chi.y, shi.y), fmaxf(chi.z, shi.z), 0.0f);
         bin_lo[parent] = make_float4(clo.x, clo.y, clo.z, __uint_as_float(r - l + 1));
         bin_hi[parent] = make_float4(chi.x, chi.y, chi.z, __uint_as_float(l));
+        if constexpr (W > 0) {
+            float scost[W];
+            if (sib & kLeafBit) {
+                const float v = cp * box_area(slo, shi);
+#pragma unroll
+                for (int k = 0; k < W; k++) scost[k] = v;
+            } else {
+#pragma unroll
+                for (int k = 0; k < W; k++) scost[k] = __ldcg(cost + 8ull * sib + k);
+            }
+            const uint32_t word = left ? dp_up_node<W>(ccost, scost, box_area(clo, chi), r - l + 1, leaf_max, cp, ccost)
+                                       : dp_up_node<W>(scost, ccost, box_area(clo, chi), r - l + 1, leaf_max, cp, ccost);
+            dp_store_costs<W>(cost + 8ull * parent, ccost);
+            other[parent] = int32_t(word);
+        }
         cur = parent;
         if (l == seg_first && r == seg_last) {
             segctl[kSegWords * s + kSegRoot] = parent;
@@ -1075,14 +1167,6 @@ __device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t
     }
 }
 
-// ---- collapse by dynamic program (Ylitie, Karras & Laine 2017, "Efficient Incoherent Ray
-// Traversal on GPUs Through Compressed Wide BVHs"): bottom-up over the binary tree, the cost of
-// each subtree given i = 1..width slots of its wide parent -- a leaf slot (at most leaf_max items,
-// cost dp_prim x area x items), a wide node of its own (cost area + the best split of `width` slots
-// between its children), or for i > 1 the best split of i slots between its children -- and the
-// decisions that reach it, which the collapse then follows instead of opening the largest child.
-// Costs are in units of the root-independent box area; a node test costs 1.
-
 // Parent of every item and internal binary node (kInvalid: none, a segment root).
 __global__ void k_dp_parents(TreeView tv, const SegInput *segs, uint32_t nseg, uint32_t n, uint32_t *parent_item,
                              uint32_t *parent_node) {
@@ -1101,76 +1185,72 @@ __global__ void k_dp_parents(TreeView tv, const SegInput *segs, uint32_t nseg, u
     }
 }
 
-__device__ __forceinline__ void dp_child_costs(const TreeView &tv, uint32_t c, int width, float cp, const float *cost,
-                                               float out[8]) {
+// The costs of child c for 1..8 slots (a leaf item: one leaf slot, whatever the slots).
+template <int W>
+__device__ __forceinline__ void dp_child_costs(const TreeView &tv, uint32_t c, float cp, const float *cost,
+                                               float out[W]) {
     if (tv.leaf(c)) {
         float4 l, h;
         tv.box(c, l, h);
         const float v = cp * box_area(l, h);
-        for (int i = 0; i < 8; i++) out[i] = v;
+#pragma unroll
+        for (int i = 0; i < W; i++) out[i] = v;
     } else {
-        for (int i = 0; i < 8; i++) out[i] = i < width ? __ldcg(cost + 8ull * c + i) : FLT_MAX;
+#pragma unroll
+        for (int i = 0; i < W; i++) out[i] = __ldcg(cost + 8ull * c + i);
     }
 }
 
-// The costs and decisions of internal node nd from its children's.  dec word: bits 0..2 the split
-// of `width` slots when nd is a wide node; bits 3(i-1)..3(i-1)+2 for i = 2..width: 0 = take i - 1
-// slots, else k = the left child's share of i slots.
-__device__ void dp_node(const TreeView &tv, uint32_t nd, int width, int leaf_max, float cp, float *cost,
-                        uint32_t *dec) {
-    float cl[8], cr[8];
-    dp_child_costs(tv, tv.child[2ull * nd], width, cp, cost, cl);
-    dp_child_costs(tv, tv.child[2ull * nd + 1], width, cp, cost, cr);
-    float dist[9];
-    uint32_t dk[9];
-    for (int j = 0; j <= 8; j++) {
-        dist[j] = FLT_MAX;
-        dk[j] = 0u;
-    }
-    for (int j = 2; j <= width; j++)
-        for (int k = 1; k < j; k++) {
-            const float v = cl[k - 1] + cr[j - k - 1];
-            if (v < dist[j]) {
-                dist[j] = v;
-                dk[j] = uint32_t(k);
-            }
-        }
+// The costs and decisions of internal node nd from its children's (dp_up_node).
+template <int W>
+__device__ __forceinline__ void dp_node(const TreeView &tv, uint32_t nd, int leaf_max, float cp, float *cost,
+                                        uint32_t *dec) {
+    float cl[W], cr[W], out[W];
+    dp_child_costs<W>(tv, tv.child[2ull * nd], cp, cost, cl);
+    dp_child_costs<W>(tv, tv.child[2ull * nd + 1], cp, cost, cr);
     float4 l, h;
     tv.box(nd, l, h);
-    const float a = box_area(l, h);
-    const uint32_t cnt = tv.count(nd);
-    uint32_t word = 0u;
-    float prev;
-    if (cnt <= uint32_t(leaf_max)) {
-        prev = cp * a * float(cnt);
-    } else {
-        prev = a + dist[width];
-        word = dk[width];
-    }
-    cost[8ull * nd] = prev;
-    for (int i = 2; i <= width; i++) {
-        if (dist[i] < prev) {
-            prev = dist[i];
-            word |= dk[i] << (3 * (i - 1));
-        }
-        cost[8ull * nd + i - 1] = prev;
-    }
-    for (int i = width + 1; i <= 8; i++) cost[8ull * nd + i - 1] = prev;
-    dec[nd] = word;
+    dec[nd] = dp_up_node<W>(cl, cr, box_area(l, h), tv.count(nd), leaf_max, cp, out);
+    dp_store_costs<W>(cost + 8ull * nd, out);
 }
 
-// One thread per item walks up; the second arrival at a node computes it (its other subtree is done).
-__global__ void k_dp_up(TreeView tv, uint32_t n, int width, int leaf_max, float cp, const uint32_t *parent_item,
-                        const uint32_t *parent_node, uint32_t *arrivals, float *cost, uint32_t *dec) {
+// One thread per item walks up; the second arrival at a node computes it (its other subtree is
+// done).  The arrival is an acquire-release atomic: it publishes the costs this thread wrote and
+// makes the sibling's visible.
+template <int W>
+__global__ void __launch_bounds__(256) k_dp_up(TreeView tv, uint32_t n, int leaf_max, float cp,
+                                               const uint32_t *parent_item, const uint32_t *parent_node,
+                                               uint32_t *arrivals, float *cost, uint32_t *dec) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     uint32_t nd = parent_item[p];
     for (uint32_t guard = 0; guard < n && nd < n; guard++) {
-        __threadfence();
-        if (atomicAdd(&arrivals[nd], 1u) == 0u) return;
-        __threadfence();
-        dp_node(tv, nd, width, leaf_max, cp, cost, dec);
+        uint32_t old;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(arrivals + nd) : "memory");
+        if (old == 0u) return;
+        dp_node<W>(tv, nd, leaf_max, cp, cost, dec);
         nd = parent_node[nd];
+    }
+}
+
+template <int W>
+void launch_dp_up(const TreeView &tv, uint32_t n, int leaf_max, float cp, const uint32_t *parent_item,
+                  const uint32_t *parent_node, uint32_t *arrivals, float *cost, uint32_t *dec, cudaStream_t st) {
+    k_dp_up<W><<<blocks_for(n, 256), 256, 0, st>>>(tv, n, leaf_max, cp, parent_item, parent_node, arrivals, cost,
+                                                   dec);
+}
+
+void launch_dp_up_width(int width, const TreeView &tv, uint32_t n, int leaf_max, float cp,
+                        const uint32_t *parent_item, const uint32_t *parent_node, uint32_t *arrivals, float *cost,
+                        uint32_t *dec, cudaStream_t st) {
+    switch (width) {
+        case 2: launch_dp_up<2>(tv, n, leaf_max, cp, parent_item, parent_node, arrivals, cost, dec, st); break;
+        case 3: launch_dp_up<3>(tv, n, leaf_max, cp, parent_item, parent_node, arrivals, cost, dec, st); break;
+        case 4: launch_dp_up<4>(tv, n, leaf_max, cp, parent_item, parent_node, arrivals, cost, dec, st); break;
+        case 5: launch_dp_up<5>(tv, n, leaf_max, cp, parent_item, parent_node, arrivals, cost, dec, st); break;
+        case 6: launch_dp_up<6>(tv, n, leaf_max, cp, parent_item, parent_node, arrivals, cost, dec, st); break;
+        case 7: launch_dp_up<7>(tv, n, leaf_max, cp, parent_item, parent_node, arrivals, cost, dec, st); break;
+        default: launch_dp_up<8>(tv, n, leaf_max, cp, parent_item, parent_node, arrivals, cost, dec, st); break;
     }
 }
 
@@ -1608,7 +1688,7 @@ int collapse_grid() {
     return grid;
 }
 
-cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st);
+cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st, bool dp_done = false);
 
 cudaError_t build_common(BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
     NvtxRange nr("LBVH: Morton codes, sort, radix tree");
@@ -1624,14 +1704,22 @@ cudaError_t build_common(BuildScratch &s, const BuildParams &bp, cudaStream_t st
         if (e != cudaSuccess) return e;
     }
     const uint32_t shift = s.nseg > 1 ? 3 * s.axis_bits : 64;
+    // 8-wide collapse by dynamic program: in the same walk (decisions over the arrival words)
+    const bool dp8 = s.dp_cost != nullptr && bp.width == 8 && n > 1;
     note_build_launches(1);
-    k_lbvh<<<blocks_for(n, 256), 256, 0, st>>>(s.segs, n, shift, s.keys_sorted, s.vals_sorted, s.box_lo, s.box_hi,
-                                                 s.bin_child, s.bin_lo, s.bin_hi, s.other, s.segctl);
-    return build_rest(s, bp, st);
+    if (dp8)
+        k_lbvh<8><<<blocks_for(n, 256), 256, 0, st>>>(s.segs, n, shift, s.keys_sorted, s.vals_sorted, s.box_lo,
+                                                       s.box_hi, s.bin_child, s.bin_lo, s.bin_hi, s.other, s.segctl,
+                                                       bp.leaf_max, bp.dp_prim, s.dp_cost);
+    else
+        k_lbvh<0><<<blocks_for(n, 256), 256, 0, st>>>(s.segs, n, shift, s.keys_sorted, s.vals_sorted, s.box_lo,
+                                                       s.box_hi, s.bin_child, s.bin_lo, s.bin_hi, s.other, s.segctl,
+                                                       bp.leaf_max, bp.dp_prim, nullptr);
+    return build_rest(s, bp, st, dp8);
 }
 
 // After the binary tree: its SAH (and the BLAS bounding spheres), then the collapse.
-cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st) {
+cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st, bool dp_done) {
     NvtxRange nr("binary SAH, bounding spheres, collapse");
     const uint32_t n = s.n;
     const uint32_t shift = s.nseg > 1 ? 3 * s.axis_bits : 64;
@@ -1639,7 +1727,9 @@ cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st) 
     k_binary_sah<<<blocks_for(n, 256), 256, 0, st>>>(n, shift, s.keys_sorted, s.vals_sorted, s.bin_lo, s.bin_hi,
                                                        s.box_lo, s.box_hi, s.segs, s.segctl, s.bin_sah);
     TreeView tv = make_view(s);
-    if (s.dp_cost != nullptr && n > 1) {
+    if (dp_done) {
+        tv.dp_dec = reinterpret_cast<const uint32_t *>(s.other);
+    } else if (s.dp_cost != nullptr && n > 1) {
         // scratch the tree no longer needs: the Morton keys hold the parents, the unsorted ids the
         // arrival counters, the LBVH's sibling words the decisions
         uint32_t *parent_item = reinterpret_cast<uint32_t *>(s.keys), *parent_node = parent_item + n;
@@ -1649,8 +1739,8 @@ cudaError_t build_rest(BuildScratch &s, const BuildParams &bp, cudaStream_t st) 
         if (e != cudaSuccess) return e;
         note_build_launches(2);
         k_dp_parents<<<blocks_for(n, 256), 256, 0, st>>>(tv, s.segs, s.nseg, n, parent_item, parent_node);
-        k_dp_up<<<blocks_for(n, 256), 256, 0, st>>>(tv, n, bp.width, bp.leaf_max, bp.dp_prim, parent_item,
-                                                     parent_node, arrivals, s.dp_cost, dec);
+        launch_dp_up_width(bp.width, tv, n, bp.leaf_max, bp.dp_prim, parent_item, parent_node, arrivals, s.dp_cost,
+                           dec, st);
         tv.dp_dec = dec;
     }
     note_build_launches(1);
@@ -1977,10 +2067,11 @@ __global__ void k_refit(RefitArgs A) {
         pf.hi_x[pslot] = nh[0];
         pf.hi_y[pslot] = nh[1];
         pf.hi_z[pslot] = nh[2];
-        __threadfence();
         const uint32_t need = __popc(__ldg(&A.qn[parent].exps) >> 24);
-        if (atomicAdd(&A.counters[parent], 1u) + 1u != need) return;
-        __threadfence();
+        // acquire-release: publishes this slot's box, sees the other slots' when last
+        uint32_t arrived;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(arrived) : "l"(A.counters + parent) : "memory");
+        if (arrived + 1u != need) return;
         w = parent;
     }
     atomicOr(&A.ctl[kCtlErr], kErrTooDeep);
