@@ -958,6 +958,24 @@ struct TreeView {
     }
 };
 
+// Arrays of up to 8 entries kept in registers: every access is an unrolled loop over the 8
+// positions, so a run-time index never sends the array to local memory (whose traffic, for the
+// whole grid's threads, leaves L1).
+template <typename T>
+__device__ __forceinline__ T get8(const T (&a)[8], int i) {
+    T v = a[0];
+#pragma unroll
+    for (int j = 1; j < 8; j++)
+        if (i == j) v = a[j];
+    return v;
+}
+template <typename T>
+__device__ __forceinline__ void set8(T (&a)[8], int i, T v) {
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        if (i == j) a[j] = v;
+}
+
 // Open up to `width` children of binary node b, assign them to octant slots
 // and allocate their wide-node / item ranges.  desc: 12 words per wide node
 // (binary node, child base, item base, segment, 8 slot children).
@@ -969,6 +987,11 @@ __device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t
                               uint32_t *segctl, int level) {
     uint32_t C[8];
     float A[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        C[k] = kInvalid;
+        A[k] = 0.0f;
+    }
     int nC;
     if (tv.leaf(b)) {
         C[0] = b;
@@ -983,19 +1006,21 @@ __device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t
         // the dynamic program's choice: `width` slots split kw | width - kw between b's children, each
         // side expanded by its own decisions (a subtree given i slots either takes i - 1, or splits
         // i = k + (i - k) between its children)
-        nC = 0;
         uint32_t sn[8], si[8];
-        int sp = 0;
-        sn[sp] = C[1];
-        si[sp++] = uint32_t(width) - kw;
-        sn[sp] = C[0];
-        si[sp++] = kw;
+        const uint32_t c0 = C[0], c1 = C[1];
+        nC = 0;
+        int sp = 2;
+        sn[0] = c1;
+        si[0] = uint32_t(width) - kw;
+        sn[1] = c0;
+        si[1] = kw;
         while (sp > 0 && nC < 8) {
             --sp;
-            uint32_t nd = sn[sp], i = si[sp];
+            uint32_t nd = get8(sn, sp), i = get8(si, sp);
             for (int guard = 0; guard < 16; guard++) {
                 if (tv.leaf(nd) || i <= 1u) {
-                    C[nC++] = nd;
+                    set8(C, nC, nd);
+                    nC++;
                     break;
                 }
                 const uint32_t d = (tv.dp_dec[nd] >> (3u * (i - 1u))) & 7u;
@@ -1004,117 +1029,119 @@ __device__ void collapse_node(const TreeView &tv, const SegInput *segs, uint32_t
                     continue;
                 }
                 if (sp < 8) {
-                    sn[sp] = tv.child[2 * nd + 1];
-                    si[sp++] = i - d;
+                    set8(sn, sp, tv.child[2 * nd + 1]);
+                    set8(si, sp, i - d);
+                    sp++;
                 }
                 nd = tv.child[2 * nd];
                 i = d;
             }
         }
-    }
-    for (int k = 0; k < nC; k++) {
-        float4 l, h;
-        tv.box(C[k], l, h);
-        A[k] = box_area(l, h);
-    }
-    while (kw == 0u && nC < width) {
-        int best = -1;
-        float best_a = -1.0f;
-        for (int k = 0; k < nC; k++) {
-            if (!tv.leaf(C[k]) && tv.count(C[k]) > uint32_t(leaf_max) && A[k] > best_a) {
-                best_a = A[k];
-                best = k;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            if (k < nC) {
+                float4 l, h;
+                tv.box(C[k], l, h);
+                A[k] = box_area(l, h);
             }
         }
-        if (best < 0) break;
-        const uint32_t x = C[best];
-        C[best] = tv.child[2 * x];
-        C[nC] = tv.child[2 * x + 1];
-        float4 l, h;
-        tv.box(C[best], l, h);
-        A[best] = box_area(l, h);
-        tv.box(C[nC], l, h);
-        A[nC] = box_area(l, h);
-        nC++;
     }
-    while (kw == 0u && fill && nC < width) {  // every child is a leaf slot now: split the largest splittable one
-        int best = -1;
-        float best_a = -1.0f;
-        for (int k = 0; k < nC; k++) {
-            if (!tv.leaf(C[k]) && A[k] > best_a) {
-                best_a = A[k];
-                best = k;
+    // greedy (kw == 0): open the largest child that can become a wide node; with `fill`, then the
+    // largest splittable leaf slot
+    for (int pass = 0; pass < 2 && kw == 0u; pass++) {
+        if (pass == 1 && !fill) break;
+        while (nC < width) {
+            int best = -1;
+            float best_a = -1.0f;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                if (k < nC && !tv.leaf(C[k]) && (pass == 1 || tv.count(C[k]) > uint32_t(leaf_max)) && A[k] > best_a) {
+                    best_a = A[k];
+                    best = k;
+                }
             }
+            if (best < 0) break;
+            const uint32_t x = get8(C, best);
+            const uint32_t xl = tv.child[2 * x], xr = tv.child[2 * x + 1];
+            set8(C, best, xl);
+            set8(C, nC, xr);
+            float4 l, h;
+            tv.box(xl, l, h);
+            set8(A, best, box_area(l, h));
+            tv.box(xr, l, h);
+            set8(A, nC, box_area(l, h));
+            nC++;
         }
-        if (best < 0) break;
-        const uint32_t x = C[best];
-        C[best] = tv.child[2 * x];
-        C[nC] = tv.child[2 * x + 1];
-        float4 l, h;
-        tv.box(C[best], l, h);
-        A[best] = box_area(l, h);
-        tv.box(C[nC], l, h);
-        A[nC] = box_area(l, h);
-        nC++;
     }
     // octant slot assignment: greedy on dot(child centroid - node centroid, octant diagonal)
     float4 nl, nh;
     tv.box(b, nl, nh);
     const float pc[3] = {0.5f * (nl.x + nh.x), 0.5f * (nl.y + nh.y), 0.5f * (nl.z + nh.z)};
-    float off[8][3];
-    for (int k = 0; k < nC; k++) {
-        float4 l, h;
-        tv.box(C[k], l, h);
-        if (box_empty(l, h) || box_empty(nl, nh)) {
-            off[k][0] = off[k][1] = off[k][2] = 0.0f;
-        } else {
-            off[k][0] = 0.5f * (l.x + h.x) - pc[0];
-            off[k][1] = 0.5f * (l.y + h.y) - pc[1];
-            off[k][2] = 0.5f * (l.z + h.z) - pc[2];
+    const bool node_empty = box_empty(nl, nh);
+    float ox[8], oy[8], oz[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        ox[k] = oy[k] = oz[k] = 0.0f;
+        if (k < nC) {
+            float4 l, h;
+            tv.box(C[k], l, h);
+            if (!(box_empty(l, h) || node_empty)) {
+                ox[k] = 0.5f * (l.x + h.x) - pc[0];
+                oy[k] = 0.5f * (l.y + h.y) - pc[1];
+                oz[k] = 0.5f * (l.z + h.z) - pc[2];
+            }
         }
     }
     uint32_t slot_child[8];
+#pragma unroll
     for (int s = 0; s < 8; s++) slot_child[s] = kInvalid;
     // Each child's best slot is the octant of its offset's signs (it maximises the dot product with
     // the octant diagonal).  When those octants are distinct, the greedy assignment below gives
-    // exactly them, so it is skipped: nearly every node, at a fraction of the greedy's cost.
-    uint32_t pref[8], pref_used = 0;
+    // exactly them, so it is skipped (nodes of a few children).
+    uint32_t pref_word = 0, pref_used = 0;  // child k's octant in bits 3k..3k+2
     bool distinct = LCX_OCTANT_FAST != 0;
-    for (int k = 0; k < nC; k++) {
-        pref[k] = (off[k][0] < 0.0f ? 1u : 0u) | (off[k][1] < 0.0f ? 2u : 0u) | (off[k][2] < 0.0f ? 4u : 0u);
-        // a zero or NaN component ties two slots: leave those nodes to the greedy
-        const bool clear = fabsf(off[k][0]) > 0.0f && fabsf(off[k][1]) > 0.0f && fabsf(off[k][2]) > 0.0f;
-        distinct = distinct && clear && !(pref_used >> pref[k] & 1u);
-        pref_used |= 1u << pref[k];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        if (k < nC) {
+            const uint32_t pref = (ox[k] < 0.0f ? 1u : 0u) | (oy[k] < 0.0f ? 2u : 0u) | (oz[k] < 0.0f ? 4u : 0u);
+            // a zero or NaN component ties two slots: leave those nodes to the greedy
+            const bool clear = fabsf(ox[k]) > 0.0f && fabsf(oy[k]) > 0.0f && fabsf(oz[k]) > 0.0f;
+            distinct = distinct && clear && !(pref_used >> pref & 1u);
+            pref_used |= 1u << pref;
+            pref_word |= pref << (3 * k);
+        }
     }
     if (distinct) {
-        for (int k = 0; k < nC; k++) slot_child[pref[k]] = C[k];
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if (k < nC) set8(slot_child, int((pref_word >> (3 * k)) & 7u), C[k]);
     } else {
-        float cost[8][8];  // dot(offset, octant diagonal) per child and slot
-        for (int k = 0; k < nC; k++)
-            for (int s = 0; s < 8; s++) {
-                const float sc = ((s & 1) ? -off[k][0] : off[k][0]) + ((s & 2) ? -off[k][1] : off[k][1]) +
-                                 ((s & 4) ? -off[k][2] : off[k][2]);
-                cost[k][s] = sc == sc ? sc : -FLT_MAX;  // NaN never blocks an assignment
-            }
+        // the largest dot(offset, octant diagonal) over the free (child, slot) pairs, first in
+        // child-major order on ties, nC times
         uint32_t used_slots = 0, used_children = 0;
         for (int it = 0; it < nC; it++) {
             float best = -INFINITY;
             int bk = -1, bs = -1;
-            for (int k = 0; k < nC; k++) {
-                if (used_children >> k & 1u) continue;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+#pragma unroll
                 for (int s = 0; s < 8; s++) {
-                    if (used_slots >> s & 1u) continue;
-                    if (bk < 0 || cost[k][s] > best) {
-                        best = cost[k][s];
-                        bk = k;
-                        bs = s;
+                    if (k < nC && !(used_children >> k & 1u) && !(used_slots >> s & 1u)) {
+                        const float sc = ((s & 1) ? -ox[k] : ox[k]) + ((s & 2) ? -oy[k] : oy[k]) +
+                                         ((s & 4) ? -oz[k] : oz[k]);
+                        const float cst = sc == sc ? sc : -FLT_MAX;  // NaN never blocks an assignment
+                        if (bk < 0 || cst > best) {
+                            best = cst;
+                            bk = k;
+                            bs = s;
+                        }
                     }
                 }
             }
             used_children |= 1u << bk;
             used_slots |= 1u << bs;
-            slot_child[bs] = C[bk];
+            set8(slot_child, bs, get8(C, bk));
         }
     }
     uint32_t n_int = 0, n_items = 0;
@@ -1267,7 +1294,14 @@ __global__ void k_collapse_init(const SegInput *segs, uint32_t nseg, uint32_t *s
     segctl[kSegWords * s + kSegNodes] = 1u;
 }
 
-__global__ void k_collapse(TreeView tv, const SegInput *segs, int leaf_max, int width, int fill, uint32_t *desc,
+#ifndef LCX_COLLAPSE_MINB
+// resident blocks per SM the collapse is compiled for (its arrays live in registers): 1024-mesh
+// sample 28.8 / 28.7 / 28.5 / 28.5 ms at 1 / 4 / 5 / 6, against 32.8 ms with the arrays in
+// local memory
+#define LCX_COLLAPSE_MINB 5
+#endif
+__global__ void __launch_bounds__(128, LCX_COLLAPSE_MINB)
+    k_collapse(TreeView tv, const SegInput *segs, int leaf_max, int width, int fill, uint32_t *desc,
                            uint2 *q0, uint2 *q1, uint32_t *ctl, uint32_t *segctl) {
     cg::grid_group grid = cg::this_grid();
     int level = 0;
