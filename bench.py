@@ -944,7 +944,7 @@ def main():
         acc.trace_closest(d_rays, out=d_hits, layout=args.layout)
         h_hits.copy_(d_hits, non_blocking=True)
 
-    def host_step():  # lcx_trace_closest_host: direct host access or chunked staged copies (auto)
+    def host_step():  # lcx_trace_closest_host: streamed, staged or direct host access (auto: streamed here)
         acc.trace_closest_host(h_rays, h_hits, layout=args.layout)
 
     from luisacompute_gb300 import _capi as C
@@ -971,6 +971,9 @@ def main():
         C.check(lib.lcx_set_host_access(C.HOST_DIRECT), "host access")
         direct_value = n * e2e_steps / (time_e2e(host_step) / 1e3) / 1e9
         C.check(lib.lcx_set_host_access(mode.value), "host access")
+    C.check(lib.lcx_set_host_access(C.HOST_STAGED), "host access")  # the staged path, for comparison
+    staged_value = n * e2e_steps / (time_e2e(host_step) / 1e3) / 1e9
+    C.check(lib.lcx_set_host_access(mode.value), "host access")
     e2e_ms = time_e2e(host_step)
     if world > 1:
         import torch.distributed as dist
@@ -994,9 +997,11 @@ def main():
                     "path": ("lcx_trace_closest_host via ctypes, pinned host rays and hits: the traversal kernel "
                              "reads the rays from and writes the hits to host memory over the coherent CPU-GPU "
                              "link (NVLink-C2C), no staging copies" if coherent.value and mode.value == C.HOST_DIRECT
-                             else "lcx_trace_closest_host via ctypes: pinned host rays and hits, 2^22-ray chunks "
-                                  "through device staging, copies in the timed region overlapped with the traversal"),
+                             else "lcx_trace_closest_host via ctypes: pinned host rays and hits, streamed (one "
+                                  "traversal launch takes each 2^17-ray copy chunk as it lands; finished chunks are "
+                                  "copied out while it runs), all copies in the timed region"),
                     "direct_host_access_value": direct_value,
+                    "staged_value": staged_value,
                     "serial_copies_value": n * e2e_steps / (e2e_serial_ms / 1e3) / 1e9},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_src,

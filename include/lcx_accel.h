@@ -530,12 +530,17 @@ LCX_API int lcx_trace_any_host(uint64_t accel, const LcxRay *h_rays, uint32_t ra
 LCX_API int lcx_set_host_chunk(uint32_t rays);
 /* Host-buffer trace path: LCX_HOST_AUTO (direct when the device has a
  * coherent host link, the buffers are pinned and the call has at most 2^18
- * rays, else staged), LCX_HOST_STAGED,
+ * rays, else streamed where the call allows it, else staged), LCX_HOST_STAGED
+ * (chunks through a ring of device slots, one traversal launch per chunk),
  * LCX_HOST_DIRECT (direct whenever the buffers are pinned: on a device without
- * a coherent link the kernel's host accesses cross PCIe one by one).
+ * a coherent link the kernel's host accesses cross PCIe one by one),
+ * LCX_HOST_STREAMED (one traversal launch over the whole call that takes each
+ * copy chunk of rays as it arrives, while finished chunks are copied out; for
+ * pinned buffers, accels without motion or curves, quantised nodes and loop
+ * mode 2, else staged; one such call at a time per device, others staged).
  * lcx_get_host_access reports the mode and whether the current device has the
  * coherent link.  Tuning knobs with no reference counterpart. */
-enum { LCX_HOST_AUTO = 0, LCX_HOST_STAGED = 1, LCX_HOST_DIRECT = 2 };
+enum { LCX_HOST_AUTO = 0, LCX_HOST_STAGED = 1, LCX_HOST_DIRECT = 2, LCX_HOST_STREAMED = 3 };
 LCX_API int lcx_set_host_access(uint32_t mode);
 LCX_API int lcx_get_host_access(uint32_t *mode, uint32_t *coherent_link);
 

@@ -26,7 +26,7 @@ ERROR_NAMES = {0: "LCX_OK", -1: "LCX_ERR_INVALID_ARG", -2: "LCX_ERR_OOM", -3: "L
 HINT_FAST_TRACE, HINT_FAST_BUILD = 0, 1
 REQUEST_PREFER_UPDATE, REQUEST_FORCE_BUILD = 0, 1
 NODES_FP32, NODES_QUANT8 = 0, 1
-HOST_AUTO, HOST_STAGED, HOST_DIRECT = 0, 1, 2
+HOST_AUTO, HOST_STAGED, HOST_DIRECT, HOST_STREAMED = 0, 1, 2, 3
 MOD_PRIMITIVE, MOD_TRANSFORM, MOD_OPAQUE_ON, MOD_OPAQUE_OFF, MOD_VISIBILITY, MOD_USER_ID = 1, 2, 4, 8, 16, 32
 
 

@@ -6,6 +6,7 @@
 // CPU: src/rust/luisa_compute_backend_impl/src/cpu/stream.rs:410-428), with
 // status codes in place of the reference's aborts.
 #include <algorithm>
+#include <chrono>
 #include <cstddef>
 #include <cmath>
 #include <unordered_set>
@@ -17,8 +18,11 @@
 #include <mutex>
 #include <shared_mutex>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
+
+#include <cuda.h>  // the types of cuStreamWriteValue32 (taken through the runtime's entry-point query)
 
 #include "lcx_internal.h"
 
@@ -64,6 +68,14 @@ struct DeviceState {
     std::atomic<uint32_t> next_graph_slot{0};
     // host-buffer traces: copy-in, copy-out and two traversal streams
     cudaStream_t io_in = nullptr, io_out = nullptr, io_trace[2] = {nullptr, nullptr};
+    // streamed host-buffer traces (one at a time per device): the copy chunks' flags (device
+    // memory, one more word for the support probe), the warps' marks (mapped pinned memory),
+    // the generation of the last call, and whether the stream memory write is available
+    std::mutex stage_mtx;
+    uint32_t *stage_flags = nullptr;
+    uint32_t *stage_marks = nullptr, *stage_marks_dev = nullptr;
+    uint32_t stage_gen = 0;
+    int stage_state = 0;  // 0: not set up yet, 1: ready, 2: unavailable
 };
 
 std::mutex g_dev_mtx;
@@ -1774,9 +1786,16 @@ static uint32_t trace_slot(DeviceState *ds, cudaStream_t st) {
     return ds->next_slot.fetch_add(1) % (kPoolSlots - kGraphSlots);
 }
 
+// A streamed host-buffer launch's copy-chunk flags and warp marks (TraceParams::stage_*).
+struct StageArgs {
+    const uint32_t *flags = nullptr;
+    uint32_t *marks = nullptr;
+    uint32_t gen = 0, shift = 0;
+};
+
 static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *d_hits,
                         uint8_t *d_occ, uint32_t *d_counts, uint32_t layout, void *stream,
-                        const float *d_times = nullptr) {
+                        const float *d_times = nullptr, const StageArgs *stage = nullptr) {
     if (layout > LCX_NODES_QUANT8) return fail(LCX_ERR_INVALID_ARG, "invalid node layout %u", layout);
     std::shared_lock<std::shared_mutex> life(g_life_mtx);  // until the kernel is enqueued
     auto a = find_accel(accel);
@@ -1831,8 +1850,16 @@ static int trace_common(uint64_t accel, const LcxRay *d_rays, uint32_t ray_count
     // regular pushes need at most tlas_depth + blas_depth + 3 entries; postponed
     // triangle groups may use what is left
     p.postpone_sp = kStackSize - int(depth_need);
+    if (stage != nullptr) {
+        if (p.motion || layout != LCX_NODES_QUANT8 || p.mode != 2 || d_counts != nullptr)
+            return fail(LCX_ERR_INVALID_ARG, "a streamed trace needs a static accel, quantised nodes and loop mode 2");
+        p.stage_flag = stage->flags;
+        p.stage_mark = stage->marks;
+        p.stage_gen = stage->gen;
+        p.stage_shift = stage->shift;
+    }
     ReorderScratch rs;
-    const uint32_t rbits = g_reorder.bits;
+    const uint32_t rbits = stage != nullptr ? 0u : g_reorder.bits;  // a streamed launch takes the rays in order
     if (rbits != 0 && ray_count >= g_reorder.min_rays) {
         if (int r = reorder_begin(p.rays, ray_count, p.tlas_f, rbits, st, &rs)) return r;
         p.order = rs.order;
@@ -1983,10 +2010,12 @@ int lcx_check_trace_errors(void) {
         return fail(LCX_ERR_INVALID_ARG,
                     "an asynchronous refit or reserved rebuild failed (bad index or unquantisable coordinates)");
     }
-    if (flags & 2u)
+    if (flags & kTraceErrSteps)
         return fail(LCX_ERR_TIMEOUT, "a ray exceeded the traversal step bound (lcx_set_trace_step_bound; the "
                                      "default bound is reached only on a corrupt BVH)");
-    if (flags & 1u) return fail(LCX_ERR_DEPTH, "a ray overflowed the traversal stack");
+    if (flags & kTraceErrStage)
+        return fail(LCX_ERR_TIMEOUT, "a streamed host-buffer trace gave up waiting for a copy of its rays");
+    if (flags & kTraceErrStack) return fail(LCX_ERR_DEPTH, "a ray overflowed the traversal stack");
     return LCX_OK;
 }
 
@@ -2119,6 +2148,195 @@ const void *pinned_device_address(const void *p, size_t bytes) {
 }
 constexpr uint32_t kHostRing = LCX_HOST_RING;
 
+// ---- streamed host-buffer traces: one traversal launch over all the rays of the call.  The rays
+// go to device memory in copy chunks of 2^shift rays on the copy-in stream, each followed by a
+// stream memory write of the call's generation to the chunk's flag; the kernel takes a window of
+// rays once its chunk's flag holds the generation (a bounded wait: LCX_ERR_TIMEOUT past it).
+// Each warp publishes, in mapped pinned memory, a ray id below which all the rays it took have
+// their results stored; this thread watches the minimum over the warps and starts each chunk's
+// copy out once it has passed the chunk.  Nothing on the device waits for anything the kernel
+// produces, and the copy-in stream has no kernel on it, so the traversal's wait for a chunk
+// ends as soon as the copy engine has moved it.  Against the chunked launches of the staged
+// path (a persistent launch per chunk, each with its own ramp and tail), the traversal runs
+// as one launch.
+using StreamWriteValueFn = CUresult(CUDAAPI *)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
+StreamWriteValueFn g_write_value = nullptr;
+constexpr uint32_t kStageMarkCap = 16384;  // warps of a streamed launch (persistent grid)
+
+// Sets up the device's streamed-trace state once (under ds->stage_mtx); false: not available.
+bool stage_setup(DeviceState *ds) {
+    if (ds->stage_state != 0) return ds->stage_state == 1;
+    ds->stage_state = 2;
+    if (g_write_value == nullptr) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || fn == nullptr) {
+            cudaGetLastError();
+            return false;
+        }
+        g_write_value = reinterpret_cast<StreamWriteValueFn>(fn);
+    }
+    if (cudaMalloc(&ds->stage_flags, sizeof(uint32_t) * (kStageMaxChunks + 1)) != cudaSuccess ||
+        cudaMemset(ds->stage_flags, 0, sizeof(uint32_t) * (kStageMaxChunks + 1)) != cudaSuccess ||
+        cudaHostAlloc(&ds->stage_marks, sizeof(uint32_t) * kStageMarkCap, cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer(reinterpret_cast<void **>(&ds->stage_marks_dev), ds->stage_marks, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    // the stream memory write, once on the spare flag word
+    if (g_write_value(reinterpret_cast<CUstream>(ds->io_in),
+                      reinterpret_cast<CUdeviceptr>(ds->stage_flags + kStageMaxChunks), 1u, 0) != CUDA_SUCCESS ||
+        cudaStreamSynchronize(ds->io_in) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    ds->stage_state = 1;
+    return true;
+}
+
+// Whether a host-buffer trace of this accel can run streamed (a static accel, quantised nodes,
+// loop mode 2, pinned buffers); the launch checks the accel again.
+bool stream_eligible(uint64_t accel, uint32_t layout, const void *h_rays, size_t ray_bytes, const void *h_out,
+                     size_t out_bytes) {
+    if (layout != LCX_NODES_QUANT8 || g_tune.mode != 2) return false;
+    {
+        auto a = find_accel(accel);
+        if (!a) return false;
+        std::lock_guard<std::mutex> lk(a->mtx);
+        if (!a->built || a->has_motion || a->has_curves) return false;
+    }
+    return pinned_device_address(h_rays, ray_bytes) != nullptr && pinned_device_address(h_out, out_bytes) != nullptr;
+}
+
+constexpr int kStreamFallback = -1000;  // not taken: the caller runs the staged path
+
+static int trace_host_streamed(DeviceState *ds, uint64_t accel, const LcxRay *h_rays, uint32_t ray_count,
+                               uint32_t mask, LcxTriangleHit *h_hits, uint8_t *h_occ, uint32_t layout,
+                               cudaStream_t st) {
+    std::unique_lock<std::mutex> lk(ds->stage_mtx, std::try_to_lock);
+    if (!lk.owns_lock() || !stage_setup(ds)) return kStreamFallback;
+    const uint32_t warps = stream_launch_warps(ray_count, h_occ != nullptr);
+    if (warps == 0 || warps > kStageMarkCap) return kStreamFallback;
+    uint32_t shift = 17;  // chunks of 2^17 rays (4 MiB), at most kStageMaxChunks of them
+    while (((uint64_t(ray_count) + (1ull << shift) - 1) >> shift) > kStageMaxChunks) shift++;
+    const uint32_t chunks = uint32_t((uint64_t(ray_count) + (1ull << shift) - 1) >> shift);
+    const size_t rec = h_hits ? sizeof(LcxTriangleHit) : 1;
+    const size_t in_bytes = (size_t(ray_count) * sizeof(LcxRay) + 255) & ~size_t(255);
+    cudaMemPool_t pool;
+    if (int r = scratch_pool(&pool)) return r;
+    void *mem = nullptr;
+    LCX_CUDA(cudaMallocFromPoolAsync(&mem, in_bytes + size_t(ray_count) * rec, pool, st), "streamed trace buffers");
+    char *d_in = static_cast<char *>(mem), *d_out = d_in + in_bytes;
+    if (++ds->stage_gen == 0) ds->stage_gen = 1;
+    const uint32_t gen = ds->stage_gen;
+    for (uint32_t w = 0; w < warps; w++) ds->stage_marks[w] = 0u;  // the last call's kernel has exited
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    cudaEvent_t ev0 = nullptr, ev_done = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&ev0, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ev0, st);
+    cudaStream_t ts = ds->io_trace[0];
+    for (cudaStream_t x : {ds->io_in, ds->io_out, ts})
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(x, ev0, 0);
+    auto chunk_rays = [&](uint32_t c) {
+        return std::min<uint64_t>(1ull << shift, uint64_t(ray_count) - (uint64_t(c) << shift));
+    };
+    auto copy_in = [&](uint32_t c) {
+        const uint64_t off = uint64_t(c) << shift;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_in + off * sizeof(LcxRay), h_rays + off, chunk_rays(c) * sizeof(LcxRay),
+                                cudaMemcpyHostToDevice, ds->io_in);
+        if (e == cudaSuccess &&
+            g_write_value(reinterpret_cast<CUstream>(ds->io_in), reinterpret_cast<CUdeviceptr>(ds->stage_flags + c),
+                          gen, 0) != CUDA_SUCCESS)
+            e = cudaErrorUnknown;
+    };
+    copy_in(0);
+    int status = LCX_OK;
+    bool launched = false;
+    if (e == cudaSuccess) {
+        StageArgs sa;
+        sa.flags = ds->stage_flags;
+        sa.marks = ds->stage_marks_dev;
+        sa.gen = gen;
+        sa.shift = shift;
+        status = trace_common(accel, reinterpret_cast<const LcxRay *>(d_in), ray_count, mask,
+                              h_hits ? reinterpret_cast<LcxTriangleHit *>(d_out) : nullptr,
+                              h_hits ? nullptr : reinterpret_cast<uint8_t *>(d_out), nullptr, layout, ts, nullptr,
+                              &sa);
+        launched = status == LCX_OK;
+        if (launched) e = cudaEventRecord(ev_done, ts);
+    }
+    // the other chunks' copies in; the kernel takes each chunk once its flag is written
+    for (uint32_t c = 1; c < chunks && launched; c++) copy_in(c);
+    if (launched && e == cudaSuccess) {
+        // copies out as the warps' marks pass the chunks (a kernel that ended has marked every
+        // warp done, its error aside)
+        uint32_t next = 0;
+        const auto t0 = std::chrono::steady_clock::now();
+        while (next < chunks && e == cudaSuccess) {
+            uint32_t m = 0xffffffffu;
+            for (uint32_t w = 0; w < warps; w++) {
+                const uint32_t v = reinterpret_cast<volatile const uint32_t *>(ds->stage_marks)[w];
+                m = std::min(m, v);
+            }
+            std::atomic_thread_fence(std::memory_order_acquire);
+            bool moved = false;
+            while (next < chunks && uint64_t(m) >= (uint64_t(next) << shift) + chunk_rays(next)) {
+                const uint64_t off = uint64_t(next) << shift;
+                char *dst = h_hits ? reinterpret_cast<char *>(h_hits) : reinterpret_cast<char *>(h_occ);
+                e = cudaMemcpyAsync(dst + off * rec, d_out + off * rec, chunk_rays(next) * rec, cudaMemcpyDeviceToHost,
+                                    ds->io_out);
+                next++;
+                moved = true;
+                if (e != cudaSuccess) break;
+            }
+            if (next >= chunks || moved) continue;
+            const cudaError_t q = cudaEventQuery(ev_done);
+            if (q != cudaSuccess && q != cudaErrorNotReady) {
+                e = q;  // a failed launch: its marks may never come
+                break;
+            }
+            if (q == cudaSuccess) {
+                // ended: re-read the marks once (the last stores are visible now)
+                bool all = true;
+                for (uint32_t w = 0; w < warps; w++)
+                    all = all && reinterpret_cast<volatile const uint32_t *>(ds->stage_marks)[w] == 0xffffffffu;
+                if (!all) {
+                    e = cudaErrorUnknown;
+                    break;
+                }
+                continue;
+            }
+            if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60)) {
+                e = cudaErrorLaunchTimeout;  // the kernel's own waits end long before this
+                break;
+            }
+            std::this_thread::yield();
+        }
+    }
+    // the kernel has exited before the next streamed call resets the marks
+    if (launched) cudaEventSynchronize(ev_done);
+    // `stream` waits for everything enqueued above; the buffers return to the pool in its order
+    const cudaError_t first = e;
+    for (cudaStream_t x : {ds->io_in, ds->io_out, ts}) {
+        cudaEvent_t tail = nullptr;
+        if (cudaEventCreateWithFlags(&tail, cudaEventDisableTiming) == cudaSuccess) {
+            cudaEventRecord(tail, x);
+            cudaStreamWaitEvent(st, tail, 0);
+            cudaEventDestroy(tail);
+        }
+    }
+    cudaFreeAsync(mem, st);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev_done) cudaEventDestroy(ev_done);
+    if (status != LCX_OK) return status;
+    if (first != cudaSuccess) return cuda_fail(first, "streamed host-buffer trace");
+    return LCX_OK;
+}
+
 static int trace_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count, uint32_t mask, LcxTriangleHit *h_hits,
                       uint8_t *h_occ, uint32_t layout, void *stream) {
     if (ray_count == 0 || !h_rays || (!h_hits && !h_occ))  // validation (and the empty call) as the device form
@@ -2150,7 +2368,16 @@ static int trace_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count, 
                                 h_hits ? nullptr : static_cast<uint8_t *>(const_cast<void *>(dout)), nullptr, layout,
                                 stream);
     }
-    // chunk sizes: a short ramp up (the first copy in is not overlapped), full
+    // streamed (explicitly, or automatically above the direct path's size) where the call allows it
+    if (access == LCX_HOST_STREAMED || access == LCX_HOST_AUTO) {
+        const size_t out_bytes = size_t(ray_count) * (h_hits ? sizeof(LcxTriangleHit) : 1);
+        if (stream_eligible(accel, layout, h_rays, size_t(ray_count) * sizeof(LcxRay),
+                            h_hits ? static_cast<const void *>(h_hits) : h_occ, out_bytes)) {
+            const int r = trace_host_streamed(ds, accel, h_rays, ray_count, mask, h_hits, h_occ, layout, st);
+            if (r != kStreamFallback) return r;
+        }
+    }
+    // staged: chunk sizes: a short ramp up (the first copy in is not overlapped), full
     // chunks, and a ramp down (nor is the last copy out)
     const uint32_t chunk = g_host_chunk;
     std::vector<uint64_t> offs, cnts;
@@ -2356,7 +2583,7 @@ int lcx_trace_any_host(uint64_t accel, const LcxRay *h_rays, uint32_t ray_count,
 }
 
 int lcx_set_host_access(uint32_t mode) {
-    if (mode > LCX_HOST_DIRECT) return fail(LCX_ERR_INVALID_ARG, "invalid host access mode %u", mode);
+    if (mode > LCX_HOST_STREAMED) return fail(LCX_ERR_INVALID_ARG, "invalid host access mode %u", mode);
     g_host_access = mode;
     return LCX_OK;
 }

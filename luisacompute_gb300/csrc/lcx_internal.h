@@ -218,6 +218,11 @@ struct __align__(16) DevJob {
 };
 static_assert(sizeof(DevJob) == 64, "DevJob size");
 
+constexpr uint32_t kStageMaxChunks = 64;  // copy chunks of one streamed host-buffer trace (at most)
+// trace error bits (TraceParams::pool[1]): stack overflow, step bound, a streamed launch's copy
+// chunk that did not arrive in time
+constexpr uint32_t kTraceErrStack = 1u, kTraceErrSteps = 2u, kTraceErrStage = 4u;
+
 struct TraceParams {
     const Node8Q *tlas_q;
     const Node8F *tlas_f;
@@ -241,8 +246,18 @@ struct TraceParams {
     bool curves;            // with `motion`: the accel has curves (the extended kernels with the curve test)
     const float *times;     // motion launches: per-ray times (null: time 0)
     uint32_t max_steps = kMaxRaySteps;  // per-ray step bound; a ray that exceeds it ends and flags LCX_ERR_TIMEOUT
+    // Streamed host-buffer launches (stage_flag non-null; single-job closest / any, quantised
+    // nodes, loop mode 2): the rays arrive by copy chunks while the kernel runs.  Chunk c holds
+    // rays [c << stage_shift, (c + 1) << stage_shift) and is in place once stage_flag[c] ==
+    // stage_gen; each warp publishes to stage_mark[its index] a ray id below which every ray it
+    // took has its result stored (0xffffffff once it has exited).
+    const uint32_t *stage_flag = nullptr;
+    uint32_t *stage_mark = nullptr;
+    uint32_t stage_gen = 0, stage_shift = 0;
 };
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st);
+// Warps of a streamed launch over ray_count rays (the stage_mark entries it writes).
+uint32_t stream_launch_warps(uint32_t ray_count, bool any);
 
 // Ray reordering (reorder.cu): sorts the rays of a call by (direction octant,
 // origin Morton cell of the TLAS root box, `bits` per axis) into a

@@ -726,17 +726,33 @@ struct DeferQueue {
     float ret_t[32], ret_u[32], ret_v[32];
     uint32_t ret_inst[32], ret_prim[32], ret_rid[32];
     void *ret_out[kMulti ? 32 : 1];  // multi-job launches: the retired ray's output buffer
+    uint32_t stage_ready;            // streamed launches: copy chunks [0, stage_ready) known in place
 };
+
+// Streamed launches: a copy chunk's flag, read with acquire semantics.
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+// Polls of a copy chunk's flag before a streamed launch gives up on it (flags
+// LCX_ERR_TIMEOUT): 2^22 polls with a 256 ns sleep each, a few seconds (a poll with its
+// sleep measured about 1.5 us on GB300).
+constexpr uint32_t kStageSpin = 1u << 22;
 
 // kCount: the counting build (single-job closest hit), for the algorithmic bytes of this loop's own
 // visits: nodes visited, triangles queued (each is tested once), instances entered.
 // kExt 1: accels with motion instances or vertex-motion meshes (each ray has a time; an instance
 // entry takes the instance's matrix at that time, and the flush interpolates a moving triangle at
 // its ray's time); accels with curves stay on loop mode 0.
-template <int kLayout, bool kAny, int kShort, bool kMulti, bool kCount = false, int kExt = 0>
+// kStream: a streamed host-buffer launch (TraceParams::stage_flag): a warp takes a window of rays
+// only once the window's copy chunk is in place, and publishes how far its results are stored.
+template <int kLayout, bool kAny, int kShort, bool kMulti, bool kCount = false, int kExt = 0, bool kStream = false>
 __global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT : LCX_DEFER_MIN_BLOCKS)
     k_trace_deferred(TraceParams P) {
     static_assert(kExt <= 1, "curves take loop mode 0");
+    static_assert(!kStream || (!kMulti && !kCount && kExt == 0 && LCX_RAY_CHUNK > 0),
+                  "streamed launches are single-job, ray-window launches");
     using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort, kExt, LCX_WT_AT_FLUSH != 0>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
     __shared__ DeferQueue<kMulti, kExt> queues[kTraceBlock / 32];
@@ -761,6 +777,42 @@ __global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT :
     uint32_t cur = 1;       // record of the current instance
     bool retired = false;   // the retire slot holds a ray waiting for queued results
     bool ret_occ = false;
+    if constexpr (kStream) {
+        if (lane == 0) Q.stage_ready = 0u;
+        __syncwarp();
+    }
+
+    // Streamed launches (warp-uniform calls).  stage_wait: the copy chunk of ray `first` is in
+    // place (chunks arrive in order; false once the wait ran out).  stage_publish: every ray this
+    // warp took below `m` has its result stored; the fence orders each lane's result stores before
+    // the mark, which the host reads to start the chunk's copy out.
+    auto stage_wait = [&](uint32_t first) -> bool {
+        const uint32_t c = first >> P.stage_shift;
+        if (c < Q.stage_ready) return true;
+        uint32_t ok = 1u;
+        if (lane == 0) {
+            for (uint32_t it = 0; ld_acquire_gpu(P.stage_flag + c) != P.stage_gen; it++) {
+                if (it >= kStageSpin) {
+                    ok = 0u;
+                    atomicOr(P.pool + 1, kTraceErrStage);
+                    break;
+                }
+                __nanosleep(256);
+            }
+            if (ok) Q.stage_ready = c + 1u;
+        }
+        ok = __shfl_sync(~0u, ok, 0);
+        __syncwarp();
+        return ok != 0u;
+    };
+    auto stage_publish = [&](uint32_t m) {
+        __threadfence_system();
+        __syncwarp();
+        if (lane == 0) {
+            uint32_t *dst = P.stage_mark + (blockIdx.x * (kTraceBlock / 32) + (threadIdx.x >> 5));
+            asm volatile("st.relaxed.sys.global.u32 [%0], %1;" ::"l"(dst), "r"(m) : "memory");
+        }
+    };
 
     // Test every queued entry (all lanes call it together), merge the results
     // into their rays and write out the retired rays.
@@ -893,6 +945,18 @@ __global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT :
                 chunk_next = base;
                 chunk_end = uint32_t(min(uint64_t(base) + LCX_RAY_CHUNK, uint64_t(P.ray_count)));
                 if (chunk_next > chunk_end) chunk_next = chunk_end;
+                if constexpr (kStream) {
+                    // a window lies in one copy chunk (chunks are multiples of the window)
+                    if (chunk_next < chunk_end && !stage_wait(chunk_next)) {
+                        chunk_next = chunk_end;  // the rays did not arrive: take no more
+                        exhausted = true;
+                    }
+                    // in flight: the lanes' rays, the retired ones, the window's untaken ones
+                    uint32_t m = active ? rid : 0xffffffffu;
+                    if (retired) m = min(m, Q.ret_rid[lane]);
+                    m = min(__reduce_min_sync(~0u, m), chunk_next);
+                    stage_publish(m);
+                }
                 if (!kMulti && P.order == nullptr) {
                     for (uint32_t r = base + lane; r < chunk_end; r += 32u)
                         asm volatile("prefetch.global.L2 [%0];" ::"l"(P.rays + r));
@@ -1089,6 +1153,7 @@ __global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT :
         // 5. test the queue once it is full enough, or a finished ray is waiting on it
         if (qn >= flush_at || __any_sync(~0u, blocked)) flush();
     }
+    if constexpr (kStream) stage_publish(0xffffffffu);
 }
 
 // ---------------------------------------------------------------------------
@@ -1185,20 +1250,25 @@ cudaError_t launch_stack(const TraceParams &p, cudaStream_t st) {
     return launch_one<L, A, false, 0, false, kDefaultShortStack>(p, st);
 }
 
-template <int L, bool A, int S, bool X = false, bool C = false, int E = 0>
-cudaError_t launch_deferred(const TraceParams &p, cudaStream_t st) {
+template <int L, bool A, int S, bool X = false, bool C = false, int E = 0, bool St = false>
+uint64_t deferred_grid(uint32_t ray_count) {
     static int per_sm = 0;
     if (per_sm == 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_deferred<L, A, S, X, C, E>, kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_deferred<L, A, S, X, C, E, St>, kTraceBlock, 0);
         per_sm = b > 0 ? b : 1;
     }
-    const uint64_t warps_needed = (uint64_t(p.ray_count) + 31) / 32;
+    const uint64_t warps_needed = (uint64_t(ray_count) + 31) / 32;
     uint64_t grid = uint64_t(sm_count()) * uint64_t(per_sm);
     const uint64_t grid_need = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
     if (grid_need < grid) grid = grid_need;
-    if (grid == 0) grid = 1;
-    k_trace_deferred<L, A, S, X, C, E><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
+    return grid == 0 ? 1 : grid;
+}
+
+template <int L, bool A, int S, bool X = false, bool C = false, int E = 0, bool St = false>
+cudaError_t launch_deferred(const TraceParams &p, cudaStream_t st) {
+    const uint64_t grid = deferred_grid<L, A, S, X, C, E, St>(p.ray_count);
+    k_trace_deferred<L, A, S, X, C, E, St><<<unsigned(grid), kTraceBlock, 0, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -1238,7 +1308,19 @@ cudaError_t launch_ext(const TraceParams &p, int layout, bool any, bool counting
 
 }  // namespace
 
+uint32_t stream_launch_warps(uint32_t ray_count, bool any) {
+    const uint64_t grid = any ? deferred_grid<LCX_NODES_QUANT8, true, LCX_DEFER_STACK, false, false, 0, true>(ray_count)
+                              : deferred_grid<LCX_NODES_QUANT8, false, LCX_DEFER_STACK, false, false, 0, true>(ray_count);
+    return uint32_t(grid * (kTraceBlock / 32));
+}
+
 cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counting, cudaStream_t st) {
+    if (p.stage_flag != nullptr) {  // streamed host-buffer launches (the host checked the form)
+        if (p.jobs != nullptr || p.motion || counting || p.order != nullptr || layout != LCX_NODES_QUANT8)
+            return cudaErrorInvalidValue;
+        return any ? launch_deferred<LCX_NODES_QUANT8, true, LCX_DEFER_STACK, false, false, 0, true>(p, st)
+                   : launch_deferred<LCX_NODES_QUANT8, false, LCX_DEFER_STACK, false, false, 0, true>(p, st);
+    }
     // loop mode 3 (one ray per thread through the device-side trace functions): single-job,
     // quantised-node, non-counting calls, static or moving; the others run mode 0
     if (p.mode == 3 && p.jobs == nullptr && !counting && layout == LCX_NODES_QUANT8)

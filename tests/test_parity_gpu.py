@@ -433,14 +433,14 @@ def test_ray_reorder_does_not_change_results(torch_cuda, lcx, oracle_mod, bits):
     no_kernel_errors()
 
 
-@pytest.mark.parametrize("chunk,access", [(1 << 14, 1), (1 << 20, 1), (1 << 20, 0), (1 << 20, 2)])
+@pytest.mark.parametrize("chunk,access", [(1 << 14, 1), (1 << 20, 1), (1 << 20, 0), (1 << 20, 2), (1 << 20, 3)])
 def test_host_buffer_traces(torch_cuda, lcx, oracle_mod, chunk, access):
     """lcx_trace_closest_host / lcx_trace_any_host (rays and results in host memory): the oracle's
     records bit for bit, for pinned and pageable buffers, both layouts, on a side stream, in every
     host access mode: staged (chunked through device staging with copies overlapped; a ray count
     that is not a multiple of the chunk, with 2^14 13 chunks through the 4-slot ring), direct (the
-    kernel reads and writes the pinned host buffers itself) and auto (staged above 2^18 rays, as
-    here); the empty call is a no-op."""
+    kernel reads and writes the pinned host buffers itself), auto (direct at this size) and streamed
+    (pinned quantised-node calls streamed, the others staged); the empty call is a no-op."""
     from luisacompute_gb300 import _capi
     lib = _capi.load()
     _capi.check(lib.lcx_set_host_access(access), "host access")
@@ -487,9 +487,42 @@ def test_host_buffer_traces(torch_cuda, lcx, oracle_mod, chunk, access):
         assert lib.lcx_trace_closest_host(acc.handle, rays.ctypes.data, 16, 0xFF, None, 1, None) \
             == _capi.LCX_ERR_INVALID_ARG
         assert lib.lcx_set_host_chunk(100) == _capi.LCX_ERR_INVALID_ARG
-        assert lib.lcx_set_host_access(3) == _capi.LCX_ERR_INVALID_ARG
+        assert lib.lcx_set_host_access(4) == _capi.LCX_ERR_INVALID_ARG
     finally:
         _capi.check(lib.lcx_set_host_chunk(1 << 22), "chunk")
+        _capi.check(lib.lcx_set_host_access(_capi.HOST_AUTO), "host access")
+    no_kernel_errors()
+
+
+@pytest.mark.parametrize("access", [3, 0])
+def test_host_streamed_traces(torch_cuda, lcx, oracle_mod, access):
+    """Streamed host-buffer traces (LCX_HOST_STREAMED, and auto above 2^18 rays): one traversal
+    launch over the call takes each 2^17-ray copy chunk as its flag arrives while finished chunks
+    are copied out; 700,001 rays are five full chunks and a partial one.  Closest and any hit, the
+    oracle's records bit for bit, back to back on one side stream and then on the current stream
+    (each call waits for the last one's kernel before it reuses the marks)."""
+    from luisacompute_gb300 import _capi
+    lib = _capi.load()
+    _capi.check(lib.lcx_set_host_access(access), "host access")
+    scene = small_terrain()
+    rays = np.concatenate([S.terrain_rays(scene, 600_000, seed=27), S.terrain_shadow_rays(scene, 100_001, seed=28)])
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_closest(rays)
+    want_any = osc.trace_any(rays)
+    acc, _ = gpu_scene(scene)
+    try:
+        h_rays = torch_cuda.from_numpy(rays.view(np.float32).reshape(-1, 8)).pin_memory()
+        for stream in (torch_cuda.cuda.Stream(), None):
+            h_hits = torch_cuda.full((rays.shape[0], 6), -7, dtype=torch_cuda.int32).pin_memory()
+            h_occ = torch_cuda.full((rays.shape[0],), 9, dtype=torch_cuda.uint8).pin_memory()
+            acc.trace_closest_host(h_rays, h_hits, stream=stream)
+            acc.trace_any_host(h_rays, h_occ, stream=stream)
+            acc.trace_closest_host(h_rays, h_hits, stream=stream)  # again over the same buffers
+            torch_cuda.cuda.synchronize()
+            got = h_hits.numpy().view(want.dtype).reshape(-1)
+            assert_bit_exact(oracle_mod, osc, rays, got, want)
+            assert np.array_equal(h_occ.numpy(), want_any)
+    finally:
         _capi.check(lib.lcx_set_host_access(_capi.HOST_AUTO), "host access")
     no_kernel_errors()
 
