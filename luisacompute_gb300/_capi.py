@@ -172,6 +172,7 @@ _SIGS = {
     "lcx_set_host_access": (c_int, [c_uint32]),
     "lcx_trace_jobs_motion": (c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p]),
     "lcx_get_host_access": (c_int, [POINTER(c_uint32), POINTER(c_uint32)]),
+    "lcx_release_scratch": (c_int, []),
     "lcx_set_host_chunk": (c_int, [c_uint32]),
     "lcx_accel_instance_buffer": (c_int, [c_uint64, POINTER(LcxInstanceBuffer)]),
     "lcx_set_build_split": (c_int, [ctypes.c_float]),

@@ -231,3 +231,20 @@ def test_dp_collapse(lcx, oracle_mod, batch):
         stats[mode] = (int(st.node_count), st.wide_sah_cost)
     assert stats[1][0] < 0.9 * stats[0][0], stats
     assert stats[1][1] <= stats[0][1] * 1.01, stats
+
+
+def test_release_scratch(lcx, oracle_mod):
+    """Builds take their scratch from a pool that keeps freed memory for the next build;
+    lcx_release_scratch hands it back to the driver.  Builds before and after it give the oracle's
+    records, and a build right after it maps its scratch again."""
+    from luisacompute_gb300 import _capi
+    lib = _capi.load()
+    rng = np.random.default_rng(31)
+    scene = _scene([_strip(3000, rng), _strip(1500, rng, jitter=0.01)], rng)
+    rays = _aimed(scene, 20_000, seed=32)
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_closest(rays)
+    for step in range(2):
+        got, _, _, _ = _trace(scene, rays, batch=True)
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+        assert lib.lcx_release_scratch() == _capi.LCX_OK
