@@ -72,6 +72,10 @@ struct DeviceState {
     // memory, one more word for the support probe), the warps' marks (mapped pinned memory),
     // the generation of the last call, and whether the stream memory write is available
     std::mutex stage_mtx;
+    // its own copy-in, copy-out and traversal streams: the traversal waits on what the copy-in
+    // stream carries, so no other call may queue work there (a staged call's waits would sit
+    // between the chunks' copies)
+    cudaStream_t stage_in = nullptr, stage_out = nullptr, stage_trace = nullptr;
     uint32_t *stage_flags = nullptr;
     uint32_t *stage_marks = nullptr, *stage_marks_dev = nullptr;
     uint32_t stage_gen = 0;
@@ -2202,7 +2206,10 @@ bool stage_setup(DeviceState *ds) {
         }
         g_write_value = reinterpret_cast<StreamWriteValueFn>(fn);
     }
-    if (cudaMalloc(&ds->stage_flags, sizeof(uint32_t) * (kStageMaxChunks + 1)) != cudaSuccess ||
+    if (cudaStreamCreateWithFlags(&ds->stage_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ds->stage_out, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ds->stage_trace, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&ds->stage_flags, sizeof(uint32_t) * (kStageMaxChunks + 1)) != cudaSuccess ||
         cudaMemset(ds->stage_flags, 0, sizeof(uint32_t) * (kStageMaxChunks + 1)) != cudaSuccess ||
         cudaHostAlloc(&ds->stage_marks, sizeof(uint32_t) * kStageMarkCap, cudaHostAllocMapped) != cudaSuccess ||
         cudaHostGetDevicePointer(reinterpret_cast<void **>(&ds->stage_marks_dev), ds->stage_marks, 0) != cudaSuccess) {
@@ -2210,9 +2217,9 @@ bool stage_setup(DeviceState *ds) {
         return false;
     }
     // the stream memory write, once on the spare flag word
-    if (g_write_value(reinterpret_cast<CUstream>(ds->io_in),
+    if (g_write_value(reinterpret_cast<CUstream>(ds->stage_in),
                       reinterpret_cast<CUdeviceptr>(ds->stage_flags + kStageMaxChunks), 1u, 0) != CUDA_SUCCESS ||
-        cudaStreamSynchronize(ds->io_in) != cudaSuccess) {
+        cudaStreamSynchronize(ds->stage_in) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
@@ -2261,8 +2268,8 @@ static int trace_host_streamed(DeviceState *ds, uint64_t accel, const LcxRay *h_
     cudaError_t e = cudaEventCreateWithFlags(&ev0, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventRecord(ev0, st);
-    cudaStream_t ts = ds->io_trace[0];
-    for (cudaStream_t x : {ds->io_in, ds->io_out, ts})
+    cudaStream_t ts = ds->stage_trace;
+    for (cudaStream_t x : {ds->stage_in, ds->stage_out, ts})
         if (e == cudaSuccess) e = cudaStreamWaitEvent(x, ev0, 0);
     auto chunk_rays = [&](uint32_t c) {
         return std::min<uint64_t>(1ull << shift, uint64_t(ray_count) - (uint64_t(c) << shift));
@@ -2271,9 +2278,9 @@ static int trace_host_streamed(DeviceState *ds, uint64_t accel, const LcxRay *h_
         const uint64_t off = uint64_t(c) << shift;
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(d_in + off * sizeof(LcxRay), h_rays + off, chunk_rays(c) * sizeof(LcxRay),
-                                cudaMemcpyHostToDevice, ds->io_in);
+                                cudaMemcpyHostToDevice, ds->stage_in);
         if (e == cudaSuccess &&
-            g_write_value(reinterpret_cast<CUstream>(ds->io_in), reinterpret_cast<CUdeviceptr>(ds->stage_flags + c),
+            g_write_value(reinterpret_cast<CUstream>(ds->stage_in), reinterpret_cast<CUdeviceptr>(ds->stage_flags + c),
                           gen, 0) != CUDA_SUCCESS)
             e = cudaErrorUnknown;
     };
@@ -2312,7 +2319,7 @@ static int trace_host_streamed(DeviceState *ds, uint64_t accel, const LcxRay *h_
                 const uint64_t off = uint64_t(next) << shift;
                 char *dst = h_hits ? reinterpret_cast<char *>(h_hits) : reinterpret_cast<char *>(h_occ);
                 e = cudaMemcpyAsync(dst + off * rec, d_out + off * rec, chunk_rays(next) * rec, cudaMemcpyDeviceToHost,
-                                    ds->io_out);
+                                    ds->stage_out);
                 next++;
                 moved = true;
                 if (e != cudaSuccess) break;
@@ -2345,7 +2352,7 @@ static int trace_host_streamed(DeviceState *ds, uint64_t accel, const LcxRay *h_
     if (launched) cudaEventSynchronize(ev_done);
     // `stream` waits for everything enqueued above; the buffers return to the pool in its order
     const cudaError_t first = e;
-    for (cudaStream_t x : {ds->io_in, ds->io_out, ts}) {
+    for (cudaStream_t x : {ds->stage_in, ds->stage_out, ts}) {
         cudaEvent_t tail = nullptr;
         if (cudaEventCreateWithFlags(&tail, cudaEventDisableTiming) == cudaSuccess) {
             cudaEventRecord(tail, x);

@@ -494,6 +494,46 @@ def test_host_buffer_traces(torch_cuda, lcx, oracle_mod, chunk, access):
     no_kernel_errors()
 
 
+def test_host_streamed_concurrent(torch_cuda, lcx, oracle_mod):
+    """Two host threads tracing host buffers at once on their own streams: one call holds the
+    device's streamed-trace state, the other takes the staged path meanwhile; both give the
+    oracle's records bit for bit."""
+    import threading
+    from luisacompute_gb300 import _capi
+    lib = _capi.load()
+    _capi.check(lib.lcx_set_host_access(3), "host access")
+    scene = small_terrain()
+    rays = S.terrain_rays(scene, 400_003, seed=37)
+    osc = oracle_mod.OracleScene(scene)
+    want = osc.trace_closest(rays)
+    acc, _ = gpu_scene(scene)
+    h_rays = torch_cuda.from_numpy(rays.view(np.float32).reshape(-1, 8)).pin_memory()
+    outs = [torch_cuda.full((rays.shape[0], 6), -7, dtype=torch_cuda.int32).pin_memory() for _ in range(2)]
+    errors = []
+
+    def worker(k):
+        try:
+            s = torch_cuda.cuda.Stream()
+            for _ in range(4):
+                acc.trace_closest_host(h_rays, outs[k], stream=s)
+            s.synchronize()
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    try:
+        ts = [threading.Thread(target=worker, args=(k,)) for k in range(2)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        assert not errors, errors
+        for k in range(2):
+            assert_bit_exact(oracle_mod, osc, rays, outs[k].numpy().view(want.dtype).reshape(-1), want)
+    finally:
+        _capi.check(lib.lcx_set_host_access(_capi.HOST_AUTO), "host access")
+    no_kernel_errors()
+
+
 @pytest.mark.parametrize("access", [3, 0])
 def test_host_streamed_traces(torch_cuda, lcx, oracle_mod, access):
     """Streamed host-buffer traces (LCX_HOST_STREAMED, and auto above 2^18 rays): one traversal
