@@ -694,7 +694,11 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
 #define LCX_TRI_PREFETCH 0
 #endif
 #ifndef LCX_DEFER_CAP
-#define LCX_DEFER_CAP 64
+// queued triangle tests per warp: a step in which many lanes reach leaves queues more than the
+// flush size at once, and a full queue flushes in mid-step.  Terrain workload, closest / any
+// Grays/s: 48: 2.639 / 4.38; 64: 2.658-2.664 / 4.37; 80: 2.696 / 4.39; 96: 2.691-2.695 / 4.47;
+// 112: 2.700 / 4.39; 128: 2.694 / 4.47 (same records)
+#define LCX_DEFER_CAP 96
 #endif
 #ifndef LCX_DEFER_MIN_BLOCKS
 #define LCX_DEFER_MIN_BLOCKS 7
@@ -714,10 +718,10 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
 #endif
 constexpr int kDeferCap = LCX_DEFER_CAP;  // queued triangle tests per warp
 
-template <bool kMulti, int kExt = 0>
+template <bool kMulti, int kExt = 0, int kCap = kDeferCap>
 struct DeferQueue {
-    const TriRec *tri[kDeferCap];
-    uint32_t rec[kDeferCap];       // ray record: lane | slot << 5
+    const TriRec *tri[kCap];
+    uint32_t rec[kCap];            // ray record: lane | slot << 5
     float rr[9][64];               // per record: ox oy oz Sx Sy Sz perm tmin inst (perm, inst as bits)
     float rtime[kExt ? 64 : 1];    // motion launches: per record, its ray's time
     unsigned long long key[64];    // per record: min (ordered t << 32 | prim)
@@ -755,16 +759,20 @@ __global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT :
                   "streamed launches are single-job, ray-window launches");
     using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort, kExt, LCX_WT_AT_FLUSH != 0>;
     __shared__ uint2 stack_mem[W_t::kShortStack * kTraceBlock];
-    __shared__ DeferQueue<kMulti, kExt> queues[kTraceBlock / 32];
+    // streamed launches keep the 64-entry queue: with 96 their host-buffer calls measured 2.20
+    // against 2.26 Grays/s (the copies beside the kernel seem to want the L1 that the larger
+    // queue's shared memory takes)
+    constexpr int kCap = kStream ? 64 : kDeferCap;
+    __shared__ DeferQueue<kMulti, kExt, kCap> queues[kTraceBlock / 32];
     uint2 deep_stack[W_t::kDeepSlots];
     const uint32_t lane = threadIdx.x & 31u;
-    DeferQueue<kMulti, kExt> &Q = queues[threadIdx.x >> 5];
+    DeferQueue<kMulti, kExt, kCap> &Q = queues[threadIdx.x >> 5];
     W_t W(P, stack_mem + threadIdx.x, deep_stack);
     const int refill = int(P.refill);
     // queue size that starts a flush: P.postpone, or 24 for closest / 16 for any hit (measured on the
     // terrain workload: closest 1.860 / 1.896 / 1.886 / 1.869 Grays/s at 32 / 24 / 16 / 12; any hit
     // 3.10 / 3.20 / 3.25 / 3.26)
-    const uint32_t flush_at = P.postpone >= 1 && P.postpone <= uint32_t(kDeferCap) ? P.postpone : (kAny ? 16u : 24u);
+    const uint32_t flush_at = P.postpone >= 1 && P.postpone <= uint32_t(kCap) ? P.postpone : (kAny ? 16u : 24u);
 
     bool active = false, exhausted = false;
     uint32_t rid = 0, ray_steps = 0;
@@ -1052,7 +1060,7 @@ __global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT :
                     total += uint32_t(__popc(m)) << b;
                 }
                 if (total == 0u) break;
-                const uint32_t space = uint32_t(kDeferCap) - qn;
+                const uint32_t space = uint32_t(kCap) - qn;
                 uint32_t pos = qn + excl;
 #else
                 uint32_t incl = cnt;
@@ -1063,10 +1071,10 @@ __global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT :
                 }
                 const uint32_t total = __shfl_sync(~0u, incl, 31);
                 if (total == 0u) break;
-                const uint32_t space = uint32_t(kDeferCap) - qn;
+                const uint32_t space = uint32_t(kCap) - qn;
                 uint32_t pos = qn + incl - cnt;
 #endif
-                while (bits != 0u && pos < uint32_t(kDeferCap)) {
+                while (bits != 0u && pos < uint32_t(kCap)) {
                     const uint32_t k = __ffs(bits) - 1u;
                     bits &= bits - 1u;
 #if LCX_TRI_PREFETCH
@@ -1085,7 +1093,7 @@ __global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT :
                     qn += total;
                     break;
                 }
-                qn = uint32_t(kDeferCap);
+                qn = uint32_t(kCap);
                 flush();
             }
         }
