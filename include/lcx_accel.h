@@ -537,7 +537,9 @@ LCX_API int lcx_set_host_chunk(uint32_t rays);
  * LCX_HOST_STREAMED (one traversal launch over the whole call that takes each
  * copy chunk of rays as it arrives, while finished chunks are copied out; for
  * pinned buffers, accels without motion or curves, quantised nodes and loop
- * mode 2, else staged; one such call at a time per device, others staged).
+ * mode 2, else staged; staged too while launches are serialised, under
+ * CUDA_LAUNCH_BLOCKING=1 or an Nsight tool; one such call at a time per
+ * device, others staged).
  * lcx_get_host_access reports the mode and whether the current device has the
  * coherent link.  Tuning knobs with no reference counterpart. */
 enum { LCX_HOST_AUTO = 0, LCX_HOST_STAGED = 1, LCX_HOST_DIRECT = 2, LCX_HOST_STREAMED = 3 };

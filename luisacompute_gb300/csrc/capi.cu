@@ -2227,11 +2227,26 @@ bool stage_setup(DeviceState *ds) {
     return true;
 }
 
+// Whether launches run one at a time to completion (CUDA_LAUNCH_BLOCKING, or an Nsight tool in
+// the process -- Nsight Compute sets NV_NSIGHT_INJECTION_* and NV_COMPUTE_PROFILER_PERFWORKS_DIR
+// in its target, other tools CUDA_INJECTION64_PATH -- which serialise them): a streamed launch
+// would then wait for copies that are enqueued only after its launch returns, until its bound
+// ran out.
+bool launches_serialized() {
+    const char *b = getenv("CUDA_LAUNCH_BLOCKING");
+    if (b != nullptr && b[0] == '1') return true;
+    for (const char *v : {"CUDA_INJECTION64_PATH", "NV_NSIGHT_INJECTION_TRANSPORT_TYPE", "NV_COMPUTE_PROFILER_PERFWORKS_DIR"}) {
+        const char *e = getenv(v);
+        if (e != nullptr && e[0] != 0) return true;
+    }
+    return false;
+}
+
 // Whether a host-buffer trace of this accel can run streamed (a static accel, quantised nodes,
-// loop mode 2, pinned buffers); the launch checks the accel again.
+// loop mode 2, pinned buffers, launches not serialised); the launch checks the accel again.
 bool stream_eligible(uint64_t accel, uint32_t layout, const void *h_rays, size_t ray_bytes, const void *h_out,
                      size_t out_bytes) {
-    if (layout != LCX_NODES_QUANT8 || g_tune.mode != 2) return false;
+    if (layout != LCX_NODES_QUANT8 || g_tune.mode != 2 || launches_serialized()) return false;
     {
         auto a = find_accel(accel);
         if (!a) return false;

@@ -740,9 +740,10 @@ __device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p) {
     return v;
 }
 // Polls of a copy chunk's flag before a streamed launch gives up on it (flags
-// LCX_ERR_TIMEOUT): 2^22 polls with a 256 ns sleep each, a few seconds (a poll with its
-// sleep measured about 1.5 us on GB300).
-constexpr uint32_t kStageSpin = 1u << 22;
+// LCX_ERR_TIMEOUT): 2^20 polls with a 256 ns sleep each, one to a few seconds (a poll with
+// its sleep measured about 1.5 us on GB300), where a chunk normally lands within microseconds
+// of the traversal reaching it.
+constexpr uint32_t kStageSpin = 1u << 20;
 
 // kCount: the counting build (single-job closest hit), for the algorithmic bytes of this loop's own
 // visits: nodes visited, triangles queued (each is tested once), instances entered.

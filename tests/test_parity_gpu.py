@@ -494,6 +494,46 @@ def test_host_buffer_traces(torch_cuda, lcx, oracle_mod, chunk, access):
     no_kernel_errors()
 
 
+_SERIALIZED_SCRIPT = """
+import sys, time
+sys.path.insert(0, {root!r})
+import numpy as np, torch
+from luisacompute_gb300 import scenes as S, _capi
+from luisacompute_gb300.accel import accel_from_scene, rays_to_device, hits_to_numpy
+lib = _capi.load()
+_capi.check(lib.lcx_set_host_access(3), "streamed")
+scene = S.terrain_scene(n=128, sphere_count=64, sphere_subdiv=3)
+rays = S.terrain_rays(scene, 400_003, seed=41)
+acc, _ = accel_from_scene(scene)
+want = hits_to_numpy(acc.trace_closest(rays_to_device(rays)))
+h_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8)).pin_memory()
+h_hits = torch.full((rays.shape[0], 6), -7, dtype=torch.int32).pin_memory()
+t = time.perf_counter()
+acc.trace_closest_host(h_rays, h_hits)
+torch.cuda.synchronize()
+dt = time.perf_counter() - t
+_capi.check(lib.lcx_check_trace_errors(), "errors")
+assert np.array_equal(h_hits.numpy().view(np.uint8).reshape(-1), want.view(np.uint8).reshape(-1))
+assert dt < 5.0, dt
+print("OK", dt)
+"""
+
+
+def test_host_streamed_serialized_launches(torch_cuda, lcx):
+    """With launches serialised (CUDA_LAUNCH_BLOCKING=1, in a child process) a streamed host
+    trace would wait for copies enqueued after its launch returned; it takes the staged path
+    instead, promptly and with the device path's records."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = str(Path(__file__).resolve().parent.parent)
+    env = dict(os.environ, CUDA_LAUNCH_BLOCKING="1")
+    r = subprocess.run([sys.executable, "-c", _SERIALIZED_SCRIPT.format(root=root)], env=env, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0 and "OK" in r.stdout, r.stdout[-2000:] + r.stderr[-2000:]
+
+
 def test_host_streamed_concurrent(torch_cuda, lcx, oracle_mod):
     """Two host threads tracing host buffers at once on their own streams: one call holds the
     device's streamed-trace state, the other takes the staged path meanwhile; both give the
