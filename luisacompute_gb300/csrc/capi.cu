@@ -131,7 +131,12 @@ struct DevBlock {
     uint32_t *d_segctl_init = nullptr;
     double *wsah = nullptr;
     ~DevBlock() {
-        if (ptr) cudaFree(ptr);  // cudaFree waits for work still using it
+        // cudaFree waits for work still using it, without stopping the host.  (BVH blocks from
+        // the stream-ordered scratch pool rebuilt a 4096-mesh batch 10 ms faster, with no
+        // unmapping, but a cudaFree of pool memory synchronises the device: a serving loop that
+        // builds scenes while other requests trace went from 0.45 / 4.3 ms to 8.2 / 150 ms at
+        // p50 / p99.)
+        if (ptr) cudaFree(ptr);
     }
 };
 
@@ -284,17 +289,6 @@ bool meshes_current(AccelObj *a, uint64_t *stale = nullptr, bool *destroyed = nu
         }
     a->checked_epoch = epoch;
     return true;
-}
-
-// A BVH's block (nodes and triangles of a build) from the scratch pool, ordered on the build's
-// stream.  Its release stays a cudaFree (DevBlock), which waits for the work queued before it on
-// every stream; the memory then goes back to the pool rather than being unmapped, so the next
-// build of a batch takes it again at once (a 4096-mesh, 12 GB block: the release took 19.9 ms of
-// the 88 ms rebuild, most of it the unmapping, and the allocation 1.7 ms).
-cudaError_t block_alloc(void **p, size_t bytes, cudaStream_t st) {
-    cudaMemPool_t pool;
-    if (scratch_pool(&pool) != LCX_OK) return cudaErrorMemoryAllocation;
-    return cudaMallocFromPoolAsync(p, bytes ? bytes : 16, pool, st);
 }
 
 // Build scratch from the stream-ordered allocator, freed on the same stream.  Outside a graph
@@ -854,7 +848,7 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
                       : 0;
         block = std::make_shared<DevBlock>();
         block->bytes = q_bytes + f_bytes + t_bytes + sah_bytes + r_bytes + res_bytes;
-        LCX_CUDA(block_alloc(&block->ptr, block->bytes, st), "BLAS block allocation");
+        LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(BLAS)");
         Node8Q *qn = static_cast<Node8Q *>(block->ptr);
         Node8F *fn = reinterpret_cast<Node8F *>(reinterpret_cast<char *>(block->ptr) + q_bytes);
         TriRec *tr = reinterpret_cast<TriRec *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes);
@@ -1633,7 +1627,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
                                 : 0;
         block = std::make_shared<DevBlock>();
         block->bytes = q_bytes + f_bytes + r_bytes + 2 * sizeof(double) + u_bytes;
-        LCX_CUDA(block_alloc(&block->ptr, block->bytes, st), "TLAS block allocation");
+        LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(TLAS)");
         Node8Q *qn = static_cast<Node8Q *>(block->ptr);
         Node8F *fn = reinterpret_cast<Node8F *>(reinterpret_cast<char *>(block->ptr) + q_bytes);
         InstRec *ir = reinterpret_cast<InstRec *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes);
