@@ -10,6 +10,7 @@
 // and radiance is summed per path in bounce order, then per pixel in sample
 // order, so the image does not depend on scheduling.
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "lcx_internal.h"
@@ -228,6 +229,28 @@ struct PtScratch {
 
 using namespace lcx;
 
+// The side stream of the shadow rays, one per device (created once).
+static cudaStream_t side_stream() {
+    static std::mutex mtx;
+    static cudaStream_t streams[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(mtx);
+    if (streams[dev] == nullptr && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        streams[dev] = nullptr;
+    }
+    return streams[dev];
+}
+
+struct PtEvent {
+    cudaEvent_t e = nullptr;
+    cudaError_t create() { return cudaEventCreateWithFlags(&e, cudaEventDisableTiming); }
+    ~PtEvent() {
+        if (e) cudaEventDestroy(e);
+    }
+};
+
 extern "C" int lcx_pt_render(uint64_t accel, const LcxPtMesh *meshes, uint32_t mesh_count, const uint32_t *inst_mesh,
                              const float *inst_o2w, uint32_t instance_count, const LcxPtParams *params,
                              float *d_image, LcxTriangleHit *d_first_hits, LcxPtStats *stats, void *stream) {
@@ -290,6 +313,28 @@ extern "C" int lcx_pt_render(uint64_t accel, const LcxPtMesh *meshes, uint32_t m
     uint64_t closest_rays = 0, any_rays = 0;
     uint32_t bounces = 0, launches = 2;  // k_pt_prep_insts, k_pt_generate
     int cur = 0;
+    // Bounce b's shadow rays (trace_any, then their radiance) run on a side stream beside bounce
+    // b+1's closest-hit trace, which fills the other launch's ramp and tail; the shading of bounce
+    // b+1 waits for them, since both add to the same paths' radiance (in bounce order) and it
+    // rewrites the shadow buffers.
+    cudaStream_t side = side_stream();
+    if (side == nullptr) return record_error(LCX_ERR_CUDA, "lcx_pt_render: side stream");
+    // on every return the caller's stream (whose order frees the scratch) waits for the side stream
+    struct SideJoin {
+        cudaStream_t st, side;
+        ~SideJoin() {
+            cudaEvent_t e = nullptr;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) {
+                cudaEventRecord(e, side);
+                cudaStreamWaitEvent(st, e, 0);
+                cudaEventDestroy(e);
+            }
+        }
+    } join{st, side};
+    PtEvent ev_shaded, ev_shadowed;
+    PT_TRY(ev_shaded.create());
+    PT_TRY(ev_shadowed.create());
+    bool shadow_pending = false;
     for (uint32_t b = 0; b < P.max_bounces && live > 0; b++) {
         PT_TRY(cudaMemsetAsync(B.counts, 0, 4 * sizeof(uint32_t), st));
         int r = lcx_trace_closest(accel, reinterpret_cast<const LcxRay *>(B.rays[cur]), live, 0xffu,
@@ -299,6 +344,8 @@ extern "C" int lcx_pt_render(uint64_t accel, const LcxPtMesh *meshes, uint32_t m
             PT_TRY(cudaMemcpyAsync(d_first_hits, B.hits, sizeof(Hit) * n, cudaMemcpyDeviceToDevice, st));
         closest_rays += live;
         launches += 2;  // k_trace, k_pt_shade
+        if (shadow_pending) PT_TRY(cudaStreamWaitEvent(st, ev_shadowed.e, 0));
+        shadow_pending = false;
         k_pt_shade<<<blocks(live, 128), 128, 0, st>>>(P, b, live, B.rays[cur], B.hits, B.path[cur], d_meshes, d_insts,
                                                        B.thr, B.rad, B.rays[cur ^ 1], B.path[cur ^ 1], B.srays,
                                                        B.spath, B.pending, B.counts);
@@ -307,16 +354,22 @@ extern "C" int lcx_pt_render(uint64_t accel, const LcxPtMesh *meshes, uint32_t m
         PT_TRY(cudaMemcpyAsync(h_counts, B.counts, sizeof(h_counts), cudaMemcpyDeviceToHost, st));
         PT_TRY(cudaStreamSynchronize(st));
         if (h_counts[1]) {
-            r = lcx_trace_any(accel, reinterpret_cast<const LcxRay *>(B.srays), h_counts[1], 0xffu, B.occ, stream);
+            PT_TRY(cudaEventRecord(ev_shaded.e, st));
+            PT_TRY(cudaStreamWaitEvent(side, ev_shaded.e, 0));
+            r = lcx_trace_any(accel, reinterpret_cast<const LcxRay *>(B.srays), h_counts[1], 0xffu, B.occ, side);
             if (r != LCX_OK) return r;
             any_rays += h_counts[1];
             launches += 2;  // k_trace, k_pt_shadow
-            k_pt_shadow<<<blocks(h_counts[1], 256), 256, 0, st>>>(h_counts[1], B.occ, B.spath, B.pending, B.rad);
+            k_pt_shadow<<<blocks(h_counts[1], 256), 256, 0, side>>>(h_counts[1], B.occ, B.spath, B.pending, B.rad);
+            PT_TRY(cudaGetLastError());
+            PT_TRY(cudaEventRecord(ev_shadowed.e, side));
+            shadow_pending = true;
         }
         live = h_counts[0];
         cur ^= 1;
         bounces = b + 1;
     }
+    if (shadow_pending) PT_TRY(cudaStreamWaitEvent(st, ev_shadowed.e, 0));
     k_pt_resolve<<<blocks(uint64_t(P.width) * P.height, 256), 256, 0, st>>>(P, B.rad, d_image);
     PT_TRY(cudaGetLastError());
     cudaEventRecord(t_end, st);
