@@ -749,13 +749,14 @@ constexpr uint32_t kStageSpin = 1u << 20;
 // visits: nodes visited, triangles queued (each is tested once), instances entered.
 // kExt 1: accels with motion instances or vertex-motion meshes (each ray has a time; an instance
 // entry takes the instance's matrix at that time, and the flush interpolates a moving triangle at
-// its ray's time); accels with curves stay on loop mode 0.
+// its ray's time); kExt 2: also curves (the flush runs the cone test of a curve segment's piece on
+// the record's object-space ray, keyframed cones at the ray's time).
 // kStream: a streamed host-buffer launch (TraceParams::stage_flag): a warp takes a window of rays
 // only once the window's copy chunk is in place, and publishes how far its results are stored.
 template <int kLayout, bool kAny, int kShort, bool kMulti, bool kCount = false, int kExt = 0, bool kStream = false>
 __global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT : LCX_DEFER_MIN_BLOCKS)
     k_trace_deferred(TraceParams P) {
-    static_assert(kExt <= 1, "curves take loop mode 0");
+    static_assert(kExt <= 1 || LCX_WT_AT_FLUSH, "a curve test reads the record's object-space direction");
     static_assert(!kStream || (!kMulti && !kCount && kExt == 0 && LCX_RAY_CHUNK > 0),
                   "streamed launches are single-job, ray-window launches");
     using W_t = Walker<kLayout, kAny, kCount, kMulti, kShort, kExt, LCX_WT_AT_FLUSH != 0>;
@@ -860,7 +861,22 @@ __global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT :
                 const float lo = Q.rr[7][r], hi = Q.tmax[r];
                 const float4 *tp = reinterpret_cast<const float4 *>(Q.tri[j]);
                 float4 a = bvh_ld(tp), b = bvh_ld(tp + 1), c = bvh_ld(tp + 2);
-                bool live = true;
+                bool live = true, cone = false;
+                if constexpr (kExt >= 2) {
+                    const uint32_t marker = __float_as_uint(b.w);
+                    if (marker == kTriCurve || marker == kTriCurveMotion) {  // a cone of a curve segment
+                        cone = true;
+                        float4 c0 = make_float4(a.x, a.y, a.z, c.x), c1 = make_float4(b.x, b.y, b.z, c.y);
+                        live = marker != kTriCurveMotion || curve_motion_cone(a, b, c, Q.rtime[r], c0, c1);
+                        const uint32_t kn = __float_as_uint(c.z);
+                        // the curve test on the record's object-space ray (origin, direction); v = -1
+                        // marks a curve hit as in the immediate loop
+                        live = live && curve_piece_entry(make_float3(Q.rr[0][r], Q.rr[1][r], Q.rr[2][r]),
+                                                         make_float3(Q.rr[3][r], Q.rr[4][r], Q.rr[5][r]), c0, c1,
+                                                         kn & 0xffffu, kn >> 16, __float_as_uint(c.w), lo, hi, t, u);
+                        v = -1.0f;
+                    }
+                }
                 if constexpr (kExt >= 1) {
                     if (__float_as_uint(b.w) == kTriMotion) {  // a vertex-motion mesh: its triangle at the ray's time
                         const MeshMotion *mm = reinterpret_cast<const MeshMotion *>(
@@ -869,7 +885,7 @@ __global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT :
                         live = motion_triangle(*mm, __float_as_uint(a.w), Q.rtime[r], a, b, c);
                     }
                 }
-                if (live && wt_intersect(ray, lo, hi, a, b, c, t, u, v)) {
+                if (live && (cone || wt_intersect(ray, lo, hi, a, b, c, t, u, v))) {
                     hit = true;
                     key = kAny ? 0ull
                                : (static_cast<unsigned long long>(float_to_ordered(t)) << 32) | __float_as_uint(a.w);
@@ -1335,10 +1351,17 @@ cudaError_t launch_trace(const TraceParams &p, int layout, bool any, bool counti
     if (p.mode == 3 && p.jobs == nullptr && !counting && layout == LCX_NODES_QUANT8)
         return any ? launch_per_thread<true>(p, st) : launch_per_thread<false>(p, st);
     if (p.motion) {
-        // accels with motion instances or vertex-motion meshes: loop mode 2 (deferred triangle batches
-        // at each ray's time) with quantised nodes; curves, FP32 nodes, the counting build and the
-        // other loop modes: the extended kernels of loop mode 0
-        if (!p.curves && p.mode == 2 && layout == LCX_NODES_QUANT8 && !counting) {
+        // accels with motion instances, vertex-motion meshes or curves: loop mode 2 (deferred
+        // triangle and cone batches at each ray's time) with quantised nodes; FP32 nodes, the
+        // counting build and the other loop modes: the extended kernels of loop mode 0
+        if (p.mode == 2 && layout == LCX_NODES_QUANT8 && !counting) {
+            if (p.curves) {  // kExt 2: curve cones tested at the flush as well
+                if (p.jobs != nullptr)
+                    return any ? launch_deferred<LCX_NODES_QUANT8, true, LCX_DEFER_STACK, true, false, 2>(p, st)
+                               : launch_deferred<LCX_NODES_QUANT8, false, LCX_DEFER_STACK, true, false, 2>(p, st);
+                return any ? launch_deferred<LCX_NODES_QUANT8, true, LCX_DEFER_STACK, false, false, 2>(p, st)
+                           : launch_deferred<LCX_NODES_QUANT8, false, LCX_DEFER_STACK, false, false, 2>(p, st);
+            }
             if (p.jobs != nullptr)
                 return any ? launch_deferred<LCX_NODES_QUANT8, true, LCX_DEFER_STACK, true, false, 1>(p, st)
                            : launch_deferred<LCX_NODES_QUANT8, false, LCX_DEFER_STACK, true, false, 1>(p, st);
