@@ -708,6 +708,12 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2                     ? L
 // at 4 / 5 / 6 / 7 blocks per SM (6 and 7 spill)
 #define LCX_DEFER_MIN_BLOCKS_EXT 5
 #endif
+#ifndef LCX_DEFER_MIN_BLOCKS_CURVE
+// curve launches (kExt 2): hair workload, Catmull-Rom camera / incoherent Grays/s 1.125 / 1.113
+// at 4 blocks per SM (127 registers, no spills), 1.072 / 0.986 at 5 (76 bytes spilled), 0.828 /
+// 0.786 at 6
+#define LCX_DEFER_MIN_BLOCKS_CURVE 4
+#endif
 #ifndef LCX_DEFER_STACK
 #define LCX_DEFER_STACK 8
 #endif
@@ -754,7 +760,8 @@ constexpr uint32_t kStageSpin = 1u << 20;
 // kStream: a streamed host-buffer launch (TraceParams::stage_flag): a warp takes a window of rays
 // only once the window's copy chunk is in place, and publishes how far its results are stored.
 template <int kLayout, bool kAny, int kShort, bool kMulti, bool kCount = false, int kExt = 0, bool kStream = false>
-__global__ void __launch_bounds__(kTraceBlock, kExt ? LCX_DEFER_MIN_BLOCKS_EXT : LCX_DEFER_MIN_BLOCKS)
+__global__ void __launch_bounds__(kTraceBlock, kExt >= 2 ? LCX_DEFER_MIN_BLOCKS_CURVE
+                                               : (kExt ? LCX_DEFER_MIN_BLOCKS_EXT : LCX_DEFER_MIN_BLOCKS))
     k_trace_deferred(TraceParams P) {
     static_assert(kExt <= 1 || LCX_WT_AT_FLUSH, "a curve test reads the record's object-space direction");
     static_assert(!kStream || (!kMulti && !kCount && kExt == 0 && LCX_RAY_CHUNK > 0),
