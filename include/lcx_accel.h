@@ -549,8 +549,10 @@ LCX_API int lcx_get_host_access(uint32_t *mode, uint32_t *coherent_link);
 /* Builds, refits and traces take their scratch from a stream-ordered pool of the
  * current device that keeps freed memory for the next call (a build of n items
  * uses a few hundred bytes per item; 135M triangles: ~34 GB).  This hands the
- * unused part back to the driver, after synchronising the device.  No
- * reference counterpart (OptiX and Embree manage their own build memory). */
+ * unused part back to the driver, after synchronising the device; a BVH
+ * allocation that finds the device out of memory does the same once before it
+ * fails.  No reference counterpart (OptiX and Embree manage their own build
+ * memory). */
 LCX_API int lcx_release_scratch(void);
 
 /* Counting build of the closest-hit traversal: per-ray visit counts

@@ -291,6 +291,18 @@ bool meshes_current(AccelObj *a, uint64_t *stale = nullptr, bool *destroyed = nu
     return true;
 }
 
+// cudaMalloc for a BVH block; when the device is out of memory, the scratch pool's unused memory
+// (which it keeps for the next build) goes back to the driver and the allocation runs once more.
+cudaError_t block_malloc(void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaErrorMemoryAllocation) return e;
+    cudaGetLastError();
+    cudaMemPool_t pool;
+    if (scratch_pool(&pool) != LCX_OK) return e;
+    if (cudaDeviceSynchronize() != cudaSuccess || cudaMemPoolTrimTo(pool, 0) != cudaSuccess) return e;
+    return cudaMalloc(p, bytes);
+}
+
 // Build scratch from the stream-ordered allocator, freed on the same stream.  Outside a graph
 // capture it comes from the library's scratch pool (reorder.cu), which keeps freed memory for the
 // next build (lcx_release_scratch hands it back): the device's default pool returns it to the
@@ -663,7 +675,7 @@ int reserve_only(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
     const size_t res_bytes = sizeof(SegInput) * count + sizeof(uint32_t) * kSegWords * count;
     auto block = std::make_shared<DevBlock>();
     block->bytes = q_bytes + f_bytes + t_bytes + sah_bytes + res_bytes;
-    LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(reserved BLAS block)");
+    LCX_CUDA(block_malloc(&block->ptr, block->bytes), "cudaMalloc(reserved BLAS block)");
     char *base = static_cast<char *>(block->ptr);
     block->qn = reinterpret_cast<Node8Q *>(base);
     block->fn = reinterpret_cast<Node8F *>(base + q_bytes);
@@ -848,7 +860,7 @@ int build_meshes(const std::vector<MeshObj *> &meshes, const std::vector<SegInpu
                       : 0;
         block = std::make_shared<DevBlock>();
         block->bytes = q_bytes + f_bytes + t_bytes + sah_bytes + r_bytes + res_bytes;
-        LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(BLAS)");
+        LCX_CUDA(block_malloc(&block->ptr, block->bytes), "cudaMalloc(BLAS)");
         Node8Q *qn = static_cast<Node8Q *>(block->ptr);
         Node8F *fn = reinterpret_cast<Node8F *>(reinterpret_cast<char *>(block->ptr) + q_bytes);
         TriRec *tr = reinterpret_cast<TriRec *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes);
@@ -1627,7 +1639,7 @@ int lcx_accel_build(uint64_t accel, uint32_t instance_count, uint32_t request, c
                                 : 0;
         block = std::make_shared<DevBlock>();
         block->bytes = q_bytes + f_bytes + r_bytes + 2 * sizeof(double) + u_bytes;
-        LCX_CUDA(cudaMalloc(&block->ptr, block->bytes), "cudaMalloc(TLAS)");
+        LCX_CUDA(block_malloc(&block->ptr, block->bytes), "cudaMalloc(TLAS)");
         Node8Q *qn = static_cast<Node8Q *>(block->ptr);
         Node8F *fn = reinterpret_cast<Node8F *>(reinterpret_cast<char *>(block->ptr) + q_bytes);
         InstRec *ir = reinterpret_cast<InstRec *>(reinterpret_cast<char *>(block->ptr) + q_bytes + f_bytes);
