@@ -37,6 +37,11 @@ constexpr int kTraceBlock = 128;
 #ifndef LCX_TRACE_MIN_BLOCKS_Q
 #define LCX_TRACE_MIN_BLOCKS_Q 7
 #endif
+#ifndef LCX_PER_THREAD_MIN_BLOCKS
+// loop mode 3 (one ray per thread): terrain workload closest / any Grays/s 1.004 / 2.45 at 7 blocks per
+// SM (72 registers, 188 bytes spilled), 1.004 / 2.48 at 6, 1.001 / 2.32 at 5 (96 registers), 0.87 at 4
+#define LCX_PER_THREAD_MIN_BLOCKS 7
+#endif
 #ifndef LCX_TRACE_MIN_BLOCKS_F
 #define LCX_TRACE_MIN_BLOCKS_F 7
 #endif
@@ -1197,7 +1202,7 @@ __global__ void __launch_bounds__(kTraceBlock, kExt >= 2 ? LCX_DEFER_MIN_BLOCKS_
 // lanes until its slowest ray ends.  Motion accels are traced by the same walk
 // (at each ray's time).
 template <bool kAny>
-__global__ void __launch_bounds__(kTraceBlock, LCX_TRACE_MIN_BLOCKS_Q) k_trace_per_thread(TraceParams P) {
+__global__ void __launch_bounds__(kTraceBlock, LCX_PER_THREAD_MIN_BLOCKS) k_trace_per_thread(TraceParams P) {
     constexpr int kShort = 16;
     __shared__ uint2 sstack[kShort * kTraceBlock];
     const uint32_t k = blockIdx.x * kTraceBlock + threadIdx.x;
